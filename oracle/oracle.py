@@ -1,0 +1,254 @@
+"""ORACLE (test infrastructure): ctypes wrapper over oracle/liboracle.so.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, as the checker.  The product package never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_pattern.so")
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+
+
+def build(force=False):
+    """Compile the restatement (g++, -ffp-contract=off) into liboracle.so."""
+    src = os.path.join(HERE, "sg_oracle.cpp")
+    if force or not os.path.exists(LIB) or os.path.getmtime(src) > os.path.getmtime(LIB):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                               "-fPIC", "-shared", src, "-o", LIB])
+
+
+def build_ref():
+    """Compile the reference's own pattern builder when its sources exist."""
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.or_pattern.restype = _I64
+        L.or_pattern.argtypes = [_I32, _P, _I64, _I32, _P, _P, _I64]
+        L.or_slots.argtypes = [_P, _I64, _I32, _P, _P, _P]
+        L.or_spmv_f64.argtypes = [_I32, _I32, _P, _P, _P, _P, _P]
+        L.or_spmv_f32.argtypes = [_I32, _I32, _P, _P, _P, _P, _P]
+        L.or_dot_f64.restype = _D
+        L.or_dot_f64.argtypes = [_I32, _I32, _P, _P]
+        L.or_cg_normr2_f64.restype = ctypes.c_int
+        L.or_cg_normr2_f64.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _D, ctypes.c_int, _P]
+        L.or_jacobi_pcg_f64.restype = ctypes.c_int
+        L.or_jacobi_pcg_f64.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _D, ctypes.c_int,
+                                        ctypes.c_int, _P]
+        L.or_springs_assemble.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _P, _I64, _P, _P, _P,
+                                          _D, _D, _P, _P, _P, _P, _P]
+        L.or_springs_step.restype = ctypes.c_int
+        L.or_springs_step.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _P, _I64, _P, _P, _P,
+                                      _D, _D, _P, _P, _P, _D, ctypes.c_int]
+        L.or_scalar_springs_assemble.argtypes = [_I32, _I64, _P, _P, _D, _D, _P, _P, _P]
+        L.or_cg_norm_f64.restype = ctypes.c_int
+        L.or_cg_norm_f64.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _D, ctypes.c_int]
+        L.or_tet_precompute.argtypes = [_I32, _P, _I64, _P, _D, _P, _P, _P]
+        L.or_tet_force.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _I64, _P, _P, _P, _P, _P,
+                                   _D, _D, _P, _P]
+        L.or_tet_stiffness.argtypes = [ctypes.c_int, _I32, _P, _P, _I64, _P, _P, _P, _P, _P,
+                                       _D, _D, _P, _P, _P]
+        L.or_tet_step.restype = ctypes.c_int
+        L.or_tet_step.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _I64, _P, _P, _P, _P, _P,
+                                  _D, _D, _P, _P, _P, _D, ctypes.c_int]
+        L.or_heat_assemble.argtypes = [_I32, _I64, _P, _P, _P, _P, _D, _P, _P, _P, _P, _P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_P)
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def pattern(n, ep, card):
+    ep = _c(ep, np.int32)
+    nE = ep.size // card
+    cap = max(1, nE * card * card + n)
+    rowptr = np.zeros(n + 1, np.uint32)
+    colidx = np.zeros(cap, np.uint32)
+    nnz = lib().or_pattern(n, _p(ep), nE, card, _p(rowptr), _p(colidx), cap)
+    assert nnz >= 0
+    return rowptr, colidx[:nnz].copy()
+
+
+def ref_pattern(n, ep, card):
+    """The reference's own PathIndexBuilder (None when not built here)."""
+    if not os.path.exists(REF_LIB):
+        return None
+    L = ctypes.CDLL(REF_LIB)
+    L.ref_pattern.restype = _I64
+    L.ref_pattern.argtypes = [_I32, _P, _I64, _I32, _P, _P, _I64]
+    ep = _c(ep, np.int32)
+    nE = ep.size // card
+    cap = max(1, nE * card * card + n)
+    rowptr = np.zeros(n + 1, np.uint32)
+    colidx = np.zeros(cap, np.uint32)
+    nnz = L.ref_pattern(n, _p(ep), nE, card, _p(rowptr), _p(colidx), cap)
+    assert nnz >= 0
+    return rowptr, colidx[:nnz].copy()
+
+
+def ref_slots(ep, card, rowptr, colidx):
+    if not os.path.exists(REF_LIB):
+        return None
+    L = ctypes.CDLL(REF_LIB)
+    L.ref_slots.argtypes = [_P, _I64, _I32, _P, _P, _P]
+    ep = _c(ep, np.int32)
+    nE = ep.size // card
+    out = np.zeros(nE * card * card, np.uint32)
+    L.ref_slots(_p(ep), nE, card, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)), _p(out))
+    return out
+
+
+def slots(ep, card, rowptr, colidx):
+    ep = _c(ep, np.int32)
+    nE = ep.size // card
+    out = np.zeros(nE * card * card, np.uint32)
+    lib().or_slots(_p(ep), nE, card, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
+                   _p(out))
+    return out
+
+
+def spmv(n, bs, rowptr, colidx, vals, x):
+    if vals.dtype == np.float32:
+        y = np.zeros(n * bs, np.float32)
+        lib().or_spmv_f32(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
+                          _p(_c(vals, np.float32)), _p(_c(x, np.float32)), _p(y))
+    else:
+        y = np.zeros(n * bs, np.float64)
+        lib().or_spmv_f64(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
+                          _p(_c(vals, np.float64)), _p(_c(x, np.float64)), _p(y))
+    return y
+
+
+def cg_normr2(n, bs, rowptr, colidx, A, b, x0, tol2, maxiters):
+    x = _c(x0, np.float64).copy()
+    nr = np.zeros(1)
+    it = lib().or_cg_normr2_f64(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
+                                _p(_c(A, np.float64)), _p(_c(b, np.float64)), _p(x), tol2,
+                                maxiters, _p(nr))
+    return x, it, float(nr[0])
+
+
+def jacobi_pcg(n, bs, rowptr, colidx, A, b, x0, tol, maxiters, refresh=50):
+    x = _c(x0, np.float64).copy()
+    rr = np.zeros(1)
+    it = lib().or_jacobi_pcg_f64(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
+                                 _p(_c(A, np.float64)), _p(_c(b, np.float64)), _p(x), tol,
+                                 maxiters, refresh, _p(rr))
+    return x, it, float(rr[0])
+
+
+def springs_assemble(form, x, v, m, fixed, ep, k, l0, h, viscous, grav, rowptr, colidx):
+    n = len(m)
+    nS = len(k)
+    MDK = np.zeros(int(rowptr[n]) * 9)
+    f = np.zeros(n * 3)
+    lib().or_springs_assemble(form, n, _p(_c(x, np.float64)), _p(_c(v, np.float64)),
+                              _p(_c(m, np.float64)), _p(_c(fixed, np.uint8)), nS,
+                              _p(_c(ep, np.int32)), _p(_c(k, np.float64)),
+                              _p(_c(l0, np.float64)), h, viscous, _p(_c(grav, np.float64)),
+                              _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)), _p(MDK),
+                              _p(f))
+    return MDK, f
+
+
+def springs_step(form, x, v, m, fixed, ep, k, l0, h, viscous, grav, rowptr, colidx, tol2,
+                 maxiters):
+    """Advances x, v (float64 arrays, modified in place); returns CG iterations."""
+    assert x.dtype == np.float64 and v.dtype == np.float64
+    n = len(m)
+    return lib().or_springs_step(form, n, _p(x), _p(v), _p(_c(m, np.float64)),
+                                 _p(_c(fixed, np.uint8)), len(k), _p(_c(ep, np.int32)),
+                                 _p(_c(k, np.float64)), _p(_c(l0, np.float64)), h, viscous,
+                                 _p(_c(grav, np.float64)), _p(_c(rowptr, np.uint32)),
+                                 _p(_c(colidx, np.uint32)), tol2, maxiters)
+
+
+def scalar_springs_assemble(n, ep, a, diag, scale, rowptr, colidx):
+    A = np.zeros(int(rowptr[n]))
+    lib().or_scalar_springs_assemble(n, len(a), _p(_c(ep, np.int32)), _p(_c(a, np.float64)),
+                                     diag, scale, _p(_c(rowptr, np.uint32)),
+                                     _p(_c(colidx, np.uint32)), _p(A))
+    return A
+
+
+def cg_norm(n, bs, rowptr, colidx, A, b, tol, maxiters):
+    x = np.zeros(n * bs)
+    it = lib().or_cg_norm_f64(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
+                              _p(_c(A, np.float64)), _p(_c(b, np.float64)), _p(x), tol,
+                              maxiters)
+    return x, it
+
+
+def tet_precompute(x, tets, rho):
+    n = len(x) // 3
+    nT = len(tets) // 4
+    B = np.zeros(nT * 9)
+    W = np.zeros(nT)
+    m = np.zeros(n)
+    lib().or_tet_precompute(n, _p(_c(x, np.float64)), nT, _p(_c(tets, np.int32)), rho, _p(B),
+                            _p(W), _p(m))
+    return B, W, m
+
+
+def tet_force(neo, x, v, c, tets, B, W, u, l, h, rho, grav):
+    n = len(x) // 3
+    f = np.zeros(n * 3)
+    lib().or_tet_force(int(neo), n, _p(_c(x, np.float64)), _p(_c(v, np.float64)),
+                       _p(_c(c, np.int32)), len(tets) // 4, _p(_c(tets, np.int32)),
+                       _p(_c(B, np.float64)), _p(_c(W, np.float64)), _p(_c(u, np.float64)),
+                       _p(_c(l, np.float64)), h, rho, _p(_c(grav, np.float64)), _p(f))
+    return f
+
+
+def tet_stiffness(neo, x, c, tets, B, W, u, l, h, rho, rowptr, colidx):
+    n = len(x) // 3
+    A = np.zeros(int(rowptr[n]) * 9)
+    lib().or_tet_stiffness(int(neo), n, _p(_c(x, np.float64)), _p(_c(c, np.int32)),
+                           len(tets) // 4, _p(_c(tets, np.int32)), _p(_c(B, np.float64)),
+                           _p(_c(W, np.float64)), _p(_c(u, np.float64)), _p(_c(l, np.float64)),
+                           h, rho, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)), _p(A))
+    return A
+
+
+def tet_step(neo, x, v, c, tets, B, W, u, l, h, rho, grav, rowptr, colidx, tol2, maxiters):
+    """Advances x, v (float64, in place); returns CG iterations."""
+    assert x.dtype == np.float64 and v.dtype == np.float64
+    return lib().or_tet_step(int(neo), len(x) // 3, _p(x), _p(v), _p(_c(c, np.int32)),
+                             len(tets) // 4, _p(_c(tets, np.int32)), _p(_c(B, np.float64)),
+                             _p(_c(W, np.float64)), _p(_c(u, np.float64)),
+                             _p(_c(l, np.float64)), h, rho, _p(_c(grav, np.float64)),
+                             _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)), tol2,
+                             maxiters)
+
+
+def heat_assemble(n, tets, B, W, kappa, dt, T0, rowptr, colidx):
+    A = np.zeros(int(rowptr[n]))
+    b = np.zeros(n)
+    lib().or_heat_assemble(n, len(tets) // 4, _p(_c(tets, np.int32)), _p(_c(B, np.float64)),
+                           _p(_c(W, np.float64)), _p(_c(kappa, np.float64)), dt,
+                           _p(_c(T0, np.float64)), _p(_c(rowptr, np.uint32)),
+                           _p(_c(colidx, np.uint32)), _p(A), _p(b))
+    return A, b

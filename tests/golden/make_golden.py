@@ -1,0 +1,81 @@
+"""Regenerate the golden fixtures in this directory from the reference tree.
+
+Run in a checkout that has the reference sources (default path below, or
+SIMIT_REFERENCE); the GPU machine has none, so the outputs are committed:
+
+  reference_golden.json   golden values asserted by the reference's tests,
+                          extracted from their sources (file:line recorded)
+  bar2k.node, bar2k.ele   the TetGen fixture test/program-fem-test.cpp loads
+  pattern_golden.json     pattern + slot map of small meshes produced by the
+                          reference's own PathIndexBuilder / `loc`
+                          (oracle/_ref/libref_pattern.so)
+"""
+import json
+import os
+import re
+import shutil
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("SIMIT_REFERENCE", "/root/reference")
+
+
+def extract_asserts(path, test_name):
+    """SIMIT_ASSERT_FLOAT_EQ(expected, expr) lines inside TEST(..., test_name)."""
+    lines = open(path).read().split("\n")
+    out, inside = [], False
+    for i, ln in enumerate(lines, 1):
+        m = re.match(r"TEST\((\w+),\s*(\w+)\)", ln)
+        if m:
+            inside = m.group(2) == test_name
+            continue
+        if inside:
+            a = re.search(r"SIMIT_ASSERT_FLOAT_EQ\(\s*([-0-9.eE+]+)\s*,\s*(.*)\);", ln)
+            if a:
+                out.append({"expected": float(a.group(1)), "expr": a.group(2).strip(),
+                            "source": "%s:%d" % (os.path.relpath(path, REF), i)})
+    return out
+
+
+def main():
+    test = os.path.join(REF, "test")
+    if not os.path.isdir(test):
+        sys.exit("reference test sources not found at %s" % test)
+    golden = {
+        "isprings": extract_asserts(os.path.join(test, "program-isprings.cpp"), "isprings"),
+        "cg": extract_asserts(os.path.join(test, "program-cg-test.cpp"), "cg"),
+        "femTet": extract_asserts(os.path.join(test, "program-fem-test.cpp"), "femTet"),
+    }
+    with open(os.path.join(HERE, "reference_golden.json"), "w") as f:
+        json.dump(golden, f, indent=1)
+    for ext in ("node", "ele"):
+        shutil.copy(os.path.join(test, "input", "program", "fem", "bar2k." + ext),
+                    os.path.join(HERE, "bar2k." + ext))
+
+    sys.path.insert(0, REPO)
+    from oracle import oracle
+    oracle.build_ref()
+    from simit_gb300 import meshgen
+    cases = {}
+    ep, n = meshgen.box_springs(4, 3, 2)
+    cases["box_springs_4x3x2"] = (n, ep, 2)
+    mesh = meshgen.tet_grid(3, 2, 2)
+    cases["tet_grid_3x2x2"] = (mesh["n"], mesh["tets"], 4)
+    rng = np.random.default_rng(7)
+    cases["random_tris_40"] = (40, rng.integers(0, 40, size=3 * 60).astype(np.int32), 3)
+    out = {}
+    for name, (n, ep, card) in cases.items():
+        rp, ci = oracle.ref_pattern(n, ep, card)
+        sl = oracle.ref_slots(ep, card, rp, ci)
+        out[name] = {"n": int(n), "card": card, "endpoints": np.asarray(ep).tolist(),
+                     "rowptr": rp.tolist(), "colidx": ci.tolist(), "slots": sl.tolist()}
+    with open(os.path.join(HERE, "pattern_golden.json"), "w") as f:
+        json.dump(out, f)
+    print("wrote golden fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main()

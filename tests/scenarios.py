@@ -1,0 +1,84 @@
+"""Inputs of the reference's own program tests, rebuilt as arrays.
+
+Each builder mirrors the set construction of one reference test so that the
+oracle and the GPU path can replay it and compare with its golden values.
+"""
+import json
+import os
+import re
+
+import numpy as np
+
+from simit_gb300 import meshgen
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden(name):
+    with open(os.path.join(GOLDEN, "reference_golden.json")) as f:
+        return json.load(f)[name]
+
+
+def golden_lookup(entry, fields):
+    """Value the golden entry's expression refers to, e.g. 'v(p1)(2)',
+    '(simit_float)c.get(p0)' or 'x.get(vertRefs[100])(0)'."""
+    e = entry["expr"].replace("(simit_float)", "")
+    m = re.match(r"(\w+)\(p(\d+)\)\((\d)\)$", e)
+    if m:
+        return fields[m.group(1)][int(m.group(2)) * 3 + int(m.group(3))]
+    m = re.match(r"(\w+)\.get\(p(\d+)\)$", e)
+    if m:
+        return fields[m.group(1)][int(m.group(2))]
+    m = re.match(r"(\w+)\.get\(vertRefs\[(\d+)\]\)\((\d)\)$", e)
+    if m:
+        return fields[m.group(1)][int(m.group(2)) * 3 + int(m.group(3))]
+    raise ValueError(e)
+
+
+def isprings_chain():
+    """test/program-isprings.cpp:91-146 (TEST(Program, isprings)): 3-point
+    vertical chain, p0 fixed (z < 0.4), 10 runs of
+    test/input/program/isprings.sim main (h=1e-2, viscous=1e-1, grav -9.81 z,
+    CG tol 1e-5 on r'r, 25 iterations)."""
+    l0_, stiffness, density, radius, PI_ = 1.0, 100.0, 1000.0, 0.01, 3.14159265358979
+    x = np.array([0, 0, 0, 0, 0, 1, 0, 0, 2], np.float64)
+    v = np.zeros(9)
+    m = np.full(3, PI_ * radius * radius * l0_ * density)
+    fixed = np.array([1, 0, 0], np.uint8)
+    ep = np.array([0, 1, 1, 2], np.int32)
+    return {"n": 3, "x": x, "v": v, "m": m, "fixed": fixed, "ep": ep,
+            "k": np.full(2, stiffness), "l0": np.full(2, l0_), "h": 1e-2, "viscous": 1e-1,
+            "grav": np.array([0, 0, -9.81]), "tol2": 1e-5, "maxiters": 25, "steps": 10,
+            "form": 1}
+
+
+def cg_chain():
+    """test/program-cg-test.cpp:10-44 with test/input/program/cg.sim: 3
+    points, b = (1,2,3), springs a = (4,5), A = I - 0.01*K, CG from 0 with
+    tol 1e-6 on ||r|| and 5 iterations."""
+    return {"n": 3, "ep": np.array([0, 1, 1, 2], np.int32), "a": np.array([4.0, 5.0]),
+            "b": np.array([1.0, 2.0, 3.0]), "diag": 1.0, "scale": -0.01, "tol": 1e-6,
+            "maxiters": 5}
+
+
+def femtet_bar2k():
+    """test/program-fem-test.cpp:14-106 with test/input/program/femTet.sim:
+    bar2k mesh (439 vertices, 1151 tets), E=5e3, nu=0.45, u = 0.5*E/nu,
+    l = E*nu/((1+nu)*(1-2nu)), v0 = (0.1, 0, 0.1), vertices with y < 1e-4
+    constrained (c=1, v=0); initializeTet then 10 runs of main (h=0.01, CG
+    tol 1e-6 on r'r, 100 iterations)."""
+    x, tets = meshgen.load_tetgen(os.path.join(GOLDEN, "bar2k.node"),
+                                  os.path.join(GOLDEN, "bar2k.ele"))
+    n = len(x) // 3
+    nT = len(tets) // 4
+    E, nu = 5e3, 0.45
+    uval = 0.5 * E / nu
+    lval = E * nu / ((1 + nu) * (1 - 2 * nu))
+    v = np.tile(np.array([0.1, 0.0, 0.1]), n)
+    c = np.zeros(n, np.int32)
+    ymask = x.reshape(-1, 3)[:, 1] < 0.0001
+    c[ymask] = 1
+    v.reshape(-1, 3)[ymask] = 0.0
+    return {"n": n, "x": x, "v": v, "c": c, "tets": tets, "u": np.full(nT, uval),
+            "l": np.full(nT, lval), "h": 0.01, "rho": 1000.0,
+            "grav": np.array([0.0, -10.0, 0.0]), "tol2": 1e-6, "maxiters": 100, "steps": 10}

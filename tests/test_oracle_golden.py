@@ -1,0 +1,102 @@
+"""Pin the oracle: reference golden values and the reference's own pattern code.
+
+CPU only (no GPU marker).  Tolerance 1e-13 absolute, as SIMIT_ASSERT_FLOAT_EQ
+in FP64 (test/simit-test.h:36-48).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from simit_gb300 import meshgen
+from tests import scenarios
+
+GOLD_TOL = 1e-13
+
+
+def test_isprings_golden(oracle):
+    s = scenarios.isprings_chain()
+    x, v = s["x"].copy(), s["v"].copy()
+    rp, ci = oracle.pattern(s["n"], s["ep"], 2)
+    for _ in range(s["steps"]):
+        oracle.springs_step(s["form"], x, v, s["m"], s["fixed"], s["ep"], s["k"], s["l0"],
+                            s["h"], s["viscous"], s["grav"], rp, ci, s["tol2"], s["maxiters"])
+    for g in scenarios.golden("isprings"):
+        got = scenarios.golden_lookup(g, {"x": x, "v": v})
+        assert abs(got - g["expected"]) <= GOLD_TOL, (g, got)
+
+
+def test_cg_golden(oracle):
+    s = scenarios.cg_chain()
+    rp, ci = oracle.pattern(s["n"], s["ep"], 2)
+    A = oracle.scalar_springs_assemble(s["n"], s["ep"], s["a"], s["diag"], s["scale"], rp, ci)
+    c, it = oracle.cg_norm(s["n"], 1, rp, ci, A, s["b"], s["tol"], s["maxiters"])
+    for g in scenarios.golden("cg"):
+        got = scenarios.golden_lookup(g, {"c": c})
+        assert abs(got - g["expected"]) <= GOLD_TOL, (g, got)
+
+
+def test_femtet_golden(oracle):
+    s = scenarios.femtet_bar2k()
+    assert s["n"] == 439 and len(s["tets"]) // 4 == 1151
+    x, v = s["x"].copy(), s["v"].copy()
+    B, W, m = oracle.tet_precompute(x, s["tets"], s["rho"])
+    rp, ci = oracle.pattern(s["n"], s["tets"], 4)
+    for _ in range(s["steps"]):
+        oracle.tet_step(1, x, v, s["c"], s["tets"], B, W, s["u"], s["l"], s["h"], s["rho"],
+                        s["grav"], rp, ci, s["tol2"], s["maxiters"])
+    for g in scenarios.golden("femTet"):
+        got = scenarios.golden_lookup(g, {"x": x})
+        assert abs(got - g["expected"]) <= GOLD_TOL, (g, got)
+
+
+def test_pattern_golden_fixtures(oracle):
+    """Pattern + slot map equal the reference's PathIndexBuilder / loc output
+    committed in tests/golden/pattern_golden.json."""
+    with open(os.path.join(scenarios.GOLDEN, "pattern_golden.json")) as f:
+        cases = json.load(f)
+    for name, c in cases.items():
+        ep = np.array(c["endpoints"], np.int32)
+        rp, ci = oracle.pattern(c["n"], ep, c["card"])
+        assert rp.tolist() == c["rowptr"], name
+        assert ci.tolist() == c["colidx"], name
+        assert oracle.slots(ep, c["card"], rp, ci).tolist() == c["slots"], name
+
+
+def test_pattern_reference_test_vectors(oracle):
+    """VERIFY_INDEX lists of test/path_indices-test.cpp: exist_and (vev on a
+    3-point chain, :155-174) and alias (two opposite edges, :309-332)."""
+    ep, n = meshgen.box_springs(3, 1, 1)
+    rp, ci = oracle.pattern(n, ep, 2)
+    rows = [ci[rp[i]:rp[i + 1]].tolist() for i in range(n)]
+    assert rows == [[0, 1], [0, 1, 2], [1, 2]]
+    rp, ci = oracle.pattern(2, np.array([0, 1, 1, 0], np.int32), 2)
+    assert [ci[rp[i]:rp[i + 1]].tolist() for i in range(2)] == [[0, 1], [0, 1]]
+    # a vertex with no edge gets an empty row (src/path_indices.cpp:359-429)
+    rp, ci = oracle.pattern(4, np.array([0, 1], np.int32), 2)
+    assert rp.tolist() == [0, 2, 4, 4, 4]
+
+
+@pytest.mark.parametrize("card,n,nE,seed", [(2, 50, 120, 1), (3, 64, 90, 2), (4, 80, 150, 3),
+                                            (4, 30, 200, 4), (1, 10, 7, 5)])
+def test_pattern_matches_reference_builder(oracle, card, n, nE, seed):
+    """Random edge sets (duplicate endpoints inside an element included)
+    against the reference's own builder compiled from its sources."""
+    if not os.path.exists(oracle.REF_LIB):
+        pytest.skip("reference pattern builder not built here (no reference sources)")
+    ep = meshgen.rng(seed).integers(0, n, size=nE * card).astype(np.int32)
+    rp, ci = oracle.pattern(n, ep, card)
+    r2, c2 = oracle.ref_pattern(n, ep, card)
+    assert np.array_equal(rp, r2) and np.array_equal(ci, c2)
+    assert np.array_equal(oracle.slots(ep, card, rp, ci), oracle.ref_slots(ep, card, rp, ci))
+
+
+def test_tet_grid_counts(oracle):
+    """5-tet lattice sizes; 16^3 nnzb 58,769 as computed for the 16^3 config."""
+    m = meshgen.tet_grid(16)
+    assert (m["n"], len(m["tets"]) // 4) == (4913, 20480)
+    rp, ci = oracle.pattern(m["n"], m["tets"], 4)
+    assert len(ci) == 58769
+    B, W, _ = oracle.tet_precompute(m["x"], m["tets"], 1e3)
+    assert W.min() > 0 and abs(W.sum() - 1.0) < 1e-12
