@@ -1,0 +1,75 @@
+"""ctypes binding of libsimit_gb300.so (the C ABI in include/simit_gb300.h).
+
+The library is built in-tree by simit_gb300/build.py.  There is no CPU
+fallback: if the library or a GPU is missing, loading fails loudly.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsimit_gb300.so")
+
+P = ctypes.c_void_p
+I32 = ctypes.c_int32
+I64 = ctypes.c_int64
+D = ctypes.c_double
+F32, F64 = 0, 1
+
+
+class SimitError(RuntimeError):
+    """A negative status from the C ABI (the analogue of SimitException)."""
+
+    def __init__(self, code, msg):
+        super().__init__("simit_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "sg_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(P)]),
+    "sg_ctx_destroy": (ctypes.c_int, [P]),
+    "sg_ctx_sync": (ctypes.c_int, [P]),
+    "sg_ctx_stream": (P, [P]),
+    "sg_last_error": (ctypes.c_char_p, []),
+    "sg_version": (ctypes.c_char_p, []),
+    "sg_incidence_build": (ctypes.c_int, [P, I32, P, I64, I32, P, P]),
+    "sg_pattern_count": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P, ctypes.POINTER(I64)]),
+    "sg_pattern_fill": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P, P]),
+    "sg_slots_build": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P]),
+    "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
+    "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError("simit_gb300: %s is missing; run simit_gb300/build.py "
+                               "(or __graft_entry__.build()) first" % path)
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            if hasattr(L, name):
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    """Names declared in SIGNATURES that the loaded library exports."""
+    L = load()
+    return [n for n in SIGNATURES if hasattr(L, n)]
+
+
+def check(rc):
+    if rc != 0:
+        raise SimitError(rc, load().sg_last_error().decode())
+    return rc
+
+
+def call(name, *args):
+    return check(getattr(load(), name)(*args))

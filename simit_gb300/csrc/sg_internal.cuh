@@ -1,0 +1,104 @@
+// Internal helpers shared by the simit_gb300 CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "../../include/simit_gb300.h"
+
+namespace sg {
+
+// Per-context state: the stream every call is ordered on, a grow-only device
+// scratch arena, a device error word and pinned host staging.
+struct Ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  char *arena = nullptr;
+  size_t arena_bytes = 0;
+  int *d_err = nullptr;      // device error word (0 = ok), see ErrCode below
+  int *h_err = nullptr;      // pinned mirror
+  void *h_stage = nullptr;   // pinned staging (64 KB)
+};
+
+// Device-side error codes written to Ctx::d_err by bounds checks.
+enum DevErr : int {
+  DEV_OK = 0,
+  DEV_BAD_ENDPOINT = 1,   // endpoint outside [0, n)
+  DEV_ROW_TOO_LONG = 2,   // candidate list exceeds the sort capacity
+  DEV_SLOT_MISSING = 3,   // (row, col) not found in the pattern
+  DEV_ROW_OVERFLOW = 4,   // assembly row longer than the accumulator
+  DEV_NO_DIAGONAL = 5,    // vertex without a diagonal block
+};
+
+int set_error(int code, const char *fmt, ...);
+
+#define SG_CHECK_CUDA(call)                                                   \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      return ::sg::set_error(SG_ERR_CUDA, "%s failed: %s (%s:%d)", #call,     \
+                             cudaGetErrorString(e_), __FILE__, __LINE__);     \
+  } while (0)
+
+#define SG_CHECK_LAUNCH() SG_CHECK_CUDA(cudaGetLastError())
+
+#define SG_REQUIRE(cond, ...)                                                 \
+  do {                                                                        \
+    if (!(cond)) return ::sg::set_error(SG_ERR_ARG, __VA_ARGS__);             \
+  } while (0)
+
+#define SG_TRY(expr)                                                          \
+  do {                                                                        \
+    int rc_ = (expr);                                                         \
+    if (rc_ != SG_OK) return rc_;                                             \
+  } while (0)
+
+// Bump allocator over the context arena.  reserve() must be called with the
+// total size before any alloc() of one call; the arena only grows (with a
+// stream sync before the old block is released).
+class Scratch {
+ public:
+  explicit Scratch(Ctx *c) : c_(c) {}
+  int reserve(size_t bytes);
+  template <typename T> T *alloc(size_t count) {
+    size_t off = (used_ + 255) & ~size_t(255);
+    used_ = off + count * sizeof(T);
+    return reinterpret_cast<T *>(c_->arena + off);
+  }
+  static size_t bytes_for(size_t count, size_t elem) {
+    return ((count * elem) + 255) & ~size_t(255);
+  }
+
+ private:
+  Ctx *c_;
+  size_t used_ = 0;
+};
+
+// Reads back and clears the device error word (synchronises the stream).
+int check_device_error(Ctx *c, const char *what);
+
+// Exclusive scan of n uint32 counts into out[0..n] (out[n] = total), using
+// scratch from `s` (at most scan_scratch_bytes(n)).  Returns the total
+// through *total_host when non-null (synchronises).
+size_t scan_scratch_bytes(int64_t n);
+int exclusive_scan_u32(Ctx *c, Scratch &s, const uint32_t *in, uint32_t *out,
+                       int64_t n);
+
+// Number of blocks for a grid-stride kernel: `per_sm` blocks on every SM.
+inline int grid_for(const Ctx *c, int64_t work_items, int threads, int per_sm) {
+  int64_t need = (work_items + threads - 1) / threads;
+  int64_t cap = (int64_t)c->num_sms * per_sm;
+  if (need < 1) need = 1;
+  return (int)(need < cap ? need : cap);
+}
+
+inline Ctx *as_ctx(sg_ctx *h) { return reinterpret_cast<Ctx *>(h); }
+
+// dtype helpers
+inline size_t dtype_size(int dt) { return dt == SG_F64 ? 8 : 4; }
+
+}  // namespace sg

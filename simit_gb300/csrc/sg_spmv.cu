@@ -1,0 +1,163 @@
+// sg_bspmv: blocked SpMV entry point (y = A x) and its lanes-per-row choice.
+#include "sg_internal.cuh"
+#include "sg_spmv.cuh"
+
+namespace sg {
+
+template <int G, typename VT, typename XT, typename AT>
+__global__ void __launch_bounds__(256) k_bsr3(int32_t n, const uint32_t *__restrict__ rowptr,
+                                              const uint32_t *__restrict__ colidx,
+                                              const VT *__restrict__ vals,
+                                              const XT *__restrict__ x, XT *__restrict__ y) {
+  const int gl = threadIdx.x & (G - 1);
+  const unsigned mask = group_mask<G>();
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x / G);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
+    AT y0, y1, y2;
+    bsr3_row<G, VT, XT, AT>(rowptr, colidx, vals, x, r, gl, mask, y0, y1, y2);
+    if (gl < 3) y[r * 3 + gl] = (XT)(gl == 0 ? y0 : (gl == 1 ? y1 : y2));
+  }
+}
+
+template <int G, typename VT, typename XT, typename AT>
+__global__ void __launch_bounds__(256) k_csr(int32_t n, const uint32_t *__restrict__ rowptr,
+                                             const uint32_t *__restrict__ colidx,
+                                             const VT *__restrict__ vals,
+                                             const XT *__restrict__ x, XT *__restrict__ y) {
+  const int gl = threadIdx.x & (G - 1);
+  const unsigned mask = group_mask<G>();
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x / G);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
+    AT s = csr_row<G, VT, XT, AT>(rowptr, colidx, vals, x, r, gl, mask);
+    if (gl == 0) y[r] = (XT)s;
+  }
+}
+
+template <int G, int BS, typename VT, typename XT, typename AT>
+__global__ void __launch_bounds__(256) k_bsr(int32_t n, const uint32_t *__restrict__ rowptr,
+                                             const uint32_t *__restrict__ colidx,
+                                             const VT *__restrict__ vals,
+                                             const XT *__restrict__ x, XT *__restrict__ y) {
+  const int gl = threadIdx.x & (G - 1);
+  const unsigned mask = group_mask<G>();
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x / G);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
+    AT o[BS];
+    bsr_row<G, BS, VT, XT, AT>(rowptr, colidx, vals, x, r, gl, mask, o);
+    if (gl == 0)
+      for (int i = 0; i < BS; ++i) y[r * BS + i] = (XT)o[i];
+  }
+}
+
+// Any block size: one thread per block row, the lowered loop order.
+template <typename VT, typename XT, typename AT>
+__global__ void k_bsr_any(int32_t n, int32_t bs, const uint32_t *__restrict__ rowptr,
+                          const uint32_t *__restrict__ colidx, const VT *__restrict__ vals,
+                          const XT *__restrict__ x, XT *__restrict__ y) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    for (int q1 = 0; q1 < bs; ++q1) {
+      AT acc = 0;
+      for (uint32_t qp = rowptr[q]; qp < rowptr[q + 1]; ++qp) {
+        const int64_t p = colidx[qp];
+        AT t = 0;
+        for (int p1 = 0; p1 < bs; ++p1)
+          t += (AT)vals[(size_t)qp * bs * bs + q1 * bs + p1] * (AT)x[p * bs + p1];
+        acc += t;
+      }
+      y[q * bs + q1] = (XT)acc;
+    }
+  }
+}
+
+template <typename VT, typename XT, typename AT>
+static int launch_typed(Ctx *c, int32_t n, int32_t bs, const uint32_t *rp, const uint32_t *ci,
+                        const VT *v, const XT *x, XT *y, int g) {
+  const int T = 256;
+  cudaStream_t st = c->stream;
+  auto grid = [&](int G) { return grid_for(c, (int64_t)n * G, T, 8); };
+#define SG_G_CASE(KERNEL, GV, ...)                                              \
+  case GV:                                                                      \
+    KERNEL<GV, __VA_ARGS__><<<grid(GV), T, 0, st>>>(n, rp, ci, v, x, y);        \
+    break;
+  if (bs == 3) {
+    switch (g) {
+      SG_G_CASE(k_bsr3, 1, VT, XT, AT)
+      SG_G_CASE(k_bsr3, 2, VT, XT, AT)
+      SG_G_CASE(k_bsr3, 4, VT, XT, AT)
+      SG_G_CASE(k_bsr3, 8, VT, XT, AT)
+      SG_G_CASE(k_bsr3, 16, VT, XT, AT)
+      SG_G_CASE(k_bsr3, 32, VT, XT, AT)
+      default: return set_error(SG_ERR_ARG, "sg_bspmv: g=%d not in {1,2,4,8,16,32}", g);
+    }
+  } else if (bs == 1) {
+    switch (g) {
+      SG_G_CASE(k_csr, 1, VT, XT, AT)
+      SG_G_CASE(k_csr, 2, VT, XT, AT)
+      SG_G_CASE(k_csr, 4, VT, XT, AT)
+      SG_G_CASE(k_csr, 8, VT, XT, AT)
+      SG_G_CASE(k_csr, 16, VT, XT, AT)
+      SG_G_CASE(k_csr, 32, VT, XT, AT)
+      default: return set_error(SG_ERR_ARG, "sg_bspmv: g=%d not in {1,2,4,8,16,32}", g);
+    }
+  } else if (bs == 2) {
+    switch (g) {
+      SG_G_CASE(k_bsr, 1, 2, VT, XT, AT)
+      SG_G_CASE(k_bsr, 2, 2, VT, XT, AT)
+      SG_G_CASE(k_bsr, 4, 2, VT, XT, AT)
+      SG_G_CASE(k_bsr, 8, 2, VT, XT, AT)
+      SG_G_CASE(k_bsr, 16, 2, VT, XT, AT)
+      SG_G_CASE(k_bsr, 32, 2, VT, XT, AT)
+      default: return set_error(SG_ERR_ARG, "sg_bspmv: g=%d not in {1,2,4,8,16,32}", g);
+    }
+  } else {
+    k_bsr_any<VT, XT, AT><<<grid_for(c, n, T, 8), T, 0, st>>>(n, bs, rp, ci, v, x, y);
+  }
+#undef SG_G_CASE
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+int default_lanes(int32_t n, int64_t nnzb, int32_t bs) {
+  const double avg = n > 0 ? (double)nnzb / n : 0.0;
+  if (bs == 1) return avg > 24 ? 16 : 8;
+  if (bs == 3) return avg > 24 ? 8 : 4;
+  return 4;
+}
+
+int bspmv_launch(Ctx *c, int32_t n, int32_t bs, const uint32_t *rp, const uint32_t *ci,
+                 int vdt, const void *v, int xdt, const void *x, void *y, int g,
+                 int64_t nnzb_hint) {
+  if (g == 0) g = default_lanes(n, nnzb_hint, bs);
+  if (vdt == SG_F64 && xdt == SG_F64)
+    return launch_typed<double, double, double>(c, n, bs, rp, ci, (const double *)v,
+                                                (const double *)x, (double *)y, g);
+  if (vdt == SG_F32 && xdt == SG_F32)
+    return launch_typed<float, float, float>(c, n, bs, rp, ci, (const float *)v,
+                                             (const float *)x, (float *)y, g);
+  if (vdt == SG_F32 && xdt == SG_F64)
+    return launch_typed<float, double, double>(c, n, bs, rp, ci, (const float *)v,
+                                               (const double *)x, (double *)y, g);
+  return set_error(SG_ERR_UNSUPPORTED, "sg_bspmv: val_dtype=%d vec_dtype=%d", vdt, xdt);
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr,
+                        const uint32_t *colidx, int vdt, const void *vals, int xdt,
+                        const void *x, void *y, int32_t g) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && rowptr && colidx && vals && x && y, "sg_bspmv: null argument");
+  SG_REQUIRE(n >= 0 && bs >= 1 && bs <= 16, "sg_bspmv: bad n=%d bs=%d", n, bs);
+  if (n == 0) return SG_OK;
+  // nnzb is only needed for the default lane choice; read rowptr[n] then.
+  int64_t nnzb = 0;
+  if (g == 0) {
+    SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, rowptr + n, 4, cudaMemcpyDeviceToHost, c->stream));
+    SG_CHECK_CUDA(cudaStreamSynchronize(c->stream));
+    nnzb = *(uint32_t *)c->h_stage;
+  }
+  return bspmv_launch(c, n, bs, rowptr, colidx, vdt, vals, xdt, x, y, g, nnzb);
+}
