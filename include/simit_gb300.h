@@ -85,6 +85,85 @@ int sg_slots_build(sg_ctx *ctx, int32_t n, const int32_t *endpoints,
                    int64_t nE, int32_t card, const uint32_t *rowptr,
                    const uint32_t *colidx, uint32_t *slots);
 
+/* Longest row (blocks) of a pattern; synchronises.  The assembly kernels keep
+ * one row image in shared memory and need this bound. */
+int sg_pattern_maxrow(sg_ctx *ctx, int32_t n, const uint32_t *rowptr,
+                      int32_t *h_maxrow);
+
+/* ---------------------------------------------------------------------
+ * Assembly ("map f to E reduce +").  Replaces the reference's map lowering
+ * (src/inline.cpp:690-888, src/lower/lower_maps.cpp:54-128) and its GPU
+ * atomics (src/backend/gpu/gpu_backend.cpp:788-846).  A group of lanes owns
+ * each block row and sums its elements' contributions in ascending element
+ * order (the reference's order) without atomics.  exact != 0 selects kernels
+ * compiled without multiply-add contraction in the reference's operation
+ * order (FP64 results equal to the reference's up to libm `log`); exact == 0
+ * selects contracted kernels (and the closed-form linear-tet stiffness).
+ * dtype (SG_F32 / SG_F64) is the type of every floating-point array.
+ * ------------------------------------------------------------------- */
+
+/* A bound edge set over one vertex set plus its pattern (all device). */
+typedef struct sg_mesh {
+  int32_t n;                  /* vertices (block rows) */
+  int32_t card;               /* endpoints per element */
+  int64_t nE;                 /* elements */
+  const int32_t *endpoints;   /* int32[nE*card] */
+  const uint32_t *ve_ptr;     /* sg_incidence_build */
+  const uint32_t *ve_idx;
+  const uint32_t *rowptr;     /* sg_pattern_count / sg_pattern_fill */
+  const uint32_t *colidx;
+  int64_t nnzb;
+  int32_t maxrow;             /* sg_pattern_maxrow */
+} sg_mesh;
+
+enum { SG_MODEL_LINEAR = 0, SG_MODEL_NEOHOOKEAN = 1 };
+
+/* Springs: compute_mass_damping over points + compute_elasticity over springs,
+ * MDK = MD + K and f = fmg + fe (apps/springs/isprings.sim:21-68 as form 0;
+ * test/input/program/isprings.sim as form 1).  x, v [n*3], mass [n],
+ * fixed uint8 [n]; k, l0 [nE]; h_grav host double[3].  vals [nnzb*9], f [n*3]. */
+int sg_assemble_springs(sg_ctx *ctx, const sg_mesh *mesh, int dtype, int form,
+                        const void *x, const void *v, const void *mass,
+                        const uint8_t *fixed, const void *k, const void *l0,
+                        double h, double viscous, const double *h_grav,
+                        void *vals, void *f, int exact);
+
+/* Scalar springs of test/input/program/cg.sim: blocks +-a, then
+ * A = diag*I + scale*K on the spring pattern.  a [nE], vals [nnzb]. */
+int sg_assemble_scalar_springs(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
+                               const void *a, double diag, double scale,
+                               void *vals, int exact);
+
+/* precomputeTetMat (femTet.sim; apps/fem/fem_linear.sim:176-193):
+ * B = inv(Ds) [nE*9], W = -det(Ds)/6 [nE], vertex mass m [n] = sum of
+ * 0.25*rho*W in element order. */
+int sg_tet_precompute(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
+                      const void *x, double rho, void *B, void *W, void *mass);
+
+/* compute_stiffness of femTet.sim (SG_MODEL_NEOHOOKEAN: dPdF tangent) or of
+ * apps/fem/fem_linear.sim:105-174 (SG_MODEL_LINEAR: W*B'*E*B), scaled by h*h,
+ * plus the lumped element mass on the diagonal; c int32 [n] (c > 0 =
+ * constrained); mu, lam [nE].  The neo-Hookean path uses nE*16*9 values of
+ * context scratch. */
+int sg_assemble_tet_stiffness(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
+                              int model, const void *x, const int32_t *c,
+                              const void *B, const void *W, const void *mu,
+                              const void *lam, double h, double rho,
+                              void *vals, int exact);
+
+/* compute_force of femTet.sim / fem_linear.sim:55-93; f [n*3]. */
+int sg_assemble_tet_force(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
+                          int model, const void *x, const void *v,
+                          const int32_t *c, const void *B, const void *W,
+                          const void *mu, const void *lam, double h,
+                          double rho, const double *h_grav, void *f, int exact);
+
+/* P1 heat, backward Euler: A = M + dt*K(kappa), b = M*T0 (scalar blocks);
+ * kappa [nE], T0 [n], vals [nnzb], b [n]. */
+int sg_assemble_heat(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
+                     const void *B, const void *W, const void *kappa,
+                     double dt, const void *T0, void *vals, void *b, int exact);
+
 /* ---------------------------------------------------------------------
  * Blocked SpMV  y = A x.  Replaces the lowered SpMV loop nest
  * (src/lower/index_expressions/lower_indexexprs.cpp:630-660).
@@ -101,6 +180,93 @@ int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
  * reduction; synchronises. */
 int sg_dot(sg_ctx *ctx, int64_t len, int vec_dtype, const void *a,
            const void *b, double *h_out);
+
+/* ---------------------------------------------------------------------
+ * Conjugate-gradient solves.  The reference has no CG routine: CG is user
+ * code in each .sim program (apps/springs/isprings.sim:77-93,
+ * apps/fem/fem_linear.sim:211-230, test/input/program/cg.sim:25-53, Jacobi
+ * PCG apps/thermal/thermal.sim:102-130).  These entry points replace those
+ * loops with fused kernels (SpMV + dot, update + preconditioner + dots,
+ * direction) captured in a CUDA graph, with FP64 deterministic reductions.
+ *
+ * precision SG_SOLVE_F64: matrix, vectors and reductions in FP64.
+ * precision SG_SOLVE_MIXED: SpMV and vector bulk in FP32 (matrix stored in
+ *   FP32), dots in FP64, and FP64 reliable updates: whenever the iterated
+ *   residual has dropped by reliable_delta (or says "converged"), x_hi +=
+ *   x_lo and r = b - A x_hi are recomputed in FP64 and the iteration
+ *   continues from the true residual (outer iterative refinement without a
+ *   Krylov restart).
+ * stop: SG_STOP_NORMR2 (r'r <= tol, isprings.sim / femTet.sim),
+ *   SG_STOP_NORMR (||r|| <= tol, cg.sim), SG_STOP_RELATIVE (||r|| <=
+ *   tol*||b||, thermal.sim).
+ * verify = 0 ends when the iterated residual passes, as the reference loops
+ *   do; verify = 1 confirms with the true FP64 residual and continues if it
+ *   does not pass.
+ * check_every > 0 replaces r by b - A x every check_every iterations
+ *   (thermal.sim's mod(iter,50) refresh).
+ * ------------------------------------------------------------------- */
+enum { SG_SOLVE_F64 = 0, SG_SOLVE_MIXED = 1 };
+enum {
+  SG_PRECOND_NONE = 0,
+  SG_PRECOND_JACOBI = 1,        /* point Jacobi (thermal.sim assemble_jacobi) */
+  SG_PRECOND_BLOCK_JACOBI = 2,  /* inverse of each 3x3 diagonal block */
+  SG_PRECOND_LEARNED = 3        /* message-passing network, sg_mpnn_* */
+};
+enum { SG_STOP_NORMR2 = 0, SG_STOP_NORMR = 1, SG_STOP_RELATIVE = 2 };
+enum {
+  SG_STATUS_CONVERGED = 1,
+  SG_STATUS_MAXITER = 2,
+  SG_STATUS_BREAKDOWN = 3,      /* p'Ap <= 0 */
+  SG_STATUS_NAN = 4
+};
+
+/* A blocked-CSR system matrix (device arrays). */
+typedef struct sg_matrix {
+  int32_t n;                 /* block rows */
+  int32_t bs;                /* block size */
+  int64_t nnzb;
+  const uint32_t *rowptr;
+  const uint32_t *colidx;
+  int dtype;                 /* type of vals */
+  const void *vals;
+} sg_matrix;
+
+typedef struct sg_solve_opts {
+  int precision;             /* SG_SOLVE_F64 / SG_SOLVE_MIXED */
+  int precond;               /* SG_PRECOND_* */
+  int stop;                  /* SG_STOP_* */
+  double tol;
+  int32_t maxiters;
+  int32_t verify;
+  int32_t check_every;
+  double reliable_delta;     /* mixed only; 0 -> 0.1 */
+  int32_t lanes;             /* SpMV lanes per block row; 0 = default */
+  int32_t batch;             /* iterations per graph launch (even); 0 = 32 */
+} sg_solve_opts;
+
+typedef struct sg_solve_result {
+  int32_t status;            /* SG_STATUS_* */
+  int32_t iters;
+  int32_t checks;            /* true-residual checks / reliable updates */
+  int32_t fallbacks;         /* learned preconditioner -> Jacobi switches */
+  double normr2;             /* last iterated r'r */
+  double true_normr2;        /* ||b - A x||^2 at exit (FP64) */
+  double bnorm2;             /* b'b */
+} sg_solve_result;
+
+typedef struct sg_solver sg_solver;
+
+/* Set-up: workspace, the FP32 matrix copy (mixed with FP64 input), the
+ * preconditioner and the captured iteration graph. */
+int sg_solver_create(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
+                     sg_solver **out);
+/* Solve A x = b; b, x FP64 device arrays of n*bs; x holds the initial guess
+ * and receives the solution.  Synchronises. */
+int sg_solver_solve(sg_solver *s, const double *b, double *x, sg_solve_result *res);
+int sg_solver_destroy(sg_solver *s);
+/* One-shot create + solve + destroy. */
+int sg_solve(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
+             const double *b, double *x, sg_solve_result *res);
 
 #ifdef __cplusplus
 }

@@ -51,7 +51,7 @@ def lib():
         L.or_cg_normr2_f64.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _D, ctypes.c_int, _P]
         L.or_jacobi_pcg_f64.restype = ctypes.c_int
         L.or_jacobi_pcg_f64.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _D, ctypes.c_int,
-                                        ctypes.c_int, _P]
+                                        ctypes.c_int, ctypes.c_int, _P]
         L.or_springs_assemble.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _P, _I64, _P, _P, _P,
                                           _D, _D, _P, _P, _P, _P, _P]
         L.or_springs_step.restype = ctypes.c_int
@@ -151,13 +151,20 @@ def cg_normr2(n, bs, rowptr, colidx, A, b, x0, tol2, maxiters):
     return x, it, float(nr[0])
 
 
-def jacobi_pcg(n, bs, rowptr, colidx, A, b, x0, tol, maxiters, refresh=50):
+def jacobi_pcg(n, bs, rowptr, colidx, A, b, x0, tol, maxiters, refresh=50, zr_stop=False):
     x = _c(x0, np.float64).copy()
     rr = np.zeros(1)
     it = lib().or_jacobi_pcg_f64(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
                                  _p(_c(A, np.float64)), _p(_c(b, np.float64)), _p(x), tol,
-                                 maxiters, refresh, _p(rr))
+                                 maxiters, refresh, int(zr_stop), _p(rr))
     return x, it, float(rr[0])
+
+
+def relres(n, bs, rowptr, colidx, A, b, x):
+    """||b - A x|| / ||b|| in FP64 with the lowered SpMV."""
+    r = np.asarray(b, np.float64) - spmv(n, bs, rowptr, colidx, np.asarray(A, np.float64),
+                                         np.asarray(x, np.float64))
+    return float(np.linalg.norm(r) / np.linalg.norm(b))
 
 
 def springs_assemble(form, x, v, m, fixed, ep, k, l0, h, viscous, grav, rowptr, colidx):

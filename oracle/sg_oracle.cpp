@@ -215,9 +215,10 @@ int or_cg_normr2_f64(i32 n, i32 bs, const u32 *rowptr, const u32 *colidx,
 // every `refresh` iterations (thermal.sim uses 50).  The preconditioner is
 // point Jacobi on the scalar diagonal of the blocked matrix.  Returns the
 // iteration count; *relres_out = ||b - A x|| / ||b|| recomputed at exit.
+// zr_stop = 1 keeps thermal.sim's second loop condition (z'r > tol^2 b'b).
 int or_jacobi_pcg_f64(i32 n, i32 bs, const u32 *rowptr, const u32 *colidx,
                       const double *A, const double *b, double *x, double tol,
-                      int maxiters, int refresh, double *relres_out) {
+                      int maxiters, int refresh, int zr_stop, double *relres_out) {
   const i64 N = (i64)n * bs, bb = (i64)bs * bs;
   std::vector<double> dinv(N), r(N), z(N), p(N), Ap(N);
   for (i32 q = 0; q < n; ++q) {
@@ -234,7 +235,7 @@ int or_jacobi_pcg_f64(i32 n, i32 bs, const u32 *rowptr, const u32 *colidx,
   const double bb2 = dot<double>(n, bs, b, b);
   const double tol2 = tol * tol * bb2;
   double nr = dot<double>(n, bs, r.data(), r.data());
-  while (nr > tol2 && rsold > tol2 && iter < maxiters) {
+  while (nr > tol2 && (!zr_stop || rsold > tol2) && iter < maxiters) {
     iter = iter + 1;
     spmv<double>(n, bs, rowptr, colidx, A, p.data(), Ap.data());
     double alpha = rsold / dot<double>(n, bs, Ap.data(), p.data());

@@ -24,6 +24,40 @@ class SimitError(RuntimeError):
         self.code = code
 
 
+class Mesh(ctypes.Structure):
+    """sg_mesh"""
+    _fields_ = [("n", I32), ("card", I32), ("nE", I64), ("endpoints", P), ("ve_ptr", P),
+                ("ve_idx", P), ("rowptr", P), ("colidx", P), ("nnzb", I64), ("maxrow", I32)]
+
+
+class Matrix(ctypes.Structure):
+    """sg_matrix"""
+    _fields_ = [("n", I32), ("bs", I32), ("nnzb", I64), ("rowptr", P), ("colidx", P),
+                ("dtype", ctypes.c_int), ("vals", P)]
+
+
+class SolveOpts(ctypes.Structure):
+    """sg_solve_opts"""
+    _fields_ = [("precision", ctypes.c_int), ("precond", ctypes.c_int), ("stop", ctypes.c_int),
+                ("tol", D), ("maxiters", I32), ("verify", I32), ("check_every", I32),
+                ("reliable_delta", D), ("lanes", I32), ("batch", I32)]
+
+
+class SolveResult(ctypes.Structure):
+    """sg_solve_result"""
+    _fields_ = [("status", I32), ("iters", I32), ("checks", I32), ("fallbacks", I32),
+                ("normr2", D), ("true_normr2", D), ("bnorm2", D)]
+
+
+SOLVE_F64, SOLVE_MIXED = 0, 1
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1, 2, 3
+STOP_NORMR2, STOP_NORMR, STOP_RELATIVE = 0, 1, 2
+STATUS = {1: "converged", 2: "maxiter", 3: "breakdown", 4: "nan"}
+MODEL_LINEAR, MODEL_NEOHOOKEAN = 0, 1
+
+_MP = ctypes.POINTER(Mesh)
+_CI = ctypes.c_int
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "sg_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(P)]),
@@ -38,6 +72,19 @@ SIGNATURES = {
     "sg_slots_build": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P]),
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
+    "sg_pattern_maxrow": (_CI, [P, I32, P, ctypes.POINTER(I32)]),
+    "sg_assemble_springs": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, D, D, P, P, P, _CI]),
+    "sg_assemble_scalar_springs": (_CI, [P, _MP, _CI, P, D, D, P, _CI]),
+    "sg_tet_precompute": (_CI, [P, _MP, _CI, P, D, P, P, P]),
+    "sg_assemble_tet_stiffness": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, D, D, P, _CI]),
+    "sg_assemble_tet_force": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, P, D, D, P, P, _CI]),
+    "sg_assemble_heat": (_CI, [P, _MP, _CI, P, P, P, D, P, P, P, _CI]),
+    "sg_solver_create": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(SolveOpts),
+                               ctypes.POINTER(P)]),
+    "sg_solver_solve": (_CI, [P, P, P, ctypes.POINTER(SolveResult)]),
+    "sg_solver_destroy": (_CI, [P]),
+    "sg_solve": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(SolveOpts), P, P,
+                       ctypes.POINTER(SolveResult)]),
 }
 
 _lib = None

@@ -1,0 +1,149 @@
+// Host launchers of the assembly kernels.  Included by sg_assemble_exact.cu
+// (compiled with --fmad=false, namespace sg::exact) and sg_assemble_fast.cu
+// (default contraction, namespace sg::fast); SG_ASM_NS names the namespace
+// and SG_ASM_EXACT selects the operation-order-exact element forms.
+#include "sg_assemble.cuh"
+#include "sg_internal.cuh"
+#include "sg_asm_api.h"
+
+namespace sg {
+namespace SG_ASM_NS {
+
+template <class Elem, int G, int BS, typename T>
+static int launch_rows(Ctx *c, AsmArgs<T> &a) {
+  if (a.n == 0) return SG_OK;
+  const int maxrow = Elem::HAS_MAT ? a.maxrow : 0;
+  const size_t per_group = (size_t)maxrow * (BS * BS * sizeof(T) + 4);
+  int threads = 128;
+  while (threads > G && (threads / G) * per_group > 96 * 1024) threads >>= 1;
+  if ((threads / G) * per_group > 96 * 1024)
+    return set_error(SG_ERR_UNSUPPORTED, "assembly: a row of %d blocks exceeds shared memory",
+                     maxrow);
+  const size_t sh = (threads / G) * per_group;
+  if (sh > 48 * 1024)
+    SG_CHECK_CUDA(cudaFuncSetAttribute(k_rows<Elem, G, BS, T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  a.err = c->d_err;
+  const int grid = grid_for(c, (int64_t)a.n * G, threads, 16);
+  k_rows<Elem, G, BS, T><<<grid, threads, sh, c->stream>>>(a);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+template <typename T>
+static void fill_mesh(AsmArgs<T> &a, const sg_mesh *m) {
+  a.n = m->n;
+  a.card = m->card;
+  a.nE = m->nE;
+  a.ep = m->endpoints;
+  a.ve_ptr = m->ve_ptr;
+  a.ve_idx = m->ve_idx;
+  a.rowptr = m->rowptr;
+  a.colidx = m->colidx;
+  a.maxrow = m->maxrow;
+}
+
+template <typename T>
+int springs(Ctx *c, const sg_mesh *m, int form, const void *x, const void *v, const void *mass,
+            const uint8_t *fixed, const void *k, const void *l0, double h, double viscous,
+            const double *grav, void *vals, void *f) {
+  AsmArgs<T> a;
+  fill_mesh(a, m);
+  a.x = (const T *)x; a.v = (const T *)v; a.m = (const T *)mass; a.fixed = fixed;
+  a.k = (const T *)k; a.l0 = (const T *)l0; a.h = (T)h; a.viscous = (T)viscous;
+  for (int q = 0; q < 3; ++q) a.grav[q] = (T)grav[q];
+  a.form = form;
+  a.vals = (T *)vals; a.f = (T *)f;
+  return launch_rows<SpringElem<T>, 8, 3, T>(c, a);
+}
+
+template <typename T>
+int scalar_springs(Ctx *c, const sg_mesh *m, const void *av, double diag, double scale,
+                   void *vals) {
+  AsmArgs<T> a;
+  fill_mesh(a, m);
+  a.a = (const T *)av; a.diag = (T)diag; a.scale = (T)scale; a.vals = (T *)vals;
+  return launch_rows<ScalarSpringElem<T>, 2, 1, T>(c, a);
+}
+
+template <typename T>
+int heat(Ctx *c, const sg_mesh *m, const void *B, const void *W, const void *kappa, double dt,
+         const void *T0, void *vals, void *b) {
+  AsmArgs<T> a;
+  fill_mesh(a, m);
+  a.B = (const T *)B; a.W = (const T *)W; a.kappa = (const T *)kappa; a.dt = (T)dt;
+  a.T0 = (const T *)T0; a.vals = (T *)vals; a.f = (T *)b;
+  return launch_rows<HeatElem<T>, 4, 1, T>(c, a);
+}
+
+template <typename T>
+int tet_precompute(Ctx *c, const sg_mesh *m, const void *x, double rho, void *B, void *W,
+                   void *mass) {
+  if (m->nE > 0) {
+    k_tet_precompute<T><<<grid_for(c, m->nE, 128, 16), 128, 0, c->stream>>>(
+        m->nE, m->endpoints, (const T *)x, (T *)B, (T *)W);
+    SG_CHECK_LAUNCH();
+  }
+  AsmArgs<T> a;
+  fill_mesh(a, m);
+  a.W = (const T *)W; a.rho = (T)rho; a.f = (T *)mass;
+  return launch_rows<TetMassElem<T>, 1, 1, T>(c, a);
+}
+
+template <typename T>
+int tet_stiffness(Ctx *c, const sg_mesh *m, int model, const void *x, const int32_t *cons,
+                  const void *B, const void *W, const void *mu, const void *lam, double h,
+                  double rho, void *vals, void *eb_scratch) {
+  AsmArgs<T> a;
+  fill_mesh(a, m);
+  a.x = (const T *)x; a.c = cons; a.B = (const T *)B; a.W = (const T *)W;
+  a.mu = (const T *)mu; a.lam = (const T *)lam; a.h = (T)h; a.rho = (T)rho;
+  a.vals = (T *)vals;
+  if (model == SG_MODEL_NEOHOOKEAN) {
+    a.eb = (const T *)eb_scratch;
+    if (m->nE > 0) {
+      k_neo_blocks<T><<<grid_for(c, m->nE, 128, 16), 128, 0, c->stream>>>(a);
+      SG_CHECK_LAUNCH();
+    }
+    return launch_rows<EbGatherElem<T>, 16, 3, T>(c, a);
+  }
+  return launch_rows<LinTetElem<T, SG_ASM_EXACT>, 16, 3, T>(c, a);
+}
+
+template <typename T>
+int tet_force(Ctx *c, const sg_mesh *m, int model, const void *x, const void *v,
+              const int32_t *cons, const void *B, const void *W, const void *mu, const void *lam,
+              double h, double rho, const double *grav, void *f) {
+  AsmArgs<T> a;
+  fill_mesh(a, m);
+  a.x = (const T *)x; a.v = (const T *)v; a.c = cons; a.B = (const T *)B; a.W = (const T *)W;
+  a.mu = (const T *)mu; a.lam = (const T *)lam; a.h = (T)h; a.rho = (T)rho;
+  for (int q = 0; q < 3; ++q) a.grav[q] = (T)grav[q];
+  a.f = (T *)f;
+  if (model == SG_MODEL_NEOHOOKEAN) return launch_rows<TetForceElem<T, true>, 4, 3, T>(c, a);
+  return launch_rows<TetForceElem<T, false>, 4, 3, T>(c, a);
+}
+
+// Explicit instantiations for both precisions.
+#define SG_INST(T)                                                                        \
+  template int springs<T>(Ctx *, const sg_mesh *, int, const void *, const void *,       \
+                          const void *, const uint8_t *, const void *, const void *, double, \
+                          double, const double *, void *, void *);                       \
+  template int scalar_springs<T>(Ctx *, const sg_mesh *, const void *, double, double,    \
+                                 void *);                                                 \
+  template int heat<T>(Ctx *, const sg_mesh *, const void *, const void *, const void *,   \
+                       double, const void *, void *, void *);                             \
+  template int tet_precompute<T>(Ctx *, const sg_mesh *, const void *, double, void *,    \
+                                 void *, void *);                                         \
+  template int tet_stiffness<T>(Ctx *, const sg_mesh *, int, const void *, const int32_t *, \
+                                const void *, const void *, const void *, const void *,   \
+                                double, double, void *, void *);                          \
+  template int tet_force<T>(Ctx *, const sg_mesh *, int, const void *, const void *,      \
+                            const int32_t *, const void *, const void *, const void *,    \
+                            const void *, double, double, const double *, void *);
+SG_INST(float)
+SG_INST(double)
+#undef SG_INST
+
+}  // namespace SG_ASM_NS
+}  // namespace sg

@@ -1,0 +1,535 @@
+// CG / PCG solver runtime: workspace, graph-captured iteration batches and the
+// host decisions taken only at rare check points (true residual, reliable
+// update, convergence).
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "sg_internal.cuh"
+#include "sg_solver_kernels.cuh"
+#include "sg_solver.h"
+
+namespace sg {
+
+__global__ void k_sum_parts(const double *part, int np, double *out) {
+  __shared__ double sh[33];
+  double t = sum_parts(part, np, sh);
+  if (threadIdx.x == 0) *out = t;
+}
+
+template <typename VT>
+__global__ void k_cast_r(int64_t len, const double *__restrict__ rhi, VT *__restrict__ r) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = (VT)rhi[i];
+}
+
+template <typename XT>
+__global__ void k_add_lo(int64_t len, double *__restrict__ xhi, XT *__restrict__ xlo) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    xhi[i] += (double)xlo[i];
+    xlo[i] = XT(0);
+  }
+}
+
+// z = M r (M from dinv), partial sums of r.z.
+template <typename VT, int PREC>
+__global__ void __launch_bounds__(RED_T) k_prec_dot(int64_t len, const VT *__restrict__ r,
+                                                    const VT *__restrict__ dinv,
+                                                    VT *__restrict__ z, double *__restrict__ part) {
+  __shared__ double sh[33];
+  double acc = 0;
+  if (PREC == PK_BLOCK3) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v * 3 < len;
+         v += (int64_t)gridDim.x * blockDim.x) {
+      const VT r0 = r[v * 3], r1 = r[v * 3 + 1], r2 = r[v * 3 + 2];
+      const VT *D = dinv + v * 9;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const VT zk = D[k * 3] * r0 + D[k * 3 + 1] * r1 + D[k * 3 + 2] * r2;
+        z[v * 3 + k] = zk;
+        acc += (double)r[v * 3 + k] * (double)zk;
+      }
+    }
+  } else {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      VT zi = r[i];
+      if (PREC == PK_JACOBI) zi = dinv[i] * zi;
+      if (PREC != PK_NONE) z[i] = zi;
+      acc += (double)r[i] * (double)zi;
+    }
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+template <typename VT>
+__global__ void k_p_update(int64_t len, const VT *__restrict__ z, double beta, VT *__restrict__ p) {
+  const VT b = (VT)beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + b * p[i];
+}
+
+__global__ void __launch_bounds__(RED_T) k_dot2(int64_t len, const double *__restrict__ a,
+                                               const double *__restrict__ b,
+                                               double *__restrict__ part) {
+  __shared__ double sh[33];
+  double acc = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    acc += a[i] * b[i];
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_f64_to_f32(int64_t len, const double *__restrict__ a, float *__restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// ---------------------------------------------------------------------------
+enum Kind { KIND_F64 = 0, KIND_F64_M32 = 1, KIND_MIXED = 2 };
+
+static int alloc_dev(Solver *S, void **p, size_t bytes) {
+  if (bytes == 0) bytes = 256;
+  SG_CHECK_CUDA(cudaMalloc(p, bytes));
+  S->allocs.push_back(*p);
+  return SG_OK;
+}
+
+template <typename MT, typename VT>
+static int launch_k1(Solver *S, cudaStream_t st) {
+  const sg_matrix &A = S->A;
+  const MT *vals = (const MT *)S->bulk_vals;
+  const VT *p = (const VT *)S->p;
+  VT *q = (VT *)S->q;
+#define SG_K1(BSV, GV)                                                                       \
+  k_cg_spmv<BSV, GV, MT, VT><<<S->P1, RED_T, 0, st>>>(S->ctl, A.n, A.bs, A.rowptr, A.colidx, \
+                                                      vals, p, q, S->part1)
+  if (A.bs == 3 || A.bs == 1) {
+    switch (S->G) {
+      case 1: if (A.bs == 3) SG_K1(3, 1); else SG_K1(1, 1); break;
+      case 2: if (A.bs == 3) SG_K1(3, 2); else SG_K1(1, 2); break;
+      case 4: if (A.bs == 3) SG_K1(3, 4); else SG_K1(1, 4); break;
+      case 8: if (A.bs == 3) SG_K1(3, 8); else SG_K1(1, 8); break;
+      case 16: if (A.bs == 3) SG_K1(3, 16); else SG_K1(1, 16); break;
+      default: if (A.bs == 3) SG_K1(3, 32); else SG_K1(1, 32); break;
+    }
+  } else {
+    SG_K1(0, 1);
+  }
+#undef SG_K1
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+template <typename VT, typename XT>
+static int launch_k2(Solver *S, cudaStream_t st, int par) {
+  const VT *p = (const VT *)S->p, *q = (const VT *)S->q, *dinv = (const VT *)S->dinv;
+  VT *r = (VT *)S->r, *z = (VT *)S->z;
+  XT *x = (XT *)S->xupd;
+  switch (S->prec) {
+    case PK_NONE:
+      k_cg_update<VT, XT, PK_NONE><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part1, S->P1,
+                                                            p, q, r, x, z, dinv, S->part2);
+      break;
+    case PK_JACOBI:
+      k_cg_update<VT, XT, PK_JACOBI><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part1,
+                                                              S->P1, p, q, r, x, z, dinv, S->part2);
+      break;
+    case PK_BLOCK3:
+      k_cg_update<VT, XT, PK_BLOCK3><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part1,
+                                                              S->P1, p, q, r, x, z, dinv, S->part2);
+      break;
+    default:
+      k_cg_update<VT, XT, PK_EXTERNAL><<<S->P2, RED_T, 0, st>>>(
+          S->ctl, par, S->len, S->part1, S->P1, p, q, r, x, z, dinv, S->part2);
+      break;
+  }
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+template <typename VT>
+static int launch_k3(Solver *S, cudaStream_t st, int par) {
+  const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
+  k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z, (VT *)S->p);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+template <typename MT, typename VT, typename XT>
+static int capture_batch(Solver *S) {
+  cudaStream_t st = S->c->stream;
+  cudaGraph_t g = nullptr;
+  SG_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int rc = SG_OK;
+  for (int k = 0; k < S->batch && rc == SG_OK; ++k) {
+    const int par = k & 1;
+    rc = launch_k1<MT, VT>(S, st);
+    if (rc == SG_OK) rc = launch_k2<VT, XT>(S, st, par);
+    if (rc == SG_OK && S->ext_prec) rc = S->ext_prec(S, st);
+    if (rc == SG_OK) rc = launch_k3<VT>(S, st, par);
+  }
+  cudaError_t e = cudaStreamEndCapture(st, &g);
+  if (rc != SG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  SG_CHECK_CUDA(e);
+  SG_CHECK_CUDA(cudaGraphInstantiate(&S->gexec, g, 0));
+  cudaGraphDestroy(g);
+  return SG_OK;
+}
+
+// r_hi = b - A x_hi in FP64 (FP64 accumulation); returns ||r_hi||^2 (sync).
+static int true_residual(Solver *S, const double *b, double *rr) {
+  const sg_matrix &A = S->A;
+  cudaStream_t st = S->c->stream;
+  const int PT = S->P1;
+  if (A.bs == 3) {
+    if (A.dtype == SG_F64)
+      k_true_residual3<4, double><<<PT, RED_T, 0, st>>>(A.n, A.rowptr, A.colidx,
+                                                         (const double *)A.vals, S->xw, b,
+                                                         S->rhi, S->part3);
+    else
+      k_true_residual3<4, float><<<PT, RED_T, 0, st>>>(A.n, A.rowptr, A.colidx,
+                                                        (const float *)A.vals, S->xw, b, S->rhi,
+                                                        S->part3);
+  } else {
+    if (A.dtype == SG_F64)
+      k_true_residual_any<double><<<PT, RED_T, 0, st>>>(A.n, A.bs, A.rowptr, A.colidx,
+                                                         (const double *)A.vals, S->xw, b,
+                                                         S->rhi, S->part3);
+    else
+      k_true_residual_any<float><<<PT, RED_T, 0, st>>>(A.n, A.bs, A.rowptr, A.colidx,
+                                                        (const float *)A.vals, S->xw, b, S->rhi,
+                                                        S->part3);
+  }
+  SG_CHECK_LAUNCH();
+  k_sum_parts<<<1, RED_T, 0, st>>>(S->part3, PT, S->dres);
+  SG_CHECK_LAUNCH();
+  SG_CHECK_CUDA(cudaMemcpyAsync(S->c->h_stage, S->dres, 8, cudaMemcpyDeviceToHost, st));
+  SG_CHECK_CUDA(cudaStreamSynchronize(st));
+  *rr = *(double *)S->c->h_stage;
+  return SG_OK;
+}
+
+// r = (VT) r_hi; z = M r (or the external preconditioner); returns r.z (sync).
+template <typename VT>
+static int restart_from_rhi(Solver *S, double *rz) {
+  cudaStream_t st = S->c->stream;
+  k_cast_r<VT><<<S->P2, RED_T, 0, st>>>(S->len, S->rhi, (VT *)S->r);
+  SG_CHECK_LAUNCH();
+  if (S->ext_prec_apply) {
+    SG_TRY(S->ext_prec_apply(S, st));
+  } else {
+    switch (S->prec) {
+      case PK_NONE:
+        k_prec_dot<VT, PK_NONE><<<S->P2, RED_T, 0, st>>>(S->len, (VT *)S->r, (VT *)S->dinv,
+                                                         (VT *)S->z, S->part3);
+        break;
+      case PK_JACOBI:
+        k_prec_dot<VT, PK_JACOBI><<<S->P2, RED_T, 0, st>>>(S->len, (VT *)S->r, (VT *)S->dinv,
+                                                           (VT *)S->z, S->part3);
+        break;
+      default:
+        k_prec_dot<VT, PK_BLOCK3><<<S->P2, RED_T, 0, st>>>(S->len, (VT *)S->r, (VT *)S->dinv,
+                                                           (VT *)S->z, S->part3);
+        break;
+    }
+    SG_CHECK_LAUNCH();
+  }
+  k_sum_parts<<<1, RED_T, 0, st>>>(S->part3, S->P2, S->dres);
+  SG_CHECK_LAUNCH();
+  SG_CHECK_CUDA(cudaMemcpyAsync(S->c->h_stage, S->dres, 8, cudaMemcpyDeviceToHost, st));
+  SG_CHECK_CUDA(cudaStreamSynchronize(st));
+  *rz = *(double *)S->c->h_stage;
+  return SG_OK;
+}
+
+template <typename MT, typename VT, typename XT>
+static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *res) {
+  Ctx *c = S->c;
+  cudaStream_t st = c->stream;
+  const bool mixed = S->kind == KIND_MIXED;
+  memset(res, 0, sizeof(*res));
+  SG_CHECK_CUDA(cudaMemcpyAsync(S->xw, x, S->len * 8, cudaMemcpyDeviceToDevice, st));
+  if (mixed) SG_CHECK_CUDA(cudaMemsetAsync(S->xlo, 0, S->len * sizeof(XT), st));
+  // b'b
+  dot_launch(c, S->len, b, b, S->part3, S->dres);
+  SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, S->dres, 8, cudaMemcpyDeviceToHost, st));
+  SG_CHECK_CUDA(cudaStreamSynchronize(st));
+  const double bb = *(double *)c->h_stage;
+  res->bnorm2 = bb;
+  double tol2;
+  switch (S->o.stop) {
+    case SG_STOP_NORMR2: tol2 = S->o.tol; break;
+    case SG_STOP_NORMR: tol2 = S->o.tol * S->o.tol; break;
+    default: tol2 = S->o.tol * S->o.tol * bb; break;
+  }
+  double rr = 0;
+  SG_TRY(true_residual(S, b, &rr));
+  res->normr2 = rr;
+  res->true_normr2 = rr;
+  int iters = 0;
+  int status = 0;
+  if (!(rr > tol2)) status = SG_STATUS_CONVERGED;
+  if (!std::isfinite(rr)) status = SG_STATUS_NAN;
+  double rz = 0;
+  if (!status) SG_TRY(restart_from_rhi<VT>(S, &rz));
+  if (!status) {
+    const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
+    SG_CHECK_CUDA(cudaMemcpyAsync(S->p, z, S->len * sizeof(VT), cudaMemcpyDeviceToDevice, st));
+  }
+  const double delta = S->o.reliable_delta > 0 ? S->o.reliable_delta : 0.1;
+  double rr_ref = rr;
+  SolveCtl *h = S->hctl;
+  while (!status) {
+    // (re)start a batch with the current state in parity slot 0
+    memset(h, 0, sizeof(*h));
+    h->status = ST_RUNNING;
+    h->iter[0] = h->iter[1] = iters;
+    h->maxiters = S->o.maxiters;
+    h->check_every = S->o.check_every;
+    h->flexible = S->flexible;
+    h->rz[0] = h->rz[1] = rz;
+    h->tol2 = tol2;
+    h->upd2 = mixed ? delta * delta * rr_ref : 0.0;
+    if (iters >= S->o.maxiters) {
+      status = SG_STATUS_MAXITER;
+      break;
+    }
+    SG_CHECK_CUDA(cudaMemcpyAsync(S->ctl, h, sizeof(SolveCtl), cudaMemcpyHostToDevice, st));
+    for (;;) {
+      SG_CHECK_CUDA(cudaGraphLaunch(S->gexec, st));
+      SG_CHECK_CUDA(cudaMemcpyAsync(h, S->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, st));
+      SG_CHECK_CUDA(cudaStreamSynchronize(st));
+      if (h->status != ST_RUNNING) break;
+    }
+    // the slot K3 wrote last holds the larger iteration count
+    const int cur = h->iter[1] > h->iter[0] ? 1 : 0;
+    iters = h->iter[cur];
+    res->normr2 = h->last_rr;
+    if (h->status == ST_BREAKDOWN) status = SG_STATUS_BREAKDOWN;
+    else if (h->status == ST_NAN) status = SG_STATUS_NAN;
+    if (status) break;
+    // ST_NEED_CHECK or ST_MAXITER: fold x_lo in, look at the true residual
+    if (mixed) {
+      k_add_lo<XT><<<S->P2, RED_T, 0, st>>>(S->len, S->xw, (XT *)S->xlo);
+      SG_CHECK_LAUNCH();
+    }
+    const bool iter_conv = h->last_rr <= tol2;
+    if (!S->o.verify && !mixed && iter_conv) {
+      status = SG_STATUS_CONVERGED;
+      break;
+    }
+    res->checks++;
+    SG_TRY(true_residual(S, b, &rr));
+    if (!std::isfinite(rr)) {
+      status = SG_STATUS_NAN;
+      break;
+    }
+    if (rr <= tol2 && (S->o.verify || iter_conv || mixed)) {
+      status = SG_STATUS_CONVERGED;
+      break;
+    }
+    if (h->status == ST_MAXITER || iters >= S->o.maxiters) {
+      status = SG_STATUS_MAXITER;
+      break;
+    }
+    // residual replacement: continue from the true residual, same direction
+    const double rz_old = h->rz[cur ^ 1];
+    double rz_new = 0;
+    SG_TRY(restart_from_rhi<VT>(S, &rz_new));
+    const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
+    k_p_update<VT><<<S->P2, RED_T, 0, st>>>(S->len, z, rz_new / rz_old, (VT *)S->p);
+    SG_CHECK_LAUNCH();
+    rz = rz_new;
+    rr_ref = rr;
+  }
+  if (mixed && status) {
+    k_add_lo<XT><<<S->P2, RED_T, 0, st>>>(S->len, S->xw, (XT *)S->xlo);
+    SG_CHECK_LAUNCH();
+  }
+  SG_CHECK_CUDA(cudaMemcpyAsync(x, S->xw, S->len * 8, cudaMemcpyDeviceToDevice, st));
+  if (S->o.verify || mixed) {
+    double rt = 0;
+    SG_TRY(true_residual(S, b, &rt));
+    res->true_normr2 = rt;
+  } else {
+    res->true_normr2 = rr;
+  }
+  SG_CHECK_CUDA(cudaStreamSynchronize(st));
+  res->status = status;
+  res->iters = iters;
+  return SG_OK;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" {
+
+int sg_solver_create(sg_ctx *h, const sg_matrix *A, const sg_solve_opts *o, sg_solver **out) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && A && o && out, "sg_solver_create: null argument");
+  SG_REQUIRE(A->n >= 1 && A->bs >= 1 && A->rowptr && A->colidx && A->vals,
+             "sg_solver_create: bad matrix");
+  SG_REQUIRE(A->dtype == SG_F32 || A->dtype == SG_F64, "sg_solver_create: dtype");
+  SG_REQUIRE(o->precision == SG_SOLVE_F64 || o->precision == SG_SOLVE_MIXED,
+             "sg_solver_create: precision %d", o->precision);
+  SG_REQUIRE(o->precond >= SG_PRECOND_NONE && o->precond <= SG_PRECOND_BLOCK_JACOBI,
+             "sg_solver_create: precond %d (learned preconditioners use sg_mpnn_solver_create)",
+             o->precond);
+  SG_REQUIRE(o->precond != SG_PRECOND_BLOCK_JACOBI || A->bs == 3,
+             "sg_solver_create: block Jacobi needs bs = 3");
+  SG_REQUIRE(o->maxiters >= 0, "sg_solver_create: maxiters");
+  Solver *S = new Solver();
+  int rc = solver_init(c, A, o, S, nullptr);
+  if (rc != SG_OK) {
+    solver_free(S);
+    return rc;
+  }
+  *out = reinterpret_cast<sg_solver *>(S);
+  return SG_OK;
+}
+
+int sg_solver_solve(sg_solver *hs, const double *b, double *x, sg_solve_result *res) {
+  Solver *S = reinterpret_cast<Solver *>(hs);
+  SG_REQUIRE(S && b && x && res, "sg_solver_solve: null argument");
+  return solver_solve(S, b, x, res);
+}
+
+int sg_solver_destroy(sg_solver *hs) {
+  solver_free(reinterpret_cast<Solver *>(hs));
+  return SG_OK;
+}
+
+int sg_solve(sg_ctx *h, const sg_matrix *A, const sg_solve_opts *o, const double *b, double *x,
+             sg_solve_result *res) {
+  sg_solver *s = nullptr;
+  SG_TRY(sg_solver_create(h, A, o, &s));
+  int rc = sg_solver_solve(s, b, x, res);
+  sg_solver_destroy(s);
+  return rc;
+}
+
+}  // extern "C"
+
+namespace sg {
+
+void dot_launch(Ctx *c, int64_t len, const double *a, const double *b, double *part,
+                double *dres) {
+  const int P = grid_for(c, len, RED_T, 4);
+  k_dot2<<<P, RED_T, 0, c->stream>>>(len, a, b, part);
+  k_sum_parts<<<1, RED_T, 0, c->stream>>>(part, P, dres);
+}
+
+int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
+                int (*ext_setup)(Solver *)) {
+  S->c = c;
+  S->A = *A;
+  S->o = *o;
+  if (S->o.batch <= 0) S->o.batch = 32;
+  S->batch = (S->o.batch + 1) & ~1;
+  S->len = (int64_t)A->n * A->bs;
+  S->G = o->lanes > 0 ? o->lanes : default_lanes(A->n, A->nnzb, A->bs);
+  if (A->bs != 3 && A->bs != 1) S->G = 1;
+  S->P1 = grid_for(c, (int64_t)A->n * (A->bs == 3 || A->bs == 1 ? S->G : 1), RED_T, 8);
+  S->P2 = grid_for(c, S->len, RED_T, 4);
+  S->prec = o->precond == SG_PRECOND_JACOBI ? PK_JACOBI
+            : o->precond == SG_PRECOND_BLOCK_JACOBI ? PK_BLOCK3
+            : o->precond == SG_PRECOND_LEARNED ? PK_EXTERNAL : PK_NONE;
+  if (o->precision == SG_SOLVE_MIXED) S->kind = KIND_MIXED;
+  else S->kind = A->dtype == SG_F64 ? KIND_F64 : KIND_F64_M32;
+  const size_t vt = S->kind == KIND_MIXED ? 4 : 8;
+  const int np = S->P1 > S->P2 ? S->P1 : S->P2;
+  SG_TRY(alloc_dev(S, (void **)&S->ctl, sizeof(SolveCtl)));
+  SG_CHECK_CUDA(cudaMallocHost((void **)&S->hctl, sizeof(SolveCtl)));
+  SG_TRY(alloc_dev(S, &S->r, S->len * vt));
+  SG_TRY(alloc_dev(S, &S->p, S->len * vt));
+  SG_TRY(alloc_dev(S, &S->q, S->len * vt));
+  SG_TRY(alloc_dev(S, &S->z, S->len * vt));
+  SG_TRY(alloc_dev(S, (void **)&S->xw, S->len * 8));
+  SG_TRY(alloc_dev(S, (void **)&S->rhi, S->len * 8));
+  SG_TRY(alloc_dev(S, (void **)&S->part1, (size_t)np * 8));
+  SG_TRY(alloc_dev(S, (void **)&S->part2, (size_t)np * 3 * 8));
+  SG_TRY(alloc_dev(S, (void **)&S->part3, (size_t)np * 8));
+  SG_TRY(alloc_dev(S, (void **)&S->dres, 64));
+  if (S->kind == KIND_MIXED) {
+    SG_TRY(alloc_dev(S, &S->xlo, S->len * 4));
+    S->xupd = S->xlo;
+  } else {
+    S->xupd = S->xw;
+  }
+  // bulk matrix values
+  S->bulk_vals = A->vals;
+  if (S->kind == KIND_MIXED && A->dtype == SG_F64) {
+    const int64_t nv = A->nnzb * A->bs * A->bs;
+    SG_TRY(alloc_dev(S, &S->vals32, nv * 4));
+    k_f64_to_f32<<<grid_for(c, nv, 256, 8), 256, 0, c->stream>>>(nv, (const double *)A->vals,
+                                                                 (float *)S->vals32);
+    SG_CHECK_LAUNCH();
+    S->bulk_vals = S->vals32;
+  }
+  // preconditioner data
+  if (S->prec == PK_JACOBI || S->prec == PK_BLOCK3) {
+    const int blk = S->prec == PK_BLOCK3;
+    SG_TRY(alloc_dev(S, &S->dinv, (blk ? (int64_t)A->n * 9 : S->len) * vt));
+    const int g = grid_for(c, A->n, 256, 8);
+    if (vt == 4) {
+      if (A->dtype == SG_F64)
+        k_diag_inv<double, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                            (const double *)A->vals,
+                                                            (float *)S->dinv, blk, c->d_err);
+      else
+        k_diag_inv<float, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                           (const float *)A->vals,
+                                                           (float *)S->dinv, blk, c->d_err);
+    } else {
+      if (A->dtype == SG_F64)
+        k_diag_inv<double, double><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                             (const double *)A->vals,
+                                                             (double *)S->dinv, blk, c->d_err);
+      else
+        k_diag_inv<float, double><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                            (const float *)A->vals,
+                                                            (double *)S->dinv, blk, c->d_err);
+    }
+    SG_CHECK_LAUNCH();
+    SG_TRY(check_device_error(c, "sg_solver_create (diagonal)"));
+  }
+  if (ext_setup) SG_TRY(ext_setup(S));
+  switch (S->kind) {
+    case KIND_F64: return capture_batch<double, double, double>(S);
+    case KIND_F64_M32: return capture_batch<float, double, double>(S);
+    default: return capture_batch<float, float, float>(S);
+  }
+}
+
+int solver_solve(Solver *S, const double *b, double *x, sg_solve_result *res) {
+  switch (S->kind) {
+    case KIND_F64: return solve_impl<double, double, double>(S, b, x, res);
+    case KIND_F64_M32: return solve_impl<float, double, double>(S, b, x, res);
+    default: return solve_impl<float, float, float>(S, b, x, res);
+  }
+}
+
+void solver_free(Solver *S) {
+  if (!S) return;
+  if (S->c) cudaStreamSynchronize(S->c->stream);
+  if (S->gexec) cudaGraphExecDestroy(S->gexec);
+  for (void *p : S->allocs) cudaFree(p);
+  if (S->hctl) cudaFreeHost(S->hctl);
+  if (S->ext_free) S->ext_free(S);
+  delete S;
+}
+
+}  // namespace sg

@@ -1,0 +1,47 @@
+// Solver state shared by sg_solver.cu and the learned-preconditioner solver.
+#pragma once
+#include <vector>
+
+#include "sg_internal.cuh"
+#include "sg_solver_kernels.cuh"
+
+namespace sg {
+
+struct Solver {
+  Ctx *c = nullptr;
+  sg_matrix A{};
+  sg_solve_opts o{};
+  int kind = 0;        // KIND_F64 / KIND_F64_M32 / KIND_MIXED
+  int prec = 0;        // PrecKind
+  int flexible = 0;    // Polak-Ribiere beta (variable preconditioner)
+  int batch = 32;
+  int64_t len = 0;     // n * bs
+  int G = 4, P1 = 1, P2 = 1;
+  const void *bulk_vals = nullptr;  // matrix values used by the iteration
+  void *vals32 = nullptr;
+  void *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *xlo = nullptr, *dinv = nullptr;
+  void *xupd = nullptr;             // the x the iteration updates (xw or xlo)
+  double *xw = nullptr, *rhi = nullptr;
+  double *part1 = nullptr, *part2 = nullptr, *part3 = nullptr, *dres = nullptr;
+  SolveCtl *ctl = nullptr, *hctl = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<void *> allocs;
+  // External preconditioner hooks (learned preconditioner).  ext_prec runs
+  // inside the captured iteration between K2 and K3: z = M(r) and the
+  // partials rr | rz | zq into part2.  ext_prec_apply: z = M(r) and the
+  // partials of r.z into part3 (set-up / restart).
+  int (*ext_prec)(Solver *, cudaStream_t) = nullptr;
+  int (*ext_prec_apply)(Solver *, cudaStream_t) = nullptr;
+  void (*ext_free)(Solver *) = nullptr;
+  void *ext = nullptr;
+};
+
+int default_lanes(int32_t n, int64_t nnzb, int32_t bs);
+int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
+                int (*ext_setup)(Solver *));
+int solver_solve(Solver *S, const double *b, double *x, sg_solve_result *res);
+void solver_free(Solver *S);
+void dot_launch(Ctx *c, int64_t len, const double *a, const double *b, double *part,
+                double *dres);
+
+}  // namespace sg

@@ -1,0 +1,352 @@
+// CG / PCG iteration kernels.
+//
+// The reference runs CG as user code (apps/springs/isprings.sim:77-93,
+// apps/fem/fem_linear.sim:211-230, Jacobi-PCG apps/thermal/thermal.sim:
+// 102-130): one SpMV, dots and axpys per iteration, each a separate loop; on
+// its GPU backend every loop is a child kernel and every dot an atomic
+// (src/backend/gpu/gpu_backend.cpp:335-365).  Here one iteration is three
+// kernels with the dots fused in:
+//   K1  q = A p                     + partial sums of p.q
+//   K2  alpha = rz/pq; x += alpha p; r -= alpha q; z = M r
+//                                   + partial sums of r.r, r.z (and z.q)
+//   K3  beta; p = z + beta p; decide RUNNING / NEED_CHECK / MAXITER
+// Every dot is an FP64 two-level sum: per-block partials in a fixed order,
+// then each consumer block re-sums the partials in the same fixed order, so
+// all blocks see identical scalars and results are run-to-run deterministic.
+// Scalars that change per iteration live in two slots indexed by iteration
+// parity, so no kernel reads a slot that another block of the same kernel
+// writes.  A batch of iterations is captured once in a CUDA graph; kernels
+// return immediately once the status leaves RUNNING.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sg_spmv.cuh"
+
+namespace sg {
+
+enum SolveStatus : int {
+  ST_RUNNING = 0,
+  ST_CONVERGED = 1,
+  ST_MAXITER = 2,
+  ST_BREAKDOWN = 3,
+  ST_NAN = 4,
+  ST_NEED_CHECK = 5,
+};
+
+struct SolveCtl {
+  int status;
+  int iter[2];        // iteration count, parity slots
+  int maxiters;
+  int check_every;    // > 0: NEED_CHECK every check_every iterations
+  int flexible;       // Polak-Ribiere beta
+  int pad[2];
+  double rz[2];       // r.z of the current direction, parity slots
+  double tol2;        // convergence threshold on r.r (iterated)
+  double upd2;        // NEED_CHECK when r.r < upd2 (reliable update); 0 = off
+  double last_rr;     // r.r at the last K3 (diagnostics)
+  double last_alpha;
+};
+
+constexpr int RED_T = 256;
+
+// Block-wide FP64 sum of one value per thread (fixed order), result to all.
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) sh[32] = t;
+  }
+  __syncthreads();
+  return sh[32];
+}
+
+// Sum of np partials (every block computes the same value).
+__device__ __forceinline__ double sum_parts(const double *part, int np, double *sh) {
+  double a = 0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) a += part[i];
+  return block_sum(a, sh);
+}
+
+template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
+
+// K1: q = A p, partial p.q.  BS = 3 or 1 (G lanes per row), 0 = any bs.
+template <int BS, int G, typename MT, typename VT>
+__global__ void __launch_bounds__(RED_T) k_cg_spmv(const SolveCtl *__restrict__ ctl, int32_t n,
+                                                   int32_t bs, const uint32_t *__restrict__ rowptr,
+                                                   const uint32_t *__restrict__ colidx,
+                                                   const MT *__restrict__ vals,
+                                                   const VT *__restrict__ p, VT *__restrict__ q,
+                                                   double *__restrict__ part) {
+  __shared__ double sh[33];
+  if (ctl->status != ST_RUNNING) return;
+  double acc = 0;
+  if (BS == 3 || BS == 1) {
+    const int gl = threadIdx.x & (G - 1);
+    const unsigned mask = group_mask<G>();
+    const int64_t stride = (int64_t)gridDim.x * (blockDim.x / G);
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
+      if (BS == 3) {
+        VT y0, y1, y2;
+        bsr3_row<G, MT, VT, VT>(rowptr, colidx, vals, p, r, gl, mask, y0, y1, y2);
+        if (gl == 0) {
+          q[r * 3 + 0] = y0; q[r * 3 + 1] = y1; q[r * 3 + 2] = y2;
+          acc += (double)p[r * 3 + 0] * (double)y0 + (double)p[r * 3 + 1] * (double)y1 +
+                 (double)p[r * 3 + 2] * (double)y2;
+        }
+      } else {
+        VT y = csr_row<G, MT, VT, VT>(rowptr, colidx, vals, p, r, gl, mask);
+        if (gl == 0) {
+          q[r] = y;
+          acc += (double)p[r] * (double)y;
+        }
+      }
+    }
+  } else {
+    for (int64_t qq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; qq < n;
+         qq += (int64_t)gridDim.x * blockDim.x) {
+      for (int q1 = 0; q1 < bs; ++q1) {
+        VT s = 0;
+        for (uint32_t qp = rowptr[qq]; qp < rowptr[qq + 1]; ++qp) {
+          const int64_t c = colidx[qp];
+          VT t = 0;
+          for (int p1 = 0; p1 < bs; ++p1)
+            t += (VT)vals[(size_t)qp * bs * bs + q1 * bs + p1] * p[c * bs + p1];
+          s += t;
+        }
+        q[qq * bs + q1] = s;
+        acc += (double)p[qq * bs + q1] * (double)s;
+      }
+    }
+  }
+  double tot = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
+// Preconditioner kinds applied inside K2.
+enum PrecKind : int { PK_NONE = 0, PK_JACOBI = 1, PK_BLOCK3 = 2, PK_EXTERNAL = 3 };
+
+// K2: alpha, x/r update, z = M r, partials of r.r, r.z, z.q.
+// part_in: np1 partials of p.q; part_out: 3 * gridDim.x (rr | rz | zq).
+template <typename VT, typename XT, int PREC>
+__global__ void __launch_bounds__(RED_T) k_cg_update(SolveCtl *ctl, int par, int64_t len,
+                                                     const double *__restrict__ part_in, int np1,
+                                                     const VT *__restrict__ p,
+                                                     const VT *__restrict__ q, VT *__restrict__ r,
+                                                     XT *__restrict__ x, VT *__restrict__ z,
+                                                     const VT *__restrict__ dinv,
+                                                     double *__restrict__ part_out) {
+  __shared__ double sh[33];
+  if (ctl->status != ST_RUNNING) return;
+  const double pq = sum_parts(part_in, np1, sh);
+  const double rz = ctl->rz[par];
+  if (!(pq > 0.0) || !isfinite(pq)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
+    return;
+  }
+  const double alpha = rz / pq;
+  const VT a = (VT)alpha;
+  double rr = 0, rzs = 0, zq = 0;
+  if (PREC == PK_BLOCK3) {
+    // 3x3 block-Jacobi: dinv holds 9 values per vertex; one thread per vertex
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v * 3 < len;
+         v += (int64_t)gridDim.x * blockDim.x) {
+      VT rv[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int64_t i = v * 3 + k;
+        x[i] = (XT)(x[i] + (XT)(a * p[i]));
+        rv[k] = r[i] - a * q[i];
+        r[i] = rv[k];
+      }
+      const VT *D = dinv + v * 9;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const VT zk = D[k * 3] * rv[0] + D[k * 3 + 1] * rv[1] + D[k * 3 + 2] * rv[2];
+        z[v * 3 + k] = zk;
+        rr += (double)rv[k] * (double)rv[k];
+        rzs += (double)rv[k] * (double)zk;
+        zq += (double)zk * (double)q[v * 3 + k];
+      }
+    }
+  } else {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const VT pi = p[i], qi = q[i];
+      x[i] = (XT)(x[i] + (XT)(a * pi));
+      const VT ri = r[i] - a * qi;
+      r[i] = ri;
+      VT zi = ri;
+      if (PREC == PK_JACOBI) zi = dinv[i] * ri;
+      if (PREC != PK_EXTERNAL) {
+        if (PREC != PK_NONE) z[i] = zi;
+        rzs += (double)ri * (double)zi;
+        zq += (double)zi * (double)qi;
+      }
+      rr += (double)ri * (double)ri;
+    }
+  }
+  const double t0 = block_sum(rr, sh);
+  const double t1 = block_sum(rzs, sh);
+  const double t2 = block_sum(zq, sh);
+  if (threadIdx.x == 0) {
+    part_out[blockIdx.x] = t0;
+    part_out[gridDim.x + blockIdx.x] = t1;
+    part_out[2 * gridDim.x + blockIdx.x] = t2;
+    if (blockIdx.x == 0) ctl->last_alpha = alpha;
+  }
+}
+
+// K3: beta, direction update, control decisions.
+// part_in: 3 * np2 partials (rr | rz | zq) from K2 (or from the external
+// preconditioner's dot kernel).
+template <typename VT>
+__global__ void __launch_bounds__(RED_T) k_cg_direction(SolveCtl *ctl, int par, int64_t len,
+                                                        const double *__restrict__ part_in,
+                                                        int np2, const VT *__restrict__ z,
+                                                        VT *__restrict__ p) {
+  __shared__ double sh[33];
+  if (ctl->status != ST_RUNNING) return;
+  const double rr = sum_parts(part_in, np2, sh);
+  const double rznew = sum_parts(part_in + np2, np2, sh);
+  const double zq = sum_parts(part_in + 2 * np2, np2, sh);
+  const double rzold = ctl->rz[par];
+  const int it = ctl->iter[par] + 1;
+  int st = ST_RUNNING;
+  if (!isfinite(rr) || !isfinite(rznew)) st = ST_NAN;
+  else if (rr <= ctl->tol2) st = ST_NEED_CHECK;
+  else if (ctl->upd2 > 0.0 && rr < ctl->upd2) st = ST_NEED_CHECK;
+  else if (ctl->check_every > 0 && it % ctl->check_every == 0) st = ST_NEED_CHECK;
+  else if (it >= ctl->maxiters) st = ST_MAXITER;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->iter[par ^ 1] = it;
+    ctl->rz[par ^ 1] = rznew;
+    ctl->last_rr = rr;
+    if (st != ST_RUNNING) ctl->status = st;
+  }
+  if (st != ST_RUNNING) return;
+  // Fletcher-Reeves (the reference's beta = r'r_new / r'r_old, with z) or
+  // Polak-Ribiere for a variable preconditioner: (z.r_new - z.r_old)/rz_old
+  // where r_new - r_old = -alpha q.
+  double beta;
+  if (ctl->flexible) beta = (-ctl->last_alpha * zq) / rzold;
+  else beta = rznew / rzold;
+  const VT b = (VT)beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + b * p[i];
+}
+
+// ---------------------------------------------------------------------------
+// Set-up / check kernels
+// ---------------------------------------------------------------------------
+
+// r_hi = b - A x_hi with FP64 accumulation (matrix MT, x FP64).
+template <int G, typename MT>
+__global__ void __launch_bounds__(RED_T) k_true_residual3(int32_t n,
+                                                          const uint32_t *__restrict__ rowptr,
+                                                          const uint32_t *__restrict__ colidx,
+                                                          const MT *__restrict__ vals,
+                                                          const double *__restrict__ x,
+                                                          const double *__restrict__ b,
+                                                          double *__restrict__ rhi,
+                                                          double *__restrict__ part) {
+  __shared__ double sh[33];
+  const int gl = threadIdx.x & (G - 1);
+  const unsigned mask = group_mask<G>();
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x / G);
+  double acc = 0;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
+    double y0, y1, y2;
+    bsr3_row<G, MT, double, double>(rowptr, colidx, vals, x, r, gl, mask, y0, y1, y2);
+    if (gl == 0) {
+      const double r0 = b[r * 3] - y0, r1 = b[r * 3 + 1] - y1, r2 = b[r * 3 + 2] - y2;
+      rhi[r * 3] = r0; rhi[r * 3 + 1] = r1; rhi[r * 3 + 2] = r2;
+      acc += r0 * r0 + r1 * r1 + r2 * r2;
+    }
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Any bs (one thread per row).
+template <typename MT>
+__global__ void k_true_residual_any(int32_t n, int32_t bs, const uint32_t *__restrict__ rowptr,
+                                    const uint32_t *__restrict__ colidx,
+                                    const MT *__restrict__ vals, const double *__restrict__ x,
+                                    const double *__restrict__ b, double *__restrict__ rhi,
+                                    double *__restrict__ part) {
+  __shared__ double sh[33];
+  double acc = 0;
+  for (int64_t qq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; qq < n;
+       qq += (int64_t)gridDim.x * blockDim.x) {
+    for (int q1 = 0; q1 < bs; ++q1) {
+      double s = 0;
+      for (uint32_t qp = rowptr[qq]; qp < rowptr[qq + 1]; ++qp) {
+        const int64_t c = colidx[qp];
+        double t = 0;
+        for (int p1 = 0; p1 < bs; ++p1)
+          t += (double)vals[(size_t)qp * bs * bs + q1 * bs + p1] * x[c * bs + p1];
+        s += t;
+      }
+      const double rv = b[qq * bs + q1] - s;
+      rhi[qq * bs + q1] = rv;
+      acc += rv * rv;
+    }
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Point-Jacobi inverse diagonal (VT) from the diagonal blocks; bs3 = 1 also
+// writes the inverted 3x3 diagonal blocks (block Jacobi).
+template <typename MT, typename VT>
+__global__ void k_diag_inv(int32_t n, int32_t bs, const uint32_t *__restrict__ rowptr,
+                           const uint32_t *__restrict__ colidx, const MT *__restrict__ vals,
+                           VT *__restrict__ dinv, int block3, int *err) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t lo = rowptr[v], hi = rowptr[v + 1];
+    const uint32_t end = hi;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (colidx[mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
+    }
+    if (lo >= end || colidx[lo] != (uint32_t)v) {
+      atomicCAS(err, 0, 5 /* DEV_NO_DIAGONAL */);
+      for (int k = 0; k < (block3 ? 9 : bs); ++k) dinv[v * (block3 ? 9 : bs) + k] = VT(0);
+      continue;
+    }
+    const MT *D = vals + (size_t)lo * bs * bs;
+    if (!block3) {
+      for (int k = 0; k < bs; ++k) {
+        const double d = (double)D[k * bs + k];
+        dinv[v * bs + k] = d != 0.0 ? (VT)(1.0 / d) : VT(0);
+      }
+    } else {
+      double a[9];
+      for (int k = 0; k < 9; ++k) a[k] = (double)D[k];
+      const double c00 = a[4] * a[8] - a[5] * a[7], c01 = a[5] * a[6] - a[3] * a[8],
+                   c02 = a[3] * a[7] - a[4] * a[6];
+      const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+      if (det == 0.0 || !isfinite(det)) {  // singular block: fall back to point Jacobi
+        for (int k = 0; k < 9; ++k) dinv[v * 9 + k] = VT(0);
+        for (int k = 0; k < 3; ++k)
+          dinv[v * 9 + k * 4] = a[k * 4] != 0.0 ? (VT)(1.0 / a[k * 4]) : VT(0);
+        continue;
+      }
+      const double id = 1.0 / det;
+      const double inv[9] = {c00 * id, (a[2] * a[7] - a[1] * a[8]) * id, (a[1] * a[5] - a[2] * a[4]) * id,
+                             c01 * id, (a[0] * a[8] - a[2] * a[6]) * id, (a[2] * a[3] - a[0] * a[5]) * id,
+                             c02 * id, (a[1] * a[6] - a[0] * a[7]) * id, (a[0] * a[4] - a[1] * a[3]) * id};
+      for (int k = 0; k < 9; ++k) dinv[v * 9 + k] = (VT)inv[k];
+    }
+  }
+}
+
+}  // namespace sg

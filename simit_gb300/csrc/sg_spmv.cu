@@ -15,7 +15,13 @@ __global__ void __launch_bounds__(256) k_bsr3(int32_t n, const uint32_t *__restr
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
     AT y0, y1, y2;
     bsr3_row<G, VT, XT, AT>(rowptr, colidx, vals, x, r, gl, mask, y0, y1, y2);
-    if (gl < 3) y[r * 3 + gl] = (XT)(gl == 0 ? y0 : (gl == 1 ? y1 : y2));
+    if (G >= 3) {
+      if (gl < 3) y[r * 3 + gl] = (XT)(gl == 0 ? y0 : (gl == 1 ? y1 : y2));
+    } else if (gl == 0) {
+      y[r * 3 + 0] = (XT)y0;
+      y[r * 3 + 1] = (XT)y1;
+      y[r * 3 + 2] = (XT)y2;
+    }
   }
 }
 

@@ -111,3 +111,140 @@ def dot(ctx, a, b):
     out = ctypes.c_double()
     call("sg_dot", ctx.h, a.numel(), dtype_code(a), ptr(a), ptr(b), ctypes.byref(out))
     return out.value
+
+
+def _host_f64(a):
+    return (ctypes.c_double * len(a))(*[float(v) for v in a])
+
+
+class Mesh:
+    """A bound edge set + its device pattern, as the sg_mesh structure."""
+
+    def __init__(self, ctx, n, endpoints, card, with_slots=False):
+        self.ctx = ctx
+        self.pattern = Pattern(ctx, n, endpoints, card, with_slots=with_slots)
+        p = self.pattern
+        mr = ctypes.c_int32()
+        call("sg_pattern_maxrow", ctx.h, n, ptr(p.rowptr), ctypes.byref(mr))
+        self.maxrow = mr.value
+        self.n, self.card, self.nE, self.nnzb = n, card, p.nE, p.nnzb
+        self.s = _lib.Mesh(n, card, p.nE, p.endpoints.data_ptr(), p.ve_ptr.data_ptr(),
+                           p.ve_idx.data_ptr(), p.rowptr.data_ptr(), p.colidx.data_ptr(),
+                           p.nnzb, self.maxrow)
+
+    def ref(self):
+        return ctypes.byref(self.s)
+
+    def empty(self, count, dtype):
+        with self.ctx.stream():
+            return torch.zeros(max(1, count), dtype=dtype, device=self.ctx.device)
+
+
+def _d(t, dtype, dev):
+    if t is None:
+        return None
+    if isinstance(t, torch.Tensor):
+        return t.to(device=dev, dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(t)).to(device=dev, dtype=dtype).contiguous()
+
+
+def assemble_springs(mesh, x, v, m, fixed, k, l0, h, viscous, grav, form=0,
+                     dtype=torch.float64, exact=True):
+    d = mesh.ctx.device
+    x, v, m, k, l0 = (_d(a, dtype, d) for a in (x, v, m, k, l0))
+    fixed = _d(fixed, torch.uint8, d)
+    vals = mesh.empty(mesh.nnzb * 9, dtype)
+    f = mesh.empty(mesh.n * 3, dtype)
+    call("sg_assemble_springs", mesh.ctx.h, mesh.ref(), dtype_code(vals), form, ptr(x), ptr(v),
+         ptr(m), ptr(fixed), ptr(k), ptr(l0), h, viscous, _host_f64(grav), ptr(vals), ptr(f),
+         int(exact))
+    return vals, f
+
+
+def assemble_scalar_springs(mesh, a, diag, scale, dtype=torch.float64, exact=True):
+    a = _d(a, dtype, mesh.ctx.device)
+    vals = mesh.empty(mesh.nnzb, dtype)
+    call("sg_assemble_scalar_springs", mesh.ctx.h, mesh.ref(), dtype_code(vals), ptr(a), diag,
+         scale, ptr(vals), int(exact))
+    return vals
+
+
+def tet_precompute(mesh, x, rho, dtype=torch.float64):
+    x = _d(x, dtype, mesh.ctx.device)
+    B = mesh.empty(mesh.nE * 9, dtype)
+    W = mesh.empty(mesh.nE, dtype)
+    m = mesh.empty(mesh.n, dtype)
+    call("sg_tet_precompute", mesh.ctx.h, mesh.ref(), dtype_code(B), ptr(x), rho, ptr(B), ptr(W),
+         ptr(m))
+    return B, W, m
+
+
+def assemble_tet_stiffness(mesh, model, x, c, B, W, mu, lam, h, rho, dtype=torch.float64,
+                           exact=True):
+    d = mesh.ctx.device
+    x, B, W, mu, lam = (_d(a, dtype, d) for a in (x, B, W, mu, lam))
+    c = _d(c, torch.int32, d)
+    vals = mesh.empty(mesh.nnzb * 9, dtype)
+    call("sg_assemble_tet_stiffness", mesh.ctx.h, mesh.ref(), dtype_code(vals), model, ptr(x),
+         ptr(c), ptr(B), ptr(W), ptr(mu), ptr(lam), h, rho, ptr(vals), int(exact))
+    return vals
+
+
+def assemble_tet_force(mesh, model, x, v, c, B, W, mu, lam, h, rho, grav, dtype=torch.float64,
+                       exact=True):
+    d = mesh.ctx.device
+    x, v, B, W, mu, lam = (_d(a, dtype, d) for a in (x, v, B, W, mu, lam))
+    c = _d(c, torch.int32, d)
+    f = mesh.empty(mesh.n * 3, dtype)
+    call("sg_assemble_tet_force", mesh.ctx.h, mesh.ref(), dtype_code(f), model, ptr(x), ptr(v),
+         ptr(c), ptr(B), ptr(W), ptr(mu), ptr(lam), h, rho, _host_f64(grav), ptr(f), int(exact))
+    return f
+
+
+def assemble_heat(mesh, B, W, kappa, dt, T0, dtype=torch.float64, exact=True):
+    d = mesh.ctx.device
+    B, W, kappa, T0 = (_d(a, dtype, d) for a in (B, W, kappa, T0))
+    vals = mesh.empty(mesh.nnzb, dtype)
+    b = mesh.empty(mesh.n, dtype)
+    call("sg_assemble_heat", mesh.ctx.h, mesh.ref(), dtype_code(vals), ptr(B), ptr(W), ptr(kappa),
+         dt, ptr(T0), ptr(vals), ptr(b), int(exact))
+    return vals, b
+
+
+def solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_RELATIVE,
+               tol=1e-8, maxiters=10000, verify=1, check_every=0, reliable_delta=0.1, lanes=0,
+               batch=32):
+    return _lib.SolveOpts(precision, precond, stop, tol, maxiters, verify, check_every,
+                          reliable_delta, lanes, batch)
+
+
+class Solver:
+    """sg_solver: set up once for a matrix, solve many right-hand sides."""
+
+    def __init__(self, ctx, n, bs, rowptr, colidx, vals, nnzb, opts):
+        self.ctx = ctx
+        self._keep = (rowptr, colidx, vals)
+        self.A = _lib.Matrix(n, bs, nnzb, rowptr.data_ptr(), colidx.data_ptr(),
+                             dtype_code(vals), vals.data_ptr())
+        self.opts = opts
+        h = P()
+        call("sg_solver_create", ctx.h, ctypes.byref(self.A), ctypes.byref(opts), ctypes.byref(h))
+        self.h = h
+
+    def solve(self, b, x):
+        """b, x: FP64 device tensors (x = initial guess, overwritten)."""
+        assert b.dtype == torch.float64 and x.dtype == torch.float64
+        res = _lib.SolveResult()
+        call("sg_solver_solve", self.h, ptr(b), ptr(x), ctypes.byref(res))
+        return res
+
+    def close(self):
+        if self.h:
+            _lib.load().sg_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
