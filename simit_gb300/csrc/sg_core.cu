@@ -42,8 +42,9 @@ int check_device_error(Ctx *c, const char *what) {
                                   "row candidate list exceeds sort capacity",
                                   "(row, col) not in pattern",
                                   "row longer than the assembly accumulator",
-                                  "vertex without a diagonal block"};
-    const char *nm = (e > 0 && e < 6) ? names[e] : "unknown";
+                                  "vertex without a diagonal block",
+                                  "bulk-copy barrier wait timed out"};
+    const char *nm = (e > 0 && e < 7) ? names[e] : "unknown";
     return set_error(SG_ERR_DEVICE, "%s: device check failed (%d: %s)", what, e,
                      nm);
   }

@@ -22,6 +22,12 @@ struct Ctx {
   int *d_err = nullptr;      // device error word (0 = ok), see ErrCode below
   int *h_err = nullptr;      // pinned mirror
   void *h_stage = nullptr;   // pinned staging (64 KB)
+  // (rowptr, n) -> longest row, for kernels that size shared memory by it
+  static constexpr int MAXROW_CACHE = 8;
+  const uint32_t *mr_ptr[MAXROW_CACHE] = {};
+  int32_t mr_n[MAXROW_CACHE] = {};
+  int32_t mr_val[MAXROW_CACHE] = {};
+  int mr_next = 0;
 };
 
 // Device-side error codes written to Ctx::d_err by bounds checks.
@@ -32,6 +38,7 @@ enum DevErr : int {
   DEV_SLOT_MISSING = 3,   // (row, col) not found in the pattern
   DEV_ROW_OVERFLOW = 4,   // assembly row longer than the accumulator
   DEV_NO_DIAGONAL = 5,    // vertex without a diagonal block
+  DEV_TMA_TIMEOUT = 6,    // a bulk-copy barrier wait ran out of polls
 };
 
 int set_error(int code, const char *fmt, ...);

@@ -9,6 +9,7 @@
 #include "sg_internal.cuh"
 #include "sg_solver_kernels.cuh"
 #include "sg_solver.h"
+#include "sg_spmv_api.h"
 
 namespace sg {
 
@@ -105,6 +106,11 @@ static int alloc_dev(Solver *S, void **p, size_t bytes) {
 template <typename MT, typename VT>
 static int launch_k1(Solver *S, cudaStream_t st) {
   const sg_matrix &A = S->A;
+  if (S->tma) {
+    const int vdt = sizeof(MT) == 8 ? SG_F64 : SG_F32, xdt = sizeof(VT) == 8 ? SG_F64 : SG_F32;
+    return bsr3_tma_launch(S->c, st, S->ctl, vdt, xdt, S->G, 1, A.n, A.rowptr, A.colidx,
+                           S->bulk_vals, S->p, S->q, S->part1, S->maxrow, S->P1, S->tma_smem);
+  }
   const MT *vals = (const MT *)S->bulk_vals;
   const VT *p = (const VT *)S->p;
   VT *q = (VT *)S->q;
@@ -450,6 +456,20 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   if (o->precision == SG_SOLVE_MIXED) S->kind = KIND_MIXED;
   else S->kind = A->dtype == SG_F64 ? KIND_F64 : KIND_F64_M32;
   const size_t vt = S->kind == KIND_MIXED ? 4 : 8;
+  // K1: the TMA-staged kernel for 3x3 blocks with 16-byte aligned arrays
+  // (unless a lane count is forced), else G lanes per row.
+  const bool aligned = ((uintptr_t)A->vals % 16 == 0) && ((uintptr_t)A->colidx % 16 == 0);
+  if (A->bs == 3 && o->lanes == 0 && aligned) {
+    SG_TRY(cached_maxrow(c, A->n, A->rowptr, &S->maxrow));
+    S->G = S->maxrow > 24 ? 8 : 4;
+    const int vdt = (S->kind == KIND_F64) ? SG_F64 : SG_F32;
+    const int xdt = S->kind == KIND_MIXED ? SG_F32 : SG_F64;
+    int grid = 0;
+    if (bsr3_tma_config(c, vdt, xdt, S->G, 1, A->n, S->maxrow, &grid, &S->tma_smem) == SG_OK) {
+      S->tma = 1;
+      S->P1 = grid;
+    }
+  }
   const int np = S->P1 > S->P2 ? S->P1 : S->P2;
   SG_TRY(alloc_dev(S, (void **)&S->ctl, sizeof(SolveCtl)));
   SG_CHECK_CUDA(cudaMallocHost((void **)&S->hctl, sizeof(SolveCtl)));

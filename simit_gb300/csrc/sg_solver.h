@@ -17,6 +17,8 @@ struct Solver {
   int batch = 32;
   int64_t len = 0;     // n * bs
   int G = 4, P1 = 1, P2 = 1;
+  int tma = 0, maxrow = 0;           // K1 uses the TMA-staged SpMV
+  size_t tma_smem = 0;
   const void *bulk_vals = nullptr;  // matrix values used by the iteration
   void *vals32 = nullptr;
   void *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *xlo = nullptr, *dinv = nullptr;

@@ -1,8 +1,93 @@
 // sg_bspmv: blocked SpMV entry point (y = A x) and its lanes-per-row choice.
 #include "sg_internal.cuh"
 #include "sg_spmv.cuh"
+#include "sg_spmv_tma.cuh"
+#include "sg_spmv_api.h"
 
 namespace sg {
+
+constexpr int TMA_ROWS = 32;
+
+template <int G, typename MT, typename VT, bool DOT>
+static int tma_config(Ctx *c, int32_t n, int maxrow, int *grid, size_t *smem) {
+  const int capb = TMA_ROWS * (maxrow > 0 ? maxrow : 1);
+  const size_t sh = tma_smem_bytes<MT>(capb);
+  if (sh > 200 * 1024) return SG_ERR_UNSUPPORTED;
+  auto kern = k_bsr3_tma<G, TMA_ROWS, MT, VT, DOT>;
+  SG_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  int per_sm = 0;
+  SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TMA_ROWS * G, sh));
+  if (per_sm < 1) return SG_ERR_UNSUPPORTED;
+  const int ntiles = (n + TMA_ROWS - 1) / TMA_ROWS;
+  int gsz = per_sm * c->num_sms;
+  if (gsz > ntiles) gsz = ntiles;
+  if (gsz < 1) gsz = 1;
+  *grid = gsz;
+  *smem = sh;
+  return SG_OK;
+}
+
+template <int G, typename MT, typename VT, bool DOT>
+static int tma_launch(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n, const uint32_t *rp,
+                      const uint32_t *ci, const MT *v, const VT *x, VT *y, double *part,
+                      int maxrow, int grid, size_t smem) {
+  const int capb = TMA_ROWS * (maxrow > 0 ? maxrow : 1);
+  k_bsr3_tma<G, TMA_ROWS, MT, VT, DOT><<<grid, TMA_ROWS * G, smem, st>>>(
+      ctl, n, rp, ci, v, x, y, part, capb, c->d_err);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+int bsr3_tma_config(Ctx *c, int vdt, int xdt, int G, int dot, int32_t n, int maxrow, int *grid,
+                    size_t *smem) {
+#define SG_CFG(MT, VT)                                                                   \
+  if (G == 8) return dot ? tma_config<8, MT, VT, true>(c, n, maxrow, grid, smem)         \
+                         : tma_config<8, MT, VT, false>(c, n, maxrow, grid, smem);       \
+  return dot ? tma_config<4, MT, VT, true>(c, n, maxrow, grid, smem)                     \
+             : tma_config<4, MT, VT, false>(c, n, maxrow, grid, smem);
+  if (vdt == SG_F32 && xdt == SG_F32) { SG_CFG(float, float) }
+  if (vdt == SG_F64 && xdt == SG_F64) { SG_CFG(double, double) }
+  if (vdt == SG_F32 && xdt == SG_F64) { SG_CFG(float, double) }
+#undef SG_CFG
+  return SG_ERR_UNSUPPORTED;
+}
+
+int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, int G, int dot,
+                    int32_t n, const uint32_t *rp, const uint32_t *ci, const void *v,
+                    const void *x, void *y, double *part, int maxrow, int grid, size_t smem) {
+  const SolveCtl *k = (const SolveCtl *)ctl;
+#define SG_L(MT, VT)                                                                          \
+  if (G == 8)                                                                                 \
+    return dot ? tma_launch<8, MT, VT, true>(c, st, k, n, rp, ci, (const MT *)v, (const VT *)x, \
+                                             (VT *)y, part, maxrow, grid, smem)                \
+               : tma_launch<8, MT, VT, false>(c, st, k, n, rp, ci, (const MT *)v,             \
+                                              (const VT *)x, (VT *)y, part, maxrow, grid, smem); \
+  return dot ? tma_launch<4, MT, VT, true>(c, st, k, n, rp, ci, (const MT *)v, (const VT *)x,   \
+                                           (VT *)y, part, maxrow, grid, smem)                  \
+             : tma_launch<4, MT, VT, false>(c, st, k, n, rp, ci, (const MT *)v, (const VT *)x,  \
+                                            (VT *)y, part, maxrow, grid, smem);
+  if (vdt == SG_F32 && xdt == SG_F32) { SG_L(float, float) }
+  if (vdt == SG_F64 && xdt == SG_F64) { SG_L(double, double) }
+  if (vdt == SG_F32 && xdt == SG_F64) { SG_L(float, double) }
+#undef SG_L
+  return SG_ERR_UNSUPPORTED;
+}
+
+int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out) {
+  for (int i = 0; i < Ctx::MAXROW_CACHE; ++i)
+    if (c->mr_ptr[i] == rowptr && c->mr_n[i] == n) {
+      *out = c->mr_val[i];
+      return SG_OK;
+    }
+  int32_t mr = 0;
+  SG_TRY(sg_pattern_maxrow(reinterpret_cast<sg_ctx *>(c), n, rowptr, &mr));
+  const int slot = c->mr_next++ % Ctx::MAXROW_CACHE;
+  c->mr_ptr[slot] = rowptr;
+  c->mr_n[slot] = n;
+  c->mr_val[slot] = mr;
+  *out = mr;
+  return SG_OK;
+}
 
 template <int G, typename VT, typename XT, typename AT>
 __global__ void __launch_bounds__(256) k_bsr3(int32_t n, const uint32_t *__restrict__ rowptr,
@@ -158,6 +243,17 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
   SG_REQUIRE(c && rowptr && colidx && vals && x && y, "sg_bspmv: null argument");
   SG_REQUIRE(n >= 0 && bs >= 1 && bs <= 16, "sg_bspmv: bad n=%d bs=%d", n, bs);
   if (n == 0) return SG_OK;
+  const bool aligned = ((uintptr_t)vals % 16 == 0) && ((uintptr_t)colidx % 16 == 0);
+  if (g == 0 && bs == 3 && aligned) {
+    // default: TMA-staged kernel (lanes per row from the row length)
+    int mr = 0, grid = 0;
+    size_t sh = 0;
+    SG_TRY(cached_maxrow(c, n, rowptr, &mr));
+    const int G = mr > 24 ? 8 : 4;
+    if (bsr3_tma_config(c, vdt, xdt, G, 0, n, mr, &grid, &sh) == SG_OK)
+      return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, G, 0, n, rowptr, colidx, vals, x, y,
+                             nullptr, mr, grid, sh);
+  }
   // nnzb is only needed for the default lane choice; read rowptr[n] then.
   int64_t nnzb = 0;
   if (g == 0) {
