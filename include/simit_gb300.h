@@ -45,6 +45,8 @@ typedef struct sg_ctx sg_ctx;
  * Replaces the device set-up of GPUFunction::init
  * (src/backend/gpu/gpu_function.cpp:113-138, 180-560). */
 int sg_ctx_create(int device, sg_ctx **out);
+/* Releases the caller's reference; the context (and its stream) lives on
+ * until every solver created on it has been destroyed too. */
 int sg_ctx_destroy(sg_ctx *ctx);
 int sg_ctx_sync(sg_ctx *ctx);
 /* The context's stream as an opaque pointer (a cudaStream_t). */
@@ -169,8 +171,10 @@ int sg_assemble_heat(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
  * (src/lower/index_expressions/lower_indexexprs.cpp:630-660).
  * bs = 1, 2, 3 have dedicated kernels; other bs use a generic kernel.
  * val_dtype is the matrix value type; vec_dtype the type of x and y;
- * accumulation is in the wider of the two.  g = lanes per block row
- * (0 = autotuned choice; else 1,2,4,8,16,32).
+ * accumulation is in the wider of the two.  g = lanes per block row:
+ * 1,2,4,8,16,32 select the streaming kernel; -4,-8,-16 the TMA-staged kernel
+ * (bs = 3, 16-byte aligned vals/colidx) with that many lanes; 0 picks (TMA
+ * for FP32 values, the streaming kernel for FP64).
  * ------------------------------------------------------------------- */
 int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
              const uint32_t *colidx, int val_dtype, const void *vals,

@@ -193,6 +193,17 @@ __global__ void sum_partials(const double *part, int np, double *out) {
   }
 }
 
+void ctx_release(Ctx *c) {
+  if (--c->refs > 0) return;
+  cudaStreamSynchronize(c->stream);
+  if (c->arena) cudaFree(c->arena);
+  if (c->d_err) cudaFree(c->d_err);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
 }  // namespace sg
 
 using namespace sg;
@@ -222,13 +233,7 @@ int sg_ctx_create(int device, sg_ctx **out) {
 int sg_ctx_destroy(sg_ctx *h) {
   Ctx *c = as_ctx(h);
   if (!c) return SG_OK;
-  cudaStreamSynchronize(c->stream);
-  if (c->arena) cudaFree(c->arena);
-  if (c->d_err) cudaFree(c->d_err);
-  if (c->h_err) cudaFreeHost(c->h_err);
-  if (c->h_stage) cudaFreeHost(c->h_stage);
-  cudaStreamDestroy(c->stream);
-  delete c;
+  ctx_release(c);
   return SG_OK;
 }
 

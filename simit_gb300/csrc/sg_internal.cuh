@@ -28,7 +28,12 @@ struct Ctx {
   int32_t mr_n[MAXROW_CACHE] = {};
   int32_t mr_val[MAXROW_CACHE] = {};
   int mr_next = 0;
+  int refs = 1;  // sg_ctx_destroy + one per live solver
 };
+
+// Drops one reference; frees the context when none are left.
+void ctx_release(Ctx *c);
+inline void ctx_retain(Ctx *c) { ++c->refs; }
 
 // Device-side error codes written to Ctx::d_err by bounds checks.
 enum DevErr : int {

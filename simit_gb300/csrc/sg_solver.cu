@@ -441,12 +441,14 @@ void dot_launch(Ctx *c, int64_t len, const double *a, const double *b, double *p
 int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
                 int (*ext_setup)(Solver *)) {
   S->c = c;
+  ctx_retain(c);
   S->A = *A;
   S->o = *o;
   if (S->o.batch <= 0) S->o.batch = 32;
   S->batch = (S->o.batch + 1) & ~1;
   S->len = (int64_t)A->n * A->bs;
   S->G = o->lanes > 0 ? o->lanes : default_lanes(A->n, A->nnzb, A->bs);
+  if (S->G < 1 || S->G > 32 || (S->G & (S->G - 1))) S->G = default_lanes(A->n, A->nnzb, A->bs);
   if (A->bs != 3 && A->bs != 1) S->G = 1;
   S->P1 = grid_for(c, (int64_t)A->n * (A->bs == 3 || A->bs == 1 ? S->G : 1), RED_T, 8);
   S->P2 = grid_for(c, S->len, RED_T, 4);
@@ -459,9 +461,9 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   // K1: the TMA-staged kernel for 3x3 blocks with 16-byte aligned arrays
   // (unless a lane count is forced), else G lanes per row.
   const bool aligned = ((uintptr_t)A->vals % 16 == 0) && ((uintptr_t)A->colidx % 16 == 0);
-  if (A->bs == 3 && o->lanes == 0 && aligned) {
+  if (A->bs == 3 && aligned && (o->lanes < 0 || (o->lanes == 0 && S->kind != KIND_F64))) {
     SG_TRY(cached_maxrow(c, A->n, A->rowptr, &S->maxrow));
-    S->G = S->maxrow > 24 ? 8 : 4;
+    S->G = o->lanes < 0 ? -o->lanes : (S->maxrow > 24 ? 8 : 4);
     const int vdt = (S->kind == KIND_F64) ? SG_F64 : SG_F32;
     const int xdt = S->kind == KIND_MIXED ? SG_F32 : SG_F64;
     int grid = 0;
@@ -549,6 +551,7 @@ void solver_free(Solver *S) {
   for (void *p : S->allocs) cudaFree(p);
   if (S->hctl) cudaFreeHost(S->hctl);
   if (S->ext_free) S->ext_free(S);
+  if (S->c) ctx_release(S->c);
   delete S;
 }
 

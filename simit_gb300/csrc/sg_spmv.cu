@@ -41,6 +41,8 @@ static int tma_launch(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n, c
 int bsr3_tma_config(Ctx *c, int vdt, int xdt, int G, int dot, int32_t n, int maxrow, int *grid,
                     size_t *smem) {
 #define SG_CFG(MT, VT)                                                                   \
+  if (G == 16) return dot ? tma_config<16, MT, VT, true>(c, n, maxrow, grid, smem)       \
+                          : tma_config<16, MT, VT, false>(c, n, maxrow, grid, smem);     \
   if (G == 8) return dot ? tma_config<8, MT, VT, true>(c, n, maxrow, grid, smem)         \
                          : tma_config<8, MT, VT, false>(c, n, maxrow, grid, smem);       \
   return dot ? tma_config<4, MT, VT, true>(c, n, maxrow, grid, smem)                     \
@@ -57,6 +59,11 @@ int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, 
                     const void *x, void *y, double *part, int maxrow, int grid, size_t smem) {
   const SolveCtl *k = (const SolveCtl *)ctl;
 #define SG_L(MT, VT)                                                                          \
+  if (G == 16)                                                                                \
+    return dot ? tma_launch<16, MT, VT, true>(c, st, k, n, rp, ci, (const MT *)v,             \
+                                              (const VT *)x, (VT *)y, part, maxrow, grid, smem) \
+               : tma_launch<16, MT, VT, false>(c, st, k, n, rp, ci, (const MT *)v,            \
+                                               (const VT *)x, (VT *)y, part, maxrow, grid, smem); \
   if (G == 8)                                                                                 \
     return dot ? tma_launch<8, MT, VT, true>(c, st, k, n, rp, ci, (const MT *)v, (const VT *)x, \
                                              (VT *)y, part, maxrow, grid, smem)                \
@@ -244,12 +251,17 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
   SG_REQUIRE(n >= 0 && bs >= 1 && bs <= 16, "sg_bspmv: bad n=%d bs=%d", n, bs);
   if (n == 0) return SG_OK;
   const bool aligned = ((uintptr_t)vals % 16 == 0) && ((uintptr_t)colidx % 16 == 0);
-  if (g == 0 && bs == 3 && aligned) {
-    // default: TMA-staged kernel (lanes per row from the row length)
+  if (g < 0) SG_REQUIRE(bs == 3 && aligned && (g == -4 || g == -8 || g == -16),
+                        "sg_bspmv: g=%d selects the TMA kernel: bs=3, 16-byte aligned arrays, "
+                        "g in {-4,-8,-16}", g);
+  if ((g == 0 && bs == 3 && aligned && !(vdt == SG_F64 && xdt == SG_F64)) || g < 0) {
+    // TMA-staged kernel (lanes per row from the row length unless given).
+    // FP64 matrices default to the plain kernel, which keeps more warps in
+    // flight for the FP64 pipe.
     int mr = 0, grid = 0;
     size_t sh = 0;
     SG_TRY(cached_maxrow(c, n, rowptr, &mr));
-    const int G = mr > 24 ? 8 : 4;
+    const int G = g < 0 ? -g : (mr > 24 ? 8 : 4);
     if (bsr3_tma_config(c, vdt, xdt, G, 0, n, mr, &grid, &sh) == SG_OK)
       return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, G, 0, n, rowptr, colidx, vals, x, y,
                              nullptr, mr, grid, sh);

@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(ROWS *G)
       const uint32_t e = rowptr[r + 1];
       VT a0 = 0, a1 = 0, a2 = 0;
       const size_t voff = vs / S, coff = cs / 4;
+#pragma unroll 4
       for (uint32_t q = rowptr[r] + gl; q < e; q += G) {
         const uint32_t c = cb[b][q - coff];
         const MT *v = vb[b] + ((size_t)q * 9 - voff);

@@ -28,7 +28,10 @@ def ptr(t):
 
 class Context:
     """One sg_ctx: a device and its stream.  `torch_stream` lets torch ops be
-    ordered on the same stream (use `with ctx.stream():`)."""
+    ordered on the same stream (use `with ctx.stream():`, or make it current).
+    Tensors handed to the C ABI must be allocated and written on this stream
+    (or synchronised with it): the C ABI's kernels run on it, and torch's
+    caching allocator only orders reuse within one stream."""
 
     def __init__(self, device=0):
         _lib.load()
@@ -65,9 +68,10 @@ class Pattern:
 
     def __init__(self, ctx, n, endpoints, card, with_slots=True):
         dev = ctx.device
-        ep = torch.as_tensor(np.ascontiguousarray(endpoints, np.int32)) \
-            if not isinstance(endpoints, torch.Tensor) else endpoints
-        ep = ep.to(device=dev, dtype=torch.int32).contiguous()
+        with ctx.stream():
+            ep = torch.as_tensor(np.ascontiguousarray(endpoints, np.int32)) \
+                if not isinstance(endpoints, torch.Tensor) else endpoints
+            ep = ep.to(device=dev, dtype=torch.int32).contiguous()
         nE = ep.numel() // card
         self.n, self.card, self.nE, self.endpoints = n, card, nE, ep
         with ctx.stream():
@@ -150,65 +154,71 @@ def _d(t, dtype, dev):
 
 def assemble_springs(mesh, x, v, m, fixed, k, l0, h, viscous, grav, form=0,
                      dtype=torch.float64, exact=True):
-    d = mesh.ctx.device
-    x, v, m, k, l0 = (_d(a, dtype, d) for a in (x, v, m, k, l0))
-    fixed = _d(fixed, torch.uint8, d)
-    vals = mesh.empty(mesh.nnzb * 9, dtype)
-    f = mesh.empty(mesh.n * 3, dtype)
-    call("sg_assemble_springs", mesh.ctx.h, mesh.ref(), dtype_code(vals), form, ptr(x), ptr(v),
-         ptr(m), ptr(fixed), ptr(k), ptr(l0), h, viscous, _host_f64(grav), ptr(vals), ptr(f),
-         int(exact))
-    return vals, f
+    with mesh.ctx.stream():
+        d = mesh.ctx.device
+        x, v, m, k, l0 = (_d(a, dtype, d) for a in (x, v, m, k, l0))
+        fixed = _d(fixed, torch.uint8, d)
+        vals = mesh.empty(mesh.nnzb * 9, dtype)
+        f = mesh.empty(mesh.n * 3, dtype)
+        call("sg_assemble_springs", mesh.ctx.h, mesh.ref(), dtype_code(vals), form, ptr(x), ptr(v),
+             ptr(m), ptr(fixed), ptr(k), ptr(l0), h, viscous, _host_f64(grav), ptr(vals), ptr(f),
+             int(exact))
+        return vals, f
 
 
 def assemble_scalar_springs(mesh, a, diag, scale, dtype=torch.float64, exact=True):
-    a = _d(a, dtype, mesh.ctx.device)
-    vals = mesh.empty(mesh.nnzb, dtype)
-    call("sg_assemble_scalar_springs", mesh.ctx.h, mesh.ref(), dtype_code(vals), ptr(a), diag,
-         scale, ptr(vals), int(exact))
-    return vals
+    with mesh.ctx.stream():
+        a = _d(a, dtype, mesh.ctx.device)
+        vals = mesh.empty(mesh.nnzb, dtype)
+        call("sg_assemble_scalar_springs", mesh.ctx.h, mesh.ref(), dtype_code(vals), ptr(a), diag,
+             scale, ptr(vals), int(exact))
+        return vals
 
 
 def tet_precompute(mesh, x, rho, dtype=torch.float64):
-    x = _d(x, dtype, mesh.ctx.device)
-    B = mesh.empty(mesh.nE * 9, dtype)
-    W = mesh.empty(mesh.nE, dtype)
-    m = mesh.empty(mesh.n, dtype)
-    call("sg_tet_precompute", mesh.ctx.h, mesh.ref(), dtype_code(B), ptr(x), rho, ptr(B), ptr(W),
-         ptr(m))
-    return B, W, m
+    with mesh.ctx.stream():
+        x = _d(x, dtype, mesh.ctx.device)
+        B = mesh.empty(mesh.nE * 9, dtype)
+        W = mesh.empty(mesh.nE, dtype)
+        m = mesh.empty(mesh.n, dtype)
+        call("sg_tet_precompute", mesh.ctx.h, mesh.ref(), dtype_code(B), ptr(x), rho, ptr(B), ptr(W),
+             ptr(m))
+        return B, W, m
 
 
 def assemble_tet_stiffness(mesh, model, x, c, B, W, mu, lam, h, rho, dtype=torch.float64,
                            exact=True):
-    d = mesh.ctx.device
-    x, B, W, mu, lam = (_d(a, dtype, d) for a in (x, B, W, mu, lam))
-    c = _d(c, torch.int32, d)
-    vals = mesh.empty(mesh.nnzb * 9, dtype)
-    call("sg_assemble_tet_stiffness", mesh.ctx.h, mesh.ref(), dtype_code(vals), model, ptr(x),
-         ptr(c), ptr(B), ptr(W), ptr(mu), ptr(lam), h, rho, ptr(vals), int(exact))
-    return vals
+    with mesh.ctx.stream():
+        d = mesh.ctx.device
+        x, B, W, mu, lam = (_d(a, dtype, d) for a in (x, B, W, mu, lam))
+        c = _d(c, torch.int32, d)
+        vals = mesh.empty(mesh.nnzb * 9, dtype)
+        call("sg_assemble_tet_stiffness", mesh.ctx.h, mesh.ref(), dtype_code(vals), model, ptr(x),
+             ptr(c), ptr(B), ptr(W), ptr(mu), ptr(lam), h, rho, ptr(vals), int(exact))
+        return vals
 
 
 def assemble_tet_force(mesh, model, x, v, c, B, W, mu, lam, h, rho, grav, dtype=torch.float64,
                        exact=True):
-    d = mesh.ctx.device
-    x, v, B, W, mu, lam = (_d(a, dtype, d) for a in (x, v, B, W, mu, lam))
-    c = _d(c, torch.int32, d)
-    f = mesh.empty(mesh.n * 3, dtype)
-    call("sg_assemble_tet_force", mesh.ctx.h, mesh.ref(), dtype_code(f), model, ptr(x), ptr(v),
-         ptr(c), ptr(B), ptr(W), ptr(mu), ptr(lam), h, rho, _host_f64(grav), ptr(f), int(exact))
-    return f
+    with mesh.ctx.stream():
+        d = mesh.ctx.device
+        x, v, B, W, mu, lam = (_d(a, dtype, d) for a in (x, v, B, W, mu, lam))
+        c = _d(c, torch.int32, d)
+        f = mesh.empty(mesh.n * 3, dtype)
+        call("sg_assemble_tet_force", mesh.ctx.h, mesh.ref(), dtype_code(f), model, ptr(x), ptr(v),
+             ptr(c), ptr(B), ptr(W), ptr(mu), ptr(lam), h, rho, _host_f64(grav), ptr(f), int(exact))
+        return f
 
 
 def assemble_heat(mesh, B, W, kappa, dt, T0, dtype=torch.float64, exact=True):
-    d = mesh.ctx.device
-    B, W, kappa, T0 = (_d(a, dtype, d) for a in (B, W, kappa, T0))
-    vals = mesh.empty(mesh.nnzb, dtype)
-    b = mesh.empty(mesh.n, dtype)
-    call("sg_assemble_heat", mesh.ctx.h, mesh.ref(), dtype_code(vals), ptr(B), ptr(W), ptr(kappa),
-         dt, ptr(T0), ptr(vals), ptr(b), int(exact))
-    return vals, b
+    with mesh.ctx.stream():
+        d = mesh.ctx.device
+        B, W, kappa, T0 = (_d(a, dtype, d) for a in (B, W, kappa, T0))
+        vals = mesh.empty(mesh.nnzb, dtype)
+        b = mesh.empty(mesh.n, dtype)
+        call("sg_assemble_heat", mesh.ctx.h, mesh.ref(), dtype_code(vals), ptr(B), ptr(W), ptr(kappa),
+             dt, ptr(T0), ptr(vals), ptr(b), int(exact))
+        return vals, b
 
 
 def solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_RELATIVE,

@@ -13,11 +13,8 @@ GOLD_TOL = 1e-13
 
 
 @pytest.fixture(scope="module")
-def ctx():
-    from simit_gb300.runtime import Context
-    c = Context(0)
-    yield c
-    c.close()
+def ctx(gpu_ctx):
+    return gpu_ctx
 
 
 def _np(t):

@@ -13,11 +13,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
-def ctx():
-    from simit_gb300.runtime import Context
-    c = Context(0)
-    yield c
-    c.close()
+def ctx(gpu_ctx):
+    return gpu_ctx
 
 
 def _check_pattern(ctx, oracle, n, ep, card):
