@@ -1,0 +1,338 @@
+"""Benchmark: time and DOF/s to a 1e-8 FP64 relative residual on the 128^3
+heterogeneous-elasticity system (6,440,067 DOF), mixed-precision PCG on the
+GB300 against plain FP64 Jacobi-CG on the same GPU.
+
+A step is one pass of the hot path: assemble the FP32 stiffness matrix and
+right-hand side from the resident mesh, refresh the preconditioner, and
+solve to ||b - A x|| <= 1e-8 ||b|| (true FP64 residual).  The matrix (1.0 GB
+in FP32) is larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--size S]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time & DOF/s to 1e-8 residual: learned+FP32 PCG vs plain FP64 CG, 1 GB300"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=128, help="cells per cube edge")
+    ap.add_argument("--cpu-sample", type=int, default=32, help="cells per edge of the CPU sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
+    return ap.parse_args()
+
+
+def workload_name(size):
+    return ("heterogeneous linear elasticity %d^3 five-tet lattice (fem_linear form, E log-uniform "
+            "[1e3,1e6], nu U[0.35,0.45], bottom face fixed), solve to 1e-8 FP64 relative residual"
+            % size)
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm (the oracle restatement of the reference's lowered loops)
+# ---------------------------------------------------------------------------
+def cpu_sample(ncell):
+    """Oracle on the ncell^3 instance of the same family: pattern (ordered
+    sets, as the reference's PathIndexBuilder) + FP64 assembly (element
+    order, loc slot search) + FP64 Jacobi-PCG to 1e-8, one thread."""
+    import numpy as np
+    from oracle import oracle
+    from simit_gb300 import problems
+    h = problems.hetero_mesh(ncell)
+    t0 = time.perf_counter()
+    rp, ci = oracle.pattern(h["n"], h["tets"], 4)
+    B, W, _ = oracle.tet_precompute(h["X0"], h["tets"], problems.RHO)
+    A = oracle.tet_stiffness(0, h["x"], h["c"], h["tets"], B, W, h["mu"], h["lam"], problems.H,
+                             problems.RHO, rp, ci)
+    b = oracle.tet_force(0, h["x"], np.zeros(h["n"] * 3), h["c"], h["tets"], B, W, h["mu"],
+                         h["lam"], problems.H, problems.RHO, problems.GRAV)
+    x, it, rr = oracle.jacobi_pcg(h["n"], 3, rp, ci, A, b, np.zeros(h["n"] * 3), 1e-8, 200000,
+                                  refresh=0)
+    t = time.perf_counter() - t0
+    dofs = h["n"] * 3
+    return {"value": dofs / t, "unit": "DOF/s", "seconds": t, "iters": it, "relres": rr,
+            "dofs": dofs}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    for _ in range(args.warmup):
+        cpu_sample(args.cpu_sample)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_sample(args.cpu_sample))
+    el = time.perf_counter() - t0
+    v = statistics.median([r["value"] for r in vals])
+    sample = ("%d^3 instance of the same family (%d DOF): ordered-set pattern + FP64 element-order "
+              "assembly + FP64 Jacobi-PCG to 1e-8, oracle restatement of the reference's CPU "
+              "loops, 1 thread" % (args.cpu_sample, vals[0]["dofs"]))
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "DOF/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded Philox)",
+           "config": {"workload": workload_name(args.size), "sample_cells": args.cpu_sample},
+           "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": 1, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "iters": vals[0]["iters"]}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index),
+                                       "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for ln in self.p.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def spmv_traffic(size):
+    """DRAM bytes per SpMV launch from a committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "spmv_bsr3_tma_f32_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get("bytes_per_launch_scaled", {}).get(str(size))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local):
+    import torch
+    from simit_gb300 import _lib, problems
+    from simit_gb300.runtime import Context, bspmv
+
+    ctx = Context(local)
+    torch.cuda.set_device(local)
+    torch.cuda.set_stream(ctx.torch_stream)
+    host = problems.hetero_mesh(args.size)
+    prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
+                                     precond=_lib.PRECOND_BLOCK_JACOBI)
+    st = ctx.torch_stream
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        res = prob.step()
+    barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    results = []
+    for _ in range(args.steps):
+        results.append(prob.step())
+    e1.record(st)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    dofs = prob.dofs
+    value = dofs * world / (ms / 1e3)
+    relres = max((r.true_normr2 / r.bnorm2) ** 0.5 for r in results)
+    iters = results[-1].iters
+    # kernels per step: stiffness + force assembly, preconditioner refresh,
+    # and the solver's own count (graph kernel nodes included)
+    launches = sum(int(r.kernels) + 3 for r in results)
+
+    # --- end to end through host buffers (pinned) -------------------------
+    n3 = prob.dofs
+    x_h = torch.tensor(host["x"], dtype=torch.float32).pin_memory()
+    mu_h = torch.tensor(host["mu"], dtype=torch.float32).pin_memory()
+    lam_h = torch.tensor(host["lam"], dtype=torch.float32).pin_memory()
+    u_h = torch.empty(n3, dtype=torch.float64).pin_memory()
+    prob.step_host(x_h, mu_h, lam_h, u_h)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        prob.step_host(x_h, mu_h, lam_h, u_h)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = (x_h.numel() + mu_h.numel() + lam_h.numel()) * 4
+    d2h = u_h.numel() * 8
+
+    # --- roofline of the dominant kernel: the TMA-staged FP32 SpMV --------
+    m = prob.mesh
+    p = torch.rand(n3, dtype=torch.float32, device=ctx.device)
+    q = torch.empty_like(p)
+    for _ in range(3):
+        bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, p, q, g=0)
+    reps = 50
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    s0.record(st)
+    for _ in range(reps):
+        bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, p, q, g=0)
+    s1.record(st)
+    s1.synchronize()
+    spmv_ms = s0.elapsed_time(s1) / reps
+    spmv_bytes = m.nnzb * (9 * 4 + 4) + (m.n + 1) * 4 + m.n * 3 * (4 + 4)
+    achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+
+    # --- plain FP64 Jacobi-CG on the same GPU (FP64 assembly + solve) -----
+    fp64 = None
+    if not args.no_fp64:
+        prob.close()
+        del prob
+        torch.cuda.empty_cache()
+        p64 = problems.HeteroElasticity(ctx, host, dtype=torch.float64,
+                                        precond=_lib.PRECOND_JACOBI)
+        p64.step()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(st)
+        r64 = p64.step()
+        f1.record(st)
+        f1.synchronize()
+        ms64 = f0.elapsed_time(f1)
+        fp64 = {"ms": ms64, "DOF_per_s": dofs / (ms64 / 1e3), "iters": r64.iters,
+                "relres": (r64.true_normr2 / r64.bnorm2) ** 0.5,
+                "method": "FP64 assembly + FP64 point-Jacobi CG (FP64 SpMV, FP64 vectors)"}
+        p64.close()
+
+    if rank != 0:
+        return
+    cpu = cpu_sample(args.cpu_sample)
+    out = {
+        "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 matrix+SpMV, f64 dots/residual",
+        "data": "synthetic (seeded Philox mesh, parameters and displacements)",
+        "config": {"workload": workload_name(args.size), "dofs": dofs, "nnzb": m.nnzb,
+                   "method": "FP32 assembly + mixed-precision block-Jacobi PCG (FP32 matrix/"
+                             "vectors, FP64 dots, FP64 reliable updates), verified FP64 residual",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (FP32 matrix 1.0 GB), no flush"},
+        "iters": iters, "relres_max": relres,
+        "e2e": {"value": dofs * world / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": spmv_traffic(args.size),
+                     "kernel": "k_bsr3_tma (FP32 3x3 blocked SpMV)", "peak_kind": peak_kind,
+                     "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes},
+        "cpu_baseline": {"value": cpu["value"], "unit": "DOF/s", "cores": 1, "kind": "port",
+                         "sample": "%d^3 instance (%d DOF) of the same family: oracle pattern + "
+                                   "FP64 assembly + FP64 Jacobi-PCG to 1e-8 (%d iterations), "
+                                   "%.1f s" % (args.cpu_sample, cpu["dofs"], cpu["iters"],
+                                               cpu["seconds"])},
+        "clocks": clk,
+        "fp64_jacobi_cg": fp64,
+        "speedup_vs_fp64_cg": (fp64["ms"] / ms) if fp64 else None,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -256,6 +256,7 @@ typedef struct sg_solve_result {
   double normr2;             /* last iterated r'r */
   double true_normr2;        /* ||b - A x||^2 at exit (FP64) */
   double bnorm2;             /* b'b */
+  int64_t kernels;           /* kernels this solve launched (graph nodes included) */
 } sg_solve_result;
 
 typedef struct sg_solver sg_solver;
@@ -267,6 +268,10 @@ int sg_solver_create(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
 /* Solve A x = b; b, x FP64 device arrays of n*bs; x holds the initial guess
  * and receives the solution.  Synchronises. */
 int sg_solver_solve(sg_solver *s, const double *b, double *x, sg_solve_result *res);
+/* Re-read the matrix values after they changed in place (re-assembly):
+ * refreshes the FP32 bulk copy and the (block-)Jacobi diagonal; the captured
+ * iteration graph is kept. */
+int sg_solver_refresh(sg_solver *s);
 int sg_solver_destroy(sg_solver *s);
 /* One-shot create + solve + destroy. */
 int sg_solve(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,

@@ -46,7 +46,7 @@ class SolveOpts(ctypes.Structure):
 class SolveResult(ctypes.Structure):
     """sg_solve_result"""
     _fields_ = [("status", I32), ("iters", I32), ("checks", I32), ("fallbacks", I32),
-                ("normr2", D), ("true_normr2", D), ("bnorm2", D)]
+                ("normr2", D), ("true_normr2", D), ("bnorm2", D), ("kernels", I64)]
 
 
 SOLVE_F64, SOLVE_MIXED = 0, 1
@@ -83,6 +83,7 @@ SIGNATURES = {
                                ctypes.POINTER(P)]),
     "sg_solver_solve": (_CI, [P, P, P, ctypes.POINTER(SolveResult)]),
     "sg_solver_destroy": (_CI, [P]),
+    "sg_solver_refresh": (_CI, [P]),
     "sg_solve": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(SolveOpts), P, P,
                        ctypes.POINTER(SolveResult)]),
 }

@@ -189,6 +189,9 @@ static int capture_batch(Solver *S) {
   }
   SG_CHECK_CUDA(e);
   SG_CHECK_CUDA(cudaGraphInstantiate(&S->gexec, g, 0));
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  S->graph_kernels = (int64_t)nn;
   cudaGraphDestroy(g);
   return SG_OK;
 }
@@ -196,6 +199,7 @@ static int capture_batch(Solver *S) {
 // r_hi = b - A x_hi in FP64 (FP64 accumulation); returns ||r_hi||^2 (sync).
 static int true_residual(Solver *S, const double *b, double *rr) {
   const sg_matrix &A = S->A;
+  S->launches += 2;
   cudaStream_t st = S->c->stream;
   const int PT = S->P1;
   if (A.bs == 3) {
@@ -230,6 +234,7 @@ static int true_residual(Solver *S, const double *b, double *rr) {
 template <typename VT>
 static int restart_from_rhi(Solver *S, double *rz) {
   cudaStream_t st = S->c->stream;
+  S->launches += 3;
   k_cast_r<VT><<<S->P2, RED_T, 0, st>>>(S->len, S->rhi, (VT *)S->r);
   SG_CHECK_LAUNCH();
   if (S->ext_prec_apply) {
@@ -265,10 +270,12 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
   cudaStream_t st = c->stream;
   const bool mixed = S->kind == KIND_MIXED;
   memset(res, 0, sizeof(*res));
+  S->launches = 0;
   SG_CHECK_CUDA(cudaMemcpyAsync(S->xw, x, S->len * 8, cudaMemcpyDeviceToDevice, st));
   if (mixed) SG_CHECK_CUDA(cudaMemsetAsync(S->xlo, 0, S->len * sizeof(XT), st));
   // b'b
   dot_launch(c, S->len, b, b, S->part3, S->dres);
+  S->launches += 2;
   SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, S->dres, 8, cudaMemcpyDeviceToHost, st));
   SG_CHECK_CUDA(cudaStreamSynchronize(st));
   const double bb = *(double *)c->h_stage;
@@ -314,6 +321,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     SG_CHECK_CUDA(cudaMemcpyAsync(S->ctl, h, sizeof(SolveCtl), cudaMemcpyHostToDevice, st));
     for (;;) {
       SG_CHECK_CUDA(cudaGraphLaunch(S->gexec, st));
+      S->launches += S->graph_kernels;
       SG_CHECK_CUDA(cudaMemcpyAsync(h, S->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, st));
       SG_CHECK_CUDA(cudaStreamSynchronize(st));
       if (h->status != ST_RUNNING) break;
@@ -329,6 +337,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     if (mixed) {
       k_add_lo<XT><<<S->P2, RED_T, 0, st>>>(S->len, S->xw, (XT *)S->xlo);
       SG_CHECK_LAUNCH();
+      S->launches += 1;
     }
     const bool iter_conv = h->last_rr <= tol2;
     if (!S->o.verify && !mixed && iter_conv) {
@@ -355,6 +364,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     SG_TRY(restart_from_rhi<VT>(S, &rz_new));
     const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
     k_p_update<VT><<<S->P2, RED_T, 0, st>>>(S->len, z, rz_new / rz_old, (VT *)S->p);
+    S->launches += 1;
     SG_CHECK_LAUNCH();
     rz = rz_new;
     rr_ref = rr;
@@ -362,6 +372,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
   if (mixed && status) {
     k_add_lo<XT><<<S->P2, RED_T, 0, st>>>(S->len, S->xw, (XT *)S->xlo);
     SG_CHECK_LAUNCH();
+    S->launches += 1;
   }
   SG_CHECK_CUDA(cudaMemcpyAsync(x, S->xw, S->len * 8, cudaMemcpyDeviceToDevice, st));
   if (S->o.verify || mixed) {
@@ -374,6 +385,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
   SG_CHECK_CUDA(cudaStreamSynchronize(st));
   res->status = status;
   res->iters = iters;
+  res->kernels = S->launches;
   return SG_OK;
 }
 
@@ -413,6 +425,12 @@ int sg_solver_solve(sg_solver *hs, const double *b, double *x, sg_solve_result *
   return solver_solve(S, b, x, res);
 }
 
+int sg_solver_refresh(sg_solver *hs) {
+  Solver *S = reinterpret_cast<Solver *>(hs);
+  SG_REQUIRE(S, "sg_solver_refresh: null solver");
+  return refresh_matrix(S);
+}
+
 int sg_solver_destroy(sg_solver *hs) {
   solver_free(reinterpret_cast<Solver *>(hs));
   return SG_OK;
@@ -436,6 +454,48 @@ void dot_launch(Ctx *c, int64_t len, const double *a, const double *b, double *p
   const int P = grid_for(c, len, RED_T, 4);
   k_dot2<<<P, RED_T, 0, c->stream>>>(len, a, b, part);
   k_sum_parts<<<1, RED_T, 0, c->stream>>>(part, P, dres);
+}
+
+// Matrix-dependent data: the FP32 bulk copy (mixed, FP64 input) and the
+// (block-)Jacobi inverse diagonal.  Re-run after the matrix values change.
+int refresh_matrix(Solver *S) {
+  Ctx *c = S->c;
+  const sg_matrix *A = &S->A;
+  const size_t vt = S->kind == KIND_MIXED ? 4 : 8;
+  S->bulk_vals = A->vals;
+  if (S->kind == KIND_MIXED && A->dtype == SG_F64) {
+    const int64_t nv = A->nnzb * A->bs * A->bs;
+    k_f64_to_f32<<<grid_for(c, nv, 256, 8), 256, 0, c->stream>>>(nv, (const double *)A->vals,
+                                                                 (float *)S->vals32);
+    SG_CHECK_LAUNCH();
+    S->bulk_vals = S->vals32;
+  }
+  if (S->prec == PK_JACOBI || S->prec == PK_BLOCK3) {
+    const int blk = S->prec == PK_BLOCK3;
+    const int g = grid_for(c, A->n, 256, 8);
+    if (vt == 4) {
+      if (A->dtype == SG_F64)
+        k_diag_inv<double, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                            (const double *)A->vals,
+                                                            (float *)S->dinv, blk, c->d_err);
+      else
+        k_diag_inv<float, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                           (const float *)A->vals,
+                                                           (float *)S->dinv, blk, c->d_err);
+    } else {
+      if (A->dtype == SG_F64)
+        k_diag_inv<double, double><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                             (const double *)A->vals,
+                                                             (double *)S->dinv, blk, c->d_err);
+      else
+        k_diag_inv<float, double><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                            (const float *)A->vals,
+                                                            (double *)S->dinv, blk, c->d_err);
+    }
+    SG_CHECK_LAUNCH();
+    SG_TRY(check_device_error(c, "solver (diagonal)"));
+  }
+  return SG_OK;
 }
 
 int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
@@ -491,43 +551,12 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   } else {
     S->xupd = S->xw;
   }
-  // bulk matrix values
-  S->bulk_vals = A->vals;
-  if (S->kind == KIND_MIXED && A->dtype == SG_F64) {
-    const int64_t nv = A->nnzb * A->bs * A->bs;
-    SG_TRY(alloc_dev(S, &S->vals32, nv * 4));
-    k_f64_to_f32<<<grid_for(c, nv, 256, 8), 256, 0, c->stream>>>(nv, (const double *)A->vals,
-                                                                 (float *)S->vals32);
-    SG_CHECK_LAUNCH();
-    S->bulk_vals = S->vals32;
-  }
-  // preconditioner data
-  if (S->prec == PK_JACOBI || S->prec == PK_BLOCK3) {
-    const int blk = S->prec == PK_BLOCK3;
-    SG_TRY(alloc_dev(S, &S->dinv, (blk ? (int64_t)A->n * 9 : S->len) * vt));
-    const int g = grid_for(c, A->n, 256, 8);
-    if (vt == 4) {
-      if (A->dtype == SG_F64)
-        k_diag_inv<double, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
-                                                            (const double *)A->vals,
-                                                            (float *)S->dinv, blk, c->d_err);
-      else
-        k_diag_inv<float, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
-                                                           (const float *)A->vals,
-                                                           (float *)S->dinv, blk, c->d_err);
-    } else {
-      if (A->dtype == SG_F64)
-        k_diag_inv<double, double><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
-                                                             (const double *)A->vals,
-                                                             (double *)S->dinv, blk, c->d_err);
-      else
-        k_diag_inv<float, double><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
-                                                            (const float *)A->vals,
-                                                            (double *)S->dinv, blk, c->d_err);
-    }
-    SG_CHECK_LAUNCH();
-    SG_TRY(check_device_error(c, "sg_solver_create (diagonal)"));
-  }
+  if (S->kind == KIND_MIXED && A->dtype == SG_F64)
+    SG_TRY(alloc_dev(S, &S->vals32, A->nnzb * A->bs * A->bs * 4));
+  if (S->prec == PK_JACOBI || S->prec == PK_BLOCK3)
+    SG_TRY(alloc_dev(S, &S->dinv,
+                     (S->prec == PK_BLOCK3 ? (int64_t)A->n * 9 : S->len) * vt));
+  SG_TRY(refresh_matrix(S));
   if (ext_setup) SG_TRY(ext_setup(S));
   switch (S->kind) {
     case KIND_F64: return capture_batch<double, double, double>(S);

@@ -19,6 +19,8 @@ struct Solver {
   int G = 4, P1 = 1, P2 = 1;
   int tma = 0, maxrow = 0;           // K1 uses the TMA-staged SpMV
   size_t tma_smem = 0;
+  int64_t launches = 0;             // kernels launched by the current solve
+  int64_t graph_kernels = 0;        // kernel nodes in one batch graph
   const void *bulk_vals = nullptr;  // matrix values used by the iteration
   void *vals32 = nullptr;
   void *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *xlo = nullptr, *dinv = nullptr;
@@ -41,6 +43,7 @@ struct Solver {
 int default_lanes(int32_t n, int64_t nnzb, int32_t bs);
 int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
                 int (*ext_setup)(Solver *));
+int refresh_matrix(Solver *S);
 int solver_solve(Solver *S, const double *b, double *x, sg_solve_result *res);
 void solver_free(Solver *S);
 void dot_launch(Ctx *c, int64_t len, const double *a, const double *b, double *part,

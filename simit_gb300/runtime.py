@@ -248,6 +248,10 @@ class Solver:
         call("sg_solver_solve", self.h, ptr(b), ptr(x), ctypes.byref(res))
         return res
 
+    def refresh(self):
+        """The matrix values changed in place (re-assembly)."""
+        call("sg_solver_refresh", self.h)
+
     def close(self):
         if self.h:
             _lib.load().sg_solver_destroy(self.h)
