@@ -34,7 +34,40 @@ def parse():
     ap.add_argument("--size", type=int, default=128, help="cells per cube edge")
     ap.add_argument("--cpu-sample", type=int, default=32, help="cells per edge of the CPU sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
+    ap.add_argument("--spmv-only", action="store_true",
+                    help="profiling driver: build the --size matrix and run sg_bspmv --reps times")
+    ap.add_argument("--lanes", type=int, default=0, help="sg_bspmv lanes (g) for --spmv-only")
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--f64", action="store_true", help="FP64 matrix for --spmv-only")
     return ap.parse_args()
+
+
+def run_spmv_only(args):
+    """Profiling driver: the --size heterogeneous-elasticity matrix, --reps
+    SpMV launches with sg_bspmv(g = --lanes), event-timed."""
+    import torch
+    from simit_gb300 import _lib, problems
+    from simit_gb300.runtime import Context, bspmv
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    dt = torch.float64 if args.f64 else torch.float32
+    p = problems.HeteroElasticity(ctx, problems.hetero_mesh(args.size), dtype=dt,
+                                  precond=_lib.PRECOND_JACOBI)
+    m = p.mesh
+    x = torch.rand(m.n * 3, dtype=dt, device=ctx.device)
+    y = torch.empty_like(x)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, x, y, g=args.lanes)
+    e0.record(ctx.torch_stream)
+    for _ in range(args.reps):
+        bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, x, y, g=args.lanes)
+    e1.record(ctx.torch_stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.reps
+    nbytes = m.nnzb * (9 * x.element_size() + 4) + (m.n + 1) * 4 + m.n * 3 * 2 * x.element_size()
+    print(json.dumps({"size": args.size, "lanes": args.lanes, "dtype": str(dt), "nnzb": m.nnzb,
+                      "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes}), flush=True)
 
 
 def workload_name(size):
@@ -324,6 +357,9 @@ def run_ours(args, rank, world, local):
 
 def main():
     args = parse()
+    if args.spmv_only:
+        run_spmv_only(args)
+        return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
