@@ -523,7 +523,7 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   const bool aligned = ((uintptr_t)A->vals % 16 == 0) && ((uintptr_t)A->colidx % 16 == 0);
   if (A->bs == 3 && aligned && (o->lanes < 0 || (o->lanes == 0 && S->kind != KIND_F64))) {
     SG_TRY(cached_maxrow(c, A->n, A->rowptr, &S->maxrow));
-    S->G = o->lanes < 0 ? -o->lanes : (S->maxrow > 24 ? 8 : 4);
+    S->G = o->lanes < 0 ? -o->lanes : 8;
     const int vdt = (S->kind == KIND_F64) ? SG_F64 : SG_F32;
     const int xdt = S->kind == KIND_MIXED ? SG_F32 : SG_F64;
     int grid = 0;

@@ -261,7 +261,7 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
     int mr = 0, grid = 0;
     size_t sh = 0;
     SG_TRY(cached_maxrow(c, n, rowptr, &mr));
-    const int G = g < 0 ? -g : (mr > 24 ? 8 : 4);
+    const int G = g < 0 ? -g : 8;
     if (bsr3_tma_config(c, vdt, xdt, G, 0, n, mr, &grid, &sh) == SG_OK)
       return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, G, 0, n, rowptr, colidx, vals, x, y,
                              nullptr, mr, grid, sh);

@@ -326,6 +326,7 @@ def test_solver_status_codes(ctx):
     A2 = assemble_scalar_springs(mesh, a, 1.0, 0.5)
     S2 = Solver(ctx, n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A2, mesh.nnzb,
                 solve_opts(tol=1e-14, maxiters=3))
+    b = torch.tensor(meshgen.rng(5).uniform(-1, 1, n), device=ctx.device)
     r2 = S2.solve(b, torch.zeros_like(b))
     assert r2.status == 2 and r2.iters == 3
     # NaN in the right-hand side
