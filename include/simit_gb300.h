@@ -277,6 +277,33 @@ int sg_solver_destroy(sg_solver *s);
 int sg_solve(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
              const double *b, double *x, sg_solve_result *res);
 
+/* ---------------------------------------------------------------------
+ * Dot product that allocates nothing.  This entry point has no counterpart
+ * in the reference; it exists for callers that may not allocate device
+ * memory while they run -- a host application that owns and budgets all GPU
+ * memory through its own pool, or a time-critical loop that must not call
+ * cudaMalloc/cudaFree because those can synchronise the device.  Such a
+ * caller cannot create an sg_ctx (its set-up allocates) or use sg_dot (its
+ * partial sums live in the context's growable scratch arena).
+ *
+ * Same result as sg_dot (FP64 accumulation, deterministic order), computed
+ * on `stream` (a cudaStream_t, NULL = legacy default stream) into the
+ * caller's DEVICE double *d_out, asynchronously.  The partial sums live in a
+ * fixed static device array (SG_DOT_NOALLOC_MAX_PARTS doubles, 512 KB, held
+ * by every GPU that loads the library until exit), so len is limited to
+ * SG_DOT_NOALLOC_MAX_LEN elements; longer vectors are rejected with
+ * SG_ERR_ARG.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) while that device is current; make it
+ * before any stream capture.  Calls share the array: calls whose kernels
+ * may overlap on the GPU (unordered streams) race, so order them on one
+ * stream.
+ * ------------------------------------------------------------------- */
+#define SG_DOT_NOALLOC_CHUNK 4096
+#define SG_DOT_NOALLOC_MAX_PARTS 65536
+#define SG_DOT_NOALLOC_MAX_LEN ((int64_t)SG_DOT_NOALLOC_CHUNK * SG_DOT_NOALLOC_MAX_PARTS)
+int sg_dot_noalloc(void *stream, int64_t len, int vec_dtype, const void *a,
+                   const void *b, double *d_out);
+
 #ifdef __cplusplus
 }
 #endif
