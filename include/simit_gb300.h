@@ -171,10 +171,11 @@ int sg_assemble_heat(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
  * (src/lower/index_expressions/lower_indexexprs.cpp:630-660).
  * bs = 1, 2, 3 have dedicated kernels; other bs use a generic kernel.
  * val_dtype is the matrix value type; vec_dtype the type of x and y;
- * accumulation is in the wider of the two.  g = lanes per block row:
- * 1,2,4,8,16,32 select the streaming kernel; -4,-8,-16 the TMA-staged kernel
- * (bs = 3, 16-byte aligned vals/colidx) with that many lanes; 0 picks (TMA
- * for FP32 values, the streaming kernel for FP64).
+ * accumulation is in the wider of the two.  g = 1,2,4,8,16,32 selects the
+ * streaming kernel with g lanes per block row; g = -1..-6 selects variant
+ * -g-1 of the TMA-staged kernel (bs = 3, 16-byte aligned vals/colidx;
+ * variants differ in lanes per row, rows per tile and pipeline stages);
+ * g = 0 picks (TMA variant 0 for FP32 values, the streaming kernel for FP64).
  * ------------------------------------------------------------------- */
 int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
              const uint32_t *colidx, int val_dtype, const void *vals,

@@ -6,19 +6,27 @@
 
 namespace sg {
 
-constexpr int TMA_ROWS = 32;
+// TMA SpMV variants: (lanes per block row, rows per tile, pipeline stages).
+// Variant 0 is the default.
+struct TmaVariant {
+  int G, ROWS, NST;
+};
+static const TmaVariant kTmaVariants[] = {
+    {8, 32, 3}, {8, 32, 2}, {8, 16, 4}, {4, 32, 3}, {16, 16, 4}, {8, 32, 4},
+};
+constexpr int kNumTmaVariants = sizeof(kTmaVariants) / sizeof(kTmaVariants[0]);
 
-template <int G, typename MT, typename VT, bool DOT>
-static int tma_config(Ctx *c, int32_t n, int maxrow, int *grid, size_t *smem) {
-  const int capb = TMA_ROWS * (maxrow > 0 ? maxrow : 1);
-  const size_t sh = tma_smem_bytes<MT>(capb);
+template <int G, int ROWS, int NST, typename MT, typename VT, bool DOT>
+static int tma_config_t(Ctx *c, int32_t n, int maxrow, int *grid, size_t *smem) {
+  const int capb = ROWS * (maxrow > 0 ? maxrow : 1);
+  const size_t sh = tma_smem_bytes<MT>(capb, NST);
   if (sh > 200 * 1024) return SG_ERR_UNSUPPORTED;
-  auto kern = k_bsr3_tma<G, TMA_ROWS, MT, VT, DOT>;
+  auto kern = k_bsr3_tma<G, ROWS, NST, MT, VT, DOT>;
   SG_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
   int per_sm = 0;
-  SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TMA_ROWS * G, sh));
+  SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, ROWS * G, sh));
   if (per_sm < 1) return SG_ERR_UNSUPPORTED;
-  const int ntiles = (n + TMA_ROWS - 1) / TMA_ROWS;
+  const int ntiles = (n + ROWS - 1) / ROWS;
   int gsz = per_sm * c->num_sms;
   if (gsz > ntiles) gsz = ntiles;
   if (gsz < 1) gsz = 1;
@@ -27,57 +35,74 @@ static int tma_config(Ctx *c, int32_t n, int maxrow, int *grid, size_t *smem) {
   return SG_OK;
 }
 
-template <int G, typename MT, typename VT, bool DOT>
-static int tma_launch(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n, const uint32_t *rp,
-                      const uint32_t *ci, const MT *v, const VT *x, VT *y, double *part,
-                      int maxrow, int grid, size_t smem) {
-  const int capb = TMA_ROWS * (maxrow > 0 ? maxrow : 1);
-  k_bsr3_tma<G, TMA_ROWS, MT, VT, DOT><<<grid, TMA_ROWS * G, smem, st>>>(
-      ctl, n, rp, ci, v, x, y, part, capb, c->d_err);
+template <int G, int ROWS, int NST, typename MT, typename VT, bool DOT>
+static int tma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n,
+                        const uint32_t *rp, const uint32_t *ci, const MT *v, const VT *x, VT *y,
+                        double *part, int maxrow, int grid, size_t smem) {
+  const int capb = ROWS * (maxrow > 0 ? maxrow : 1);
+  k_bsr3_tma<G, ROWS, NST, MT, VT, DOT><<<grid, ROWS * G, smem, st>>>(ctl, n, rp, ci, v, x, y,
+                                                                      part, capb, c->d_err);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
 
-int bsr3_tma_config(Ctx *c, int vdt, int xdt, int G, int dot, int32_t n, int maxrow, int *grid,
-                    size_t *smem) {
-#define SG_CFG(MT, VT)                                                                   \
-  if (G == 16) return dot ? tma_config<16, MT, VT, true>(c, n, maxrow, grid, smem)       \
-                          : tma_config<16, MT, VT, false>(c, n, maxrow, grid, smem);     \
-  if (G == 8) return dot ? tma_config<8, MT, VT, true>(c, n, maxrow, grid, smem)         \
-                         : tma_config<8, MT, VT, false>(c, n, maxrow, grid, smem);       \
-  return dot ? tma_config<4, MT, VT, true>(c, n, maxrow, grid, smem)                     \
-             : tma_config<4, MT, VT, false>(c, n, maxrow, grid, smem);
-  if (vdt == SG_F32 && xdt == SG_F32) { SG_CFG(float, float) }
-  if (vdt == SG_F64 && xdt == SG_F64) { SG_CFG(double, double) }
-  if (vdt == SG_F32 && xdt == SG_F64) { SG_CFG(float, double) }
-#undef SG_CFG
+// Dispatch over (variant, dot) for one (MT, VT).
+template <typename MT, typename VT>
+static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
+                        const SolveCtl *ctl, int32_t n, const uint32_t *rp, const uint32_t *ci,
+                        const void *v, const void *x, void *y, double *part, int maxrow,
+                        int *grid, size_t *smem) {
+#define SG_V(ID, G, R, N)                                                                      \
+  case ID:                                                                                     \
+    if (launch)                                                                                \
+      return dot ? tma_launch_t<G, R, N, MT, VT, true>(c, st, ctl, n, rp, ci, (const MT *)v,   \
+                                                       (const VT *)x, (VT *)y, part, maxrow,   \
+                                                       *grid, *smem)                           \
+                 : tma_launch_t<G, R, N, MT, VT, false>(c, st, ctl, n, rp, ci, (const MT *)v,  \
+                                                        (const VT *)x, (VT *)y, part, maxrow,  \
+                                                        *grid, *smem);                         \
+    return dot ? tma_config_t<G, R, N, MT, VT, true>(c, n, maxrow, grid, smem)                 \
+               : tma_config_t<G, R, N, MT, VT, false>(c, n, maxrow, grid, smem);
+  switch (var) {
+    SG_V(0, 8, 32, 3)
+    SG_V(1, 8, 32, 2)
+    SG_V(2, 8, 16, 4)
+    SG_V(3, 4, 32, 3)
+    SG_V(4, 16, 16, 4)
+    SG_V(5, 8, 32, 4)
+    default: return SG_ERR_ARG;
+  }
+#undef SG_V
+}
+
+static int tma_any(Ctx *c, cudaStream_t st, bool launch, int vdt, int xdt, int var, int dot,
+                   const void *ctl, int32_t n, const uint32_t *rp, const uint32_t *ci,
+                   const void *v, const void *x, void *y, double *part, int maxrow, int *grid,
+                   size_t *smem) {
+  const SolveCtl *k = (const SolveCtl *)ctl;
+  if (vdt == SG_F32 && xdt == SG_F32)
+    return tma_dispatch<float, float>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part,
+                                      maxrow, grid, smem);
+  if (vdt == SG_F64 && xdt == SG_F64)
+    return tma_dispatch<double, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part,
+                                        maxrow, grid, smem);
+  if (vdt == SG_F32 && xdt == SG_F64)
+    return tma_dispatch<float, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part,
+                                       maxrow, grid, smem);
   return SG_ERR_UNSUPPORTED;
 }
 
-int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, int G, int dot,
+int bsr3_tma_config(Ctx *c, int vdt, int xdt, int var, int dot, int32_t n, int maxrow,
+                    int *grid, size_t *smem) {
+  return tma_any(c, nullptr, false, vdt, xdt, var, dot, nullptr, n, nullptr, nullptr, nullptr,
+                 nullptr, nullptr, nullptr, maxrow, grid, smem);
+}
+
+int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, int var, int dot,
                     int32_t n, const uint32_t *rp, const uint32_t *ci, const void *v,
                     const void *x, void *y, double *part, int maxrow, int grid, size_t smem) {
-  const SolveCtl *k = (const SolveCtl *)ctl;
-#define SG_L(MT, VT)                                                                          \
-  if (G == 16)                                                                                \
-    return dot ? tma_launch<16, MT, VT, true>(c, st, k, n, rp, ci, (const MT *)v,             \
-                                              (const VT *)x, (VT *)y, part, maxrow, grid, smem) \
-               : tma_launch<16, MT, VT, false>(c, st, k, n, rp, ci, (const MT *)v,            \
-                                               (const VT *)x, (VT *)y, part, maxrow, grid, smem); \
-  if (G == 8)                                                                                 \
-    return dot ? tma_launch<8, MT, VT, true>(c, st, k, n, rp, ci, (const MT *)v, (const VT *)x, \
-                                             (VT *)y, part, maxrow, grid, smem)                \
-               : tma_launch<8, MT, VT, false>(c, st, k, n, rp, ci, (const MT *)v,             \
-                                              (const VT *)x, (VT *)y, part, maxrow, grid, smem); \
-  return dot ? tma_launch<4, MT, VT, true>(c, st, k, n, rp, ci, (const MT *)v, (const VT *)x,   \
-                                           (VT *)y, part, maxrow, grid, smem)                  \
-             : tma_launch<4, MT, VT, false>(c, st, k, n, rp, ci, (const MT *)v, (const VT *)x,  \
-                                            (VT *)y, part, maxrow, grid, smem);
-  if (vdt == SG_F32 && xdt == SG_F32) { SG_L(float, float) }
-  if (vdt == SG_F64 && xdt == SG_F64) { SG_L(double, double) }
-  if (vdt == SG_F32 && xdt == SG_F64) { SG_L(float, double) }
-#undef SG_L
-  return SG_ERR_UNSUPPORTED;
+  return tma_any(c, st, true, vdt, xdt, var, dot, ctl, n, rp, ci, v, x, y, part, maxrow, &grid,
+                 &smem);
 }
 
 int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out) {
@@ -251,9 +276,9 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
   SG_REQUIRE(n >= 0 && bs >= 1 && bs <= 16, "sg_bspmv: bad n=%d bs=%d", n, bs);
   if (n == 0) return SG_OK;
   const bool aligned = ((uintptr_t)vals % 16 == 0) && ((uintptr_t)colidx % 16 == 0);
-  if (g < 0) SG_REQUIRE(bs == 3 && aligned && (g == -4 || g == -8 || g == -16),
-                        "sg_bspmv: g=%d selects the TMA kernel: bs=3, 16-byte aligned arrays, "
-                        "g in {-4,-8,-16}", g);
+  if (g < 0) SG_REQUIRE(bs == 3 && aligned && -g - 1 < kNumTmaVariants,
+                        "sg_bspmv: g=%d selects TMA variant %d: bs=3, 16-byte aligned arrays, "
+                        "-%d <= g <= -1", g, -g - 1, kNumTmaVariants);
   if ((g == 0 && bs == 3 && aligned && !(vdt == SG_F64 && xdt == SG_F64)) || g < 0) {
     // TMA-staged kernel (lanes per row from the row length unless given).
     // FP64 matrices default to the plain kernel, which keeps more warps in
@@ -261,10 +286,10 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
     int mr = 0, grid = 0;
     size_t sh = 0;
     SG_TRY(cached_maxrow(c, n, rowptr, &mr));
-    const int G = g < 0 ? -g : 8;
-    if (bsr3_tma_config(c, vdt, xdt, G, 0, n, mr, &grid, &sh) == SG_OK)
-      return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, G, 0, n, rowptr, colidx, vals, x, y,
-                             nullptr, mr, grid, sh);
+    const int var = g < 0 ? -g - 1 : 0;
+    if (bsr3_tma_config(c, vdt, xdt, var, 0, n, mr, &grid, &sh) == SG_OK)
+      return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, var, 0, n, rowptr, colidx, vals, x,
+                             y, nullptr, mr, grid, sh);
   }
   // nnzb is only needed for the default lane choice; read rowptr[n] then.
   int64_t nnzb = 0;
