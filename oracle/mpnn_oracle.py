@@ -1,0 +1,143 @@
+"""ORACLE (test infrastructure): numpy restatement of the message-passing
+preconditioner network, forward and backward, used only by tests to check the
+GPU kernels (simit_gb300/csrc/sg_mpnn.cu).  The network has no counterpart in
+the reference; this file states its definition:
+
+  s_v  = D_v^-1 r_v                       (3x3 block-Jacobi of A)
+  m1_v = sum_{u in N(v), u != v} a_vu s_u
+  g1_v = W1s s_v + W1m m1_v,  h1 = relu(g1)          (64)
+  q2_v = P2 h1_v                                     (8)
+  m2_v = sum a_vu q2_u
+  g2_v = W2h bf(h1_v) + W2m m2_v,  h2 = relu(g2)     (64)
+  q3_v = P3 h2_v
+  m3_v = sum a_vu q3_u
+  g3_v = W3h bf(h2_v) + W3m m3_v,  h3 = relu(g3)     (64)
+  z_v  = s_v + Wout h3_v
+
+with a_vu = ||A_vu||_F / sqrt(||A_vv||_F ||A_uu||_F) for the off-diagonal
+blocks of the pattern, bf() rounding to bfloat16 (round to nearest even), and
+W2h, W3h rounded to bfloat16 (the tensor-core operands).  No biases: the map
+r -> z is positively homogeneous.
+"""
+import numpy as np
+
+H, K = 64, 8
+SHAPES = [("W1s", (H, 3)), ("W1m", (H, 3)), ("P2", (K, H)), ("W2h", (H, H)), ("W2m", (H, K)),
+          ("P3", (K, H)), ("W3h", (H, H)), ("W3m", (H, K)), ("Wout", (3, H))]
+NPARAM = sum(a * b for _, (a, b) in SHAPES)
+
+
+def unpack(flat):
+    out, o = {}, 0
+    for name, (a, b) in SHAPES:
+        out[name] = np.asarray(flat[o:o + a * b], np.float64).reshape(a, b)
+        o += a * b
+    return out
+
+
+def bf16(x):
+    """Round float values to bfloat16 (nearest even), returned as float64."""
+    f = np.asarray(x, np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def edge_weights(n, rowptr, colidx, vals):
+    """a per nonzero block (0 on the diagonal blocks)."""
+    A = np.asarray(vals, np.float64).reshape(-1, 9)
+    nrm = np.sqrt((A * A).sum(1))
+    rows = np.repeat(np.arange(n), np.diff(rowptr.astype(np.int64)))
+    cols = colidx.astype(np.int64)
+    dn = np.zeros(n)
+    diag = rows == cols
+    dn[rows[diag]] = nrm[diag]
+    a = nrm / np.sqrt(dn[rows] * dn[cols])
+    a[diag] = 0.0
+    return a, rows, cols
+
+
+def block_jacobi(n, rowptr, colidx, vals):
+    A = np.asarray(vals, np.float64).reshape(-1, 3, 3)
+    rows = np.repeat(np.arange(n), np.diff(rowptr.astype(np.int64)))
+    d = rows == colidx.astype(np.int64)
+    Dinv = np.zeros((n, 3, 3))
+    Dinv[rows[d]] = np.linalg.inv(A[d])
+    return Dinv
+
+
+def _agg(a, rows, cols, x, n):
+    out = np.zeros((n,) + x.shape[1:])
+    np.add.at(out, rows, a[:, None] * x[cols])
+    return out
+
+
+def forward(params, n, rowptr, colidx, vals, r):
+    p = unpack(params)
+    W2h, W3h = bf16(p["W2h"]), bf16(p["W3h"])
+    a, rows, cols = edge_weights(n, rowptr, colidx, vals)
+    Dinv = block_jacobi(n, rowptr, colidx, vals)
+    rv = np.asarray(r, np.float64).reshape(n, 3)
+    s = np.einsum("vij,vj->vi", Dinv, rv)
+    m1 = _agg(a, rows, cols, s, n)
+    g1 = s @ p["W1s"].T + m1 @ p["W1m"].T
+    h1 = np.maximum(g1, 0)
+    q2 = h1 @ p["P2"].T
+    m2 = _agg(a, rows, cols, q2, n)
+    h1b = bf16(h1)
+    g2 = h1b @ W2h.T + m2 @ p["W2m"].T
+    h2 = np.maximum(g2, 0)
+    q3 = h2 @ p["P3"].T
+    m3 = _agg(a, rows, cols, q3, n)
+    h2b = bf16(h2)
+    g3 = h2b @ W3h.T + m3 @ p["W3m"].T
+    h3 = np.maximum(g3, 0)
+    z = s + h3 @ p["Wout"].T
+    cache = dict(a=a, rows=rows, cols=cols, s=s, m1=m1, g1=g1, h1=h1, h1b=h1b, q2=q2, m2=m2,
+                 g2=g2, h2=h2, h2b=h2b, q3=q3, m3=m3, g3=g3, h3=h3, W2h=W2h, W3h=W3h, p=p, n=n)
+    return z.reshape(-1), cache
+
+
+def backward(cache, dz):
+    """Weight gradients (flat, in SHAPES order) for dL/dz = dz.  The bf16
+    roundings pass gradients straight through."""
+    c = cache
+    p, n = c["p"], c["n"]
+    a, rows, cols = c["a"], c["rows"], c["cols"]
+    dz = np.asarray(dz, np.float64).reshape(n, 3)
+    g = {}
+    g["Wout"] = dz.T @ c["h3"]
+    dh3 = dz @ p["Wout"]
+    dg3 = dh3 * (c["g3"] > 0)
+    g["W3h"] = dg3.T @ c["h2b"]
+    g["W3m"] = dg3.T @ c["m3"]
+    dh2 = dg3 @ c["W3h"]
+    dm3 = dg3 @ p["W3m"]
+    dq3 = _agg(a, rows, cols, dm3, n)  # a is symmetric: the transpose aggregation
+    g["P3"] = dq3.T @ c["h2"]
+    dh2 = dh2 + dq3 @ p["P3"]
+    dg2 = dh2 * (c["g2"] > 0)
+    g["W2h"] = dg2.T @ c["h1b"]
+    g["W2m"] = dg2.T @ c["m2"]
+    dh1 = dg2 @ c["W2h"]
+    dm2 = dg2 @ p["W2m"]
+    dq2 = _agg(a, rows, cols, dm2, n)
+    g["P2"] = dq2.T @ c["h1"]
+    dh1 = dh1 + dq2 @ p["P2"]
+    dg1 = dh1 * (c["g1"] > 0)
+    g["W1s"] = dg1.T @ c["s"]
+    g["W1m"] = dg1.T @ c["m1"]
+    return np.concatenate([g[name].reshape(-1) for name, _ in SHAPES])
+
+
+def init_params(seed=0, out_scale=0.0):
+    """He-style initialisation; Wout scaled by out_scale (0 = start exactly at
+    block-Jacobi)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    parts = []
+    for name, (a, b) in SHAPES:
+        w = rng.normal(0, np.sqrt(2.0 / b), size=(a, b))
+        if name == "Wout":
+            w *= out_scale
+        parts.append(w.reshape(-1))
+    return np.concatenate(parts).astype(np.float32)

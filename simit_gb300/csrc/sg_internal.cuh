@@ -27,6 +27,8 @@ struct Ctx {
   const uint32_t *mr_ptr[MAXROW_CACHE] = {};
   int32_t mr_n[MAXROW_CACHE] = {};
   int32_t mr_val[MAXROW_CACHE] = {};
+  int32_t mr_t16[MAXROW_CACHE] = {};  // largest 16-row tile, in blocks
+  int32_t mr_t32[MAXROW_CACHE] = {};  // largest 32-row tile, in blocks
   int mr_next = 0;
   int refs = 1;  // sg_ctx_destroy + one per live solver
 };

@@ -4,6 +4,7 @@
 
 #include "sg_internal.cuh"
 #include "sg_solver_kernels.cuh"
+#include "sg_spmv_api.h"
 
 namespace sg {
 
@@ -18,6 +19,7 @@ struct Solver {
   int64_t len = 0;     // n * bs
   int G = 4, P1 = 1, P2 = 1;
   int tma = 0, tma_var = 0, maxrow = 0;  // K1 uses the TMA-staged SpMV (variant)
+  PatternStats pstats;
   size_t tma_smem = 0;
   int64_t launches = 0;             // kernels launched by the current solve
   int64_t graph_kernels = 0;        // kernel nodes in one batch graph

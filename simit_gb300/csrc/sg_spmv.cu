@@ -12,13 +12,20 @@ struct TmaVariant {
   int G, ROWS, NST;
 };
 static const TmaVariant kTmaVariants[] = {
-    {8, 32, 3}, {8, 32, 2}, {8, 16, 4}, {4, 32, 3}, {16, 16, 4}, {8, 32, 4},
+    {8, 32, 2}, {8, 32, 3}, {8, 16, 4}, {4, 32, 3}, {16, 16, 4}, {8, 16, 2},
 };
 constexpr int kNumTmaVariants = sizeof(kTmaVariants) / sizeof(kTmaVariants[0]);
 
+// Blocks in the largest tile of `rows` consecutive rows (the buffer size).
+static int tile_cap(int rows, const PatternStats &ps) {
+  const int bound = rows * (ps.maxrow > 0 ? ps.maxrow : 1);
+  const int t = rows == 16 ? ps.tile16 : (rows == 32 ? ps.tile32 : 0);
+  return (t > 0 && t < bound) ? t : bound;
+}
+
 template <int G, int ROWS, int NST, typename MT, typename VT, bool DOT>
-static int tma_config_t(Ctx *c, int32_t n, int maxrow, int *grid, size_t *smem) {
-  const int capb = ROWS * (maxrow > 0 ? maxrow : 1);
+static int tma_config_t(Ctx *c, int32_t n, const PatternStats &ps, int *grid, size_t *smem) {
+  const int capb = tile_cap(ROWS, ps);
   const size_t sh = tma_smem_bytes<MT>(capb, NST);
   if (sh > 200 * 1024) return SG_ERR_UNSUPPORTED;
   auto kern = k_bsr3_tma<G, ROWS, NST, MT, VT, DOT>;
@@ -38,8 +45,8 @@ static int tma_config_t(Ctx *c, int32_t n, int maxrow, int *grid, size_t *smem) 
 template <int G, int ROWS, int NST, typename MT, typename VT, bool DOT>
 static int tma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n,
                         const uint32_t *rp, const uint32_t *ci, const MT *v, const VT *x, VT *y,
-                        double *part, int maxrow, int grid, size_t smem) {
-  const int capb = ROWS * (maxrow > 0 ? maxrow : 1);
+                        double *part, const PatternStats &ps, int grid, size_t smem) {
+  const int capb = tile_cap(ROWS, ps);
   k_bsr3_tma<G, ROWS, NST, MT, VT, DOT><<<grid, ROWS * G, smem, st>>>(ctl, n, rp, ci, v, x, y,
                                                                       part, capb, c->d_err);
   SG_CHECK_LAUNCH();
@@ -50,26 +57,26 @@ static int tma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n,
 template <typename MT, typename VT>
 static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
                         const SolveCtl *ctl, int32_t n, const uint32_t *rp, const uint32_t *ci,
-                        const void *v, const void *x, void *y, double *part, int maxrow,
-                        int *grid, size_t *smem) {
+                        const void *v, const void *x, void *y, double *part,
+                        const PatternStats &ps, int *grid, size_t *smem) {
 #define SG_V(ID, G, R, N)                                                                      \
   case ID:                                                                                     \
     if (launch)                                                                                \
       return dot ? tma_launch_t<G, R, N, MT, VT, true>(c, st, ctl, n, rp, ci, (const MT *)v,   \
-                                                       (const VT *)x, (VT *)y, part, maxrow,   \
+                                                       (const VT *)x, (VT *)y, part, ps,       \
                                                        *grid, *smem)                           \
                  : tma_launch_t<G, R, N, MT, VT, false>(c, st, ctl, n, rp, ci, (const MT *)v,  \
-                                                        (const VT *)x, (VT *)y, part, maxrow,  \
+                                                        (const VT *)x, (VT *)y, part, ps,      \
                                                         *grid, *smem);                         \
-    return dot ? tma_config_t<G, R, N, MT, VT, true>(c, n, maxrow, grid, smem)                 \
-               : tma_config_t<G, R, N, MT, VT, false>(c, n, maxrow, grid, smem);
+    return dot ? tma_config_t<G, R, N, MT, VT, true>(c, n, ps, grid, smem)                     \
+               : tma_config_t<G, R, N, MT, VT, false>(c, n, ps, grid, smem);
   switch (var) {
-    SG_V(0, 8, 32, 3)
-    SG_V(1, 8, 32, 2)
+    SG_V(0, 8, 32, 2)
+    SG_V(1, 8, 32, 3)
     SG_V(2, 8, 16, 4)
     SG_V(3, 4, 32, 3)
     SG_V(4, 16, 16, 4)
-    SG_V(5, 8, 32, 4)
+    SG_V(5, 8, 16, 2)
     default: return SG_ERR_ARG;
   }
 #undef SG_V
@@ -77,47 +84,88 @@ static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
 
 static int tma_any(Ctx *c, cudaStream_t st, bool launch, int vdt, int xdt, int var, int dot,
                    const void *ctl, int32_t n, const uint32_t *rp, const uint32_t *ci,
-                   const void *v, const void *x, void *y, double *part, int maxrow, int *grid,
-                   size_t *smem) {
+                   const void *v, const void *x, void *y, double *part, const PatternStats &ps,
+                   int *grid, size_t *smem) {
   const SolveCtl *k = (const SolveCtl *)ctl;
   if (vdt == SG_F32 && xdt == SG_F32)
-    return tma_dispatch<float, float>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part,
-                                      maxrow, grid, smem);
+    return tma_dispatch<float, float>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part, ps,
+                                      grid, smem);
   if (vdt == SG_F64 && xdt == SG_F64)
-    return tma_dispatch<double, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part,
-                                        maxrow, grid, smem);
+    return tma_dispatch<double, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part, ps,
+                                        grid, smem);
   if (vdt == SG_F32 && xdt == SG_F64)
-    return tma_dispatch<float, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part,
-                                       maxrow, grid, smem);
+    return tma_dispatch<float, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part, ps,
+                                       grid, smem);
   return SG_ERR_UNSUPPORTED;
 }
 
-int bsr3_tma_config(Ctx *c, int vdt, int xdt, int var, int dot, int32_t n, int maxrow,
-                    int *grid, size_t *smem) {
+int bsr3_tma_config(Ctx *c, int vdt, int xdt, int var, int dot, int32_t n,
+                    const PatternStats &ps, int *grid, size_t *smem) {
   return tma_any(c, nullptr, false, vdt, xdt, var, dot, nullptr, n, nullptr, nullptr, nullptr,
-                 nullptr, nullptr, nullptr, maxrow, grid, smem);
+                 nullptr, nullptr, nullptr, ps, grid, smem);
 }
 
 int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, int var, int dot,
                     int32_t n, const uint32_t *rp, const uint32_t *ci, const void *v,
-                    const void *x, void *y, double *part, int maxrow, int grid, size_t smem) {
-  return tma_any(c, st, true, vdt, xdt, var, dot, ctl, n, rp, ci, v, x, y, part, maxrow, &grid,
+                    const void *x, void *y, double *part, const PatternStats &ps, int grid,
+                    size_t smem) {
+  return tma_any(c, st, true, vdt, xdt, var, dot, ctl, n, rp, ci, v, x, y, part, ps, &grid,
                  &smem);
 }
 
-int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out) {
+// Longest row and largest 16- / 32-row tiles (blocks) of a pattern.
+__global__ void k_pattern_stats(const uint32_t *rowptr, int32_t n, uint32_t *out) {
+  uint32_t mr = 0, t16 = 0, t32 = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    mr = max(mr, rowptr[i + 1] - rowptr[i]);
+    if (i % 16 == 0) t16 = max(t16, rowptr[min((int64_t)n, i + 16)] - rowptr[i]);
+    if (i % 32 == 0) t32 = max(t32, rowptr[min((int64_t)n, i + 32)] - rowptr[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mr = max(mr, __shfl_down_sync(0xffffffffu, mr, o));
+    t16 = max(t16, __shfl_down_sync(0xffffffffu, t16, o));
+    t32 = max(t32, __shfl_down_sync(0xffffffffu, t32, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], mr);
+    atomicMax(&out[1], t16);
+    atomicMax(&out[2], t32);
+  }
+}
+
+int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps) {
   for (int i = 0; i < Ctx::MAXROW_CACHE; ++i)
     if (c->mr_ptr[i] == rowptr && c->mr_n[i] == n) {
-      *out = c->mr_val[i];
+      ps->maxrow = c->mr_val[i];
+      ps->tile16 = c->mr_t16[i];
+      ps->tile32 = c->mr_t32[i];
       return SG_OK;
     }
-  int32_t mr = 0;
-  SG_TRY(sg_pattern_maxrow(reinterpret_cast<sg_ctx *>(c), n, rowptr, &mr));
+  Scratch s(c);
+  SG_TRY(s.reserve(256));
+  uint32_t *d = s.alloc<uint32_t>(4);
+  SG_CHECK_CUDA(cudaMemsetAsync(d, 0, 16, c->stream));
+  if (n > 0) {
+    k_pattern_stats<<<grid_for(c, n, 256, 4), 256, 0, c->stream>>>(rowptr, n, d);
+    SG_CHECK_LAUNCH();
+  }
+  SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, d, 16, cudaMemcpyDeviceToHost, c->stream));
+  SG_CHECK_CUDA(cudaStreamSynchronize(c->stream));
+  const uint32_t *h = (const uint32_t *)c->h_stage;
   const int slot = c->mr_next++ % Ctx::MAXROW_CACHE;
   c->mr_ptr[slot] = rowptr;
   c->mr_n[slot] = n;
-  c->mr_val[slot] = mr;
-  *out = mr;
+  c->mr_val[slot] = ps->maxrow = (int32_t)h[0];
+  c->mr_t16[slot] = ps->tile16 = (int32_t)h[1];
+  c->mr_t32[slot] = ps->tile32 = (int32_t)h[2];
+  return SG_OK;
+}
+
+int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out) {
+  PatternStats ps;
+  SG_TRY(cached_stats(c, n, rowptr, &ps));
+  *out = ps.maxrow;
   return SG_OK;
 }
 
@@ -283,13 +331,14 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
     // TMA-staged kernel (lanes per row from the row length unless given).
     // FP64 matrices default to the plain kernel, which keeps more warps in
     // flight for the FP64 pipe.
-    int mr = 0, grid = 0;
+    int grid = 0;
     size_t sh = 0;
-    SG_TRY(cached_maxrow(c, n, rowptr, &mr));
+    PatternStats ps;
+    SG_TRY(cached_stats(c, n, rowptr, &ps));
     const int var = g < 0 ? -g - 1 : 0;
-    if (bsr3_tma_config(c, vdt, xdt, var, 0, n, mr, &grid, &sh) == SG_OK)
+    if (bsr3_tma_config(c, vdt, xdt, var, 0, n, ps, &grid, &sh) == SG_OK)
       return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, var, 0, n, rowptr, colidx, vals, x,
-                             y, nullptr, mr, grid, sh);
+                             y, nullptr, ps, grid, sh);
   }
   // nnzb is only needed for the default lane choice; read rowptr[n] then.
   int64_t nnzb = 0;

@@ -5,14 +5,19 @@
 
 namespace sg {
 struct Ctx;
+struct PatternStats {
+  int maxrow = 0, tile16 = 0, tile32 = 0;
+};
 int default_lanes(int32_t n, int64_t nnzb, int32_t bs);
 int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out);
+int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps);
 // TMA-staged 3x3 SpMV: grid/shared-memory for variant `var` (0 = default;
 // see kTmaVariants in sg_spmv.cu); launch.  dot = 1 also writes per-CTA
 // partials of x.y (CG K1) and honours ctl.
-int bsr3_tma_config(Ctx *c, int vdt, int xdt, int var, int dot, int32_t n, int maxrow, int *grid,
-                    size_t *smem);
+int bsr3_tma_config(Ctx *c, int vdt, int xdt, int var, int dot, int32_t n,
+                    const PatternStats &ps, int *grid, size_t *smem);
 int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, int var, int dot,
                     int32_t n, const uint32_t *rp, const uint32_t *ci, const void *v,
-                    const void *x, void *y, double *part, int maxrow, int grid, size_t smem);
+                    const void *x, void *y, double *part, const PatternStats &ps, int grid,
+                    size_t smem);
 }  // namespace sg
