@@ -215,7 +215,10 @@ enum {
   SG_PRECOND_NONE = 0,
   SG_PRECOND_JACOBI = 1,        /* point Jacobi (thermal.sim assemble_jacobi) */
   SG_PRECOND_BLOCK_JACOBI = 2,  /* inverse of each 3x3 diagonal block */
-  SG_PRECOND_LEARNED = 3        /* message-passing network, sg_mpnn_* */
+  SG_PRECOND_LEARNED = 3        /* message-passing network (sg_mpnn_*) in flexible
+                                   PCG; needs SG_SOLVE_MIXED and bs = 3.  Falls back
+                                   to block Jacobi when r.z <= 0 or the residual
+                                   grows 100x (result.fallbacks counts it). */
 };
 enum { SG_STOP_NORMR2 = 0, SG_STOP_NORMR = 1, SG_STOP_RELATIVE = 2 };
 enum {
@@ -247,6 +250,7 @@ typedef struct sg_solve_opts {
   double reliable_delta;     /* mixed only; 0 -> 0.1 */
   int32_t lanes;             /* SpMV lanes per block row; 0 = default */
   int32_t batch;             /* iterations per graph launch (even); 0 = 32 */
+  const float *learned_params; /* SG_PRECOND_LEARNED: device FP32[sg_mpnn_nparams()] */
 } sg_solve_opts;
 
 typedef struct sg_solve_result {
@@ -277,6 +281,34 @@ int sg_solver_destroy(sg_solver *s);
 /* One-shot create + solve + destroy. */
 int sg_solve(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
              const double *b, double *x, sg_solve_result *res);
+
+/* ---------------------------------------------------------------------
+ * Learned preconditioner: a 3-layer message-passing network (hidden 64,
+ * messages of 8, no biases) over the matrix graph, z = D^-1 r + Wout h3,
+ * where D is the 3x3 block diagonal; the 64x64 layers run on the tensor
+ * cores with bf16 weights and FP32 accumulation.  It has no counterpart in
+ * the reference (the benchmark spec's learned part).  Parameters are one flat
+ * FP32 device array of sg_mpnn_nparams() values.  Training: forward with
+ * train = 1 keeps activations, sg_mpnn_loss gives the A-norm error
+ * (z-e)'A(z-e)/e'Ae of a residual/correction pair (r, e = A^-1 r) and dL/dz,
+ * sg_mpnn_backward the parameter gradient, sg_mpnn_adam the update.
+ * ------------------------------------------------------------------- */
+typedef struct sg_mpnn_graph sg_mpnn_graph;
+int sg_mpnn_nparams(void);
+/* Edge weights and block-Jacobi of a 3x3-blocked matrix (FP32 or FP64). */
+int sg_mpnn_graph_create(sg_ctx *ctx, const sg_matrix *A, sg_mpnn_graph **out);
+int sg_mpnn_graph_refresh(sg_mpnn_graph *g);
+int sg_mpnn_graph_destroy(sg_mpnn_graph *g);
+/* z = net(r); r, z FP32 [n*3]. */
+int sg_mpnn_forward(sg_mpnn_graph *g, const float *params, const float *r, float *z,
+                    int train);
+/* grad (FP32[nparams], overwritten) of the last train-mode forward for dz. */
+int sg_mpnn_backward(sg_mpnn_graph *g, const float *params, const float *dz, float *grad);
+/* A-norm loss of z against e (FP32 matrix graphs); dz = 2 A (z-e) / e'Ae. */
+int sg_mpnn_loss(sg_mpnn_graph *g, const float *z, const float *e, double eAe, float *dz,
+                 double *h_loss);
+int sg_mpnn_adam(sg_ctx *ctx, float *params, const float *grad, float *m, float *v, int step,
+                 float lr, float beta1, float beta2, float eps);
 
 /* ---------------------------------------------------------------------
  * Dot product that allocates nothing.  This entry point has no counterpart

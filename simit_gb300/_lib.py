@@ -40,7 +40,7 @@ class SolveOpts(ctypes.Structure):
     """sg_solve_opts"""
     _fields_ = [("precision", ctypes.c_int), ("precond", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", D), ("maxiters", I32), ("verify", I32), ("check_every", I32),
-                ("reliable_delta", D), ("lanes", I32), ("batch", I32)]
+                ("reliable_delta", D), ("lanes", I32), ("batch", I32), ("learned_params", P)]
 
 
 class SolveResult(ctypes.Structure):
@@ -85,6 +85,15 @@ SIGNATURES = {
     "sg_solver_destroy": (_CI, [P]),
     "sg_solver_refresh": (_CI, [P]),
     "sg_dot_noalloc": (_CI, [P, I64, _CI, P, P, P]),
+    "sg_mpnn_nparams": (_CI, []),
+    "sg_mpnn_graph_create": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(P)]),
+    "sg_mpnn_graph_refresh": (_CI, [P]),
+    "sg_mpnn_graph_destroy": (_CI, [P]),
+    "sg_mpnn_forward": (_CI, [P, P, P, P, _CI]),
+    "sg_mpnn_backward": (_CI, [P, P, P, P]),
+    "sg_mpnn_loss": (_CI, [P, P, P, D, P, ctypes.POINTER(D)]),
+    "sg_mpnn_adam": (_CI, [P, P, P, P, P, _CI, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_float]),
     "sg_solve": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(SolveOpts), P, P,
                        ctypes.POINTER(SolveResult)]),
 }

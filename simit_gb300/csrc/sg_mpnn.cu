@@ -1,0 +1,481 @@
+// Learned (message-passing) preconditioner: graph data, forward, backward,
+// loss, optimiser and the flexible-PCG hook.  Definitions in sg_mpnn.cuh.
+#include <math.h>
+
+#include "sg_internal.cuh"
+#include "sg_mpnn_fwd.cuh"
+#include "sg_solver.h"
+#include "sg_spmv_api.h"
+
+namespace sg {
+namespace mpnn {
+
+struct GraphH {
+  Ctx *c = nullptr;
+  Graph g;
+  std::vector<void *> allocs;
+  bool train_ready = false;
+};
+
+static int galloc(GraphH *G, void **p, size_t bytes) {
+  SG_CHECK_CUDA(cudaMalloc(p, bytes < 256 ? 256 : bytes));
+  G->allocs.push_back(*p);
+  return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// backward (FP32, one warp per vertex; training meshes only)
+// ---------------------------------------------------------------------------
+// B1: dg3 = (Wout^T dz) * [g3 > 0]; dm3 = W3m^T dg3; dh2a = bf(W3h)^T dg3.
+__global__ void k_b1(int32_t n, const float *__restrict__ prm, const float *__restrict__ dz,
+                     const float *__restrict__ g3, float *__restrict__ dg3,
+                     float *__restrict__ dm3, float *__restrict__ dh2a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = wid; v < n; v += nw) {
+    const float d0 = dz[v * 3], d1 = dz[v * 3 + 1], d2 = dz[v * 3 + 2];
+    float dg[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int h = lane * 2 + e;
+      const float d = prm[O_WOUT + h] * d0 + prm[O_WOUT + H + h] * d1 + prm[O_WOUT + 2 * H + h] * d2;
+      dg[e] = g3[v * H + h] > 0.f ? d : 0.f;
+      dg3[v * H + h] = dg[e];
+    }
+    // dm3_j = sum_h W3m[h][j] dg3[h]
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      float p = prm[O_W3M + (lane * 2) * K + j] * dg[0] + prm[O_W3M + (lane * 2 + 1) * K + j] * dg[1];
+      for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+      if (lane == 0) dm3[v * K + j] = p;
+    }
+    // dh2a[c] = sum_h bf(W3h[h][c]) dg3[h]; lane owns c = 2*lane + e
+    float acc0 = 0.f, acc1 = 0.f;
+    for (int h = 0; h < H; ++h) {
+      const float dgh = __shfl_sync(0xffffffffu, dg[h & 1], h >> 1);
+      acc0 += bf16r(prm[O_W3H + h * H + lane * 2]) * dgh;
+      acc1 += bf16r(prm[O_W3H + h * H + lane * 2 + 1]) * dgh;
+    }
+    dh2a[v * H + lane * 2] = acc0;
+    dh2a[v * H + lane * 2 + 1] = acc1;
+  }
+}
+
+// Generic middle step: dq = sum_u a dm_u (K); dh = dha + P^T dq; dg = dh *
+// [g > 0]; optional dm_next = Wm^T dg (K), dha_next = bf(Wh)^T dg (H).
+__global__ void k_bmid(int32_t n, const uint32_t *__restrict__ rowptr,
+                       const uint32_t *__restrict__ colidx, const float *__restrict__ a,
+                       const float *__restrict__ prm, int oP, int oWm, int oWh,
+                       const float *__restrict__ dm, const float *__restrict__ dha,
+                       const float *__restrict__ g, float *__restrict__ dq,
+                       float *__restrict__ dgout, float *__restrict__ dm_next,
+                       float *__restrict__ dha_next) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = wid; v < n; v += nw) {
+    // dq (K values): lanes 0..7 gather one component each
+    float dqj = 0.f;
+    if (lane < K)
+      for (uint32_t q = rowptr[v]; q < rowptr[v + 1]; ++q) dqj += a[q] * dm[(size_t)colidx[q] * K + lane];
+    if (lane < K) dq[v * K + lane] = dqj;
+    float dg[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int h = lane * 2 + e;
+      float d = dha[v * H + h];
+#pragma unroll
+      for (int j = 0; j < K; ++j) d += prm[oP + j * H + h] * __shfl_sync(0xffffffffu, dqj, j);
+      dg[e] = g[v * H + h] > 0.f ? d : 0.f;
+      dgout[v * H + h] = dg[e];
+    }
+    if (dm_next) {
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        float p = prm[oWm + (lane * 2) * K + j] * dg[0] + prm[oWm + (lane * 2 + 1) * K + j] * dg[1];
+        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+        if (lane == 0) dm_next[v * K + j] = p;
+      }
+      float acc0 = 0.f, acc1 = 0.f;
+      for (int h = 0; h < H; ++h) {
+        const float dgh = __shfl_sync(0xffffffffu, dg[h & 1], h >> 1);
+        acc0 += bf16r(prm[oWh + h * H + lane * 2]) * dgh;
+        acc1 += bf16r(prm[oWh + h * H + lane * 2 + 1]) * dgh;
+      }
+      dha_next[v * H + lane * 2] = acc0;
+      dha_next[v * H + lane * 2 + 1] = acc1;
+    }
+  }
+}
+
+// Outer-product reduction dW[o][i] = sum_v X_v[o] * Y_v[i] over a chunk of
+// vertices per CTA; partials part[chunk][O*I], summed in order afterwards.
+// Y is transformed: 0 identity, 1 relu, 2 bf16(relu).
+constexpr int OUTER_CHUNK = 1024;
+__global__ void k_outer(int32_t n, const float *__restrict__ X, int O, const float *__restrict__ Y,
+                        int I, int ytr, float *__restrict__ part) {
+  const int64_t v0 = (int64_t)blockIdx.x * OUTER_CHUNK;
+  const int64_t v1 = min((int64_t)n, v0 + OUTER_CHUNK);
+  for (int e = threadIdx.x; e < O * I; e += blockDim.x) {
+    const int o = e / I, i = e % I;
+    float acc = 0.f;
+    for (int64_t v = v0; v < v1; ++v) {
+      float y = Y[v * I + i];
+      if (ytr >= 1) y = fmaxf(y, 0.f);
+      if (ytr == 2) y = bf16r(y);
+      acc += X[v * O + o] * y;
+    }
+    part[(size_t)blockIdx.x * O * I + e] = acc;
+  }
+}
+
+__global__ void k_outer_sum(const float *__restrict__ part, int chunks, int len,
+                            float *__restrict__ out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < len; e += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int c = 0; c < chunks; ++c) s += part[(size_t)c * len + e];
+    out[e] = s;
+  }
+}
+
+__global__ void k_adam(int np, float *__restrict__ p, const float *__restrict__ g,
+                       float *__restrict__ m, float *__restrict__ v, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    const float gi = isfinite(g[i]) ? g[i] : 0.f;
+    m[i] = b1 * m[i] + (1.f - b1) * gi;
+    v[i] = b2 * v[i] + (1.f - b2) * gi * gi;
+    p[i] -= lr * (m[i] / c1) / (sqrtf(v[i] / c2) + eps);
+  }
+}
+
+// d = z - e
+__global__ void k_sub(int64_t len, const float *a, const float *b, float *d) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    d[i] = a[i] - b[i];
+}
+__global__ void k_scale(int64_t len, const float *a, float s, float *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = s * a[i];
+}
+
+// rz = r.z and zq = z.q partials for the CG's K3 (grid = P2 blocks).
+__global__ void __launch_bounds__(RED_T) k_rz_zq(const SolveCtl *ctl, int64_t len,
+                                                 const float *__restrict__ r,
+                                                 const float *__restrict__ z,
+                                                 const float *__restrict__ q,
+                                                 double *__restrict__ part) {
+  __shared__ double sh[33];
+  if (ctl && ctl->status != ST_RUNNING) return;
+  double rz = 0, zq = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    rz += (double)r[i] * (double)z[i];
+    zq += (double)z[i] * (double)q[i];
+  }
+  const double t0 = block_sum(rz, sh);
+  const double t1 = block_sum(zq, sh);
+  if (threadIdx.x == 0) {
+    part[gridDim.x + blockIdx.x] = t0;
+    part[2 * gridDim.x + blockIdx.x] = t1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+static int graph_refresh(GraphH *G) {
+  Ctx *c = G->c;
+  Graph &g = G->g;
+  Scratch s(c);
+  SG_TRY(s.reserve(Scratch::bytes_for(g.n, 4) + 256));
+  float *dn = s.alloc<float>(g.n);
+  const int gr = grid_for(c, g.n, 256, 8);
+  if (g.vdt == SG_F64) {
+    k_diag_norm<double><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const double *)g.vals, dn);
+    k_edge_weights<double><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const double *)g.vals, dn, g.a);
+    k_diag_inv<double, float><<<gr, 256, 0, c->stream>>>(g.n, 3, g.rowptr, g.colidx, (const double *)g.vals, g.dinv, 1, c->d_err);
+  } else {
+    k_diag_norm<float><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const float *)g.vals, dn);
+    k_edge_weights<float><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const float *)g.vals, dn, g.a);
+    k_diag_inv<float, float><<<gr, 256, 0, c->stream>>>(g.n, 3, g.rowptr, g.colidx, (const float *)g.vals, g.dinv, 1, c->d_err);
+  }
+  SG_CHECK_LAUNCH();
+  return check_device_error(c, "mpnn graph");
+}
+
+static int graph_init(Ctx *c, const sg_matrix *A, GraphH *G) {
+  SG_REQUIRE(A && A->bs == 3 && A->n > 0 && A->vals && A->rowptr && A->colidx,
+             "mpnn: needs a 3x3-blocked matrix");
+  G->c = c;
+  Graph &g = G->g;
+  g.n = A->n;
+  g.nnzb = A->nnzb;
+  g.rowptr = A->rowptr;
+  g.colidx = A->colidx;
+  g.vals = A->vals;
+  g.vdt = A->dtype;
+  const size_t n = (size_t)A->n;
+  SG_TRY(galloc(G, (void **)&g.a, A->nnzb * 4));
+  SG_TRY(galloc(G, (void **)&g.dinv, n * 9 * 4));
+  SG_TRY(galloc(G, (void **)&g.s, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.m1, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.q2, n * K * 4));
+  SG_TRY(galloc(G, (void **)&g.m2, n * K * 4));
+  SG_TRY(galloc(G, (void **)&g.q3, n * K * 4));
+  SG_TRY(galloc(G, (void **)&g.m3, n * K * 4));
+  SG_TRY(galloc(G, (void **)&g.dres, 64));
+  static bool attr = false;
+  if (!attr) {
+    SG_CHECK_CUDA(cudaFuncSetAttribute(k_f3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
+    SG_CHECK_CUDA(cudaFuncSetAttribute(k_f4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
+    attr = true;
+  }
+  return graph_refresh(G);
+}
+
+static int ensure_train(GraphH *G) {
+  if (G->train_ready) return SG_OK;
+  Graph &g = G->g;
+  const size_t n = (size_t)g.n;
+  for (float **p : {&g.g1, &g.g2, &g.g3, &g.dg1, &g.dg2, &g.dg3, &g.dh1a, &g.dh2a})
+    SG_TRY(galloc(G, (void **)p, n * H * 4));
+  for (float **p : {&g.dm2, &g.dm3, &g.dq2, &g.dq3}) SG_TRY(galloc(G, (void **)p, n * K * 4));
+  g.gpart_chunks = (int)((n + OUTER_CHUNK - 1) / OUTER_CHUNK);
+  SG_TRY(galloc(G, (void **)&g.gpart, (size_t)g.gpart_chunks * H * H * 4));
+  SG_TRY(galloc(G, (void **)&g.ld, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.lq, n * 3 * 4));
+  G->train_ready = true;
+  return SG_OK;
+}
+
+// Forward on stream st; ctl may be null (standalone) or the solver control.
+static int forward(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, const float *prm,
+                   const float *r, float *z, bool train) {
+  Ctx *c = G->c;
+  Graph &g = G->g;
+  const int gv = grid_for(c, g.n, 256, 8);
+  k_f1<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.dinv, r, g.s, z);
+  SG_CHECK_LAUNCH();
+  k_f2<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.rowptr, g.colidx, g.a, prm, g.s, g.m1, g.q2,
+                           train ? g.g1 : nullptr);
+  SG_CHECK_LAUNCH();
+  const int64_t ntile = ((int64_t)g.n + 15) / 16;
+  int gt = (int)((ntile + TC_WARPS - 1) / TC_WARPS);
+  const int cap = c->num_sms * 4;
+  if (gt > cap) gt = cap;
+  k_f3<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
+                                                   g.m1, g.q2, g.m2, g.q3, train ? g.g2 : nullptr);
+  SG_CHECK_LAUNCH();
+  k_f4<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
+                                                   g.m1, g.m2, g.q3, g.m3, z, train ? g.g3 : nullptr);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+static int outer(GraphH *G, const float *X, int O, const float *Y, int I, int ytr, float *dst) {
+  Ctx *c = G->c;
+  Graph &g = G->g;
+  k_outer<<<g.gpart_chunks, 256, 0, c->stream>>>(g.n, X, O, Y, I, ytr, g.gpart);
+  SG_CHECK_LAUNCH();
+  k_outer_sum<<<(O * I + 255) / 256, 256, 0, c->stream>>>(g.gpart, g.gpart_chunks, O * I, dst);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+static int backward(GraphH *G, const float *prm, const float *dz, float *grad) {
+  Ctx *c = G->c;
+  Graph &g = G->g;
+  SG_TRY(ensure_train(G));
+  const int gw = grid_for(c, (int64_t)g.n * 32, 256, 8);
+  cudaStream_t st = c->stream;
+  k_b1<<<gw, 256, 0, st>>>(g.n, prm, dz, g.g3, g.dg3, g.dm3, g.dh2a);
+  SG_CHECK_LAUNCH();
+  k_bmid<<<gw, 256, 0, st>>>(g.n, g.rowptr, g.colidx, g.a, prm, O_P3, O_W2M, O_W2H, g.dm3, g.dh2a,
+                             g.g2, g.dq3, g.dg2, g.dm2, g.dh1a);
+  SG_CHECK_LAUNCH();
+  k_bmid<<<gw, 256, 0, st>>>(g.n, g.rowptr, g.colidx, g.a, prm, O_P2, 0, 0, g.dm2, g.dh1a, g.g1,
+                             g.dq2, g.dg1, nullptr, nullptr);
+  SG_CHECK_LAUNCH();
+  // weight gradients; h3 = relu(g3), h2 = relu(g2), h1 = relu(g1)
+  SG_TRY(outer(G, dz, 3, g.g3, H, 1, grad + O_WOUT));
+  SG_TRY(outer(G, g.dg3, H, g.g2, H, 2, grad + O_W3H));
+  SG_TRY(outer(G, g.dg3, H, g.m3, K, 0, grad + O_W3M));
+  SG_TRY(outer(G, g.dq3, K, g.g2, H, 1, grad + O_P3));
+  SG_TRY(outer(G, g.dg2, H, g.g1, H, 2, grad + O_W2H));
+  SG_TRY(outer(G, g.dg2, H, g.m2, K, 0, grad + O_W2M));
+  SG_TRY(outer(G, g.dq2, K, g.g1, H, 1, grad + O_P2));
+  SG_TRY(outer(G, g.dg1, H, g.s, 3, 0, grad + O_W1S));
+  SG_TRY(outer(G, g.dg1, H, g.m1, 3, 0, grad + O_W1M));
+  return SG_OK;
+}
+
+}  // namespace mpnn
+
+// ---------------------------------------------------------------------------
+// solver hooks (SG_PRECOND_LEARNED)
+// ---------------------------------------------------------------------------
+struct LearnedExt {
+  mpnn::GraphH *G = nullptr;
+  const float *prm = nullptr;
+};
+
+static int learned_prec(Solver *S, cudaStream_t st) {
+  LearnedExt *L = (LearnedExt *)S->ext;
+  SG_TRY(mpnn::forward(L->G, st, S->ctl, 1, L->prm, (const float *)S->r, (float *)S->z, false));
+  mpnn::k_rz_zq<<<S->P2, RED_T, 0, st>>>(S->ctl, S->len, (const float *)S->r, (const float *)S->z,
+                                         (const float *)S->q, S->part2);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+// Set-up / restart: z = M(r) with the network (or Jacobi after a fallback),
+// partials of r.z into part3 (P2 blocks).
+__global__ void __launch_bounds__(RED_T) k_rz_only(int64_t len, const float *r, const float *z,
+                                                   double *part) {
+  __shared__ double sh[33];
+  double rz = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    rz += (double)r[i] * (double)z[i];
+  const double t = block_sum(rz, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+static int learned_apply(Solver *S, cudaStream_t st) {
+  LearnedExt *L = (LearnedExt *)S->ext;
+  // the control block's fallback flag also governs restarts
+  SG_TRY(mpnn::forward(L->G, st, S->ctl, 0, L->prm, (const float *)S->r, (float *)S->z, false));
+  k_rz_only<<<S->P2, RED_T, 0, st>>>(S->len, (const float *)S->r, (const float *)S->z, S->part3);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+static void learned_free(Solver *S) {
+  LearnedExt *L = (LearnedExt *)S->ext;
+  if (!L) return;
+  if (L->G) {
+    for (void *p : L->G->allocs) cudaFree(p);
+    delete L->G;
+  }
+  delete L;
+  S->ext = nullptr;
+}
+
+static const float *g_pending_params = nullptr;
+static int learned_setup(Solver *S) {
+  LearnedExt *L = new LearnedExt();
+  S->ext = L;
+  S->ext_free = learned_free;
+  L->prm = g_pending_params;
+  L->G = new mpnn::GraphH();
+  SG_TRY(mpnn::graph_init(S->c, &S->A, L->G));
+  S->ext_prec = learned_prec;
+  S->ext_prec_apply = learned_apply;
+  S->flexible = 1;
+  return SG_OK;
+}
+
+int learned_refresh(Solver *S) {
+  LearnedExt *L = (LearnedExt *)S->ext;
+  return L ? mpnn::graph_refresh(L->G) : SG_OK;
+}
+
+int learned_solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, const float *params,
+                        Solver *S) {
+  g_pending_params = params;
+  int rc = solver_init(c, A, o, S, learned_setup);
+  g_pending_params = nullptr;
+  return rc;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" {
+
+int sg_mpnn_nparams(void) { return mpnn::NPARAM; }
+
+int sg_mpnn_graph_create(sg_ctx *h, const sg_matrix *A, sg_mpnn_graph **out) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && A && out, "sg_mpnn_graph_create: null argument");
+  mpnn::GraphH *G = new mpnn::GraphH();
+  int rc = mpnn::graph_init(c, A, G);
+  if (rc != SG_OK) {
+    for (void *p : G->allocs) cudaFree(p);
+    delete G;
+    return rc;
+  }
+  ctx_retain(c);
+  *out = reinterpret_cast<sg_mpnn_graph *>(G);
+  return SG_OK;
+}
+
+int sg_mpnn_graph_refresh(sg_mpnn_graph *hg) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  SG_REQUIRE(G, "sg_mpnn_graph_refresh: null graph");
+  return mpnn::graph_refresh(G);
+}
+
+int sg_mpnn_graph_destroy(sg_mpnn_graph *hg) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  if (!G) return SG_OK;
+  cudaStreamSynchronize(G->c->stream);
+  for (void *p : G->allocs) cudaFree(p);
+  Ctx *c = G->c;
+  delete G;
+  ctx_release(c);
+  return SG_OK;
+}
+
+int sg_mpnn_forward(sg_mpnn_graph *hg, const float *params, const float *r, float *z, int train) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  SG_REQUIRE(G && params && r && z, "sg_mpnn_forward: null argument");
+  if (train) SG_TRY(mpnn::ensure_train(G));
+  return mpnn::forward(G, G->c->stream, nullptr, 0, params, r, z, train != 0);
+}
+
+int sg_mpnn_backward(sg_mpnn_graph *hg, const float *params, const float *dz, float *grad) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  SG_REQUIRE(G && params && dz && grad, "sg_mpnn_backward: null argument");
+  SG_REQUIRE(G->train_ready, "sg_mpnn_backward: run sg_mpnn_forward with train=1 first");
+  return mpnn::backward(G, params, dz, grad);
+}
+
+int sg_mpnn_loss(sg_mpnn_graph *hg, const float *z, const float *e, double eAe, float *dz,
+                 double *h_loss) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  SG_REQUIRE(G && z && e && dz && h_loss && eAe > 0, "sg_mpnn_loss: bad argument");
+  SG_REQUIRE(G->g.vdt == SG_F32, "sg_mpnn_loss: the graph's matrix must be FP32");
+  SG_TRY(mpnn::ensure_train(G));
+  Ctx *c = G->c;
+  mpnn::Graph &g = G->g;
+  const int64_t len = (int64_t)g.n * 3;
+  const int gr = grid_for(c, len, 256, 8);
+  mpnn::k_sub<<<gr, 256, 0, c->stream>>>(len, z, e, g.ld);
+  SG_CHECK_LAUNCH();
+  SG_TRY(bspmv_launch(c, g.n, 3, g.rowptr, g.colidx, g.vdt, g.vals, SG_F32, g.ld, g.lq, 0, g.nnzb));
+  double dAd = 0;
+  SG_TRY(sg_dot(reinterpret_cast<sg_ctx *>(c), len, SG_F32, g.ld, g.lq, &dAd));
+  *h_loss = dAd / eAe;
+  mpnn::k_scale<<<gr, 256, 0, c->stream>>>(len, g.lq, (float)(2.0 / eAe), dz);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+int sg_mpnn_adam(sg_ctx *h, float *params, const float *grad, float *m, float *v, int step,
+                 float lr, float beta1, float beta2, float eps) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && params && grad && m && v && step >= 1, "sg_mpnn_adam: bad argument");
+  const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
+  mpnn::k_adam<<<(mpnn::NPARAM + 255) / 256, 256, 0, c->stream>>>(mpnn::NPARAM, params, grad, m, v,
+                                                                  lr, beta1, beta2, eps, c1, c2);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+}  // extern "C"

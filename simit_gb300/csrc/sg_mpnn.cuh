@@ -1,0 +1,64 @@
+// Message-passing preconditioner network: shared definitions.
+//
+//   s_v  = D_v^-1 r_v                      (3x3 block Jacobi of A)
+//   m1_v = sum_{u != v} a_vu s_u
+//   g1   = W1s s + W1m m1,      h1 = relu(g1)               (64)
+//   q2   = P2 h1                                           (8)
+//   m2_v = sum a_vu q2_u
+//   g2   = W2h bf16(h1) + W2m m2, h2 = relu(g2)            (64)
+//   q3   = P3 h2;  m3_v = sum a_vu q3_u
+//   g3   = W3h bf16(h2) + W3m m3, h3 = relu(g3)            (64)
+//   z    = s + Wout h3
+// a_vu = ||A_vu||_F / sqrt(||A_vv||_F ||A_uu||_F) on the matrix pattern
+// (0 on the diagonal).  W2h and W3h are bf16 tensor-core operands (mma.sync
+// m16n8k16, FP32 accumulate); everything else is FP32.  No biases, so the
+// map r -> z is positively homogeneous.  This network has no counterpart in
+// the reference; it is the learned preconditioner of the flexible PCG.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sg {
+namespace mpnn {
+
+constexpr int H = 64, K = 8;
+// flat FP32 parameter layout (row-major [out][in] each)
+constexpr int O_W1S = 0;                 // 64x3
+constexpr int O_W1M = O_W1S + H * 3;     // 64x3
+constexpr int O_P2 = O_W1M + H * 3;      // 8x64
+constexpr int O_W2H = O_P2 + K * H;      // 64x64
+constexpr int O_W2M = O_W2H + H * H;     // 64x8
+constexpr int O_P3 = O_W2M + H * K;      // 8x64
+constexpr int O_W3H = O_P3 + K * H;      // 64x64
+constexpr int O_W3M = O_W3H + H * H;     // 64x8
+constexpr int O_WOUT = O_W3M + H * K;    // 3x64
+constexpr int NPARAM = O_WOUT + 3 * H;   // 10816
+
+// Per-matrix graph data and workspace.
+struct Graph {
+  int32_t n = 0;
+  int64_t nnzb = 0;
+  const uint32_t *rowptr = nullptr, *colidx = nullptr;
+  const void *vals = nullptr;
+  int vdt = 0;
+  float *a = nullptr;      // [nnzb] edge weights
+  float *dinv = nullptr;   // [n*9] block-Jacobi inverse
+  // forward intermediates (always kept)
+  float *s = nullptr, *m1 = nullptr, *q2 = nullptr, *m2 = nullptr, *q3 = nullptr, *m3 = nullptr;
+  // training activations / backward temporaries (allocated on first use)
+  float *g1 = nullptr, *g2 = nullptr, *g3 = nullptr;
+  float *dg1 = nullptr, *dg2 = nullptr, *dg3 = nullptr, *dh1a = nullptr, *dh2a = nullptr;
+  float *dm2 = nullptr, *dm3 = nullptr, *dq2 = nullptr, *dq3 = nullptr;
+  float *gpart = nullptr;  // weight-gradient partials
+  int gpart_chunks = 0;
+  float *ld = nullptr, *lq = nullptr;  // loss temporaries
+  double *dres = nullptr;
+};
+
+__device__ __forceinline__ float bf16r(float x) {
+  return __bfloat162float(__float2bfloat16_rn(x));
+}
+
+}  // namespace mpnn
+}  // namespace sg

@@ -272,6 +272,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
   memset(res, 0, sizeof(*res));
   S->launches = 0;
   SG_CHECK_CUDA(cudaMemcpyAsync(S->xw, x, S->len * 8, cudaMemcpyDeviceToDevice, st));
+  SG_CHECK_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(SolveCtl), st));
   if (mixed) SG_CHECK_CUDA(cudaMemsetAsync(S->xlo, 0, S->len * sizeof(XT), st));
   // b'b
   dot_launch(c, S->len, b, b, S->part3, S->dres);
@@ -302,6 +303,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
   }
   const double delta = S->o.reliable_delta > 0 ? S->o.reliable_delta : 0.1;
   double rr_ref = rr;
+  int fallback = 0;
   SolveCtl *h = S->hctl;
   while (!status) {
     // (re)start a batch with the current state in parity slot 0
@@ -314,6 +316,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     h->rz[0] = h->rz[1] = rz;
     h->tol2 = tol2;
     h->upd2 = mixed ? delta * delta * rr_ref : 0.0;
+    h->fallback = fallback;
     if (iters >= S->o.maxiters) {
       status = SG_STATUS_MAXITER;
       break;
@@ -325,6 +328,17 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
       SG_CHECK_CUDA(cudaMemcpyAsync(h, S->ctl, sizeof(SolveCtl), cudaMemcpyDeviceToHost, st));
       SG_CHECK_CUDA(cudaStreamSynchronize(st));
       if (h->status != ST_RUNNING) break;
+      // a variable preconditioner that lets the residual grow 100x over the
+      // last reference point is abandoned for block Jacobi
+      if (S->flexible && !h->fallback && h->last_rr > 1e4 * rr_ref) {
+        SolveCtl one = *h;
+        one.fallback = 1;
+        one.status = ST_NEED_CHECK;
+        SG_CHECK_CUDA(cudaMemcpyAsync(S->ctl, &one, sizeof(SolveCtl), cudaMemcpyHostToDevice, st));
+        SG_CHECK_CUDA(cudaStreamSynchronize(st));
+        *h = one;
+        break;
+      }
     }
     // the slot K3 wrote last holds the larger iteration count
     const int cur = h->iter[1] > h->iter[0] ? 1 : 0;
@@ -359,11 +373,18 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
       break;
     }
     // residual replacement: continue from the true residual, same direction
+    // (a fresh direction after a switch to the fallback preconditioner)
+    const bool switched = h->fallback && !fallback;
+    if (switched) {
+      fallback = 1;
+      res->fallbacks++;
+    }
     const double rz_old = h->rz[cur ^ 1];
     double rz_new = 0;
     SG_TRY(restart_from_rhi<VT>(S, &rz_new));
     const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
-    k_p_update<VT><<<S->P2, RED_T, 0, st>>>(S->len, z, rz_new / rz_old, (VT *)S->p);
+    k_p_update<VT><<<S->P2, RED_T, 0, st>>>(S->len, z, switched ? 0.0 : rz_new / rz_old,
+                                            (VT *)S->p);
     S->launches += 1;
     SG_CHECK_LAUNCH();
     rz = rz_new;
@@ -403,14 +424,19 @@ int sg_solver_create(sg_ctx *h, const sg_matrix *A, const sg_solve_opts *o, sg_s
   SG_REQUIRE(A->dtype == SG_F32 || A->dtype == SG_F64, "sg_solver_create: dtype");
   SG_REQUIRE(o->precision == SG_SOLVE_F64 || o->precision == SG_SOLVE_MIXED,
              "sg_solver_create: precision %d", o->precision);
-  SG_REQUIRE(o->precond >= SG_PRECOND_NONE && o->precond <= SG_PRECOND_BLOCK_JACOBI,
-             "sg_solver_create: precond %d (learned preconditioners use sg_mpnn_solver_create)",
-             o->precond);
+  SG_REQUIRE(o->precond >= SG_PRECOND_NONE && o->precond <= SG_PRECOND_LEARNED,
+             "sg_solver_create: precond %d", o->precond);
+  SG_REQUIRE(o->precond != SG_PRECOND_LEARNED ||
+                 (o->learned_params && A->bs == 3 && o->precision == SG_SOLVE_MIXED),
+             "sg_solver_create: the learned preconditioner needs learned_params, bs = 3 and "
+             "SG_SOLVE_MIXED");
   SG_REQUIRE(o->precond != SG_PRECOND_BLOCK_JACOBI || A->bs == 3,
              "sg_solver_create: block Jacobi needs bs = 3");
   SG_REQUIRE(o->maxiters >= 0, "sg_solver_create: maxiters");
   Solver *S = new Solver();
-  int rc = solver_init(c, A, o, S, nullptr);
+  int rc = o->precond == SG_PRECOND_LEARNED
+               ? learned_solver_init(c, A, o, o->learned_params, S)
+               : solver_init(c, A, o, S, nullptr);
   if (rc != SG_OK) {
     solver_free(S);
     return rc;
@@ -495,6 +521,7 @@ int refresh_matrix(Solver *S) {
     SG_CHECK_LAUNCH();
     SG_TRY(check_device_error(c, "solver (diagonal)"));
   }
+  if (S->prec == PK_EXTERNAL && S->ext) SG_TRY(learned_refresh(S));
   return SG_OK;
 }
 

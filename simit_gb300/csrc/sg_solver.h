@@ -48,6 +48,9 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
 int refresh_matrix(Solver *S);
 int solver_solve(Solver *S, const double *b, double *x, sg_solve_result *res);
 void solver_free(Solver *S);
+int learned_refresh(Solver *S);
+int learned_solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, const float *params,
+                        Solver *S);
 void dot_launch(Ctx *c, int64_t len, const double *a, const double *b, double *part,
                 double *dres);
 

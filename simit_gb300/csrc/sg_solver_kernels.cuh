@@ -40,7 +40,8 @@ struct SolveCtl {
   int maxiters;
   int check_every;    // > 0: NEED_CHECK every check_every iterations
   int flexible;       // Polak-Ribiere beta
-  int pad[2];
+  int fallback;       // learned preconditioner replaced by block Jacobi
+  int pad;
   double rz[2];       // r.z of the current direction, parity slots
   double tol2;        // convergence threshold on r.r (iterated)
   double upd2;        // NEED_CHECK when r.r < upd2 (reliable update); 0 = off
@@ -218,7 +219,9 @@ __global__ void __launch_bounds__(RED_T) k_cg_direction(SolveCtl *ctl, int par, 
   const double rzold = ctl->rz[par];
   const int it = ctl->iter[par] + 1;
   int st = ST_RUNNING;
-  if (!isfinite(rr) || !isfinite(rznew)) st = ST_NAN;
+  const bool lost = ctl->flexible && !ctl->fallback && !(rznew > 0.0);
+  if (lost) st = ST_NEED_CHECK;  // z is no descent direction: fall back
+  else if (!isfinite(rr) || !isfinite(rznew)) st = ST_NAN;
   else if (rr <= ctl->tol2) st = ST_NEED_CHECK;
   else if (ctl->upd2 > 0.0 && rr < ctl->upd2) st = ST_NEED_CHECK;
   else if (ctl->check_every > 0 && it % ctl->check_every == 0) st = ST_NEED_CHECK;
@@ -227,6 +230,7 @@ __global__ void __launch_bounds__(RED_T) k_cg_direction(SolveCtl *ctl, int par, 
     ctl->iter[par ^ 1] = it;
     ctl->rz[par ^ 1] = rznew;
     ctl->last_rr = rr;
+    if (lost) ctl->fallback = 1;
     if (st != ST_RUNNING) ctl->status = st;
   }
   if (st != ST_RUNNING) return;

@@ -11,6 +11,8 @@ struct PatternStats {
 int default_lanes(int32_t n, int64_t nnzb, int32_t bs);
 int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out);
 int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps);
+int bspmv_launch(Ctx *c, int32_t n, int32_t bs, const uint32_t *rp, const uint32_t *ci, int vdt,
+                 const void *v, int xdt, const void *x, void *y, int g, int64_t nnzb_hint);
 // TMA-staged 3x3 SpMV: grid/shared-memory for variant `var` (0 = default;
 // see kTmaVariants in sg_spmv.cu); launch.  dot = 1 also writes per-CTA
 // partials of x.y (CG K1) and honours ctl.

@@ -1,0 +1,242 @@
+"""Learned preconditioner: data, training and evaluation on the C ABI.
+
+The network (3 message-passing layers, hidden 64, bf16 tensor-core weights,
+FP32 accumulation) is defined in simit_gb300/csrc/sg_mpnn.cuh; its forward,
+backward, A-norm loss and Adam step are CUDA kernels behind sg_mpnn_*.
+
+Training pairs come from the solver itself: on seeded heterogeneous-elasticity
+meshes of 16^3 .. 48^3 cells, for random right-hand sides b, the
+mixed-precision block-Jacobi PCG is stopped after k iterations (k in KS); the
+pair is (r_k = b - A x_k, e_k = x* - x_k) with x* the converged solution, so
+e_k = A^-1 r_k.  The loss is the A-norm error (z - e)'A(z - e) / e'Ae of the
+network's output z = M(r) — zero for the exact inverse, one for z = 0.
+"""
+import ctypes
+import os
+
+import numpy as np
+import torch
+
+from . import _lib, meshgen, problems
+from ._lib import call
+from .runtime import Solver, bspmv, dtype_code, ptr, solve_opts
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WEIGHTS = os.path.join(HERE, "data", "mpnn_elasticity.npy")
+KS = (1, 3, 8, 16, 32, 64, 128, 256, 512, 1024)
+H, K = 64, 8
+SHAPES = [("W1s", (H, 3)), ("W1m", (H, 3)), ("P2", (K, H)), ("W2h", (H, H)), ("W2m", (H, K)),
+          ("P3", (K, H)), ("W3h", (H, H)), ("W3m", (H, K)), ("Wout", (3, H))]
+
+
+def nparams():
+    return _lib.load().sg_mpnn_nparams()
+
+
+def init_params(seed=0, out_scale=0.0):
+    """He-style initial weights; Wout scaled by out_scale (0 = block Jacobi)."""
+    rng = meshgen.rng(seed)
+    parts = []
+    for name, (a, b) in SHAPES:
+        w = rng.normal(0, np.sqrt(2.0 / b), size=(a, b))
+        if name == "Wout":
+            w *= out_scale
+        parts.append(w.reshape(-1))
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.size == nparams()
+    return p
+
+
+def load_weights(path=WEIGHTS):
+    return np.load(path).astype(np.float32)
+
+
+class Graph:
+    """sg_mpnn_graph of a 3x3-blocked matrix."""
+
+    def __init__(self, ctx, mesh, A):
+        self.ctx = ctx
+        self.A = A
+        self.m = _lib.Matrix(mesh.n, 3, mesh.nnzb, mesh.pattern.rowptr.data_ptr(),
+                             mesh.pattern.colidx.data_ptr(), dtype_code(A), A.data_ptr())
+        h = ctypes.c_void_p()
+        call("sg_mpnn_graph_create", ctx.h, ctypes.byref(self.m), ctypes.byref(h))
+        self.h = h
+        self.n = mesh.n
+
+    def forward(self, params, r, z, train=False):
+        call("sg_mpnn_forward", self.h, ptr(params), ptr(r), ptr(z), int(train))
+
+    def backward(self, params, dz, grad):
+        call("sg_mpnn_backward", self.h, ptr(params), ptr(dz), ptr(grad))
+
+    def loss(self, z, e, eAe, dz):
+        out = ctypes.c_double()
+        call("sg_mpnn_loss", self.h, ptr(z), ptr(e), float(eAe), ptr(dz), ctypes.byref(out))
+        return out.value
+
+    def close(self):
+        if self.h:
+            _lib.load().sg_mpnn_graph_destroy(self.h)
+            self.h = None
+
+
+def make_pairs(ctx, ncell, seed, n_rhs, ks=KS):
+    """Residual/correction pairs of one seeded mesh (FP32 device tensors)."""
+    host = problems.hetero_mesh(ncell, seed=seed)
+    prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
+                                     precond=_lib.PRECOND_BLOCK_JACOBI, tol=1e-11)
+    m = prob.mesh
+    d = ctx.device
+    g = meshgen.rng(seed + 1000)
+    cons = torch.tensor(np.repeat(host["c"], 3) > 0, device=d)
+    pairs = []
+    with ctx.stream():
+        for _ in range(n_rhs):
+            b = torch.tensor(g.normal(size=m.n * 3), device=d)
+            b[cons] = 0.0
+            xs = torch.zeros_like(b)
+            prob.solver.solve(b, xs)
+            for k in ks:
+                S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, m.nnzb,
+                           solve_opts(precision=_lib.SOLVE_MIXED,
+                                      precond=_lib.PRECOND_BLOCK_JACOBI, tol=1e-14,
+                                      maxiters=k, verify=0))
+                xk = torch.zeros_like(b)
+                S.solve(b, xk)
+                S.close()
+                e = (xs - xk).float()
+                Ax = bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A,
+                           xk.float().contiguous())
+                r = (b.float() - Ax).contiguous()
+                Ae = bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, e)
+                eAe = float((e.double() * Ae.double()).sum())
+                if eAe > 0:
+                    pairs.append((r, e, eAe))
+    return prob, pairs
+
+
+class Trainer:
+    def __init__(self, ctx, params=None, lr=1e-3, seed=0):
+        self.ctx = ctx
+        d = ctx.device
+        p = init_params(seed) if params is None else np.asarray(params, np.float32)
+        with ctx.stream():
+            self.params = torch.tensor(p, device=d)
+            self.grad = torch.zeros_like(self.params)
+            self.m = torch.zeros_like(self.params)
+            self.v = torch.zeros_like(self.params)
+        self.step_n = 0
+        self.lr = lr
+
+    def step(self, graph, r, e, eAe):
+        with self.ctx.stream():
+            z = torch.empty_like(r)
+            dz = torch.empty_like(r)
+        graph.forward(self.params, r, z, train=True)
+        L = graph.loss(z, e, eAe, dz)
+        graph.backward(self.params, dz, self.grad)
+        self.step_n += 1
+        call("sg_mpnn_adam", self.ctx.h, ptr(self.params), ptr(self.grad), ptr(self.m), ptr(self.v),
+             self.step_n, self.lr, 0.9, 0.999, 1e-8)
+        return L
+
+    def eval_loss(self, graph, pairs):
+        tot = 0.0
+        for r, e, eAe in pairs:
+            with self.ctx.stream():
+                z = torch.empty_like(r)
+                dz = torch.empty_like(r)
+            graph.forward(self.params, r, z, train=True)
+            tot += graph.loss(z, e, eAe, dz)
+        return tot / max(1, len(pairs))
+
+
+def train(ctx, sizes=(16, 24, 32, 40, 48), n_pairs=2000, epochs=6, lr=1e-3, seed=0,
+          log=print):
+    """Train on n_pairs pairs spread over the meshes; returns (params, history)."""
+    per_mesh = max(1, n_pairs // (len(sizes) * len(KS)))
+    data = []
+    for i, nc in enumerate(sizes):
+        prob, pairs = make_pairs(ctx, nc, seed=100 + i, n_rhs=per_mesh)
+        data.append((prob, Graph(ctx, prob.mesh, prob.A), pairs))
+        log("mesh %d^3: %d pairs" % (nc, len(pairs)))
+    tr = Trainer(ctx, lr=lr, seed=seed)
+    hist = []
+    L0 = np.mean([tr.eval_loss(g, p) for _, g, p in data])
+    hist.append(L0)
+    log("epoch 0 loss %.5f" % L0)
+    rng = meshgen.rng(seed + 7)
+    for ep in range(epochs):
+        order = [(i, j) for i, (_, _, p) in enumerate(data) for j in range(len(p))]
+        rng.shuffle(order)
+        for i, j in order:
+            prob, g, pairs = data[i]
+            r, e, eAe = pairs[j]
+            tr.step(g, r, e, eAe)
+        L = np.mean([tr.eval_loss(g, p) for _, g, p in data])
+        hist.append(L)
+        log("epoch %d loss %.5f" % (ep + 1, L))
+    params = tr.params.detach().cpu().numpy()
+    for prob, g, _ in data:
+        g.close()
+        prob.close()
+    return params, hist
+
+
+def compare(ctx, params, ncell, seed=999, tol=1e-8):
+    """Flexible PCG with the network vs block-Jacobi PCG on a held-out mesh."""
+    host = problems.hetero_mesh(ncell, seed=seed)
+    out = {}
+    d = ctx.device
+    with ctx.stream():
+        prm = torch.tensor(np.asarray(params, np.float32), device=d)
+    for name, pc in (("block_jacobi", _lib.PRECOND_BLOCK_JACOBI),
+                     ("learned", _lib.PRECOND_LEARNED)):
+        prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
+                                         precond=_lib.PRECOND_BLOCK_JACOBI)
+        m = prob.mesh
+        S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, m.nnzb,
+                   solve_opts(precision=_lib.SOLVE_MIXED, precond=pc, tol=tol, maxiters=100000,
+                              learned_params=prm if pc == _lib.PRECOND_LEARNED else None),
+                   learned_params_keep=prm)
+        x = torch.zeros_like(prob.b)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ctx.torch_stream)
+        r = S.solve(prob.b, x)
+        e1.record(ctx.torch_stream)
+        e1.synchronize()
+        out[name] = {"iters": r.iters, "status": r.status, "fallbacks": r.fallbacks,
+                     "relres": (r.true_normr2 / r.bnorm2) ** 0.5, "ms": e0.elapsed_time(e1)}
+        S.close()
+        prob.close()
+    return out
+
+
+def main():
+    import argparse
+    import json
+    import time
+    from .runtime import Context
+    ap = argparse.ArgumentParser(description="train the learned preconditioner")
+    ap.add_argument("--pairs", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=6)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--eval-size", type=int, default=32)
+    a = ap.parse_args()
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    t0 = time.time()
+    params, hist = train(ctx, n_pairs=a.pairs, epochs=a.epochs, lr=a.lr)
+    os.makedirs(os.path.dirname(a.out), exist_ok=True)
+    np.save(a.out, params)
+    res = compare(ctx, params, a.eval_size)
+    print(json.dumps({"train_seconds": time.time() - t0, "loss_history": hist,
+                      "eval": res, "weights": a.out}))
+
+
+if __name__ == "__main__":
+    main()

@@ -223,20 +223,22 @@ def assemble_heat(mesh, B, W, kappa, dt, T0, dtype=torch.float64, exact=True):
 
 def solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_RELATIVE,
                tol=1e-8, maxiters=10000, verify=1, check_every=0, reliable_delta=0.1, lanes=0,
-               batch=32):
+               batch=32, learned_params=None):
+    lp = learned_params.data_ptr() if learned_params is not None else None
     return _lib.SolveOpts(precision, precond, stop, tol, maxiters, verify, check_every,
-                          reliable_delta, lanes, batch)
+                          reliable_delta, lanes, batch, lp)
 
 
 class Solver:
     """sg_solver: set up once for a matrix, solve many right-hand sides."""
 
-    def __init__(self, ctx, n, bs, rowptr, colidx, vals, nnzb, opts):
+    def __init__(self, ctx, n, bs, rowptr, colidx, vals, nnzb, opts, learned_params_keep=None):
         self.ctx = ctx
         self._keep = (rowptr, colidx, vals)
         self.A = _lib.Matrix(n, bs, nnzb, rowptr.data_ptr(), colidx.data_ptr(),
                              dtype_code(vals), vals.data_ptr())
         self.opts = opts
+        self._keep_params = learned_params_keep
         h = P()
         call("sg_solver_create", ctx.h, ctypes.byref(self.A), ctypes.byref(opts), ctypes.byref(h))
         self.h = h

@@ -1,0 +1,97 @@
+"""GPU checks of the learned preconditioner: forward and backward against the
+numpy oracle (oracle/mpnn_oracle.py), training, and its use in flexible PCG."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from simit_gb300 import _lib, problems
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_ctx):
+    return gpu_ctx
+
+
+def _small(ctx, ncell=4, seed=3):
+    host = problems.hetero_mesh(ncell, seed=seed)
+    return problems.HeteroElasticity(ctx, host, dtype=torch.float32,
+                                     precond=_lib.PRECOND_BLOCK_JACOBI)
+
+
+def test_forward_backward_match_oracle(ctx):
+    from oracle import mpnn_oracle as mo
+    from simit_gb300 import learned
+    prob = _small(ctx, 4)
+    m = prob.mesh
+    rp, ci = m.pattern.host()
+    vals = prob.A.cpu().numpy()
+    g = learned.Graph(ctx, m, prob.A)
+    params = learned.init_params(seed=5, out_scale=1.0)
+    rng = np.random.Generator(np.random.Philox(11))
+    r = rng.normal(size=m.n * 3).astype(np.float32)
+    dz = rng.normal(size=m.n * 3).astype(np.float32)
+    d = ctx.device
+    pt = torch.tensor(params, device=d)
+    rt = torch.tensor(r, device=d)
+    zt = torch.empty_like(rt)
+    g.forward(pt, rt, zt, train=True)
+    grad = torch.zeros_like(pt)
+    g.backward(pt, torch.tensor(dz, device=d), grad)
+    z_ref, cache = mo.forward(params, m.n, rp, ci, vals, r)
+    gref = mo.backward(cache, dz)
+    z = zt.cpu().numpy()
+    s = cache["s"].reshape(-1)
+    # FP32 accumulation vs FP64 (bf16 operands rounded identically up to
+    # ties flipped by the accumulation order)
+    assert np.linalg.norm(z - z_ref) <= 1e-3 * np.linalg.norm(z_ref - s) + 1e-6 * np.linalg.norm(s)
+    gg = grad.cpu().numpy()
+    o = 0
+    for name, (a, b) in mo.SHAPES:
+        seg = slice(o, o + a * b)
+        o += a * b
+        err = np.linalg.norm(gg[seg] - gref[seg])
+        assert err <= 2e-3 * np.linalg.norm(gref[seg]) + 1e-6, (name, err, np.linalg.norm(gref[seg]))
+    g.close()
+    prob.close()
+
+
+def test_training_reduces_loss(ctx):
+    from simit_gb300 import learned
+    prob, pairs = learned.make_pairs(ctx, 6, seed=21, n_rhs=2, ks=(4, 16, 64))
+    g = learned.Graph(ctx, prob.mesh, prob.A)
+    tr = learned.Trainer(ctx, lr=3e-3, seed=1)
+    L0 = tr.eval_loss(g, pairs)
+    for _ in range(40):
+        for r, e, eAe in pairs:
+            tr.step(g, r, e, eAe)
+    L1 = tr.eval_loss(g, pairs)
+    assert L1 < 0.95 * L0, (L0, L1)
+    g.close()
+    prob.close()
+
+
+def test_learned_fpcg_converges_and_falls_back(ctx):
+    from simit_gb300 import learned
+    res = learned.compare(ctx, learned.init_params(seed=2, out_scale=0.01), 8)
+    assert res["learned"]["status"] == 1 and res["learned"]["relres"] <= 1e-8
+    bad = learned.init_params(seed=2, out_scale=1.0)
+    bad[-1] = np.nan  # a NaN output weight poisons z: the solver falls back
+    res = learned.compare(ctx, bad, 8)
+    assert res["learned"]["fallbacks"] >= 1
+    assert res["learned"]["status"] == 1 and res["learned"]["relres"] <= 1e-8
+
+
+def test_trained_network_gain(ctx):
+    """The committed trained weights against block-Jacobi PCG (no network) on
+    a held-out mesh: fewer iterations to the same FP64 residual."""
+    from simit_gb300 import learned
+    if not os.path.exists(learned.WEIGHTS):
+        pytest.skip("no trained weights committed")
+    res = learned.compare(ctx, learned.load_weights(), 24, seed=777)
+    assert res["learned"]["status"] == 1 and res["block_jacobi"]["status"] == 1
+    print("learned vs block-Jacobi:", res)
+    assert res["learned"]["iters"] < res["block_jacobi"]["iters"]
