@@ -1,6 +1,7 @@
 // CG / PCG solver runtime: workspace, graph-captured iteration batches and the
 // host decisions taken only at rare check points (true residual, reliable
 // update, convergence).
+#include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -296,14 +297,24 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
   if (!(rr > tol2)) status = SG_STATUS_CONVERGED;
   if (!std::isfinite(rr)) status = SG_STATUS_NAN;
   double rz = 0;
+  int fallback = 0;
   if (!status) SG_TRY(restart_from_rhi<VT>(S, &rz));
+  if (!status && S->flexible && !(rz > 0.0)) {
+    // the variable preconditioner gives no descent direction from the start:
+    // switch to its fallback (block Jacobi) before the first iteration
+    fallback = 1;
+    res->fallbacks++;
+    const int one = 1;
+    SG_CHECK_CUDA(cudaMemcpyAsync((char *)S->ctl + offsetof(SolveCtl, fallback), &one,
+                                  sizeof(int), cudaMemcpyHostToDevice, st));
+    SG_TRY(restart_from_rhi<VT>(S, &rz));
+  }
   if (!status) {
     const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
     SG_CHECK_CUDA(cudaMemcpyAsync(S->p, z, S->len * sizeof(VT), cudaMemcpyDeviceToDevice, st));
   }
   const double delta = S->o.reliable_delta > 0 ? S->o.reliable_delta : 0.1;
   double rr_ref = rr;
-  int fallback = 0;
   SolveCtl *h = S->hctl;
   while (!status) {
     // (re)start a batch with the current state in parity slot 0

@@ -111,7 +111,10 @@ def make_pairs(ctx, ncell, seed, n_rhs, ks=KS):
                 r = (b.float() - Ax).contiguous()
                 Ae = bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, e)
                 eAe = float((e.double() * Ae.double()).sum())
-                if eAe > 0:
+                # keep pairs whose residual is well above the converged level
+                # (past convergence e is round-off and e'Ae meaningless)
+                rel = float(r.double().norm() / b.norm())
+                if eAe > 0 and rel > 1e-6:
                     pairs.append((r, e, eAe))
     return prob, pairs
 
