@@ -283,6 +283,27 @@ int sg_solve(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
              const double *b, double *x, sg_solve_result *res);
 
 /* ---------------------------------------------------------------------
+ * Batched PCG: nsys independent 3x3-blocked systems concatenated into one
+ * block-diagonal FP32 matrix (system s = block rows [sys_ptr[s],
+ * sys_ptr[s+1]), columns inside that range only), solved in ONE persistent
+ * launch: each CTA takes whole systems from a queue in the given order
+ * (`order`, largest first for load balance) and runs mixed-precision
+ * block-Jacobi PCG on them with CTA-local barriers only.  Each system stops
+ * at ||b_s - A_s x_s|| <= tol ||b_s|| (confirmed in FP64) or maxiters.
+ * b, x FP32 [n*3] device (x: guess in, solution out); iters, status
+ * (SG_STATUS_*), relres per system (device).  config selects threads per
+ * CTA and lanes per row (0 .. sg_batched_configs()-1; the autotuner in the
+ * host runtime picks one).  Asynchronous; capturable after a first call has
+ * sized the context scratch.  Replaces running one Simit program per mesh
+ * (no batched counterpart in the reference).
+ * ------------------------------------------------------------------- */
+int sg_batched_pcg(sg_ctx *ctx, int32_t nsys, const int32_t *sys_ptr, const int32_t *order,
+                   const sg_matrix *A, const float *b, float *x, double tol,
+                   int32_t maxiters, int32_t config, int32_t *iters, int32_t *status,
+                   double *relres);
+int sg_batched_configs(void);
+
+/* ---------------------------------------------------------------------
  * Learned preconditioner: a 3-layer message-passing network (hidden 64,
  * messages of 8, no biases) over the matrix graph, z = D^-1 r + Wout h3,
  * where D is the 3x3 block diagonal; the 64x64 layers run on the tensor

@@ -85,6 +85,8 @@ SIGNATURES = {
     "sg_solver_destroy": (_CI, [P]),
     "sg_solver_refresh": (_CI, [P]),
     "sg_dot_noalloc": (_CI, [P, I64, _CI, P, P, P]),
+    "sg_batched_pcg": (_CI, [P, I32, P, P, ctypes.POINTER(Matrix), P, P, D, I32, I32, P, P, P]),
+    "sg_batched_configs": (_CI, []),
     "sg_mpnn_nparams": (_CI, []),
     "sg_mpnn_graph_create": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(P)]),
     "sg_mpnn_graph_refresh": (_CI, [P]),

@@ -114,3 +114,120 @@ class HeteroElasticity:
 
     def close(self):
         self.solver.close()
+
+
+# ---------------------------------------------------------------------------
+# Batched cloth (apps/cloth form, implicit springs as apps/springs/isprings.sim)
+# ---------------------------------------------------------------------------
+CLOTH = {"k_stretch": 5e3, "k_bend": 50.0, "mass": 1e-3, "dt": 1.0 / 240.0, "viscous": 0.0,
+         "grav": (0.0, 0.0, -9.81), "tol": 1e-6}
+
+
+def cloth_batch(nsheets=256, lo=32, hi=256, seed=5, jitter=0.2):
+    """nsheets triangulated square sheets with side lengths uniform in
+    [lo, hi] vertices, concatenated (vertex and spring offsets) into one
+    edge set.  Positions: unit sheet, z jittered by +/- jitter * spacing
+    (seeded), rest lengths of the flat sheet, v = 0, two corners pinned."""
+    g = meshgen.rng(seed)
+    sides = g.integers(lo, hi + 1, size=nsheets)
+    xs, eps, ks, l0s, fixed, sys_ptr = [], [], [], [], [], [0]
+    off = 0
+    for i, s in enumerate(sides):
+        sh = meshgen.cloth_sheet(int(s))
+        x = sh["x"].reshape(-1, 3).copy()
+        spacing = 1.0 / (s - 1)
+        x[:, 2] += meshgen.rng(seed * 7919 + i).uniform(-jitter, jitter, len(x)) * spacing
+        xs.append(x.reshape(-1))
+        eps.append(sh["ep"] + off)
+        ks.append(np.where(sh["is_bend"] > 0, CLOTH["k_bend"], CLOTH["k_stretch"]))
+        l0s.append(sh["l0"])
+        fixed.append(sh["fixed"])
+        off += sh["n"]
+        sys_ptr.append(off)
+    return {"n": off, "x": np.concatenate(xs), "ep": np.concatenate(eps).astype(np.int32),
+            "k": np.concatenate(ks), "l0": np.concatenate(l0s), "fixed": np.concatenate(fixed),
+            "sys_ptr": np.array(sys_ptr, np.int32), "sides": sides}
+
+
+class ClothBatch:
+    """Device-resident cloth batch: assembly of all sheets in one launch and
+    the batched PCG (one persistent launch), optionally captured as one CUDA
+    graph."""
+
+    def __init__(self, ctx, host, config=None):
+        from .runtime import assemble_springs
+        self.ctx, self.host = ctx, host
+        self.mesh = Mesh(ctx, host["n"], host["ep"], 2)
+        d = ctx.device
+        n = host["n"]
+        sp = host["sys_ptr"]
+        sizes = np.diff(sp)
+        order = np.argsort(-sizes, kind="stable").astype(np.int32)
+        with ctx.stream():
+            self.x = torch.tensor(host["x"], dtype=torch.float32, device=d)
+            self.v = torch.zeros(n * 3, dtype=torch.float32, device=d)
+            self.m = torch.full((n,), CLOTH["mass"], dtype=torch.float32, device=d)
+            self.fixed = torch.tensor(host["fixed"], dtype=torch.uint8, device=d)
+            self.k = torch.tensor(host["k"], dtype=torch.float32, device=d)
+            self.l0 = torch.tensor(host["l0"], dtype=torch.float32, device=d)
+            self.sys_ptr = torch.tensor(sp, device=d)
+            self.order = torch.tensor(order, device=d)
+            self.iters = torch.zeros(len(sizes), dtype=torch.int32, device=d)
+            self.status = torch.zeros(len(sizes), dtype=torch.int32, device=d)
+            self.relres = torch.zeros(len(sizes), dtype=torch.float64, device=d)
+            self.vout = torch.zeros(n * 3, dtype=torch.float32, device=d)
+        self.nsys = len(sizes)
+        self.A, self.f = assemble_springs(self.mesh, self.x, self.v, self.m, self.fixed, self.k,
+                                          self.l0, CLOTH["dt"], CLOTH["viscous"], CLOTH["grav"],
+                                          form=0, dtype=torch.float32, exact=False)
+        self.Am = _lib.Matrix(n, 3, self.mesh.nnzb, self.mesh.pattern.rowptr.data_ptr(),
+                              self.mesh.pattern.colidx.data_ptr(), _lib.F32, self.A.data_ptr())
+        self.config = config if config is not None else self.autotune()
+        self.graph = None
+
+    def step(self, config=None, maxiters=10000):
+        """Assemble every sheet and solve every system (the batched path)."""
+        import ctypes
+        from .runtime import call, ptr, dtype_code
+        m = self.mesh
+        call("sg_assemble_springs", self.ctx.h, m.ref(), dtype_code(self.A), 0, ptr(self.x),
+             ptr(self.v), ptr(self.m), ptr(self.fixed), ptr(self.k), ptr(self.l0), CLOTH["dt"],
+             CLOTH["viscous"], (ctypes.c_double * 3)(*CLOTH["grav"]), ptr(self.A), ptr(self.f), 0)
+        with self.ctx.stream():
+            self.vout.copy_(self.v)
+        call("sg_batched_pcg", self.ctx.h, self.nsys, ptr(self.sys_ptr), ptr(self.order),
+             ctypes.byref(self.Am), ptr(self.f), ptr(self.vout), CLOTH["tol"], maxiters,
+             self.config if config is None else config, ptr(self.iters), ptr(self.status),
+             ptr(self.relres))
+
+    def autotune(self):
+        """Time every batched-PCG configuration once; keep the fastest."""
+        best, best_ms = 0, None
+        st = self.ctx.torch_stream
+        self.config = 0
+        self.step(config=0)  # sizes the scratch arena
+        for cfg in range(_lib.load().sg_batched_configs()):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            self.step(config=cfg)
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            if best_ms is None or ms < best_ms:
+                best, best_ms = cfg, ms
+        self.tuned_ms = best_ms
+        return best
+
+    def capture(self):
+        """One CUDA graph holding the assembly and the batched solve."""
+        self.step()  # warm (arena sized, attributes set)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=self.ctx.torch_stream):
+            self.step()
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
