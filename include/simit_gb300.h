@@ -181,6 +181,11 @@ int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
              const uint32_t *colidx, int val_dtype, const void *vals,
              int vec_dtype, const void *x, void *y, int32_t g);
 
+/* y = y + alpha * x (two separately rounded operations, as the lowered
+ * `points.x = points.x + h * points.v` of apps/springs/isprings.sim:94 and
+ * `verts.x = h * x + verts.x` of femTet.sim); vec_dtype for x and y. */
+int sg_axpy(sg_ctx *ctx, int64_t len, int vec_dtype, double alpha, const void *x, void *y);
+
 /* Dot product of two blocked vectors with an FP64 deterministic two-level
  * reduction; synchronises. */
 int sg_dot(sg_ctx *ctx, int64_t len, int vec_dtype, const void *a,

@@ -193,6 +193,18 @@ __global__ void sum_partials(const double *part, int np, double *out) {
   }
 }
 
+template <typename T>
+__global__ void k_axpy(int64_t len, T alpha, const T *__restrict__ x, T *__restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    // separate rounding of the product and the sum (no contraction)
+    if (sizeof(T) == 8)
+      y[i] = (T)__dadd_rn((double)y[i], __dmul_rn((double)alpha, (double)x[i]));
+    else
+      y[i] = (T)__fadd_rn((float)y[i], __fmul_rn((float)alpha, (float)x[i]));
+  }
+}
+
 void ctx_release(Ctx *c) {
   if (--c->refs > 0) return;
   cudaStreamSynchronize(c->stream);
@@ -249,6 +261,20 @@ void *sg_ctx_stream(sg_ctx *h) { return h ? (void *)as_ctx(h)->stream : nullptr;
 const char *sg_last_error(void) { return g_last_error.c_str(); }
 
 const char *sg_version(void) { return "simit_gb300 0.1 (sm_103a)"; }
+
+int sg_axpy(sg_ctx *h, int64_t len, int vdt, double alpha, const void *x, void *y) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && (len == 0 || (x && y)), "sg_axpy: null argument");
+  SG_REQUIRE(len >= 0 && (vdt == SG_F32 || vdt == SG_F64), "sg_axpy: bad len/dtype");
+  if (len == 0) return SG_OK;
+  const int G = grid_for(c, len, 256, 8);
+  if (vdt == SG_F64)
+    k_axpy<double><<<G, 256, 0, c->stream>>>(len, alpha, (const double *)x, (double *)y);
+  else
+    k_axpy<float><<<G, 256, 0, c->stream>>>(len, (float)alpha, (const float *)x, (float *)y);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
 
 int sg_dot(sg_ctx *h, int64_t len, int vdt, const void *a, const void *b,
            double *h_out) {
