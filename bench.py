@@ -42,7 +42,127 @@ def parse():
     ap.add_argument("--cloth", action="store_true",
                     help="batched cloth: 256 uneven sheets in one graph launch vs one at a time")
     ap.add_argument("--sheets", type=int, default=256)
+    ap.add_argument("--neo", action="store_true",
+                    help="neo-Hookean Newton step (64^3): FP64 vs FP32-bulk mixed precision")
+    ap.add_argument("--heat", action="store_true",
+                    help="P1 heat (128^3): 1000 SpMVs FP32 vs FP64, CG FP64 vs mixed")
     return ap.parse_args()
+
+
+def _ev_ms(st, fn, reps=1):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        out = fn()
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps, out
+
+
+def run_neo(args):
+    """femTet.sim form: one implicit Newton step (A = M + h^2 K_neo(x), b =
+    compute_force, h = 0.01) on the 64^3 five-tet lattice, E = 1e5, nu = 0.4,
+    rho = 1e3, displacement +/-1e-3, bottom face fixed; CG to 1e-8.  FP64
+    assembly + FP64 Jacobi-CG against FP32 assembly + mixed block-Jacobi PCG;
+    the mixed solution's relative error against the FP64 one."""
+    import numpy as np
+    import torch
+    from simit_gb300 import _lib, meshgen
+    from simit_gb300.runtime import (Context, Mesh, Solver, assemble_tet_force,
+                                     assemble_tet_stiffness, solve_opts, tet_precompute)
+    size = args.size if args.size != 128 else 64
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    st = ctx.torch_stream
+    mg = meshgen.tet_grid(size, disp=1e-3, seed=2)
+    nT = len(mg["tets"]) // 4
+    E, nu = 1e5, 0.4
+    mu = np.full(nT, E / (2 * (1 + nu)))
+    lam = np.full(nT, E * nu / ((1 + nu) * (1 - 2 * nu)))
+    c = (mg["X0"].reshape(-1, 3)[:, 2] == 0).astype(np.int32)
+    mesh = Mesh(ctx, mg["n"], mg["tets"], 4)
+    d = ctx.device
+    out = {"workload": "neo-Hookean Newton step %d^3 (%d tets, %d DOF)" % (size, nT, mg["n"] * 3)}
+    sols = {}
+    for name, dt, prec, pc in (("fp64", torch.float64, _lib.SOLVE_F64, _lib.PRECOND_JACOBI),
+                               ("fp32_bulk", torch.float32, _lib.SOLVE_MIXED,
+                                _lib.PRECOND_BLOCK_JACOBI)):
+        t = lambda a: torch.tensor(a, dtype=dt, device=d)  # noqa: E731
+        x, X0, v = t(mg["x"]), t(mg["X0"]), t(np.zeros(mg["n"] * 3))
+        mu_d, lam_d, c_d = t(mu), t(lam), torch.tensor(c, device=d)
+        B, W, _ = tet_precompute(mesh, X0, 1e3, dtype=dt)
+        asm = lambda: (assemble_tet_stiffness(mesh, _lib.MODEL_NEOHOOKEAN, x, c_d, B, W, mu_d,  # noqa
+                                              lam_d, 0.01, 1e3, dtype=dt, exact=False),
+                       assemble_tet_force(mesh, _lib.MODEL_NEOHOOKEAN, x, v, c_d, B, W, mu_d, lam_d,
+                                          0.01, 1e3, np.array([0, 0, -9.81]), dtype=dt,
+                                          exact=False))
+        asm()
+        ms_asm, (A, f) = _ev_ms(st, asm, reps=3)
+        S = Solver(ctx, mesh.n, 3, mesh.pattern.rowptr, mesh.pattern.colidx, A, mesh.nnzb,
+                   solve_opts(precision=prec, precond=pc, tol=1e-8, maxiters=100000))
+        b = f.double()
+        xs = torch.zeros_like(b)
+        ms_solve, r = _ev_ms(st, lambda: S.solve(b, xs.zero_()))
+        S.close()
+        sols[name] = xs.cpu().numpy()
+        out[name] = {"assembly_ms": ms_asm, "elements_per_s": nT / (ms_asm / 1e3),
+                     "solve_ms": ms_solve, "iters": r.iters,
+                     "relres": (r.true_normr2 / r.bnorm2) ** 0.5}
+    out["fp32_bulk_rel_error_vs_fp64"] = float(np.linalg.norm(sols["fp32_bulk"] - sols["fp64"]) /
+                                               np.linalg.norm(sols["fp64"]))
+    out["speedup_solve"] = out["fp64"]["solve_ms"] / out["fp32_bulk"]["solve_ms"]
+    print(json.dumps(out), flush=True)
+
+
+def run_heat(args):
+    """P1 heat on the 128^3 lattice (2,146,689 DOF): kappa log-uniform
+    [1e-2, 1e2] per tet, T0 uniform [0, 1], dt = 1e-2; A = M + dt K,
+    b = M T0.  1,000 scalar SpMVs FP32 vs FP64, then CG to 1e-8: FP64
+    Jacobi-CG against the FP32 matrix with FP64 reductions (mixed)."""
+    import numpy as np
+    import torch
+    from simit_gb300 import _lib, meshgen
+    from simit_gb300.runtime import (Context, Mesh, Solver, assemble_heat, bspmv, solve_opts,
+                                     tet_precompute)
+    size = args.size
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    st = ctx.torch_stream
+    mg = meshgen.tet_grid(size)
+    nT = len(mg["tets"]) // 4
+    g = meshgen.rng(31)
+    kappa = 10 ** g.uniform(-2, 2, nT)
+    T0 = g.uniform(0, 1, mg["n"])
+    mesh = Mesh(ctx, mg["n"], mg["tets"], 4)
+    d = ctx.device
+    out = {"workload": "P1 heat %d^3 (%d DOF, nnz %d)" % (size, mg["n"], mesh.nnzb)}
+    for name, dt, prec in (("fp64", torch.float64, _lib.SOLVE_F64),
+                           ("fp32_matrix", torch.float32, _lib.SOLVE_MIXED)):
+        B, W, _ = tet_precompute(mesh, torch.tensor(mg["x"], dtype=dt, device=d), 1.0, dtype=dt)
+        kap = torch.tensor(kappa, dtype=dt, device=d)
+        T = torch.tensor(T0, dtype=dt, device=d)
+        ms_asm, (A, b) = _ev_ms(st, lambda: assemble_heat(mesh, B, W, kap, 1e-2, T, dtype=dt,
+                                                          exact=False))
+        xv = torch.rand(mesh.n, dtype=dt, device=d)
+        y = torch.empty_like(xv)
+        bspmv(ctx, mesh.n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A, xv, y)
+        ms_spmv, _ = _ev_ms(st, lambda: bspmv(ctx, mesh.n, 1, mesh.pattern.rowptr,
+                                             mesh.pattern.colidx, A, xv, y), reps=1000)
+        es = A.element_size()
+        nbytes = mesh.nnzb * (es + 4) + (mesh.n + 1) * 4 + mesh.n * 2 * es
+        S = Solver(ctx, mesh.n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A, mesh.nnzb,
+                   solve_opts(precision=prec, precond=_lib.PRECOND_JACOBI, tol=1e-8,
+                              maxiters=100000))
+        b64 = b.double()
+        xs = torch.zeros_like(b64)
+        ms_solve, r = _ev_ms(st, lambda: S.solve(b64, xs.zero_()))
+        S.close()
+        out[name] = {"assembly_ms": ms_asm, "spmv_ms": ms_spmv, "spmv_GBps": nbytes / ms_spmv / 1e6,
+                     "spmv_1000_ms": ms_spmv * 1000, "solve_ms": ms_solve, "iters": r.iters,
+                     "relres": (r.true_normr2 / r.bnorm2) ** 0.5}
+    print(json.dumps(out), flush=True)
 
 
 def run_cloth(args):
@@ -445,6 +565,12 @@ def main():
         return
     if args.cloth:
         run_cloth(args)
+        return
+    if args.neo:
+        run_neo(args)
+        return
+    if args.heat:
+        run_heat(args)
         return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":

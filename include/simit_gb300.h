@@ -256,6 +256,7 @@ typedef struct sg_solve_opts {
   int32_t lanes;             /* SpMV lanes per block row; 0 = default */
   int32_t batch;             /* iterations per graph launch (even); 0 = 32 */
   const float *learned_params; /* SG_PRECOND_LEARNED: device FP32[sg_mpnn_nparams()] */
+  int32_t learned_linear;      /* 1: identity activations (linear variant) */
 } sg_solve_opts;
 
 typedef struct sg_solve_result {
@@ -324,6 +325,9 @@ int sg_mpnn_nparams(void);
 /* Edge weights and block-Jacobi of a 3x3-blocked matrix (FP32 or FP64). */
 int sg_mpnn_graph_create(sg_ctx *ctx, const sg_matrix *A, sg_mpnn_graph **out);
 int sg_mpnn_graph_refresh(sg_mpnn_graph *g);
+/* linear = 1: identity activations instead of relu (z is then linear in r,
+ * a fixed linear preconditioner); 0 (default): relu. */
+int sg_mpnn_graph_set_linear(sg_mpnn_graph *g, int linear);
 int sg_mpnn_graph_destroy(sg_mpnn_graph *g);
 /* z = net(r); r, z FP32 [n*3]. */
 int sg_mpnn_forward(sg_mpnn_graph *g, const float *params, const float *r, float *z,

@@ -72,7 +72,9 @@ def _agg(a, rows, cols, x, n):
     return out
 
 
-def forward(params, n, rowptr, colidx, vals, r):
+def forward(params, n, rowptr, colidx, vals, r, linear=False):
+    """linear=True: identity activations instead of relu."""
+    act = (lambda g: g) if linear else (lambda g: np.maximum(g, 0))
     p = unpack(params)
     W2h, W3h = bf16(p["W2h"]), bf16(p["W3h"])
     a, rows, cols = edge_weights(n, rowptr, colidx, vals)
@@ -81,20 +83,21 @@ def forward(params, n, rowptr, colidx, vals, r):
     s = np.einsum("vij,vj->vi", Dinv, rv)
     m1 = _agg(a, rows, cols, s, n)
     g1 = s @ p["W1s"].T + m1 @ p["W1m"].T
-    h1 = np.maximum(g1, 0)
+    h1 = act(g1)
     q2 = h1 @ p["P2"].T
     m2 = _agg(a, rows, cols, q2, n)
     h1b = bf16(h1)
     g2 = h1b @ W2h.T + m2 @ p["W2m"].T
-    h2 = np.maximum(g2, 0)
+    h2 = act(g2)
     q3 = h2 @ p["P3"].T
     m3 = _agg(a, rows, cols, q3, n)
     h2b = bf16(h2)
     g3 = h2b @ W3h.T + m3 @ p["W3m"].T
-    h3 = np.maximum(g3, 0)
+    h3 = act(g3)
     z = s + h3 @ p["Wout"].T
     cache = dict(a=a, rows=rows, cols=cols, s=s, m1=m1, g1=g1, h1=h1, h1b=h1b, q2=q2, m2=m2,
-                 g2=g2, h2=h2, h2b=h2b, q3=q3, m3=m3, g3=g3, h3=h3, W2h=W2h, W3h=W3h, p=p, n=n)
+                 g2=g2, h2=h2, h2b=h2b, q3=q3, m3=m3, g3=g3, h3=h3, W2h=W2h, W3h=W3h, p=p, n=n,
+                 linear=linear)
     return z.reshape(-1), cache
 
 
@@ -108,7 +111,8 @@ def backward(cache, dz):
     g = {}
     g["Wout"] = dz.T @ c["h3"]
     dh3 = dz @ p["Wout"]
-    dg3 = dh3 * (c["g3"] > 0)
+    mask = (lambda g: np.ones_like(g)) if c["linear"] else (lambda g: (g > 0))
+    dg3 = dh3 * mask(c["g3"])
     g["W3h"] = dg3.T @ c["h2b"]
     g["W3m"] = dg3.T @ c["m3"]
     dh2 = dg3 @ c["W3h"]
@@ -116,7 +120,7 @@ def backward(cache, dz):
     dq3 = _agg(a, rows, cols, dm3, n)  # a is symmetric: the transpose aggregation
     g["P3"] = dq3.T @ c["h2"]
     dh2 = dh2 + dq3 @ p["P3"]
-    dg2 = dh2 * (c["g2"] > 0)
+    dg2 = dh2 * mask(c["g2"])
     g["W2h"] = dg2.T @ c["h1b"]
     g["W2m"] = dg2.T @ c["m2"]
     dh1 = dg2 @ c["W2h"]
@@ -124,7 +128,7 @@ def backward(cache, dz):
     dq2 = _agg(a, rows, cols, dm2, n)
     g["P2"] = dq2.T @ c["h1"]
     dh1 = dh1 + dq2 @ p["P2"]
-    dg1 = dh1 * (c["g1"] > 0)
+    dg1 = dh1 * mask(c["g1"])
     g["W1s"] = dg1.T @ c["s"]
     g["W1m"] = dg1.T @ c["m1"]
     return np.concatenate([g[name].reshape(-1) for name, _ in SHAPES])

@@ -40,7 +40,8 @@ class SolveOpts(ctypes.Structure):
     """sg_solve_opts"""
     _fields_ = [("precision", ctypes.c_int), ("precond", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", D), ("maxiters", I32), ("verify", I32), ("check_every", I32),
-                ("reliable_delta", D), ("lanes", I32), ("batch", I32), ("learned_params", P)]
+                ("reliable_delta", D), ("lanes", I32), ("batch", I32), ("learned_params", P),
+                ("learned_linear", I32)]
 
 
 class SolveResult(ctypes.Structure):
@@ -91,6 +92,7 @@ SIGNATURES = {
     "sg_mpnn_nparams": (_CI, []),
     "sg_mpnn_graph_create": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(P)]),
     "sg_mpnn_graph_refresh": (_CI, [P]),
+    "sg_mpnn_graph_set_linear": (_CI, [P, _CI]),
     "sg_mpnn_graph_destroy": (_CI, [P]),
     "sg_mpnn_forward": (_CI, [P, P, P, P, _CI]),
     "sg_mpnn_backward": (_CI, [P, P, P, P]),

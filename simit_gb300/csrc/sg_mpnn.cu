@@ -27,7 +27,7 @@ static int galloc(GraphH *G, void **p, size_t bytes) {
 // backward (FP32, one warp per vertex; training meshes only)
 // ---------------------------------------------------------------------------
 // B1: dg3 = (Wout^T dz) * [g3 > 0]; dm3 = W3m^T dg3; dh2a = bf(W3h)^T dg3.
-__global__ void k_b1(int32_t n, const float *__restrict__ prm, const float *__restrict__ dz,
+__global__ void k_b1(int32_t n, int lin, const float *__restrict__ prm, const float *__restrict__ dz,
                      const float *__restrict__ g3, float *__restrict__ dg3,
                      float *__restrict__ dm3, float *__restrict__ dh2a) {
   const int lane = threadIdx.x & 31;
@@ -40,7 +40,7 @@ __global__ void k_b1(int32_t n, const float *__restrict__ prm, const float *__re
     for (int e = 0; e < 2; ++e) {
       const int h = lane * 2 + e;
       const float d = prm[O_WOUT + h] * d0 + prm[O_WOUT + H + h] * d1 + prm[O_WOUT + 2 * H + h] * d2;
-      dg[e] = g3[v * H + h] > 0.f ? d : 0.f;
+      dg[e] = (lin || g3[v * H + h] > 0.f) ? d : 0.f;
       dg3[v * H + h] = dg[e];
     }
     // dm3_j = sum_h W3m[h][j] dg3[h]
@@ -64,7 +64,7 @@ __global__ void k_b1(int32_t n, const float *__restrict__ prm, const float *__re
 
 // Generic middle step: dq = sum_u a dm_u (K); dh = dha + P^T dq; dg = dh *
 // [g > 0]; optional dm_next = Wm^T dg (K), dha_next = bf(Wh)^T dg (H).
-__global__ void k_bmid(int32_t n, const uint32_t *__restrict__ rowptr,
+__global__ void k_bmid(int32_t n, int lin, const uint32_t *__restrict__ rowptr,
                        const uint32_t *__restrict__ colidx, const float *__restrict__ a,
                        const float *__restrict__ prm, int oP, int oWm, int oWh,
                        const float *__restrict__ dm, const float *__restrict__ dha,
@@ -87,7 +87,7 @@ __global__ void k_bmid(int32_t n, const uint32_t *__restrict__ rowptr,
       float d = dha[v * H + h];
 #pragma unroll
       for (int j = 0; j < K; ++j) d += prm[oP + j * H + h] * __shfl_sync(0xffffffffu, dqj, j);
-      dg[e] = g[v * H + h] > 0.f ? d : 0.f;
+      dg[e] = (lin || g[v * H + h] > 0.f) ? d : 0.f;
       dgout[v * H + h] = dg[e];
     }
     if (dm_next) {
@@ -111,7 +111,7 @@ __global__ void k_bmid(int32_t n, const uint32_t *__restrict__ rowptr,
 
 // Outer-product reduction dW[o][i] = sum_v X_v[o] * Y_v[i] over a chunk of
 // vertices per CTA; partials part[chunk][O*I], summed in order afterwards.
-// Y is transformed: 0 identity, 1 relu, 2 bf16(relu).
+// Y is transformed: 0 identity, 1 relu, 2 bf16(relu), 4 bf16.
 constexpr int OUTER_CHUNK = 1024;
 __global__ void k_outer(int32_t n, const float *__restrict__ X, int O, const float *__restrict__ Y,
                         int I, int ytr, float *__restrict__ part) {
@@ -122,8 +122,8 @@ __global__ void k_outer(int32_t n, const float *__restrict__ X, int O, const flo
     float acc = 0.f;
     for (int64_t v = v0; v < v1; ++v) {
       float y = Y[v * I + i];
-      if (ytr >= 1) y = fmaxf(y, 0.f);
-      if (ytr == 2) y = bf16r(y);
+      if (ytr == 1 || ytr == 2) y = fmaxf(y, 0.f);
+      if (ytr == 2 || ytr == 4) y = bf16r(y);
       acc += X[v * O + o] * y;
     }
     part[(size_t)blockIdx.x * O * I + e] = acc;
@@ -260,17 +260,17 @@ static int forward(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, co
   const int gv = grid_for(c, g.n, 256, 8);
   k_f1<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.dinv, r, g.s, z);
   SG_CHECK_LAUNCH();
-  k_f2<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.rowptr, g.colidx, g.a, prm, g.s, g.m1, g.q2,
+  k_f2<<<gv, 256, 0, st>>>(ctl, gate, g.lin, g.n, g.rowptr, g.colidx, g.a, prm, g.s, g.m1, g.q2,
                            train ? g.g1 : nullptr);
   SG_CHECK_LAUNCH();
   const int64_t ntile = ((int64_t)g.n + 15) / 16;
   int gt = (int)((ntile + TC_WARPS - 1) / TC_WARPS);
   const int cap = c->num_sms * 4;
   if (gt > cap) gt = cap;
-  k_f3<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
+  k_f3<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.lin, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
                                                    g.m1, g.q2, g.m2, g.q3, train ? g.g2 : nullptr);
   SG_CHECK_LAUNCH();
-  k_f4<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
+  k_f4<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.lin, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
                                                    g.m1, g.m2, g.q3, g.m3, z, train ? g.g3 : nullptr);
   SG_CHECK_LAUNCH();
   return SG_OK;
@@ -292,22 +292,23 @@ static int backward(GraphH *G, const float *prm, const float *dz, float *grad) {
   SG_TRY(ensure_train(G));
   const int gw = grid_for(c, (int64_t)g.n * 32, 256, 8);
   cudaStream_t st = c->stream;
-  k_b1<<<gw, 256, 0, st>>>(g.n, prm, dz, g.g3, g.dg3, g.dm3, g.dh2a);
+  k_b1<<<gw, 256, 0, st>>>(g.n, g.lin, prm, dz, g.g3, g.dg3, g.dm3, g.dh2a);
   SG_CHECK_LAUNCH();
-  k_bmid<<<gw, 256, 0, st>>>(g.n, g.rowptr, g.colidx, g.a, prm, O_P3, O_W2M, O_W2H, g.dm3, g.dh2a,
+  k_bmid<<<gw, 256, 0, st>>>(g.n, g.lin, g.rowptr, g.colidx, g.a, prm, O_P3, O_W2M, O_W2H, g.dm3, g.dh2a,
                              g.g2, g.dq3, g.dg2, g.dm2, g.dh1a);
   SG_CHECK_LAUNCH();
-  k_bmid<<<gw, 256, 0, st>>>(g.n, g.rowptr, g.colidx, g.a, prm, O_P2, 0, 0, g.dm2, g.dh1a, g.g1,
+  k_bmid<<<gw, 256, 0, st>>>(g.n, g.lin, g.rowptr, g.colidx, g.a, prm, O_P2, 0, 0, g.dm2, g.dh1a, g.g1,
                              g.dq2, g.dg1, nullptr, nullptr);
   SG_CHECK_LAUNCH();
-  // weight gradients; h3 = relu(g3), h2 = relu(g2), h1 = relu(g1)
-  SG_TRY(outer(G, dz, 3, g.g3, H, 1, grad + O_WOUT));
-  SG_TRY(outer(G, g.dg3, H, g.g2, H, 2, grad + O_W3H));
+  // weight gradients; h = act(g) (relu, or identity in the linear variant)
+  const int A_ = g.lin ? 0 : 1, AB = g.lin ? 4 : 2;
+  SG_TRY(outer(G, dz, 3, g.g3, H, A_, grad + O_WOUT));
+  SG_TRY(outer(G, g.dg3, H, g.g2, H, AB, grad + O_W3H));
   SG_TRY(outer(G, g.dg3, H, g.m3, K, 0, grad + O_W3M));
-  SG_TRY(outer(G, g.dq3, K, g.g2, H, 1, grad + O_P3));
-  SG_TRY(outer(G, g.dg2, H, g.g1, H, 2, grad + O_W2H));
+  SG_TRY(outer(G, g.dq3, K, g.g2, H, A_, grad + O_P3));
+  SG_TRY(outer(G, g.dg2, H, g.g1, H, AB, grad + O_W2H));
   SG_TRY(outer(G, g.dg2, H, g.m2, K, 0, grad + O_W2M));
-  SG_TRY(outer(G, g.dq2, K, g.g1, H, 1, grad + O_P2));
+  SG_TRY(outer(G, g.dq2, K, g.g1, H, A_, grad + O_P2));
   SG_TRY(outer(G, g.dg1, H, g.s, 3, 0, grad + O_W1S));
   SG_TRY(outer(G, g.dg1, H, g.m1, 3, 0, grad + O_W1M));
   return SG_OK;
@@ -366,6 +367,7 @@ static void learned_free(Solver *S) {
 }
 
 static const float *g_pending_params = nullptr;
+static int g_pending_linear = 0;
 static int learned_setup(Solver *S) {
   LearnedExt *L = new LearnedExt();
   S->ext = L;
@@ -373,6 +375,7 @@ static int learned_setup(Solver *S) {
   L->prm = g_pending_params;
   L->G = new mpnn::GraphH();
   SG_TRY(mpnn::graph_init(S->c, &S->A, L->G));
+  L->G->g.lin = g_pending_linear;
   S->ext_prec = learned_prec;
   S->ext_prec_apply = learned_apply;
   S->flexible = 1;
@@ -387,6 +390,7 @@ int learned_refresh(Solver *S) {
 int learned_solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, const float *params,
                         Solver *S) {
   g_pending_params = params;
+  g_pending_linear = o->learned_linear;
   int rc = solver_init(c, A, o, S, learned_setup);
   g_pending_params = nullptr;
   return rc;
@@ -412,6 +416,13 @@ int sg_mpnn_graph_create(sg_ctx *h, const sg_matrix *A, sg_mpnn_graph **out) {
   }
   ctx_retain(c);
   *out = reinterpret_cast<sg_mpnn_graph *>(G);
+  return SG_OK;
+}
+
+int sg_mpnn_graph_set_linear(sg_mpnn_graph *hg, int linear) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  SG_REQUIRE(G, "sg_mpnn_graph_set_linear: null graph");
+  G->g.lin = linear ? 1 : 0;
   return SG_OK;
 }
 

@@ -54,6 +54,7 @@ struct Graph {
   int gpart_chunks = 0;
   float *ld = nullptr, *lq = nullptr;  // loss temporaries
   double *dres = nullptr;
+  int lin = 0;  // identity activations (a linear preconditioner) instead of relu
 };
 
 __device__ __forceinline__ float bf16r(float x) {

@@ -77,7 +77,7 @@ struct L1W {
 };
 
 // F2: m1 = sum a s_u; h1 = relu(W1s s + W1m m1); q2 = P2 h1.  One thread per vertex.
-__global__ void __launch_bounds__(256) k_f2(const SolveCtl *ctl, int gate, int32_t n,
+__global__ void __launch_bounds__(256) k_f2(const SolveCtl *ctl, int gate, int lin, int32_t n,
                                             const uint32_t *__restrict__ rowptr,
                                             const uint32_t *__restrict__ colidx,
                                             const float *__restrict__ a,
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(256) k_f2(const SolveCtl *ctl, int gate, int32
       const float g = w.w1s[h * 3] * s0 + w.w1s[h * 3 + 1] * s1 + w.w1s[h * 3 + 2] * s2 +
                       w.w1m[h * 3] * mm0 + w.w1m[h * 3 + 1] * mm1 + w.w1m[h * 3 + 2] * mm2;
       if (g1) g1[v * H + h] = g;
-      const float hv = fmaxf(g, 0.f);
+      const float hv = lin ? g : fmaxf(g, 0.f);
 #pragma unroll
       for (int j = 0; j < K; ++j) qq[j] += w.p2[j * H + h] * hv;
     }
@@ -192,7 +192,7 @@ __device__ __forceinline__ void load_tc_weights(TCW &w, const float *prm, bool n
 
 // The warp's 16 vertices: gather m = sum a q_u (8-dim) into dst[16*K]; load
 // s and m1; rebuild bf16(h1) into x1.
-__device__ __forceinline__ void tc_prologue(const TCW &w, TCWarp &tw, int64_t v0, int32_t n,
+__device__ __forceinline__ void tc_prologue(const TCW &w, TCWarp &tw, int lin, int64_t v0, int32_t n,
                                             const uint32_t *rowptr, const uint32_t *colidx,
                                             const float *a, const float *qsrc, float *dst,
                                             const float *s, const float *m1) {
@@ -228,7 +228,7 @@ __device__ __forceinline__ void tc_prologue(const TCW &w, TCWarp &tw, int64_t v0
     for (int h = h0; h < h0 + 32; ++h) {
       const float g = w.w1s[h * 3] * sv[0] + w.w1s[h * 3 + 1] * sv[1] + w.w1s[h * 3 + 2] * sv[2] +
                       w.w1m[h * 3] * mv[0] + w.w1m[h * 3 + 1] * mv[1] + w.w1m[h * 3 + 2] * mv[2];
-      tw.x1[vi * HP + h] = __float2bfloat16_rn(fmaxf(g, 0.f));
+      tw.x1[vi * HP + h] = __float2bfloat16_rn(lin ? g : fmaxf(g, 0.f));
     }
   }
   __syncwarp();
@@ -238,7 +238,7 @@ __device__ __forceinline__ void tc_prologue(const TCW &w, TCWarp &tw, int64_t v0
 // of the pre-activation g; acc <- relu(acc).
 __device__ __forceinline__ void tc_layer_epilogue(float acc[8][4], const float *Wm,
                                                   const float *msrc, int64_t v0, int32_t n,
-                                                  float *g_out) {
+                                                  float *g_out, int lin) {
   const int lane = threadIdx.x & 31, gid = lane >> 2, t = lane & 3;
 #pragma unroll
   for (int nt = 0; nt < 8; ++nt)
@@ -249,13 +249,13 @@ __device__ __forceinline__ void tc_layer_epilogue(float acc[8][4], const float *
 #pragma unroll
       for (int j = 0; j < K; ++j) gsum += Wm[col * K + j] * msrc[row * K + j];
       if (g_out && v0 + row < n) g_out[(v0 + row) * H + col] = gsum;
-      acc[nt][e] = fmaxf(gsum, 0.f);
+      acc[nt][e] = lin ? gsum : fmaxf(gsum, 0.f);
     }
 }
 
 // F3: m2 = sum a q2_u; g2 = W2h bf16(h1) + W2m m2; h2 = relu(g2); q3 = P3 h2.
 __global__ void __launch_bounds__(TC_WARPS * 32)
-    k_f3(const SolveCtl *ctl, int gate, int32_t n, const uint32_t *__restrict__ rowptr,
+    k_f3(const SolveCtl *ctl, int gate, int lin, int32_t n, const uint32_t *__restrict__ rowptr,
          const uint32_t *__restrict__ colidx, const float *__restrict__ a,
          const float *__restrict__ prm, const float *__restrict__ s,
          const float *__restrict__ m1, const float *__restrict__ q2, float *__restrict__ m2,
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
   for (int64_t tile = (int64_t)blockIdx.x * TC_WARPS + (threadIdx.x >> 5); tile < ntile;
        tile += (int64_t)gridDim.x * TC_WARPS) {
     const int64_t v0 = tile * 16;
-    tc_prologue(w, tw, v0, n, rowptr, colidx, a, q2, tw.mA, s, m1);
+    tc_prologue(w, tw, lin, v0, n, rowptr, colidx, a, q2, tw.mA, s, m1);
     for (int i = lane; i < 16 * K; i += 32)
       if (v0 + i / K < n) m2[v0 * K + i] = tw.mA[i];
     float acc[8][4];
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
     gemm16x64(tw.x1, w.w2h, acc);
-    tc_layer_epilogue(acc, w.w2m, tw.mA, v0, n, g2);
+    tc_layer_epilogue(acc, w.w2m, tw.mA, v0, n, g2, lin);
     // q3[row][j] = sum_n P3[j][n] h2[row][n]: quad partials then shuffles
     float qa[K], qb[K];
 #pragma unroll
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 // F4: m3 = sum a q3_u; h2 = relu(W2h bf16(h1) + W2m m2); g3 = W3h bf16(h2) +
 // W3m m3; h3 = relu(g3); z = s + Wout h3.
 __global__ void __launch_bounds__(TC_WARPS * 32)
-    k_f4(const SolveCtl *ctl, int gate, int32_t n, const uint32_t *__restrict__ rowptr,
+    k_f4(const SolveCtl *ctl, int gate, int lin, int32_t n, const uint32_t *__restrict__ rowptr,
          const uint32_t *__restrict__ colidx, const float *__restrict__ a,
          const float *__restrict__ prm, const float *__restrict__ s,
          const float *__restrict__ m1, const float *__restrict__ m2,
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
   for (int64_t tile = (int64_t)blockIdx.x * TC_WARPS + (threadIdx.x >> 5); tile < ntile;
        tile += (int64_t)gridDim.x * TC_WARPS) {
     const int64_t v0 = tile * 16;
-    tc_prologue(w, tw, v0, n, rowptr, colidx, a, q3, tw.mA, s, m1);
+    tc_prologue(w, tw, lin, v0, n, rowptr, colidx, a, q3, tw.mA, s, m1);
     for (int i = lane; i < 16 * K; i += 32) {
       const bool in = v0 + i / K < n;
       tw.mB[i] = in ? m2[v0 * K + i] : 0.f;
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
     gemm16x64(tw.x1, w.w2h, acc);
-    tc_layer_epilogue(acc, w.w2m, tw.mB, v0, n, nullptr);
+    tc_layer_epilogue(acc, w.w2m, tw.mB, v0, n, nullptr, lin);
     // h2 -> bf16 tile x2
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt)
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
     gemm16x64(tw.x2, w.w3h, acc);
-    tc_layer_epilogue(acc, w.w3m, tw.mA, v0, n, g3);
+    tc_layer_epilogue(acc, w.w3m, tw.mA, v0, n, g3, lin);
     float za[3], zb[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {

@@ -23,6 +23,7 @@ from .runtime import Solver, bspmv, dtype_code, ptr, solve_opts
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS = os.path.join(HERE, "data", "mpnn_elasticity.npy")
+WEIGHTS_LINEAR = os.path.join(HERE, "data", "mpnn_elasticity_linear.npy")
 KS = (1, 3, 8, 16, 32, 64, 128, 256, 512, 1024)
 H, K = 64, 8
 SHAPES = [("W1s", (H, 3)), ("W1m", (H, 3)), ("P2", (K, H)), ("W2h", (H, H)), ("W2m", (H, K)),
@@ -54,7 +55,7 @@ def load_weights(path=WEIGHTS):
 class Graph:
     """sg_mpnn_graph of a 3x3-blocked matrix."""
 
-    def __init__(self, ctx, mesh, A):
+    def __init__(self, ctx, mesh, A, linear=False):
         self.ctx = ctx
         self.A = A
         self.m = _lib.Matrix(mesh.n, 3, mesh.nnzb, mesh.pattern.rowptr.data_ptr(),
@@ -63,6 +64,7 @@ class Graph:
         call("sg_mpnn_graph_create", ctx.h, ctypes.byref(self.m), ctypes.byref(h))
         self.h = h
         self.n = mesh.n
+        call("sg_mpnn_graph_set_linear", h, int(linear))
 
     def forward(self, params, r, z, train=False):
         call("sg_mpnn_forward", self.h, ptr(params), ptr(r), ptr(z), int(train))
@@ -156,13 +158,13 @@ class Trainer:
 
 
 def train(ctx, sizes=(16, 24, 32, 40, 48), n_pairs=2000, epochs=6, lr=1e-3, seed=0,
-          log=print):
+          log=print, linear=False):
     """Train on n_pairs pairs spread over the meshes; returns (params, history)."""
     per_mesh = max(1, n_pairs // (len(sizes) * len(KS)))
     data = []
     for i, nc in enumerate(sizes):
         prob, pairs = make_pairs(ctx, nc, seed=100 + i, n_rhs=per_mesh)
-        data.append((prob, Graph(ctx, prob.mesh, prob.A), pairs))
+        data.append((prob, Graph(ctx, prob.mesh, prob.A, linear=linear), pairs))
         log("mesh %d^3: %d pairs" % (nc, len(pairs)))
     tr = Trainer(ctx, lr=lr, seed=seed)
     hist = []
@@ -187,7 +189,7 @@ def train(ctx, sizes=(16, 24, 32, 40, 48), n_pairs=2000, epochs=6, lr=1e-3, seed
     return params, hist
 
 
-def compare(ctx, params, ncell, seed=999, tol=1e-8):
+def compare(ctx, params, ncell, seed=999, tol=1e-8, linear=False):
     """Flexible PCG with the network vs block-Jacobi PCG on a held-out mesh."""
     host = problems.hetero_mesh(ncell, seed=seed)
     out = {}
@@ -201,7 +203,8 @@ def compare(ctx, params, ncell, seed=999, tol=1e-8):
         m = prob.mesh
         S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, m.nnzb,
                    solve_opts(precision=_lib.SOLVE_MIXED, precond=pc, tol=tol, maxiters=100000,
-                              learned_params=prm if pc == _lib.PRECOND_LEARNED else None),
+                              learned_params=prm if pc == _lib.PRECOND_LEARNED else None,
+                              learned_linear=linear),
                    learned_params_keep=prm)
         x = torch.zeros_like(prob.b)
         torch.cuda.synchronize()
@@ -229,14 +232,15 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval-size", type=int, default=32)
+    ap.add_argument("--linear", action="store_true", help="identity activations")
     a = ap.parse_args()
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
     t0 = time.time()
-    params, hist = train(ctx, n_pairs=a.pairs, epochs=a.epochs, lr=a.lr)
-    os.makedirs(os.path.dirname(a.out), exist_ok=True)
+    params, hist = train(ctx, n_pairs=a.pairs, epochs=a.epochs, lr=a.lr, linear=a.linear)
+    os.makedirs(os.path.dirname(a.out) or ".", exist_ok=True)
     np.save(a.out, params)
-    res = compare(ctx, params, a.eval_size)
+    res = compare(ctx, params, a.eval_size, linear=a.linear)
     print(json.dumps({"train_seconds": time.time() - t0, "loss_history": hist,
                       "eval": res, "weights": a.out}))
 
