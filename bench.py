@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--sheets", type=int, default=256)
     ap.add_argument("--neo", action="store_true",
                     help="neo-Hookean Newton step (64^3): FP64 vs FP32-bulk mixed precision")
+    ap.add_argument("--solve-only", action="store_true",
+                    help="profiling driver: two steps of the --size system with the solver "
+                         "capped at --iters iterations")
+    ap.add_argument("--iters", type=int, default=64)
     ap.add_argument("--heat", action="store_true",
                     help="P1 heat (128^3): 1000 SpMVs FP32 vs FP64, CG FP64 vs mixed")
     return ap.parse_args()
@@ -243,6 +247,23 @@ def run_cloth(args):
                       "iters_max": int(iters.max()), "iters_mean": float(iters.mean()),
                       "autotuned_config": cb.config, "dofs": h["n"] * 3,
                       "DOF_per_s_batched": h["n"] * 3 / (batched_ms / 1e3)}), flush=True)
+
+
+def run_solve_only(args):
+    """Profiling driver: the --size heterogeneous-elasticity step (FP32
+    assembly + mixed block-Jacobi PCG) with the solver capped at --iters
+    iterations; the second step is event-timed."""
+    import torch
+    from simit_gb300 import _lib, problems
+    from simit_gb300.runtime import Context
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    p = problems.HeteroElasticity(ctx, problems.hetero_mesh(args.size), dtype=torch.float32,
+                                  precond=_lib.PRECOND_BLOCK_JACOBI, maxiters=args.iters)
+    p.step()
+    ms, r = _ev_ms(ctx.torch_stream, p.step)
+    print(json.dumps({"size": args.size, "iters": r.iters, "status": r.status, "step_ms": ms,
+                      "kernels": r.kernels}), flush=True)
 
 
 def run_spmv_only(args):
@@ -560,6 +581,9 @@ def run_ours(args, rank, world, local):
 
 def main():
     args = parse()
+    if args.solve_only:
+        run_solve_only(args)
+        return
     if args.spmv_only:
         run_spmv_only(args)
         return

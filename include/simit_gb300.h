@@ -172,9 +172,11 @@ int sg_assemble_heat(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
  * bs = 1, 2, 3 have dedicated kernels; other bs use a generic kernel.
  * val_dtype is the matrix value type; vec_dtype the type of x and y;
  * accumulation is in the wider of the two.  g = 1,2,4,8,16,32 selects the
- * streaming kernel with g lanes per block row; g = -1..-6 selects variant
+ * streaming kernel with g lanes per block row; g = -1..-11 selects variant
  * -g-1 of the TMA-staged kernel (bs = 3, 16-byte aligned vals/colidx;
- * variants differ in lanes per row, rows per tile and pipeline stages);
+ * variants differ in lanes per row, rows per tile, pipeline stages and
+ * whether a CTA or each warp runs the copy pipeline; a variant whose
+ * buffers cannot hold the pattern's largest tile runs the streaming kernel);
  * g = 0 picks (TMA variant 0 for FP32 values, the streaming kernel for FP64).
  * ------------------------------------------------------------------- */
 int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
@@ -256,7 +258,7 @@ typedef struct sg_solve_opts {
   int32_t lanes;             /* SpMV lanes per block row; 0 = default */
   int32_t batch;             /* iterations per graph launch (even); 0 = 32 */
   const float *learned_params; /* SG_PRECOND_LEARNED: device FP32[sg_mpnn_nparams()] */
-  int32_t learned_linear;      /* 1: identity activations (linear variant) */
+  int32_t learned_form;        /* SG_MPNN_RELU / SG_MPNN_LINEAR / SG_MPNN_SYM */
 } sg_solve_opts;
 
 typedef struct sg_solve_result {
@@ -314,7 +316,12 @@ int sg_batched_configs(void);
  * messages of 8, no biases) over the matrix graph, z = D^-1 r + Wout h3,
  * where D is the 3x3 block diagonal; the 64x64 layers run on the tensor
  * cores with bf16 weights and FP32 accumulation.  It has no counterpart in
- * the reference (the benchmark spec's learned part).  Parameters are one flat
+ * the reference (it preconditions the flexible PCG).  Three forms
+ * (SG_MPNN_*): relu activations; identity activations (z linear in r); and
+ * the symmetric factorized form M = L^-T (I+N)^T (I+N) L^-1 of the linear
+ * network N with D = L L^T per vertex, symmetric positive definite by
+ * construction and equal to block Jacobi when Wout = 0 ((I+N)^T runs as the
+ * same layers with transposed weights).  Parameters are one flat
  * FP32 device array of sg_mpnn_nparams() values.  Training: forward with
  * train = 1 keeps activations, sg_mpnn_loss gives the A-norm error
  * (z-e)'A(z-e)/e'Ae of a residual/correction pair (r, e = A^-1 r) and dL/dz,
@@ -325,14 +332,15 @@ int sg_mpnn_nparams(void);
 /* Edge weights and block-Jacobi of a 3x3-blocked matrix (FP32 or FP64). */
 int sg_mpnn_graph_create(sg_ctx *ctx, const sg_matrix *A, sg_mpnn_graph **out);
 int sg_mpnn_graph_refresh(sg_mpnn_graph *g);
-/* linear = 1: identity activations instead of relu (z is then linear in r,
- * a fixed linear preconditioner); 0 (default): relu. */
-int sg_mpnn_graph_set_linear(sg_mpnn_graph *g, int linear);
+enum { SG_MPNN_RELU = 0, SG_MPNN_LINEAR = 1, SG_MPNN_SYM = 2 };
+/* Select the form (default SG_MPNN_RELU). */
+int sg_mpnn_graph_set_form(sg_mpnn_graph *g, int form);
 int sg_mpnn_graph_destroy(sg_mpnn_graph *g);
-/* z = net(r); r, z FP32 [n*3]. */
+/* z = M(r); r, z FP32 [n*3]. */
 int sg_mpnn_forward(sg_mpnn_graph *g, const float *params, const float *r, float *z,
                     int train);
-/* grad (FP32[nparams], overwritten) of the last train-mode forward for dz. */
+/* grad (FP32[nparams], overwritten) of <dz, M(r)> for the r of the last
+ * train-mode forward. */
 int sg_mpnn_backward(sg_mpnn_graph *g, const float *params, const float *dz, float *grad);
 /* A-norm loss of z against e (FP32 matrix graphs); dz = 2 A (z-e) / e'Ae. */
 int sg_mpnn_loss(sg_mpnn_graph *g, const float *z, const float *e, double eAe, float *dz,

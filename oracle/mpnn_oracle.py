@@ -18,6 +18,20 @@ with a_vu = ||A_vu||_F / sqrt(||A_vv||_F ||A_uu||_F) for the off-diagonal
 blocks of the pattern, bf() rounding to bfloat16 (round to nearest even), and
 W2h, W3h rounded to bfloat16 (the tensor-core operands).  No biases: the map
 r -> z is positively homogeneous.
+
+Forms: relu (above), linear (identity activations, so z = M r with a fixed
+matrix M), and the symmetric factorized form (forward_sym): with the linear
+network N (s -> Wout h3), D_v = L_v L_v^T the Cholesky factors of the
+diagonal blocks,
+
+  M = L^-T (I + N)^T (I + N) L^-1,
+
+symmetric positive definite by construction and equal to block Jacobi when
+Wout = 0.  The hidden activations enter the tensor-core products as two bf16 terms
+(bf16_split) in this form, so the operator is linear and symmetric to about
+2^-16.  (I + N)^T is applied as the same network with transposed weights
+(transpose_params) plus one extra aggregation: N^T y = W1s^T h3' +
+sum_u a_vu W1m^T h3'_u, h3' the transposed network's last hidden layer.
 """
 import numpy as np
 
@@ -66,32 +80,66 @@ def block_jacobi(n, rowptr, colidx, vals):
     return Dinv
 
 
+def chol_inv(n, rowptr, colidx, vals):
+    """Per vertex L_v^-1 with D_v = L_v L_v^T (lower Cholesky factor)."""
+    A = np.asarray(vals, np.float64).reshape(-1, 3, 3)
+    rows = np.repeat(np.arange(n), np.diff(rowptr.astype(np.int64)))
+    d = rows == colidx.astype(np.int64)
+    D = np.zeros((n, 3, 3))
+    D[rows[d]] = A[d]
+    return np.linalg.inv(np.linalg.cholesky(D))
+
+
+def transpose_params(params):
+    """Parameters of the transposed network (same layout): layer 1 <- Wout^T
+    (no message), layer 2 <- layer 3 transposed, layer 3 <- layer 2
+    transposed, output <- W1s^T.  W1m^T is the extra output projection."""
+    p = unpack(params)
+    q = {"W1s": p["Wout"].T, "W1m": np.zeros((H, 3)), "P2": p["W3m"].T, "W2h": p["W3h"].T,
+         "W2m": p["P3"].T, "P3": p["W2m"].T, "W3h": p["W2h"].T, "W3m": p["P2"].T,
+         "Wout": p["W1s"].T}
+    return np.concatenate([q[name].reshape(-1) for name, _ in SHAPES])
+
+
 def _agg(a, rows, cols, x, n):
     out = np.zeros((n,) + x.shape[1:])
     np.add.at(out, rows, a[:, None] * x[cols])
     return out
 
 
-def forward(params, n, rowptr, colidx, vals, r, linear=False):
-    """linear=True: identity activations instead of relu."""
+def bf16_split(x):
+    """bf16(x) + bf16(x - bf16(x)): the two-term bf16 operand of the split
+    activations."""
+    hi = bf16(x)
+    return hi + bf16(np.asarray(x, np.float64) - hi)
+
+
+def forward(params, n, rowptr, colidx, vals, r, linear=False, stage="dinv", split=False):
+    """linear=True: identity activations instead of relu.  stage: the input
+    map s = D^-1 r ("dinv"), L^-1 r ("linv") or r ("id").  split: the hidden
+    activations enter the tensor-core products as two bf16 terms."""
     act = (lambda g: g) if linear else (lambda g: np.maximum(g, 0))
+    rnd = bf16_split if split else bf16
     p = unpack(params)
     W2h, W3h = bf16(p["W2h"]), bf16(p["W3h"])
     a, rows, cols = edge_weights(n, rowptr, colidx, vals)
-    Dinv = block_jacobi(n, rowptr, colidx, vals)
     rv = np.asarray(r, np.float64).reshape(n, 3)
-    s = np.einsum("vij,vj->vi", Dinv, rv)
+    if stage == "id":
+        s = rv.copy()
+    else:
+        St = (block_jacobi if stage == "dinv" else chol_inv)(n, rowptr, colidx, vals)
+        s = np.einsum("vij,vj->vi", St, rv)
     m1 = _agg(a, rows, cols, s, n)
     g1 = s @ p["W1s"].T + m1 @ p["W1m"].T
     h1 = act(g1)
     q2 = h1 @ p["P2"].T
     m2 = _agg(a, rows, cols, q2, n)
-    h1b = bf16(h1)
+    h1b = rnd(h1)
     g2 = h1b @ W2h.T + m2 @ p["W2m"].T
     h2 = act(g2)
     q3 = h2 @ p["P3"].T
     m3 = _agg(a, rows, cols, q3, n)
-    h2b = bf16(h2)
+    h2b = rnd(h2)
     g3 = h2b @ W3h.T + m3 @ p["W3m"].T
     h3 = act(g3)
     z = s + h3 @ p["Wout"].T
@@ -99,6 +147,29 @@ def forward(params, n, rowptr, colidx, vals, r, linear=False):
                  g2=g2, h2=h2, h2b=h2b, q3=q3, m3=m3, g3=g3, h3=h3, W2h=W2h, W3h=W3h, p=p, n=n,
                  linear=linear)
     return z.reshape(-1), cache
+
+
+def forward_sym(params, n, rowptr, colidx, vals, r):
+    """z = L^-T (I + N)^T (I + N) L^-1 r (linear network N)."""
+    y, cu = forward(params, n, rowptr, colidx, vals, r, linear=True, stage="linv", split=True)
+    wp, ca = forward(transpose_params(params), n, rowptr, colidx, vals, y, linear=True,
+                     stage="id", split=True)
+    p = unpack(params)
+    a, rows, cols = ca["a"], ca["rows"], ca["cols"]
+    t = ca["h3"] @ p["W1m"]
+    w = wp.reshape(n, 3) + _agg(a, rows, cols, t, n)
+    Li = chol_inv(n, rowptr, colidx, vals)
+    z = np.einsum("vji,vj->vi", Li, w)
+    return z.reshape(-1), dict(cu=cu, y=y, Li=Li, args=(params, n, rowptr, colidx, vals))
+
+
+def backward_sym(cache, dz):
+    """Weight gradient of <dz, M r> for the symmetric form:
+    grad_N(input L^-1 r, cotangent (I + N) L^-1 dz) + grad_N(input L^-1 dz,
+    cotangent (I + N) L^-1 r)."""
+    params, n, rowptr, colidx, vals = cache["args"]
+    yt, cg = forward(params, n, rowptr, colidx, vals, dz, linear=True, stage="linv", split=True)
+    return backward(cache["cu"], yt) + backward(cg, cache["y"])
 
 
 def backward(cache, dz):

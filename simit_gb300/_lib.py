@@ -41,7 +41,7 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("precond", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", D), ("maxiters", I32), ("verify", I32), ("check_every", I32),
                 ("reliable_delta", D), ("lanes", I32), ("batch", I32), ("learned_params", P),
-                ("learned_linear", I32)]
+                ("learned_form", I32)]
 
 
 class SolveResult(ctypes.Structure):
@@ -51,6 +51,7 @@ class SolveResult(ctypes.Structure):
 
 
 SOLVE_F64, SOLVE_MIXED = 0, 1
+MPNN_RELU, MPNN_LINEAR, MPNN_SYM = 0, 1, 2
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1, 2, 3
 STOP_NORMR2, STOP_NORMR, STOP_RELATIVE = 0, 1, 2
 STATUS = {1: "converged", 2: "maxiter", 3: "breakdown", 4: "nan"}
@@ -92,7 +93,7 @@ SIGNATURES = {
     "sg_mpnn_nparams": (_CI, []),
     "sg_mpnn_graph_create": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(P)]),
     "sg_mpnn_graph_refresh": (_CI, [P]),
-    "sg_mpnn_graph_set_linear": (_CI, [P, _CI]),
+    "sg_mpnn_graph_set_form": (_CI, [P, _CI]),
     "sg_mpnn_graph_destroy": (_CI, [P]),
     "sg_mpnn_forward": (_CI, [P, P, P, P, _CI]),
     "sg_mpnn_backward": (_CI, [P, P, P, P]),

@@ -29,6 +29,8 @@ struct Ctx {
   int32_t mr_val[MAXROW_CACHE] = {};
   int32_t mr_t16[MAXROW_CACHE] = {};  // largest 16-row tile, in blocks
   int32_t mr_t32[MAXROW_CACHE] = {};  // largest 32-row tile, in blocks
+  int32_t mr_t4[MAXROW_CACHE] = {};   // largest 4-row tile
+  int32_t mr_t8[MAXROW_CACHE] = {};   // largest 8-row tile
   int mr_next = 0;
   int refs = 1;  // sg_ctx_destroy + one per live solver
 };

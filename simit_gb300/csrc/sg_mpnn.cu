@@ -15,12 +15,22 @@ struct GraphH {
   Graph g;
   std::vector<void *> allocs;
   bool train_ready = false;
+  // symmetric form: a second set of layer buffers over the same graph data
+  // (the transposed network's pass, and the second training forward)
+  GraphH *twin = nullptr;
 };
 
 static int galloc(GraphH *G, void **p, size_t bytes) {
   SG_CHECK_CUDA(cudaMalloc(p, bytes < 256 ? 256 : bytes));
   G->allocs.push_back(*p);
   return SG_OK;
+}
+
+static void graph_free(GraphH *G) {
+  if (!G) return;
+  graph_free(G->twin);
+  for (void *p : G->allocs) cudaFree(p);
+  delete G;
 }
 
 // ---------------------------------------------------------------------------
@@ -203,8 +213,62 @@ static int graph_refresh(GraphH *G) {
     k_edge_weights<float><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const float *)g.vals, dn, g.a);
     k_diag_inv<float, float><<<gr, 256, 0, c->stream>>>(g.n, 3, g.rowptr, g.colidx, (const float *)g.vals, g.dinv, 1, c->d_err);
   }
+  if (g.linv) {
+    if (g.vdt == SG_F64)
+      k_chol_inv<double><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const double *)g.vals, g.linv);
+    else
+      k_chol_inv<float><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const float *)g.vals, g.linv);
+  }
   SG_CHECK_LAUNCH();
   return check_device_error(c, "mpnn graph");
+}
+
+// Layer buffers of one pass (s, m1, q2, m2, q3, m3).
+static int alloc_layers(GraphH *G) {
+  Graph &g = G->g;
+  const size_t n = (size_t)g.n;
+  SG_TRY(galloc(G, (void **)&g.s, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.m1, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.q2, n * K * 4));
+  SG_TRY(galloc(G, (void **)&g.m2, n * K * 4));
+  SG_TRY(galloc(G, (void **)&g.q3, n * K * 4));
+  SG_TRY(galloc(G, (void **)&g.m3, n * K * 4));
+  return SG_OK;
+}
+
+// Switch to the symmetric factorized form: L^-1, the extra vectors and the
+// twin's layer buffers (allocated once).
+static int set_sym(GraphH *G, int sym) {
+  Graph &g = G->g;
+  g.sym = sym ? 1 : 0;
+  if (!sym) return SG_OK;
+  g.lin = 1;
+  if (G->twin) return SG_OK;
+  const size_t n = (size_t)g.n;
+  SG_TRY(galloc(G, (void **)&g.linv, n * 9 * 4));
+  SG_TRY(galloc(G, (void **)&g.y, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.wp, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.t, n * 3 * 4));
+  SG_TRY(galloc(G, (void **)&g.prmT, NPARAM * 4));
+  SG_TRY(galloc(G, (void **)&g.gtmp, NPARAM * 4));
+  GraphH *T = new GraphH();
+  G->twin = T;
+  T->c = G->c;
+  Graph &tg = T->g;
+  tg.n = g.n;
+  tg.nnzb = g.nnzb;
+  tg.rowptr = g.rowptr;
+  tg.colidx = g.colidx;
+  tg.vals = g.vals;
+  tg.vdt = g.vdt;
+  tg.a = g.a;
+  tg.dinv = g.dinv;
+  tg.linv = g.linv;
+  tg.lin = 1;
+  SG_TRY(alloc_layers(T));
+  SG_TRY(galloc(T, (void **)&tg.y, n * 3 * 4));
+  SG_TRY(galloc(T, (void **)&tg.dres, 64));
+  return graph_refresh(G);
 }
 
 static int graph_init(Ctx *c, const sg_matrix *A, GraphH *G) {
@@ -221,12 +285,7 @@ static int graph_init(Ctx *c, const sg_matrix *A, GraphH *G) {
   const size_t n = (size_t)A->n;
   SG_TRY(galloc(G, (void **)&g.a, A->nnzb * 4));
   SG_TRY(galloc(G, (void **)&g.dinv, n * 9 * 4));
-  SG_TRY(galloc(G, (void **)&g.s, n * 3 * 4));
-  SG_TRY(galloc(G, (void **)&g.m1, n * 3 * 4));
-  SG_TRY(galloc(G, (void **)&g.q2, n * K * 4));
-  SG_TRY(galloc(G, (void **)&g.m2, n * K * 4));
-  SG_TRY(galloc(G, (void **)&g.q3, n * K * 4));
-  SG_TRY(galloc(G, (void **)&g.m3, n * K * 4));
+  SG_TRY(alloc_layers(G));
   SG_TRY(galloc(G, (void **)&g.dres, 64));
   static bool attr = false;
   if (!attr) {
@@ -252,26 +311,53 @@ static int ensure_train(GraphH *G) {
   return SG_OK;
 }
 
-// Forward on stream st; ctl may be null (standalone) or the solver control.
-static int forward(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, const float *prm,
-                   const float *r, float *z, bool train) {
+// The network's layers F2..F4 on input s (already staged): out = s + Wout h3.
+// wx/tout: the extra projection of the transposed network's pass.
+static int layers(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, const float *prm,
+                  const float *s, float *out, bool train, const float *wx = nullptr,
+                  float *tout = nullptr) {
   Ctx *c = G->c;
   Graph &g = G->g;
   const int gv = grid_for(c, g.n, 256, 8);
-  k_f1<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.dinv, r, g.s, z);
-  SG_CHECK_LAUNCH();
-  k_f2<<<gv, 256, 0, st>>>(ctl, gate, g.lin, g.n, g.rowptr, g.colidx, g.a, prm, g.s, g.m1, g.q2,
+  const int lin = g.lin | (g.sym ? 2 : 0);
+  k_f2<<<gv, 256, 0, st>>>(ctl, gate, lin, g.n, g.rowptr, g.colidx, g.a, prm, s, g.m1, g.q2,
                            train ? g.g1 : nullptr);
   SG_CHECK_LAUNCH();
   const int64_t ntile = ((int64_t)g.n + 15) / 16;
   int gt = (int)((ntile + TC_WARPS - 1) / TC_WARPS);
   const int cap = c->num_sms * 4;
   if (gt > cap) gt = cap;
-  k_f3<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.lin, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
+  k_f3<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, lin, g.n, g.rowptr, g.colidx, g.a, prm, s,
                                                    g.m1, g.q2, g.m2, g.q3, train ? g.g2 : nullptr);
   SG_CHECK_LAUNCH();
-  k_f4<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, g.lin, g.n, g.rowptr, g.colidx, g.a, prm, g.s,
-                                                   g.m1, g.m2, g.q3, g.m3, z, train ? g.g3 : nullptr);
+  k_f4<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, lin, g.n, g.rowptr, g.colidx, g.a, prm, s,
+                                                   g.m1, g.m2, g.q3, g.m3, out, train ? g.g3 : nullptr,
+                                                   wx, tout);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+// Forward on stream st; ctl may be null (standalone) or the solver control.
+// Symmetric form: y = (I + N) L^-1 r on this graph's buffers (training
+// activations kept when train), then the transposed network on the twin's
+// buffers, then z = L^-T (wp + sum_u a_vu t_u).
+static int forward(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, const float *prm,
+                   const float *r, float *z, bool train) {
+  Ctx *c = G->c;
+  Graph &g = G->g;
+  const int gv = grid_for(c, g.n, 256, 8);
+  if (!g.sym) {
+    k_f1<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.dinv, r, g.s, z);
+    SG_CHECK_LAUNCH();
+    return layers(G, st, ctl, gate, prm, g.s, z, train);
+  }
+  k_f1<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.linv, r, g.s, nullptr);
+  SG_CHECK_LAUNCH();
+  SG_TRY(layers(G, st, ctl, gate, prm, g.s, g.y, train));
+  k_transpose_params<<<(NPARAM + 255) / 256, 256, 0, st>>>(prm, g.prmT);
+  SG_CHECK_LAUNCH();
+  SG_TRY(layers(G->twin, st, ctl, gate, g.prmT, g.y, g.wp, false, prm, g.t));
+  k_sym_out<<<gv, 256, 0, st>>>(ctl, gate, g.n, g.rowptr, g.colidx, g.a, g.linv, g.wp, g.t, g.s, z);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
@@ -286,7 +372,30 @@ static int outer(GraphH *G, const float *X, int O, const float *Y, int I, int yt
   return SG_OK;
 }
 
+static int backward_net(GraphH *G, const float *prm, const float *dz, float *grad);
+
+// Weight gradient of <dz, M r>.  Symmetric form: the network's gradient at
+// input L^-1 r with cotangent (I + N) L^-1 dz, plus its gradient at input
+// L^-1 dz with cotangent y = (I + N) L^-1 r; the second forward runs on the
+// twin's buffers so the first pass's activations survive.
 static int backward(GraphH *G, const float *prm, const float *dz, float *grad) {
+  Graph &g = G->g;
+  if (!g.sym) return backward_net(G, prm, dz, grad);
+  GraphH *T = G->twin;
+  Ctx *c = G->c;
+  SG_TRY(ensure_train(T));
+  const int gv = grid_for(c, g.n, 256, 8);
+  k_f1<<<gv, 256, 0, c->stream>>>(nullptr, 0, g.n, g.linv, dz, T->g.s, nullptr);
+  SG_CHECK_LAUNCH();
+  SG_TRY(layers(T, c->stream, nullptr, 0, prm, T->g.s, T->g.y, true));
+  SG_TRY(backward_net(G, prm, T->g.y, grad));
+  SG_TRY(backward_net(T, prm, g.y, g.gtmp));
+  k_add_f<<<(NPARAM + 255) / 256, 256, 0, c->stream>>>(NPARAM, grad, g.gtmp);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+static int backward_net(GraphH *G, const float *prm, const float *dz, float *grad) {
   Ctx *c = G->c;
   Graph &g = G->g;
   SG_TRY(ensure_train(G));
@@ -301,7 +410,8 @@ static int backward(GraphH *G, const float *prm, const float *dz, float *grad) {
                              g.dq2, g.dg1, nullptr, nullptr);
   SG_CHECK_LAUNCH();
   // weight gradients; h = act(g) (relu, or identity in the linear variant)
-  const int A_ = g.lin ? 0 : 1, AB = g.lin ? 4 : 2;
+  // the tensor-core operand is bf16(h), or ~h itself with split activations
+  const int A_ = g.lin ? 0 : 1, AB = g.sym ? 0 : (g.lin ? 4 : 2);
   SG_TRY(outer(G, dz, 3, g.g3, H, A_, grad + O_WOUT));
   SG_TRY(outer(G, g.dg3, H, g.g2, H, AB, grad + O_W3H));
   SG_TRY(outer(G, g.dg3, H, g.m3, K, 0, grad + O_W3M));
@@ -358,16 +468,13 @@ static int learned_apply(Solver *S, cudaStream_t st) {
 static void learned_free(Solver *S) {
   LearnedExt *L = (LearnedExt *)S->ext;
   if (!L) return;
-  if (L->G) {
-    for (void *p : L->G->allocs) cudaFree(p);
-    delete L->G;
-  }
+  mpnn::graph_free(L->G);
   delete L;
   S->ext = nullptr;
 }
 
 static const float *g_pending_params = nullptr;
-static int g_pending_linear = 0;
+static int g_pending_form = 0;
 static int learned_setup(Solver *S) {
   LearnedExt *L = new LearnedExt();
   S->ext = L;
@@ -375,7 +482,8 @@ static int learned_setup(Solver *S) {
   L->prm = g_pending_params;
   L->G = new mpnn::GraphH();
   SG_TRY(mpnn::graph_init(S->c, &S->A, L->G));
-  L->G->g.lin = g_pending_linear;
+  SG_TRY(mpnn::set_sym(L->G, g_pending_form == SG_MPNN_SYM));
+  L->G->g.lin = g_pending_form != SG_MPNN_RELU;
   S->ext_prec = learned_prec;
   S->ext_prec_apply = learned_apply;
   S->flexible = 1;
@@ -390,7 +498,7 @@ int learned_refresh(Solver *S) {
 int learned_solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, const float *params,
                         Solver *S) {
   g_pending_params = params;
-  g_pending_linear = o->learned_linear;
+  g_pending_form = o->learned_form;
   int rc = solver_init(c, A, o, S, learned_setup);
   g_pending_params = nullptr;
   return rc;
@@ -410,8 +518,7 @@ int sg_mpnn_graph_create(sg_ctx *h, const sg_matrix *A, sg_mpnn_graph **out) {
   mpnn::GraphH *G = new mpnn::GraphH();
   int rc = mpnn::graph_init(c, A, G);
   if (rc != SG_OK) {
-    for (void *p : G->allocs) cudaFree(p);
-    delete G;
+    mpnn::graph_free(G);
     return rc;
   }
   ctx_retain(c);
@@ -419,10 +526,12 @@ int sg_mpnn_graph_create(sg_ctx *h, const sg_matrix *A, sg_mpnn_graph **out) {
   return SG_OK;
 }
 
-int sg_mpnn_graph_set_linear(sg_mpnn_graph *hg, int linear) {
+int sg_mpnn_graph_set_form(sg_mpnn_graph *hg, int form) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
-  SG_REQUIRE(G, "sg_mpnn_graph_set_linear: null graph");
-  G->g.lin = linear ? 1 : 0;
+  SG_REQUIRE(G, "sg_mpnn_graph_set_form: null graph");
+  SG_REQUIRE(form >= SG_MPNN_RELU && form <= SG_MPNN_SYM, "sg_mpnn_graph_set_form: form %d", form);
+  SG_TRY(mpnn::set_sym(G, form == SG_MPNN_SYM));
+  G->g.lin = form != SG_MPNN_RELU;
   return SG_OK;
 }
 
@@ -436,9 +545,8 @@ int sg_mpnn_graph_destroy(sg_mpnn_graph *hg) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
   if (!G) return SG_OK;
   cudaStreamSynchronize(G->c->stream);
-  for (void *p : G->allocs) cudaFree(p);
   Ctx *c = G->c;
-  delete G;
+  mpnn::graph_free(G);
   ctx_release(c);
   return SG_OK;
 }

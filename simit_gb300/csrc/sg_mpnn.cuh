@@ -9,6 +9,8 @@
 //   q3   = P3 h2;  m3_v = sum a_vu q3_u
 //   g3   = W3h bf16(h2) + W3m m3, h3 = relu(g3)            (64)
 //   z    = s + Wout h3
+// (identity activations in the linear form; see Graph::sym for the
+// symmetric factorized form built from the linear network)
 // a_vu = ||A_vu||_F / sqrt(||A_vv||_F ||A_uu||_F) on the matrix pattern
 // (0 on the diagonal).  W2h and W3h are bf16 tensor-core operands (mma.sync
 // m16n8k16, FP32 accumulate); everything else is FP32.  No biases, so the
@@ -55,6 +57,14 @@ struct Graph {
   float *ld = nullptr, *lq = nullptr;  // loss temporaries
   double *dres = nullptr;
   int lin = 0;  // identity activations (a linear preconditioner) instead of relu
+  // Symmetric factorized form M = L^-T (I+N)^T (I+N) L^-1 (sym = 1, lin = 1):
+  // L^-1 per vertex, y = (I+N) L^-1 r, the transposed network's outputs
+  // wp = y + W1s^T h3' and t = W1m^T h3', transposed parameters, and a
+  // gradient buffer for the second weight-gradient pass.
+  int sym = 0;
+  float *linv = nullptr;   // [n*9]
+  float *y = nullptr, *wp = nullptr, *t = nullptr;  // [n*3]
+  float *prmT = nullptr, *gtmp = nullptr;           // [NPARAM]
 };
 
 __device__ __forceinline__ float bf16r(float x) {

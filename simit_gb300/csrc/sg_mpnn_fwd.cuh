@@ -66,7 +66,7 @@ __global__ void k_f1(const SolveCtl *ctl, int gate, int32_t n, const float *__re
     for (int k = 0; k < 3; ++k) {
       const float sk = D[k * 3] * r0 + D[k * 3 + 1] * r1 + D[k * 3 + 2] * r2;
       s[v * 3 + k] = sk;
-      if (fb) z[v * 3 + k] = sk;
+      if (fb && z) z[v * 3 + k] = sk;
     }
   }
 }
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(256) k_f2(const SolveCtl *ctl, int gate, int l
       const float g = w.w1s[h * 3] * s0 + w.w1s[h * 3 + 1] * s1 + w.w1s[h * 3 + 2] * s2 +
                       w.w1m[h * 3] * mm0 + w.w1m[h * 3 + 1] * mm1 + w.w1m[h * 3 + 2] * mm2;
       if (g1) g1[v * H + h] = g;
-      const float hv = lin ? g : fmaxf(g, 0.f);
+      const float hv = (lin & 1) ? g : fmaxf(g, 0.f);
 #pragma unroll
       for (int j = 0; j < K; ++j) qq[j] += w.p2[j * H + h] * hv;
     }
@@ -125,6 +125,10 @@ __global__ void __launch_bounds__(256) k_f2(const SolveCtl *ctl, int gate, int l
 // ---------------------------------------------------------------------------
 // F3 / F4: a warp owns 16 consecutive vertices; the 64x64 layers run on the
 // tensor cores (mma.sync m16n8k16, bf16 operands, FP32 accumulators).
+// lin: bit 0 identity activations; bit 1 split activations (the symmetric
+// form): h = bf16(h) + bf16(h - bf16(h)), two products with the same bf16
+// weights, so the layer is linear to about 2^-16 and the preconditioner
+// stays a fixed symmetric operator to that accuracy.
 // ---------------------------------------------------------------------------
 constexpr int TC_WARPS = 4;
 constexpr int HP = H + 8;  // padded bf16 row (36 words: conflict-free fragments)
@@ -163,10 +167,13 @@ struct TCW {
   __nv_bfloat16 w2h[H * HP];
   __nv_bfloat16 w3h[H * HP];
   float w1s[H * 3], w1m[H * 3], w2m[H * K], w3m[H * K], p3[K * H], wout[3 * H];
+  float wx[3 * H];  // extra output projection (F4 of the transposed network)
 };
 struct TCWarp {
   __nv_bfloat16 x1[16 * HP];
   __nv_bfloat16 x2[16 * HP];
+  __nv_bfloat16 x1lo[16 * HP];  // split activations: bf16(h - bf16(h))
+  __nv_bfloat16 x2lo[16 * HP];
   float mA[16 * K];  // m2 (F3) or m3 (F4)
   float mB[16 * K];  // m2 (F4)
   float sv[16 * 3], m1v[16 * 3];
@@ -228,7 +235,10 @@ __device__ __forceinline__ void tc_prologue(const TCW &w, TCWarp &tw, int lin, i
     for (int h = h0; h < h0 + 32; ++h) {
       const float g = w.w1s[h * 3] * sv[0] + w.w1s[h * 3 + 1] * sv[1] + w.w1s[h * 3 + 2] * sv[2] +
                       w.w1m[h * 3] * mv[0] + w.w1m[h * 3 + 1] * mv[1] + w.w1m[h * 3 + 2] * mv[2];
-      tw.x1[vi * HP + h] = __float2bfloat16_rn(lin ? g : fmaxf(g, 0.f));
+      const float hv = (lin & 1) ? g : fmaxf(g, 0.f);
+      const __nv_bfloat16 hi = __float2bfloat16_rn(hv);
+      tw.x1[vi * HP + h] = hi;
+      if (lin & 2) tw.x1lo[vi * HP + h] = __float2bfloat16_rn(hv - __bfloat162float(hi));
     }
   }
   __syncwarp();
@@ -249,7 +259,7 @@ __device__ __forceinline__ void tc_layer_epilogue(float acc[8][4], const float *
 #pragma unroll
       for (int j = 0; j < K; ++j) gsum += Wm[col * K + j] * msrc[row * K + j];
       if (g_out && v0 + row < n) g_out[(v0 + row) * H + col] = gsum;
-      acc[nt][e] = lin ? gsum : fmaxf(gsum, 0.f);
+      acc[nt][e] = (lin & 1) ? gsum : fmaxf(gsum, 0.f);
     }
 }
 
@@ -280,6 +290,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
     gemm16x64(tw.x1, w.w2h, acc);
+    if (lin & 2) gemm16x64(tw.x1lo, w.w2h, acc);
     tc_layer_epilogue(acc, w.w2m, tw.mA, v0, n, g2, lin);
     // q3[row][j] = sum_n P3[j][n] h2[row][n]: quad partials then shuffles
     float qa[K], qb[K];
@@ -314,19 +325,26 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 }
 
 // F4: m3 = sum a q3_u; h2 = relu(W2h bf16(h1) + W2m m2); g3 = W3h bf16(h2) +
-// W3m m3; h3 = relu(g3); z = s + Wout h3.
+// W3m m3; h3 = relu(g3); z = s + Wout h3.  With wx_prm (the untransposed
+// parameters, for the transposed network) also tout = W1m^T h3.
 __global__ void __launch_bounds__(TC_WARPS * 32)
     k_f4(const SolveCtl *ctl, int gate, int lin, int32_t n, const uint32_t *__restrict__ rowptr,
          const uint32_t *__restrict__ colidx, const float *__restrict__ a,
          const float *__restrict__ prm, const float *__restrict__ s,
          const float *__restrict__ m1, const float *__restrict__ m2,
          const float *__restrict__ q3, float *__restrict__ m3, float *__restrict__ z,
-         float *__restrict__ g3) {
+         float *__restrict__ g3, const float *__restrict__ wx_prm = nullptr,
+         float *__restrict__ tout = nullptr) {
   if (ctl && ((gate && ctl->status != ST_RUNNING) || ctl->fallback)) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   TCW &w = *reinterpret_cast<TCW *>(smraw);
   TCWarp &tw = reinterpret_cast<TCWarp *>(smraw + sizeof(TCW))[threadIdx.x >> 5];
   load_tc_weights(w, prm, true);
+  if (wx_prm)
+    for (int i = threadIdx.x; i < 3 * H; i += blockDim.x) {
+      const int k = i / H, h = i % H;
+      w.wx[i] = wx_prm[O_W1M + h * 3 + k];
+    }
   __syncthreads();
   const int lane = threadIdx.x & 31, gid = lane >> 2, t = lane & 3;
   const int64_t ntile = ((int64_t)n + 15) / 16;
@@ -346,6 +364,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
     gemm16x64(tw.x1, w.w2h, acc);
+    if (lin & 2) gemm16x64(tw.x1lo, w.w2h, acc);
     tc_layer_epilogue(acc, w.w2m, tw.mB, v0, n, nullptr, lin);
     // h2 -> bf16 tile x2
 #pragma unroll
@@ -353,7 +372,9 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const int row = gid + (e >> 1) * 8, col = nt * 8 + 2 * t + (e & 1);
-        tw.x2[row * HP + col] = __float2bfloat16_rn(acc[nt][e]);
+        const __nv_bfloat16 hi = __float2bfloat16_rn(acc[nt][e]);
+        tw.x2[row * HP + col] = hi;
+        if (lin & 2) tw.x2lo[row * HP + col] = __float2bfloat16_rn(acc[nt][e] - __bfloat162float(hi));
       }
     __syncwarp();
 #pragma unroll
@@ -361,6 +382,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
       for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
     gemm16x64(tw.x2, w.w3h, acc);
+    if (lin & 2) gemm16x64(tw.x2lo, w.w3h, acc);
     tc_layer_epilogue(acc, w.w3m, tw.mA, v0, n, g3, lin);
     float za[3], zb[3];
 #pragma unroll
@@ -389,8 +411,136 @@ __global__ void __launch_bounds__(TC_WARPS * 32)
 #pragma unroll
         for (int k = 0; k < 3; ++k) z[(v0 + gid + 8) * 3 + k] = tw.sv[(gid + 8) * 3 + k] + zb[k];
     }
+    if (wx_prm) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float pa = 0.f, pb = 0.f;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int col = nt * 8 + 2 * t + e;
+            pa += w.wx[k * H + col] * acc[nt][e];
+            pb += w.wx[k * H + col] * acc[nt][2 + e];
+          }
+        pa += __shfl_xor_sync(0xffffffffu, pa, 1);
+        pa += __shfl_xor_sync(0xffffffffu, pa, 2);
+        pb += __shfl_xor_sync(0xffffffffu, pb, 1);
+        pb += __shfl_xor_sync(0xffffffffu, pb, 2);
+        za[k] = pa;
+        zb[k] = pb;
+      }
+      if (t == 0) {
+        if (v0 + gid < n)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) tout[(v0 + gid) * 3 + k] = za[k];
+        if (v0 + gid + 8 < n)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) tout[(v0 + gid + 8) * 3 + k] = zb[k];
+      }
+    }
     __syncwarp();
   }
+}
+
+// ---------------------------------------------------------------------------
+// Symmetric factorized form
+// ---------------------------------------------------------------------------
+// L_v^-1 (row-major 3x3, lower triangular) with D_v = L_v L_v^T, in FP64
+// from the lower triangle of the diagonal block.  A block that is not
+// positive definite gets diag(1/sqrt|d_kk|) (0 for d_kk = 0).
+template <typename MT>
+__global__ void k_chol_inv(int32_t n, const uint32_t *rowptr, const uint32_t *colidx,
+                           const MT *vals, float *linv) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t lo = rowptr[v], hi = rowptr[v + 1];
+    const uint32_t end = hi;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (colidx[mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
+    }
+    double d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (lo < end && colidx[lo] == (uint32_t)v)
+      for (int k = 0; k < 9; ++k) d[k] = (double)vals[(size_t)lo * 9 + k];
+    double x[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const double l00 = sqrt(d[0]);
+    const double l10 = d[3] / l00, l20 = d[6] / l00;
+    const double t11 = d[4] - l10 * l10;
+    const double l11 = sqrt(t11);
+    const double l21 = (d[7] - l20 * l10) / l11;
+    const double t22 = d[8] - l20 * l20 - l21 * l21;
+    const double l22 = sqrt(t22);
+    if (d[0] > 0 && t11 > 0 && t22 > 0 && isfinite(l22)) {
+      // solve L X = I column by column
+      x[0] = 1.0 / l00;
+      x[3] = -l10 * x[0] / l11;
+      x[6] = -(l20 * x[0] + l21 * x[3]) / l22;
+      x[4] = 1.0 / l11;
+      x[7] = -l21 * x[4] / l22;
+      x[8] = 1.0 / l22;
+    } else {
+      for (int k = 0; k < 3; ++k) {
+        const double a = fabs(d[k * 4]);
+        x[k * 4] = a > 0 ? 1.0 / sqrt(a) : 0.0;
+      }
+    }
+    for (int k = 0; k < 9; ++k) linv[(size_t)v * 9 + k] = (float)x[k];
+  }
+}
+
+// Parameters of the transposed network (same flat layout): layer 1 <- Wout^T
+// with no message, layer 2 <- layer 3 transposed, layer 3 <- layer 2
+// transposed, output <- W1s^T.
+__global__ void k_transpose_params(const float *__restrict__ p, float *__restrict__ q) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NPARAM; i += gridDim.x * blockDim.x) {
+    float v;
+    if (i < O_W1M) { const int h = (i - O_W1S) / 3, k = (i - O_W1S) % 3; v = p[O_WOUT + k * H + h]; }
+    else if (i < O_P2) v = 0.f;
+    else if (i < O_W2H) { const int j = (i - O_P2) / H, h = (i - O_P2) % H; v = p[O_W3M + h * K + j]; }
+    else if (i < O_W2M) { const int r = (i - O_W2H) / H, c = (i - O_W2H) % H; v = p[O_W3H + c * H + r]; }
+    else if (i < O_P3) { const int h = (i - O_W2M) / K, j = (i - O_W2M) % K; v = p[O_P3 + j * H + h]; }
+    else if (i < O_W3H) { const int j = (i - O_P3) / H, h = (i - O_P3) % H; v = p[O_W2M + h * K + j]; }
+    else if (i < O_W3M) { const int r = (i - O_W3H) / H, c = (i - O_W3H) % H; v = p[O_W2H + c * H + r]; }
+    else if (i < O_WOUT) { const int h = (i - O_W3M) / K, j = (i - O_W3M) % K; v = p[O_P2 + j * H + h]; }
+    else { const int k = (i - O_WOUT) / H, h = (i - O_WOUT) % H; v = p[O_W1S + h * 3 + k]; }
+    q[i] = v;
+  }
+}
+
+// z_v = L_v^-T (wp_v + sum_u a_vu t_u); after a fallback z_v = L_v^-T s_v
+// (= D_v^-1 r_v, block Jacobi).
+__global__ void k_sym_out(const SolveCtl *ctl, int gate, int32_t n,
+                          const uint32_t *__restrict__ rowptr, const uint32_t *__restrict__ colidx,
+                          const float *__restrict__ a, const float *__restrict__ linv,
+                          const float *__restrict__ wp, const float *__restrict__ t,
+                          const float *__restrict__ s, float *__restrict__ z) {
+  if (ctl && gate && ctl->status != ST_RUNNING) return;
+  const bool fb = ctl && ctl->fallback;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    float w0, w1, w2;
+    if (fb) {
+      w0 = s[v * 3]; w1 = s[v * 3 + 1]; w2 = s[v * 3 + 2];
+    } else {
+      w0 = wp[v * 3]; w1 = wp[v * 3 + 1]; w2 = wp[v * 3 + 2];
+      for (uint32_t q = rowptr[v]; q < rowptr[v + 1]; ++q) {
+        const float aq = a[q];
+        const uint32_t u = colidx[q];
+        w0 += aq * t[(size_t)u * 3];
+        w1 += aq * t[(size_t)u * 3 + 1];
+        w2 += aq * t[(size_t)u * 3 + 2];
+      }
+    }
+    const float *Li = linv + (size_t)v * 9;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) z[v * 3 + k] = Li[k] * w0 + Li[3 + k] * w1 + Li[6 + k] * w2;
+  }
+}
+
+__global__ void k_add_f(int n, float *__restrict__ a, const float *__restrict__ b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    a[i] += b[i];
 }
 
 inline size_t tc_smem_bytes() { return sizeof(TCW) + TC_WARPS * sizeof(TCWarp); }

@@ -135,11 +135,29 @@ static int launch_k1(Solver *S, cudaStream_t st) {
   return SG_OK;
 }
 
+template <int PREC>
+static void launch_k2_v4(Solver *S, cudaStream_t st, int par) {
+  k_cg_update_v4<PREC><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part1, S->P1,
+                                                (const float *)S->p, (const float *)S->q,
+                                                (float *)S->r, (float *)S->xupd, (float *)S->z,
+                                                (const float *)S->dinv, S->part2);
+}
+
 template <typename VT, typename XT>
 static int launch_k2(Solver *S, cudaStream_t st, int par) {
   const VT *p = (const VT *)S->p, *q = (const VT *)S->q, *dinv = (const VT *)S->dinv;
   VT *r = (VT *)S->r, *z = (VT *)S->z;
   XT *x = (XT *)S->xupd;
+  if (sizeof(VT) == 4 && sizeof(XT) == 4) {
+    switch (S->prec) {
+      case PK_NONE: launch_k2_v4<PK_NONE>(S, st, par); break;
+      case PK_JACOBI: launch_k2_v4<PK_JACOBI>(S, st, par); break;
+      case PK_BLOCK3: launch_k2_v4<PK_BLOCK3>(S, st, par); break;
+      default: launch_k2_v4<PK_EXTERNAL>(S, st, par); break;
+    }
+    SG_CHECK_LAUNCH();
+    return SG_OK;
+  }
   switch (S->prec) {
     case PK_NONE:
       k_cg_update<VT, XT, PK_NONE><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part1, S->P1,
@@ -165,7 +183,12 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
 template <typename VT>
 static int launch_k3(Solver *S, cudaStream_t st, int par) {
   const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
-  k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z, (VT *)S->p);
+  if (sizeof(VT) == 4)
+    k_cg_direction_v4<<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2,
+                                               (const float *)z, (float *)S->p);
+  else
+    k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z,
+                                                (VT *)S->p);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
@@ -560,7 +583,7 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   // (unless a lane count is forced), else G lanes per row.
   const bool aligned = ((uintptr_t)A->vals % 16 == 0) && ((uintptr_t)A->colidx % 16 == 0);
   if (A->bs == 3 && aligned && (o->lanes < 0 || (o->lanes == 0 && S->kind != KIND_F64))) {
-    SG_TRY(cached_stats(c, A->n, A->rowptr, &S->pstats));
+    SG_TRY(cached_stats(c, A->n, A->rowptr, &S->pstats, true));
     S->maxrow = S->pstats.maxrow;
     S->tma_var = o->lanes < 0 ? -o->lanes - 1 : 0;
     const int vdt = (S->kind == KIND_F64) ? SG_F64 : SG_F32;

@@ -247,6 +247,178 @@ __global__ void __launch_bounds__(RED_T) k_cg_direction(SolveCtl *ctl, int par, 
 }
 
 // ---------------------------------------------------------------------------
+// FP32 (mixed-precision) K2 / K3 with 16-byte loads and stores.  One thread
+// takes four vertices at a time: three float4 of each vector and nine of the
+// block-Jacobi inverse, all contiguous across the warp.  The buffers are
+// cudaMalloc'd (256-byte aligned); the last len % 12 (or len % 4) entries go
+// through the scalar loop of thread 0 of the last block.  Same partial sums
+// as the scalar kernels, in a different (fixed) order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void ld4(const float *p, int64_t i, float *o) {
+  const float4 v = reinterpret_cast<const float4 *>(p)[i];
+  o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void st4(float *p, int64_t i, const float *o) {
+  reinterpret_cast<float4 *>(p)[i] = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(RED_T) k_cg_update_v4(SolveCtl *ctl, int par, int64_t len,
+                                                        const double *__restrict__ part_in,
+                                                        int np1, const float *__restrict__ p,
+                                                        const float *__restrict__ q,
+                                                        float *__restrict__ r,
+                                                        float *__restrict__ x,
+                                                        float *__restrict__ z,
+                                                        const float *__restrict__ dinv,
+                                                        double *__restrict__ part_out) {
+  __shared__ double sh[33];
+  if (ctl->status != ST_RUNNING) return;
+  const double pq = sum_parts(part_in, np1, sh);
+  const double rz = ctl->rz[par];
+  if (!(pq > 0.0) || !isfinite(pq)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
+    return;
+  }
+  const double alpha = rz / pq;
+  const float a = (float)alpha;
+  double rr = 0, rzs = 0, zq = 0;
+  constexpr int W = PREC == PK_BLOCK3 ? 12 : 4;  // floats per thread step
+  constexpr int NV = W / 4;                      // float4 per vector
+  const int64_t nu = len / W;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    float pv[W], qv[W], rv[W], xv[W], zv[W];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      ld4(p, u * NV + k, pv + 4 * k);
+      ld4(q, u * NV + k, qv + 4 * k);
+      ld4(r, u * NV + k, rv + 4 * k);
+      ld4(x, u * NV + k, xv + 4 * k);
+    }
+    float dv[PREC == PK_BLOCK3 ? 36 : (PREC == PK_JACOBI ? 4 : 1)];
+    if (PREC == PK_BLOCK3) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) ld4(dinv, u * 9 + k, dv + 4 * k);
+    } else if (PREC == PK_JACOBI) {
+      ld4(dinv, u, dv);
+    }
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      xv[k] = xv[k] + a * pv[k];
+      rv[k] = rv[k] - a * qv[k];
+    }
+    if (PREC == PK_BLOCK3) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          zv[v * 3 + k] = dv[v * 9 + k * 3] * rv[v * 3] + dv[v * 9 + k * 3 + 1] * rv[v * 3 + 1] +
+                          dv[v * 9 + k * 3 + 2] * rv[v * 3 + 2];
+    } else {
+#pragma unroll
+      for (int k = 0; k < W; ++k) zv[k] = PREC == PK_JACOBI ? dv[k] * rv[k] : rv[k];
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      st4(x, u * NV + k, xv + 4 * k);
+      st4(r, u * NV + k, rv + 4 * k);
+      if (PREC == PK_BLOCK3 || PREC == PK_JACOBI) st4(z, u * NV + k, zv + 4 * k);
+    }
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      rr += (double)rv[k] * (double)rv[k];
+      if (PREC != PK_EXTERNAL) {
+        rzs += (double)rv[k] * (double)zv[k];
+        zq += (double)zv[k] * (double)qv[k];
+      }
+    }
+  }
+  // tail: the last len % W entries, scalar, by one thread
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    for (int64_t i0 = nu * W; i0 < len; i0 += (PREC == PK_BLOCK3 ? 3 : 1)) {
+      const int m = PREC == PK_BLOCK3 ? 3 : 1;
+      float rv[3], zv[3];
+      for (int k = 0; k < m; ++k) {
+        const int64_t i = i0 + k;
+        x[i] = x[i] + a * p[i];
+        rv[k] = r[i] - a * q[i];
+        r[i] = rv[k];
+      }
+      for (int k = 0; k < m; ++k) {
+        const int64_t i = i0 + k;
+        if (PREC == PK_BLOCK3) {
+          const float *D = dinv + (i0 / 3) * 9;
+          zv[k] = D[k * 3] * rv[0] + D[k * 3 + 1] * rv[1] + D[k * 3 + 2] * rv[2];
+        } else {
+          zv[k] = PREC == PK_JACOBI ? dinv[i] * rv[k] : rv[k];
+        }
+        if (PREC == PK_BLOCK3 || PREC == PK_JACOBI) z[i] = zv[k];
+        rr += (double)rv[k] * (double)rv[k];
+        if (PREC != PK_EXTERNAL) {
+          rzs += (double)rv[k] * (double)zv[k];
+          zq += (double)zv[k] * (double)q[i];
+        }
+      }
+    }
+  }
+  const double t0 = block_sum(rr, sh);
+  const double t1 = block_sum(rzs, sh);
+  const double t2 = block_sum(zq, sh);
+  if (threadIdx.x == 0) {
+    part_out[blockIdx.x] = t0;
+    part_out[gridDim.x + blockIdx.x] = t1;
+    part_out[2 * gridDim.x + blockIdx.x] = t2;
+    if (blockIdx.x == 0) ctl->last_alpha = alpha;
+  }
+}
+
+// K3 for FP32 vectors: the control decisions of k_cg_direction, then
+// p = z + beta p with float4 accesses.
+static __global__ void __launch_bounds__(RED_T) k_cg_direction_v4(SolveCtl *ctl, int par, int64_t len,
+                                                           const double *__restrict__ part_in,
+                                                           int np2, const float *__restrict__ z,
+                                                           float *__restrict__ p) {
+  __shared__ double sh[33];
+  if (ctl->status != ST_RUNNING) return;
+  const double rr = sum_parts(part_in, np2, sh);
+  const double rznew = sum_parts(part_in + np2, np2, sh);
+  const double zq = sum_parts(part_in + 2 * np2, np2, sh);
+  const double rzold = ctl->rz[par];
+  const int it = ctl->iter[par] + 1;
+  int st = ST_RUNNING;
+  const bool lost = ctl->flexible && !ctl->fallback && !(rznew > 0.0);
+  if (lost) st = ST_NEED_CHECK;
+  else if (!isfinite(rr) || !isfinite(rznew)) st = ST_NAN;
+  else if (rr <= ctl->tol2) st = ST_NEED_CHECK;
+  else if (ctl->upd2 > 0.0 && rr < ctl->upd2) st = ST_NEED_CHECK;
+  else if (ctl->check_every > 0 && it % ctl->check_every == 0) st = ST_NEED_CHECK;
+  else if (it >= ctl->maxiters) st = ST_MAXITER;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->iter[par ^ 1] = it;
+    ctl->rz[par ^ 1] = rznew;
+    ctl->last_rr = rr;
+    if (lost) ctl->fallback = 1;
+    if (st != ST_RUNNING) ctl->status = st;
+  }
+  if (st != ST_RUNNING) return;
+  const double beta = ctl->flexible ? (-ctl->last_alpha * zq) / rzold : rznew / rzold;
+  const float b = (float)beta;
+  const int64_t nu = len / 4;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    float zv[4], pv[4];
+    ld4(z, u, zv);
+    ld4(p, u, pv);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) pv[k] = zv[k] + b * pv[k];
+    st4(p, u, pv);
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+    for (int64_t i = nu * 4; i < len; ++i) p[i] = z[i] + b * p[i];
+}
+
+// ---------------------------------------------------------------------------
 // Set-up / check kernels
 // ---------------------------------------------------------------------------
 

@@ -6,20 +6,25 @@
 
 namespace sg {
 
-// TMA SpMV variants: (lanes per block row, rows per tile, pipeline stages).
-// Variant 0 is the default.
+// TMA SpMV variants: (lanes per block row, rows per CTA tile, pipeline
+// stages); ROWS = 0 selects the per-warp pipeline (tiles of 32/G rows per
+// warp).  Variant 0 is the default.
 struct TmaVariant {
   int G, ROWS, NST;
 };
 static const TmaVariant kTmaVariants[] = {
     {8, 32, 2}, {8, 32, 3}, {8, 16, 4}, {4, 32, 3}, {16, 16, 4}, {8, 16, 2},
+    {8, 0, 2},  {8, 0, 3},  {8, 0, 4},  {4, 0, 2},  {4, 0, 3},
 };
 constexpr int kNumTmaVariants = sizeof(kTmaVariants) / sizeof(kTmaVariants[0]);
 
 // Blocks in the largest tile of `rows` consecutive rows (the buffer size).
 static int tile_cap(int rows, const PatternStats &ps) {
   const int bound = rows * (ps.maxrow > 0 ? ps.maxrow : 1);
-  const int t = rows == 16 ? ps.tile16 : (rows == 32 ? ps.tile32 : 0);
+  const int t = rows == 16 ? ps.tile16
+              : rows == 32 ? ps.tile32
+              : rows == 4  ? ps.tile4
+              : rows == 8  ? ps.tile8 : 0;
   return (t > 0 && t < bound) ? t : bound;
 }
 
@@ -53,6 +58,38 @@ static int tma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n,
   return SG_OK;
 }
 
+template <int G, int NST, typename MT, typename VT, bool DOT>
+static int wtma_config_t(Ctx *c, int32_t n, const PatternStats &ps, int *grid, size_t *smem) {
+  const int rows = 32 / G;
+  const int capb = tile_cap(rows, ps);
+  const size_t sh = wtma_smem_bytes<MT>(capb, NST);
+  if (sh > 200 * 1024) return SG_ERR_UNSUPPORTED;
+  auto kern = k_bsr3_wtma<G, NST, MT, VT, DOT>;
+  SG_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  int per_sm = 0;
+  SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WTMA_WARPS * 32, sh));
+  if (per_sm < 1) return SG_ERR_UNSUPPORTED;
+  const int64_t ntiles = ((int64_t)n + rows - 1) / rows;
+  int64_t gsz = (int64_t)per_sm * c->num_sms;
+  const int64_t need = (ntiles + WTMA_WARPS - 1) / WTMA_WARPS;
+  if (gsz > need) gsz = need;
+  if (gsz < 1) gsz = 1;
+  *grid = (int)gsz;
+  *smem = sh;
+  return SG_OK;
+}
+
+template <int G, int NST, typename MT, typename VT, bool DOT>
+static int wtma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n,
+                         const uint32_t *rp, const uint32_t *ci, const MT *v, const VT *x, VT *y,
+                         double *part, const PatternStats &ps, int grid, size_t smem) {
+  const int capb = tile_cap(32 / G, ps);
+  k_bsr3_wtma<G, NST, MT, VT, DOT><<<grid, WTMA_WARPS * 32, smem, st>>>(ctl, n, rp, ci, v, x, y,
+                                                                       part, capb, c->d_err);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
 // Dispatch over (variant, dot) for one (MT, VT).
 template <typename MT, typename VT>
 static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
@@ -77,9 +114,26 @@ static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
     SG_V(3, 4, 32, 3)
     SG_V(4, 16, 16, 4)
     SG_V(5, 8, 16, 2)
+#define SG_W(ID, G, N)                                                                         \
+  case ID:                                                                                     \
+    if (launch)                                                                                \
+      return dot ? wtma_launch_t<G, N, MT, VT, true>(c, st, ctl, n, rp, ci, (const MT *)v,     \
+                                                     (const VT *)x, (VT *)y, part, ps, *grid,  \
+                                                     *smem)                                    \
+                 : wtma_launch_t<G, N, MT, VT, false>(c, st, ctl, n, rp, ci, (const MT *)v,    \
+                                                      (const VT *)x, (VT *)y, part, ps, *grid, \
+                                                      *smem);                                  \
+    return dot ? wtma_config_t<G, N, MT, VT, true>(c, n, ps, grid, smem)                       \
+               : wtma_config_t<G, N, MT, VT, false>(c, n, ps, grid, smem);
+    SG_W(6, 8, 2)
+    SG_W(7, 8, 3)
+    SG_W(8, 8, 4)
+    SG_W(9, 4, 2)
+    SG_W(10, 4, 3)
     default: return SG_ERR_ARG;
   }
 #undef SG_V
+#undef SG_W
 }
 
 static int tma_any(Ctx *c, cudaStream_t st, bool launch, int vdt, int xdt, int var, int dot,
@@ -115,50 +169,67 @@ int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, 
 
 // Longest row and largest 16- / 32-row tiles (blocks) of a pattern.
 __global__ void k_pattern_stats(const uint32_t *rowptr, int32_t n, uint32_t *out) {
-  uint32_t mr = 0, t16 = 0, t32 = 0;
+  uint32_t mr = 0, t16 = 0, t32 = 0, t4 = 0, t8 = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     mr = max(mr, rowptr[i + 1] - rowptr[i]);
     if (i % 16 == 0) t16 = max(t16, rowptr[min((int64_t)n, i + 16)] - rowptr[i]);
     if (i % 32 == 0) t32 = max(t32, rowptr[min((int64_t)n, i + 32)] - rowptr[i]);
+    if (i % 4 == 0) t4 = max(t4, rowptr[min((int64_t)n, i + 4)] - rowptr[i]);
+    if (i % 8 == 0) t8 = max(t8, rowptr[min((int64_t)n, i + 8)] - rowptr[i]);
   }
   for (int o = 16; o > 0; o >>= 1) {
     mr = max(mr, __shfl_down_sync(0xffffffffu, mr, o));
     t16 = max(t16, __shfl_down_sync(0xffffffffu, t16, o));
     t32 = max(t32, __shfl_down_sync(0xffffffffu, t32, o));
+    t4 = max(t4, __shfl_down_sync(0xffffffffu, t4, o));
+    t8 = max(t8, __shfl_down_sync(0xffffffffu, t8, o));
   }
   if ((threadIdx.x & 31) == 0) {
     atomicMax(&out[0], mr);
     atomicMax(&out[1], t16);
     atomicMax(&out[2], t32);
+    atomicMax(&out[3], t4);
+    atomicMax(&out[4], t8);
   }
 }
 
-int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps) {
+// Pattern statistics, cached per (rowptr, n).  The cache cannot see a new
+// pattern written at the same address, so callers that own a pattern for a
+// long time (the solver) pass refresh = true; the SpMV kernels never rely on
+// the statistics for memory safety (a tile larger than the buffers is read
+// straight from global memory).
+int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps, bool refresh) {
+  int slot = -1;
   for (int i = 0; i < Ctx::MAXROW_CACHE; ++i)
-    if (c->mr_ptr[i] == rowptr && c->mr_n[i] == n) {
-      ps->maxrow = c->mr_val[i];
-      ps->tile16 = c->mr_t16[i];
-      ps->tile32 = c->mr_t32[i];
-      return SG_OK;
-    }
+    if (c->mr_ptr[i] == rowptr && c->mr_n[i] == n) slot = i;
+  if (slot >= 0 && !refresh) {
+    ps->maxrow = c->mr_val[slot];
+    ps->tile16 = c->mr_t16[slot];
+    ps->tile32 = c->mr_t32[slot];
+    ps->tile4 = c->mr_t4[slot];
+    ps->tile8 = c->mr_t8[slot];
+    return SG_OK;
+  }
   Scratch s(c);
   SG_TRY(s.reserve(256));
-  uint32_t *d = s.alloc<uint32_t>(4);
-  SG_CHECK_CUDA(cudaMemsetAsync(d, 0, 16, c->stream));
+  uint32_t *d = s.alloc<uint32_t>(8);
+  SG_CHECK_CUDA(cudaMemsetAsync(d, 0, 32, c->stream));
   if (n > 0) {
     k_pattern_stats<<<grid_for(c, n, 256, 4), 256, 0, c->stream>>>(rowptr, n, d);
     SG_CHECK_LAUNCH();
   }
-  SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, d, 16, cudaMemcpyDeviceToHost, c->stream));
+  SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, d, 32, cudaMemcpyDeviceToHost, c->stream));
   SG_CHECK_CUDA(cudaStreamSynchronize(c->stream));
   const uint32_t *h = (const uint32_t *)c->h_stage;
-  const int slot = c->mr_next++ % Ctx::MAXROW_CACHE;
+  if (slot < 0) slot = c->mr_next++ % Ctx::MAXROW_CACHE;
   c->mr_ptr[slot] = rowptr;
   c->mr_n[slot] = n;
   c->mr_val[slot] = ps->maxrow = (int32_t)h[0];
   c->mr_t16[slot] = ps->tile16 = (int32_t)h[1];
   c->mr_t32[slot] = ps->tile32 = (int32_t)h[2];
+  c->mr_t4[slot] = ps->tile4 = (int32_t)h[3];
+  c->mr_t8[slot] = ps->tile8 = (int32_t)h[4];
   return SG_OK;
 }
 
@@ -339,6 +410,9 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
     if (bsr3_tma_config(c, vdt, xdt, var, 0, n, ps, &grid, &sh) == SG_OK)
       return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, var, 0, n, rowptr, colidx, vals, x,
                              y, nullptr, ps, grid, sh);
+    // the variant's buffers do not fit the largest tile (very long rows):
+    // the streaming G-lane kernel needs no staging
+    g = 0;
   }
   // nnzb is only needed for the default lane choice; read rowptr[n] then.
   int64_t nnzb = 0;

@@ -6,11 +6,12 @@
 namespace sg {
 struct Ctx;
 struct PatternStats {
-  int maxrow = 0, tile16 = 0, tile32 = 0;
+  int maxrow = 0, tile16 = 0, tile32 = 0, tile4 = 0, tile8 = 0;
 };
 int default_lanes(int32_t n, int64_t nnzb, int32_t bs);
 int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out);
-int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps);
+int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps,
+                 bool refresh = false);
 int bspmv_launch(Ctx *c, int32_t n, int32_t bs, const uint32_t *rp, const uint32_t *ci, int vdt,
                  const void *v, int xdt, const void *x, void *y, int g, int64_t nnzb_hint);
 // TMA-staged 3x3 SpMV: grid/shared-memory for variant `var` (0 = default;

@@ -28,7 +28,9 @@ template <typename MT> inline size_t tma_smem_bytes(int capb, int nst) {
 }
 
 // NST-stage pipeline: while the CTA computes tile k, the copies of tiles
-// k+1 .. k+NST-1 are in flight.
+// k+1 .. k+NST-1 are in flight.  A tile of more than capb blocks (the
+// buffers' capacity) is never staged: it is read straight from global
+// memory, so a stale tile statistic costs speed, never memory safety.
 template <int G, int ROWS, int NST, typename MT, typename VT, bool DOT>
 __global__ void __launch_bounds__(ROWS *G)
     k_bsr3_tma(const SolveCtl *__restrict__ ctl, int32_t n, const uint32_t *__restrict__ rowptr,
@@ -67,6 +69,10 @@ __global__ void __launch_bounds__(ROWS *G)
     const size_t vs = ((size_t)b0 * 9 * S) & ~size_t(15), ve = ((size_t)b1 * 9 * S) & ~size_t(15);
     const size_t cs = ((size_t)b0 * 4) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
     fence_proxy_async_smem();
+    if (b1 - b0 > (uint32_t)capb) {  // larger than the buffers: read from global
+      mbar_arrive_expect_tx(&bar[b], 0);
+      return;
+    }
     mbar_arrive_expect_tx(&bar[b], (uint32_t)((ve - vs) + (ce - cs)));
     if (ve > vs)
       bulk_g2s(vbuf(b), reinterpret_cast<const unsigned char *>(vals) + vs, (uint32_t)(ve - vs),
@@ -100,26 +106,57 @@ __global__ void __launch_bounds__(ROWS *G)
     }
     __syncthreads();
     if (!ok_flag) break;
-    MT *vb = vbuf(b);
-    uint32_t *cb = cbuf(b);
     uint32_t b0, b1;
     tile_range(tile, b0, b1);
-    const size_t vs = ((size_t)b0 * 9 * S) & ~size_t(15), ve = ((size_t)b1 * 9 * S) & ~size_t(15);
-    const size_t cs = ((size_t)b0 * 4) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
-    // unaligned tails (< 16 bytes each)
-    const int vt = (int)(((size_t)b1 * 9 * S - ve) / S);
-    const int ct = (int)(((size_t)b1 * 4 - ce) / 4);
-    if ((int)threadIdx.x < vt) vb[(ve - vs) / S + threadIdx.x] = vals[ve / S + threadIdx.x];
-    if ((int)threadIdx.x >= 32 && (int)threadIdx.x < 32 + ct)
-      cb[(ce - cs) / 4 + threadIdx.x - 32] = colidx[ce / 4 + threadIdx.x - 32];
+    const bool staged = b1 - b0 <= (uint32_t)capb;
+    const MT *vb = staged ? vbuf(b) : vals;
+    const uint32_t *cb = staged ? cbuf(b) : colidx;
+    const size_t vs = staged ? ((size_t)b0 * 9 * S) & ~size_t(15) : 0;
+    const size_t cs = staged ? ((size_t)b0 * 4) & ~size_t(15) : 0;
+    if (staged) {
+      // unaligned tails (< 16 bytes each)
+      const size_t ve = ((size_t)b1 * 9 * S) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
+      const int vt = (int)(((size_t)b1 * 9 * S - ve) / S);
+      const int ct = (int)(((size_t)b1 * 4 - ce) / 4);
+      if ((int)threadIdx.x < vt) vbuf(b)[(ve - vs) / S + threadIdx.x] = vals[ve / S + threadIdx.x];
+      if ((int)threadIdx.x >= 32 && (int)threadIdx.x < 32 + ct)
+        cbuf(b)[(ce - cs) / 4 + threadIdx.x - 32] = colidx[ce / 4 + threadIdx.x - 32];
+    }
     __syncthreads();
     const int r = tile * ROWS + (int)(threadIdx.x / G);
     if (r < n) {
       const uint32_t e = rowptr[r + 1];
       VT a0 = 0, a1 = 0, a2 = 0;
       const size_t voff = vs / S, coff = cs / 4;
+      // The first U blocks of the lane (rows of up to U*G blocks): a fixed,
+      // predicated trip count, so all of the lane's x gathers are in flight
+      // at once; same accumulation order as the loop below.
+      constexpr int U = (24 + G - 1) / G;
+      const uint32_t q0 = rowptr[r] + gl;
+      VT xg[U][3];
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const uint32_t q = q0 + k * G;
+        if (q < e) {
+          const uint32_t c = cb[q - coff];
+          xg[k][0] = ldg(x + (size_t)c * 3 + 0);
+          xg[k][1] = ldg(x + (size_t)c * 3 + 1);
+          xg[k][2] = ldg(x + (size_t)c * 3 + 2);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const uint32_t q = q0 + k * G;
+        if (q < e) {
+          const MT *v = vb + ((size_t)q * 9 - voff);
+          const VT x0 = xg[k][0], x1 = xg[k][1], x2 = xg[k][2];
+          a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
+          a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
+          a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
+        }
+      }
 #pragma unroll 4
-      for (uint32_t q = rowptr[r] + gl; q < e; q += G) {
+      for (uint32_t q = q0 + U * G; q < e; q += G) {
         const uint32_t c = cb[q - coff];
         const MT *v = vb + ((size_t)q * 9 - voff);
         const VT x0 = ldg(x + (size_t)c * 3 + 0), x1 = ldg(x + (size_t)c * 3 + 1),
@@ -138,6 +175,162 @@ __global__ void __launch_bounds__(ROWS *G)
       }
     }
     __syncthreads();
+  }
+  if (DOT) {
+    const double t = block_sum(acc, shred);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+  }
+}
+
+}  // namespace sg
+
+namespace sg {
+
+// Per-warp variant: every warp runs its own NST-stage bulk-copy pipeline
+// over tiles of RW = 32/G consecutive block rows (global warp w takes tiles
+// w, w + total warps, ...), waits on its own mbarriers and synchronises only
+// with __syncwarp, so no warp waits for another's copy or compute.  Each
+// warp's buffers hold capb blocks; a larger tile (the caller's statistics
+// were stale, or a very long row) is read straight from global memory.
+constexpr int WTMA_WARPS = 4;
+
+template <typename MT> inline size_t wtma_smem_bytes(int capb, int nst) {
+  return (((size_t)WTMA_WARPS * nst * 8 + 15) & ~size_t(15)) +
+         (size_t)WTMA_WARPS * nst * (tma_vbytes<MT>(capb) + tma_cbytes(capb));
+}
+
+template <int G, int NST, typename MT, typename VT, bool DOT>
+__global__ void __launch_bounds__(WTMA_WARPS * 32)
+    k_bsr3_wtma(const SolveCtl *__restrict__ ctl, int32_t n, const uint32_t *__restrict__ rowptr,
+                const uint32_t *__restrict__ colidx, const MT *__restrict__ vals,
+                const VT *__restrict__ x, VT *__restrict__ y, double *__restrict__ part,
+                int capb, int *err) {
+  static_assert(NST >= 2 && NST <= 6, "stages");
+  constexpr int RW = 32 / G;
+  constexpr size_t S = sizeof(MT);
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ double shred[33];
+  if (ctl && ctl->status != ST_RUNNING) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t vbytes = tma_vbytes<MT>(capb), cbytes = tma_cbytes(capb);
+  const size_t stage = vbytes + cbytes;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm) + warp * NST;
+  unsigned char *base =
+      sm + (((size_t)WTMA_WARPS * NST * 8 + 15) & ~size_t(15)) + (size_t)warp * NST * stage;
+  auto vbuf = [&](int b) { return reinterpret_cast<MT *>(base + (size_t)b * stage); };
+  auto cbuf = [&](int b) { return reinterpret_cast<uint32_t *>(base + (size_t)b * stage + vbytes); };
+  if (lane == 0) {
+    for (int b = 0; b < NST; ++b) mbar_init(&bar[b], 1);
+    mbar_fence_init();
+  }
+  __syncwarp();
+  const int64_t ntiles = ((int64_t)n + RW - 1) / RW;
+  const int64_t gw = (int64_t)blockIdx.x * WTMA_WARPS + warp;
+  const int64_t nw = (int64_t)gridDim.x * WTMA_WARPS;
+  const int64_t my = gw < ntiles ? (ntiles - 1 - gw) / nw + 1 : 0;
+  auto issue = [&](int64_t tile, int b) {
+    const int64_t r0 = tile * RW;
+    const int64_t r1 = min((int64_t)n, r0 + RW);
+    const uint32_t b0 = rowptr[r0], b1 = rowptr[r1];
+    const size_t vs = ((size_t)b0 * 9 * S) & ~size_t(15), ve = ((size_t)b1 * 9 * S) & ~size_t(15);
+    const size_t cs = ((size_t)b0 * 4) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
+    fence_proxy_async_smem();
+    if (b1 - b0 > (uint32_t)capb) {  // larger than the buffers: read from global
+      mbar_arrive_expect_tx(&bar[b], 0);
+      return;
+    }
+    mbar_arrive_expect_tx(&bar[b], (uint32_t)((ve - vs) + (ce - cs)));
+    if (ve > vs)
+      bulk_g2s(vbuf(b), reinterpret_cast<const unsigned char *>(vals) + vs, (uint32_t)(ve - vs),
+               &bar[b]);
+    if (ce > cs)
+      bulk_g2s(cbuf(b), reinterpret_cast<const unsigned char *>(colidx) + cs,
+               (uint32_t)(ce - cs), &bar[b]);
+  };
+  if (lane == 0)
+    for (int k = 0; k < NST - 1 && k < my; ++k) issue(gw + k * nw, k);
+  const int gl = lane & (G - 1);
+  const unsigned mask = group_mask<G>();
+  double acc = 0;
+  for (int64_t k = 0; k < my; ++k) {
+    const int b = (int)(k % NST);
+    const int64_t tile = gw + k * nw;
+    const int64_t kn = k + NST - 1;
+    if (lane == 0 && kn < my) issue(gw + kn * nw, (int)(kn % NST));
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[b], (uint32_t)((k / NST) & 1)));
+    if (!ok) {
+      if (lane == 0) {
+        atomicCAS(err, 0, 6 /* DEV_TMA_TIMEOUT */);
+        for (int64_t kk = k + 1; kk < my && kk <= kn; ++kk)
+          mbar_wait(&bar[kk % NST], (uint32_t)((kk / NST) & 1));
+      }
+      break;
+    }
+    const int64_t r0 = tile * RW;
+    const uint32_t b0 = rowptr[r0], b1 = rowptr[min((int64_t)n, r0 + RW)];
+    const bool staged = b1 - b0 <= (uint32_t)capb;
+    const MT *vb = staged ? vbuf(b) : vals;
+    const uint32_t *cb = staged ? cbuf(b) : colidx;
+    const size_t vs = staged ? ((size_t)b0 * 9 * S) & ~size_t(15) : 0;
+    const size_t cs = staged ? ((size_t)b0 * 4) & ~size_t(15) : 0;
+    if (staged) {
+      // unaligned tails (< 16 bytes each)
+      const size_t ve = ((size_t)b1 * 9 * S) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
+      const int vt = (int)(((size_t)b1 * 9 * S - ve) / S);
+      const int ct = (int)(((size_t)b1 * 4 - ce) / 4);
+      if (lane < vt) vbuf(b)[(ve - vs) / S + lane] = vals[ve / S + lane];
+      if (lane >= 16 && lane < 16 + ct)
+        cbuf(b)[(ce - cs) / 4 + lane - 16] = colidx[ce / 4 + lane - 16];
+    }
+    __syncwarp();
+    const int64_t r = r0 + lane / G;
+    if (r < n) {
+      const uint32_t e = rowptr[r + 1];
+      VT a0 = 0, a1 = 0, a2 = 0;
+      const size_t voff = vs / S, coff = cs / 4;
+      constexpr int U = (24 + G - 1) / G;
+      const uint32_t q0 = rowptr[r] + gl;
+      VT xg[U][3];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t q = q0 + u * G;
+        if (q < e) {
+          const uint32_t c = cb[q - coff];
+          xg[u][0] = ldg(x + (size_t)c * 3 + 0);
+          xg[u][1] = ldg(x + (size_t)c * 3 + 1);
+          xg[u][2] = ldg(x + (size_t)c * 3 + 2);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t q = q0 + u * G;
+        if (q < e) {
+          const MT *v = vb + ((size_t)q * 9 - voff);
+          const VT x0 = xg[u][0], x1 = xg[u][1], x2 = xg[u][2];
+          a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
+          a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
+          a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
+        }
+      }
+      for (uint32_t q = q0 + U * G; q < e; q += G) {
+        const uint32_t c = cb[q - coff];
+        const MT *v = vb + ((size_t)q * 9 - voff);
+        const VT x0 = ldg(x + (size_t)c * 3 + 0), x1 = ldg(x + (size_t)c * 3 + 1),
+                 x2 = ldg(x + (size_t)c * 3 + 2);
+        a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
+        a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
+        a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
+      }
+      a0 = group_sum<G>(a0, mask);
+      a1 = group_sum<G>(a1, mask);
+      a2 = group_sum<G>(a2, mask);
+      if (gl < 3) {
+        const VT yv = gl == 0 ? a0 : (gl == 1 ? a1 : a2);
+        y[(size_t)r * 3 + gl] = yv;
+        if (DOT) acc += (double)x[(size_t)r * 3 + gl] * (double)yv;
+      }
+    }
+    __syncwarp();
   }
   if (DOT) {
     const double t = block_sum(acc, shred);

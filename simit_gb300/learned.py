@@ -22,8 +22,8 @@ from ._lib import call
 from .runtime import Solver, bspmv, dtype_code, ptr, solve_opts
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-WEIGHTS = os.path.join(HERE, "data", "mpnn_elasticity.npy")
-WEIGHTS_LINEAR = os.path.join(HERE, "data", "mpnn_elasticity_linear.npy")
+FORMS = {"relu": _lib.MPNN_RELU, "linear": _lib.MPNN_LINEAR, "sym": _lib.MPNN_SYM}
+WEIGHTS = {f: os.path.join(HERE, "data", "mpnn_elasticity_%s.npy" % f) for f in FORMS}
 KS = (1, 3, 8, 16, 32, 64, 128, 256, 512, 1024)
 H, K = 64, 8
 SHAPES = [("W1s", (H, 3)), ("W1m", (H, 3)), ("P2", (K, H)), ("W2h", (H, H)), ("W2m", (H, K)),
@@ -48,14 +48,14 @@ def init_params(seed=0, out_scale=0.0):
     return p
 
 
-def load_weights(path=WEIGHTS):
-    return np.load(path).astype(np.float32)
+def load_weights(form="sym"):
+    return np.load(WEIGHTS[form]).astype(np.float32)
 
 
 class Graph:
     """sg_mpnn_graph of a 3x3-blocked matrix."""
 
-    def __init__(self, ctx, mesh, A, linear=False):
+    def __init__(self, ctx, mesh, A, form="relu"):
         self.ctx = ctx
         self.A = A
         self.m = _lib.Matrix(mesh.n, 3, mesh.nnzb, mesh.pattern.rowptr.data_ptr(),
@@ -64,7 +64,7 @@ class Graph:
         call("sg_mpnn_graph_create", ctx.h, ctypes.byref(self.m), ctypes.byref(h))
         self.h = h
         self.n = mesh.n
-        call("sg_mpnn_graph_set_linear", h, int(linear))
+        call("sg_mpnn_graph_set_form", h, FORMS[form])
 
     def forward(self, params, r, z, train=False):
         call("sg_mpnn_forward", self.h, ptr(params), ptr(r), ptr(z), int(train))
@@ -157,20 +157,57 @@ class Trainer:
         return tot / max(1, len(pairs))
 
 
+class Validator:
+    """PCG iterations with the current weights on a held-out mesh (the
+    quantity the preconditioner exists to reduce; the training loss is a
+    one-step proxy for it)."""
+
+    def __init__(self, ctx, ncell=16, seed=555, form="sym", maxiters=5000):
+        host = problems.hetero_mesh(ncell, seed=seed)
+        self.ctx = ctx
+        self.prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
+                                              precond=_lib.PRECOND_BLOCK_JACOBI)
+        m = self.prob.mesh
+        with ctx.stream():
+            self.prm = torch.zeros(nparams(), dtype=torch.float32, device=ctx.device)
+        self.S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, self.prob.A, m.nnzb,
+                        solve_opts(precision=_lib.SOLVE_MIXED, precond=_lib.PRECOND_LEARNED,
+                                   tol=1e-8, maxiters=maxiters, learned_params=self.prm,
+                                   learned_form=FORMS[form]),
+                        learned_params_keep=self.prm)
+
+    def iters(self, params):
+        with self.ctx.stream():
+            self.prm.copy_(params)
+            x = torch.zeros_like(self.prob.b)
+        r = self.S.solve(self.prob.b, x)
+        ok = r.status == 1 and r.fallbacks == 0
+        return r.iters if ok else None
+
+    def close(self):
+        self.S.close()
+        self.prob.close()
+
+
 def train(ctx, sizes=(16, 24, 32, 40, 48), n_pairs=2000, epochs=6, lr=1e-3, seed=0,
-          log=print, linear=False):
-    """Train on n_pairs pairs spread over the meshes; returns (params, history)."""
+          log=print, form="sym", val_every=100):
+    """Train on n_pairs pairs spread over the meshes.  Every val_every steps
+    the weights are scored by PCG iterations on a held-out mesh and the best
+    scoring weights are kept.  Returns (params, history)."""
     per_mesh = max(1, n_pairs // (len(sizes) * len(KS)))
     data = []
     for i, nc in enumerate(sizes):
         prob, pairs = make_pairs(ctx, nc, seed=100 + i, n_rhs=per_mesh)
-        data.append((prob, Graph(ctx, prob.mesh, prob.A, linear=linear), pairs))
+        data.append((prob, Graph(ctx, prob.mesh, prob.A, form=form), pairs))
         log("mesh %d^3: %d pairs" % (nc, len(pairs)))
     tr = Trainer(ctx, lr=lr, seed=seed)
-    hist = []
+    val = Validator(ctx, form=form)
+    hist = {"loss": [], "val_iters": []}
+    best = (val.iters(tr.params), 0, tr.params.detach().clone())
+    hist["val_iters"].append((0, best[0]))
     L0 = np.mean([tr.eval_loss(g, p) for _, g, p in data])
-    hist.append(L0)
-    log("epoch 0 loss %.5f" % L0)
+    hist["loss"].append(L0)
+    log("epoch 0 loss %.5f val iters %s" % (L0, best[0]))
     rng = meshgen.rng(seed + 7)
     for ep in range(epochs):
         order = [(i, j) for i, (_, _, p) in enumerate(data) for j in range(len(p))]
@@ -179,17 +216,24 @@ def train(ctx, sizes=(16, 24, 32, 40, 48), n_pairs=2000, epochs=6, lr=1e-3, seed
             prob, g, pairs = data[i]
             r, e, eAe = pairs[j]
             tr.step(g, r, e, eAe)
+            if tr.step_n % val_every == 0:
+                it = val.iters(tr.params)
+                hist["val_iters"].append((tr.step_n, it))
+                if it is not None and (best[0] is None or it < best[0]):
+                    best = (it, tr.step_n, tr.params.detach().clone())
         L = np.mean([tr.eval_loss(g, p) for _, g, p in data])
-        hist.append(L)
-        log("epoch %d loss %.5f" % (ep + 1, L))
-    params = tr.params.detach().cpu().numpy()
+        hist["loss"].append(L)
+        log("epoch %d loss %.5f best val iters %s (step %d)" % (ep + 1, L, best[0], best[1]))
+    hist["best_step"] = best[1]
+    params = best[2].cpu().numpy()
+    val.close()
     for prob, g, _ in data:
         g.close()
         prob.close()
     return params, hist
 
 
-def compare(ctx, params, ncell, seed=999, tol=1e-8, linear=False):
+def compare(ctx, params, ncell, seed=999, tol=1e-8, form="sym"):
     """Flexible PCG with the network vs block-Jacobi PCG on a held-out mesh."""
     host = problems.hetero_mesh(ncell, seed=seed)
     out = {}
@@ -204,7 +248,7 @@ def compare(ctx, params, ncell, seed=999, tol=1e-8, linear=False):
         S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, m.nnzb,
                    solve_opts(precision=_lib.SOLVE_MIXED, precond=pc, tol=tol, maxiters=100000,
                               learned_params=prm if pc == _lib.PRECOND_LEARNED else None,
-                              learned_linear=linear),
+                              learned_form=FORMS[form]),
                    learned_params_keep=prm)
         x = torch.zeros_like(prob.b)
         torch.cuda.synchronize()
@@ -230,17 +274,18 @@ def main():
     ap.add_argument("--pairs", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=6)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--out", default=None, help="weights file (default: the package's)")
     ap.add_argument("--eval-size", type=int, default=32)
-    ap.add_argument("--linear", action="store_true", help="identity activations")
+    ap.add_argument("--form", default="sym", choices=sorted(FORMS))
     a = ap.parse_args()
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
     t0 = time.time()
-    params, hist = train(ctx, n_pairs=a.pairs, epochs=a.epochs, lr=a.lr, linear=a.linear)
-    os.makedirs(os.path.dirname(a.out) or ".", exist_ok=True)
-    np.save(a.out, params)
-    res = compare(ctx, params, a.eval_size, linear=a.linear)
+    params, hist = train(ctx, n_pairs=a.pairs, epochs=a.epochs, lr=a.lr, form=a.form)
+    out = a.out or WEIGHTS[a.form]
+    os.makedirs(os.path.dirname(out) or ".", exist_ok=True)
+    np.save(out, params)
+    res = compare(ctx, params, a.eval_size, form=a.form)
     print(json.dumps({"train_seconds": time.time() - t0, "loss_history": hist,
                       "eval": res, "weights": a.out}))
 

@@ -223,10 +223,10 @@ def assemble_heat(mesh, B, W, kappa, dt, T0, dtype=torch.float64, exact=True):
 
 def solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_RELATIVE,
                tol=1e-8, maxiters=10000, verify=1, check_every=0, reliable_delta=0.1, lanes=0,
-               batch=32, learned_params=None, learned_linear=False):
+               batch=32, learned_params=None, learned_form=0):
     lp = learned_params.data_ptr() if learned_params is not None else None
     return _lib.SolveOpts(precision, precond, stop, tol, maxiters, verify, check_every,
-                          reliable_delta, lanes, batch, lp, int(learned_linear))
+                          reliable_delta, lanes, batch, lp, int(learned_form))
 
 
 class Solver:

@@ -133,6 +133,80 @@ def test_spmv_f32(ctx, oracle, bs):
     assert np.all(np.abs(y.cpu().numpy() - ref) <= 2e-6 * scale + 1e-30)
 
 
+N_TMA_VARIANTS = 11
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("variant", range(N_TMA_VARIANTS))
+def test_spmv_tma_variants(ctx, oracle, variant, dt):
+    """Every TMA-staged SpMV variant (CTA tiles and per-warp pipelines), on
+    a random graph plus a hub vertex whose ~60-block row runs past the
+    predicated part of each lane's loop; unaligned tile heads and tails
+    throughout (36- and 72-byte blocks)."""
+    from simit_gb300.runtime import bspmv
+    n = 3001
+    g0 = meshgen.rng(90 + variant)
+    ep = np.concatenate([g0.integers(0, n, size=12000 * 2),
+                         np.stack([np.full(60, 7), g0.integers(0, n, 60)], 1).reshape(-1)])
+    rp, ci = oracle.pattern(n, ep.astype(np.int32), 2)
+    g = meshgen.rng(91 + variant)
+    vals = g.uniform(-1, 1, size=len(ci) * 9).astype(dt)
+    x = g.uniform(-1, 1, size=n * 3).astype(dt)
+    ref = oracle.spmv(n, 3, rp, ci, vals.astype(np.float64), x.astype(np.float64))
+    scale = oracle.spmv(n, 3, rp, ci, np.abs(vals).astype(np.float64),
+                        np.abs(x).astype(np.float64))
+    d = ctx.device
+    t = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(d)  # noqa
+    y = bspmv(ctx, n, 3, t(rp), t(ci), t(vals), t(x), g=-1 - variant)
+    ctx.sync()
+    tol = 2e-6 if dt == np.float32 else 1e-14
+    assert np.all(np.abs(y.cpu().numpy() - ref) <= tol * scale + 1e-300)
+
+
+def test_spmv_tma_stale_statistics(ctx, oracle):
+    """Pattern statistics are cached per (rowptr address, n); a new pattern
+    written at the same address with longer rows must still multiply
+    correctly (oversize tiles are read from global memory, never staged
+    past the buffers)."""
+    from simit_gb300.runtime import bspmv
+    n = 4000
+    d = ctx.device
+    t = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(d)  # noqa
+    ep = meshgen.rng(5).integers(0, n, size=8000 * 2).astype(np.int32)
+    rp1, ci1 = oracle.pattern(n, ep, 2)
+    ep2 = np.concatenate([ep, np.stack([np.full(80, 3), np.arange(100, 180)], 1).reshape(-1)
+                          .astype(np.int32)])
+    rp2, ci2 = oracle.pattern(n, ep2, 2)
+    assert len(ci2) > len(ci1)
+    with ctx.stream():
+        rp_d = torch.zeros(n + 1, dtype=torch.int32, device=d)
+        ci_d = torch.zeros(len(ci2), dtype=torch.int32, device=d)
+    g = meshgen.rng(6)
+    for rp, ci in ((rp1, ci1), (rp2, ci2)):
+        rp_d.copy_(t(rp))
+        ci_d[:len(ci)].copy_(t(ci))
+        vals = g.uniform(-1, 1, size=len(ci) * 9).astype(np.float32)
+        x = g.uniform(-1, 1, size=n * 3).astype(np.float32)
+        ref = oracle.spmv(n, 3, rp, ci, vals.astype(np.float64), x.astype(np.float64))
+        scale = oracle.spmv(n, 3, rp, ci, np.abs(vals).astype(np.float64),
+                            np.abs(x).astype(np.float64))
+        for variant in range(N_TMA_VARIANTS):
+            y = bspmv(ctx, n, 3, rp_d, ci_d, t(vals), t(x), g=-1 - variant)
+            ctx.sync()
+            assert np.all(np.abs(y.cpu().numpy() - ref) <= 2e-6 * scale + 1e-30), variant
+
+
+def test_spmv_tma_variant_out_of_range(ctx, oracle):
+    from simit_gb300._lib import SimitError
+    from simit_gb300.runtime import bspmv
+    n = 50
+    rp, ci, vals, x = _random_bsr(oracle, n, 100, 3, 1, np.float32)
+    d = ctx.device
+    t = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(d)  # noqa
+    with pytest.raises(SimitError):
+        bspmv(ctx, n, 3, t(rp), t(ci), t(vals), t(x), g=-1 - N_TMA_VARIANTS)
+
+
 def test_spmv_f32_matrix_f64_vector(ctx, oracle):
     """FP32 values, FP64 x/y and accumulation (the refinement residual path)."""
     from simit_gb300.runtime import bspmv

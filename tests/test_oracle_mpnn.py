@@ -1,0 +1,88 @@
+"""CPU checks of the learned-preconditioner oracle (oracle/mpnn_oracle.py):
+its weight gradients against central finite differences for the three
+forms, and the symmetric form's defining properties (symmetric, positive
+definite, block Jacobi when the output weights are zero).  The GPU kernels
+are checked against this oracle in test_gpu_learned.py."""
+import numpy as np
+import pytest
+
+from oracle import mpnn_oracle as mo
+from oracle import oracle
+from simit_gb300 import problems
+
+
+@pytest.fixture(scope="module")
+def system():
+    oracle.build()
+    h = problems.hetero_mesh(3, seed=3)
+    rp, ci = oracle.pattern(h["n"], h["tets"], 4)
+    B, W, _ = oracle.tet_precompute(h["X0"], h["tets"], problems.RHO)
+    A = oracle.tet_stiffness(0, h["x"], h["c"], h["tets"], B, W, h["mu"], h["lam"], problems.H,
+                             problems.RHO, rp, ci)
+    return h["n"], rp, ci, np.asarray(A)
+
+
+@pytest.fixture
+def exact(monkeypatch):
+    # exact arithmetic: the bf16 roundings pass gradients straight through and
+    # would make the map non-differentiable at rounding boundaries
+    monkeypatch.setattr(mo, "bf16", lambda x: np.asarray(x, np.float64))
+
+
+def _apply(form, p, n, rp, ci, A, r):
+    if form == "sym":
+        return mo.forward_sym(p, n, rp, ci, A, r)
+    return mo.forward(p, n, rp, ci, A, r, linear=form == "linear")
+
+
+def _grad(form, cache, w):
+    return mo.backward_sym(cache, w) if form == "sym" else mo.backward(cache, w)
+
+
+@pytest.mark.parametrize("form", ["relu", "linear", "sym"])
+def test_gradient_matches_finite_differences(system, exact, form):
+    n, rp, ci, A = system
+    rng = np.random.default_rng(0)
+    p = mo.init_params(1, out_scale=0.5).astype(np.float64) * 0.5
+    r = rng.normal(size=n * 3)
+    w = rng.normal(size=n * 3)
+    _, cache = _apply(form, p, n, rp, ci, A, r)
+    g = _grad(form, cache, w)
+    f = lambda q: float(np.dot(_apply(form, q, n, rp, ci, A, r)[0], w))  # noqa: E731
+    errs = []
+    for i in rng.choice(len(p), 40, replace=False):
+        e = np.zeros_like(p)
+        e[i] = 1e-6 * max(1.0, abs(p[i]))
+        fd = (f(p + e) - f(p - e)) / (2 * e[i])
+        errs.append(abs(fd - g[i]) / (abs(fd) + abs(g[i]) + 1e-9))
+    # relu kinks can sit inside a difference interval: median for relu
+    assert (np.median(errs) if form == "relu" else max(errs)) < 1e-3, errs
+
+
+def test_symmetric_form_properties(system, exact):
+    n, rp, ci, A = system
+    rng = np.random.default_rng(1)
+    p = mo.init_params(2, out_scale=1.0).astype(np.float64)
+    u, v = rng.normal(size=n * 3), rng.normal(size=n * 3)
+    Mu = mo.forward_sym(p, n, rp, ci, A, u)[0]
+    Mv = mo.forward_sym(p, n, rp, ci, A, v)[0]
+    assert abs(v @ Mu - u @ Mv) <= 1e-10 * abs(v @ Mu)
+    assert u @ Mu > 0 and v @ Mv > 0
+    p[-3 * mo.H:] = 0.0  # Wout = 0
+    z0 = mo.forward_sym(p, n, rp, ci, A, u)[0]
+    bj = np.einsum("vij,vj->vi", mo.block_jacobi(n, rp, ci, A), u.reshape(n, 3)).reshape(-1)
+    assert np.allclose(z0, bj, rtol=1e-12, atol=1e-14 * np.abs(bj).max())
+
+
+def test_transpose_params_is_the_adjoint(system, exact):
+    """<v, N u> = <N^T v, u> with N^T run as the transposed network plus the
+    extra aggregation of W1m^T h3'."""
+    n, rp, ci, A = system
+    rng = np.random.default_rng(2)
+    p = mo.init_params(3, out_scale=1.0).astype(np.float64)
+    u, v = rng.normal(size=(n, 3)), rng.normal(size=(n, 3))
+    Nu = mo.forward(p, n, rp, ci, A, u, linear=True, stage="id")[0].reshape(n, 3) - u
+    wp, c = mo.forward(mo.transpose_params(p), n, rp, ci, A, v, linear=True, stage="id")
+    NTv = wp.reshape(n, 3) - v + mo._agg(c["a"], c["rows"], c["cols"],
+                                         c["h3"] @ mo.unpack(p)["W1m"], n)
+    assert abs((v * Nu).sum() - (NTv * u).sum()) <= 1e-10 * abs((v * Nu).sum())
