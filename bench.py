@@ -34,6 +34,8 @@ def parse():
     ap.add_argument("--size", type=int, default=128, help="cells per cube edge")
     ap.add_argument("--cpu-sample", type=int, default=32, help="cells per edge of the CPU sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-preconditioner comparison")
     ap.add_argument("--spmv-only", action="store_true",
                     help="profiling driver: build the --size matrix and run sg_bspmv --reps times")
     ap.add_argument("--lanes", type=int, default=0, help="sg_bspmv lanes (g) for --spmv-only")
@@ -523,6 +525,39 @@ def run_ours(args, rank, world, local):
     achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
 
+    # --- the same system solved with the learned (symmetric) preconditioner
+    # against block-Jacobi, solve only (same matrix and right-hand side) ----
+    learned = None
+    if not args.no_learned:
+        from simit_gb300 import learned as lrn
+        from simit_gb300.runtime import Solver, solve_opts
+        with ctx.stream():
+            prm = torch.tensor(lrn.load_weights("sym"), device=ctx.device)
+            xs = torch.zeros_like(prob.b)
+        S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, m.nnzb,
+                   solve_opts(precision=_lib.SOLVE_MIXED, precond=_lib.PRECOND_LEARNED,
+                              tol=1e-8, maxiters=200000, learned_params=prm,
+                              learned_form=_lib.MPNN_SYM), learned_params_keep=prm)
+        res = {}
+        for name, solver in (("block_jacobi", prob.solver), ("learned_sym", S)):
+            def one():
+                with ctx.stream():
+                    xs.zero_()
+                return solver.solve(prob.b, xs)
+            l0 = torch.cuda.Event(enable_timing=True)
+            l1 = torch.cuda.Event(enable_timing=True)
+            l0.record(st)
+            r = one()
+            l1.record(st)
+            l1.synchronize()
+            res[name] = {"solve_ms": l0.elapsed_time(l1), "iters": r.iters,
+                         "fallbacks": r.fallbacks,
+                         "relres": (r.true_normr2 / r.bnorm2) ** 0.5}
+        S.close()
+        res["iteration_gain"] = res["block_jacobi"]["iters"] / max(1, res["learned_sym"]["iters"])
+        res["time_ratio"] = res["block_jacobi"]["solve_ms"] / res["learned_sym"]["solve_ms"]
+        learned = res
+
     # --- plain FP64 Jacobi-CG on the same GPU (FP64 assembly + solve) -----
     fp64 = None
     if not args.no_fp64:
@@ -565,7 +600,8 @@ def run_ours(args, rank, world, local):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": spmv_traffic(args.size),
-                     "kernel": "k_bsr3_tma (FP32 3x3 blocked SpMV)", "peak_kind": peak_kind,
+                     "kernel": "k_bsr3_wtma (FP32 3x3 blocked SpMV, per-warp TMA pipeline)",
+                     "peak_kind": peak_kind,
                      "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes},
         "cpu_baseline": {"value": cpu["value"], "unit": "DOF/s", "cores": 1, "kind": "port",
                          "sample": "%d^3 instance (%d DOF) of the same family: oracle pattern + "
@@ -574,6 +610,7 @@ def run_ours(args, rank, world, local):
                                                cpu["seconds"])},
         "clocks": clk,
         "fp64_jacobi_cg": fp64,
+        "learned_vs_block_jacobi": learned,
         "speedup_vs_fp64_cg": (fp64["ms"] / ms) if fp64 else None,
     }
     print(json.dumps(out), flush=True)

@@ -172,12 +172,13 @@ int sg_assemble_heat(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
  * bs = 1, 2, 3 have dedicated kernels; other bs use a generic kernel.
  * val_dtype is the matrix value type; vec_dtype the type of x and y;
  * accumulation is in the wider of the two.  g = 1,2,4,8,16,32 selects the
- * streaming kernel with g lanes per block row; g = -1..-11 selects variant
+ * streaming kernel with g lanes per block row; g = -1..-12 selects variant
  * -g-1 of the TMA-staged kernel (bs = 3, 16-byte aligned vals/colidx;
  * variants differ in lanes per row, rows per tile, pipeline stages and
  * whether a CTA or each warp runs the copy pipeline; a variant whose
  * buffers cannot hold the pattern's largest tile runs the streaming kernel);
- * g = 0 picks (TMA variant 0 for FP32 values, the streaming kernel for FP64).
+ * g = 0 picks (the default TMA variant for FP32 values, the streaming kernel
+ * for FP64).
  * ------------------------------------------------------------------- */
 int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
              const uint32_t *colidx, int val_dtype, const void *vals,

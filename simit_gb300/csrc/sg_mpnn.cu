@@ -265,6 +265,7 @@ static int set_sym(GraphH *G, int sym) {
   tg.dinv = g.dinv;
   tg.linv = g.linv;
   tg.lin = 1;
+  tg.sym = 1;  // split activations in its passes too (it has no twin of its own)
   SG_TRY(alloc_layers(T));
   SG_TRY(galloc(T, (void **)&tg.y, n * 3 * 4));
   SG_TRY(galloc(T, (void **)&tg.dres, 64));

@@ -572,7 +572,7 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   if (S->G < 1 || S->G > 32 || (S->G & (S->G - 1))) S->G = default_lanes(A->n, A->nnzb, A->bs);
   if (A->bs != 3 && A->bs != 1) S->G = 1;
   S->P1 = grid_for(c, (int64_t)A->n * (A->bs == 3 || A->bs == 1 ? S->G : 1), RED_T, 8);
-  S->P2 = grid_for(c, S->len, RED_T, 4);
+  S->P2 = grid_for(c, S->len, RED_T, 3);  // K2 holds 3 CTAs per SM
   S->prec = o->precond == SG_PRECOND_JACOBI ? PK_JACOBI
             : o->precond == SG_PRECOND_BLOCK_JACOBI ? PK_BLOCK3
             : o->precond == SG_PRECOND_LEARNED ? PK_EXTERNAL : PK_NONE;
@@ -585,7 +585,7 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   if (A->bs == 3 && aligned && (o->lanes < 0 || (o->lanes == 0 && S->kind != KIND_F64))) {
     SG_TRY(cached_stats(c, A->n, A->rowptr, &S->pstats, true));
     S->maxrow = S->pstats.maxrow;
-    S->tma_var = o->lanes < 0 ? -o->lanes - 1 : 0;
+    S->tma_var = o->lanes < 0 ? -o->lanes - 1 : default_tma_variant();
     const int vdt = (S->kind == KIND_F64) ? SG_F64 : SG_F32;
     const int xdt = S->kind == KIND_MIXED ? SG_F32 : SG_F64;
     int grid = 0;

@@ -263,7 +263,7 @@ __device__ __forceinline__ void st4(float *p, int64_t i, const float *o) {
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(RED_T) k_cg_update_v4(SolveCtl *ctl, int par, int64_t len,
+__global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int par, int64_t len,
                                                         const double *__restrict__ part_in,
                                                         int np1, const float *__restrict__ p,
                                                         const float *__restrict__ q,

@@ -8,15 +8,18 @@ namespace sg {
 
 // TMA SpMV variants: (lanes per block row, rows per CTA tile, pipeline
 // stages); ROWS = 0 selects the per-warp pipeline (tiles of 32/G rows per
-// warp).  Variant 0 is the default.
+// warp).
 struct TmaVariant {
   int G, ROWS, NST;
 };
 static const TmaVariant kTmaVariants[] = {
     {8, 32, 2}, {8, 32, 3}, {8, 16, 4}, {4, 32, 3}, {16, 16, 4}, {8, 16, 2},
-    {8, 0, 2},  {8, 0, 3},  {8, 0, 4},  {4, 0, 2},  {4, 0, 3},
+    {8, 0, 2},  {8, 0, 3},  {8, 0, 4},  {4, 0, 2},  {4, 0, 3},  {2, 0, 2},
 };
 constexpr int kNumTmaVariants = sizeof(kTmaVariants) / sizeof(kTmaVariants[0]);
+// The variant g = 0 (and the solver) use: the fastest on the 128^3 lattice.
+constexpr int kDefaultTmaVariant = 9;  // per-warp, 4 lanes per row, 2 stages
+int default_tma_variant() { return kDefaultTmaVariant; }
 
 // Blocks in the largest tile of `rows` consecutive rows (the buffer size).
 static int tile_cap(int rows, const PatternStats &ps) {
@@ -130,6 +133,7 @@ static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
     SG_W(8, 8, 4)
     SG_W(9, 4, 2)
     SG_W(10, 4, 3)
+    SG_W(11, 2, 2)
     default: return SG_ERR_ARG;
   }
 #undef SG_V
@@ -406,7 +410,7 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
     size_t sh = 0;
     PatternStats ps;
     SG_TRY(cached_stats(c, n, rowptr, &ps));
-    const int var = g < 0 ? -g - 1 : 0;
+    const int var = g < 0 ? -g - 1 : kDefaultTmaVariant;
     if (bsr3_tma_config(c, vdt, xdt, var, 0, n, ps, &grid, &sh) == SG_OK)
       return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, var, 0, n, rowptr, colidx, vals, x,
                              y, nullptr, ps, grid, sh);

@@ -9,6 +9,7 @@ struct PatternStats {
   int maxrow = 0, tile16 = 0, tile32 = 0, tile4 = 0, tile8 = 0;
 };
 int default_lanes(int32_t n, int64_t nnzb, int32_t bs);
+int default_tma_variant();
 int cached_maxrow(Ctx *c, int32_t n, const uint32_t *rowptr, int *out);
 int cached_stats(Ctx *c, int32_t n, const uint32_t *rowptr, PatternStats *ps,
                  bool refresh = false);

@@ -27,6 +27,74 @@ template <typename MT> inline size_t tma_smem_bytes(int capb, int nst) {
   return 64 + (size_t)nst * (tma_vbytes<MT>(capb) + tma_cbytes(capb));
 }
 
+// y_r = (A x)_r for block row r from its tile's values vb and columns cb
+// (block q at vb[q*9 - voff], cb[q - coff]); G lanes per row, lane gl takes
+// blocks rowptr[r]+gl, +G, ...  The first U blocks of each lane (rows of up
+// to 24 blocks) use a fixed, predicated trip count so all of the lane's x
+// gathers are in flight at once; the remainder loop keeps the same
+// accumulation order.  With DOT, acc += x_r . y_r.
+template <int G, typename MT, typename VT, bool DOT>
+__device__ __forceinline__ void tile_row(int64_t r, int gl, unsigned mask,
+                                         const uint32_t *__restrict__ rowptr,
+                                         const MT *__restrict__ vb,
+                                         const uint32_t *__restrict__ cb, size_t voff,
+                                         size_t coff, const VT *__restrict__ x,
+                                         VT *__restrict__ y, double &acc) {
+  const uint32_t e = rowptr[r + 1];
+  VT a0 = 0, a1 = 0, a2 = 0;
+  constexpr int U = (24 + G - 1) / G;
+  const uint32_t q0 = rowptr[r] + gl;
+  VT xg[U][3];
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const uint32_t q = q0 + k * G;
+    if (q < e) {
+      const uint32_t c = cb[q - coff];
+      xg[k][0] = ldg(x + (size_t)c * 3 + 0);
+      xg[k][1] = ldg(x + (size_t)c * 3 + 1);
+      xg[k][2] = ldg(x + (size_t)c * 3 + 2);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const uint32_t q = q0 + k * G;
+    if (q < e) {
+      const MT *v = vb + ((size_t)q * 9 - voff);
+      const VT x0 = xg[k][0], x1 = xg[k][1], x2 = xg[k][2];
+      a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
+      a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
+      a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
+    }
+  }
+#pragma unroll 4
+  for (uint32_t q = q0 + U * G; q < e; q += G) {
+    const uint32_t c = cb[q - coff];
+    const MT *v = vb + ((size_t)q * 9 - voff);
+    const VT x0 = ldg(x + (size_t)c * 3 + 0), x1 = ldg(x + (size_t)c * 3 + 1),
+             x2 = ldg(x + (size_t)c * 3 + 2);
+    a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
+    a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
+    a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
+  }
+  a0 = group_sum<G>(a0, mask);
+  a1 = group_sum<G>(a1, mask);
+  a2 = group_sum<G>(a2, mask);
+  if (G >= 3) {
+    if (gl < 3) {
+      const VT yv = gl == 0 ? a0 : (gl == 1 ? a1 : a2);
+      y[(size_t)r * 3 + gl] = yv;
+      if (DOT) acc += (double)x[(size_t)r * 3 + gl] * (double)yv;
+    }
+  } else if (gl == 0) {  // fewer than 3 lanes: lane 0 writes the row
+    y[(size_t)r * 3 + 0] = a0;
+    y[(size_t)r * 3 + 1] = a1;
+    y[(size_t)r * 3 + 2] = a2;
+    if (DOT)
+      acc += (double)x[(size_t)r * 3] * (double)a0 + (double)x[(size_t)r * 3 + 1] * (double)a1 +
+             (double)x[(size_t)r * 3 + 2] * (double)a2;
+  }
+}
+
 // NST-stage pipeline: while the CTA computes tile k, the copies of tiles
 // k+1 .. k+NST-1 are in flight.  A tile of more than capb blocks (the
 // buffers' capacity) is never staged: it is read straight from global
@@ -109,8 +177,6 @@ __global__ void __launch_bounds__(ROWS *G)
     uint32_t b0, b1;
     tile_range(tile, b0, b1);
     const bool staged = b1 - b0 <= (uint32_t)capb;
-    const MT *vb = staged ? vbuf(b) : vals;
-    const uint32_t *cb = staged ? cbuf(b) : colidx;
     const size_t vs = staged ? ((size_t)b0 * 9 * S) & ~size_t(15) : 0;
     const size_t cs = staged ? ((size_t)b0 * 4) & ~size_t(15) : 0;
     if (staged) {
@@ -125,54 +191,12 @@ __global__ void __launch_bounds__(ROWS *G)
     __syncthreads();
     const int r = tile * ROWS + (int)(threadIdx.x / G);
     if (r < n) {
-      const uint32_t e = rowptr[r + 1];
-      VT a0 = 0, a1 = 0, a2 = 0;
-      const size_t voff = vs / S, coff = cs / 4;
-      // The first U blocks of the lane (rows of up to U*G blocks): a fixed,
-      // predicated trip count, so all of the lane's x gathers are in flight
-      // at once; same accumulation order as the loop below.
-      constexpr int U = (24 + G - 1) / G;
-      const uint32_t q0 = rowptr[r] + gl;
-      VT xg[U][3];
-#pragma unroll
-      for (int k = 0; k < U; ++k) {
-        const uint32_t q = q0 + k * G;
-        if (q < e) {
-          const uint32_t c = cb[q - coff];
-          xg[k][0] = ldg(x + (size_t)c * 3 + 0);
-          xg[k][1] = ldg(x + (size_t)c * 3 + 1);
-          xg[k][2] = ldg(x + (size_t)c * 3 + 2);
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < U; ++k) {
-        const uint32_t q = q0 + k * G;
-        if (q < e) {
-          const MT *v = vb + ((size_t)q * 9 - voff);
-          const VT x0 = xg[k][0], x1 = xg[k][1], x2 = xg[k][2];
-          a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
-          a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
-          a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
-        }
-      }
-#pragma unroll 4
-      for (uint32_t q = q0 + U * G; q < e; q += G) {
-        const uint32_t c = cb[q - coff];
-        const MT *v = vb + ((size_t)q * 9 - voff);
-        const VT x0 = ldg(x + (size_t)c * 3 + 0), x1 = ldg(x + (size_t)c * 3 + 1),
-                 x2 = ldg(x + (size_t)c * 3 + 2);
-        a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
-        a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
-        a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
-      }
-      a0 = group_sum<G>(a0, mask);
-      a1 = group_sum<G>(a1, mask);
-      a2 = group_sum<G>(a2, mask);
-      if (gl < 3) {
-        const VT yv = gl == 0 ? a0 : (gl == 1 ? a1 : a2);
-        y[(size_t)r * 3 + gl] = yv;
-        if (DOT) acc += (double)x[(size_t)r * 3 + gl] * (double)yv;
-      }
+      // two inlined copies: shared-memory loads for a staged tile, global
+      // loads for an oversize one
+      if (staged)
+        tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vbuf(b), cbuf(b), vs / S, cs / 4, x, y, acc);
+      else
+        tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vals, colidx, 0, 0, x, y, acc);
     }
     __syncthreads();
   }
@@ -269,8 +293,6 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32)
     const int64_t r0 = tile * RW;
     const uint32_t b0 = rowptr[r0], b1 = rowptr[min((int64_t)n, r0 + RW)];
     const bool staged = b1 - b0 <= (uint32_t)capb;
-    const MT *vb = staged ? vbuf(b) : vals;
-    const uint32_t *cb = staged ? cbuf(b) : colidx;
     const size_t vs = staged ? ((size_t)b0 * 9 * S) & ~size_t(15) : 0;
     const size_t cs = staged ? ((size_t)b0 * 4) & ~size_t(15) : 0;
     if (staged) {
@@ -285,50 +307,10 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32)
     __syncwarp();
     const int64_t r = r0 + lane / G;
     if (r < n) {
-      const uint32_t e = rowptr[r + 1];
-      VT a0 = 0, a1 = 0, a2 = 0;
-      const size_t voff = vs / S, coff = cs / 4;
-      constexpr int U = (24 + G - 1) / G;
-      const uint32_t q0 = rowptr[r] + gl;
-      VT xg[U][3];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const uint32_t q = q0 + u * G;
-        if (q < e) {
-          const uint32_t c = cb[q - coff];
-          xg[u][0] = ldg(x + (size_t)c * 3 + 0);
-          xg[u][1] = ldg(x + (size_t)c * 3 + 1);
-          xg[u][2] = ldg(x + (size_t)c * 3 + 2);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const uint32_t q = q0 + u * G;
-        if (q < e) {
-          const MT *v = vb + ((size_t)q * 9 - voff);
-          const VT x0 = xg[u][0], x1 = xg[u][1], x2 = xg[u][2];
-          a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
-          a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
-          a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
-        }
-      }
-      for (uint32_t q = q0 + U * G; q < e; q += G) {
-        const uint32_t c = cb[q - coff];
-        const MT *v = vb + ((size_t)q * 9 - voff);
-        const VT x0 = ldg(x + (size_t)c * 3 + 0), x1 = ldg(x + (size_t)c * 3 + 1),
-                 x2 = ldg(x + (size_t)c * 3 + 2);
-        a0 += (VT)v[0] * x0 + (VT)v[1] * x1 + (VT)v[2] * x2;
-        a1 += (VT)v[3] * x0 + (VT)v[4] * x1 + (VT)v[5] * x2;
-        a2 += (VT)v[6] * x0 + (VT)v[7] * x1 + (VT)v[8] * x2;
-      }
-      a0 = group_sum<G>(a0, mask);
-      a1 = group_sum<G>(a1, mask);
-      a2 = group_sum<G>(a2, mask);
-      if (gl < 3) {
-        const VT yv = gl == 0 ? a0 : (gl == 1 ? a1 : a2);
-        y[(size_t)r * 3 + gl] = yv;
-        if (DOT) acc += (double)x[(size_t)r * 3 + gl] * (double)yv;
-      }
+      if (staged)
+        tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vbuf(b), cbuf(b), vs / S, cs / 4, x, y, acc);
+      else
+        tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vals, colidx, 0, 0, x, y, acc);
     }
     __syncwarp();
   }

@@ -133,7 +133,7 @@ def test_spmv_f32(ctx, oracle, bs):
     assert np.all(np.abs(y.cpu().numpy() - ref) <= 2e-6 * scale + 1e-30)
 
 
-N_TMA_VARIANTS = 11
+N_TMA_VARIANTS = 12
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
