@@ -431,7 +431,7 @@ def peaks():
 
 def spmv_traffic(size):
     """DRAM bytes per SpMV launch from a committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "spmv_bsr3_tma_f32_traffic.json")
+    p = os.path.join(ROOT, "profiles", "spmv_bsr3_wtma_f32_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
