@@ -172,7 +172,7 @@ int sg_assemble_heat(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
  * bs = 1, 2, 3 have dedicated kernels; other bs use a generic kernel.
  * val_dtype is the matrix value type; vec_dtype the type of x and y;
  * accumulation is in the wider of the two.  g = 1,2,4,8,16,32 selects the
- * streaming kernel with g lanes per block row; g = -1..-12 selects variant
+ * streaming kernel with g lanes per block row; g = -1..-15 selects variant
  * -g-1 of the TMA-staged kernel (bs = 3, 16-byte aligned vals/colidx;
  * variants differ in lanes per row, rows per tile, pipeline stages and
  * whether a CTA or each warp runs the copy pipeline; a variant whose

@@ -68,31 +68,38 @@ __device__ __forceinline__ double cta_spmv(const BatchArgs &a, int r0, int r1, c
   double acc = 0;
   for (int r = r0 + (int)(threadIdx.x / G); r < r1; r += groups) {
     const uint32_t e = a.rowptr[r + 1];
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (uint32_t q = a.rowptr[r] + gl; q < e; q += G) {
-      const uint32_t c = a.colidx[q];
-      const float *v = a.vals + (size_t)q * 9;
-      const float x0 = xv[c * 3], x1 = xv[c * 3 + 1], x2 = xv[c * 3 + 2];
-      if (residual) {
+    if (residual) {  // FP64 accumulation (the true residual)
+      double s0 = 0, s1 = 0, s2 = 0;
+      for (uint32_t q = a.rowptr[r] + gl; q < e; q += G) {
+        const uint32_t c = a.colidx[q];
+        const float *v = a.vals + (size_t)q * 9;
+        const float x0 = xv[c * 3], x1 = xv[c * 3 + 1], x2 = xv[c * 3 + 2];
         s0 += (double)v[0] * x0 + (double)v[1] * x1 + (double)v[2] * x2;
         s1 += (double)v[3] * x0 + (double)v[4] * x1 + (double)v[5] * x2;
         s2 += (double)v[6] * x0 + (double)v[7] * x1 + (double)v[8] * x2;
-      } else {
-        s0 += (double)(v[0] * x0 + v[1] * x1 + v[2] * x2);
-        s1 += (double)(v[3] * x0 + v[4] * x1 + v[5] * x2);
-        s2 += (double)(v[6] * x0 + v[7] * x1 + v[8] * x2);
       }
-    }
-    s0 = group_sum<G>(s0, mask);
-    s1 = group_sum<G>(s1, mask);
-    s2 = group_sum<G>(s2, mask);
-    if (gl < 3) {
-      double val = gl == 0 ? s0 : (gl == 1 ? s1 : s2);
-      if (residual) {
-        val = (double)a.b[r * 3 + gl] - val;
+      s0 = group_sum<G>(s0, mask);
+      s1 = group_sum<G>(s1, mask);
+      s2 = group_sum<G>(s2, mask);
+      if (gl < 3) {
+        const double val = (double)a.b[r * 3 + gl] - (gl == 0 ? s0 : (gl == 1 ? s1 : s2));
         acc += val * val;
+        y[r * 3 + gl] = (float)val;
       }
-      y[r * 3 + gl] = (float)val;
+    } else {  // the iteration's SpMV: FP32, as the single-system solver
+      float s0 = 0, s1 = 0, s2 = 0;
+      for (uint32_t q = a.rowptr[r] + gl; q < e; q += G) {
+        const uint32_t c = a.colidx[q];
+        const float *v = a.vals + (size_t)q * 9;
+        const float x0 = xv[c * 3], x1 = xv[c * 3 + 1], x2 = xv[c * 3 + 2];
+        s0 += v[0] * x0 + v[1] * x1 + v[2] * x2;
+        s1 += v[3] * x0 + v[4] * x1 + v[5] * x2;
+        s2 += v[6] * x0 + v[7] * x1 + v[8] * x2;
+      }
+      s0 = group_sum<G>(s0, mask);
+      s1 = group_sum<G>(s1, mask);
+      s2 = group_sum<G>(s2, mask);
+      if (gl < 3) y[r * 3 + gl] = gl == 0 ? s0 : (gl == 1 ? s1 : s2);
     }
   }
   if (rr_out) *rr_out = acc;
@@ -160,17 +167,17 @@ __global__ void k_batched_pcg(BatchArgs a) {
     int it = 0, st = 0;
     double rz = 0;
     auto precondition = [&]() {
-      double t = 0;
+      DotAcc<float> t;
       for (int v = r0 + threadIdx.x; v < r1; v += blockDim.x) {
         const float *D = a.dinv + (size_t)v * 9;
         const float q0 = a.r[v * 3], q1 = a.r[v * 3 + 1], q2 = a.r[v * 3 + 2];
         for (int k = 0; k < 3; ++k) {
           const float zk = D[k * 3] * q0 + D[k * 3 + 1] * q1 + D[k * 3 + 2] * q2;
           a.z[v * 3 + k] = zk;
-          t += (double)a.r[v * 3 + k] * zk;
+          t.add(a.r[v * 3 + k], zk);
         }
       }
-      return cta_sum<G>(t, sh);
+      return cta_sum<G>(t.value(), sh);
     };
     if (!(rr > tol2)) {
       st = SG_STATUS_CONVERGED;
@@ -187,22 +194,22 @@ __global__ void k_batched_pcg(BatchArgs a) {
       // q = A p, p.q
       cta_spmv<G>(a, r0, r1, a.p, a.q, false, nullptr);
       __syncthreads();
-      double pq = 0;
-      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) pq += (double)a.p[i] * a.q[i];
-      pq = cta_sum<G>(pq, sh);
+      DotAcc<float> pqa;
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) pqa.add(a.p[i], a.q[i]);
+      const double pq = cta_sum<G>(pqa.value(), sh);
       if (!(pq > 0.0) || !isfinite(pq)) {
         st = isfinite(pq) ? SG_STATUS_BREAKDOWN : SG_STATUS_NAN;
         break;
       }
       const float al = (float)(rz / pq);
-      double rrl = 0;
+      DotAcc<float> rra;
       for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         a.x[i] += al * a.p[i];
         const float ri = a.r[i] - al * a.q[i];
         a.r[i] = ri;
-        rrl += (double)ri * ri;
+        rra.add(ri, ri);
       }
-      rrl = cta_sum<G>(rrl, sh);
+      const double rrl = cta_sum<G>(rra.value(), sh);
       ++it;
       double rznew = precondition();
       if (rrl <= tol2) {

@@ -180,14 +180,14 @@ __global__ void __launch_bounds__(RED_T) k_rz_zq(const SolveCtl *ctl, int64_t le
                                                  double *__restrict__ part) {
   __shared__ double sh[33];
   if (ctl && ctl->status != ST_RUNNING) return;
-  double rz = 0, zq = 0;
+  DotAcc<float> rz, zq;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
        i += (int64_t)gridDim.x * blockDim.x) {
-    rz += (double)r[i] * (double)z[i];
-    zq += (double)z[i] * (double)q[i];
+    rz.add(r[i], z[i]);
+    zq.add(z[i], q[i]);
   }
-  const double t0 = block_sum(rz, sh);
-  const double t1 = block_sum(zq, sh);
+  const double t0 = block_sum(rz.value(), sh);
+  const double t1 = block_sum(zq.value(), sh);
   if (threadIdx.x == 0) {
     part[gridDim.x + blockIdx.x] = t0;
     part[2 * gridDim.x + blockIdx.x] = t1;

@@ -109,8 +109,9 @@ static int launch_k1(Solver *S, cudaStream_t st) {
   const sg_matrix &A = S->A;
   if (S->tma) {
     const int vdt = sizeof(MT) == 8 ? SG_F64 : SG_F32, xdt = sizeof(VT) == 8 ? SG_F64 : SG_F32;
-    return bsr3_tma_launch(S->c, st, S->ctl, vdt, xdt, S->tma_var, 1, A.n, A.rowptr, A.colidx,
-                           S->bulk_vals, S->p, S->q, S->part1, S->pstats, S->P1, S->tma_smem);
+    return bsr3_tma_launch(S->c, st, S->ctl, A.bs, vdt, xdt, S->tma_var, 1, A.n, A.rowptr,
+                           A.colidx, S->bulk_vals, S->p, S->q, S->part1, S->pstats, S->P1,
+                           S->tma_smem);
   }
   const MT *vals = (const MT *)S->bulk_vals;
   const VT *p = (const VT *)S->p;
@@ -579,17 +580,19 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   if (o->precision == SG_SOLVE_MIXED) S->kind = KIND_MIXED;
   else S->kind = A->dtype == SG_F64 ? KIND_F64 : KIND_F64_M32;
   const size_t vt = S->kind == KIND_MIXED ? 4 : 8;
-  // K1: the TMA-staged kernel for 3x3 blocks with 16-byte aligned arrays
-  // (unless a lane count is forced), else G lanes per row.
+  // K1: the TMA-staged kernel for 3x3 or scalar blocks with 16-byte aligned
+  // arrays (unless a lane count is forced), else G lanes per row.
   const bool aligned = ((uintptr_t)A->vals % 16 == 0) && ((uintptr_t)A->colidx % 16 == 0);
-  if (A->bs == 3 && aligned && (o->lanes < 0 || (o->lanes == 0 && S->kind != KIND_F64))) {
+  if ((A->bs == 3 || A->bs == 1) && aligned &&
+      (o->lanes < 0 || (o->lanes == 0 && S->kind != KIND_F64))) {
     SG_TRY(cached_stats(c, A->n, A->rowptr, &S->pstats, true));
     S->maxrow = S->pstats.maxrow;
-    S->tma_var = o->lanes < 0 ? -o->lanes - 1 : default_tma_variant();
+    S->tma_var = o->lanes < 0 ? -o->lanes - 1 : default_tma_variant(A->bs);
     const int vdt = (S->kind == KIND_F64) ? SG_F64 : SG_F32;
     const int xdt = S->kind == KIND_MIXED ? SG_F32 : SG_F64;
     int grid = 0;
-    if (bsr3_tma_config(c, vdt, xdt, S->tma_var, 1, A->n, S->pstats, &grid, &S->tma_smem) ==
+    if (bsr3_tma_config(c, A->bs, vdt, xdt, S->tma_var, 1, A->n, S->pstats, &grid,
+                        &S->tma_smem) ==
         SG_OK) {
       S->tma = 1;
       S->P1 = grid;

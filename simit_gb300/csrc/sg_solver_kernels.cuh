@@ -76,6 +76,36 @@ __device__ __forceinline__ double sum_parts(const double *part, int np, double *
 
 template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
 
+// Per-thread dot-product accumulator.  FP64 arithmetic is scarce on this GPU
+// (a few FP64 FMAs per SM per cycle), so the FP32 kernels accumulate their
+// dot products as an unevaluated pair of floats: each product is split
+// exactly into p + e with the FMA residual (TwoProduct) and added with
+// Knuth's TwoSum, the compensated dot product "Dot2" of Ogita, Rump and
+// Oishi (SIAM J. Sci. Comput. 26(6), 2005).  The pair carries about 48
+// significant bits; value() converts it once to FP64, and the per-thread
+// values are summed in FP64 from there on.  The intrinsics (_rn) are never
+// contracted or reassociated by the compiler.  For FP64 operands the
+// accumulator is a plain FP64 sum.
+template <typename T> struct DotAcc;
+template <> struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);
+    const float s = __fadd_rn(hi, p);
+    const float bv = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(e, pe));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+template <> struct DotAcc<double> {
+  double v = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { v += a * b; }
+  __device__ __forceinline__ double value() const { return v; }
+};
+
 // K1: q = A p, partial p.q.  BS = 3 or 1 (G lanes per row), 0 = any bs.
 template <int BS, int G, typename MT, typename VT>
 __global__ void __launch_bounds__(RED_T) k_cg_spmv(const SolveCtl *__restrict__ ctl, int32_t n,
@@ -282,7 +312,7 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
   }
   const double alpha = rz / pq;
   const float a = (float)alpha;
-  double rr = 0, rzs = 0, zq = 0;
+  DotAcc<float> rr, rzs, zq;
   constexpr int W = PREC == PK_BLOCK3 ? 12 : 4;  // floats per thread step
   constexpr int NV = W / 4;                      // float4 per vector
   const int64_t nu = len / W;
@@ -327,10 +357,10 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
     }
 #pragma unroll
     for (int k = 0; k < W; ++k) {
-      rr += (double)rv[k] * (double)rv[k];
+      rr.add(rv[k], rv[k]);
       if (PREC != PK_EXTERNAL) {
-        rzs += (double)rv[k] * (double)zv[k];
-        zq += (double)zv[k] * (double)qv[k];
+        rzs.add(rv[k], zv[k]);
+        zq.add(zv[k], qv[k]);
       }
     }
   }
@@ -354,17 +384,17 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
           zv[k] = PREC == PK_JACOBI ? dinv[i] * rv[k] : rv[k];
         }
         if (PREC == PK_BLOCK3 || PREC == PK_JACOBI) z[i] = zv[k];
-        rr += (double)rv[k] * (double)rv[k];
+        rr.add(rv[k], rv[k]);
         if (PREC != PK_EXTERNAL) {
-          rzs += (double)rv[k] * (double)zv[k];
-          zq += (double)zv[k] * (double)q[i];
+          rzs.add(rv[k], zv[k]);
+          zq.add(zv[k], q[i]);
         }
       }
     }
   }
-  const double t0 = block_sum(rr, sh);
-  const double t1 = block_sum(rzs, sh);
-  const double t2 = block_sum(zq, sh);
+  const double t0 = block_sum(rr.value(), sh);
+  const double t1 = block_sum(rzs.value(), sh);
+  const double t2 = block_sum(zq.value(), sh);
   if (threadIdx.x == 0) {
     part_out[blockIdx.x] = t0;
     part_out[gridDim.x + blockIdx.x] = t1;

@@ -7,19 +7,22 @@
 namespace sg {
 
 // TMA SpMV variants: (lanes per block row, rows per CTA tile, pipeline
-// stages); ROWS = 0 selects the per-warp pipeline (tiles of 32/G rows per
-// warp).
+// stages); ROWS <= 0 selects the per-warp pipeline with warp tiles of
+// max(1, -ROWS) passes of 32/G rows (passes > 1 only for scalar CSR; for
+// 3x3 blocks those variants run one pass).
 struct TmaVariant {
   int G, ROWS, NST;
 };
 static const TmaVariant kTmaVariants[] = {
     {8, 32, 2}, {8, 32, 3}, {8, 16, 4}, {4, 32, 3}, {16, 16, 4}, {8, 16, 2},
     {8, 0, 2},  {8, 0, 3},  {8, 0, 4},  {4, 0, 2},  {4, 0, 3},  {2, 0, 2},
+    {4, -4, 2}, {4, -8, 2}, {8, -8, 2},
 };
 constexpr int kNumTmaVariants = sizeof(kTmaVariants) / sizeof(kTmaVariants[0]);
 // The variant g = 0 (and the solver) use: the fastest on the 128^3 lattice.
-constexpr int kDefaultTmaVariant = 9;  // per-warp, 4 lanes per row, 2 stages
-int default_tma_variant() { return kDefaultTmaVariant; }
+constexpr int kDefaultTmaVariant = 9;   // 3x3: per-warp, 4 lanes per row, 2 stages
+constexpr int kDefaultTmaVariant1 = 12; // scalar: per-warp, 4 lanes, 4 passes (32 rows)
+int default_tma_variant(int bs) { return bs == 1 ? kDefaultTmaVariant1 : kDefaultTmaVariant; }
 
 // Blocks in the largest tile of `rows` consecutive rows (the buffer size).
 static int tile_cap(int rows, const PatternStats &ps) {
@@ -61,13 +64,13 @@ static int tma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n,
   return SG_OK;
 }
 
-template <int G, int NST, typename MT, typename VT, bool DOT>
+template <int BS, int G, int NST, int P, typename MT, typename VT, bool DOT>
 static int wtma_config_t(Ctx *c, int32_t n, const PatternStats &ps, int *grid, size_t *smem) {
-  const int rows = 32 / G;
+  const int rows = 32 / G * P;
   const int capb = tile_cap(rows, ps);
-  const size_t sh = wtma_smem_bytes<MT>(capb, NST);
+  const size_t sh = wtma_smem_bytes<MT, BS * BS>(capb, NST);
   if (sh > 200 * 1024) return SG_ERR_UNSUPPORTED;
-  auto kern = k_bsr3_wtma<G, NST, MT, VT, DOT>;
+  auto kern = BS == 3 ? k_bsr3_wtma<G, NST, MT, VT, DOT> : k_csr_wtma<G, NST, P, MT, VT, DOT>;
   SG_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
   int per_sm = 0;
   SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WTMA_WARPS * 32, sh));
@@ -82,25 +85,30 @@ static int wtma_config_t(Ctx *c, int32_t n, const PatternStats &ps, int *grid, s
   return SG_OK;
 }
 
-template <int G, int NST, typename MT, typename VT, bool DOT>
+template <int BS, int G, int NST, int P, typename MT, typename VT, bool DOT>
 static int wtma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n,
                          const uint32_t *rp, const uint32_t *ci, const MT *v, const VT *x, VT *y,
                          double *part, const PatternStats &ps, int grid, size_t smem) {
-  const int capb = tile_cap(32 / G, ps);
-  k_bsr3_wtma<G, NST, MT, VT, DOT><<<grid, WTMA_WARPS * 32, smem, st>>>(ctl, n, rp, ci, v, x, y,
-                                                                       part, capb, c->d_err);
+  const int capb = tile_cap(32 / G * P, ps);
+  if (BS == 3)
+    k_bsr3_wtma<G, NST, MT, VT, DOT><<<grid, WTMA_WARPS * 32, smem, st>>>(ctl, n, rp, ci, v, x,
+                                                                         y, part, capb, c->d_err);
+  else
+    k_csr_wtma<G, NST, P, MT, VT, DOT><<<grid, WTMA_WARPS * 32, smem, st>>>(
+        ctl, n, rp, ci, v, x, y, part, capb, c->d_err);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
 
 // Dispatch over (variant, dot) for one (MT, VT).
 template <typename MT, typename VT>
-static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
+static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int bs, int var, int dot,
                         const SolveCtl *ctl, int32_t n, const uint32_t *rp, const uint32_t *ci,
                         const void *v, const void *x, void *y, double *part,
                         const PatternStats &ps, int *grid, size_t *smem) {
 #define SG_V(ID, G, R, N)                                                                      \
   case ID:                                                                                     \
+    if (bs != 3) return SG_ERR_UNSUPPORTED;                                                    \
     if (launch)                                                                                \
       return dot ? tma_launch_t<G, R, N, MT, VT, true>(c, st, ctl, n, rp, ci, (const MT *)v,   \
                                                        (const VT *)x, (VT *)y, part, ps,       \
@@ -117,57 +125,67 @@ static int tma_dispatch(Ctx *c, cudaStream_t st, bool launch, int var, int dot,
     SG_V(3, 4, 32, 3)
     SG_V(4, 16, 16, 4)
     SG_V(5, 8, 16, 2)
-#define SG_W(ID, G, N)                                                                         \
-  case ID:                                                                                     \
+#define SG_W1(ID, BS, G, N, P)                                                                    \
     if (launch)                                                                                \
-      return dot ? wtma_launch_t<G, N, MT, VT, true>(c, st, ctl, n, rp, ci, (const MT *)v,     \
-                                                     (const VT *)x, (VT *)y, part, ps, *grid,  \
-                                                     *smem)                                    \
-                 : wtma_launch_t<G, N, MT, VT, false>(c, st, ctl, n, rp, ci, (const MT *)v,    \
-                                                      (const VT *)x, (VT *)y, part, ps, *grid, \
-                                                      *smem);                                  \
-    return dot ? wtma_config_t<G, N, MT, VT, true>(c, n, ps, grid, smem)                       \
-               : wtma_config_t<G, N, MT, VT, false>(c, n, ps, grid, smem);
-    SG_W(6, 8, 2)
-    SG_W(7, 8, 3)
-    SG_W(8, 8, 4)
-    SG_W(9, 4, 2)
-    SG_W(10, 4, 3)
-    SG_W(11, 2, 2)
+      return dot ? wtma_launch_t<BS, G, N, P, MT, VT, true>(c, st, ctl, n, rp, ci, (const MT *)v, \
+                                                         (const VT *)x, (VT *)y, part, ps,     \
+                                                         *grid, *smem)                         \
+                 : wtma_launch_t<BS, G, N, P, MT, VT, false>(c, st, ctl, n, rp, ci,               \
+                                                          (const MT *)v, (const VT *)x,        \
+                                                          (VT *)y, part, ps, *grid, *smem);    \
+    return dot ? wtma_config_t<BS, G, N, P, MT, VT, true>(c, n, ps, grid, smem)                   \
+               : wtma_config_t<BS, G, N, P, MT, VT, false>(c, n, ps, grid, smem);
+#define SG_W(ID, G, N, P)                                                                      \
+  case ID:                                                                                     \
+    if (bs == 3) {                                                                             \
+      SG_W1(ID, 3, G, N, 1)                                                                    \
+    } else {                                                                                   \
+      SG_W1(ID, 1, G, N, P)                                                                    \
+    }
+    SG_W(6, 8, 2, 1)
+    SG_W(7, 8, 3, 1)
+    SG_W(8, 8, 4, 1)
+    SG_W(9, 4, 2, 1)
+    SG_W(10, 4, 3, 1)
+    SG_W(11, 2, 2, 1)
+    SG_W(12, 4, 2, 4)
+    SG_W(13, 4, 2, 8)
+    SG_W(14, 8, 2, 8)
     default: return SG_ERR_ARG;
   }
 #undef SG_V
 #undef SG_W
+#undef SG_W1
 }
 
-static int tma_any(Ctx *c, cudaStream_t st, bool launch, int vdt, int xdt, int var, int dot,
+static int tma_any(Ctx *c, cudaStream_t st, bool launch, int bs, int vdt, int xdt, int var, int dot,
                    const void *ctl, int32_t n, const uint32_t *rp, const uint32_t *ci,
                    const void *v, const void *x, void *y, double *part, const PatternStats &ps,
                    int *grid, size_t *smem) {
   const SolveCtl *k = (const SolveCtl *)ctl;
   if (vdt == SG_F32 && xdt == SG_F32)
-    return tma_dispatch<float, float>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part, ps,
+    return tma_dispatch<float, float>(c, st, launch, bs, var, dot, k, n, rp, ci, v, x, y, part, ps,
                                       grid, smem);
   if (vdt == SG_F64 && xdt == SG_F64)
-    return tma_dispatch<double, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part, ps,
+    return tma_dispatch<double, double>(c, st, launch, bs, var, dot, k, n, rp, ci, v, x, y, part, ps,
                                         grid, smem);
   if (vdt == SG_F32 && xdt == SG_F64)
-    return tma_dispatch<float, double>(c, st, launch, var, dot, k, n, rp, ci, v, x, y, part, ps,
+    return tma_dispatch<float, double>(c, st, launch, bs, var, dot, k, n, rp, ci, v, x, y, part, ps,
                                        grid, smem);
   return SG_ERR_UNSUPPORTED;
 }
 
-int bsr3_tma_config(Ctx *c, int vdt, int xdt, int var, int dot, int32_t n,
+int bsr3_tma_config(Ctx *c, int bs, int vdt, int xdt, int var, int dot, int32_t n,
                     const PatternStats &ps, int *grid, size_t *smem) {
-  return tma_any(c, nullptr, false, vdt, xdt, var, dot, nullptr, n, nullptr, nullptr, nullptr,
+  return tma_any(c, nullptr, false, bs, vdt, xdt, var, dot, nullptr, n, nullptr, nullptr, nullptr,
                  nullptr, nullptr, nullptr, ps, grid, smem);
 }
 
-int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int vdt, int xdt, int var, int dot,
-                    int32_t n, const uint32_t *rp, const uint32_t *ci, const void *v,
+int bsr3_tma_launch(Ctx *c, cudaStream_t st, const void *ctl, int bs, int vdt, int xdt, int var,
+                    int dot, int32_t n, const uint32_t *rp, const uint32_t *ci, const void *v,
                     const void *x, void *y, double *part, const PatternStats &ps, int grid,
                     size_t smem) {
-  return tma_any(c, st, true, vdt, xdt, var, dot, ctl, n, rp, ci, v, x, y, part, ps, &grid,
+  return tma_any(c, st, true, bs, vdt, xdt, var, dot, ctl, n, rp, ci, v, x, y, part, ps, &grid,
                  &smem);
 }
 
@@ -399,10 +417,11 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
   SG_REQUIRE(n >= 0 && bs >= 1 && bs <= 16, "sg_bspmv: bad n=%d bs=%d", n, bs);
   if (n == 0) return SG_OK;
   const bool aligned = ((uintptr_t)vals % 16 == 0) && ((uintptr_t)colidx % 16 == 0);
-  if (g < 0) SG_REQUIRE(bs == 3 && aligned && -g - 1 < kNumTmaVariants,
-                        "sg_bspmv: g=%d selects TMA variant %d: bs=3, 16-byte aligned arrays, "
-                        "-%d <= g <= -1", g, -g - 1, kNumTmaVariants);
-  if ((g == 0 && bs == 3 && aligned && !(vdt == SG_F64 && xdt == SG_F64)) || g < 0) {
+  if (g < 0) SG_REQUIRE((bs == 3 || bs == 1) && aligned && -g - 1 < kNumTmaVariants,
+                        "sg_bspmv: g=%d selects TMA variant %d: bs=3 or 1, 16-byte aligned "
+                        "arrays, -%d <= g <= -1", g, -g - 1, kNumTmaVariants);
+  if ((g == 0 && (bs == 3 || bs == 1) && aligned && !(vdt == SG_F64 && xdt == SG_F64)) ||
+      g < 0) {
     // TMA-staged kernel (lanes per row from the row length unless given).
     // FP64 matrices default to the plain kernel, which keeps more warps in
     // flight for the FP64 pipe.
@@ -410,10 +429,10 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
     size_t sh = 0;
     PatternStats ps;
     SG_TRY(cached_stats(c, n, rowptr, &ps));
-    const int var = g < 0 ? -g - 1 : kDefaultTmaVariant;
-    if (bsr3_tma_config(c, vdt, xdt, var, 0, n, ps, &grid, &sh) == SG_OK)
-      return bsr3_tma_launch(c, c->stream, nullptr, vdt, xdt, var, 0, n, rowptr, colidx, vals, x,
-                             y, nullptr, ps, grid, sh);
+    const int var = g < 0 ? -g - 1 : default_tma_variant(bs);
+    if (bsr3_tma_config(c, bs, vdt, xdt, var, 0, n, ps, &grid, &sh) == SG_OK)
+      return bsr3_tma_launch(c, c->stream, nullptr, bs, vdt, xdt, var, 0, n, rowptr, colidx, vals,
+                             x, y, nullptr, ps, grid, sh);
     // the variant's buffers do not fit the largest tile (very long rows):
     // the streaming G-lane kernel needs no staging
     g = 0;

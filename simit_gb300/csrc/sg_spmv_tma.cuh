@@ -16,9 +16,9 @@
 
 namespace sg {
 
-template <typename MT>
+template <typename MT, int BB = 9>
 __host__ __device__ inline size_t tma_vbytes(int capb) {
-  return (((size_t)capb * 9 * sizeof(MT) + 32) + 15) & ~size_t(15);
+  return (((size_t)capb * BB * sizeof(MT) + 32) + 15) & ~size_t(15);
 }
 __host__ __device__ inline size_t tma_cbytes(int capb) {
   return (((size_t)capb * 4 + 32) + 15) & ~size_t(15);
@@ -32,14 +32,14 @@ template <typename MT> inline size_t tma_smem_bytes(int capb, int nst) {
 // blocks rowptr[r]+gl, +G, ...  The first U blocks of each lane (rows of up
 // to 24 blocks) use a fixed, predicated trip count so all of the lane's x
 // gathers are in flight at once; the remainder loop keeps the same
-// accumulation order.  With DOT, acc += x_r . y_r.
+// accumulation order.  With DOT, acc accumulates x_r . y_r (DotAcc).
 template <int G, typename MT, typename VT, bool DOT>
 __device__ __forceinline__ void tile_row(int64_t r, int gl, unsigned mask,
                                          const uint32_t *__restrict__ rowptr,
                                          const MT *__restrict__ vb,
                                          const uint32_t *__restrict__ cb, size_t voff,
                                          size_t coff, const VT *__restrict__ x,
-                                         VT *__restrict__ y, double &acc) {
+                                         VT *__restrict__ y, DotAcc<VT> &acc) {
   const uint32_t e = rowptr[r + 1];
   VT a0 = 0, a1 = 0, a2 = 0;
   constexpr int U = (24 + G - 1) / G;
@@ -83,15 +83,50 @@ __device__ __forceinline__ void tile_row(int64_t r, int gl, unsigned mask,
     if (gl < 3) {
       const VT yv = gl == 0 ? a0 : (gl == 1 ? a1 : a2);
       y[(size_t)r * 3 + gl] = yv;
-      if (DOT) acc += (double)x[(size_t)r * 3 + gl] * (double)yv;
+      if (DOT) acc.add(x[(size_t)r * 3 + gl], yv);
     }
   } else if (gl == 0) {  // fewer than 3 lanes: lane 0 writes the row
     y[(size_t)r * 3 + 0] = a0;
     y[(size_t)r * 3 + 1] = a1;
     y[(size_t)r * 3 + 2] = a2;
-    if (DOT)
-      acc += (double)x[(size_t)r * 3] * (double)a0 + (double)x[(size_t)r * 3 + 1] * (double)a1 +
-             (double)x[(size_t)r * 3 + 2] * (double)a2;
+    if (DOT) {
+      acc.add(x[(size_t)r * 3], a0);
+      acc.add(x[(size_t)r * 3 + 1], a1);
+      acc.add(x[(size_t)r * 3 + 2], a2);
+    }
+  }
+}
+
+// Scalar CSR row (1x1 blocks): y_r = sum_q vb[q - voff] x[cb[q - coff]],
+// same lane split, predicated gathers and accumulation order as tile_row.
+template <int G, typename MT, typename VT, bool DOT>
+__device__ __forceinline__ void tile_row1(int64_t r, int gl, unsigned mask,
+                                          const uint32_t *__restrict__ rowptr,
+                                          const MT *__restrict__ vb,
+                                          const uint32_t *__restrict__ cb, size_t voff,
+                                          size_t coff, const VT *__restrict__ x,
+                                          VT *__restrict__ y, DotAcc<VT> &acc) {
+  const uint32_t e = rowptr[r + 1];
+  VT a = 0;
+  constexpr int U = (24 + G - 1) / G;
+  const uint32_t q0 = rowptr[r] + gl;
+  VT xg[U];
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const uint32_t q = q0 + k * G;
+    if (q < e) xg[k] = ldg(x + cb[q - coff]);
+  }
+#pragma unroll
+  for (int k = 0; k < U; ++k) {
+    const uint32_t q = q0 + k * G;
+    if (q < e) a += (VT)vb[q - voff] * xg[k];
+  }
+#pragma unroll 4
+  for (uint32_t q = q0 + U * G; q < e; q += G) a += (VT)vb[q - voff] * ldg(x + cb[q - coff]);
+  a = group_sum<G>(a, mask);
+  if (gl == 0) {
+    y[r] = a;
+    if (DOT) acc.add(x[r], a);
   }
 }
 
@@ -152,7 +187,7 @@ __global__ void __launch_bounds__(ROWS *G)
 
   const int gl = threadIdx.x & (G - 1);
   const unsigned mask = group_mask<G>();
-  double acc = 0;
+  DotAcc<VT> acc;
   // local tile k of this CTA is global tile blockIdx.x + k*gridDim.x
   const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   if (threadIdx.x == 0)
@@ -201,7 +236,7 @@ __global__ void __launch_bounds__(ROWS *G)
     __syncthreads();
   }
   if (DOT) {
-    const double t = block_sum(acc, shred);
+    const double t = block_sum(acc.value(), shred);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
   }
 }
@@ -218,25 +253,30 @@ namespace sg {
 // were stale, or a very long row) is read straight from global memory.
 constexpr int WTMA_WARPS = 4;
 
-template <typename MT> inline size_t wtma_smem_bytes(int capb, int nst) {
+template <typename MT, int BB = 9> inline size_t wtma_smem_bytes(int capb, int nst) {
   return (((size_t)WTMA_WARPS * nst * 8 + 15) & ~size_t(15)) +
-         (size_t)WTMA_WARPS * nst * (tma_vbytes<MT>(capb) + tma_cbytes(capb));
+         (size_t)WTMA_WARPS * nst * (tma_vbytes<MT, BB>(capb) + tma_cbytes(capb));
 }
 
-template <int G, int NST, typename MT, typename VT, bool DOT>
-__global__ void __launch_bounds__(WTMA_WARPS * 32)
-    k_bsr3_wtma(const SolveCtl *__restrict__ ctl, int32_t n, const uint32_t *__restrict__ rowptr,
-                const uint32_t *__restrict__ colidx, const MT *__restrict__ vals,
-                const VT *__restrict__ x, VT *__restrict__ y, double *__restrict__ part,
-                int capb, int *err) {
+// Body shared by the 3x3 (BS = 3) and scalar CSR (BS = 1) kernels.  A warp
+// tile is P passes of 32/G rows (P > 1 makes the bulk copies of short
+// scalar rows larger).
+template <int BS, int G, int NST, int P, typename MT, typename VT, bool DOT>
+__device__ __forceinline__ void wtma_body(const SolveCtl *__restrict__ ctl, int32_t n,
+                                          const uint32_t *__restrict__ rowptr,
+                                          const uint32_t *__restrict__ colidx,
+                                          const MT *__restrict__ vals, const VT *__restrict__ x,
+                                          VT *__restrict__ y, double *__restrict__ part,
+                                          int capb, int *err, unsigned char *sm,
+                                          double *shred) {
   static_assert(NST >= 2 && NST <= 6, "stages");
-  constexpr int RW = 32 / G;
+  static_assert(BS == 1 || BS == 3, "block size");
+  constexpr int RW = 32 / G * P;
+  constexpr int BB = BS * BS;
   constexpr size_t S = sizeof(MT);
-  extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ double shred[33];
   if (ctl && ctl->status != ST_RUNNING) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t vbytes = tma_vbytes<MT>(capb), cbytes = tma_cbytes(capb);
+  const size_t vbytes = tma_vbytes<MT, BB>(capb), cbytes = tma_cbytes(capb);
   const size_t stage = vbytes + cbytes;
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm) + warp * NST;
   unsigned char *base =
@@ -256,7 +296,7 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32)
     const int64_t r0 = tile * RW;
     const int64_t r1 = min((int64_t)n, r0 + RW);
     const uint32_t b0 = rowptr[r0], b1 = rowptr[r1];
-    const size_t vs = ((size_t)b0 * 9 * S) & ~size_t(15), ve = ((size_t)b1 * 9 * S) & ~size_t(15);
+    const size_t vs = ((size_t)b0 * BB * S) & ~size_t(15), ve = ((size_t)b1 * BB * S) & ~size_t(15);
     const size_t cs = ((size_t)b0 * 4) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
     fence_proxy_async_smem();
     if (b1 - b0 > (uint32_t)capb) {  // larger than the buffers: read from global
@@ -275,7 +315,7 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32)
     for (int k = 0; k < NST - 1 && k < my; ++k) issue(gw + k * nw, k);
   const int gl = lane & (G - 1);
   const unsigned mask = group_mask<G>();
-  double acc = 0;
+  DotAcc<VT> acc;
   for (int64_t k = 0; k < my; ++k) {
     const int b = (int)(k % NST);
     const int64_t tile = gw + k * nw;
@@ -293,31 +333,68 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32)
     const int64_t r0 = tile * RW;
     const uint32_t b0 = rowptr[r0], b1 = rowptr[min((int64_t)n, r0 + RW)];
     const bool staged = b1 - b0 <= (uint32_t)capb;
-    const size_t vs = staged ? ((size_t)b0 * 9 * S) & ~size_t(15) : 0;
+    const size_t vs = staged ? ((size_t)b0 * BB * S) & ~size_t(15) : 0;
     const size_t cs = staged ? ((size_t)b0 * 4) & ~size_t(15) : 0;
     if (staged) {
       // unaligned tails (< 16 bytes each)
-      const size_t ve = ((size_t)b1 * 9 * S) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
-      const int vt = (int)(((size_t)b1 * 9 * S - ve) / S);
+      const size_t ve = ((size_t)b1 * BB * S) & ~size_t(15), ce = ((size_t)b1 * 4) & ~size_t(15);
+      const int vt = (int)(((size_t)b1 * BB * S - ve) / S);
       const int ct = (int)(((size_t)b1 * 4 - ce) / 4);
       if (lane < vt) vbuf(b)[(ve - vs) / S + lane] = vals[ve / S + lane];
       if (lane >= 16 && lane < 16 + ct)
         cbuf(b)[(ce - cs) / 4 + lane - 16] = colidx[ce / 4 + lane - 16];
     }
     __syncwarp();
-    const int64_t r = r0 + lane / G;
+#pragma unroll
+    for (int pp = 0; pp < P; ++pp) {
+    const int64_t r = r0 + pp * (32 / G) + lane / G;
     if (r < n) {
-      if (staged)
-        tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vbuf(b), cbuf(b), vs / S, cs / 4, x, y, acc);
-      else
-        tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vals, colidx, 0, 0, x, y, acc);
+      if (BS == 3) {
+        if (staged)
+          tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vbuf(b), cbuf(b), vs / S, cs / 4, x, y,
+                                   acc);
+        else
+          tile_row<G, MT, VT, DOT>(r, gl, mask, rowptr, vals, colidx, 0, 0, x, y, acc);
+      } else {
+        if (staged)
+          tile_row1<G, MT, VT, DOT>(r, gl, mask, rowptr, vbuf(b), cbuf(b), vs / S, cs / 4, x, y,
+                                    acc);
+        else
+          tile_row1<G, MT, VT, DOT>(r, gl, mask, rowptr, vals, colidx, 0, 0, x, y, acc);
+      }
+    }
     }
     __syncwarp();
   }
   if (DOT) {
-    const double t = block_sum(acc, shred);
+    const double t = block_sum(acc.value(), shred);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
   }
+}
+
+template <int G, int NST, typename MT, typename VT, bool DOT>
+__global__ void __launch_bounds__(WTMA_WARPS * 32)
+    k_bsr3_wtma(const SolveCtl *__restrict__ ctl, int32_t n, const uint32_t *__restrict__ rowptr,
+                const uint32_t *__restrict__ colidx, const MT *__restrict__ vals,
+                const VT *__restrict__ x, VT *__restrict__ y, double *__restrict__ part,
+                int capb, int *err) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ double shred[33];
+  wtma_body<3, G, NST, 1, MT, VT, DOT>(ctl, n, rowptr, colidx, vals, x, y, part, capb, err, sm,
+                                       shred);
+}
+
+// Scalar CSR (bs = 1) with the same per-warp pipeline, tiles of P passes.
+template <int G, int NST, int P, typename MT, typename VT, bool DOT>
+__global__ void __launch_bounds__(WTMA_WARPS * 32)
+    k_csr_wtma(const SolveCtl *__restrict__ ctl, int32_t n, const uint32_t *__restrict__ rowptr,
+               const uint32_t *__restrict__ colidx, const MT *__restrict__ vals,
+               const VT *__restrict__ x, VT *__restrict__ y, double *__restrict__ part,
+               int capb, int *err) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ double shred[33];
+  wtma_body<1, G, NST, P, MT, VT, DOT>(ctl, n, rowptr, colidx, vals, x, y, part, capb, err, sm,
+                                       shred);
 }
 
 }  // namespace sg

@@ -133,13 +133,15 @@ def test_spmv_f32(ctx, oracle, bs):
     assert np.all(np.abs(y.cpu().numpy() - ref) <= 2e-6 * scale + 1e-30)
 
 
-N_TMA_VARIANTS = 12
+N_TMA_VARIANTS = 15
 
 
+@pytest.mark.parametrize("bs", [3, 1])
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 @pytest.mark.parametrize("variant", range(N_TMA_VARIANTS))
-def test_spmv_tma_variants(ctx, oracle, variant, dt):
-    """Every TMA-staged SpMV variant (CTA tiles and per-warp pipelines), on
+def test_spmv_tma_variants(ctx, oracle, variant, dt, bs):
+    """Every TMA-staged SpMV variant (CTA tiles and per-warp pipelines; for
+    scalar CSR the per-warp ones, the others run the streaming kernel), on
     a random graph plus a hub vertex whose ~60-block row runs past the
     predicated part of each lane's loop; unaligned tile heads and tails
     throughout (36- and 72-byte blocks)."""
@@ -150,14 +152,14 @@ def test_spmv_tma_variants(ctx, oracle, variant, dt):
                          np.stack([np.full(60, 7), g0.integers(0, n, 60)], 1).reshape(-1)])
     rp, ci = oracle.pattern(n, ep.astype(np.int32), 2)
     g = meshgen.rng(91 + variant)
-    vals = g.uniform(-1, 1, size=len(ci) * 9).astype(dt)
-    x = g.uniform(-1, 1, size=n * 3).astype(dt)
-    ref = oracle.spmv(n, 3, rp, ci, vals.astype(np.float64), x.astype(np.float64))
-    scale = oracle.spmv(n, 3, rp, ci, np.abs(vals).astype(np.float64),
+    vals = g.uniform(-1, 1, size=len(ci) * bs * bs).astype(dt)
+    x = g.uniform(-1, 1, size=n * bs).astype(dt)
+    ref = oracle.spmv(n, bs, rp, ci, vals.astype(np.float64), x.astype(np.float64))
+    scale = oracle.spmv(n, bs, rp, ci, np.abs(vals).astype(np.float64),
                         np.abs(x).astype(np.float64))
     d = ctx.device
     t = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(d)  # noqa
-    y = bspmv(ctx, n, 3, t(rp), t(ci), t(vals), t(x), g=-1 - variant)
+    y = bspmv(ctx, n, bs, t(rp), t(ci), t(vals), t(x), g=-1 - variant)
     ctx.sync()
     tol = 2e-6 if dt == np.float32 else 1e-14
     assert np.all(np.abs(y.cpu().numpy() - ref) <= tol * scale + 1e-300)
