@@ -138,10 +138,9 @@ static int launch_k1(Solver *S, cudaStream_t st) {
 
 template <int PREC>
 static void launch_k2_v4(Solver *S, cudaStream_t st, int par) {
-  k_cg_update_v4<PREC><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part1, S->P1,
-                                                (const float *)S->p, (const float *)S->q,
-                                                (float *)S->r, (float *)S->xupd, (float *)S->z,
-                                                (const float *)S->dinv, S->part2);
+  k_cg_update_v4<PREC, PREC != PK_EXTERNAL><<<S->P2, RED_T, 0, st>>>(
+      S->ctl, par, S->len, S->part1, S->P1, S->tma, (const float *)S->p, (const float *)S->q,
+      (float *)S->r, (float *)S->xupd, (float *)S->z, (const float *)S->dinv, S->part2);
 }
 
 template <typename VT, typename XT>
@@ -184,9 +183,10 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
 template <typename VT>
 static int launch_k3(Solver *S, cudaStream_t st, int par) {
   const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
-  if (sizeof(VT) == 4)
+  if (sizeof(VT) == 4)  // K2 decided unless an external preconditioner ran after it
     k_cg_direction_v4<<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2,
-                                               (const float *)z, (float *)S->p);
+                                               S->prec != PK_EXTERNAL, (const float *)z,
+                                               (float *)S->p);
   else
     k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z,
                                                 (VT *)S->p);

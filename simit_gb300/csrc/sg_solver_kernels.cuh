@@ -47,6 +47,13 @@ struct SolveCtl {
   double upd2;        // NEED_CHECK when r.r < upd2 (reliable update); 0 = off
   double last_rr;     // r.r at the last K3 (diagnostics)
   double last_alpha;
+  // Last-CTA finalisation (see finalize_partials): K1's p.q total, and the
+  // direction coefficient K2 decides for K3.  One slot each suffices: the
+  // kernel that writes a slot never reads it, and stream order separates
+  // the next write from the last read.
+  double pq_tot;
+  double beta;
+  unsigned int tick1, tick2;
 };
 
 constexpr int RED_T = 256;
@@ -75,6 +82,61 @@ __device__ __forceinline__ double sum_parts(const double *part, int np, double *
 }
 
 template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
+
+// Last-CTA finalisation of per-CTA partial sums (nv arrays of gridDim.x
+// values at part, part + gridDim.x, ...): every CTA stores its partials and
+// takes a ticket; the CTA that takes the last ticket sums each array in index
+// order (so the totals are deterministic), stores them in tot[0..nv) and
+// re-arms the ticket.  Returns true in that CTA.  Called by all threads.
+__device__ __forceinline__ bool finalize_partials(const double *t, int nv, double *part,
+                                                  unsigned int *ticket, double *tot,
+                                                  double *sh) {
+  __shared__ int last;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < nv; ++k) part[k * gridDim.x + blockIdx.x] = t[k];
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  for (int k = 0; k < nv; ++k) {
+    double a = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      a += __ldcg(part + k * gridDim.x + i);
+    const double s = block_sum(a, sh);
+    if (threadIdx.x == 0) tot[k] = s;
+  }
+  if (threadIdx.x == 0) *ticket = 0;
+  return true;
+}
+
+// The control decision after K2's dots (shared by the finalising K2 and the
+// reducing K3): iteration count, r.z slot, status, beta.  Executed by one
+// thread; returns the new status.
+__device__ __forceinline__ int cg_decide(SolveCtl *ctl, int par, double rr, double rznew,
+                                         double zq, double alpha) {
+  const double rzold = ctl->rz[par];
+  const int it = ctl->iter[par] + 1;
+  int st = ST_RUNNING;
+  const bool lost = ctl->flexible && !ctl->fallback && !(rznew > 0.0);
+  if (lost) st = ST_NEED_CHECK;  // z is no descent direction: fall back
+  else if (!isfinite(rr) || !isfinite(rznew)) st = ST_NAN;
+  else if (rr <= ctl->tol2) st = ST_NEED_CHECK;
+  else if (ctl->upd2 > 0.0 && rr < ctl->upd2) st = ST_NEED_CHECK;
+  else if (ctl->check_every > 0 && it % ctl->check_every == 0) st = ST_NEED_CHECK;
+  else if (it >= ctl->maxiters) st = ST_MAXITER;
+  ctl->iter[par ^ 1] = it;
+  ctl->rz[par ^ 1] = rznew;
+  ctl->last_rr = rr;
+  if (lost) ctl->fallback = 1;
+  // Fletcher-Reeves (the reference's beta = r'r_new / r'r_old, with z) or
+  // Polak-Ribiere for a variable preconditioner: (z.r_new - z.r_old)/rz_old
+  // where r_new - r_old = -alpha q.
+  ctl->beta = ctl->flexible ? (-alpha * zq) / rzold : rznew / rzold;
+  if (st != ST_RUNNING) ctl->status = st;
+  return st;
+}
 
 // Per-thread dot-product accumulator.  FP64 arithmetic is scarce on this GPU
 // (a few FP64 FMAs per SM per cycle), so the FP32 kernels accumulate their
@@ -292,10 +354,14 @@ __device__ __forceinline__ void st4(float *p, int64_t i, const float *o) {
   reinterpret_cast<float4 *>(p)[i] = make_float4(o[0], o[1], o[2], o[3]);
 }
 
-template <int PREC>
+// pq_fin: K1 left the p.q total in ctl->pq_tot (else the np1 partials are
+// summed here).  FIN (not with an external preconditioner, whose dots come
+// after K2): the last CTA sums r.r, r.z, z.q and takes K3's decision.
+template <int PREC, bool FIN>
 __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int par, int64_t len,
                                                         const double *__restrict__ part_in,
-                                                        int np1, const float *__restrict__ p,
+                                                        int np1, int pq_fin,
+                                                        const float *__restrict__ p,
                                                         const float *__restrict__ q,
                                                         float *__restrict__ r,
                                                         float *__restrict__ x,
@@ -304,7 +370,7 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
                                                         double *__restrict__ part_out) {
   __shared__ double sh[33];
   if (ctl->status != ST_RUNNING) return;
-  const double pq = sum_parts(part_in, np1, sh);
+  const double pq = pq_fin ? ctl->pq_tot : sum_parts(part_in, np1, sh);
   const double rz = ctl->rz[par];
   if (!(pq > 0.0) || !isfinite(pq)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
@@ -392,25 +458,48 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
       }
     }
   }
-  const double t0 = block_sum(rr.value(), sh);
-  const double t1 = block_sum(rzs.value(), sh);
-  const double t2 = block_sum(zq.value(), sh);
-  if (threadIdx.x == 0) {
-    part_out[blockIdx.x] = t0;
-    part_out[gridDim.x + blockIdx.x] = t1;
-    part_out[2 * gridDim.x + blockIdx.x] = t2;
+  const double t[3] = {block_sum(rr.value(), sh), block_sum(rzs.value(), sh),
+                       block_sum(zq.value(), sh)};
+  if (FIN) {
+    double tot[3];  // written and read by thread 0 of the last CTA
+    if (finalize_partials(t, 3, part_out, &ctl->tick2, tot, sh) && threadIdx.x == 0) {
+      ctl->last_alpha = alpha;
+      cg_decide(ctl, par, tot[0], tot[1], tot[2], alpha);
+    }
+  } else if (threadIdx.x == 0) {
+    part_out[blockIdx.x] = t[0];
+    part_out[gridDim.x + blockIdx.x] = t[1];
+    part_out[2 * gridDim.x + blockIdx.x] = t[2];
     if (blockIdx.x == 0) ctl->last_alpha = alpha;
   }
 }
 
 // K3 for FP32 vectors: the control decisions of k_cg_direction, then
 // p = z + beta p with float4 accesses.
+// fin: K2 already took the decision and left beta in ctl->beta.
 static __global__ void __launch_bounds__(RED_T) k_cg_direction_v4(SolveCtl *ctl, int par, int64_t len,
                                                            const double *__restrict__ part_in,
-                                                           int np2, const float *__restrict__ z,
+                                                           int np2, int fin,
+                                                           const float *__restrict__ z,
                                                            float *__restrict__ p) {
   __shared__ double sh[33];
   if (ctl->status != ST_RUNNING) return;
+  if (fin) {
+    const float b = (float)ctl->beta;
+    const int64_t nu = len / 4;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu;
+         u += (int64_t)gridDim.x * blockDim.x) {
+      float zv[4], pv[4];
+      ld4(z, u, zv);
+      ld4(p, u, pv);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) pv[k] = zv[k] + b * pv[k];
+      st4(p, u, pv);
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
+      for (int64_t i = nu * 4; i < len; ++i) p[i] = z[i] + b * p[i];
+    return;
+  }
   const double rr = sum_parts(part_in, np2, sh);
   const double rznew = sum_parts(part_in + np2, np2, sh);
   const double zq = sum_parts(part_in + 2 * np2, np2, sh);

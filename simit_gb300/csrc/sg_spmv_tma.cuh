@@ -235,9 +235,10 @@ __global__ void __launch_bounds__(ROWS *G)
     }
     __syncthreads();
   }
-  if (DOT) {
+  if (DOT) {  // CG K1: the last CTA leaves the p.q total in ctl->pq_tot
     const double t = block_sum(acc.value(), shred);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    SolveCtl *c = const_cast<SolveCtl *>(ctl);
+    finalize_partials(&t, 1, part, &c->tick1, &c->pq_tot, shred);
   }
 }
 
@@ -366,9 +367,10 @@ __device__ __forceinline__ void wtma_body(const SolveCtl *__restrict__ ctl, int3
     }
     __syncwarp();
   }
-  if (DOT) {
+  if (DOT) {  // CG K1: the last CTA leaves the p.q total in ctl->pq_tot
     const double t = block_sum(acc.value(), shred);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    SolveCtl *c = const_cast<SolveCtl *>(ctl);
+    finalize_partials(&t, 1, part, &c->tick1, &c->pq_tot, shred);
   }
 }
 
