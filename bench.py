@@ -50,6 +50,9 @@ def parse():
                     help="profiling driver: two steps of the --size system with the solver "
                          "capped at --iters iterations")
     ap.add_argument("--iters", type=int, default=64)
+    ap.add_argument("--learned-solve", action="store_true",
+                    help="profiling driver: the --size system with the learned preconditioner, "
+                         "capped at --iters iterations")
     ap.add_argument("--heat", action="store_true",
                     help="P1 heat (128^3): 1000 SpMVs FP32 vs FP64, CG FP64 vs mixed")
     return ap.parse_args()
@@ -266,6 +269,38 @@ def run_solve_only(args):
     ms, r = _ev_ms(ctx.torch_stream, p.step)
     print(json.dumps({"size": args.size, "iters": r.iters, "status": r.status, "step_ms": ms,
                       "kernels": r.kernels}), flush=True)
+
+
+def run_learned_solve(args):
+    """Profiling driver: the --size heterogeneous-elasticity system solved
+    with the learned (symmetric form) preconditioner, capped at --iters
+    iterations; the second solve is event-timed."""
+    import torch
+    from simit_gb300 import _lib, problems
+    from simit_gb300 import learned as lrn
+    from simit_gb300.runtime import Context, Solver, solve_opts
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    p = problems.HeteroElasticity(ctx, problems.hetero_mesh(args.size), dtype=torch.float32,
+                                  precond=_lib.PRECOND_BLOCK_JACOBI)
+    m = p.mesh
+    with ctx.stream():
+        prm = torch.tensor(lrn.load_weights("sym"), device=ctx.device)
+        xs = torch.zeros_like(p.b)
+    S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, m.nnzb,
+               solve_opts(precision=_lib.SOLVE_MIXED, precond=_lib.PRECOND_LEARNED, tol=1e-8,
+                          maxiters=args.iters, learned_params=prm, learned_form=_lib.MPNN_SYM),
+               learned_params_keep=prm)
+
+    def one():
+        with ctx.stream():
+            xs.zero_()
+        return S.solve(p.b, xs)
+    one()
+    ms, r = _ev_ms(ctx.torch_stream, one)
+    print(json.dumps({"size": args.size, "iters": r.iters, "solve_ms": ms,
+                      "ms_per_iter": ms / max(1, r.iters)}), flush=True)
+    S.close()
 
 
 def run_spmv_only(args):
@@ -620,6 +655,9 @@ def main():
     args = parse()
     if args.solve_only:
         run_solve_only(args)
+        return
+    if args.learned_solve:
+        run_learned_solve(args)
         return
     if args.spmv_only:
         run_spmv_only(args)

@@ -136,6 +136,16 @@ int sg_assemble_scalar_springs(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
                                const void *a, double diag, double scale,
                                void *vals, int exact);
 
+/* Generic `map f to E reduce +` for a caller-evaluated element function
+ * (src/lower/lower_maps.cpp:54-128; src/inline.cpp:690-888): eb holds
+ * nE*card*card blocks of bs*bs values, block (i, j) of element e at
+ * ((e*card + i)*card + j)*bs*bs, row-major, zero where the function writes
+ * nothing; each is added into the slot of (endpoint i, endpoint j) of the
+ * mesh's pattern, in element order (so FP64 sums are the reference's).
+ * bs 1..3, card 2..4.  exact = 1: no contraction (parity mode). */
+int sg_assemble_blocks(sg_ctx *ctx, const sg_mesh *mesh, int dtype, int bs, const void *eb,
+                       void *vals, int exact);
+
 /* precomputeTetMat (femTet.sim; apps/fem/fem_linear.sim:176-193):
  * B = inv(Ds) [nE*9], W = -det(Ds)/6 [nE], vertex mass m [n] = sum of
  * 0.25*rho*W in element order. */

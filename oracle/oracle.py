@@ -130,6 +130,19 @@ def slots(ep, card, rowptr, colidx):
     return out
 
 
+def assemble_blocks(ep, card, bs, eb, rowptr, colidx):
+    """`map f to E reduce +` (src/lower/lower_maps.cpp:54-128): for elements
+    in order, for (i, j), += block (i, j) into the slot loc(ep[i], ep[j])
+    (src/runtime.cpp:19-23), FP64."""
+    sl = slots(ep, card, rowptr, colidx).astype(np.int64)
+    eb = np.asarray(eb, np.float64).reshape(-1, card * card, bs * bs)
+    vals = np.zeros((len(colidx), bs * bs))
+    for e in range(eb.shape[0]):
+        for ij in range(card * card):
+            vals[sl[e * card * card + ij]] += eb[e, ij]
+    return vals.reshape(-1)
+
+
 def spmv(n, bs, rowptr, colidx, vals, x):
     if vals.dtype == np.float32:
         y = np.zeros(n * bs, np.float32)

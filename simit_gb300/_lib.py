@@ -78,6 +78,7 @@ SIGNATURES = {
     "sg_pattern_maxrow": (_CI, [P, I32, P, ctypes.POINTER(I32)]),
     "sg_assemble_springs": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, D, D, P, P, P, _CI]),
     "sg_assemble_scalar_springs": (_CI, [P, _MP, _CI, P, D, D, P, _CI]),
+    "sg_assemble_blocks": (_CI, [P, _MP, _CI, _CI, P, P, _CI]),
     "sg_tet_precompute": (_CI, [P, _MP, _CI, P, D, P, P, P]),
     "sg_assemble_tet_stiffness": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, D, D, P, _CI]),
     "sg_assemble_tet_force": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, P, D, D, P, P, _CI]),

@@ -22,6 +22,8 @@ struct Ctx;
   template <typename T>                                                                   \
   int tet_precompute(Ctx *, const sg_mesh *, const void *, double, void *, void *, void *); \
   template <typename T>                                                                   \
+  int blocks(Ctx *, const sg_mesh *, int, const void *, void *);                          \
+  template <typename T>                                                                   \
   int tet_stiffness(Ctx *, const sg_mesh *, int, const void *, const int32_t *,           \
                     const void *, const void *, const void *, const void *, double, double, \
                     void *, void *);                                                      \

@@ -150,21 +150,54 @@ __global__ void __launch_bounds__(128) k_rows(AsmArgs<T> a) {
       const int i = (int)(t - (uint32_t)e * a.card);
       if (Elem::HAS_MAT && gl < Elem::LANES) {
         const int j = gl / BS, l = gl % BS;
-        T out[2][BS];
-        const int nt = Elem::block(a, e, i, j, l, out);
-        if (nt > 0) {
-          const uint32_t col = (uint32_t)a.ep[e * a.card + j];
+        const uint32_t col = (uint32_t)a.ep[e * a.card + j];
+        // An element that lists the same vertex twice sends blocks (i, j)
+        // and (i, j2) to one slot: the lane of the first such j adds them
+        // all, in ascending j (the reference's order), and the others skip.
+        bool first = true, dup = false;
+        constexpr int CARD = Elem::LANES / BS;  // every matrix element uses card * BS lanes
+#pragma unroll
+        for (int j2 = 0; j2 < CARD; ++j2) {
+          const bool same = j2 != j && (uint32_t)a.ep[e * a.card + j2] == col;
+          dup = dup || same;
+          first = first && !(same && j2 < j);
+        }
+        if (!dup) {  // the usual case: one block per slot
+          T out[2][BS];
+          const int nt = Elem::block(a, e, i, j, l, out);
+          if (nt > 0) {
+            uint32_t lo = 0, hi = rlen;
+            while (lo < hi) {
+              uint32_t mid = (lo + hi) >> 1;
+              if (cols[mid] < col) lo = mid + 1; else hi = mid;
+            }
+            T *dst = acc + (size_t)lo * BS * BS + l * BS;
+#pragma unroll
+            for (int q = 0; q < BS; ++q) dst[q] += out[0][q];
+            if (nt > 1) {
+#pragma unroll
+              for (int q = 0; q < BS; ++q) dst[q] += out[1][q];
+            }
+          }
+        } else if (first) {
           uint32_t lo = 0, hi = rlen;
           while (lo < hi) {
             uint32_t mid = (lo + hi) >> 1;
             if (cols[mid] < col) lo = mid + 1; else hi = mid;
           }
           T *dst = acc + (size_t)lo * BS * BS + l * BS;
+          for (int jj = j; jj < CARD; ++jj) {
+            if (jj != j && (uint32_t)a.ep[e * a.card + jj] != col) continue;
+            T out[2][BS];
+            const int nt = Elem::block(a, e, i, jj, l, out);
+            if (nt > 0) {
 #pragma unroll
-          for (int q = 0; q < BS; ++q) dst[q] += out[0][q];
-          if (nt > 1) {
+              for (int q = 0; q < BS; ++q) dst[q] += out[0][q];
+            }
+            if (nt > 1) {
 #pragma unroll
-            for (int q = 0; q < BS; ++q) dst[q] += out[1][q];
+              for (int q = 0; q < BS; ++q) dst[q] += out[1][q];
+            }
           }
         }
       }
@@ -460,6 +493,26 @@ __global__ void k_neo_blocks(AsmArgs<T> a) {
     }
   }
 }
+
+// Generic `map f to E reduce +` with the element function already evaluated
+// by the caller: block (i, j) of element e is eb[((e*CARD + i)*CARD + j)*BS*BS
+// + l*BS + m] (src/lower/lower_maps.cpp:54-128 lowers `A(p(i),p(j)) = blk`
+// to `+=` of blk into the slot of (p(i), p(j)); blocks f does not write are
+// zero).  The row owners add them in element order, as the reference's loop.
+template <typename T, int BS, int CARD> struct BlocksElem {
+  static constexpr bool HAS_MAT = true, HAS_VEC = false;
+  static constexpr int LANES = CARD * BS;
+  __device__ static int block(const AsmArgs<T> &a, int64_t e, int i, int j, int l,
+                              T out[2][BS]) {
+    const T *b = a.eb + (((size_t)e * CARD + i) * CARD + j) * BS * BS + l * BS;
+#pragma unroll
+    for (int q = 0; q < BS; ++q) out[0][q] = b[q];
+    return 1;
+  }
+  __device__ static int vec(const AsmArgs<T> &, int64_t, int, int, T *) { return 0; }
+  __device__ static T fin_block(const AsmArgs<T> &, int32_t, bool, int, int, T acc) { return acc; }
+  __device__ static T fin_vec(const AsmArgs<T> &, int32_t, int, T acc) { return acc; }
+};
 
 // Row owner over element blocks: block (i, j) of tet e from eb, then m*I on
 // the diagonal (the element's second write to K(v(i), v(i))).

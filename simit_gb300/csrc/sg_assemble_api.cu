@@ -73,6 +73,17 @@ int sg_assemble_scalar_springs(sg_ctx *h, const sg_mesh *m, int dt, const void *
   return SG_DISPATCH(exact, dt, scalar_springs, c, m, a, diag, scale, vals);
 }
 
+int sg_assemble_blocks(sg_ctx *h, const sg_mesh *m, int dt, int bs, const void *eb, void *vals,
+                       int exact) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c, "sg_assemble_blocks: null context");
+  SG_TRY(check_mesh(m, true, "sg_assemble_blocks"));
+  SG_REQUIRE(bs >= 1 && bs <= 3 && m->card >= 2 && m->card <= 4,
+             "sg_assemble_blocks: bs %d card %d (bs 1..3, card 2..4)", bs, m->card);
+  SG_REQUIRE(vals && (m->nE == 0 || eb), "sg_assemble_blocks: null array");
+  return SG_DISPATCH(exact, dt, blocks, c, m, bs, eb, vals);
+}
+
 int sg_tet_precompute(sg_ctx *h, const sg_mesh *m, int dt, const void *x, double rho, void *B,
                       void *W, void *mass) {
   Ctx *c = as_ctx(h);

@@ -91,6 +91,22 @@ int tet_precompute(Ctx *c, const sg_mesh *m, const void *x, double rho, void *B,
 }
 
 template <typename T>
+int blocks(Ctx *c, const sg_mesh *m, int bs, const void *eb, void *vals) {
+  AsmArgs<T> a;
+  fill_mesh(a, m);
+  a.eb = (const T *)eb;
+  a.vals = (T *)vals;
+#define SG_BLK(BSV, CV)                                                     \
+  if (bs == BSV && m->card == CV) return launch_rows<BlocksElem<T, BSV, CV>, 16, BSV, T>(c, a);
+  SG_BLK(1, 2) SG_BLK(1, 3) SG_BLK(1, 4)
+  SG_BLK(2, 2) SG_BLK(2, 3) SG_BLK(2, 4)
+  SG_BLK(3, 2) SG_BLK(3, 3) SG_BLK(3, 4)
+#undef SG_BLK
+  return set_error(SG_ERR_UNSUPPORTED, "sg_assemble_blocks: bs %d, card %d (bs 1..3, card 2..4)",
+                   bs, m->card);
+}
+
+template <typename T>
 int tet_stiffness(Ctx *c, const sg_mesh *m, int model, const void *x, const int32_t *cons,
                   const void *B, const void *W, const void *mu, const void *lam, double h,
                   double rho, void *vals, void *eb_scratch) {
@@ -135,6 +151,7 @@ int tet_force(Ctx *c, const sg_mesh *m, int model, const void *x, const void *v,
                        double, const void *, void *, void *);                             \
   template int tet_precompute<T>(Ctx *, const sg_mesh *, const void *, double, void *,    \
                                  void *, void *);                                         \
+  template int blocks<T>(Ctx *, const sg_mesh *, int, const void *, void *);               \
   template int tet_stiffness<T>(Ctx *, const sg_mesh *, int, const void *, const int32_t *, \
                                 const void *, const void *, const void *, const void *,   \
                                 double, double, void *, void *);                          \

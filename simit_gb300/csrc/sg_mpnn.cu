@@ -324,9 +324,21 @@ static int layers(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, con
   k_f2<<<gv, 256, 0, st>>>(ctl, gate, lin, g.n, g.rowptr, g.colidx, g.a, prm, s, g.m1, g.q2,
                            train ? g.g1 : nullptr);
   SG_CHECK_LAUNCH();
+  // one wave of resident CTAs (a partial second wave would run the last
+  // CTAs' tiles at a fraction of the occupancy)
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int a3 = 0, a4 = 0;
+    SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a3, k_f3, TC_WARPS * 32,
+                                                                tc_smem_bytes()));
+    SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a4, k_f4, TC_WARPS * 32,
+                                                                tc_smem_bytes()));
+    per_sm = a3 < a4 ? a3 : a4;
+    if (per_sm < 1) per_sm = 1;
+  }
   const int64_t ntile = ((int64_t)g.n + 15) / 16;
   int gt = (int)((ntile + TC_WARPS - 1) / TC_WARPS);
-  const int cap = c->num_sms * 4;
+  const int cap = c->num_sms * per_sm;
   if (gt > cap) gt = cap;
   k_f3<<<gt, TC_WARPS * 32, tc_smem_bytes(), st>>>(ctl, gate, lin, g.n, g.rowptr, g.colidx, g.a, prm, s,
                                                    g.m1, g.q2, g.m2, g.q3, train ? g.g2 : nullptr);

@@ -6,6 +6,10 @@
 namespace sg {
 namespace mpnn {
 
+// Neighbour gathers run in rounds of GU: each round issues all of its loads
+// before the first accumulation, which keeps the sequential sum order.
+constexpr int GU = 8;
+
 // ---------------------------------------------------------------------------
 // graph data
 // ---------------------------------------------------------------------------
@@ -95,12 +99,23 @@ __global__ void __launch_bounds__(256) k_f2(const SolveCtl *ctl, int gate, int l
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     float mm0 = 0, mm1 = 0, mm2 = 0;
-    for (uint32_t q = rowptr[v]; q < rowptr[v + 1]; ++q) {
-      const float wq = a[q];
-      const uint32_t u = colidx[q];
-      mm0 += wq * s[u * 3];
-      mm1 += wq * s[u * 3 + 1];
-      mm2 += wq * s[u * 3 + 2];
+    const uint32_t qe = rowptr[v + 1];
+    for (uint32_t qb = rowptr[v]; qb < qe; qb += GU) {
+      float wq[GU], g0[GU], g1[GU], g2[GU];  // all gathers of the round in flight
+#pragma unroll
+      for (int k = 0; k < GU; ++k)
+        if (qb + k < qe) {
+          const uint32_t u = colidx[qb + k];
+          wq[k] = a[qb + k];
+          g0[k] = s[u * 3]; g1[k] = s[u * 3 + 1]; g2[k] = s[u * 3 + 2];
+        }
+#pragma unroll
+      for (int k = 0; k < GU; ++k)
+        if (qb + k < qe) {
+          mm0 += wq[k] * g0[k];
+          mm1 += wq[k] * g1[k];
+          mm2 += wq[k] * g2[k];
+        }
     }
     const float s0 = s[v * 3], s1 = s[v * 3 + 1], s2 = s[v * 3 + 2];
     m1[v * 3] = mm0;
@@ -209,13 +224,24 @@ __device__ __forceinline__ void tc_prologue(const TCW &w, TCWarp &tw, int lin, i
     const int64_t v = v0 + vi;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (v < n) {
-      for (uint32_t q = rowptr[v]; q < rowptr[v + 1]; ++q) {
-        const float wq = a[q];
-        const float4 x = *reinterpret_cast<const float4 *>(qsrc + (size_t)colidx[q] * K + half * 4);
-        acc.x += wq * x.x;
-        acc.y += wq * x.y;
-        acc.z += wq * x.z;
-        acc.w += wq * x.w;
+      const uint32_t qe = rowptr[v + 1];
+      for (uint32_t qb = rowptr[v]; qb < qe; qb += GU) {
+        float wq[GU];
+        float4 xg[GU];  // all gathers of the round in flight
+#pragma unroll
+        for (int k = 0; k < GU; ++k)
+          if (qb + k < qe) {
+            wq[k] = a[qb + k];
+            xg[k] = *reinterpret_cast<const float4 *>(qsrc + (size_t)colidx[qb + k] * K + half * 4);
+          }
+#pragma unroll
+        for (int k = 0; k < GU; ++k)
+          if (qb + k < qe) {
+            acc.x += wq[k] * xg[k].x;
+            acc.y += wq[k] * xg[k].y;
+            acc.z += wq[k] * xg[k].z;
+            acc.w += wq[k] * xg[k].w;
+          }
       }
     }
     dst[vi * K + half * 4 + 0] = acc.x;
@@ -524,12 +550,23 @@ __global__ void k_sym_out(const SolveCtl *ctl, int gate, int32_t n,
       w0 = s[v * 3]; w1 = s[v * 3 + 1]; w2 = s[v * 3 + 2];
     } else {
       w0 = wp[v * 3]; w1 = wp[v * 3 + 1]; w2 = wp[v * 3 + 2];
-      for (uint32_t q = rowptr[v]; q < rowptr[v + 1]; ++q) {
-        const float aq = a[q];
-        const uint32_t u = colidx[q];
-        w0 += aq * t[(size_t)u * 3];
-        w1 += aq * t[(size_t)u * 3 + 1];
-        w2 += aq * t[(size_t)u * 3 + 2];
+      const uint32_t qe = rowptr[v + 1];
+      for (uint32_t qb = rowptr[v]; qb < qe; qb += GU) {
+        float aq[GU], g0[GU], g1[GU], g2[GU];
+#pragma unroll
+        for (int k = 0; k < GU; ++k)
+          if (qb + k < qe) {
+            const uint32_t u = colidx[qb + k];
+            aq[k] = a[qb + k];
+            g0[k] = t[(size_t)u * 3]; g1[k] = t[(size_t)u * 3 + 1]; g2[k] = t[(size_t)u * 3 + 2];
+          }
+#pragma unroll
+        for (int k = 0; k < GU; ++k)
+          if (qb + k < qe) {
+            w0 += aq[k] * g0[k];
+            w1 += aq[k] * g1[k];
+            w2 += aq[k] * g2[k];
+          }
       }
     }
     const float *Li = linv + (size_t)v * 9;

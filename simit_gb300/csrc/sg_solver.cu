@@ -152,7 +152,24 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
     switch (S->prec) {
       case PK_NONE: launch_k2_v4<PK_NONE>(S, st, par); break;
       case PK_JACOBI: launch_k2_v4<PK_JACOBI>(S, st, par); break;
-      case PK_BLOCK3: launch_k2_v4<PK_BLOCK3>(S, st, par); break;
+      case PK_BLOCK3: {
+        static bool attr = false;
+        const size_t sm = K2W_WARPS * sizeof(K2WarpSmem);
+        if (!attr) {
+          SG_CHECK_CUDA(cudaFuncSetAttribute(k_cg_update_w<true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+          attr = true;
+        }
+        const int64_t nchunks = (S->len / 12 + 31) / 32;
+        int64_t grid = (nchunks + K2W_WARPS - 1) / K2W_WARPS;
+        if (grid > 2 * (int64_t)S->c->num_sms) grid = 2 * (int64_t)S->c->num_sms;
+        if (grid < 1) grid = 1;
+        k_cg_update_w<true><<<(int)grid, K2W_WARPS * 32, sm, st>>>(
+            S->ctl, par, S->len, S->part1, S->P1, S->tma, (const float *)S->p,
+            (const float *)S->q, (float *)S->r, (float *)S->xupd, (float *)S->z,
+            (const float *)S->dinv, S->part2);
+        break;
+      }
       default: launch_k2_v4<PK_EXTERNAL>(S, st, par); break;
     }
     SG_CHECK_LAUNCH();

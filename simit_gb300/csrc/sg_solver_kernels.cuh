@@ -474,6 +474,159 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
   }
 }
 
+// K2 for FP32 vectors and 3x3 block Jacobi with warp-staged, fully coalesced
+// accesses.  A warp takes 128 vertices at a time: it loads the chunk of
+// p, q, r, x (96 float4 each) and of D^-1 (288 float4) with lane-consecutive
+// 16-byte loads into its shared-memory slice, each lane then reads its four
+// vertices (3 and 9 consecutive float4, conflict-free), and the results go
+// back through shared memory to lane-consecutive stores.  Same arithmetic,
+// partial sums and finalisation as k_cg_update_v4<PK_BLOCK3>.  The last
+// len % 12 entries are done by the scalar tail of thread 0 of the last CTA.
+constexpr int K2W_WARPS = 8;
+struct K2WarpSmem {
+  float4 p[96], q[96], r[96], x[96], d[288];
+};
+
+template <bool FIN>
+__global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
+    SolveCtl *ctl, int par, int64_t len, const double *__restrict__ part_in, int np1,
+    int pq_fin, const float *__restrict__ p, const float *__restrict__ q, float *__restrict__ r,
+    float *__restrict__ x, float *__restrict__ z, const float *__restrict__ dinv,
+    double *__restrict__ part_out) {
+  extern __shared__ __align__(16) unsigned char k2w_raw[];
+  __shared__ double sh[33];
+  if (ctl->status != ST_RUNNING) return;
+  const double pq = pq_fin ? ctl->pq_tot : sum_parts(part_in, np1, sh);
+  const double rz = ctl->rz[par];
+  if (!(pq > 0.0) || !isfinite(pq)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->status = isfinite(pq) ? ST_BREAKDOWN : ST_NAN;
+    return;
+  }
+  const double alpha = rz / pq;
+  const float a = (float)alpha;
+  const int lane = threadIdx.x & 31;
+  K2WarpSmem &w = reinterpret_cast<K2WarpSmem *>(k2w_raw)[threadIdx.x >> 5];
+  const float4 *p4 = reinterpret_cast<const float4 *>(p);
+  const float4 *q4 = reinterpret_cast<const float4 *>(q);
+  float4 *r4 = reinterpret_cast<float4 *>(r);
+  float4 *x4 = reinterpret_cast<float4 *>(x);
+  float4 *z4 = reinterpret_cast<float4 *>(z);
+  const float4 *d4 = reinterpret_cast<const float4 *>(dinv);
+  const int64_t nu = len / 12;          // complete 4-vertex units
+  const int64_t nf = nu * 3;            // their float4 of each vector
+  const int64_t nchunks = (nu + 31) / 32;
+  DotAcc<float> rr, rzs, zq;
+  for (int64_t c = (int64_t)blockIdx.x * K2W_WARPS + (threadIdx.x >> 5); c < nchunks;
+       c += (int64_t)gridDim.x * K2W_WARPS) {
+    const int64_t f0 = c * 96, d0 = c * 288;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int64_t f = f0 + lane + 32 * j;
+      if (f < nf) {
+        w.p[lane + 32 * j] = p4[f];
+        w.q[lane + 32 * j] = q4[f];
+        w.r[lane + 32 * j] = r4[f];
+        w.x[lane + 32 * j] = x4[f];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+      const int64_t f = d0 + lane + 32 * j;
+      if (f < nf * 3) w.d[lane + 32 * j] = d4[f];
+    }
+    __syncwarp();
+    const bool mine = c * 32 + lane < nu;
+    float pv[12], qv[12], rv[12], xv[12], zv[12], dv[36];
+    if (mine) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float4 a4 = w.p[3 * lane + j], b4 = w.q[3 * lane + j], c4 = w.r[3 * lane + j],
+                     e4 = w.x[3 * lane + j];
+        pv[4 * j] = a4.x; pv[4 * j + 1] = a4.y; pv[4 * j + 2] = a4.z; pv[4 * j + 3] = a4.w;
+        qv[4 * j] = b4.x; qv[4 * j + 1] = b4.y; qv[4 * j + 2] = b4.z; qv[4 * j + 3] = b4.w;
+        rv[4 * j] = c4.x; rv[4 * j + 1] = c4.y; rv[4 * j + 2] = c4.z; rv[4 * j + 3] = c4.w;
+        xv[4 * j] = e4.x; xv[4 * j + 1] = e4.y; xv[4 * j + 2] = e4.z; xv[4 * j + 3] = e4.w;
+      }
+#pragma unroll
+      for (int j = 0; j < 9; ++j) {
+        const float4 g4 = w.d[9 * lane + j];
+        dv[4 * j] = g4.x; dv[4 * j + 1] = g4.y; dv[4 * j + 2] = g4.z; dv[4 * j + 3] = g4.w;
+      }
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        xv[k] = xv[k] + a * pv[k];
+        rv[k] = rv[k] - a * qv[k];
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          zv[v * 3 + k] = dv[v * 9 + k * 3] * rv[v * 3] + dv[v * 9 + k * 3 + 1] * rv[v * 3 + 1] +
+                          dv[v * 9 + k * 3 + 2] * rv[v * 3 + 2];
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        rr.add(rv[k], rv[k]);
+        rzs.add(rv[k], zv[k]);
+        zq.add(zv[k], qv[k]);
+      }
+    }
+    __syncwarp();  // every lane has read its inputs
+    if (mine) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        w.x[3 * lane + j] = make_float4(xv[4 * j], xv[4 * j + 1], xv[4 * j + 2], xv[4 * j + 3]);
+        w.r[3 * lane + j] = make_float4(rv[4 * j], rv[4 * j + 1], rv[4 * j + 2], rv[4 * j + 3]);
+        w.p[3 * lane + j] = make_float4(zv[4 * j], zv[4 * j + 1], zv[4 * j + 2], zv[4 * j + 3]);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int64_t f = f0 + lane + 32 * j;
+      if (f < nf) {
+        x4[f] = w.x[lane + 32 * j];
+        r4[f] = w.r[lane + 32 * j];
+        z4[f] = w.p[lane + 32 * j];
+      }
+    }
+    __syncwarp();  // the slice is refilled by the next chunk
+  }
+  // tail: the last len % 12 entries, scalar, by one thread
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    for (int64_t i0 = nu * 12; i0 < len; i0 += 3) {
+      float rv[3];
+      for (int k = 0; k < 3; ++k) {
+        const int64_t i = i0 + k;
+        x[i] = x[i] + a * p[i];
+        rv[k] = r[i] - a * q[i];
+        r[i] = rv[k];
+      }
+      const float *D = dinv + (i0 / 3) * 9;
+      for (int k = 0; k < 3; ++k) {
+        const float zk = D[k * 3] * rv[0] + D[k * 3 + 1] * rv[1] + D[k * 3 + 2] * rv[2];
+        z[i0 + k] = zk;
+        rr.add(rv[k], rv[k]);
+        rzs.add(rv[k], zk);
+        zq.add(zk, q[i0 + k]);
+      }
+    }
+  }
+  const double t[3] = {block_sum(rr.value(), sh), block_sum(rzs.value(), sh),
+                       block_sum(zq.value(), sh)};
+  if (FIN) {
+    double tot[3];
+    if (finalize_partials(t, 3, part_out, &ctl->tick2, tot, sh) && threadIdx.x == 0) {
+      ctl->last_alpha = alpha;
+      cg_decide(ctl, par, tot[0], tot[1], tot[2], alpha);
+    }
+  } else if (threadIdx.x == 0) {
+    part_out[blockIdx.x] = t[0];
+    part_out[gridDim.x + blockIdx.x] = t[1];
+    part_out[2 * gridDim.x + blockIdx.x] = t[2];
+    if (blockIdx.x == 0) ctl->last_alpha = alpha;
+  }
+}
+
 // K3 for FP32 vectors: the control decisions of k_cg_direction, then
 // p = z + beta p with float4 accesses.
 // fin: K2 already took the decision and left beta in ctl->beta.

@@ -175,6 +175,17 @@ def assemble_scalar_springs(mesh, a, diag, scale, dtype=torch.float64, exact=Tru
         return vals
 
 
+def assemble_blocks(mesh, eb, bs, dtype=torch.float64, exact=True):
+    """`map f to E reduce +` of caller-evaluated element blocks eb
+    [nE, card, card, bs, bs] into the mesh's pattern (values [nnzb*bs*bs])."""
+    with mesh.ctx.stream():
+        eb = _d(eb, dtype, mesh.ctx.device).contiguous()
+        vals = mesh.empty(mesh.nnzb * bs * bs, dtype)
+        call("sg_assemble_blocks", mesh.ctx.h, mesh.ref(), dtype_code(vals), int(bs), ptr(eb),
+             ptr(vals), int(exact))
+        return vals
+
+
 def tet_precompute(mesh, x, rho, dtype=torch.float64):
     with mesh.ctx.stream():
         x = _d(x, dtype, mesh.ctx.device)

@@ -40,6 +40,23 @@ def extract_asserts(path, test_name):
     return out
 
 
+def extract_assert_eq(path, test_name):
+    """ASSERT_EQ(expected, expr) lines inside TEST(..., test_name)."""
+    lines = open(path).read().split("\n")
+    out, inside = [], False
+    for i, ln in enumerate(lines, 1):
+        m = re.match(r"TEST\((\w+),\s*(\w+)\)", ln)
+        if m:
+            inside = m.group(2) == test_name
+            continue
+        if inside:
+            a = re.search(r"ASSERT_EQ\(\s*([-0-9.eE+]+)\s*,\s*(.*)\);", ln)
+            if a:
+                out.append({"expected": float(a.group(1)), "expr": a.group(2).strip(),
+                            "source": "%s:%d" % (os.path.relpath(path, REF), i)})
+    return out
+
+
 def main():
     test = os.path.join(REF, "test")
     if not os.path.isdir(test):
@@ -48,6 +65,15 @@ def main():
         "isprings": extract_asserts(os.path.join(test, "program-isprings.cpp"), "isprings"),
         "cg": extract_asserts(os.path.join(test, "program-cg-test.cpp"), "cg"),
         "femTet": extract_asserts(os.path.join(test, "program-fem-test.cpp"), "femTet"),
+        # assembly + SpMV of small element functions (test/input/system/*.sim,
+        # test/input/assembly/matrix_vv.sim)
+        "gemv_blocked": extract_assert_eq(os.path.join(test, "system-gemv-tests.cpp"),
+                                          "gemv_blocked"),
+        "gemv_blocked_nw": extract_assert_eq(os.path.join(test, "system-gemv-tests.cpp"),
+                                             "gemv_blocked_nw"),
+        "gemv_blocked_computed": extract_assert_eq(os.path.join(test, "system-gemv-tests.cpp"),
+                                                   "gemv_blocked_computed"),
+        "matrix_vv": extract_assert_eq(os.path.join(test, "assembly-tests.cpp"), "matrix_vv"),
     }
     with open(os.path.join(HERE, "reference_golden.json"), "w") as f:
         json.dump(golden, f, indent=1)

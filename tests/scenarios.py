@@ -82,3 +82,34 @@ def femtet_bar2k():
     return {"n": n, "x": x, "v": v, "c": c, "tets": tets, "u": np.full(nT, uval),
             "l": np.full(nT, lval), "h": 0.01, "rho": 1000.0,
             "grav": np.array([0.0, -10.0, 0.0]), "tol2": 1e-6, "maxiters": 100, "steps": 10}
+
+
+def element_block_scenarios():
+    """The small `map f to E reduce +` programs of the reference's gemv and
+    assembly tests, with f evaluated here: (name, n, endpoints, bs, element
+    blocks [nE, 2, 2, bs, bs], vector x, expected-order labels).  The
+    product A x is compared with the golden values in test order
+    (c(p0)(0), c(p0)(1), c(p1)(0), ...)."""
+    out = []
+    b = np.array([[1.0, 2.0], [3.0, 4.0], [5.0, 6.0]])
+    ep = np.array([0, 1, 1, 2], np.int32)
+    a = np.array([[[1.0, 2.0], [3.0, 4.0]], [[5.0, 6.0], [7.0, 8.0]]])
+    # test/input/system/gemv_blocked.sim: all four blocks are s.a
+    eb = np.zeros((2, 2, 2, 2, 2))
+    for s in range(2):
+        eb[s, :, :] = a[s]
+    out.append(("gemv_blocked", 3, ep, 2, eb, b.reshape(-1)))
+    # gemv_blocked_nw.sim: only M(p(0), p(0)) = s.a
+    eb = np.zeros((2, 2, 2, 2, 2))
+    for s in range(2):
+        eb[s, 0, 0] = a[s]
+    out.append(("gemv_blocked_nw", 3, ep, 2, eb, b.reshape(-1)))
+    # gemv_blocked_computed.sim: all four blocks are p(0).x * p(1).x' (x = b)
+    eb = np.zeros((2, 2, 2, 2, 2))
+    for s in range(2):
+        eb[s, :, :] = np.outer(b[ep[2 * s]], b[ep[2 * s + 1]])
+    out.append(("gemv_blocked_computed", 3, ep, 2, eb, b.reshape(-1)))
+    # test/input/assembly/matrix_vv.sim: all four (scalar) blocks are 1, a = 1
+    eb = np.ones((2, 2, 2, 1, 1))
+    out.append(("matrix_vv", 3, ep, 1, eb, np.ones(3)))
+    return out

@@ -100,3 +100,16 @@ def test_tet_grid_counts(oracle):
     assert len(ci) == 58769
     B, W, _ = oracle.tet_precompute(m["x"], m["tets"], 1e3)
     assert W.min() > 0 and abs(W.sum() - 1.0) < 1e-12
+
+
+def test_element_block_assembly_golden(oracle):
+    """Oracle `map ... reduce +` of caller-evaluated element blocks, then the
+    blocked SpMV, against the golden values of the reference's gemv_blocked*
+    (test/system-gemv-tests.cpp) and matrix_vv (test/assembly-tests.cpp)."""
+    from tests import scenarios
+    for name, n, ep, bs, eb, x in scenarios.element_block_scenarios():
+        rp, ci = oracle.pattern(n, ep, 2)
+        vals = oracle.assemble_blocks(ep, 2, bs, eb, rp, ci)
+        y = oracle.spmv(n, bs, rp, ci, vals, x)
+        want = [g["expected"] for g in scenarios.golden(name)]
+        assert list(y) == want, (name, list(y), want)
