@@ -174,21 +174,26 @@ def run_heat(args):
     print(json.dumps(out), flush=True)
 
 
-def run_cloth(args):
+def run_cloth(args, rank=0, world=1, local=0):
     """256 triangulated sheets (sides U{32..256}), implicit springs, PCG to
     1e-6: one CUDA-graph replay (assembly of all sheets + the persistent
     batched PCG) against the same sheets assembled and solved one at a time
     by the general solver (meshes and solvers built outside the timed
-    region)."""
+    region).  Under torchrun the sheets are sharded across ranks by
+    vertex count (size-balanced, no exchange); times are maxima over ranks."""
     import numpy as np
     import torch
     from simit_gb300 import _lib, problems
+    from simit_gb300 import dist as sgd
     from simit_gb300.runtime import (Context, Mesh, Solver, assemble_springs, call, dtype_code,
                                      ptr, solve_opts)
-    ctx = Context(0)
+    ctx = Context(local)
+    torch.cuda.set_device(local)
     torch.cuda.set_stream(ctx.torch_stream)
     st = ctx.torch_stream
-    h = problems.cloth_batch(nsheets=args.sheets)
+    sides = problems.cloth_sides(args.sheets)
+    shard = sgd.shard_by_cost(sides.astype(np.float64) ** 2, world)[rank]
+    h = problems.cloth_batch(nsheets=args.sheets, select=shard)
     cb = problems.ClothBatch(ctx, h)
     cb.capture()
     for _ in range(2):
@@ -201,8 +206,8 @@ def run_cloth(args):
         cb.replay()
     e1.record(st)
     e1.synchronize()
-    batched_ms = e0.elapsed_time(e1) / args.steps
-    ok = bool((cb.status == 1).all().item())
+    batched_ms = sgd.max_over_ranks(e0.elapsed_time(e1) / args.steps, "cuda")
+    ok = sgd.sum_over_ranks(float(not bool((cb.status == 1).all().item())), "cuda") == 0
     iters = cb.iters.cpu().numpy()
     # one at a time
     c = problems.CLOTH
@@ -241,17 +246,21 @@ def run_cloth(args):
     t0 = time.perf_counter()
     one_at_a_time()
     torch.cuda.synchronize()
-    seq_ms = (time.perf_counter() - t0) * 1e3
+    seq_ms = sgd.max_over_ranks((time.perf_counter() - t0) * 1e3, "cuda")
     for item in seq:
         item[-1].close()
+    n_all = sgd.sum_over_ranks(h["n"], "cuda")
+    if rank != 0:
+        return
     print(json.dumps({"workload": "batched cloth: %d sheets, sides U{32..256}, %d vertices, "
                                   "implicit springs (stretch 5e3, bend 50), PCG to 1e-6"
-                                  % (cb.nsys, h["n"]),
+                                  % (args.sheets, n_all), "n_gpus": world,
+                      "scaling": "strong" if world > 1 else None,
                       "batched_graph_ms": batched_ms, "one_at_a_time_ms": seq_ms,
                       "speedup": seq_ms / batched_ms, "all_converged": ok,
                       "iters_max": int(iters.max()), "iters_mean": float(iters.mean()),
-                      "autotuned_config": cb.config, "dofs": h["n"] * 3,
-                      "DOF_per_s_batched": h["n"] * 3 / (batched_ms / 1e3)}), flush=True)
+                      "autotuned_config": cb.config, "dofs": int(n_all) * 3,
+                      "DOF_per_s_batched": n_all * 3 / (batched_ms / 1e3)}), flush=True)
 
 
 def run_solve_only(args):
@@ -338,9 +347,8 @@ def workload_name(size):
 
 
 def dist_setup(args):
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from simit_gb300 import dist as sgd
+    rank, world, local = sgd.env()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
@@ -511,12 +519,8 @@ def run_ours(args, rank, world, local):
     e1.record(st)
     barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from simit_gb300 import dist as sgd
+    ms = sgd.max_over_ranks(e0.elapsed_time(e1) / args.steps, "cuda")
     dofs = prob.dofs
     value = dofs * world / (ms / 1e3)
     relres = max((r.true_normr2 / r.bnorm2) ** 0.5 for r in results)
@@ -537,7 +541,7 @@ def run_ours(args, rank, world, local):
     for _ in range(args.steps):
         prob.step_host(x_h, mu_h, lam_h, u_h)
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = sgd.max_over_ranks((time.perf_counter() - t0) / args.steps, "cuda")
     h2d = (x_h.numel() + mu_h.numel() + lam_h.numel()) * 4
     d2h = u_h.numel() * 8
 
@@ -663,7 +667,11 @@ def main():
         run_spmv_only(args)
         return
     if args.cloth:
-        run_cloth(args)
+        rank, world, local = dist_setup(args)
+        run_cloth(args, rank, world, local)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
         return
     if args.neo:
         run_neo(args)

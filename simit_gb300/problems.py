@@ -123,16 +123,24 @@ CLOTH = {"k_stretch": 5e3, "k_bend": 50.0, "mass": 1e-3, "dt": 1.0 / 240.0, "vis
          "grav": (0.0, 0.0, -9.81), "tol": 1e-6}
 
 
-def cloth_batch(nsheets=256, lo=32, hi=256, seed=5, jitter=0.2):
+def cloth_sides(nsheets=256, lo=32, hi=256, seed=5):
+    """Side lengths (vertices per side) of the seeded sheet batch."""
+    return meshgen.rng(seed).integers(lo, hi + 1, size=nsheets)
+
+
+def cloth_batch(nsheets=256, lo=32, hi=256, seed=5, jitter=0.2, select=None):
     """nsheets triangulated square sheets with side lengths uniform in
     [lo, hi] vertices, concatenated (vertex and spring offsets) into one
     edge set.  Positions: unit sheet, z jittered by +/- jitter * spacing
-    (seeded), rest lengths of the flat sheet, v = 0, two corners pinned."""
-    g = meshgen.rng(seed)
-    sides = g.integers(lo, hi + 1, size=nsheets)
+    (seeded), rest lengths of the flat sheet, v = 0, two corners pinned.
+    select: the indices of the sheets to build (a shard); each sheet is the
+    same whichever shard holds it."""
+    sides = cloth_sides(nsheets, lo, hi, seed)
+    idx = range(nsheets) if select is None else [int(i) for i in select]
     xs, eps, ks, l0s, fixed, sys_ptr = [], [], [], [], [], [0]
     off = 0
-    for i, s in enumerate(sides):
+    for i in idx:
+        s = sides[i]
         sh = meshgen.cloth_sheet(int(s))
         x = sh["x"].reshape(-1, 3).copy()
         spacing = 1.0 / (s - 1)
@@ -146,7 +154,7 @@ def cloth_batch(nsheets=256, lo=32, hi=256, seed=5, jitter=0.2):
         sys_ptr.append(off)
     return {"n": off, "x": np.concatenate(xs), "ep": np.concatenate(eps).astype(np.int32),
             "k": np.concatenate(ks), "l0": np.concatenate(l0s), "fixed": np.concatenate(fixed),
-            "sys_ptr": np.array(sys_ptr, np.int32), "sides": sides}
+            "sys_ptr": np.array(sys_ptr, np.int32), "sides": np.asarray(sides)[list(idx)]}
 
 
 class ClothBatch:
