@@ -34,6 +34,8 @@ def parse():
     ap.add_argument("--size", type=int, default=128, help="cells per cube edge")
     ap.add_argument("--cpu-sample", type=int, default=32, help="cells per edge of the CPU sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
+    ap.add_argument("--no-reorder", action="store_true",
+                    help="keep the lattice vertex order (no Hilbert reordering)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner comparison")
     ap.add_argument("--spmv-only", action="store_true",
@@ -53,6 +55,8 @@ def parse():
     ap.add_argument("--learned-solve", action="store_true",
                     help="profiling driver: the --size system with the learned preconditioner, "
                          "capped at --iters iterations")
+    ap.add_argument("--springs", action="store_true",
+                    help="createBox springs 10^3: 10 implicit FP64 steps, parity vs the oracle")
     ap.add_argument("--heat", action="store_true",
                     help="P1 heat (128^3): 1000 SpMVs FP32 vs FP64, CG FP64 vs mixed")
     return ap.parse_args()
@@ -123,6 +127,86 @@ def run_neo(args):
                                                np.linalg.norm(sols["fp64"]))
     out["speedup_solve"] = out["fp64"]["solve_ms"] / out["fp32_bulk"]["solve_ms"]
     print(json.dumps(out), flush=True)
+
+
+def run_springs(args):
+    """createBox springs 10x10x10 (spacing 0.1, jitter 0.01, k = 1e4, m = 1,
+    dt = 1e-3, gravity, bottom layer pinned), 10 implicit steps in FP64
+    (apps/springs/isprings.sim form): pattern build, exact-mode assembly and
+    CG to a 1e-8 relative residual per step, against the oracle (the
+    reference's pattern builder and `loc`; its loops restated) on one core."""
+    import numpy as np
+    import torch
+    from oracle import oracle
+    from simit_gb300 import _lib, meshgen
+    from simit_gb300.runtime import Context, Mesh, Solver, assemble_springs, solve_opts
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    L = meshgen.springs_lattice(10, 10, 10, 0.1, 0.01, seed=1)
+    n, ep = L["n"], L["ep"]
+    k = np.full(len(L["l0"]), 1e4)
+    m = np.ones(n)
+    h, grav, steps = 1e-3, np.array([0.0, 0.0, -9.81]), 10
+    Mesh(ctx, n, ep, 2)  # warm (module load, scratch)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mesh = Mesh(ctx, n, ep, 2, with_slots=True)
+    torch.cuda.synchronize()
+    pattern_ms = (time.perf_counter() - t0) * 1e3
+    rp, ci = mesh.pattern.host()
+    # the oracle's pattern and slots (pinned bit-exact to the reference's
+    # PathIndexBuilder and loc by the CPU tests)
+    orp, oci = oracle.pattern(n, ep, 2)
+    pattern_exact = bool(np.array_equal(rp, orp) and np.array_equal(ci, oci))
+    slots_exact = bool(np.array_equal(mesh.pattern.slots.cpu().numpy().view(np.uint32),
+                                      oracle.slots(ep, 2, orp, oci)))
+    d = ctx.device
+    x = torch.tensor(L["x"], device=d)
+    v = torch.zeros(n * 3, dtype=torch.float64, device=d)
+    xo, vo = L["x"].copy(), np.zeros(n * 3)
+    asm_ms, cg_ms, iters, vals_err = [], [], [], 0.0
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        ms, (vals, f) = _ev_ms(ctx.torch_stream, lambda: assemble_springs(
+            mesh, x, v, m, L["fixed"], k, L["l0"], h, 0.0, grav, form=0))
+        asm_ms.append(ms)
+        oA, of = oracle.springs_assemble(0, xo, vo, m, L["fixed"], ep, k, L["l0"], h, 0.0, grav,
+                                         orp, oci)
+        vals_err = max(vals_err, float(np.abs(vals.cpu().numpy() - oA).max() /
+                                       np.abs(oA).max()))
+        S = Solver(ctx, n, 3, mesh.pattern.rowptr, mesh.pattern.colidx, vals, mesh.nnzb,
+                   solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, tol=1e-8,
+                              maxiters=10000))
+        ms, r = _ev_ms(ctx.torch_stream, lambda: S.solve(f, v))
+        S.close()
+        cg_ms.append(ms)
+        iters.append(r.iters)
+        with ctx.stream():
+            x.add_(h * v)
+        t0 = time.perf_counter()
+        bb = float(of @ of)
+        it = oracle.cg_normr2(n, 3, orp, oci, oA, of, vo, 1e-16 * bb, 10000)
+        vo = it[0] if isinstance(it, tuple) else vo
+        xo = xo + h * vo
+    xg = x.cpu().numpy()
+    # the CPU oracle step (1 core), assembly + CG, for the baseline column
+    t0 = time.perf_counter()
+    xc, vc = L["x"].copy(), np.zeros(n * 3)
+    for _ in range(steps):
+        oracle.springs_step(0, xc, vc, m, L["fixed"], ep, k, L["l0"], h, 0.0, grav, orp, oci,
+                            1e-16, 10000)  # r.r <= 1e-16
+    cpu_step_ms = (time.perf_counter() - t0) * 1e3 / steps
+    print(json.dumps({
+        "workload": "springs createBox 10^3 (1000 vertices, 2700 springs, nnzb %d), 10 implicit "
+                    "steps, FP64, CG to 1e-8" % mesh.nnzb,
+        "pattern_ms": pattern_ms, "assembly_ms_median": float(np.median(asm_ms)),
+        "cg_ms_median": float(np.median(cg_ms)), "cg_iters": iters,
+        "parity": {"pattern_bit_exact_vs_oracle": pattern_exact,
+                   "slots_bit_exact_vs_oracle": slots_exact,
+                   "assembled_values_max_rel_diff": vals_err,
+                   "positions_rel_diff_after_10_steps":
+                       float(np.linalg.norm(xg - xo) / np.linalg.norm(xo))},
+        "cpu_oracle_step_ms": cpu_step_ms, "cpu_cores": 1}), flush=True)
 
 
 def run_heat(args):
@@ -272,7 +356,10 @@ def run_solve_only(args):
     from simit_gb300.runtime import Context
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
-    p = problems.HeteroElasticity(ctx, problems.hetero_mesh(args.size), dtype=torch.float32,
+    h = problems.hetero_mesh(args.size)
+    if not args.no_reorder:
+        h = problems.reorder_hetero(h)
+    p = problems.HeteroElasticity(ctx, h, dtype=torch.float32,
                                   precond=_lib.PRECOND_BLOCK_JACOBI, maxiters=args.iters)
     p.step()
     ms, r = _ev_ms(ctx.torch_stream, p.step)
@@ -290,7 +377,10 @@ def run_learned_solve(args):
     from simit_gb300.runtime import Context, Solver, solve_opts
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
-    p = problems.HeteroElasticity(ctx, problems.hetero_mesh(args.size), dtype=torch.float32,
+    h = problems.hetero_mesh(args.size)
+    if not args.no_reorder:
+        h = problems.reorder_hetero(h)
+    p = problems.HeteroElasticity(ctx, h, dtype=torch.float32,
                                   precond=_lib.PRECOND_BLOCK_JACOBI)
     m = p.mesh
     with ctx.stream():
@@ -321,8 +411,10 @@ def run_spmv_only(args):
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
     dt = torch.float64 if args.f64 else torch.float32
-    p = problems.HeteroElasticity(ctx, problems.hetero_mesh(args.size), dtype=dt,
-                                  precond=_lib.PRECOND_JACOBI)
+    h = problems.hetero_mesh(args.size)
+    if not args.no_reorder:
+        h = problems.reorder_hetero(h)
+    p = problems.HeteroElasticity(ctx, h, dtype=dt, precond=_lib.PRECOND_JACOBI)
     m = p.mesh
     x = torch.rand(m.n * 3, dtype=dt, device=ctx.device)
     y = torch.empty_like(x)
@@ -340,10 +432,10 @@ def run_spmv_only(args):
                       "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes}), flush=True)
 
 
-def workload_name(size):
+def workload_name(size, reorder=True):
     return ("heterogeneous linear elasticity %d^3 five-tet lattice (fem_linear form, E log-uniform "
-            "[1e3,1e6], nu U[0.35,0.45], bottom face fixed), solve to 1e-8 FP64 relative residual"
-            % size)
+            "[1e3,1e6], nu U[0.35,0.45], bottom face fixed)%s, solve to 1e-8 FP64 relative "
+            "residual" % (size, ", vertices in Hilbert order (simit::reorder)" if reorder else ""))
 
 
 def dist_setup(args):
@@ -401,7 +493,8 @@ def run_reference(args, rank, world):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded Philox)",
-           "config": {"workload": workload_name(args.size), "sample_cells": args.cpu_sample},
+           "config": {"workload": workload_name(args.size, not args.no_reorder),
+                      "sample_cells": args.cpu_sample},
            "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": 1, "kind": "port",
                             "sample": sample},
            "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -494,6 +587,8 @@ def run_ours(args, rank, world, local):
     torch.cuda.set_device(local)
     torch.cuda.set_stream(ctx.torch_stream)
     host = problems.hetero_mesh(args.size)
+    if not args.no_reorder:
+        host = problems.reorder_hetero(host)
     prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
                                      precond=_lib.PRECOND_BLOCK_JACOBI)
     st = ctx.torch_stream
@@ -628,7 +723,8 @@ def run_ours(args, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 matrix+SpMV, f64 dots/residual",
         "data": "synthetic (seeded Philox mesh, parameters and displacements)",
-        "config": {"workload": workload_name(args.size), "dofs": dofs, "nnzb": m.nnzb,
+        "config": {"workload": workload_name(args.size, not args.no_reorder), "dofs": dofs,
+                   "nnzb": m.nnzb,
                    "method": "FP32 assembly + mixed-precision block-Jacobi PCG (FP32 matrix/"
                              "vectors, FP64 dots, FP64 reliable updates), verified FP64 residual",
                    "parallelism": "replicas" if world > 1 else "single GPU",
@@ -678,6 +774,9 @@ def main():
         return
     if args.heat:
         run_heat(args)
+        return
+    if args.springs:
+        run_springs(args)
         return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":

@@ -323,6 +323,18 @@ int sg_batched_pcg(sg_ctx *ctx, int32_t nsys, const int32_t *sys_ptr, const int3
 int sg_batched_configs(void);
 
 /* ---------------------------------------------------------------------
+ * Locality reordering (host; simit::reorder, src/reorder.cpp:252-273).
+ * sg_hilbert_order: vertex_ordering[old] = new index of each vertex, by the
+ * Hilbert index of its position on a 2^bits lattice spanning the bounding
+ * box (ties by old index).  sg_element_order: element_order[new] = old index,
+ * elements sorted by their sorted endpoint tuples (apply after relabelling
+ * the endpoints).  sg_hilbert_index exposes the curve for tests.
+ * ------------------------------------------------------------------- */
+int sg_hilbert_order(int32_t n, const double *coords, int32_t bits, int32_t *vertex_ordering);
+int sg_element_order(int32_t nE, int32_t card, const int32_t *endpoints, int32_t *element_order);
+int sg_hilbert_index(uint32_t x, uint32_t y, uint32_t z, int32_t bits, uint64_t *out);
+
+/* ---------------------------------------------------------------------
  * Learned preconditioner: a 3-layer message-passing network (hidden 64,
  * messages of 8, no biases) over the matrix graph, z = D^-1 r + Wout h3,
  * where D is the 3x3 block diagonal; the 64x64 layers run on the tensor

@@ -1,0 +1,113 @@
+// Locality reordering of a mesh (host code): vertices along a Hilbert curve
+// over their positions, elements by their sorted endpoint tuples.  This is
+// what simit::reorder does (src/reorder.cpp:252-273: the vertex Hilbert
+// order of hilbertReorder :25-112, the element order of
+// edgeVertexSortReordering :145-170) before a mesh is bound; here it serves
+// the SpMV's x gathers (neighbouring rows touch nearby columns) and the row
+// owners' vertex gathers.  The Hilbert index is Skilling's transform
+// ("Programming the Hilbert curve", AIP Conf. Proc. 707, 2004): the lattice
+// coordinates are transposed to the curve's Gray-coded form and their bits
+// interleaved.  Any Hilbert curve serves locality equally; this one need not
+// have the orientation of the reference's hilbert_c2i.
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "sg_internal.cuh"
+
+namespace sg {
+
+// Hilbert index of a point of a 2^bits lattice in 3-D (Skilling 2004).
+static uint64_t hilbert3(uint32_t x0, uint32_t x1, uint32_t x2, int bits) {
+  uint32_t X[3] = {x0, x1, x2};
+  const uint32_t M = 1u << (bits - 1);
+  for (uint32_t Q = M; Q > 1; Q >>= 1) {  // inverse undo
+    const uint32_t P = Q - 1;
+    for (int i = 0; i < 3; ++i) {
+      if (X[i] & Q) {
+        X[0] ^= P;
+      } else {
+        const uint32_t t = (X[0] ^ X[i]) & P;
+        X[0] ^= t;
+        X[i] ^= t;
+      }
+    }
+  }
+  for (int i = 1; i < 3; ++i) X[i] ^= X[i - 1];  // Gray encode
+  uint32_t t = 0;
+  for (uint32_t Q = M; Q > 1; Q >>= 1)
+    if (X[2] & Q) t ^= Q - 1;
+  for (int i = 0; i < 3; ++i) X[i] ^= t;
+  uint64_t h = 0;
+  for (int j = bits - 1; j >= 0; --j)
+    for (int i = 0; i < 3; ++i) h = (h << 1) | ((X[i] >> j) & 1u);
+  return h;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+extern "C" {
+
+int sg_hilbert_index(uint32_t x, uint32_t y, uint32_t z, int32_t bits, uint64_t *out) {
+  SG_REQUIRE(out && bits >= 1 && bits <= 21, "sg_hilbert_index: bits %d (1..21)", bits);
+  *out = hilbert3(x, y, z, bits);
+  return SG_OK;
+}
+
+int sg_hilbert_order(int32_t n, const double *coords, int32_t bits, int32_t *vertex_ordering) {
+  SG_REQUIRE(n >= 0 && (n == 0 || (coords && vertex_ordering)), "sg_hilbert_order: null array");
+  SG_REQUIRE(bits >= 1 && bits <= 21, "sg_hilbert_order: bits %d (1..21)", bits);
+  if (n == 0) return SG_OK;
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) lo[d] = hi[d] = coords[d];
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const double v = coords[i * 3 + d];
+      SG_REQUIRE(std::isfinite(v), "sg_hilbert_order: coordinate %lld is not finite",
+                 (long long)i);
+      lo[d] = std::min(lo[d], v);
+      hi[d] = std::max(hi[d], v);
+    }
+  const double cells = (double)((1u << bits) - 1);
+  std::vector<uint64_t> key(n);
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t c[3];
+    for (int d = 0; d < 3; ++d) {
+      const double ext = hi[d] - lo[d];
+      c[d] = ext > 0 ? (uint32_t)std::lround((coords[i * 3 + d] - lo[d]) * cells / ext) : 0u;
+    }
+    key[i] = hilbert3(c[0], c[1], c[2], bits);
+  }
+  std::vector<int32_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  for (int32_t k = 0; k < n; ++k) vertex_ordering[idx[k]] = k;  // old -> new
+  return SG_OK;
+}
+
+int sg_element_order(int32_t nE, int32_t card, const int32_t *endpoints, int32_t *element_order) {
+  SG_REQUIRE(nE >= 0 && card >= 1 && card <= 16, "sg_element_order: nE %d card %d", nE, card);
+  SG_REQUIRE(nE == 0 || (endpoints && element_order), "sg_element_order: null array");
+  std::vector<int32_t> s((size_t)nE * card);
+  for (int64_t e = 0; e < nE; ++e) {
+    std::copy(endpoints + e * card, endpoints + (e + 1) * card, s.begin() + e * card);
+    std::sort(s.begin() + e * card, s.begin() + (e + 1) * card);
+  }
+  std::vector<int32_t> idx(nE);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) {
+    return std::lexicographical_compare(s.begin() + (size_t)a * card,
+                                        s.begin() + (size_t)(a + 1) * card,
+                                        s.begin() + (size_t)b * card,
+                                        s.begin() + (size_t)(b + 1) * card);
+  });
+  std::copy(idx.begin(), idx.end(), element_order);  // new position -> old element
+  return SG_OK;
+}
+
+}  // extern "C"

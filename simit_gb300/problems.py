@@ -39,6 +39,26 @@ def hetero_mesh(ncell, seed=1):
             "lam": lam, "c": c, "ncell": ncell}
 
 
+def reorder_hetero(host, bits=10):
+    """The workload with vertices in Hilbert order and elements sorted by
+    their endpoints (simit::reorder); also returns vertex_ordering
+    (old -> new) to map solutions back: u_old = u_new.reshape(-1, 3)[vo]."""
+    from .runtime import reorder_mesh
+    vo, eo, tets = reorder_mesh(host["n"], host["tets"], 4, host["X0"], bits)
+    out = dict(host)
+    out["tets"] = tets
+    for k in ("X0", "x"):
+        a = np.empty_like(host[k].reshape(-1, 3))
+        a[vo] = host[k].reshape(-1, 3)
+        out[k] = a.reshape(-1)
+    c = np.empty_like(host["c"])
+    c[vo] = host["c"]
+    out["c"] = c
+    out["mu"], out["lam"] = host["mu"][eo], host["lam"][eo]
+    out["vertex_ordering"] = vo
+    return out
+
+
 class HeteroElasticity:
     """Device-resident instance: pattern, B/W, parameters, matrix and solver.
 

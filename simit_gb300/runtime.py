@@ -175,6 +175,35 @@ def assemble_scalar_springs(mesh, a, diag, scale, dtype=torch.float64, exact=Tru
         return vals
 
 
+def hilbert_order(coords, bits=10):
+    """vertex_ordering[old] = new (sg_hilbert_order) of host coordinates [n*3]."""
+    c = np.ascontiguousarray(coords, np.float64).reshape(-1)
+    n = c.size // 3
+    out = np.empty(n, np.int32)
+    call("sg_hilbert_order", n, c.ctypes.data, int(bits), out.ctypes.data)
+    return out
+
+
+def element_order(endpoints, card):
+    """element_order[new] = old (sg_element_order) of host endpoints."""
+    ep = np.ascontiguousarray(endpoints, np.int32).reshape(-1)
+    nE = ep.size // card
+    out = np.empty(nE, np.int32)
+    call("sg_element_order", nE, int(card), ep.ctypes.data, out.ctypes.data)
+    return out
+
+
+def reorder_mesh(n, endpoints, card, coords, bits=10):
+    """simit::reorder (src/reorder.cpp:252-273) of a host mesh: returns
+    (vertex_ordering old->new, element_order new->old, new endpoints).
+    Permute vertex fields with f_new[vo] = f_old and element fields with
+    f_new = f_old[eo]."""
+    vo = hilbert_order(coords, bits)
+    ep = vo[np.asarray(endpoints, np.int64).reshape(-1)].astype(np.int32)
+    eo = element_order(ep, card)
+    return vo, eo, ep.reshape(-1, card)[eo].reshape(-1)
+
+
 def assemble_blocks(mesh, eb, bs, dtype=torch.float64, exact=True):
     """`map f to E reduce +` of caller-evaluated element blocks eb
     [nE, card, card, bs, bs] into the mesh's pattern (values [nnzb*bs*bs])."""

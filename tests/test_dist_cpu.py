@@ -42,7 +42,8 @@ def _worker(rank, world, port, q):
     sm = sgd.sum_over_ranks(float(len(shard)))
     # the reference arm: rank 0 alone runs and prints (tiny sample)
     import bench
-    args = type("A", (), {"warmup": 0, "steps": 1, "cpu_sample": 3, "size": 128})()
+    args = type("A", (), {"warmup": 0, "steps": 1, "cpu_sample": 3, "size": 128,
+                           "no_reorder": False})()
     buf = io.StringIO()
     with redirect_stdout(buf):
         bench.run_reference(args, r, w)
@@ -59,7 +60,7 @@ def test_two_gloo_ranks():
     procs = [ctx.Process(target=_worker, args=(r, world, port, q)) for r in range(world)]
     for p in procs:
         p.start()
-    res = [q.get(timeout=300) for _ in range(world)]
+    res = [q.get(timeout=120) for _ in range(world)]
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0

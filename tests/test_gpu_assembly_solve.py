@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 import torch
 
-from simit_gb300 import _lib, meshgen
+from simit_gb300 import _lib, meshgen, problems
 from tests import scenarios
 
 pytestmark = pytest.mark.gpu
@@ -368,3 +368,26 @@ def test_solver_status_codes(ctx):
     bn[3] = float("nan")
     r3 = S2.solve(bn, torch.zeros_like(b))
     assert r3.status == 4
+
+
+def test_reordered_workload_solves_to_the_same_displacements(ctx, oracle):
+    """The Hilbert-reordered workload (simit::reorder) is the same system
+    renumbered: its solution, mapped back, solves the lattice-ordered system
+    to the same FP64 residual (FP64 assembly, so the two matrices differ by
+    element-order rounding only)."""
+    h = problems.hetero_mesh(10)
+    r = problems.reorder_hetero(h)
+    vo = r["vertex_ordering"]
+    sysm = []
+    for H in (h, r):
+        p = problems.HeteroElasticity(ctx, H, dtype=torch.float64, precond=_lib.PRECOND_JACOBI)
+        res = p.step()
+        ctx.sync()
+        assert res.status == 1
+        rp, ci = p.mesh.pattern.host()
+        sysm.append((rp, ci, _np(p.A), _np(p.b), _np(p.u).reshape(-1, 3)))
+        p.close()
+    rp, ci, A0, b0, u0 = sysm[0]
+    u1 = sysm[1][4][vo].reshape(-1)
+    r0 = b0 - oracle.spmv(h["n"], 3, rp, ci, A0, u1)
+    assert np.linalg.norm(r0) <= 1.01e-8 * np.linalg.norm(b0)
