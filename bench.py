@@ -35,7 +35,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=32, help="cells per edge of the CPU sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
     ap.add_argument("--no-reorder", action="store_true",
-                    help="keep the lattice vertex order (no Hilbert reordering)")
+                    help="keep the lattice vertex order (no space-filling-curve reordering)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner comparison")
     ap.add_argument("--spmv-only", action="store_true",
@@ -435,7 +435,8 @@ def run_spmv_only(args):
 def workload_name(size, reorder=True):
     return ("heterogeneous linear elasticity %d^3 five-tet lattice (fem_linear form, E log-uniform "
             "[1e3,1e6], nu U[0.35,0.45], bottom face fixed)%s, solve to 1e-8 FP64 relative "
-            "residual" % (size, ", vertices in Hilbert order (simit::reorder)" if reorder else ""))
+            "residual" % (size, ", vertices in Morton order, elements sorted (simit::reorder with a "
+                              "Z-curve)" if reorder else ""))
 
 
 def dist_setup(args):

@@ -325,12 +325,14 @@ int sg_batched_configs(void);
 /* ---------------------------------------------------------------------
  * Locality reordering (host; simit::reorder, src/reorder.cpp:252-273).
  * sg_hilbert_order: vertex_ordering[old] = new index of each vertex, by the
- * Hilbert index of its position on a 2^bits lattice spanning the bounding
- * box (ties by old index).  sg_element_order: element_order[new] = old index,
+ * Hilbert index of its position on a 2^bits lattice of cells spanning the
+ * bounding box (cell = floor((x - min) 2^bits / extent); ties by old index).  sg_element_order: element_order[new] = old index,
  * elements sorted by their sorted endpoint tuples (apply after relabelling
  * the endpoints).  sg_hilbert_index exposes the curve for tests.
  * ------------------------------------------------------------------- */
 int sg_hilbert_order(int32_t n, const double *coords, int32_t bits, int32_t *vertex_ordering);
+/* The same with the Morton (Z-order) curve (no counterpart in the reference). */
+int sg_morton_order(int32_t n, const double *coords, int32_t bits, int32_t *vertex_ordering);
 int sg_element_order(int32_t nE, int32_t card, const int32_t *endpoints, int32_t *element_order);
 int sg_hilbert_index(uint32_t x, uint32_t y, uint32_t z, int32_t bits, uint64_t *out);
 

@@ -80,6 +80,7 @@ SIGNATURES = {
     "sg_assemble_scalar_springs": (_CI, [P, _MP, _CI, P, D, D, P, _CI]),
     "sg_assemble_blocks": (_CI, [P, _MP, _CI, _CI, P, P, _CI]),
     "sg_hilbert_order": (_CI, [_CI, P, _CI, P]),
+    "sg_morton_order": (_CI, [_CI, P, _CI, P]),
     "sg_element_order": (_CI, [_CI, _CI, P, P]),
     "sg_hilbert_index": (_CI, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _CI, P]),
     "sg_tet_precompute": (_CI, [P, _MP, _CI, P, D, P, P, P]),

@@ -39,12 +39,13 @@ def hetero_mesh(ncell, seed=1):
             "lam": lam, "c": c, "ncell": ncell}
 
 
-def reorder_hetero(host, bits=10):
-    """The workload with vertices in Hilbert order and elements sorted by
-    their endpoints (simit::reorder); also returns vertex_ordering
-    (old -> new) to map solutions back: u_old = u_new.reshape(-1, 3)[vo]."""
+def reorder_hetero(host, bits=10, curve="morton"):
+    """The workload with vertices along a space-filling curve of their rest
+    positions (Morton by default; "hilbert" as simit::reorder) and elements
+    sorted by their endpoints; also returns vertex_ordering (old -> new) to
+    map solutions back: u_old = u_new.reshape(-1, 3)[vo]."""
     from .runtime import reorder_mesh
-    vo, eo, tets = reorder_mesh(host["n"], host["tets"], 4, host["X0"], bits)
+    vo, eo, tets = reorder_mesh(host["n"], host["tets"], 4, host["X0"], bits, curve)
     out = dict(host)
     out["tets"] = tets
     for k in ("X0", "x"):

@@ -175,12 +175,14 @@ def assemble_scalar_springs(mesh, a, diag, scale, dtype=torch.float64, exact=Tru
         return vals
 
 
-def hilbert_order(coords, bits=10):
-    """vertex_ordering[old] = new (sg_hilbert_order) of host coordinates [n*3]."""
+def hilbert_order(coords, bits=10, curve="hilbert"):
+    """vertex_ordering[old] = new (sg_hilbert_order, or sg_morton_order with
+    curve="morton") of host coordinates [n*3]."""
     c = np.ascontiguousarray(coords, np.float64).reshape(-1)
     n = c.size // 3
     out = np.empty(n, np.int32)
-    call("sg_hilbert_order", n, c.ctypes.data, int(bits), out.ctypes.data)
+    fn = {"hilbert": "sg_hilbert_order", "morton": "sg_morton_order"}[curve]
+    call(fn, n, c.ctypes.data, int(bits), out.ctypes.data)
     return out
 
 
@@ -193,12 +195,12 @@ def element_order(endpoints, card):
     return out
 
 
-def reorder_mesh(n, endpoints, card, coords, bits=10):
+def reorder_mesh(n, endpoints, card, coords, bits=10, curve="hilbert"):
     """simit::reorder (src/reorder.cpp:252-273) of a host mesh: returns
     (vertex_ordering old->new, element_order new->old, new endpoints).
     Permute vertex fields with f_new[vo] = f_old and element fields with
     f_new = f_old[eo]."""
-    vo = hilbert_order(coords, bits)
+    vo = hilbert_order(coords, bits, curve)
     ep = vo[np.asarray(endpoints, np.int64).reshape(-1)].astype(np.int32)
     eo = element_order(ep, card)
     return vo, eo, ep.reshape(-1, card)[eo].reshape(-1)

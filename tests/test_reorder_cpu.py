@@ -70,3 +70,15 @@ def test_reordered_system_is_the_permuted_system(oracle):
         lo, hi = rp1[a], rp1[a + 1]
         s = lo + np.searchsorted(ci1[lo:hi], b)
         assert np.allclose(A1[s], A0[q], rtol=1e-12, atol=1e-12 * np.abs(A0).max())
+
+
+def test_morton_order_groups_aligned_cubes():
+    side = 8
+    pts = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    vo = hilbert_order(pts.astype(np.float64), bits=3, curve="morton")
+    walk = np.empty_like(pts)
+    walk[vo] = pts
+    # every run of 8 consecutive vertices is one aligned 2x2x2 cube
+    cubes = walk.reshape(-1, 8, 3) // 2
+    assert np.all(cubes == cubes[:, :1, :])
+    assert sorted(vo) == list(range(side ** 3))
