@@ -325,8 +325,9 @@ int sg_batched_configs(void);
 /* ---------------------------------------------------------------------
  * Locality reordering (host; simit::reorder, src/reorder.cpp:252-273).
  * sg_hilbert_order: vertex_ordering[old] = new index of each vertex, by the
- * Hilbert index of its position on a 2^bits lattice of cells spanning the
- * bounding box (cell = floor((x - min) 2^bits / extent); ties by old index).  sg_element_order: element_order[new] = old index,
+ * Hilbert index of its cell, cell = floor((x - min) 2^bits / extent) in
+ * 0 .. 2^bits per axis (the curve spans 2^(bits+1) cells, so the upper
+ * faces come last; bits 1..20; ties by old index).  sg_element_order: element_order[new] = old index,
  * elements sorted by their sorted endpoint tuples (apply after relabelling
  * the endpoints).  sg_hilbert_index exposes the curve for tests.
  * ------------------------------------------------------------------- */

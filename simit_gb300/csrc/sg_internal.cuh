@@ -13,6 +13,16 @@ namespace sg {
 
 // Per-context state: the stream every call is ordered on, a grow-only device
 // scratch arena, a device error word and pinned host staging.
+// Per-device one-time flags (function attributes and occupancy are properties
+// of a device's context, not of the process).
+constexpr int SG_MAX_DEVICES = 64;
+inline bool first_on_device(bool (&done)[SG_MAX_DEVICES], int device) {
+  if (device < 0 || device >= SG_MAX_DEVICES) return true;
+  const bool first = !done[device];
+  done[device] = true;
+  return first;
+}
+
 struct Ctx {
   int device = 0;
   int num_sms = 0;

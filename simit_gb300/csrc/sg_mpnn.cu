@@ -288,11 +288,10 @@ static int graph_init(Ctx *c, const sg_matrix *A, GraphH *G) {
   SG_TRY(galloc(G, (void **)&g.dinv, n * 9 * 4));
   SG_TRY(alloc_layers(G));
   SG_TRY(galloc(G, (void **)&g.dres, 64));
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[SG_MAX_DEVICES] = {};
+  if (first_on_device(attr, c->device)) {
     SG_CHECK_CUDA(cudaFuncSetAttribute(k_f3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
     SG_CHECK_CUDA(cudaFuncSetAttribute(k_f4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
-    attr = true;
   }
   return graph_refresh(G);
 }
@@ -326,7 +325,8 @@ static int layers(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, con
   SG_CHECK_LAUNCH();
   // one wave of resident CTAs (a partial second wave would run the last
   // CTAs' tiles at a fraction of the occupancy)
-  static int per_sm = 0;
+  static int per_sm_dev[SG_MAX_DEVICES] = {};
+  int &per_sm = per_sm_dev[(c->device >= 0 && c->device < SG_MAX_DEVICES) ? c->device : 0];
   if (per_sm == 0) {
     int a3 = 0, a4 = 0;
     SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a3, k_f3, TC_WARPS * 32,

@@ -70,20 +70,23 @@ static int curve_order(int32_t n, const double *coords, int32_t bits, bool morto
       lo[d] = std::min(lo[d], v);
       hi[d] = std::max(hi[d], v);
     }
-  // cells of size extent / 2^bits, [lo, hi] -> 0 .. 2^bits - 1 (floor): a
-  // lattice with a power-of-two number of intervals keeps its points on
-  // aligned cells, so the curve's 2x2x2 groups are lattice cubes
+  // Cells of size extent / 2^bits: c = floor((x - lo) 2^bits / extent) in
+  // 0 .. 2^bits, and the curve runs on a 2^(bits+1) lattice, so points on
+  // the upper faces (c = 2^bits) follow all others instead of crowding into
+  // the last cells.  A lattice with a power-of-two number of intervals then
+  // keeps its interior points on aligned cells and the curve's 2x2x2 groups
+  // are lattice cubes, in step with the SpMV's 8-row tiles.
   const double cells = (double)(1u << bits);
-  const uint32_t top = (1u << bits) - 1;
+  const uint32_t top = 1u << bits;
   std::vector<uint64_t> key(n);
   for (int64_t i = 0; i < n; ++i) {
     uint32_t c[3];
     for (int d = 0; d < 3; ++d) {
       const double ext = hi[d] - lo[d];
       const double t = ext > 0 ? std::floor((coords[i * 3 + d] - lo[d]) * cells / ext) : 0.0;
-      c[d] = t >= (double)top ? top : (uint32_t)t;
+      c[d] = t >= (double)top ? top : (t < 0 ? 0u : (uint32_t)t);
     }
-    key[i] = morton ? morton3(c[0], c[1], c[2], bits) : hilbert3(c[0], c[1], c[2], bits);
+    key[i] = morton ? morton3(c[0], c[1], c[2], bits + 1) : hilbert3(c[0], c[1], c[2], bits + 1);
   }
   std::vector<int32_t> idx(n);
   std::iota(idx.begin(), idx.end(), 0);
@@ -106,13 +109,13 @@ int sg_hilbert_index(uint32_t x, uint32_t y, uint32_t z, int32_t bits, uint64_t 
 
 int sg_hilbert_order(int32_t n, const double *coords, int32_t bits, int32_t *vertex_ordering) {
   SG_REQUIRE(n >= 0 && (n == 0 || (coords && vertex_ordering)), "sg_hilbert_order: null array");
-  SG_REQUIRE(bits >= 1 && bits <= 21, "sg_hilbert_order: bits %d (1..21)", bits);
+  SG_REQUIRE(bits >= 1 && bits <= 20, "sg_hilbert_order: bits %d (1..20)", bits);
   return n == 0 ? SG_OK : curve_order(n, coords, bits, false, vertex_ordering);
 }
 
 int sg_morton_order(int32_t n, const double *coords, int32_t bits, int32_t *vertex_ordering) {
   SG_REQUIRE(n >= 0 && (n == 0 || (coords && vertex_ordering)), "sg_morton_order: null array");
-  SG_REQUIRE(bits >= 1 && bits <= 21, "sg_morton_order: bits %d (1..21)", bits);
+  SG_REQUIRE(bits >= 1 && bits <= 20, "sg_morton_order: bits %d (1..20)", bits);
   return n == 0 ? SG_OK : curve_order(n, coords, bits, true, vertex_ordering);
 }
 

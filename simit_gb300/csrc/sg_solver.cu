@@ -153,13 +153,11 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
       case PK_NONE: launch_k2_v4<PK_NONE>(S, st, par); break;
       case PK_JACOBI: launch_k2_v4<PK_JACOBI>(S, st, par); break;
       case PK_BLOCK3: {
-        static bool attr = false;
+        static bool attr[SG_MAX_DEVICES] = {};
         const size_t sm = K2W_WARPS * sizeof(K2WarpSmem);
-        if (!attr) {
+        if (first_on_device(attr, S->c->device))
           SG_CHECK_CUDA(cudaFuncSetAttribute(k_cg_update_w<true>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-          attr = true;
-        }
         const int64_t nchunks = (S->len / 12 + 31) / 32;
         int64_t grid = (nchunks + K2W_WARPS - 1) / K2W_WARPS;
         if (grid > 2 * (int64_t)S->c->num_sms) grid = 2 * (int64_t)S->c->num_sms;

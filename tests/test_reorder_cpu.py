@@ -25,13 +25,18 @@ def test_hilbert_index_is_a_bijection_with_unit_steps():
 
 
 def test_hilbert_order_of_a_lattice_walks_neighbours():
-    side = 8
+    """A lattice of 2^3 + 1 points per axis: the 8^3 interior cells come
+    first along the curve in unit steps, then the upper faces."""
+    side = 9
     pts = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)
     vo = hilbert_order(pts.astype(np.float64) * 0.125 + 0.3, bits=3)
     assert sorted(vo) == list(range(side ** 3))
     walk = np.empty_like(pts)
     walk[vo] = pts
-    assert np.all(np.abs(np.diff(walk, axis=0)).sum(1) == 1)
+    inner = walk[:512]
+    assert np.all(inner < 8)
+    assert np.all(np.abs(np.diff(inner, axis=0)).sum(1) == 1)
+    assert np.all((walk[512:] == 8).any(1))
 
 
 def test_element_order_sorts_sorted_tuples():
@@ -73,12 +78,12 @@ def test_reordered_system_is_the_permuted_system(oracle):
 
 
 def test_morton_order_groups_aligned_cubes():
-    side = 8
+    side = 9
     pts = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)
     vo = hilbert_order(pts.astype(np.float64), bits=3, curve="morton")
     walk = np.empty_like(pts)
     walk[vo] = pts
-    # every run of 8 consecutive vertices is one aligned 2x2x2 cube
-    cubes = walk.reshape(-1, 8, 3) // 2
+    # every run of 8 consecutive interior vertices is one aligned 2x2x2 cube
+    cubes = walk[:512].reshape(-1, 8, 3) // 2
     assert np.all(cubes == cubes[:, :1, :])
     assert sorted(vo) == list(range(side ** 3))
