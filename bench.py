@@ -74,6 +74,21 @@ def _ev_ms(st, fn, reps=1):
     return e0.elapsed_time(e1) / reps, out
 
 
+def _reorder_grid(mg, with_orders=False):
+    """A meshgen.tet_grid mesh renumbered along the Morton curve of its rest
+    positions, elements sorted by endpoints (as the elasticity workload)."""
+    import numpy as np
+    from simit_gb300.runtime import reorder_mesh
+    vo, eo, tets = reorder_mesh(mg["n"], mg["tets"], 4, mg["X0"], curve="morton")
+    out = dict(mg)
+    out["tets"] = tets
+    for k in ("X0", "x"):
+        a = np.empty_like(mg[k].reshape(-1, 3))
+        a[vo] = mg[k].reshape(-1, 3)
+        out[k] = a.reshape(-1)
+    return (out, vo, eo) if with_orders else out
+
+
 def run_neo(args):
     """femTet.sim form: one implicit Newton step (A = M + h^2 K_neo(x), b =
     compute_force, h = 0.01) on the 64^3 five-tet lattice, E = 1e5, nu = 0.4,
@@ -90,6 +105,8 @@ def run_neo(args):
     torch.cuda.set_stream(ctx.torch_stream)
     st = ctx.torch_stream
     mg = meshgen.tet_grid(size, disp=1e-3, seed=2)
+    if not args.no_reorder:
+        mg = _reorder_grid(mg)
     nT = len(mg["tets"]) // 4
     E, nu = 1e5, 0.4
     mu = np.full(nT, E / (2 * (1 + nu)))
@@ -228,6 +245,12 @@ def run_heat(args):
     g = meshgen.rng(31)
     kappa = 10 ** g.uniform(-2, 2, nT)
     T0 = g.uniform(0, 1, mg["n"])
+    if not args.no_reorder:
+        mg, vo, eo = _reorder_grid(mg, with_orders=True)
+        kappa = kappa[eo]
+        T0n = np.empty_like(T0)
+        T0n[vo] = T0
+        T0 = T0n
     mesh = Mesh(ctx, mg["n"], mg["tets"], 4)
     d = ctx.device
     out = {"workload": "P1 heat %d^3 (%d DOF, nnz %d)" % (size, mg["n"], mesh.nnzb)}
