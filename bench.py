@@ -430,7 +430,7 @@ def run_spmv_only(args):
     SpMV launches with sg_bspmv(g = --lanes), event-timed."""
     import torch
     from simit_gb300 import _lib, problems
-    from simit_gb300.runtime import Context, bspmv
+    from simit_gb300.runtime import Context, bspmv, bsr_add_diag
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
     dt = torch.float64 if args.f64 else torch.float32
@@ -450,9 +450,25 @@ def run_spmv_only(args):
     e1.record(ctx.torch_stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / args.reps
-    nbytes = m.nnzb * (9 * x.element_size() + 4) + (m.n + 1) * 4 + m.n * 3 * 2 * x.element_size()
+    s = x.element_size()
+    nbytes = m.nnzb * (9 * s + 4) + (m.n + 1) * 4 + m.n * 3 * 2 * s
+    # the matrix expression MD + K (sg_bsr_add_diag) on the same pattern:
+    # K read and the result written once, the row's column indices and D once
+    D = torch.rand(m.n * 9, dtype=dt, device=ctx.device)
+    out = torch.empty_like(p.A)
+    bsr_add_diag(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, diag=D, out=out)
+    e0.record(ctx.torch_stream)
+    for _ in range(args.reps):
+        bsr_add_diag(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, diag=D, out=out)
+    e1.record(ctx.torch_stream)
+    e1.synchronize()
+    ctx.sync()
+    ad_ms = e0.elapsed_time(e1) / args.reps
+    ad_bytes = m.nnzb * (2 * 9 * s + 4) + (m.n + 1) * 4 + m.n * 9 * s
     print(json.dumps({"size": args.size, "lanes": args.lanes, "dtype": str(dt), "nnzb": m.nnzb,
-                      "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes}), flush=True)
+                      "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes,
+                      "add_diag_ms": ad_ms, "add_diag_GBps": ad_bytes / ad_ms / 1e6,
+                      "add_diag_bytes": ad_bytes}), flush=True)
 
 
 def workload_name(size, reorder=True):

@@ -48,6 +48,9 @@ int sg_ctx_create(int device, sg_ctx **out);
 /* Releases the caller's reference; the context (and its stream) lives on
  * until every solver created on it has been destroyed too. */
 int sg_ctx_destroy(sg_ctx *ctx);
+/* Waits for the context's stream, then reports (SG_ERR_DEVICE) and clears a
+ * device-side check that failed in an asynchronous call since the last
+ * check (an assembly row longer than its bound, a missing diagonal block). */
 int sg_ctx_sync(sg_ctx *ctx);
 /* The context's stream as an opaque pointer (a cudaStream_t). */
 void *sg_ctx_stream(sg_ctx *ctx);
@@ -198,6 +201,18 @@ int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
  * `points.x = points.x + h * points.v` of apps/springs/isprings.sim:94 and
  * `verts.x = h * x + verts.x` of femTet.sim); vec_dtype for x and y. */
 int sg_axpy(sg_ctx *ctx, int64_t len, int vec_dtype, double alpha, const void *x, void *y);
+
+/* System-matrix expression out = D + scale*K on K's pattern (replaces the
+ * lowered `MDK = MD + K` of apps/springs/isprings.sim:74, with the storage
+ * rules of src/storage.cpp:358-360 and 416-470).  D is Diagonal storage:
+ * diag [n*bs*bs] (block of vertex v at v*bs*bs, row-major), or, with diag
+ * NULL, ident*I (ident = 0: no diagonal term, out = 0 + scale*K).  A diagonal
+ * slot holds D + (scale*K), every other slot 0 + (scale*K), each operation
+ * rounded separately in dtype.  out may alias vals.  Asynchronous; a row
+ * without its diagonal block, when D is given, fails the next sg_ctx_sync. */
+int sg_bsr_add_diag(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
+                    const uint32_t *colidx, int dtype, const void *diag,
+                    double ident, double scale, const void *vals, void *out);
 
 /* Dot product of two blocked vectors with an FP64 deterministic two-level
  * reduction; synchronises. */

@@ -69,6 +69,9 @@ def lib():
         L.or_tet_step.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _I64, _P, _P, _P, _P, _P,
                                   _D, _D, _P, _P, _P, _D, ctypes.c_int]
         L.or_heat_assemble.argtypes = [_I32, _I64, _P, _P, _P, _P, _D, _P, _P, _P, _P, _P]
+        L.or_add_diag_f64.argtypes = [_I32, _I32, _P, _P, _P, _D, ctypes.c_int, _D, _P, _P]
+        L.or_add_diag_f32.argtypes = [_I32, _I32, _P, _P, _P, ctypes.c_float, ctypes.c_int,
+                                      ctypes.c_float, _P, _P]
         _lib = L
     return _lib
 
@@ -153,6 +156,20 @@ def spmv(n, bs, rowptr, colidx, vals, x):
         lib().or_spmv_f64(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
                           _p(_c(vals, np.float64)), _p(_c(x, np.float64)), _p(y))
     return y
+
+
+def add_diag(n, bs, rowptr, colidx, K, diag=None, ident=0.0, scale=1.0):
+    """out = D + scale*K on K's pattern, the lowered `MDK = MD + K` of
+    apps/springs/isprings.sim:74 (MDK = 0; MDK[loc(l,l)] = D[l];
+    MDK[lm] = MDK[lm] + scale*K[lm]) in K's dtype; diag None: D = ident*I."""
+    dt = np.float32 if K.dtype == np.float32 else np.float64
+    out = np.zeros(len(K), dt)
+    has_d = int(diag is not None or ident != 0.0)
+    d = None if diag is None else _c(diag, dt)
+    f = lib().or_add_diag_f32 if dt == np.float32 else lib().or_add_diag_f64
+    f(n, bs, _p(_c(rowptr, np.uint32)), _p(_c(colidx, np.uint32)),
+      None if d is None else _p(d), ident, has_d, scale, _p(_c(K, dt)), _p(out))
+    return out
 
 
 def cg_normr2(n, bs, rowptr, colidx, A, b, x0, tol2, maxiters):

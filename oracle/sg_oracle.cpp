@@ -21,6 +21,7 @@
 //   ascending / per block-row dot over the block columns then `+=`, and dot
 //   products as a per-vertex partial sum added to the total.
 // Compile with -ffp-contract=off: the reference JIT does not fuse multiply-adds.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -718,6 +719,42 @@ void or_heat_assemble(i32 n, i64 nT, const i32 *tets, const double *B,
       b[vv[i]] += bi;
     }
   }
+}
+
+// System-matrix expression out = D + s*K on K's pattern, the lowered loop of
+// `MDK = MD + K` (apps/springs/isprings.sim:74): MDK = 0; MDK[loc(l,l)] =
+// D[l] (or ident*I); MDK[lm] = MDK[lm] + (s*K[lm]) over the row's slots.
+// has_d = 0: no diagonal term.
+}  // extern "C"
+namespace {
+template <typename T>
+void add_diag(i32 n, i32 bs, const u32 *rowptr, const u32 *colidx, const T *D,
+                     T ident, int has_d, T s, const T *K, T *out) {
+  const i64 bb = (i64)bs * bs, nnz = rowptr[n];
+  std::vector<T> M((size_t)(nnz * bb), T(0));
+  for (i32 l = 0; l < n; ++l) {
+    if (has_d) {
+      const u32 d = loc(l, l, rowptr, colidx);
+      for (i64 q = 0; q < bb; ++q)
+        M[(size_t)(d * bb + q)] = D ? D[(i64)l * bb + q] : (q / bs == q % bs ? ident : T(0));
+    }
+    for (u32 lm = rowptr[l]; lm < rowptr[l + 1]; ++lm)
+      for (i64 q = 0; q < bb; ++q) {
+        const T sk = s * K[(i64)lm * bb + q];
+        M[(size_t)(lm * bb + q)] = M[(size_t)(lm * bb + q)] + sk;
+      }
+  }
+  std::copy(M.begin(), M.end(), out);
+}
+}  // namespace
+extern "C" {
+void or_add_diag_f64(i32 n, i32 bs, const u32 *rowptr, const u32 *colidx, const double *D,
+                     double ident, int has_d, double s, const double *K, double *out) {
+  add_diag<double>(n, bs, rowptr, colidx, D, ident, has_d, s, K, out);
+}
+void or_add_diag_f32(i32 n, i32 bs, const u32 *rowptr, const u32 *colidx, const float *D,
+                     float ident, int has_d, float s, const float *K, float *out) {
+  add_diag<float>(n, bs, rowptr, colidx, D, ident, has_d, s, K, out);
 }
 
 }  // extern "C"

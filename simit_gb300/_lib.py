@@ -75,6 +75,7 @@ SIGNATURES = {
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),
+    "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, _CI, P, D, D, P, P]),
     "sg_pattern_maxrow": (_CI, [P, I32, P, ctypes.POINTER(I32)]),
     "sg_assemble_springs": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, D, D, P, P, P, _CI]),
     "sg_assemble_scalar_springs": (_CI, [P, _MP, _CI, P, D, D, P, _CI]),

@@ -252,8 +252,7 @@ int sg_ctx_destroy(sg_ctx *h) {
 int sg_ctx_sync(sg_ctx *h) {
   Ctx *c = as_ctx(h);
   if (!c) return set_error(SG_ERR_ARG, "sg_ctx_sync: null context");
-  SG_CHECK_CUDA(cudaStreamSynchronize(c->stream));
-  return SG_OK;
+  return check_device_error(c, "sg_ctx_sync");
 }
 
 void *sg_ctx_stream(sg_ctx *h) { return h ? (void *)as_ctx(h)->stream : nullptr; }

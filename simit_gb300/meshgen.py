@@ -152,24 +152,71 @@ def cloth_sheet(side, seed=0, spacing=None):
             "l0": l0, "fixed": fixed}
 
 
-def load_tetgen(node_path, ele_path):
-    """TetGen .node/.ele reader following MeshVol::loadTet (src/mesh.cpp:
-    246-321): first token of the header is the count, '#' lines and lines
-    shorter than 3 characters are skipped, the leading index is dropped."""
-    def rows(path):
-        with open(path) as f:
-            head = f.readline().split()
-            out = []
-            for ln in f:
-                if len(ln.rstrip("\n")) < 3 or ln.startswith("#"):
-                    continue
-                out.append(ln.split())
-        return head, out
+def _tetgen_records(text, nhead, width):
+    """Records of one TetGen file as MeshVol::loadTet / loadTetEdge read them
+    (src/mesh.cpp:253-321, 341-373): the first nhead tokens are the header
+    (the record count first), the rest of that line is dropped; then lines
+    are read while the stream has not hit its end, so a last line without a
+    newline is not read; lines shorter than 3 characters and lines starting
+    with '#' are skipped; each record drops its leading index and keeps the
+    next `width` integers or numbers (width from the header when None).  The
+    result has exactly `count` rows, zero-filled past the records present."""
+    first, _, rest = text.partition("\n")
+    head = first.split()[:nhead]
+    count = int(head[0])
+    width = int(head[1]) if width is None else width
+    segments = rest.split("\n")[:-1]  # the last segment ends at end-of-file
+    rows = []
+    for ln in segments:
+        if len(rows) >= count:
+            break
+        if len(ln) < 3 or ln[0] == "#":
+            continue
+        rows.append(ln.split()[1:1 + width])
+    return count, width, rows
 
-    h, r = rows(node_path)
-    nv = int(h[0])
-    x = np.array([[float(t) for t in row[1:4]] for row in r[:nv]], np.float64)
-    h, r = rows(ele_path)
-    ne, per = int(h[0]), int(h[1])
-    e = np.array([[int(t) for t in row[1:1 + per]] for row in r[:ne]], np.int32)
+
+def parse_tetgen_nodes(text):
+    """Vertex positions [n, 3] (float64) of a TetGen .node text."""
+    n, _, rows = _tetgen_records(text, 1, 3)
+    x = np.zeros((n, 3), np.float64)
+    for i, r in enumerate(rows):
+        x[i, :len(r)] = [float(t) for t in r]
+    return x
+
+
+def parse_tetgen_elements(text):
+    """Element endpoints [nE, per] (int32) of a TetGen .ele text (the
+    header's second token is the endpoints per element)."""
+    ne, per, rows = _tetgen_records(text, 2, None)
+    e = np.zeros((ne, per), np.int32)
+    for i, r in enumerate(rows):
+        e[i, :len(r)] = [int(t) for t in r]
+    return e
+
+
+def parse_tetgen_edges(text):
+    """Edge endpoints [nEdges, 2] (int32) of a TetGen .edge text (boundary
+    markers after the two endpoints are ignored)."""
+    ne, _, rows = _tetgen_records(text, 1, 2)
+    e = np.zeros((ne, 2), np.int32)
+    for i, r in enumerate(rows):
+        e[i, :len(r)] = [int(t) for t in r]
+    return e
+
+
+def load_tetgen(node_path, ele_path):
+    """TetGen .node/.ele files (MeshVol::loadTet): flat positions [n*3] and
+    endpoints [nE*per]; indices are kept as written (no 1-based shift)."""
+    with open(node_path) as f:
+        x = parse_tetgen_nodes(f.read())
+    with open(ele_path) as f:
+        e = parse_tetgen_elements(f.read())
     return x.reshape(-1), e.reshape(-1)
+
+
+def load_tetgen_edges(edge_path):
+    """TetGen .edge file (MeshVol::loadTetEdge): flat endpoints [nEdges*2],
+    the spring set of apps/springs/springs.cpp."""
+    with open(edge_path) as f:
+        return parse_tetgen_edges(f.read()).reshape(-1)

@@ -111,6 +111,20 @@ def bspmv(ctx, n, bs, rowptr, colidx, vals, x, y=None, g=0):
     return y
 
 
+def bsr_add_diag(ctx, n, bs, rowptr, colidx, vals, diag=None, ident=0.0, scale=1.0, out=None):
+    """System-matrix expression D + scale*K on K's pattern (`MDK = MD + K`):
+    diag [n*bs*bs] Diagonal storage or, with diag None, ident*I.  out may be
+    vals (in place).  Values and diag share vals' dtype."""
+    if out is None:
+        with ctx.stream():
+            out = torch.empty_like(vals)
+    if diag is not None:
+        assert diag.dtype == vals.dtype and diag.numel() == n * bs * bs
+    call("sg_bsr_add_diag", ctx.h, n, bs, ptr(rowptr), ptr(colidx), dtype_code(vals),
+         ptr(diag) if diag is not None else None, float(ident), float(scale), ptr(vals), ptr(out))
+    return out
+
+
 def dot(ctx, a, b):
     out = ctypes.c_double()
     call("sg_dot", ctx.h, a.numel(), dtype_code(a), ptr(a), ptr(b), ctypes.byref(out))

@@ -6,6 +6,9 @@ SIMIT_REFERENCE); the GPU machine has none, so the outputs are committed:
   reference_golden.json   golden values asserted by the reference's tests,
                           extracted from their sources (file:line recorded)
   bar2k.node, bar2k.ele   the TetGen fixture test/program-fem-test.cpp loads
+  tetgen_golden.json      the TetGen .node/.ele/.edge texts of
+                          test/mesh-test.cpp (TetgenTest, TetgenEdgeTest)
+                          with the values those tests assert
   pattern_golden.json     pattern + slot map of small meshes produced by the
                           reference's own PathIndexBuilder / `loc`
                           (oracle/_ref/libref_pattern.so)
@@ -57,6 +60,16 @@ def extract_assert_eq(path, test_name):
     return out
 
 
+def extract_raw_strings(path, test_name):
+    """The R"(...)" string constants inside TEST(..., test_name), by name."""
+    src = open(path).read()
+    m = re.search(r"TEST\(\w+,\s*%s\)\s*\{" % test_name, src)
+    body = src[m.end():]
+    nxt = re.search(r"\nTEST\(", body)
+    body = body[:nxt.start()] if nxt else body
+    return {k: v for k, v in re.findall(r"string\s+(\w+)\s*=\s*R\"\((.*?)\)\";", body, re.S)}
+
+
 def main():
     test = os.path.join(REF, "test")
     if not os.path.isdir(test):
@@ -77,6 +90,13 @@ def main():
     }
     with open(os.path.join(HERE, "reference_golden.json"), "w") as f:
         json.dump(golden, f, indent=1)
+    mesh_test = os.path.join(test, "mesh-test.cpp")
+    tetgen = {}
+    for name in ("TetgenTest", "TetgenEdgeTest"):
+        tetgen[name] = {"texts": extract_raw_strings(mesh_test, name),
+                        "asserts": extract_assert_eq(mesh_test, name)}
+    with open(os.path.join(HERE, "tetgen_golden.json"), "w") as f:
+        json.dump(tetgen, f, indent=1)
     for ext in ("node", "ele"):
         shutil.copy(os.path.join(test, "input", "program", "fem", "bar2k." + ext),
                     os.path.join(HERE, "bar2k." + ext))

@@ -113,3 +113,43 @@ def element_block_scenarios():
     eb = np.ones((2, 2, 2, 1, 1))
     out.append(("matrix_vv", 3, ep, 1, eb, np.ones(3)))
     return out
+
+
+def tet_edges(tets):
+    """Unique undirected edges (i < j, sorted) of a tet mesh's elements."""
+    t = np.asarray(tets, np.int64).reshape(-1, 4)
+    pairs = np.concatenate([t[:, [a, b]] for a in range(4) for b in range(a + 1, 4)], 0)
+    pairs.sort(axis=1)
+    return np.unique(pairs, axis=0).astype(np.int32)
+
+
+def write_tetgen_edges(path, edges):
+    """A TetGen .edge file: header "count 1", then "index v0 v1 marker"."""
+    with open(path, "w") as f:
+        f.write("%d  1\n" % len(edges))
+        for i, (a, b) in enumerate(edges):
+            f.write("%5d %6d %6d  -1\n" % (i, a, b))
+        f.write("# written by tests/scenarios.py\n")
+
+
+def springs_from_tetgen(node_path, edge_path):
+    """apps/springs/springs.cpp:15-90 on TetGen files: positions normalised to
+    [0, 1] per axis, points below z = 0.1 fixed, one spring per .edge record
+    with k = 1e4, l0 its rest length and half its mass (pi r^2 l0 * 1e3,
+    r = 0.01) on each endpoint; apps/springs/isprings.sim constants (h = 1e-2,
+    viscous = 2, gravity -9.81 y, CG while r'r > 1e-12, at most 50 steps)."""
+    x = meshgen.parse_tetgen_nodes(open(node_path).read())
+    ep = meshgen.load_tetgen_edges(edge_path).reshape(-1, 2)
+    mn, mx = x.min(0), x.max(0)
+    x = (x - mn) / (mx - mn)
+    d = x[ep[:, 1]] - x[ep[:, 0]]
+    l0 = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+    mass = (3.14159265358979 * 0.01 * 0.01 * l0) * 1e3
+    m = np.zeros(len(x))
+    for (a, b), ms in zip(ep, mass):  # element order, as the reference's loop
+        m[a] += 0.5 * ms
+        m[b] += 0.5 * ms
+    return {"n": len(x), "x": x.reshape(-1), "v": np.zeros(x.size), "m": m,
+            "fixed": (x[:, 2] < 0.1).astype(np.uint8), "ep": ep.reshape(-1).astype(np.int32),
+            "k": np.full(len(ep), 1e4), "l0": l0, "h": 1e-2, "viscous": 2.0,
+            "grav": np.array([0.0, -9.81, 0.0]), "tol2": 1e-12, "maxiters": 50, "form": 0}

@@ -61,6 +61,38 @@ def test_isprings_golden_gpu(ctx, oracle):
         assert abs(got - g["expected"]) <= GOLD_TOL, (g, got)
 
 
+def test_springs_on_tetgen_edges_gpu(ctx, oracle, tmp_path):
+    """apps/springs/springs.cpp end to end: the bar2k TetGen mesh's edges
+    written as a .edge file, read back with the MeshVol::loadTetEdge rules,
+    three implicit steps of apps/springs/isprings.sim (FP64, exact-mode
+    assembly, 50 CG iterations) on the GPU against the oracle."""
+    import os
+    from simit_gb300.runtime import Mesh, assemble_springs
+    node = os.path.join(scenarios.GOLDEN, "bar2k.node")
+    _, tets = meshgen.load_tetgen(node, os.path.join(scenarios.GOLDEN, "bar2k.ele"))
+    edge = str(tmp_path / "bar2k.edge")
+    scenarios.write_tetgen_edges(edge, scenarios.tet_edges(tets))
+    s = scenarios.springs_from_tetgen(node, edge)
+    mesh = Mesh(ctx, s["n"], s["ep"], 2)
+    rp, ci = mesh.pattern.host()
+    d = ctx.device
+    x, v = torch.tensor(s["x"], device=d), torch.tensor(s["v"], device=d)
+    ox, ov = s["x"].copy(), s["v"].copy()
+    for _ in range(3):
+        vals, f = assemble_springs(mesh, x, v, s["m"], s["fixed"], s["k"], s["l0"], s["h"],
+                                   s["viscous"], s["grav"], form=s["form"])
+        v, res = _cg_ref_form(ctx, mesh, vals, f, v, 3, s["tol2"], s["maxiters"],
+                              _lib.STOP_NORMR2)
+        with ctx.stream():
+            x = x + s["h"] * v
+        oracle.springs_step(s["form"], ox, ov, s["m"], s["fixed"], s["ep"], s["k"], s["l0"],
+                            s["h"], s["viscous"], s["grav"], rp, ci, s["tol2"], s["maxiters"])
+    ctx.sync()
+    # the same 50 CG iterations; only the dot products' summation order differs
+    assert np.abs(_np(v) - ov).max() <= 1e-9 * np.abs(ov).max()
+    assert np.abs(_np(x) - ox).max() <= 1e-12 * np.abs(ox).max()
+
+
 def test_cg_golden_gpu(ctx):
     from simit_gb300.runtime import Mesh, assemble_scalar_springs
     s = scenarios.cg_chain()

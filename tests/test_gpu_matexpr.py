@@ -1,0 +1,127 @@
+"""GPU parity of the system-matrix expression D + s*K (sg_bsr_add_diag)
+against the oracle's lowered `MDK = MD + K` loop, bit-exact, and the unfused
+isprings composition (K alone, then MD + K) against the fused assembly."""
+import numpy as np
+import pytest
+import torch
+
+from simit_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_ctx):
+    return gpu_ctx
+
+
+def _system(oracle, n, nE, bs, seed, dt, with_diag=True):
+    g = meshgen.rng(seed)
+    ep = g.integers(0, n, size=nE * 2).astype(np.int32)
+    if with_diag:  # a self-edge per vertex: every row holds its diagonal block
+        ep = np.concatenate([ep, np.repeat(np.arange(n, dtype=np.int32), 2)])
+    rp, ci = oracle.pattern(n, ep, 2)
+    K = g.uniform(-1, 1, size=len(ci) * bs * bs).astype(dt)
+    K[::7] = -0.0  # signed zeros: 0 + (-0) is +0 in the lowered loop
+    D = g.uniform(-2, 2, size=n * bs * bs).astype(dt)
+    return rp, ci, K, D
+
+
+def _t(a, d):
+    return torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(d)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("bs", [1, 2, 3])
+@pytest.mark.parametrize("mode", ["diag", "ident", "none"])
+@pytest.mark.parametrize("scale", [1.0, -0.37])
+def test_add_diag_bit_exact(ctx, oracle, dt, bs, mode, scale):
+    from simit_gb300.runtime import bsr_add_diag
+    n = 1500
+    rp, ci, K, D = _system(oracle, n, 5000, bs, 11 + bs, dt)
+    d = ctx.device
+    kw = {"diag": D, "ident": 0.0} if mode == "diag" else (
+        {"diag": None, "ident": 2.5} if mode == "ident" else {"diag": None, "ident": 0.0})
+    ref = oracle.add_diag(n, bs, rp, ci, K, scale=scale, **kw)
+    got = bsr_add_diag(ctx, n, bs, _t(rp, d), _t(ci, d), _t(K, d),
+                       diag=None if kw["diag"] is None else _t(D, d), ident=kw["ident"],
+                       scale=scale)
+    ctx.sync()
+    g = got.cpu().numpy()
+    assert g.tobytes() == ref.tobytes()  # bit-exact, signed zeros included
+
+
+def test_add_diag_in_place(ctx, oracle):
+    from simit_gb300.runtime import bsr_add_diag
+    n = 800
+    rp, ci, K, D = _system(oracle, n, 3000, 3, 5, np.float32)
+    d = ctx.device
+    ref = oracle.add_diag(n, 3, rp, ci, K, diag=D, scale=0.5)
+    Kd = _t(K.copy(), d)
+    out = bsr_add_diag(ctx, n, 3, _t(rp, d), _t(ci, d), Kd, diag=_t(D, d), scale=0.5, out=Kd)
+    ctx.sync()
+    assert out.data_ptr() == Kd.data_ptr()
+    assert Kd.cpu().numpy().tobytes() == ref.tobytes()
+
+
+def test_add_diag_missing_diagonal(ctx, oracle):
+    """A vertex without incident elements has no diagonal slot: adding a
+    diagonal fails the next sync (and the error is cleared)."""
+    from simit_gb300._lib import SimitError
+    from simit_gb300.runtime import bsr_add_diag
+    n = 300
+    rp, ci, K, D = _system(oracle, n, 50, 1, 9, np.float64, with_diag=False)
+    assert np.any(np.diff(rp.astype(np.int64)) == 0)
+    d = ctx.device
+    args = (ctx, n, 1, _t(rp, d), _t(ci, d), _t(K, d))
+    bsr_add_diag(*args, diag=_t(D, d))
+    with pytest.raises(SimitError):
+        ctx.sync()
+    bsr_add_diag(*args, diag=None, ident=0.0)  # no diagonal term: fine
+    ctx.sync()
+
+
+def test_add_diag_empty_and_bad_args(ctx, oracle):
+    from simit_gb300._lib import SimitError
+    from simit_gb300.runtime import bsr_add_diag
+    d = ctx.device
+    z = torch.zeros(1, dtype=torch.int32, device=d)
+    e = torch.zeros(0, dtype=torch.float64, device=d)
+    bsr_add_diag(ctx, 0, 3, z, z, e)
+    ctx.sync()
+    rp, ci, K, D = _system(oracle, 20, 40, 3, 2, np.float64)
+    with pytest.raises(SimitError):  # both a diagonal array and ident
+        bsr_add_diag(ctx, 20, 3, _t(rp, d), _t(ci, d), _t(K, d), diag=_t(D, d), ident=1.0)
+    with pytest.raises(SimitError):  # block size out of range
+        bsr_add_diag(ctx, 20, 4, _t(rp, d), _t(ci, d), _t(K, d))
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_isprings_unfused_matches_fused(ctx, oracle, dtype):
+    """isprings.sim unchanged: K from the springs map alone (zero mass and
+    damping, so its diagonal term is 0), MD = (m + h*viscous)*I per point as
+    Diagonal storage, then MDK = MD + K — equal to the fused assembly (the
+    exact kernels, so h*viscous + m is not contracted)."""
+    from simit_gb300.runtime import Mesh, assemble_springs, bsr_add_diag
+    L = meshgen.springs_lattice(10, 10, 10, 0.1, 0.01, seed=4)
+    n = L["n"]
+    g = meshgen.rng(8)
+    v = g.uniform(-0.1, 0.1, n * 3)
+    m = g.uniform(0.5, 2.0, n)
+    k = np.full(len(L["l0"]), 1e4)
+    l0 = L["l0"] * g.uniform(0.9, 1.1, len(L["l0"]))
+    fixed = np.zeros(n, np.uint8)
+    grav = np.array([0, 0, -9.81])
+    h, visc = 1e-3, 0.5
+    mesh = Mesh(ctx, n, L["ep"], 2)
+    fused, _ = assemble_springs(mesh, L["x"], v, m, fixed, k, l0, h, visc, grav, dtype=dtype)
+    K, _ = assemble_springs(mesh, L["x"], v, np.zeros(n), fixed, k, l0, h, 0.0, grav,
+                            dtype=dtype)
+    np_dt = np.float64 if dtype == torch.float64 else np.float32
+    md = (m.astype(np_dt) + np_dt(h) * np_dt(visc)).astype(np_dt)
+    MD = (md[:, None, None] * np.eye(3, dtype=np_dt)[None]).reshape(-1)
+    p = mesh.pattern
+    MDK = bsr_add_diag(ctx, n, 3, p.rowptr, p.colidx, K,
+                       diag=torch.from_numpy(MD).to(ctx.device))
+    ctx.sync()
+    assert torch.equal(MDK, fused)

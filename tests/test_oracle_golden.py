@@ -113,3 +113,35 @@ def test_element_block_assembly_golden(oracle):
         y = oracle.spmv(n, bs, rp, ci, vals, x)
         want = [g["expected"] for g in scenarios.golden(name)]
         assert list(y) == want, (name, list(y), want)
+
+
+def test_add_diag_semantics(oracle):
+    """The oracle's `MDK = MD + K` (apps/springs/isprings.sim:74) on a hand
+    case: rows {0: cols 0, 1}, {1: col 1}; diagonal slots get D + s*K, the
+    others 0 + s*K (a -0 becomes +0), ident*I when no array is given."""
+    rp = np.array([0, 2, 3], np.uint32)
+    ci = np.array([0, 1, 1], np.uint32)
+    K = np.array([1.0, -0.0, 3.0])
+    out = oracle.add_diag(2, 1, rp, ci, K, diag=np.array([10.0, 20.0]))
+    assert out.tolist() == [11.0, 0.0, 23.0] and not np.signbit(out[1])
+    out = oracle.add_diag(2, 1, rp, ci, K, ident=2.0, scale=-0.5)
+    assert out.tolist() == [1.5, 0.0, 0.5]
+    # 3x3 blocks: the identity lands on each diagonal block's diagonal only
+    K3 = np.zeros(27)
+    out = oracle.add_diag(2, 3, rp, ci, K3, ident=1.0)
+    blocks = out.reshape(3, 3, 3)
+    assert np.array_equal(blocks[0], np.eye(3)) and np.array_equal(blocks[2], np.eye(3))
+    assert not blocks[1].any()
+    # the springs oracle's fused MD + K is this expression of its own parts
+    L = meshgen.springs_lattice(4, 4, 4, 0.1, 0.01, seed=2)
+    n, ep = L["n"], L["ep"]
+    rp, ci = oracle.pattern(n, ep, 2)
+    g = meshgen.rng(3)
+    v, m = g.uniform(-0.1, 0.1, n * 3), g.uniform(0.5, 2.0, n)
+    k, l0 = np.full(len(L["l0"]), 1e4), L["l0"] * 1.05
+    fixed, grav = np.zeros(n, np.uint8), np.array([0, 0, -9.81])
+    fused, _ = oracle.springs_assemble(0, L["x"], v, m, fixed, ep, k, l0, 1e-3, 0.5, grav, rp, ci)
+    K, _ = oracle.springs_assemble(0, L["x"], v, np.zeros(n), fixed, ep, k, l0, 1e-3, 0.0, grav,
+                                   rp, ci)
+    MD = ((m + 1e-3 * 0.5)[:, None, None] * np.eye(3)[None]).reshape(-1)
+    assert np.array_equal(oracle.add_diag(n, 3, rp, ci, K, diag=MD), fused)
