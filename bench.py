@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--lanes", type=int, default=0, help="sg_bspmv lanes (g) for --spmv-only")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--f64", action="store_true", help="FP64 matrix for --spmv-only")
+    ap.add_argument("--sym", action="store_true",
+                    help="symmetric storage for the iteration's SpMV (and for --spmv-only)")
     ap.add_argument("--cloth", action="store_true",
                     help="batched cloth: 256 uneven sheets in one graph launch vs one at a time")
     ap.add_argument("--sheets", type=int, default=256)
@@ -443,15 +445,25 @@ def run_spmv_only(args):
     y = torch.empty_like(x)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, x, y, g=args.lanes)
+    s = x.element_size()
+    if args.sym:  # the symmetric-storage kernel (k_sbsr3_wtma)
+        from simit_gb300.runtime import SymBsr
+        sb = SymBsr(ctx, m.n, m.pattern.rowptr, m.pattern.colidx, m.nnzb)
+        sb.fill(p.A)
+        spmv = lambda: sb.spmv(x, y)  # noqa: E731
+        nl = (m.nnzb - m.n) // 2
+        nbytes = (m.nnzb - nl) * (9 * s + 4) + nl * 8 + 2 * (m.n + 1) * 4 + m.n * 3 * 2 * s
+    else:
+        spmv = lambda: bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, x, y,  # noqa
+                             g=args.lanes)
+        nbytes = m.nnzb * (9 * s + 4) + (m.n + 1) * 4 + m.n * 3 * 2 * s
+    spmv()
     e0.record(ctx.torch_stream)
     for _ in range(args.reps):
-        bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, x, y, g=args.lanes)
+        spmv()
     e1.record(ctx.torch_stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / args.reps
-    s = x.element_size()
-    nbytes = m.nnzb * (9 * s + 4) + (m.n + 1) * 4 + m.n * 3 * 2 * s
     # the matrix expression MD + K (sg_bsr_add_diag) on the same pattern:
     # K read and the result written once, the row's column indices and D once
     D = torch.rand(m.n * 9, dtype=dt, device=ctx.device)
@@ -465,8 +477,8 @@ def run_spmv_only(args):
     ctx.sync()
     ad_ms = e0.elapsed_time(e1) / args.reps
     ad_bytes = m.nnzb * (2 * 9 * s + 4) + (m.n + 1) * 4 + m.n * 9 * s
-    print(json.dumps({"size": args.size, "lanes": args.lanes, "dtype": str(dt), "nnzb": m.nnzb,
-                      "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes,
+    print(json.dumps({"size": args.size, "lanes": args.lanes, "sym": args.sym, "dtype": str(dt),
+                      "nnzb": m.nnzb, "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes,
                       "add_diag_ms": ad_ms, "add_diag_GBps": ad_bytes / ad_ms / 1e6,
                       "add_diag_bytes": ad_bytes}), flush=True)
 
@@ -605,9 +617,10 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def spmv_traffic(size):
+def spmv_traffic(size, sym=False):
     """DRAM bytes per SpMV launch from a committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "spmv_bsr3_wtma_f32_traffic.json")
+    p = os.path.join(ROOT, "profiles", "spmv_sbsr3_wtma_f32_traffic.json" if sym
+                     else "spmv_bsr3_wtma_f32_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
@@ -630,7 +643,9 @@ def run_ours(args, rank, world, local):
     if not args.no_reorder:
         host = problems.reorder_hetero(host)
     prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
-                                     precond=_lib.PRECOND_BLOCK_JACOBI)
+                                     precond=_lib.PRECOND_BLOCK_JACOBI,
+                                     storage=_lib.STORAGE_SYMMETRIC if args.sym
+                                     else _lib.STORAGE_FULL)
     st = ctx.torch_stream
 
     def barrier():
@@ -680,22 +695,46 @@ def run_ours(args, rank, world, local):
     h2d = (x_h.numel() + mu_h.numel() + lam_h.numel()) * 4
     d2h = u_h.numel() * 8
 
-    # --- roofline of the dominant kernel: the TMA-staged FP32 SpMV --------
+    # --- roofline of the dominant kernel: the iteration's FP32 SpMV --------
+    # (the solver's K1 without its p.q epilogue, on the same matrix and
+    # stream); the full-storage kernel is timed beside it for reference
     m = prob.mesh
     p = torch.rand(n3, dtype=torch.float32, device=ctx.device)
     q = torch.empty_like(p)
-    for _ in range(3):
-        bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, p, q, g=0)
+    sym = prob.opts.storage == _lib.STORAGE_SYMMETRIC
+    full_fn = lambda: bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, p, q, g=0)  # noqa: E731
+    full_bytes = m.nnzb * (9 * 4 + 4) + (m.n + 1) * 4 + m.n * 3 * (4 + 4)
+    if sym:
+        from simit_gb300.runtime import SymBsr
+        sb = SymBsr(ctx, m.n, m.pattern.rowptr, m.pattern.colidx, m.nnzb)
+        sb.fill(prob.A)
+        nl = (m.nnzb - m.n) // 2
+        nu = m.nnzb - nl
+        fn = lambda: sb.spmv(p, q)  # noqa: E731
+        spmv_bytes = nu * (9 * 4 + 4) + nl * 8 + 2 * (m.n + 1) * 4 + m.n * 3 * (4 + 4)
+        kernel = ("k_sbsr3_wtma (FP32 3x3 blocked SpMV on symmetric storage: upper blocks "
+                  "and the lower-block index streamed by per-warp TMA pipelines)")
+    else:
+        fn, spmv_bytes = full_fn, full_bytes
+        kernel = "k_bsr3_wtma (FP32 3x3 blocked SpMV, per-warp TMA pipeline)"
     reps = 50
-    s0 = torch.cuda.Event(enable_timing=True)
-    s1 = torch.cuda.Event(enable_timing=True)
-    s0.record(st)
-    for _ in range(reps):
-        bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, p, q, g=0)
-    s1.record(st)
-    s1.synchronize()
-    spmv_ms = s0.elapsed_time(s1) / reps
-    spmv_bytes = m.nnzb * (9 * 4 + 4) + (m.n + 1) * 4 + m.n * 3 * (4 + 4)
+    spmv_ms = full_ms = None
+    for which in ("kernel", "full"):
+        f = fn if which == "kernel" else full_fn
+        for _ in range(3):
+            f()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(st)
+        for _ in range(reps):
+            f()
+        s1.record(st)
+        s1.synchronize()
+        if which == "kernel":
+            spmv_ms = s0.elapsed_time(s1) / reps
+        else:
+            full_ms = s0.elapsed_time(s1) / reps
+    ctx.sync()
     achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
 
@@ -766,7 +805,8 @@ def run_ours(args, rank, world, local):
         "config": {"workload": workload_name(args.size, not args.no_reorder), "dofs": dofs,
                    "nnzb": m.nnzb,
                    "method": "FP32 assembly + mixed-precision block-Jacobi PCG (FP32 matrix/"
-                             "vectors, FP64 dots, FP64 reliable updates), verified FP64 residual",
+                             "vectors, FP64 dots, FP64 reliable updates), verified FP64 residual"
+                             + ("; the iteration's SpMV on symmetric storage" if sym else ""),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (FP32 matrix 1.0 GB), no flush"},
         "iters": iters, "relres_max": relres,
@@ -774,10 +814,12 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": spmv_traffic(args.size),
-                     "kernel": "k_bsr3_wtma (FP32 3x3 blocked SpMV, per-warp TMA pipeline)",
-                     "peak_kind": peak_kind,
-                     "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes},
+                     "frac": achieved / peak, "traffic": spmv_traffic(args.size, sym),
+                     "kernel": kernel, "peak_kind": peak_kind,
+                     "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes,
+                     "full_storage_spmv": {"ms_per_launch": full_ms,
+                                           "algorithmic_bytes": full_bytes,
+                                           "GBps": full_bytes / (full_ms / 1e3) / 1e9}},
         "cpu_baseline": {"value": cpu["value"], "unit": "DOF/s", "cores": 1, "kind": "port",
                          "sample": "%d^3 instance (%d DOF) of the same family: oracle pattern + "
                                    "FP64 assembly + FP64 Jacobi-PCG to 1e-8 (%d iterations), "

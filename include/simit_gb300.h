@@ -202,6 +202,23 @@ int sg_bspmv(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
  * `verts.x = h * x + verts.x` of femTet.sim); vec_dtype for x and y. */
 int sg_axpy(sg_ctx *ctx, int64_t len, int vec_dtype, double alpha, const void *x, void *y);
 
+/* Symmetric storage of a 3x3-blocked FP32 matrix (the layout the solver's
+ * SG_STORAGE_SYMMETRIC option iterates on).  create: from a full pattern that
+ * is symmetric, sorted and has every diagonal block, builds the upper-half
+ * CSR and, per row, the index {column, upper slot} of its blocks below the
+ * diagonal (synchronises; SG_ERR_DEVICE for a missing diagonal block or an
+ * asymmetric pattern).  fill: copies the upper blocks out of full values
+ * [nnzb*9] (the lower ones are not read).  spmv: y = A x with A the
+ * symmetric matrix whose upper half was filled; FP32 x, y [n*3].  The
+ * reference has no symmetric storage: it always reads full blocked CSR
+ * (src/lower/index_expressions/lower_indexexprs.cpp:630-665). */
+typedef struct sg_symbsr sg_symbsr;
+int sg_symbsr_create(sg_ctx *ctx, int32_t n, const uint32_t *rowptr, const uint32_t *colidx,
+                     int64_t nnzb, sg_symbsr **out);
+int sg_symbsr_fill(sg_symbsr *s, const float *vals);
+int sg_symbsr_spmv(sg_symbsr *s, const float *x, float *y);
+int sg_symbsr_destroy(sg_symbsr *s);
+
 /* System-matrix expression out = D + scale*K on K's pattern (replaces the
  * lowered `MDK = MD + K` of apps/springs/isprings.sim:74, with the storage
  * rules of src/storage.cpp:358-360 and 416-470).  D is Diagonal storage:
@@ -272,6 +289,12 @@ typedef struct sg_matrix {
   const void *vals;
 } sg_matrix;
 
+/* Storage the iteration's SpMV reads.  SG_STORAGE_SYMMETRIC keeps the blocks
+ * on and above the diagonal plus an index of the blocks below it (see
+ * sg_symbsr_create); the matrix must be symmetric bit for bit, as the tet
+ * stiffness maps assemble it.  The true residual still uses the full matrix. */
+enum { SG_STORAGE_FULL = 0, SG_STORAGE_SYMMETRIC = 1 };
+
 typedef struct sg_solve_opts {
   int precision;             /* SG_SOLVE_F64 / SG_SOLVE_MIXED */
   int precond;               /* SG_PRECOND_* */
@@ -285,6 +308,8 @@ typedef struct sg_solve_opts {
   int32_t batch;             /* iterations per graph launch (even); 0 = 32 */
   const float *learned_params; /* SG_PRECOND_LEARNED: device FP32[sg_mpnn_nparams()] */
   int32_t learned_form;        /* SG_MPNN_RELU / SG_MPNN_LINEAR / SG_MPNN_SYM */
+  int32_t storage;             /* SG_STORAGE_FULL / SG_STORAGE_SYMMETRIC (mixed, bs 3):
+                                  the iteration's SpMV reads the upper half only */
 } sg_solve_opts;
 
 typedef struct sg_solve_result {

@@ -41,7 +41,7 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("precond", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", D), ("maxiters", I32), ("verify", I32), ("check_every", I32),
                 ("reliable_delta", D), ("lanes", I32), ("batch", I32), ("learned_params", P),
-                ("learned_form", I32)]
+                ("learned_form", I32), ("storage", I32)]
 
 
 class SolveResult(ctypes.Structure):
@@ -52,6 +52,7 @@ class SolveResult(ctypes.Structure):
 
 SOLVE_F64, SOLVE_MIXED = 0, 1
 MPNN_RELU, MPNN_LINEAR, MPNN_SYM = 0, 1, 2
+STORAGE_FULL, STORAGE_SYMMETRIC = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1, 2, 3
 STOP_NORMR2, STOP_NORMR, STOP_RELATIVE = 0, 1, 2
 STATUS = {1: "converged", 2: "maxiter", 3: "breakdown", 4: "nan"}
@@ -76,6 +77,10 @@ SIGNATURES = {
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),
     "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, _CI, P, D, D, P, P]),
+    "sg_symbsr_create": (_CI, [P, I32, P, P, I64, ctypes.POINTER(P)]),
+    "sg_symbsr_fill": (_CI, [P, P]),
+    "sg_symbsr_spmv": (_CI, [P, P, P]),
+    "sg_symbsr_destroy": (_CI, [P]),
     "sg_pattern_maxrow": (_CI, [P, I32, P, ctypes.POINTER(I32)]),
     "sg_assemble_springs": (_CI, [P, _MP, _CI, _CI, P, P, P, P, P, P, D, D, P, P, P, _CI]),
     "sg_assemble_scalar_springs": (_CI, [P, _MP, _CI, P, D, D, P, _CI]),

@@ -101,6 +101,11 @@ __device__ __forceinline__ float d_log(float x) { return logf(x); }
 __device__ __forceinline__ double d_log(double x) { return log(x); }
 __device__ __forceinline__ float d_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double d_sqrt(double x) { return sqrt(x); }
+// Separately rounded products and sums (never contracted into a multiply-add).
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 
 // ---------------------------------------------------------------------------
 // Row-owner kernel
@@ -595,14 +600,23 @@ template <typename T, bool EXACT> struct LinTetElem {
           k3[m] = (a.h * a.h) * s;
         }
       } else {
+        // Every product pairs one factor of vertex i with one of vertex j and
+        // no operation is contracted, so the (j, i) block is bitwise the
+        // transpose of the (i, j) block and the assembled matrix is exactly
+        // symmetric (the symmetric-storage SpMV reads only its upper half).
         T gi[3], gj[3];
         dN(Bt, i, gi);
         dN(Bt, j, gj);
-        const T gij = gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2];
-        const T hw = (a.h * a.h) * W;
+        const T gij =
+            add_rn(add_rn(mul_rn(gi[0], gj[0]), mul_rn(gi[1], gj[1])), mul_rn(gi[2], gj[2]));
+        const T hw = mul_rn(mul_rn(a.h, a.h), W);
+        const T ug = mul_rn(u, gij);
 #pragma unroll
-        for (int m = 0; m < 3; ++m)
-          k3[m] = hw * (lm * gi[l] * gj[m] + u * gi[m] * gj[l] + (l == m ? u * gij : T(0)));
+        for (int m = 0; m < 3; ++m) {
+          T t = add_rn(mul_rn(lm, mul_rn(gi[l], gj[m])), mul_rn(u, mul_rn(gi[m], gj[l])));
+          if (l == m) t = add_rn(t, ug);
+          k3[m] = mul_rn(hw, t);
+        }
       }
     }
     int nt = 0;

@@ -107,6 +107,8 @@ static int alloc_dev(Solver *S, void **p, size_t bytes) {
 template <typename MT, typename VT>
 static int launch_k1(Solver *S, cudaStream_t st) {
   const sg_matrix &A = S->A;
+  if (S->sym)
+    return sym_launch(S->sym, st, S->ctl, true, (const float *)S->p, (float *)S->q, S->part1);
   if (S->tma) {
     const int vdt = sizeof(MT) == 8 ? SG_F64 : SG_F32, xdt = sizeof(VT) == 8 ? SG_F64 : SG_F32;
     return bsr3_tma_launch(S->c, st, S->ctl, A.bs, vdt, xdt, S->tma_var, 1, A.n, A.rowptr,
@@ -483,6 +485,8 @@ int sg_solver_create(sg_ctx *h, const sg_matrix *A, const sg_solve_opts *o, sg_s
   SG_REQUIRE(o->precond != SG_PRECOND_BLOCK_JACOBI || A->bs == 3,
              "sg_solver_create: block Jacobi needs bs = 3");
   SG_REQUIRE(o->maxiters >= 0, "sg_solver_create: maxiters");
+  SG_REQUIRE(o->storage == SG_STORAGE_FULL || o->storage == SG_STORAGE_SYMMETRIC,
+             "sg_solver_create: storage %d", o->storage);
   Solver *S = new Solver();
   int rc = o->precond == SG_PRECOND_LEARNED
                ? learned_solver_init(c, A, o, o->learned_params, S)
@@ -546,6 +550,7 @@ int refresh_matrix(Solver *S) {
     SG_CHECK_LAUNCH();
     S->bulk_vals = S->vals32;
   }
+  if (S->sym) SG_TRY(sym_fill(S->sym, c->stream, (const float *)S->bulk_vals));
   if (S->prec == PK_JACOBI || S->prec == PK_BLOCK3) {
     const int blk = S->prec == PK_BLOCK3;
     const int g = grid_for(c, A->n, 256, 8);
@@ -613,6 +618,14 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
       S->P1 = grid;
     }
   }
+  if (o->storage == SG_STORAGE_SYMMETRIC) {
+    SG_REQUIRE(A->bs == 3 && S->kind == KIND_MIXED,
+               "sg_solver_create: symmetric storage needs bs = 3 and SG_SOLVE_MIXED");
+    S->sym = new SymBsr();
+    SG_TRY(sym_create(c, A->n, A->rowptr, A->colidx, A->nnzb, S->sym));
+    S->tma = 1;  // K1 leaves the finished p.q in ctl, as the TMA kernels do
+    S->P1 = S->sym->grid[1];
+  }
   const int np = S->P1 > S->P2 ? S->P1 : S->P2;
   SG_TRY(alloc_dev(S, (void **)&S->ctl, sizeof(SolveCtl)));
   SG_CHECK_CUDA(cudaMallocHost((void **)&S->hctl, sizeof(SolveCtl)));
@@ -661,6 +674,10 @@ void solver_free(Solver *S) {
   for (void *p : S->allocs) cudaFree(p);
   if (S->hctl) cudaFreeHost(S->hctl);
   if (S->ext_free) S->ext_free(S);
+  if (S->sym) {
+    sym_free(S->sym);
+    delete S->sym;
+  }
   if (S->c) ctx_release(S->c);
   delete S;
 }

@@ -6,6 +6,8 @@
 #include "sg_solver_kernels.cuh"
 #include "sg_spmv_api.h"
 
+#include "sg_sym.h"
+
 namespace sg {
 
 struct Solver {
@@ -40,6 +42,7 @@ struct Solver {
   int (*ext_prec_apply)(Solver *, cudaStream_t) = nullptr;
   void (*ext_free)(Solver *) = nullptr;
   void *ext = nullptr;
+  SymBsr *sym = nullptr;  // SG_STORAGE_SYMMETRIC: K1 reads the upper half
 };
 
 int default_lanes(int32_t n, int64_t nnzb, int32_t bs);

@@ -65,11 +65,12 @@ class HeteroElasticity:
 
     dtype float32: FP32 assembly and the mixed-precision solver
     (FP32 matrix/SpMV, FP64 dots and reliable updates); float64: FP64
-    assembly and FP64 CG.
+    assembly and FP64 CG.  storage = STORAGE_SYMMETRIC iterates on the
+    matrix's upper half (the FP32 linear-tet stiffness is exactly symmetric).
     """
 
     def __init__(self, ctx, host, dtype=torch.float32, precond=_lib.PRECOND_BLOCK_JACOBI,
-                 precision=None, tol=1e-8, maxiters=200000, lanes=0):
+                 precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None):
         self.ctx, self.host, self.dtype = ctx, host, dtype
         self.mesh = Mesh(ctx, host["n"], host["tets"], 4)
         d = ctx.device
@@ -85,8 +86,11 @@ class HeteroElasticity:
         self.assemble()
         if precision is None:
             precision = _lib.SOLVE_MIXED if dtype == torch.float32 else _lib.SOLVE_F64
+        if storage is None:
+            storage = _lib.STORAGE_FULL
         self.opts = solve_opts(precision=precision, precond=precond, stop=_lib.STOP_RELATIVE,
-                               tol=tol, maxiters=maxiters, verify=1, lanes=lanes)
+                               tol=tol, maxiters=maxiters, verify=1, lanes=lanes,
+                               storage=storage)
         self.solver = Solver(ctx, self.mesh.n, 3, self.mesh.pattern.rowptr,
                              self.mesh.pattern.colidx, self.A, self.mesh.nnzb, self.opts)
 

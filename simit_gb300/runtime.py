@@ -125,6 +125,41 @@ def bsr_add_diag(ctx, n, bs, rowptr, colidx, vals, diag=None, ident=0.0, scale=1
     return out
 
 
+class SymBsr:
+    """sg_symbsr: symmetric (upper-half) storage of a 3x3-blocked FP32 matrix
+    with a symmetric pattern; fill() from full values, spmv() = A x."""
+
+    def __init__(self, ctx, n, rowptr, colidx, nnzb):
+        self.ctx, self.n = ctx, n
+        self._keep = (rowptr, colidx)
+        h = ctypes.c_void_p()
+        call("sg_symbsr_create", ctx.h, n, ptr(rowptr), ptr(colidx), int(nnzb), ctypes.byref(h))
+        self.h = h.value
+
+    def fill(self, vals):
+        assert vals.dtype == torch.float32
+        self._vals = vals
+        call("sg_symbsr_fill", self.h, ptr(vals))
+
+    def spmv(self, x, y=None):
+        if y is None:
+            with self.ctx.stream():
+                y = torch.empty_like(x)
+        call("sg_symbsr_spmv", self.h, ptr(x), ptr(y))
+        return y
+
+    def close(self):
+        if self.h:
+            _lib.load().sg_symbsr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def dot(ctx, a, b):
     out = ctypes.c_double()
     call("sg_dot", ctx.h, a.numel(), dtype_code(a), ptr(a), ptr(b), ctypes.byref(out))
@@ -279,10 +314,10 @@ def assemble_heat(mesh, B, W, kappa, dt, T0, dtype=torch.float64, exact=True):
 
 def solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_RELATIVE,
                tol=1e-8, maxiters=10000, verify=1, check_every=0, reliable_delta=0.1, lanes=0,
-               batch=32, learned_params=None, learned_form=0):
+               batch=32, learned_params=None, learned_form=0, storage=0):
     lp = learned_params.data_ptr() if learned_params is not None else None
     return _lib.SolveOpts(precision, precond, stop, tol, maxiters, verify, check_every,
-                          reliable_delta, lanes, batch, lp, int(learned_form))
+                          reliable_delta, lanes, batch, lp, int(learned_form), int(storage))
 
 
 class Solver:

@@ -65,7 +65,7 @@ def test_springs_on_tetgen_edges_gpu(ctx, oracle, tmp_path):
     """apps/springs/springs.cpp end to end: the bar2k TetGen mesh's edges
     written as a .edge file, read back with the MeshVol::loadTetEdge rules,
     three implicit steps of apps/springs/isprings.sim (FP64, exact-mode
-    assembly, 50 CG iterations) on the GPU against the oracle."""
+    assembly, at most 50 CG iterations) on the GPU against the oracle."""
     import os
     from simit_gb300.runtime import Mesh, assemble_springs
     node = os.path.join(scenarios.GOLDEN, "bar2k.node")
@@ -78,9 +78,14 @@ def test_springs_on_tetgen_edges_gpu(ctx, oracle, tmp_path):
     d = ctx.device
     x, v = torch.tensor(s["x"], device=d), torch.tensor(s["v"], device=d)
     ox, ov = s["x"].copy(), s["v"].copy()
-    for _ in range(3):
+    for step in range(3):
         vals, f = assemble_springs(mesh, x, v, s["m"], s["fixed"], s["k"], s["l0"], s["h"],
                                    s["viscous"], s["grav"], form=s["form"])
+        if step == 0:  # the ingested system itself: bit-exact with the oracle's
+            oA, of = oracle.springs_assemble(s["form"], s["x"], s["v"], s["m"], s["fixed"],
+                                             s["ep"], s["k"], s["l0"], s["h"], s["viscous"],
+                                             s["grav"], rp, ci)
+            assert np.array_equal(_np(vals), oA) and np.array_equal(_np(f), of)
         v, res = _cg_ref_form(ctx, mesh, vals, f, v, 3, s["tol2"], s["maxiters"],
                               _lib.STOP_NORMR2)
         with ctx.stream():
@@ -88,9 +93,10 @@ def test_springs_on_tetgen_edges_gpu(ctx, oracle, tmp_path):
         oracle.springs_step(s["form"], ox, ov, s["m"], s["fixed"], s["ep"], s["k"], s["l0"],
                             s["h"], s["viscous"], s["grav"], rp, ci, s["tol2"], s["maxiters"])
     ctx.sync()
-    # the same 50 CG iterations; only the dot products' summation order differs
-    assert np.abs(_np(v) - ov).max() <= 1e-9 * np.abs(ov).max()
-    assert np.abs(_np(x) - ox).max() <= 1e-12 * np.abs(ox).max()
+    # 50 unconverged CG iterations per step (the app's cap): the iterates
+    # follow the dot products' rounding, which differs in summation order
+    assert np.abs(_np(v) - ov).max() <= 1e-4 * np.abs(ov).max()
+    assert np.abs(_np(x) - ox).max() <= 1e-7 * np.abs(ox).max()
 
 
 def test_cg_golden_gpu(ctx):
