@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--f64", action="store_true", help="FP64 matrix for --spmv-only")
     ap.add_argument("--sym", action="store_true",
                     help="symmetric storage for the iteration's SpMV (and for --spmv-only)")
+    ap.add_argument("--stages", type=int, default=0,
+                    help="--spmv-only --sym: bulk-copy stages per warp (2..4, 0 = default)")
     ap.add_argument("--cloth", action="store_true",
                     help="batched cloth: 256 uneven sheets in one graph launch vs one at a time")
     ap.add_argument("--sheets", type=int, default=256)
@@ -448,7 +450,7 @@ def run_spmv_only(args):
     s = x.element_size()
     if args.sym:  # the symmetric-storage kernel (k_sbsr3_wtma)
         from simit_gb300.runtime import SymBsr
-        sb = SymBsr(ctx, m.n, m.pattern.rowptr, m.pattern.colidx, m.nnzb)
+        sb = SymBsr(ctx, m.n, m.pattern.rowptr, m.pattern.colidx, m.nnzb, stages=args.stages)
         sb.fill(p.A)
         spmv = lambda: sb.spmv(x, y)  # noqa: E731
         nl = (m.nnzb - m.n) // 2
@@ -465,7 +467,7 @@ def run_spmv_only(args):
     e1.synchronize()
     ms = e0.elapsed_time(e1) / args.reps
     # the matrix expression MD + K (sg_bsr_add_diag) on the same pattern:
-    # K read and the result written once, the row's column indices and D once
+    # K read and the result written once, D and the row pointers once
     D = torch.rand(m.n * 9, dtype=dt, device=ctx.device)
     out = torch.empty_like(p.A)
     bsr_add_diag(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, diag=D, out=out)
@@ -476,8 +478,9 @@ def run_spmv_only(args):
     e1.synchronize()
     ctx.sync()
     ad_ms = e0.elapsed_time(e1) / args.reps
-    ad_bytes = m.nnzb * (2 * 9 * s + 4) + (m.n + 1) * 4 + m.n * 9 * s
-    print(json.dumps({"size": args.size, "lanes": args.lanes, "sym": args.sym, "dtype": str(dt),
+    ad_bytes = m.nnzb * 2 * 9 * s + (m.n + 1) * 4 + m.n * 9 * s
+    print(json.dumps({"size": args.size, "lanes": args.lanes, "sym": args.sym,
+                      "stages": args.stages, "dtype": str(dt),
                       "nnzb": m.nnzb, "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes,
                       "add_diag_ms": ad_ms, "add_diag_GBps": ad_bytes / ad_ms / 1e6,
                       "add_diag_bytes": ad_bytes}), flush=True)

@@ -214,7 +214,8 @@ int sg_axpy(sg_ctx *ctx, int64_t len, int vec_dtype, double alpha, const void *x
  * (src/lower/index_expressions/lower_indexexprs.cpp:630-665). */
 typedef struct sg_symbsr sg_symbsr;
 int sg_symbsr_create(sg_ctx *ctx, int32_t n, const uint32_t *rowptr, const uint32_t *colidx,
-                     int64_t nnzb, sg_symbsr **out);
+                     int64_t nnzb, int32_t stages /* bulk-copy stages 2..4, 0 = default */,
+                     sg_symbsr **out);
 int sg_symbsr_fill(sg_symbsr *s, const float *vals);
 int sg_symbsr_spmv(sg_symbsr *s, const float *x, float *y);
 int sg_symbsr_destroy(sg_symbsr *s);
@@ -228,7 +229,7 @@ int sg_symbsr_destroy(sg_symbsr *s);
  * rounded separately in dtype.  out may alias vals.  Asynchronous; a row
  * without its diagonal block, when D is given, fails the next sg_ctx_sync. */
 int sg_bsr_add_diag(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
-                    const uint32_t *colidx, int dtype, const void *diag,
+                    const uint32_t *colidx, int64_t nnzb, int dtype, const void *diag,
                     double ident, double scale, const void *vals, void *out);
 
 /* Dot product of two blocked vectors with an FP64 deterministic two-level

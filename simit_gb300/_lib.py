@@ -76,8 +76,8 @@ SIGNATURES = {
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),
-    "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, _CI, P, D, D, P, P]),
-    "sg_symbsr_create": (_CI, [P, I32, P, P, I64, ctypes.POINTER(P)]),
+    "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, I64, _CI, P, D, D, P, P]),
+    "sg_symbsr_create": (_CI, [P, I32, P, P, I64, I32, ctypes.POINTER(P)]),
     "sg_symbsr_fill": (_CI, [P, P]),
     "sg_symbsr_spmv": (_CI, [P, P, P]),
     "sg_symbsr_destroy": (_CI, [P]),

@@ -622,7 +622,7 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
     SG_REQUIRE(A->bs == 3 && S->kind == KIND_MIXED,
                "sg_solver_create: symmetric storage needs bs = 3 and SG_SOLVE_MIXED");
     S->sym = new SymBsr();
-    SG_TRY(sym_create(c, A->n, A->rowptr, A->colidx, A->nnzb, S->sym));
+    SG_TRY(sym_create(c, A->n, A->rowptr, A->colidx, A->nnzb, 0, S->sym));
     S->tma = 1;  // K1 leaves the finished p.q in ctl, as the TMA kernels do
     S->P1 = S->sym->grid[1];
   }

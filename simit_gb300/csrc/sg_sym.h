@@ -27,15 +27,17 @@ struct SymBsr {
   uint2 *lidx = nullptr;                     // lower block: {column, upper slot}
   float *uvals = nullptr;                    // nu blocks of 9 values, row-major
   int capu = 0, capl = 0;                    // blocks of the largest warp tile
+  int nst = 3;                               // bulk-copy pipeline stages per warp
   int grid[2] = {0, 0};                      // [dot]: persistent grid
   size_t smem[2] = {0, 0};
   std::vector<void *> allocs;
 };
 
 // Builds the upper pattern and lower index from a full symmetric pattern
-// (rows sorted, every row with its diagonal block).  Synchronises.
+// (rows sorted, every row with its diagonal block); stages 0 = default.
+// Synchronises.
 int sym_create(Ctx *c, int32_t n, const uint32_t *rowptr, const uint32_t *colidx, int64_t nnzb,
-               SymBsr *S);
+               int stages, SymBsr *S);
 // Copies the upper blocks out of full FP32 values [nnzb*9].
 int sym_fill(SymBsr *S, cudaStream_t st, const float *vals);
 // y = A x; with dot, also the CG K1 epilogue (p.q into ctl->pq_tot via part).

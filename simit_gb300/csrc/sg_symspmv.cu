@@ -28,15 +28,15 @@ namespace {
 
 constexpr int SYM_G = 4;                  // lanes per block row
 constexpr int SYM_RW = 32 / SYM_G;        // rows per warp tile
-constexpr int SYM_NST = 2;                // pipeline stages per warp
+constexpr int SYM_NST_DEFAULT = 3;        // pipeline stages per warp (2..4)
 
 inline __host__ __device__ size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 inline __host__ __device__ size_t sym_vbytes(int capu) { return align16((size_t)capu * 36 + 32); }
 inline __host__ __device__ size_t sym_cbytes(int capu) { return align16((size_t)capu * 4 + 32); }
 inline __host__ __device__ size_t sym_lbytes(int capl) { return align16((size_t)capl * 8 + 32); }
-inline size_t sym_smem_bytes(int capu, int capl) {
-  return align16((size_t)WTMA_WARPS * SYM_NST * 8) +
-         (size_t)WTMA_WARPS * SYM_NST * (sym_vbytes(capu) + sym_cbytes(capu) + sym_lbytes(capl));
+inline size_t sym_smem_bytes(int capu, int capl, int nst) {
+  return align16((size_t)WTMA_WARPS * nst * 8) +
+         (size_t)WTMA_WARPS * nst * (sym_vbytes(capu) + sym_cbytes(capu) + sym_lbytes(capl));
 }
 
 // First slot of row v (in [s, e)) whose column is >= key.
@@ -135,7 +135,8 @@ __device__ __forceinline__ void sym_row(int64_t r, int gl, unsigned mask,
                                         const float *__restrict__ vb,
                                         const uint32_t *__restrict__ cb,
                                         const uint2 *__restrict__ lb, size_t voff, size_t coff,
-                                        size_t loff, const float *__restrict__ uv,
+                                        size_t loff, uint32_t su0, uint32_t su1,
+                                        const float *__restrict__ uv,
                                         const float *__restrict__ x, float *__restrict__ y,
                                         DotAcc<float> &acc) {
   constexpr int G = SYM_G;
@@ -182,9 +183,11 @@ __device__ __forceinline__ void sym_row(int64_t r, int gl, unsigned mask,
       const uint32_t q = q0 + k * G;
       if (q < e) {
         const uint2 ent = lb[q - loff];
-        const float *v = uv + (size_t)ent.y * 9;
+        // the mirror block is an upper block of this tile: already staged
+        const bool in_tile = ent.y >= su0 && ent.y < su1;
+        const float *v = in_tile ? vb + ((size_t)ent.y * 9 - voff) : uv + (size_t)ent.y * 9;
 #pragma unroll
-        for (int w = 0; w < 9; ++w) lv[k][w] = ldg(v + w);
+        for (int w = 0; w < 9; ++w) lv[k][w] = in_tile ? v[w] : ldg(v + w);
         xg[k][0] = ldg(x + (size_t)ent.x * 3 + 0);
         xg[k][1] = ldg(x + (size_t)ent.x * 3 + 1);
         xg[k][2] = ldg(x + (size_t)ent.x * 3 + 2);
@@ -219,8 +222,8 @@ __device__ __forceinline__ void sym_row(int64_t r, int gl, unsigned mask,
   }
 }
 
-template <bool DOT>
-__global__ void __launch_bounds__(WTMA_WARPS * 32, 4)
+template <bool DOT, int NST>
+__global__ void __launch_bounds__(WTMA_WARPS * 32, 6)
     k_sbsr3_wtma(const SolveCtl *__restrict__ ctl, int32_t n, const uint32_t *__restrict__ urp,
                  const uint32_t *__restrict__ ucol, const float *__restrict__ uv,
                  const uint32_t *__restrict__ lrp, const uint2 *__restrict__ lidx,
@@ -228,7 +231,8 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32, 4)
                  int capu, int capl, int *err) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ double shred[33];
-  constexpr int NST = SYM_NST, RW = SYM_RW, G = SYM_G;
+  constexpr int RW = SYM_RW, G = SYM_G;
+  static_assert(NST >= 2 && NST <= 4, "stages");
   if (ctl && ctl->status != ST_RUNNING) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t vb = sym_vbytes(capu), cbt = sym_cbytes(capu), lbt = sym_lbytes(capl);
@@ -245,15 +249,10 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32, 4)
     mbar_fence_init();
   }
   __syncwarp();
-  // Each warp walks a contiguous run of tiles, so the rows whose upper
-  // blocks a row's lower blocks mirror (mostly a few rows back) were streamed
-  // by this warp shortly before and are still in L2.
   const int64_t ntiles = ((int64_t)n + RW - 1) / RW;
   const int64_t gw = (int64_t)blockIdx.x * WTMA_WARPS + warp;
   const int64_t nw = (int64_t)gridDim.x * WTMA_WARPS;
-  const int64_t chunk = (ntiles + nw - 1) / nw;
-  const int64_t t_begin = gw * chunk;
-  const int64_t my = t_begin < ntiles ? min(chunk, ntiles - t_begin) : 0;
+  const int64_t my = gw < ntiles ? (ntiles - 1 - gw) / nw + 1 : 0;
   auto fits = [&](uint32_t u0, uint32_t u1, uint32_t l0, uint32_t l1) {
     return u1 - u0 <= (uint32_t)capu && l1 - l0 <= (uint32_t)capl;
   };
@@ -280,15 +279,15 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32, 4)
                &bar[b]);
   };
   if (lane == 0)
-    for (int k = 0; k < NST - 1 && k < my; ++k) issue(t_begin + k, k);
+    for (int k = 0; k < NST - 1 && k < my; ++k) issue(gw + k * nw, k);
   const int gl = lane & (G - 1);
   const unsigned mask = group_mask<G>();
   DotAcc<float> acc;
   for (int64_t k = 0; k < my; ++k) {
     const int b = (int)(k % NST);
-    const int64_t tile = t_begin + k;
+    const int64_t tile = gw + k * nw;
     const int64_t kn = k + NST - 1;
-    if (lane == 0 && kn < my) issue(t_begin + kn, (int)(kn % NST));
+    if (lane == 0 && kn < my) issue(gw + kn * nw, (int)(kn % NST));
     const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[b], (uint32_t)((k / NST) & 1)));
     if (!ok) {
       if (lane == 0) {
@@ -300,10 +299,13 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32, 4)
     }
     const int64_t r0 = tile * RW, r1 = min((int64_t)n, r0 + RW);
     const uint32_t u0 = urp[r0], u1 = urp[r1], l0 = lrp[r0], l1 = lrp[r1];
+    // capu / capl are the largest tile's counts, so every tile is staged;
+    // a tile that is not (a corrupted structure) is skipped and reported
     const bool staged = fits(u0, u1, l0, l1);
-    const size_t vs = staged ? ((size_t)u0 * 36) & ~size_t(15) : 0;
-    const size_t cs = staged ? ((size_t)u0 * 4) & ~size_t(15) : 0;
-    const size_t ls = staged ? ((size_t)l0 * 8) & ~size_t(15) : 0;
+    if (!staged && lane == 0) atomicCAS(err, 0, 4 /* DEV_ROW_OVERFLOW */);
+    const size_t vs = ((size_t)u0 * 36) & ~size_t(15);
+    const size_t cs = ((size_t)u0 * 4) & ~size_t(15);
+    const size_t ls = ((size_t)l0 * 8) & ~size_t(15);
     if (staged) {  // the unaligned tails (< 16 bytes each)
       const size_t ve = ((size_t)u1 * 36) & ~size_t(15), ce = ((size_t)u1 * 4) & ~size_t(15);
       const size_t le = ((size_t)l1 * 8) & ~size_t(15);
@@ -318,13 +320,9 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32, 4)
     }
     __syncwarp();
     const int64_t r = r0 + lane / G;
-    if (r < n) {
-      if (staged)
-        sym_row<DOT>(r, gl, mask, urp, lrp, vbuf(b), cbuf(b), lbuf(b), vs / 4, cs / 4, ls / 8, uv,
-                     x, y, acc);
-      else
-        sym_row<DOT>(r, gl, mask, urp, lrp, uv, ucol, lidx, 0, 0, 0, uv, x, y, acc);
-    }
+    if (r < n && staged)
+      sym_row<DOT>(r, gl, mask, urp, lrp, vbuf(b), cbuf(b), lbuf(b), vs / 4, cs / 4, ls / 8, u0,
+                   u1, uv, x, y, acc);
     __syncwarp();
   }
   if (DOT) {  // CG K1: the last CTA leaves the p.q total in ctl->pq_tot
@@ -334,10 +332,10 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32, 4)
   }
 }
 
-template <bool DOT> int sym_config(Ctx *c, SymBsr *S) {
-  const size_t sh = sym_smem_bytes(S->capu, S->capl);
+template <bool DOT, int NST> int sym_config_t(Ctx *c, SymBsr *S) {
+  const size_t sh = sym_smem_bytes(S->capu, S->capl, NST);
   if (sh > 200 * 1024) return SG_ERR_UNSUPPORTED;
-  auto kern = k_sbsr3_wtma<DOT>;
+  auto kern = k_sbsr3_wtma<DOT, NST>;
   SG_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
   int per_sm = 0;
   SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WTMA_WARPS * 32, sh));
@@ -352,6 +350,23 @@ template <bool DOT> int sym_config(Ctx *c, SymBsr *S) {
   return SG_OK;
 }
 
+template <bool DOT> int sym_config(Ctx *c, SymBsr *S) {
+  switch (S->nst) {
+    case 2: return sym_config_t<DOT, 2>(c, S);
+    case 3: return sym_config_t<DOT, 3>(c, S);
+    case 4: return sym_config_t<DOT, 4>(c, S);
+    default: return SG_ERR_UNSUPPORTED;
+  }
+}
+
+template <bool DOT, int NST>
+void sym_launch_t(SymBsr *S, cudaStream_t st, const SolveCtl *ctl, const float *x, float *y,
+                  double *part) {
+  k_sbsr3_wtma<DOT, NST><<<S->grid[DOT], WTMA_WARPS * 32, S->smem[DOT], st>>>(
+      ctl, S->n, S->urowptr, S->ucol, S->uvals, S->lrowptr, S->lidx, x, y, part, S->capu,
+      S->capl, S->c->d_err);
+}
+
 int alloc(SymBsr *S, void **p, size_t bytes) {
   SG_CHECK_CUDA(cudaMalloc(p, bytes ? bytes : 256));
   S->allocs.push_back(*p);
@@ -361,8 +376,10 @@ int alloc(SymBsr *S, void **p, size_t bytes) {
 }  // namespace
 
 int sym_create(Ctx *c, int32_t n, const uint32_t *rowptr, const uint32_t *colidx, int64_t nnzb,
-               SymBsr *S) {
+               int stages, SymBsr *S) {
   S->c = c;
+  S->nst = stages == 0 ? SYM_NST_DEFAULT : stages;
+  SG_REQUIRE(S->nst >= 2 && S->nst <= 4, "symmetric storage: stages %d (2..4)", stages);
   S->n = n;
   S->nnzb = nnzb;
   S->rowptr = rowptr;
@@ -431,14 +448,14 @@ int sym_fill(SymBsr *S, cudaStream_t st, const float *vals) {
 
 int sym_launch(SymBsr *S, cudaStream_t st, const SolveCtl *ctl, bool dot, const float *x,
                float *y, double *part) {
-  if (dot)
-    k_sbsr3_wtma<true><<<S->grid[1], WTMA_WARPS * 32, S->smem[1], st>>>(
-        ctl, S->n, S->urowptr, S->ucol, S->uvals, S->lrowptr, S->lidx, x, y, part, S->capu,
-        S->capl, S->c->d_err);
-  else
-    k_sbsr3_wtma<false><<<S->grid[0], WTMA_WARPS * 32, S->smem[0], st>>>(
-        nullptr, S->n, S->urowptr, S->ucol, S->uvals, S->lrowptr, S->lidx, x, y, part, S->capu,
-        S->capl, S->c->d_err);
+  switch (S->nst * 2 + (dot ? 1 : 0)) {
+    case 4: sym_launch_t<false, 2>(S, st, nullptr, x, y, part); break;
+    case 5: sym_launch_t<true, 2>(S, st, ctl, x, y, part); break;
+    case 6: sym_launch_t<false, 3>(S, st, nullptr, x, y, part); break;
+    case 7: sym_launch_t<true, 3>(S, st, ctl, x, y, part); break;
+    case 8: sym_launch_t<false, 4>(S, st, nullptr, x, y, part); break;
+    default: sym_launch_t<true, 4>(S, st, ctl, x, y, part); break;
+  }
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
@@ -456,11 +473,11 @@ using namespace sg;
 extern "C" {
 
 int sg_symbsr_create(sg_ctx *h, int32_t n, const uint32_t *rowptr, const uint32_t *colidx,
-                     int64_t nnzb, sg_symbsr **out) {
+                     int64_t nnzb, int32_t stages, sg_symbsr **out) {
   Ctx *c = as_ctx(h);
   SG_REQUIRE(c && out && rowptr && colidx, "sg_symbsr_create: null argument");
   auto *S = new SymBsr();
-  const int rc = sym_create(c, n, rowptr, colidx, nnzb, S);
+  const int rc = sym_create(c, n, rowptr, colidx, nnzb, stages, S);
   if (rc != SG_OK) {
     sym_free(S);
     delete S;

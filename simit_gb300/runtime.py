@@ -120,8 +120,8 @@ def bsr_add_diag(ctx, n, bs, rowptr, colidx, vals, diag=None, ident=0.0, scale=1
             out = torch.empty_like(vals)
     if diag is not None:
         assert diag.dtype == vals.dtype and diag.numel() == n * bs * bs
-    call("sg_bsr_add_diag", ctx.h, n, bs, ptr(rowptr), ptr(colidx), dtype_code(vals),
-         ptr(diag) if diag is not None else None, float(ident), float(scale), ptr(vals), ptr(out))
+    call("sg_bsr_add_diag", ctx.h, n, bs, ptr(rowptr), ptr(colidx), vals.numel() // (bs * bs),
+         dtype_code(vals), ptr(diag), float(ident), float(scale), ptr(vals), ptr(out))
     return out
 
 
@@ -129,11 +129,12 @@ class SymBsr:
     """sg_symbsr: symmetric (upper-half) storage of a 3x3-blocked FP32 matrix
     with a symmetric pattern; fill() from full values, spmv() = A x."""
 
-    def __init__(self, ctx, n, rowptr, colidx, nnzb):
+    def __init__(self, ctx, n, rowptr, colidx, nnzb, stages=0):
         self.ctx, self.n = ctx, n
         self._keep = (rowptr, colidx)
         h = ctypes.c_void_p()
-        call("sg_symbsr_create", ctx.h, n, ptr(rowptr), ptr(colidx), int(nnzb), ctypes.byref(h))
+        call("sg_symbsr_create", ctx.h, n, ptr(rowptr), ptr(colidx), int(nnzb), int(stages),
+             ctypes.byref(h))
         self.h = h.value
 
     def fill(self, vals):
