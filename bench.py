@@ -812,7 +812,7 @@ def run_ours(args, rank, world, local):
                              + ("; the iteration's SpMV on symmetric storage" if sym else ""),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (FP32 matrix 1.0 GB), no flush"},
-        "iters": iters, "relres_max": relres,
+        "iters": iters, "checks": int(results[-1].checks), "relres_max": relres,
         "e2e": {"value": dofs * world / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

@@ -342,6 +342,17 @@ int sg_solver_destroy(sg_solver *s);
 int sg_solve(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
              const double *b, double *x, sg_solve_result *res);
 
+/* True residual r = b - A x (FP64 x, b, r [n*bs]) and h_rr = ||r||^2;
+ * synchronises.  mode SG_RESIDUAL_FP64: FP64 accumulation (any bs and
+ * dtype).  SG_RESIDUAL_COMPENSATED (FP32 3x3 matrices): x split into float
+ * pairs and compensated FP32 products and sums, about 2^-46 of sum |A||x|
+ * accurate, without FP64 multiply-adds (the solver's checks between
+ * residual replacements).  The reference computes residuals in its .sim
+ * programs (apps/thermal/thermal.sim:88-93) with the lowered SpMV. */
+enum { SG_RESIDUAL_FP64 = 0, SG_RESIDUAL_COMPENSATED = 1 };
+int sg_residual(sg_ctx *ctx, const sg_matrix *A, const double *x, const double *b, double *r,
+                double *h_rr, int mode);
+
 /* ---------------------------------------------------------------------
  * Batched PCG: nsys independent 3x3-blocked systems concatenated into one
  * block-diagonal FP32 matrix (system s = block rows [sys_ptr[s],

@@ -53,6 +53,7 @@ class SolveResult(ctypes.Structure):
 SOLVE_F64, SOLVE_MIXED = 0, 1
 MPNN_RELU, MPNN_LINEAR, MPNN_SYM = 0, 1, 2
 STORAGE_FULL, STORAGE_SYMMETRIC = 0, 1
+RESIDUAL_FP64, RESIDUAL_COMPENSATED = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1, 2, 3
 STOP_NORMR2, STOP_NORMR, STOP_RELATIVE = 0, 1, 2
 STATUS = {1: "converged", 2: "maxiter", 3: "breakdown", 4: "nan"}
@@ -76,6 +77,7 @@ SIGNATURES = {
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),
+    "sg_residual": (_CI, [P, ctypes.POINTER(Matrix), P, P, P, ctypes.POINTER(D), _CI]),
     "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, I64, _CI, P, D, D, P, P]),
     "sg_symbsr_create": (_CI, [P, I32, P, P, I64, I32, ctypes.POINTER(P)]),
     "sg_symbsr_fill": (_CI, [P, P]),

@@ -272,6 +272,25 @@ static int true_residual(Solver *S, const double *b, double *rr) {
   return SG_OK;
 }
 
+// The same residual from the float split of x_hi without FP64 multiply-adds
+// (k_true_residual3c); S->xsplit must hold the split of the current x_hi.
+static int true_residual_fast(Solver *S, const double *b, double *rr) {
+  const sg_matrix &A = S->A;
+  S->launches += 2;
+  cudaStream_t st = S->c->stream;
+  const int PT = S->P1;
+  k_true_residual3c<4><<<PT, RED_T, 0, st>>>(A.n, A.rowptr, A.colidx, (const float *)A.vals,
+                                             S->xsplit, S->xsplit + S->len, b, S->rhi,
+                                             S->part3);
+  SG_CHECK_LAUNCH();
+  k_sum_parts<<<1, RED_T, 0, st>>>(S->part3, PT, S->dres);
+  SG_CHECK_LAUNCH();
+  SG_CHECK_CUDA(cudaMemcpyAsync(S->c->h_stage, S->dres, 8, cudaMemcpyDeviceToHost, st));
+  SG_CHECK_CUDA(cudaStreamSynchronize(st));
+  *rr = *(double *)S->c->h_stage;
+  return SG_OK;
+}
+
 // r = (VT) r_hi; z = M r (or the external preconditioner); returns r.z (sync).
 template <typename VT>
 static int restart_from_rhi(Solver *S, double *rz) {
@@ -329,8 +348,32 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     case SG_STOP_NORMR: tol2 = S->o.tol * S->o.tol; break;
     default: tol2 = S->o.tol * S->o.tol * bb; break;
   }
+  // Checks run the compensated FP32 residual when the matrix is FP32; one
+  // that meets the tolerance (with 10 % slack in the norm) is recomputed with
+  // FP64 accumulation, and only that decides convergence.
+  const bool fast = S->xsplit != nullptr;
+  bool exact = false;  // the last residual was the FP64 one
+  auto check = [&](double *out) -> int {
+    if (fast) {
+      k_fold_split<XT><<<S->P2, RED_T, 0, st>>>(S->len, S->xw, (XT *)S->xlo, S->xsplit,
+                                                 S->xsplit + S->len);
+      SG_CHECK_LAUNCH();
+      S->launches += 1;
+      SG_TRY(true_residual_fast(S, b, out));
+      if (std::isfinite(*out) && *out > 1.21 * tol2) {
+        exact = false;
+        return SG_OK;
+      }
+    } else if (mixed) {
+      k_add_lo<XT><<<S->P2, RED_T, 0, st>>>(S->len, S->xw, (XT *)S->xlo);
+      SG_CHECK_LAUNCH();
+      S->launches += 1;
+    }
+    exact = true;
+    return true_residual(S, b, out);
+  };
   double rr = 0;
-  SG_TRY(true_residual(S, b, &rr));
+  SG_TRY(check(&rr));
   res->normr2 = rr;
   res->true_normr2 = rr;
   int iters = 0;
@@ -392,6 +435,7 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
         break;
       }
     }
+    exact = false;  // x moved since the last residual
     // the slot K3 wrote last holds the larger iteration count
     const int cur = h->iter[1] > h->iter[0] ? 1 : 0;
     iters = h->iter[cur];
@@ -400,18 +444,13 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     else if (h->status == ST_NAN) status = SG_STATUS_NAN;
     if (status) break;
     // ST_NEED_CHECK or ST_MAXITER: fold x_lo in, look at the true residual
-    if (mixed) {
-      k_add_lo<XT><<<S->P2, RED_T, 0, st>>>(S->len, S->xw, (XT *)S->xlo);
-      SG_CHECK_LAUNCH();
-      S->launches += 1;
-    }
     const bool iter_conv = h->last_rr <= tol2;
     if (!S->o.verify && !mixed && iter_conv) {
       status = SG_STATUS_CONVERGED;
       break;
     }
     res->checks++;
-    SG_TRY(true_residual(S, b, &rr));
+    SG_TRY(check(&rr));
     if (!std::isfinite(rr)) {
       status = SG_STATUS_NAN;
       break;
@@ -448,7 +487,11 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     S->launches += 1;
   }
   SG_CHECK_CUDA(cudaMemcpyAsync(x, S->xw, S->len * 8, cudaMemcpyDeviceToDevice, st));
-  if (S->o.verify || mixed) {
+  if (status == SG_STATUS_CONVERGED && exact) {
+    // converged on an FP64 residual of this very x (x_lo was folded into
+    // x_hi before it, so the fold above added zeros)
+    res->true_normr2 = rr;
+  } else if (S->o.verify || mixed) {
     double rt = 0;
     SG_TRY(true_residual(S, b, &rt));
     res->true_normr2 = rt;
@@ -513,6 +556,53 @@ int sg_solver_refresh(sg_solver *hs) {
 
 int sg_solver_destroy(sg_solver *hs) {
   solver_free(reinterpret_cast<Solver *>(hs));
+  return SG_OK;
+}
+
+int sg_residual(sg_ctx *h, const sg_matrix *A, const double *x, const double *b, double *r,
+                double *h_rr, int mode) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && A && x && b && r && h_rr, "sg_residual: null argument");
+  SG_REQUIRE(A->n >= 1 && A->bs >= 1 && A->rowptr && A->colidx && A->vals,
+             "sg_residual: bad matrix");
+  SG_REQUIRE(A->dtype == SG_F32 || A->dtype == SG_F64, "sg_residual: dtype");
+  SG_REQUIRE(mode == SG_RESIDUAL_FP64 ||
+                 (mode == SG_RESIDUAL_COMPENSATED && A->dtype == SG_F32 && A->bs == 3),
+             "sg_residual: mode %d (compensated needs an FP32 3x3 matrix)", mode);
+  cudaStream_t st = c->stream;
+  const int64_t len = (int64_t)A->n * A->bs;
+  const int PT = grid_for(c, (int64_t)A->n * 4, RED_T, 8);
+  Scratch s(c);
+  SG_TRY(s.reserve(Scratch::bytes_for(PT, 8) + Scratch::bytes_for(1, 8) +
+                   (mode ? Scratch::bytes_for(len * 2, 4) : 0) + 1024));
+  double *part = s.alloc<double>(PT), *dres = s.alloc<double>(1);
+  if (mode == SG_RESIDUAL_COMPENSATED) {
+    float *xs = s.alloc<float>(len * 2);
+    k_split_x<<<grid_for(c, len, RED_T, 8), RED_T, 0, st>>>(len, x, xs, xs + len);
+    SG_CHECK_LAUNCH();
+    k_true_residual3c<4><<<PT, RED_T, 0, st>>>(A->n, A->rowptr, A->colidx,
+                                               (const float *)A->vals, xs, xs + len, b, r, part);
+  } else if (A->bs == 3) {
+    if (A->dtype == SG_F64)
+      k_true_residual3<4, double><<<PT, RED_T, 0, st>>>(A->n, A->rowptr, A->colidx,
+                                                         (const double *)A->vals, x, b, r, part);
+    else
+      k_true_residual3<4, float><<<PT, RED_T, 0, st>>>(A->n, A->rowptr, A->colidx,
+                                                        (const float *)A->vals, x, b, r, part);
+  } else {
+    if (A->dtype == SG_F64)
+      k_true_residual_any<double><<<PT, RED_T, 0, st>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                         (const double *)A->vals, x, b, r, part);
+    else
+      k_true_residual_any<float><<<PT, RED_T, 0, st>>>(A->n, A->bs, A->rowptr, A->colidx,
+                                                        (const float *)A->vals, x, b, r, part);
+  }
+  SG_CHECK_LAUNCH();
+  k_sum_parts<<<1, RED_T, 0, st>>>(part, PT, dres);
+  SG_CHECK_LAUNCH();
+  SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, dres, 8, cudaMemcpyDeviceToHost, st));
+  SG_CHECK_CUDA(cudaStreamSynchronize(st));
+  *h_rr = *(double *)c->h_stage;
   return SG_OK;
 }
 
@@ -647,6 +737,8 @@ int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
   }
   if (S->kind == KIND_MIXED && A->dtype == SG_F64)
     SG_TRY(alloc_dev(S, &S->vals32, A->nnzb * A->bs * A->bs * 4));
+  if (S->kind == KIND_MIXED && A->dtype == SG_F32 && A->bs == 3)
+    SG_TRY(alloc_dev(S, (void **)&S->xsplit, S->len * 8));
   if (S->prec == PK_JACOBI || S->prec == PK_BLOCK3)
     SG_TRY(alloc_dev(S, &S->dinv,
                      (S->prec == PK_BLOCK3 ? (int64_t)A->n * 9 : S->len) * vt));

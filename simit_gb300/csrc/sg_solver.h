@@ -30,6 +30,7 @@ struct Solver {
   void *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr, *xlo = nullptr, *dinv = nullptr;
   void *xupd = nullptr;             // the x the iteration updates (xw or xlo)
   double *xw = nullptr, *rhi = nullptr;
+  float *xsplit = nullptr;          // x_hi as floats xh | xl (compensated residual checks)
   double *part1 = nullptr, *part2 = nullptr, *part3 = nullptr, *dres = nullptr;
   SolveCtl *ctl = nullptr, *hctl = nullptr;
   cudaGraphExec_t gexec = nullptr;

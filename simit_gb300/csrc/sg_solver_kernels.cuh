@@ -722,6 +722,113 @@ __global__ void __launch_bounds__(RED_T) k_true_residual3(int32_t n,
   if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// r_hi = b - A x for an FP32 3x3 matrix without FP64 multiply-adds, which
+// are scarce on this GPU.  x arrives split into floats xh + xl (48
+// significant bits); each product a*xh is split exactly by the FMA residual
+// and summed with TwoSum into a float pair per row component, a*xl goes into
+// the low part (the compensated dot product of Ogita, Rump and Oishi, 2005);
+// the lanes of a row combine their pairs the same way and lane 0 converts
+// once to FP64 for b - y.  The error is about 2^-46 of sum |a||x| against
+// 2^-52 for FP64 accumulation: ample for the residual replacement between
+// checks, whose residual is never below the tolerance.  A residual that
+// meets the tolerance is recomputed with k_true_residual3 before the solver
+// accepts it.
+template <int G>
+__global__ void __launch_bounds__(RED_T)
+    k_true_residual3c(int32_t n, const uint32_t *__restrict__ rowptr,
+                      const uint32_t *__restrict__ colidx, const float *__restrict__ vals,
+                      const float *__restrict__ xh, const float *__restrict__ xl,
+                      const double *__restrict__ b, double *__restrict__ rhi,
+                      double *__restrict__ part) {
+  __shared__ double sh[33];
+  const int gl = threadIdx.x & (G - 1);
+  const unsigned mask = group_mask<G>();
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x / G);
+  double acc = 0;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
+    float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+    const uint32_t e = rowptr[r + 1];
+    for (uint32_t q = rowptr[r] + gl; q < e; q += G) {
+      const uint32_t c = colidx[q];
+      const float *v = vals + (size_t)q * 9;
+      float xa[3], xb[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        xa[k] = ldg(xh + (size_t)c * 3 + k);
+        xb[k] = ldg(xl + (size_t)c * 3 + k);
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float a = ldg(v + i * 3 + k);
+          const float p = __fmul_rn(a, xa[k]);
+          const float pe = __fmaf_rn(a, xa[k], -p);  // a*xh - p, exact
+          float s, se;
+          two_sum(h[i], p, s, se);
+          h[i] = s;
+          l[i] = __fadd_rn(l[i], __fadd_rn(se, __fmaf_rn(a, xb[k], pe)));
+        }
+    }
+#pragma unroll
+    for (int o = G >> 1; o > 0; o >>= 1)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float oh = __shfl_xor_sync(mask, h[i], o, G);
+        const float ol = __shfl_xor_sync(mask, l[i], o, G);
+        float s, se;
+        two_sum(h[i], oh, s, se);
+        h[i] = s;
+        l[i] = __fadd_rn(__fadd_rn(l[i], ol), se);
+      }
+    if (gl == 0) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const double y = (double)h[i] + (double)l[i];
+        const double rv = b[r * 3 + i] - y;
+        rhi[r * 3 + i] = rv;
+        acc += rv * rv;
+      }
+    }
+  }
+  double t = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// x_hi += x_lo, x_lo = 0, and the float split xh + xl of the new x_hi.
+template <typename XT>
+__global__ void k_fold_split(int64_t len, double *__restrict__ xhi, XT *__restrict__ xlo,
+                             float *__restrict__ xh, float *__restrict__ xl) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = xhi[i] + (double)xlo[i];
+    xhi[i] = x;
+    xlo[i] = XT(0);
+    const float a = (float)x;
+    xh[i] = a;
+    xl[i] = (float)(x - (double)a);
+  }
+}
+
+// The float split xh + xl of x.
+static __global__ void __launch_bounds__(RED_T) k_split_x(int64_t len, const double *__restrict__ x,
+                                                   float *__restrict__ xh,
+                                                   float *__restrict__ xl) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float a = (float)x[i];
+    xh[i] = a;
+    xl[i] = (float)(x[i] - (double)a);
+  }
+}
+
 // Any bs (one thread per row).
 template <typename MT>
 __global__ void k_true_residual_any(int32_t n, int32_t bs, const uint32_t *__restrict__ rowptr,

@@ -161,6 +161,18 @@ class SymBsr:
             pass
 
 
+def residual(ctx, n, bs, rowptr, colidx, vals, nnzb, x, b, mode=_lib.RESIDUAL_FP64):
+    """r = b - A x (FP64 x, b) and ||r||^2 through sg_residual."""
+    A = _lib.Matrix(n, bs, nnzb, rowptr.data_ptr(), colidx.data_ptr(), dtype_code(vals),
+                    vals.data_ptr())
+    with ctx.stream():
+        r = torch.empty_like(b)
+    rr = ctypes.c_double()
+    call("sg_residual", ctx.h, ctypes.byref(A), ptr(x), ptr(b), ptr(r), ctypes.byref(rr),
+         int(mode))
+    return r, rr.value
+
+
 def dot(ctx, a, b):
     out = ctypes.c_double()
     call("sg_dot", ctx.h, a.numel(), dtype_code(a), ptr(a), ptr(b), ctypes.byref(out))

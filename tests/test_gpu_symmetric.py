@@ -125,3 +125,29 @@ def test_symmetric_storage_needs_mixed_bs3(ctx):
     h = problems.hetero_mesh(4)
     with pytest.raises(SimitError):
         problems.HeteroElasticity(ctx, h, dtype=torch.float64, storage=_lib.STORAGE_SYMMETRIC)
+
+
+@pytest.mark.parametrize("n,nE,seed", [(5, 8, 1), (2000, 9000, 2)])
+def test_residual_modes_against_oracle(ctx, oracle, n, nE, seed):
+    """sg_residual: FP64 accumulation within 1e-14 and the compensated FP32
+    mode within 1e-12 of sum |A||x| + |b| (per entry) of the oracle's FP64
+    residual of the FP32 matrix (plain FP32 accumulation: ~1e-7); both
+    return ||r||^2 consistently."""
+    from simit_gb300.runtime import residual
+    rp, ci, vals = _sym_system(oracle, n, nE, seed)
+    g = meshgen.rng(seed + 7)
+    x = g.uniform(-1, 1, size=n * 3) * 10.0 ** g.uniform(-3, 3, size=n * 3)
+    b = g.uniform(-1, 1, size=n * 3)
+    v64 = vals.astype(np.float64)
+    ref = b - oracle.spmv(n, 3, rp, ci, v64, x)
+    scale = oracle.spmv(n, 3, rp, ci, np.abs(v64), np.abs(x)) + np.abs(b)
+    d = ctx.device
+    args = (ctx, n, 3, _t(rp, d), _t(ci, d), _t(vals, d), len(ci), _t(x, d), _t(b, d))
+    for mode, tol in ((_lib.RESIDUAL_FP64, 1e-14), (_lib.RESIDUAL_COMPENSATED, 1e-12)):
+        r, rr = residual(*args, mode=mode)
+        got = r.cpu().numpy()
+        assert np.all(np.abs(got - ref) <= tol * scale), mode
+        assert abs(rr - float(got @ got)) <= 1e-12 * rr
+    with pytest.raises(_lib.SimitError):  # compensated mode needs FP32 values
+        residual(ctx, n, 3, _t(rp, d), _t(ci, d), _t(v64, d), len(ci), _t(x, d), _t(b, d),
+                 mode=_lib.RESIDUAL_COMPENSATED)
