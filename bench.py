@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--f64", action="store_true", help="FP64 matrix for --spmv-only")
     ap.add_argument("--sym", action="store_true",
                     help="symmetric storage for the iteration's SpMV (and for --spmv-only)")
+    ap.add_argument("--pdl", action="store_true",
+                    help="programmatic dependent launch inside the solver's iteration graph")
     ap.add_argument("--stages", type=int, default=0,
                     help="--spmv-only --sym: bulk-copy stages per warp (2..4, 0 = default)")
     ap.add_argument("--cloth", action="store_true",
@@ -648,7 +650,7 @@ def run_ours(args, rank, world, local):
     prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
                                      precond=_lib.PRECOND_BLOCK_JACOBI,
                                      storage=_lib.STORAGE_SYMMETRIC if args.sym
-                                     else _lib.STORAGE_FULL)
+                                     else _lib.STORAGE_FULL, pdl=int(args.pdl))
     st = ctx.torch_stream
 
     def barrier():

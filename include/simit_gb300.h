@@ -90,6 +90,23 @@ int sg_slots_build(sg_ctx *ctx, int32_t n, const int32_t *endpoints,
                    int64_t nE, int32_t card, const uint32_t *rowptr,
                    const uint32_t *colidx, uint32_t *slots);
 
+/* Incidence matrices of an edge set over one of its vertex sets, the
+ * reference's non-square assembly patterns (src/path_expression_analysis
+ * .cpp:95-105).  sel int32[nE*npos]: each element's endpoints that lie in
+ * that vertex set, in endpoint order (all card endpoints for a homogeneous
+ * edge set); n: that vertex set's size.
+ *   SG_INCIDENCE_EV, tensor[E,V] (Link::ev, src/path_indices.cpp:207-246):
+ *     rowptr[nE+1] = e*npos, colidx[nE*npos] = sel (repeats kept);
+ *     slot_of unused (the slot of listing (e, k) is e*npos + k).
+ *   SG_INCIDENCE_VE, tensor[V,E] (Link::ve, :248-276): rowptr[n+1];
+ *     colidx[nE*npos] = per vertex the elements that list it, ascending,
+ *     once per listing; slot_of[nE*npos] = the slot of listing (e, k).
+ * Synchronises. */
+enum { SG_INCIDENCE_EV = 0, SG_INCIDENCE_VE = 1 };
+int sg_incidence_pattern(sg_ctx *ctx, int kind, int32_t n, int64_t nE, int32_t npos,
+                         const int32_t *sel, uint32_t *rowptr, uint32_t *colidx,
+                         uint32_t *slot_of);
+
 /* Longest row (blocks) of a pattern; synchronises.  The assembly kernels keep
  * one row image in shared memory and need this bound. */
 int sg_pattern_maxrow(sg_ctx *ctx, int32_t n, const uint32_t *rowptr,
@@ -148,6 +165,16 @@ int sg_assemble_scalar_springs(sg_ctx *ctx, const sg_mesh *mesh, int dtype,
  * bs 1..3, card 2..4.  exact = 1: no contraction (parity mode). */
 int sg_assemble_blocks(sg_ctx *ctx, const sg_mesh *mesh, int dtype, int bs, const void *eb,
                        void *vals, int exact);
+
+/* `map f to E reduce +` into an incidence matrix (sg_incidence_pattern):
+ * eb[(e*npos + k)*bs*bs] is the bs x bs block the element function writes at
+ * (endpoint k, e) for VE or (e, endpoint k) for EV, zero where it writes
+ * nothing.  Each is added, in ascending k from zero, into the first slot of
+ * its (row, column) -- the slot `loc` finds -- so a repeated endpoint's
+ * second slot holds zero.  vals [nE*npos*bs*bs]; bs 1..4. */
+int sg_assemble_incidence(sg_ctx *ctx, int kind, int64_t nE, int32_t npos, const int32_t *sel,
+                          const uint32_t *slot_of, int dtype, int32_t bs, const void *eb,
+                          void *vals);
 
 /* precomputeTetMat (femTet.sim; apps/fem/fem_linear.sim:176-193):
  * B = inv(Ds) [nE*9], W = -det(Ds)/6 [nE], vertex mass m [n] = sum of
@@ -311,6 +338,11 @@ typedef struct sg_solve_opts {
   int32_t learned_form;        /* SG_MPNN_RELU / SG_MPNN_LINEAR / SG_MPNN_SYM */
   int32_t storage;             /* SG_STORAGE_FULL / SG_STORAGE_SYMMETRIC (mixed, bs 3):
                                   the iteration's SpMV reads the upper half only */
+  int32_t pdl;                 /* 1: programmatic dependent launch between the
+                                  iteration's kernels in the captured graph (the
+                                  next kernel launches while its predecessor
+                                  drains); 0 (default): plain graph edges, which
+                                  measured 4 % faster at 128^3 */
 } sg_solve_opts;
 
 typedef struct sg_solve_result {

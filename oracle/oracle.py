@@ -172,6 +172,47 @@ def add_diag(n, bs, rowptr, colidx, K, diag=None, ident=0.0, scale=1.0):
     return out
 
 
+def incidence_pattern(kind, n, sel, npos):
+    """Link::ev (kind 0, src/path_indices.cpp:207-246: row e = its endpoints
+    in endpoint order) or Link::ve (kind 1, :248-276: per vertex the edges
+    that list it, pushed back in edge order, then packed)."""
+    sel = np.asarray(sel, np.int64).reshape(-1, npos)
+    nE = sel.shape[0]
+    if kind == 0:
+        return (np.arange(nE + 1, dtype=np.uint32) * npos).astype(np.uint32), \
+            sel.reshape(-1).astype(np.uint32)
+    nbrs = [[] for _ in range(n)]
+    for e in range(nE):
+        for k in range(npos):
+            nbrs[sel[e, k]].append(e)
+    rowptr = np.zeros(n + 1, np.uint32)
+    rowptr[1:] = np.cumsum([len(x) for x in nbrs])
+    colidx = np.array([e for x in nbrs for e in x], np.uint32)
+    return rowptr, colidx
+
+
+def assemble_incidence(kind, sel, npos, bs, eb, rowptr, colidx):
+    """`map` into an incidence matrix: for elements in order, for each write
+    (endpoint k, in order) `+=` into loc(row, col) (src/runtime.cpp:19-23:
+    the first slot of that column in the row), FP64, zero-initialised."""
+    sel = np.asarray(sel, np.int64).reshape(-1, npos)
+    bb = bs * bs
+    eb = np.asarray(eb, np.float64).reshape(sel.shape[0], npos, bb)
+    vals = np.zeros((len(colidx), bb))
+
+    def loc(r, c):
+        q = int(rowptr[r])
+        while int(colidx[q]) != c:
+            q += 1
+        return q
+    for e in range(sel.shape[0]):
+        for k in range(npos):
+            v = int(sel[e, k])
+            q = loc(e, v) if kind == 0 else loc(v, e)
+            vals[q] += eb[e, k]
+    return vals.reshape(-1)
+
+
 def cg_normr2(n, bs, rowptr, colidx, A, b, x0, tol2, maxiters):
     x = _c(x0, np.float64).copy()
     nr = np.zeros(1)

@@ -41,7 +41,7 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("precond", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", D), ("maxiters", I32), ("verify", I32), ("check_every", I32),
                 ("reliable_delta", D), ("lanes", I32), ("batch", I32), ("learned_params", P),
-                ("learned_form", I32), ("storage", I32)]
+                ("learned_form", I32), ("storage", I32), ("pdl", I32)]
 
 
 class SolveResult(ctypes.Structure):
@@ -54,6 +54,7 @@ SOLVE_F64, SOLVE_MIXED = 0, 1
 MPNN_RELU, MPNN_LINEAR, MPNN_SYM = 0, 1, 2
 STORAGE_FULL, STORAGE_SYMMETRIC = 0, 1
 RESIDUAL_FP64, RESIDUAL_COMPENSATED = 0, 1
+INCIDENCE_EV, INCIDENCE_VE = 0, 1
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1, 2, 3
 STOP_NORMR2, STOP_NORMR, STOP_RELATIVE = 0, 1, 2
 STATUS = {1: "converged", 2: "maxiter", 3: "breakdown", 4: "nan"}
@@ -78,6 +79,8 @@ SIGNATURES = {
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),
     "sg_residual": (_CI, [P, ctypes.POINTER(Matrix), P, P, P, ctypes.POINTER(D), _CI]),
+    "sg_incidence_pattern": (_CI, [P, _CI, I32, I64, I32, P, P, P, P]),
+    "sg_assemble_incidence": (_CI, [P, _CI, I64, I32, P, P, _CI, I32, P, P]),
     "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, I64, _CI, P, D, D, P, P]),
     "sg_symbsr_create": (_CI, [P, I32, P, P, I64, I32, ctypes.POINTER(P)]),
     "sg_symbsr_fill": (_CI, [P, P]),

@@ -43,7 +43,32 @@ struct Ctx {
   int32_t mr_t8[MAXROW_CACHE] = {};   // largest 8-row tile
   int mr_next = 0;
   int refs = 1;  // sg_ctx_destroy + one per live solver
+  // Set while a solver captures its iteration graph: kernels launched with
+  // launch_k then carry programmatic stream serialisation, so each may start
+  // while its predecessor drains (the kernels wait with griddepcontrol.wait
+  // before their first global access).
+  bool pdl = false;
 };
+
+// Kernel launch honouring Ctx::pdl (cudaLaunchKernelEx with the
+// programmatic-stream-serialisation attribute when it is set).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(const Ctx *c, void (*kern)(KArgs...), dim3 grid, dim3 block,
+                            size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  if (c->pdl) {
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
 
 // Drops one reference; frees the context when none are left.
 void ctx_release(Ctx *c);

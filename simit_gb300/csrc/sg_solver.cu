@@ -164,10 +164,11 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
         int64_t grid = (nchunks + K2W_WARPS - 1) / K2W_WARPS;
         if (grid > 2 * (int64_t)S->c->num_sms) grid = 2 * (int64_t)S->c->num_sms;
         if (grid < 1) grid = 1;
-        k_cg_update_w<true><<<(int)grid, K2W_WARPS * 32, sm, st>>>(
-            S->ctl, par, S->len, S->part1, S->P1, S->tma, (const float *)S->p,
-            (const float *)S->q, (float *)S->r, (float *)S->xupd, (float *)S->z,
-            (const float *)S->dinv, S->part2);
+        SG_CHECK_CUDA(launch_k(S->c, k_cg_update_w<true>, (int)grid, K2W_WARPS * 32, sm, st,
+                               S->ctl, par, S->len, (const double *)S->part1, S->P1, S->tma,
+                               (const float *)S->p, (const float *)S->q, (float *)S->r,
+                               (float *)S->xupd, (float *)S->z, (const float *)S->dinv,
+                               S->part2));
         break;
       }
       default: launch_k2_v4<PK_EXTERNAL>(S, st, par); break;
@@ -201,9 +202,9 @@ template <typename VT>
 static int launch_k3(Solver *S, cudaStream_t st, int par) {
   const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
   if (sizeof(VT) == 4)  // K2 decided unless an external preconditioner ran after it
-    k_cg_direction_v4<<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2,
-                                               S->prec != PK_EXTERNAL, (const float *)z,
-                                               (float *)S->p);
+    SG_CHECK_CUDA(launch_k(S->c, k_cg_direction_v4, S->P2, RED_T, 0, st, S->ctl, par, S->len,
+                           (const double *)S->part2, S->P2, (int)(S->prec != PK_EXTERNAL),
+                           (const float *)z, (float *)S->p));
   else
     k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z,
                                                 (VT *)S->p);
@@ -217,6 +218,9 @@ static int capture_batch(Solver *S) {
   cudaGraph_t g = nullptr;
   SG_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   int rc = SG_OK;
+  // optional programmatic dependent launch for the kernels launched through
+  // launch_k (K1 per-warp TMA SpMV, K2 warp-staged update, K3 FP32 direction)
+  S->c->pdl = S->o.pdl != 0;
   for (int k = 0; k < S->batch && rc == SG_OK; ++k) {
     const int par = k & 1;
     rc = launch_k1<MT, VT>(S, st);
@@ -224,6 +228,7 @@ static int capture_batch(Solver *S) {
     if (rc == SG_OK && S->ext_prec) rc = S->ext_prec(S, st);
     if (rc == SG_OK) rc = launch_k3<VT>(S, st, par);
   }
+  S->c->pdl = false;
   cudaError_t e = cudaStreamEndCapture(st, &g);
   if (rc != SG_OK) {
     if (g) cudaGraphDestroy(g);

@@ -22,6 +22,7 @@
 #include <stdint.h>
 
 #include "sg_spmv.cuh"
+#include "sg_tma.cuh"
 
 namespace sg {
 
@@ -495,6 +496,7 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
     double *__restrict__ part_out) {
   extern __shared__ __align__(16) unsigned char k2w_raw[];
   __shared__ double sh[33];
+  pdl_wait_and_release();
   if (ctl->status != ST_RUNNING) return;
   const double pq = pq_fin ? ctl->pq_tot : sum_parts(part_in, np1, sh);
   const double rz = ctl->rz[par];
@@ -636,6 +638,7 @@ static __global__ void __launch_bounds__(RED_T) k_cg_direction_v4(SolveCtl *ctl,
                                                            const float *__restrict__ z,
                                                            float *__restrict__ p) {
   __shared__ double sh[33];
+  pdl_wait_and_release();
   if (ctl->status != ST_RUNNING) return;
   if (fin) {
     const float b = (float)ctl->beta;

@@ -90,13 +90,14 @@ static int wtma_launch_t(Ctx *c, cudaStream_t st, const SolveCtl *ctl, int32_t n
                          const uint32_t *rp, const uint32_t *ci, const MT *v, const VT *x, VT *y,
                          double *part, const PatternStats &ps, int grid, size_t smem) {
   const int capb = tile_cap(32 / G * P, ps);
+  // launch_k: inside a solver's graph capture the launch may overlap the
+  // previous kernel's tail (the kernel waits for it before any access)
   if (BS == 3)
-    k_bsr3_wtma<G, NST, MT, VT, DOT><<<grid, WTMA_WARPS * 32, smem, st>>>(ctl, n, rp, ci, v, x,
-                                                                         y, part, capb, c->d_err);
+    SG_CHECK_CUDA(launch_k(c, k_bsr3_wtma<G, NST, MT, VT, DOT>, grid, WTMA_WARPS * 32, smem, st,
+                           ctl, n, rp, ci, v, x, y, part, capb, c->d_err));
   else
-    k_csr_wtma<G, NST, P, MT, VT, DOT><<<grid, WTMA_WARPS * 32, smem, st>>>(
-        ctl, n, rp, ci, v, x, y, part, capb, c->d_err);
-  SG_CHECK_LAUNCH();
+    SG_CHECK_CUDA(launch_k(c, k_csr_wtma<G, NST, P, MT, VT, DOT>, grid, WTMA_WARPS * 32, smem,
+                           st, ctl, n, rp, ci, v, x, y, part, capb, c->d_err));
   return SG_OK;
 }
 

@@ -275,6 +275,7 @@ __device__ __forceinline__ void wtma_body(const SolveCtl *__restrict__ ctl, int3
   constexpr int RW = 32 / G * P;
   constexpr int BB = BS * BS;
   constexpr size_t S = sizeof(MT);
+  pdl_wait_and_release();
   if (ctl && ctl->status != ST_RUNNING) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t vbytes = tma_vbytes<MT, BB>(capb), cbytes = tma_cbytes(capb);

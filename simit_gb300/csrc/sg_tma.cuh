@@ -9,6 +9,14 @@ namespace sg {
 
 constexpr uint32_t SG_WAIT_LIMIT = 1u << 26;
 
+// Programmatic dependent launch: wait until the preceding kernel in the
+// stream has completed and its writes are visible (a no-op for a kernel
+// launched without the attribute), then let the next kernel begin launching.
+__device__ __forceinline__ void pdl_wait_and_release() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }

@@ -70,7 +70,7 @@ class HeteroElasticity:
     """
 
     def __init__(self, ctx, host, dtype=torch.float32, precond=_lib.PRECOND_BLOCK_JACOBI,
-                 precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None):
+                 precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None, pdl=0):
         self.ctx, self.host, self.dtype = ctx, host, dtype
         self.mesh = Mesh(ctx, host["n"], host["tets"], 4)
         d = ctx.device
@@ -90,7 +90,7 @@ class HeteroElasticity:
             storage = _lib.STORAGE_FULL
         self.opts = solve_opts(precision=precision, precond=precond, stop=_lib.STOP_RELATIVE,
                                tol=tol, maxiters=maxiters, verify=1, lanes=lanes,
-                               storage=storage)
+                               storage=storage, pdl=pdl)
         self.solver = Solver(ctx, self.mesh.n, 3, self.mesh.pattern.rowptr,
                              self.mesh.pattern.colidx, self.A, self.mesh.nnzb, self.opts)
 

@@ -103,9 +103,13 @@ class Pattern:
 
 
 def bspmv(ctx, n, bs, rowptr, colidx, vals, x, y=None, g=0):
+    """y [n*bs] = A x for n block rows (x is indexed by column, so its length
+    is the column count times bs: a rectangular matrix's differs from n*bs)."""
     if y is None:
         with ctx.stream():
-            y = torch.empty_like(x)
+            y = torch.empty(n * bs, dtype=x.dtype, device=x.device)
+    if y.numel() < n * bs or y.dtype != x.dtype:
+        raise ValueError("bspmv: y needs %d %s entries" % (n * bs, x.dtype))
     call("sg_bspmv", ctx.h, n, bs, ptr(rowptr), ptr(colidx), dtype_code(vals), ptr(vals),
          dtype_code(x), ptr(x), ptr(y), g)
     return y
@@ -143,9 +147,13 @@ class SymBsr:
         call("sg_symbsr_fill", self.h, ptr(vals))
 
     def spmv(self, x, y=None):
+        if x.numel() != self.n * 3 or x.dtype != torch.float32:
+            raise ValueError("symmetric spmv: x needs %d float32 entries" % (self.n * 3))
         if y is None:
             with self.ctx.stream():
-                y = torch.empty_like(x)
+                y = torch.empty(self.n * 3, dtype=torch.float32, device=x.device)
+        if y.numel() < self.n * 3:
+            raise ValueError("symmetric spmv: y needs %d entries" % (self.n * 3))
         call("sg_symbsr_spmv", self.h, ptr(x), ptr(y))
         return y
 
@@ -171,6 +179,44 @@ def residual(ctx, n, bs, rowptr, colidx, vals, nnzb, x, b, mode=_lib.RESIDUAL_FP
     call("sg_residual", ctx.h, ctypes.byref(A), ptr(x), ptr(b), ptr(r), ctypes.byref(rr),
          int(mode))
     return r, rr.value
+
+
+class IncidenceMatrix:
+    """An edge set's incidence pattern over one vertex set (sg_incidence_pattern):
+    kind INCIDENCE_EV (rows = elements, tensor[E,V]) or INCIDENCE_VE (rows =
+    vertices, tensor[V,E]).  sel [nE*npos]: each element's endpoints in that
+    vertex set, in endpoint order; n: the vertex set's size."""
+
+    def __init__(self, ctx, kind, n, sel, npos):
+        d = ctx.device
+        self.ctx, self.kind, self.n, self.npos = ctx, kind, n, npos
+        with ctx.stream():
+            self.sel = torch.as_tensor(np.ascontiguousarray(sel, np.int32)).to(d)
+        self.nE = self.sel.numel() // npos
+        m = self.nE * npos
+        self.rows = self.nE if kind == _lib.INCIDENCE_EV else n
+        with ctx.stream():
+            self.rowptr = torch.empty(self.rows + 1, dtype=torch.int32, device=d)
+            self.colidx = torch.empty(max(1, m), dtype=torch.int32, device=d)
+            self.slot_of = torch.empty(max(1, m), dtype=torch.int32, device=d)
+        call("sg_incidence_pattern", ctx.h, kind, n, self.nE, npos, ptr(self.sel),
+             ptr(self.rowptr), ptr(self.colidx), ptr(self.slot_of))
+        self.nnzb = m
+
+    def assemble(self, eb, bs, dtype=torch.float64):
+        """Values [nnzb*bs*bs] from the element function's blocks eb [nE, npos, bs, bs]."""
+        with self.ctx.stream():
+            eb = _d(eb, dtype, self.ctx.device)
+            vals = torch.empty(max(1, self.nnzb * bs * bs), dtype=dtype, device=self.ctx.device)
+        call("sg_assemble_incidence", self.ctx.h, self.kind, self.nE, self.npos, ptr(self.sel),
+             ptr(self.slot_of), dtype_code(vals), int(bs), ptr(eb), ptr(vals))
+        return vals
+
+    def spmv(self, bs, vals, x):
+        cols = self.n if self.kind == _lib.INCIDENCE_EV else self.nE
+        if x.numel() != cols * bs:
+            raise ValueError("incidence spmv: x needs %d entries" % (cols * bs))
+        return bspmv(self.ctx, self.rows, bs, self.rowptr, self.colidx, vals, x)
 
 
 def dot(ctx, a, b):
@@ -327,10 +373,11 @@ def assemble_heat(mesh, B, W, kappa, dt, T0, dtype=torch.float64, exact=True):
 
 def solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_RELATIVE,
                tol=1e-8, maxiters=10000, verify=1, check_every=0, reliable_delta=0.1, lanes=0,
-               batch=32, learned_params=None, learned_form=0, storage=0):
+               batch=32, learned_params=None, learned_form=0, storage=0, pdl=0):
     lp = learned_params.data_ptr() if learned_params is not None else None
     return _lib.SolveOpts(precision, precond, stop, tol, maxiters, verify, check_every,
-                          reliable_delta, lanes, batch, lp, int(learned_form), int(storage))
+                          reliable_delta, lanes, batch, lp, int(learned_form), int(storage),
+                          int(pdl))
 
 
 class Solver:

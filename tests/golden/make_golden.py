@@ -4,7 +4,8 @@ Run in a checkout that has the reference sources (default path below, or
 SIMIT_REFERENCE); the GPU machine has none, so the outputs are committed:
 
   reference_golden.json   golden values asserted by the reference's tests,
-                          extracted from their sources (file:line recorded)
+                          extracted from their sources (file:line recorded),
+                          including the incidence-matrix assembly tests
   bar2k.node, bar2k.ele   the TetGen fixture test/program-fem-test.cpp loads
   tetgen_golden.json      the TetGen .node/.ele/.edge texts of
                           test/mesh-test.cpp (TetgenTest, TetgenEdgeTest)
@@ -70,6 +71,32 @@ def extract_raw_strings(path, test_name):
     return {k: v for k, v in re.findall(r"string\s+(\w+)\s*=\s*R\"\((.*?)\)\";", body, re.S)}
 
 
+def extract_incidence_asserts(path, test_name):
+    """Expected ints of TEST(..., test_name) in test/assembly-tests.cpp, in
+    either ASSERT_EQ order, plus `const std::vector<int> name = {...}`."""
+    src = open(path).read()
+    m = re.search(r"TEST\(\w+,\s*%s\)\s*\{" % test_name, src)
+    start = src[:m.start()].count("\n") + 1
+    body = src[m.end():]
+    nxt = re.search(r"\nTEST\(", body)
+    body = body[:nxt.start()] if nxt else body
+    out = {"source": "%s:%d" % (os.path.relpath(path, REF), start), "asserts": [], "vectors": {}}
+    arg = r"((?:[^(),]|\((?:[^()]|\([^()]*\))*\))+)"
+    for a, b in re.findall(r"ASSERT_EQ\(\s*" + arg + r"\s*,\s*" + arg + r"\s*\);", body):
+        a, b = a.strip(), b.strip()
+        if re.fullmatch(r"-?\d+", a):
+            out["asserts"].append({"expected": int(a), "expr": b})
+        elif re.fullmatch(r"-?\d+", b):
+            out["asserts"].append({"expected": int(b), "expr": a})
+    # for (int i = 0; i < N; ++i) { ASSERT_EQ(i + 1, (int)f(v[i])); }
+    for cnt, fld in re.findall(r"for \(int i = 0; i < (\d+); \+\+i\) \{\s*"
+                               r"ASSERT_EQ\(i \+ 1, \(int\)(\w+)\(\w+\[i\]\)\);", body):
+        out["vectors"][fld + "_loop"] = [i + 1 for i in range(int(cnt))]
+    for name, vals in re.findall(r"std::vector<int>\s+(\w+)\s*=\s*\{([^}]*)\}", body):
+        out["vectors"][name] = [int(t) for t in vals.split(",")]
+    return out
+
+
 def main():
     test = os.path.join(REF, "test")
     if not os.path.isdir(test):
@@ -88,6 +115,9 @@ def main():
                                                    "gemv_blocked_computed"),
         "matrix_vv": extract_assert_eq(os.path.join(test, "assembly-tests.cpp"), "matrix_vv"),
     }
+    for name in ("matrix_ve", "matrix_ev", "matrix_ve_heterogeneous", "matrix_ev_heterogeneous"):
+        golden["incidence_" + name] = extract_incidence_asserts(
+            os.path.join(test, "assembly-tests.cpp"), name)
     with open(os.path.join(HERE, "reference_golden.json"), "w") as f:
         json.dump(golden, f, indent=1)
     mesh_test = os.path.join(test, "mesh-test.cpp")

@@ -14,6 +14,11 @@ from simit_gb300 import meshgen
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+def _golden_map():
+    with open(os.path.join(GOLDEN, "reference_golden.json")) as f:
+        return json.load(f)
+
+
 def golden(name):
     with open(os.path.join(GOLDEN, "reference_golden.json")) as f:
         return json.load(f)[name]
@@ -153,3 +158,31 @@ def springs_from_tetgen(node_path, edge_path):
             "fixed": (x[:, 2] < 0.1).astype(np.uint8), "ep": ep.reshape(-1).astype(np.int32),
             "k": np.full(len(ep), 1e4), "l0": l0, "h": 1e-2, "viscous": 2.0,
             "grav": np.array([0.0, -9.81, 0.0]), "tol2": 1e-12, "maxiters": 50, "form": 0}
+
+
+def incidence_scenarios():
+    """The four incidence-matrix programs of test/assembly-tests.cpp as
+    (kind, n, sel, npos, element blocks, vector, expected result, name):
+    matrix_ve / matrix_ev (test/input/assembly/matrix_{ve,ev}.sim: every
+    write is 1; c = A * E.a and E.a = A * V.c) and their heterogeneous forms
+    (an edge set over (V1, V1, V0, V1, V1): the V0 matrix takes endpoint 2,
+    the V1 matrix endpoints 0, 1, 3, 4 with writes 1, 2, 3, 4)."""
+    g = {k: v for k, v in _golden_map().items() if k.startswith("incidence_")}
+    out = []
+    ep2 = np.array([[0, 1], [1, 2]])
+    exp = [a["expected"] for a in g["incidence_matrix_ve"]["asserts"]]
+    out.append((1, 3, ep2, 2, np.ones((2, 2)), np.array([1.0, 2.0]), exp, "matrix_ve"))
+    exp = [a["expected"] for a in g["incidence_matrix_ev"]["asserts"]]
+    out.append((0, 3, ep2, 2, np.ones((2, 2)), np.array([1.0, 2.0, 3.0]), exp, "matrix_ev"))
+    het = np.array([[0, 1, 0, 3, 4], [1, 2, 1, 4, 5], [3, 4, 2, 6, 7], [4, 5, 3, 7, 8]])
+    v0, v1 = het[:, [2]], het[:, [0, 1, 3, 4]]
+    w1 = np.tile(np.array([1.0, 2.0, 3.0, 4.0]), (4, 1))
+    gv = g["incidence_matrix_ve_heterogeneous"]["vectors"]
+    ea = np.array([1.0, 2.0, 3.0, 4.0])
+    out.append((1, 4, v0, 1, np.ones((4, 1)), ea, gv["b0_loop"], "matrix_ve_heterogeneous V0"))
+    out.append((1, 9, v1, 4, w1, ea, gv["b1Expected"], "matrix_ve_heterogeneous V1"))
+    ga = [a["expected"] for a in g["incidence_matrix_ev_heterogeneous"]["asserts"]]
+    out.append((0, 4, v0, 1, np.ones((4, 1)), np.arange(1.0, 5.0), ga[:4],
+                "matrix_ev_heterogeneous V0"))
+    out.append((0, 9, v1, 4, w1, np.arange(1.0, 10.0), ga[4:], "matrix_ev_heterogeneous V1"))
+    return out

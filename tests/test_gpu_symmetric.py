@@ -151,3 +151,18 @@ def test_residual_modes_against_oracle(ctx, oracle, n, nE, seed):
     with pytest.raises(_lib.SimitError):  # compensated mode needs FP32 values
         residual(ctx, n, 3, _t(rp, d), _t(ci, d), _t(v64, d), len(ci), _t(x, d), _t(b, d),
                  mode=_lib.RESIDUAL_COMPENSATED)
+
+
+def test_solver_pdl_same_result(ctx):
+    """Programmatic dependent launch inside the iteration graph (opt-in)
+    changes no arithmetic: the same iterations and the same solution bits."""
+    h = problems.reorder_hetero(problems.hetero_mesh(12))
+    out = []
+    for pdl in (0, 1):
+        p = problems.HeteroElasticity(ctx, h, dtype=torch.float32, pdl=pdl)
+        assert p.opts.pdl == pdl
+        res = p.step()
+        ctx.sync()
+        out.append((res.iters, res.true_normr2, p.u.cpu().numpy().copy()))
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])

@@ -145,3 +145,16 @@ def test_add_diag_semantics(oracle):
                                    rp, ci)
     MD = ((m + 1e-3 * 0.5)[:, None, None] * np.eye(3)[None]).reshape(-1)
     assert np.array_equal(oracle.add_diag(n, 3, rp, ci, K, diag=MD), fused)
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_incidence_matrices_golden(oracle, case):
+    """Link::ev / Link::ve patterns and the `map` into them (the oracle's
+    restatement) reproduce test/assembly-tests.cpp's matrix_ve, matrix_ev
+    and heterogeneous results (A * field)."""
+    kind, n, sel, npos, eb, vec, expected, name = scenarios.incidence_scenarios()[case]
+    rp, ci = oracle.incidence_pattern(kind, n, sel, npos)
+    vals = oracle.assemble_incidence(kind, sel, npos, 1, eb, rp, ci)
+    rows = len(rp) - 1
+    y = oracle.spmv(rows, 1, rp, ci, vals, vec)
+    assert y.tolist() == [float(v) for v in expected], name
