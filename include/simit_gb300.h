@@ -107,6 +107,20 @@ int sg_incidence_pattern(sg_ctx *ctx, int kind, int32_t n, int64_t nE, int32_t n
                          const int32_t *sel, uint32_t *rowptr, uint32_t *colidx,
                          uint32_t *slot_of);
 
+/* Rectangular pattern ∃e.(v-e ∧ e-u) between two vertex sets of one edge
+ * set (src/path_expression_analysis.cpp:80-92 with v and u in different
+ * sets, e.g. matrix[V0,V1] over Set E(V1,V1,V0,V1,V1)): rows are the nr
+ * vertices of the row set, reached through the elements' row-set endpoints;
+ * ve_ptr / ve_idx are their incidence (sg_incidence_build over those
+ * endpoints, npos_r per element); sel_c int32[nE*npos_c] the elements'
+ * column-set endpoints (nc vertices).  Row v lists, sorted and unique, the
+ * column-set endpoints of its elements (at most 64).  Call with colidx NULL
+ * for rowptr[nr+1] and *h_nnzb, then with colidx[nnzb].  Synchronises. */
+int sg_pattern_rect(sg_ctx *ctx, int32_t nr, int32_t nc, int64_t nE, int32_t npos_r,
+                    int32_t npos_c, const int32_t *sel_c, const uint32_t *ve_ptr,
+                    const uint32_t *ve_idx, uint32_t *rowptr, uint32_t *colidx,
+                    int64_t *h_nnzb);
+
 /* Longest row (blocks) of a pattern; synchronises.  The assembly kernels keep
  * one row image in shared memory and need this bound. */
 int sg_pattern_maxrow(sg_ctx *ctx, int32_t n, const uint32_t *rowptr,
@@ -175,6 +189,15 @@ int sg_assemble_blocks(sg_ctx *ctx, const sg_mesh *mesh, int dtype, int bs, cons
 int sg_assemble_incidence(sg_ctx *ctx, int kind, int64_t nE, int32_t npos, const int32_t *sel,
                           const uint32_t *slot_of, int dtype, int32_t bs, const void *eb,
                           void *vals);
+
+/* `map f to E reduce +` into a rectangular pattern (sg_pattern_rect):
+ * eb[((e*npos_r + k)*npos_c + j)*bs*bs] is the block written at (row-set
+ * endpoint k, column-set endpoint j) of element e; each row owner adds them
+ * in ascending (e, k, j) from zero.  vals [nnzb*bs*bs]; bs 1..4. */
+int sg_assemble_rect(sg_ctx *ctx, int32_t nr, int32_t npos_r, int32_t npos_c,
+                     const int32_t *sel_c, const uint32_t *ve_ptr, const uint32_t *ve_idx,
+                     const uint32_t *rowptr, const uint32_t *colidx, int dtype, int32_t bs,
+                     const void *eb, void *vals);
 
 /* precomputeTetMat (femTet.sim; apps/fem/fem_linear.sim:176-193):
  * B = inv(Ds) [nE*9], W = -det(Ds)/6 [nE], vertex mass m [n] = sum of

@@ -213,6 +213,40 @@ def assemble_incidence(kind, sel, npos, bs, eb, rowptr, colidx):
     return vals.reshape(-1)
 
 
+def rect_pattern(nr, sel_r, npos_r, sel_c, npos_c):
+    """∃e.(v-e ∧ e-u) with v and u in different vertex sets
+    (src/path_indices.cpp:359-429, And of Link::ve over the row set's
+    endpoints and Link::ev over the column set's): sorted unique columns."""
+    sr = np.asarray(sel_r, np.int64).reshape(-1, npos_r)
+    sc = np.asarray(sel_c, np.int64).reshape(-1, npos_c)
+    rows = [set() for _ in range(nr)]
+    for e in range(sr.shape[0]):
+        for v in sr[e]:
+            rows[v].update(int(u) for u in sc[e])
+    rowptr = np.zeros(nr + 1, np.uint32)
+    rowptr[1:] = np.cumsum([len(r) for r in rows])
+    colidx = np.array([u for r in rows for u in sorted(r)], np.uint32)
+    return rowptr, colidx
+
+
+def assemble_rect(sel_r, npos_r, sel_c, npos_c, bs, eb, rowptr, colidx):
+    """`map` into it: elements in order, writes (k, j) in order, `+=` into
+    loc(row endpoint k, column endpoint j), FP64."""
+    sr = np.asarray(sel_r, np.int64).reshape(-1, npos_r)
+    sc = np.asarray(sel_c, np.int64).reshape(-1, npos_c)
+    bb = bs * bs
+    eb = np.asarray(eb, np.float64).reshape(sr.shape[0], npos_r, npos_c, bb)
+    vals = np.zeros((len(colidx), bb))
+    for e in range(sr.shape[0]):
+        for k in range(npos_r):
+            for j in range(npos_c):
+                q = int(rowptr[sr[e, k]])
+                while int(colidx[q]) != sc[e, j]:
+                    q += 1
+                vals[q] += eb[e, k, j]
+    return vals.reshape(-1)
+
+
 def cg_normr2(n, bs, rowptr, colidx, A, b, x0, tol2, maxiters):
     x = _c(x0, np.float64).copy()
     nr = np.zeros(1)

@@ -81,6 +81,8 @@ SIGNATURES = {
     "sg_residual": (_CI, [P, ctypes.POINTER(Matrix), P, P, P, ctypes.POINTER(D), _CI]),
     "sg_incidence_pattern": (_CI, [P, _CI, I32, I64, I32, P, P, P, P]),
     "sg_assemble_incidence": (_CI, [P, _CI, I64, I32, P, P, _CI, I32, P, P]),
+    "sg_pattern_rect": (_CI, [P, I32, I32, I64, I32, I32, P, P, P, P, P, ctypes.POINTER(I64)]),
+    "sg_assemble_rect": (_CI, [P, I32, I32, I32, P, P, P, P, P, _CI, I32, P, P]),
     "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, I64, _CI, P, D, D, P, P]),
     "sg_symbsr_create": (_CI, [P, I32, P, P, I64, I32, ctypes.POINTER(P)]),
     "sg_symbsr_fill": (_CI, [P, P]),

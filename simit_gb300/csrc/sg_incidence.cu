@@ -149,3 +149,177 @@ int sg_assemble_incidence(sg_ctx *h, int kind, int64_t nE, int32_t npos, const i
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Rectangular vertex-vertex pattern ∃e.(v-e ∧ e-u) between two vertex sets of
+// one edge set (src/path_expression_analysis.cpp:80-92 with v and u in
+// different sets): row v of the row set lists, sorted and unique, the column
+// set's endpoints of every element that has v among its row-set endpoints.
+// A thread per row gathers the candidates through the row set's incidence
+// (sg_incidence_build over sel_r) into a sorted local list.
+// ---------------------------------------------------------------------------
+namespace sg {
+namespace {
+
+constexpr int RECT_CAP = 64;  // columns of one row (DEV_ROW_TOO_LONG beyond)
+
+__device__ int rect_row(uint32_t v, const uint32_t *__restrict__ ve_ptr,
+                        const uint32_t *__restrict__ ve_idx, int32_t npos_r, int32_t npos_c,
+                        const int32_t *__restrict__ sel_c, int32_t nc, uint32_t *cols,
+                        int *err) {
+  int len = 0;
+  for (uint32_t q = ve_ptr[v]; q < ve_ptr[v + 1]; ++q) {
+    const uint32_t e = ve_idx[q] / (uint32_t)npos_r;
+    for (int j = 0; j < npos_c; ++j) {
+      const int32_t u = sel_c[(size_t)e * npos_c + j];
+      if (u < 0 || u >= nc) {
+        atomicCAS(err, 0, (int)DEV_BAD_ENDPOINT);
+        continue;
+      }
+      int pos = len;  // insertion into the sorted unique list
+      while (pos > 0 && cols[pos - 1] > (uint32_t)u) --pos;
+      if (pos > 0 && cols[pos - 1] == (uint32_t)u) continue;
+      if (len == RECT_CAP) {
+        atomicCAS(err, 0, (int)DEV_ROW_TOO_LONG);
+        return len;
+      }
+      for (int i = len; i > pos; --i) cols[i] = cols[i - 1];
+      cols[pos] = (uint32_t)u;
+      ++len;
+    }
+  }
+  return len;
+}
+
+__global__ void k_rect_count(int32_t nr, const uint32_t *__restrict__ ve_ptr,
+                             const uint32_t *__restrict__ ve_idx, int32_t npos_r,
+                             int32_t npos_c, const int32_t *__restrict__ sel_c, int32_t nc,
+                             uint32_t *__restrict__ cnt, int *err) {
+  uint32_t cols[RECT_CAP];
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nr;
+       v += (int64_t)gridDim.x * blockDim.x)
+    cnt[v] = (uint32_t)rect_row((uint32_t)v, ve_ptr, ve_idx, npos_r, npos_c, sel_c, nc, cols,
+                                err);
+}
+
+__global__ void k_rect_fill(int32_t nr, const uint32_t *__restrict__ ve_ptr,
+                            const uint32_t *__restrict__ ve_idx, int32_t npos_r, int32_t npos_c,
+                            const int32_t *__restrict__ sel_c, int32_t nc,
+                            const uint32_t *__restrict__ rowptr, uint32_t *__restrict__ colidx,
+                            int *err) {
+  uint32_t cols[RECT_CAP];
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nr;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int len = rect_row((uint32_t)v, ve_ptr, ve_idx, npos_r, npos_c, sel_c, nc, cols, err);
+    const uint32_t r0 = rowptr[v];
+    if ((int64_t)len != (int64_t)rowptr[v + 1] - r0) {
+      atomicCAS(err, 0, (int)DEV_SLOT_MISSING);
+      continue;
+    }
+    for (int i = 0; i < len; ++i) colidx[r0 + i] = cols[i];
+  }
+}
+
+// Row owner: zero the row, then for its listings (e ascending, then k) and
+// the element's column endpoints j, add block (e, k, j) into its slot.
+template <typename T>
+__global__ void k_rect_assemble(int32_t nr, const uint32_t *__restrict__ ve_ptr,
+                                const uint32_t *__restrict__ ve_idx, int32_t npos_r,
+                                int32_t npos_c, const int32_t *__restrict__ sel_c,
+                                const uint32_t *__restrict__ rowptr,
+                                const uint32_t *__restrict__ colidx, int bb,
+                                const T *__restrict__ eb, T *__restrict__ vals, int *err) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nr;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t r0 = rowptr[v], r1 = rowptr[v + 1];
+    for (size_t q = (size_t)r0 * bb; q < (size_t)r1 * bb; ++q) vals[q] = T(0);
+    for (uint32_t it = ve_ptr[v]; it < ve_ptr[v + 1]; ++it) {
+      const uint32_t t = ve_idx[it];  // e*npos_r + k
+      const uint32_t e = t / (uint32_t)npos_r;
+      for (int j = 0; j < npos_c; ++j) {
+        const uint32_t u = (uint32_t)sel_c[(size_t)e * npos_c + j];
+        uint32_t lo = r0, hi = r1;
+        while (lo < hi) {
+          const uint32_t m = lo + ((hi - lo) >> 1);
+          if (colidx[m] < u) lo = m + 1;
+          else hi = m;
+        }
+        if (lo == r1 || colidx[lo] != u) {
+          atomicCAS(err, 0, (int)DEV_SLOT_MISSING);
+          continue;
+        }
+        const T *b = eb + ((size_t)t * npos_c + j) * bb;
+        for (int w = 0; w < bb; ++w) vals[(size_t)lo * bb + w] += b[w];
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace sg
+
+extern "C" {
+
+int sg_pattern_rect(sg_ctx *h, int32_t nr, int32_t nc, int64_t nE, int32_t npos_r,
+                    int32_t npos_c, const int32_t *sel_c, const uint32_t *ve_ptr,
+                    const uint32_t *ve_idx, uint32_t *rowptr, uint32_t *colidx,
+                    int64_t *h_nnzb) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && rowptr && h_nnzb && ve_ptr, "sg_pattern_rect: null argument");
+  SG_REQUIRE(nr >= 0 && nc >= 0 && nE >= 0 && npos_r >= 1 && npos_r <= 16 && npos_c >= 1 &&
+                 npos_c <= 16,
+             "sg_pattern_rect: nr %d nc %d nE %lld npos %d/%d", nr, nc, (long long)nE, npos_r,
+             npos_c);
+  SG_REQUIRE(nE == 0 || (sel_c && ve_idx), "sg_pattern_rect: null array");
+  const int g = grid_for(c, nr, 128, 8);
+  if (!colidx) {  // count pass: rowptr and nnzb
+    Scratch s(c);
+    SG_TRY(s.reserve(Scratch::bytes_for((size_t)nr + 1, 4) + scan_scratch_bytes(nr) + 512));
+    uint32_t *cnt = s.alloc<uint32_t>((size_t)nr + 1);
+    if (nr > 0) {
+      k_rect_count<<<g, 128, 0, c->stream>>>(nr, ve_ptr, ve_idx, npos_r, npos_c, sel_c, nc, cnt,
+                                            c->d_err);
+      SG_CHECK_LAUNCH();
+    }
+    SG_TRY(exclusive_scan_u32(c, s, cnt, rowptr, nr));
+    SG_TRY(check_device_error(c, "sg_pattern_rect"));
+    uint32_t tot = 0;
+    SG_CHECK_CUDA(cudaMemcpyAsync(&tot, rowptr + nr, 4, cudaMemcpyDeviceToHost, c->stream));
+    SG_CHECK_CUDA(cudaStreamSynchronize(c->stream));
+    *h_nnzb = tot;
+    return SG_OK;
+  }
+  if (nr > 0) {
+    k_rect_fill<<<g, 128, 0, c->stream>>>(nr, ve_ptr, ve_idx, npos_r, npos_c, sel_c, nc, rowptr,
+                                         colidx, c->d_err);
+    SG_CHECK_LAUNCH();
+  }
+  return check_device_error(c, "sg_pattern_rect");
+}
+
+int sg_assemble_rect(sg_ctx *h, int32_t nr, int32_t npos_r, int32_t npos_c,
+                     const int32_t *sel_c, const uint32_t *ve_ptr, const uint32_t *ve_idx,
+                     const uint32_t *rowptr, const uint32_t *colidx, int dtype, int32_t bs,
+                     const void *eb, void *vals) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && ve_ptr && rowptr, "sg_assemble_rect: null argument");
+  SG_REQUIRE(nr >= 0 && npos_r >= 1 && npos_r <= 16 && npos_c >= 1 && npos_c <= 16 && bs >= 1 &&
+                 bs <= 4,
+             "sg_assemble_rect: nr %d npos %d/%d bs %d", nr, npos_r, npos_c, bs);
+  SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, "sg_assemble_rect: dtype %d", dtype);
+  if (nr == 0) return SG_OK;
+  const int g = grid_for(c, nr, 128, 8);
+  if (dtype == SG_F64)
+    k_rect_assemble<double><<<g, 128, 0, c->stream>>>(nr, ve_ptr, ve_idx, npos_r, npos_c, sel_c,
+                                                     rowptr, colidx, bs * bs,
+                                                     (const double *)eb, (double *)vals,
+                                                     c->d_err);
+  else
+    k_rect_assemble<float><<<g, 128, 0, c->stream>>>(nr, ve_ptr, ve_idx, npos_r, npos_c, sel_c,
+                                                    rowptr, colidx, bs * bs, (const float *)eb,
+                                                    (float *)vals, c->d_err);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+}  // extern "C"

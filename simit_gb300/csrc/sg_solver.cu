@@ -47,12 +47,21 @@ __global__ void __launch_bounds__(RED_T) k_prec_dot(int64_t len, const VT *__res
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v * 3 < len;
          v += (int64_t)gridDim.x * blockDim.x) {
       const VT r0 = r[v * 3], r1 = r[v * 3 + 1], r2 = r[v * 3 + 2];
-      const VT *D = dinv + v * 9;
+      VT zz[3];
+      if (sizeof(VT) == 4) {  // mixed: packed symmetric inverse (k_diag_inv PACK6)
+        const VT *m = dinv + v * 6;
+        zz[0] = m[0] * r0 + m[1] * r1 + m[2] * r2;
+        zz[1] = m[1] * r0 + m[3] * r1 + m[4] * r2;
+        zz[2] = m[2] * r0 + m[4] * r1 + m[5] * r2;
+      } else {
+        const VT *D = dinv + v * 9;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) zz[k] = D[k * 3] * r0 + D[k * 3 + 1] * r1 + D[k * 3 + 2] * r2;
+      }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const VT zk = D[k * 3] * r0 + D[k * 3 + 1] * r1 + D[k * 3 + 2] * r2;
-        z[v * 3 + k] = zk;
-        acc += (double)r[v * 3 + k] * (double)zk;
+        z[v * 3 + k] = zz[k];
+        acc += (double)r[v * 3 + k] * (double)zz[k];
       }
     }
   } else {
@@ -649,15 +658,15 @@ int refresh_matrix(Solver *S) {
   if (S->prec == PK_JACOBI || S->prec == PK_BLOCK3) {
     const int blk = S->prec == PK_BLOCK3;
     const int g = grid_for(c, A->n, 256, 8);
-    if (vt == 4) {
+    if (vt == 4) {  // mixed: block inverses packed as 6 values (K2 and k_prec_dot read them so)
       if (A->dtype == SG_F64)
-        k_diag_inv<double, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
-                                                            (const double *)A->vals,
-                                                            (float *)S->dinv, blk, c->d_err);
+        k_diag_inv<double, float, true><<<g, 256, 0, c->stream>>>(
+            A->n, A->bs, A->rowptr, A->colidx, (const double *)A->vals, (float *)S->dinv, blk,
+            c->d_err);
       else
-        k_diag_inv<float, float><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,
-                                                           (const float *)A->vals,
-                                                           (float *)S->dinv, blk, c->d_err);
+        k_diag_inv<float, float, true><<<g, 256, 0, c->stream>>>(
+            A->n, A->bs, A->rowptr, A->colidx, (const float *)A->vals, (float *)S->dinv, blk,
+            c->d_err);
     } else {
       if (A->dtype == SG_F64)
         k_diag_inv<double, double><<<g, 256, 0, c->stream>>>(A->n, A->bs, A->rowptr, A->colidx,

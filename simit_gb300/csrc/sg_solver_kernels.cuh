@@ -369,6 +369,8 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
                                                         float *__restrict__ z,
                                                         const float *__restrict__ dinv,
                                                         double *__restrict__ part_out) {
+  // FP32 block Jacobi runs k_cg_update_w, whose inverse blocks are packed
+  static_assert(PREC != PK_BLOCK3, "FP32 block Jacobi: use k_cg_update_w");
   __shared__ double sh[33];
   if (ctl->status != ST_RUNNING) return;
   const double pq = pq_fin ? ctl->pq_tot : sum_parts(part_in, np1, sh);
@@ -477,7 +479,8 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
 
 // K2 for FP32 vectors and 3x3 block Jacobi with warp-staged, fully coalesced
 // accesses.  A warp takes 128 vertices at a time: it loads the chunk of
-// p, q, r, x (96 float4 each) and of D^-1 (288 float4) with lane-consecutive
+// p, q, r, x (96 float4 each) and of the packed symmetric D^-1 (6 values per
+// vertex, k_diag_inv PACK6: 192 float4) with lane-consecutive
 // 16-byte loads into its shared-memory slice, each lane then reads its four
 // vertices (3 and 9 consecutive float4, conflict-free), and the results go
 // back through shared memory to lane-consecutive stores.  Same arithmetic,
@@ -485,7 +488,7 @@ __global__ void __launch_bounds__(RED_T, 3) k_cg_update_v4(SolveCtl *ctl, int pa
 // len % 12 entries are done by the scalar tail of thread 0 of the last CTA.
 constexpr int K2W_WARPS = 8;
 struct K2WarpSmem {
-  float4 p[96], q[96], r[96], x[96], d[288];
+  float4 p[96], q[96], r[96], x[96], d[192];
 };
 
 template <bool FIN>
@@ -520,7 +523,7 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
   DotAcc<float> rr, rzs, zq;
   for (int64_t c = (int64_t)blockIdx.x * K2W_WARPS + (threadIdx.x >> 5); c < nchunks;
        c += (int64_t)gridDim.x * K2W_WARPS) {
-    const int64_t f0 = c * 96, d0 = c * 288;
+    const int64_t f0 = c * 96, d0 = c * 192;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       const int64_t f = f0 + lane + 32 * j;
@@ -532,13 +535,13 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
       }
     }
 #pragma unroll
-    for (int j = 0; j < 9; ++j) {
+    for (int j = 0; j < 6; ++j) {
       const int64_t f = d0 + lane + 32 * j;
-      if (f < nf * 3) w.d[lane + 32 * j] = d4[f];
+      if (f < nf * 2) w.d[lane + 32 * j] = d4[f];
     }
     __syncwarp();
     const bool mine = c * 32 + lane < nu;
-    float pv[12], qv[12], rv[12], xv[12], zv[12], dv[36];
+    float pv[12], qv[12], rv[12], xv[12], zv[12], dv[24];
     if (mine) {
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
@@ -550,8 +553,8 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
         xv[4 * j] = e4.x; xv[4 * j + 1] = e4.y; xv[4 * j + 2] = e4.z; xv[4 * j + 3] = e4.w;
       }
 #pragma unroll
-      for (int j = 0; j < 9; ++j) {
-        const float4 g4 = w.d[9 * lane + j];
+      for (int j = 0; j < 6; ++j) {
+        const float4 g4 = w.d[6 * lane + j];
         dv[4 * j] = g4.x; dv[4 * j + 1] = g4.y; dv[4 * j + 2] = g4.z; dv[4 * j + 3] = g4.w;
       }
 #pragma unroll
@@ -560,11 +563,12 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
         rv[k] = rv[k] - a * qv[k];
       }
 #pragma unroll
-      for (int v = 0; v < 4; ++v)
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-          zv[v * 3 + k] = dv[v * 9 + k * 3] * rv[v * 3] + dv[v * 9 + k * 3 + 1] * rv[v * 3 + 1] +
-                          dv[v * 9 + k * 3 + 2] * rv[v * 3 + 2];
+      for (int v = 0; v < 4; ++v) {  // symmetric inverse, upper triangle
+        const float *m = dv + v * 6, *rq = rv + v * 3;
+        zv[v * 3 + 0] = m[0] * rq[0] + m[1] * rq[1] + m[2] * rq[2];
+        zv[v * 3 + 1] = m[1] * rq[0] + m[3] * rq[1] + m[4] * rq[2];
+        zv[v * 3 + 2] = m[2] * rq[0] + m[4] * rq[1] + m[5] * rq[2];
+      }
 #pragma unroll
       for (int k = 0; k < 12; ++k) {
         rr.add(rv[k], rv[k]);
@@ -603,9 +607,12 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
         rv[k] = r[i] - a * q[i];
         r[i] = rv[k];
       }
-      const float *D = dinv + (i0 / 3) * 9;
+      const float *m = dinv + (i0 / 3) * 6;
+      const float zz[3] = {m[0] * rv[0] + m[1] * rv[1] + m[2] * rv[2],
+                           m[1] * rv[0] + m[3] * rv[1] + m[4] * rv[2],
+                           m[2] * rv[0] + m[4] * rv[1] + m[5] * rv[2]};
       for (int k = 0; k < 3; ++k) {
-        const float zk = D[k * 3] * rv[0] + D[k * 3 + 1] * rv[1] + D[k * 3 + 2] * rv[2];
+        const float zk = zz[k];
         z[i0 + k] = zk;
         rr.add(rv[k], rv[k]);
         rzs.add(rv[k], zk);
@@ -862,8 +869,11 @@ __global__ void k_true_residual_any(int32_t n, int32_t bs, const uint32_t *__res
 }
 
 // Point-Jacobi inverse diagonal (VT) from the diagonal blocks; bs3 = 1 also
-// writes the inverted 3x3 diagonal blocks (block Jacobi).
-template <typename MT, typename VT>
+// writes the inverted 3x3 diagonal blocks (block Jacobi).  PACK6: the block
+// inverse symmetrised ((M + M^T) / 2 in FP64) and stored as its upper
+// triangle m00 m01 m02 m11 m12 m22, 6 values per vertex (the mixed solver's
+// layout: a third fewer bytes per K2, and an exactly symmetric M).
+template <typename MT, typename VT, bool PACK6 = false>
 __global__ void k_diag_inv(int32_t n, int32_t bs, const uint32_t *__restrict__ rowptr,
                            const uint32_t *__restrict__ colidx, const MT *__restrict__ vals,
                            VT *__restrict__ dinv, int block3, int *err) {
@@ -875,9 +885,10 @@ __global__ void k_diag_inv(int32_t n, int32_t bs, const uint32_t *__restrict__ r
       uint32_t mid = (lo + hi) >> 1;
       if (colidx[mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
     }
+    const int per = block3 ? (PACK6 ? 6 : 9) : bs;
     if (lo >= end || colidx[lo] != (uint32_t)v) {
       atomicCAS(err, 0, 5 /* DEV_NO_DIAGONAL */);
-      for (int k = 0; k < (block3 ? 9 : bs); ++k) dinv[v * (block3 ? 9 : bs) + k] = VT(0);
+      for (int k = 0; k < per; ++k) dinv[v * per + k] = VT(0);
       continue;
     }
     const MT *D = vals + (size_t)lo * bs * bs;
@@ -893,16 +904,27 @@ __global__ void k_diag_inv(int32_t n, int32_t bs, const uint32_t *__restrict__ r
                    c02 = a[3] * a[7] - a[4] * a[6];
       const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
       if (det == 0.0 || !isfinite(det)) {  // singular block: fall back to point Jacobi
-        for (int k = 0; k < 9; ++k) dinv[v * 9 + k] = VT(0);
+        for (int k = 0; k < per; ++k) dinv[v * per + k] = VT(0);
         for (int k = 0; k < 3; ++k)
-          dinv[v * 9 + k * 4] = a[k * 4] != 0.0 ? (VT)(1.0 / a[k * 4]) : VT(0);
+          dinv[v * per + (PACK6 ? (k == 0 ? 0 : (k == 1 ? 3 : 5)) : k * 4)] =
+              a[k * 4] != 0.0 ? (VT)(1.0 / a[k * 4]) : VT(0);
         continue;
       }
       const double id = 1.0 / det;
       const double inv[9] = {c00 * id, (a[2] * a[7] - a[1] * a[8]) * id, (a[1] * a[5] - a[2] * a[4]) * id,
                              c01 * id, (a[0] * a[8] - a[2] * a[6]) * id, (a[2] * a[3] - a[0] * a[5]) * id,
                              c02 * id, (a[1] * a[6] - a[0] * a[7]) * id, (a[0] * a[4] - a[1] * a[3]) * id};
-      for (int k = 0; k < 9; ++k) dinv[v * 9 + k] = (VT)inv[k];
+      if (PACK6) {
+        VT *m = dinv + v * 6;
+        m[0] = (VT)inv[0];
+        m[1] = (VT)(0.5 * (inv[1] + inv[3]));
+        m[2] = (VT)(0.5 * (inv[2] + inv[6]));
+        m[3] = (VT)inv[4];
+        m[4] = (VT)(0.5 * (inv[5] + inv[7]));
+        m[5] = (VT)inv[8];
+      } else {
+        for (int k = 0; k < 9; ++k) dinv[v * 9 + k] = (VT)inv[k];
+      }
     }
   }
 }

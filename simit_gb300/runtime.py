@@ -219,6 +219,50 @@ class IncidenceMatrix:
         return bspmv(self.ctx, self.rows, bs, self.rowptr, self.colidx, vals, x)
 
 
+class RectMatrix:
+    """matrix[Vr, Vc] of `map f to E` for an edge set over two vertex sets
+    (sg_pattern_rect): sel_r [nE*npos_r] / sel_c [nE*npos_c] are each
+    element's endpoints in the row and column sets; nr, nc their sizes."""
+
+    def __init__(self, ctx, nr, nc, sel_r, npos_r, sel_c, npos_c):
+        d = ctx.device
+        self.ctx, self.nr, self.nc, self.npos_r, self.npos_c = ctx, nr, nc, npos_r, npos_c
+        with ctx.stream():
+            self.sel_r = torch.as_tensor(np.ascontiguousarray(sel_r, np.int32)).to(d)
+            self.sel_c = torch.as_tensor(np.ascontiguousarray(sel_c, np.int32)).to(d)
+        self.nE = self.sel_r.numel() // npos_r
+        assert self.sel_c.numel() == self.nE * npos_c
+        with ctx.stream():
+            self.ve_ptr = torch.empty(nr + 1, dtype=torch.int32, device=d)
+            self.ve_idx = torch.empty(max(1, self.nE * npos_r), dtype=torch.int32, device=d)
+            self.rowptr = torch.empty(nr + 1, dtype=torch.int32, device=d)
+        call("sg_incidence_build", ctx.h, nr, ptr(self.sel_r), self.nE, npos_r, ptr(self.ve_ptr),
+             ptr(self.ve_idx))
+        nnzb = ctypes.c_int64()
+        args = (ctx.h, nr, nc, self.nE, npos_r, npos_c, ptr(self.sel_c), ptr(self.ve_ptr),
+                ptr(self.ve_idx), ptr(self.rowptr))
+        call("sg_pattern_rect", *args, None, ctypes.byref(nnzb))
+        self.nnzb = nnzb.value
+        with ctx.stream():
+            self.colidx = torch.empty(max(1, self.nnzb), dtype=torch.int32, device=d)
+        call("sg_pattern_rect", *args, ptr(self.colidx), ctypes.byref(nnzb))
+
+    def assemble(self, eb, bs, dtype=torch.float64):
+        """Values [nnzb*bs*bs] from blocks eb [nE, npos_r, npos_c, bs, bs]."""
+        with self.ctx.stream():
+            eb = _d(eb, dtype, self.ctx.device)
+            vals = torch.empty(max(1, self.nnzb * bs * bs), dtype=dtype, device=self.ctx.device)
+        call("sg_assemble_rect", self.ctx.h, self.nr, self.npos_r, self.npos_c, ptr(self.sel_c),
+             ptr(self.ve_ptr), ptr(self.ve_idx), ptr(self.rowptr), ptr(self.colidx),
+             dtype_code(vals), int(bs), ptr(eb), ptr(vals))
+        return vals
+
+    def spmv(self, bs, vals, x):
+        if x.numel() != self.nc * bs:
+            raise ValueError("rect spmv: x needs %d entries" % (self.nc * bs))
+        return bspmv(self.ctx, self.nr, bs, self.rowptr, self.colidx, vals, x)
+
+
 def dot(ctx, a, b):
     out = ctypes.c_double()
     call("sg_dot", ctx.h, a.numel(), dtype_code(a), ptr(a), ptr(b), ctypes.byref(out))

@@ -115,7 +115,8 @@ def main():
                                                    "gemv_blocked_computed"),
         "matrix_vv": extract_assert_eq(os.path.join(test, "assembly-tests.cpp"), "matrix_vv"),
     }
-    for name in ("matrix_ve", "matrix_ev", "matrix_ve_heterogeneous", "matrix_ev_heterogeneous"):
+    for name in ("matrix_ve", "matrix_ev", "matrix_ve_heterogeneous", "matrix_ev_heterogeneous",
+                 "matrix_vv_heterogeneous"):
         golden["incidence_" + name] = extract_incidence_asserts(
             os.path.join(test, "assembly-tests.cpp"), name)
     with open(os.path.join(HERE, "reference_golden.json"), "w") as f:

@@ -186,3 +186,20 @@ def incidence_scenarios():
                 "matrix_ev_heterogeneous V0"))
     out.append((0, 9, v1, 4, w1, np.arange(1.0, 10.0), ga[4:], "matrix_ev_heterogeneous V1"))
     return out
+
+
+def rect_scenarios():
+    """matrix_vv_heterogeneous of test/assembly-tests.cpp
+    (test/input/assembly/matrix_vv_heterogeneous.sim): over
+    Set E(V1,V1,V0,V1,V1), A01 = matrix[V0,V1] with Ae(v0, vk) = k and
+    A10 = matrix[V1,V0] with Ae(vk, v0) = k (k = 1..4); V0.b = A01 * V1.a and
+    V1.b = A10 * V0.a with a = i + 1.  Items: (nr, nc, sel_r, npos_r, sel_c,
+    npos_c, blocks [nE, npos_r, npos_c], vector, expected, name)."""
+    g = _golden_map()["incidence_matrix_vv_heterogeneous"]["vectors"]
+    het = np.array([[0, 1, 0, 3, 4], [1, 2, 1, 4, 5], [3, 4, 2, 6, 7], [4, 5, 3, 7, 8]])
+    v0, v1 = het[:, [2]], het[:, [0, 1, 3, 4]]
+    w = np.array([1.0, 2.0, 3.0, 4.0])
+    return [(4, 9, v0, 1, v1, 4, np.tile(w, (4, 1)).reshape(4, 1, 4), np.arange(1.0, 10.0),
+             g["b0Expected"], "A01 * V1.a"),
+            (9, 4, v1, 4, v0, 1, np.tile(w, (4, 1)).reshape(4, 4, 1), np.arange(1.0, 5.0),
+             g["b1Expected"], "A10 * V0.a")]

@@ -173,3 +173,41 @@ def test_incidence_random_repeats(ctx, oracle, kind, bs):
     yr = oracle.spmv(len(rp) - 1, bs, rp, ci, ref, x)
     sc = oracle.spmv(len(rp) - 1, bs, rp, ci, np.abs(ref), np.abs(x))
     assert np.all(np.abs(y.cpu().numpy() - yr) <= 1e-14 * sc + 1e-300)
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_rect_matrix_golden_gpu(ctx, oracle, case):
+    """matrix_vv_heterogeneous: the rectangular pattern, its values and
+    A * field on the GPU against the oracle and the reference's results."""
+    from simit_gb300.runtime import RectMatrix
+    from tests import scenarios
+    nr, nc, sr, npr, sc, npc, eb, vec, expected, name = scenarios.rect_scenarios()[case]
+    M = RectMatrix(ctx, nr, nc, sr.reshape(-1), npr, sc.reshape(-1), npc)
+    vals = M.assemble(eb, 1)
+    y = M.spmv(1, vals, torch.tensor(vec, dtype=torch.float64, device=ctx.device))
+    ctx.sync()
+    rp, ci = oracle.rect_pattern(nr, sr, npr, sc, npc)
+    assert np.array_equal(M.rowptr.cpu().numpy().view(np.uint32), rp)
+    assert np.array_equal(M.colidx[:M.nnzb].cpu().numpy().view(np.uint32), ci)
+    assert np.array_equal(vals[:M.nnzb].cpu().numpy(),
+                          oracle.assemble_rect(sr, npr, sc, npc, 1, eb, rp, ci))
+    assert y.cpu().numpy().tolist() == [float(v) for v in expected], name
+
+
+def test_rect_matrix_random(ctx, oracle):
+    """Random two-set edge set (3 row-set and 2 column-set endpoints, with
+    repeats), 3x3 FP64 blocks: pattern and values bit-exact with the oracle."""
+    from simit_gb300.runtime import RectMatrix
+    g = meshgen.rng(77)
+    nr, nc, nE = 200, 150, 600
+    sr = g.integers(0, nr, size=(nE, 3))
+    sc = g.integers(0, nc, size=(nE, 2))
+    sr[::7, 1] = sr[::7, 0]
+    eb = g.uniform(-1, 1, size=(nE, 3, 2, 3, 3))
+    M = RectMatrix(ctx, nr, nc, sr.reshape(-1), 3, sc.reshape(-1), 2)
+    vals = M.assemble(eb, 3)
+    ctx.sync()
+    rp, ci = oracle.rect_pattern(nr, sr, 3, sc, 2)
+    assert np.array_equal(M.colidx[:M.nnzb].cpu().numpy().view(np.uint32), ci)
+    ref = oracle.assemble_rect(sr, 3, sc, 2, 3, eb, rp, ci)
+    assert np.array_equal(vals[:M.nnzb * 9].cpu().numpy(), ref)

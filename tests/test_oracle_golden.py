@@ -158,3 +158,14 @@ def test_incidence_matrices_golden(oracle, case):
     rows = len(rp) - 1
     y = oracle.spmv(rows, 1, rp, ci, vals, vec)
     assert y.tolist() == [float(v) for v in expected], name
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_rect_matrix_golden(oracle, case):
+    """∃e.(v0-e ∧ e-v1) between two vertex sets (the oracle's restatement)
+    reproduces test/assembly-tests.cpp's matrix_vv_heterogeneous results."""
+    nr, nc, sr, npr, sc, npc, eb, vec, expected, name = scenarios.rect_scenarios()[case]
+    rp, ci = oracle.rect_pattern(nr, sr, npr, sc, npc)
+    vals = oracle.assemble_rect(sr, npr, sc, npc, 1, eb, rp, ci)
+    y = oracle.spmv(nr, 1, rp, ci, vals, vec)
+    assert y.tolist() == [float(v) for v in expected], name
