@@ -27,6 +27,15 @@ __global__ void k_cast_r(int64_t len, const double *__restrict__ rhi, VT *__rest
     r[i] = (VT)rhi[i];
 }
 
+// x += a p: the last iteration's update when K2 stopped the batch and K3,
+// which applies it otherwise, returned early.
+__global__ void k_x_pending(int64_t len, float a, const float *__restrict__ p,
+                            float *__restrict__ x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = x[i] + a * p[i];
+}
+
 template <typename XT>
 __global__ void k_add_lo(int64_t len, double *__restrict__ xhi, XT *__restrict__ xlo) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
@@ -167,13 +176,14 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
         static bool attr[SG_MAX_DEVICES] = {};
         const size_t sm = K2W_WARPS * sizeof(K2WarpSmem);
         if (first_on_device(attr, S->c->device))
-          SG_CHECK_CUDA(cudaFuncSetAttribute(k_cg_update_w<true>,
+          SG_CHECK_CUDA(cudaFuncSetAttribute(k_cg_update_w<true, false>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         const int64_t nchunks = (S->len / 12 + 31) / 32;
         int64_t grid = (nchunks + K2W_WARPS - 1) / K2W_WARPS;
         if (grid > 2 * (int64_t)S->c->num_sms) grid = 2 * (int64_t)S->c->num_sms;
         if (grid < 1) grid = 1;
-        SG_CHECK_CUDA(launch_k(S->c, k_cg_update_w<true>, (int)grid, K2W_WARPS * 32, sm, st,
+        S->k3_xupd = 1;  // x += alpha p moves to K3
+        SG_CHECK_CUDA(launch_k(S->c, k_cg_update_w<true, false>, (int)grid, K2W_WARPS * 32, sm, st,
                                S->ctl, par, S->len, (const double *)S->part1, S->P1, S->tma,
                                (const float *)S->p, (const float *)S->q, (float *)S->r,
                                (float *)S->xupd, (float *)S->z, (const float *)S->dinv,
@@ -213,7 +223,7 @@ static int launch_k3(Solver *S, cudaStream_t st, int par) {
   if (sizeof(VT) == 4)  // K2 decided unless an external preconditioner ran after it
     SG_CHECK_CUDA(launch_k(S->c, k_cg_direction_v4, S->P2, RED_T, 0, st, S->ctl, par, S->len,
                            (const double *)S->part2, S->P2, (int)(S->prec != PK_EXTERNAL),
-                           (const float *)z, (float *)S->p));
+                           (const float *)z, (float *)S->p, (float *)S->xupd, S->k3_xupd));
   else
     k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z,
                                                 (VT *)S->p);
@@ -450,6 +460,13 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
       }
     }
     exact = false;  // x moved since the last residual
+    if (S->k3_xupd && (h->status == ST_NEED_CHECK || h->status == ST_MAXITER)) {
+      // K2 updated r with alpha and stopped the batch; K3 returned early
+      k_x_pending<<<S->P2, RED_T, 0, st>>>(S->len, (float)h->last_alpha, (const float *)S->p,
+                                           (float *)S->xupd);
+      SG_CHECK_LAUNCH();
+      S->launches += 1;
+    }
     // the slot K3 wrote last holds the larger iteration count
     const int cur = h->iter[1] > h->iter[0] ? 1 : 0;
     iters = h->iter[cur];

@@ -44,6 +44,7 @@ struct Solver {
   void (*ext_free)(Solver *) = nullptr;
   void *ext = nullptr;
   SymBsr *sym = nullptr;  // SG_STORAGE_SYMMETRIC: K1 reads the upper half
+  int k3_xupd = 0;        // K3 applies x += alpha p (K2 = k_cg_update_w without x)
 };
 
 int default_lanes(int32_t n, int64_t nnzb, int32_t bs);

@@ -491,7 +491,9 @@ struct K2WarpSmem {
   float4 p[96], q[96], r[96], x[96], d[192];
 };
 
-template <bool FIN>
+// XUPD = false: x += alpha p is left to K3 (k_cg_direction_v4 with xupd), so
+// this kernel neither reads p and x nor writes x.
+template <bool FIN, bool XUPD = true>
 __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
     SolveCtl *ctl, int par, int64_t len, const double *__restrict__ part_in, int np1,
     int pq_fin, const float *__restrict__ p, const float *__restrict__ q, float *__restrict__ r,
@@ -528,10 +530,10 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
     for (int j = 0; j < 3; ++j) {
       const int64_t f = f0 + lane + 32 * j;
       if (f < nf) {
-        w.p[lane + 32 * j] = p4[f];
+        if (XUPD) w.p[lane + 32 * j] = p4[f];
         w.q[lane + 32 * j] = q4[f];
         w.r[lane + 32 * j] = r4[f];
-        w.x[lane + 32 * j] = x4[f];
+        if (XUPD) w.x[lane + 32 * j] = x4[f];
       }
     }
 #pragma unroll
@@ -545,12 +547,14 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
     if (mine) {
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const float4 a4 = w.p[3 * lane + j], b4 = w.q[3 * lane + j], c4 = w.r[3 * lane + j],
-                     e4 = w.x[3 * lane + j];
-        pv[4 * j] = a4.x; pv[4 * j + 1] = a4.y; pv[4 * j + 2] = a4.z; pv[4 * j + 3] = a4.w;
+        const float4 b4 = w.q[3 * lane + j], c4 = w.r[3 * lane + j];
         qv[4 * j] = b4.x; qv[4 * j + 1] = b4.y; qv[4 * j + 2] = b4.z; qv[4 * j + 3] = b4.w;
         rv[4 * j] = c4.x; rv[4 * j + 1] = c4.y; rv[4 * j + 2] = c4.z; rv[4 * j + 3] = c4.w;
-        xv[4 * j] = e4.x; xv[4 * j + 1] = e4.y; xv[4 * j + 2] = e4.z; xv[4 * j + 3] = e4.w;
+        if (XUPD) {
+          const float4 a4 = w.p[3 * lane + j], e4 = w.x[3 * lane + j];
+          pv[4 * j] = a4.x; pv[4 * j + 1] = a4.y; pv[4 * j + 2] = a4.z; pv[4 * j + 3] = a4.w;
+          xv[4 * j] = e4.x; xv[4 * j + 1] = e4.y; xv[4 * j + 2] = e4.z; xv[4 * j + 3] = e4.w;
+        }
       }
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
@@ -559,7 +563,7 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
       }
 #pragma unroll
       for (int k = 0; k < 12; ++k) {
-        xv[k] = xv[k] + a * pv[k];
+        if (XUPD) xv[k] = xv[k] + a * pv[k];
         rv[k] = rv[k] - a * qv[k];
       }
 #pragma unroll
@@ -580,7 +584,8 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
     if (mine) {
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        w.x[3 * lane + j] = make_float4(xv[4 * j], xv[4 * j + 1], xv[4 * j + 2], xv[4 * j + 3]);
+        if (XUPD)
+          w.x[3 * lane + j] = make_float4(xv[4 * j], xv[4 * j + 1], xv[4 * j + 2], xv[4 * j + 3]);
         w.r[3 * lane + j] = make_float4(rv[4 * j], rv[4 * j + 1], rv[4 * j + 2], rv[4 * j + 3]);
         w.p[3 * lane + j] = make_float4(zv[4 * j], zv[4 * j + 1], zv[4 * j + 2], zv[4 * j + 3]);
       }
@@ -590,7 +595,7 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
     for (int j = 0; j < 3; ++j) {
       const int64_t f = f0 + lane + 32 * j;
       if (f < nf) {
-        x4[f] = w.x[lane + 32 * j];
+        if (XUPD) x4[f] = w.x[lane + 32 * j];
         r4[f] = w.r[lane + 32 * j];
         z4[f] = w.p[lane + 32 * j];
       }
@@ -603,7 +608,7 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
       float rv[3];
       for (int k = 0; k < 3; ++k) {
         const int64_t i = i0 + k;
-        x[i] = x[i] + a * p[i];
+        if (XUPD) x[i] = x[i] + a * p[i];
         rv[k] = r[i] - a * q[i];
         r[i] = rv[k];
       }
@@ -639,28 +644,43 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
 // K3 for FP32 vectors: the control decisions of k_cg_direction, then
 // p = z + beta p with float4 accesses.
 // fin: K2 already took the decision and left beta in ctl->beta.
+// xupd (with fin): K2 left x += alpha p to this kernel, which applies it with
+// the direction it is about to replace; when K2 stopped the batch, the host
+// applies that last update instead (the early return below).
 static __global__ void __launch_bounds__(RED_T) k_cg_direction_v4(SolveCtl *ctl, int par, int64_t len,
                                                            const double *__restrict__ part_in,
                                                            int np2, int fin,
                                                            const float *__restrict__ z,
-                                                           float *__restrict__ p) {
+                                                           float *__restrict__ p,
+                                                           float *__restrict__ x, int xupd) {
   __shared__ double sh[33];
   pdl_wait_and_release();
   if (ctl->status != ST_RUNNING) return;
   if (fin) {
     const float b = (float)ctl->beta;
+    const float a = (float)ctl->last_alpha;
     const int64_t nu = len / 4;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu;
          u += (int64_t)gridDim.x * blockDim.x) {
       float zv[4], pv[4];
       ld4(z, u, zv);
       ld4(p, u, pv);
+      if (xupd) {
+        float xv[4];
+        ld4(x, u, xv);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) xv[k] = xv[k] + a * pv[k];
+        st4(x, u, xv);
+      }
 #pragma unroll
       for (int k = 0; k < 4; ++k) pv[k] = zv[k] + b * pv[k];
       st4(p, u, pv);
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
-      for (int64_t i = nu * 4; i < len; ++i) p[i] = z[i] + b * p[i];
+      for (int64_t i = nu * 4; i < len; ++i) {
+        if (xupd) x[i] = x[i] + a * p[i];
+        p[i] = z[i] + b * p[i];
+      }
     return;
   }
   const double rr = sum_parts(part_in, np2, sh);
