@@ -88,7 +88,8 @@ template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfi
 // values at part, part + gridDim.x, ...): every CTA stores its partials and
 // takes a ticket; the CTA that takes the last ticket sums each array in index
 // order (so the totals are deterministic), stores them in tot[0..nv) and
-// re-arms the ticket.  Returns true in that CTA.  Called by all threads.
+// re-arms the ticket.  Returns true in that CTA.  Called by all threads;
+// nv <= 3.
 __device__ __forceinline__ bool finalize_partials(const double *t, int nv, double *part,
                                                   unsigned int *ticket, double *tot,
                                                   double *sh) {
@@ -101,11 +102,17 @@ __device__ __forceinline__ bool finalize_partials(const double *t, int nv, doubl
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  for (int k = 0; k < nv; ++k) {
-    double a = 0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
-      a += __ldcg(part + k * gridDim.x + i);
-    const double s = block_sum(a, sh);
+  // all nv arrays loaded in one pass (the last CTA works alone here, so its
+  // load latency is the kernel's tail), then reduced one after the other
+  double a[3] = {0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (k < nv) a[k] += __ldcg(part + k * gridDim.x + i);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (k >= nv) break;
+    const double s = block_sum(a[k], sh);
     if (threadIdx.x == 0) tot[k] = s;
   }
   if (threadIdx.x == 0) *ticket = 0;

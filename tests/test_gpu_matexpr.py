@@ -211,3 +211,31 @@ def test_rect_matrix_random(ctx, oracle):
     assert np.array_equal(M.colidx[:M.nnzb].cpu().numpy().view(np.uint32), ci)
     ref = oracle.assemble_rect(sr, 3, sc, 2, 3, eb, rp, ci)
     assert np.array_equal(vals[:M.nnzb * 9].cpu().numpy(), ref)
+
+
+def test_cg_sim_unfused_matches_golden(ctx):
+    """test/input/program/cg.sim as written: K from the scalar springs map
+    alone, then A = I - 0.01 K as the matrix expression, CG from 0 — the
+    values of test/program-cg-test.cpp, and bit-equal to the fused map."""
+    from simit_gb300 import _lib
+    from simit_gb300.runtime import Mesh, Solver, assemble_scalar_springs, solve_opts
+    from tests import scenarios
+    s = scenarios.cg_chain()
+    mesh = Mesh(ctx, s["n"], s["ep"], 2)
+    p = mesh.pattern
+    fused = assemble_scalar_springs(mesh, s["a"], s["diag"], s["scale"])
+    K = assemble_scalar_springs(mesh, s["a"], 0.0, 1.0)
+    from simit_gb300.runtime import bsr_add_diag
+    A = bsr_add_diag(ctx, s["n"], 1, p.rowptr, p.colidx, K, ident=s["diag"], scale=s["scale"])
+    ctx.sync()
+    assert torch.equal(A, fused)
+    b = torch.tensor(s["b"], device=ctx.device)
+    opts = solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_NORMR,
+                      tol=s["tol"], maxiters=s["maxiters"], verify=0)
+    S = Solver(ctx, mesh.n, 1, p.rowptr, p.colidx, A, mesh.nnzb, opts)
+    c = torch.zeros_like(b)
+    S.solve(b, c)
+    S.close()
+    for g in scenarios.golden("cg"):
+        got = scenarios.golden_lookup(g, {"c": c.cpu().numpy()})
+        assert abs(got - g["expected"]) <= 1e-13, (g, got)
