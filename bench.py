@@ -743,6 +743,25 @@ def run_ours(args, rank, world, local):
     achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
 
+    # --- the step's assembly alone (stiffness map in place + force map) ----
+    # algorithmic bytes: element ids and parameters (B 9, W, mu, lam) once,
+    # vertex positions once, the matrix values and the force written once
+    nE = m.nE
+    for _ in range(2):
+        prob.assemble_in_place()
+    a0 = torch.cuda.Event(enable_timing=True)
+    a1 = torch.cuda.Event(enable_timing=True)
+    a0.record(st)
+    for _ in range(3):
+        prob.assemble_in_place()
+    a1.record(st)
+    a1.synchronize()
+    asm_ms = a0.elapsed_time(a1) / 3
+    asm_bytes = nE * (4 * 4 + 12 * 4) + m.n * 3 * 4 + m.nnzb * 36 + m.n * 3 * 4
+    assembly = {"ms": asm_ms, "elements_per_s": nE / (asm_ms / 1e3),
+                "algorithmic_bytes": asm_bytes, "GBps": asm_bytes / (asm_ms / 1e3) / 1e9,
+                "kernels": "k_rows<LinTetElem> (stiffness) + k_rows<TetForceElem> (force)"}
+
     # --- the same system solved with the learned (symmetric) preconditioner
     # against block-Jacobi, solve only (same matrix and right-hand side) ----
     learned = None
@@ -831,6 +850,7 @@ def run_ours(args, rank, world, local):
                                    "%.1f s" % (args.cpu_sample, cpu["dofs"], cpu["iters"],
                                                cpu["seconds"])},
         "clocks": clk,
+        "assembly": assembly,
         "fp64_jacobi_cg": fp64,
         "learned_vs_block_jacobi": learned,
         "speedup_vs_fp64_cg": (fp64["ms"] / ms) if fp64 else None,

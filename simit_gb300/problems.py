@@ -109,15 +109,20 @@ class HeteroElasticity:
             self.b = f.to(torch.float64)
         return self.A, self.b
 
-    def step(self):
-        """One pass of the hot path: assemble in place, refresh, solve from 0."""
+    def assemble_in_place(self):
+        """The step's assembly: the stiffness map into A in place and the
+        force map; returns the force."""
         m = self.mesh
         from .runtime import call, ptr, dtype_code
         call("sg_assemble_tet_stiffness", self.ctx.h, m.ref(), dtype_code(self.A),
              _lib.MODEL_LINEAR, ptr(self.x), ptr(self.c), ptr(self.B), ptr(self.W), ptr(self.mu),
              ptr(self.lam), H, RHO, ptr(self.A), 0)
-        f = assemble_tet_force(m, _lib.MODEL_LINEAR, self.x, self.v0, self.c, self.B, self.W,
-                               self.mu, self.lam, H, RHO, GRAV, dtype=self.dtype, exact=False)
+        return assemble_tet_force(m, _lib.MODEL_LINEAR, self.x, self.v0, self.c, self.B, self.W,
+                                  self.mu, self.lam, H, RHO, GRAV, dtype=self.dtype, exact=False)
+
+    def step(self):
+        """One pass of the hot path: assemble in place, refresh, solve from 0."""
+        f = self.assemble_in_place()
         with self.ctx.stream():
             self.b.copy_(f)
             self.u.zero_()
