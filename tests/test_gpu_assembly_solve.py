@@ -429,3 +429,38 @@ def test_reordered_workload_solves_to_the_same_displacements(ctx, oracle):
     u1 = sysm[1][4][vo].reshape(-1)
     r0 = b0 - oracle.spmv(h["n"], 3, rp, ci, A0, u1)
     assert np.linalg.norm(r0) <= 1.01e-8 * np.linalg.norm(b0)
+
+
+def test_thermal_jacobi_pcg_refresh_matches_oracle(ctx, oracle):
+    """apps/thermal/thermal.sim:102-130's solver form on the P1 heat system
+    (12^3 lattice, kappa log-uniform [1e-2, 1e2], dt 1e-2): point-Jacobi PCG
+    with the true residual recomputed every 50 iterations (check_every), FP64,
+    against the oracle's restatement of that loop — same convergence to
+    1e-8 and iteration counts within 2 %."""
+    from simit_gb300.runtime import Mesh, Solver, assemble_heat, solve_opts, tet_precompute
+    mg = meshgen.tet_grid(12)
+    nT = len(mg["tets"]) // 4
+    g = meshgen.rng(31)
+    kappa = 10 ** g.uniform(-2, 2, nT)
+    T0 = g.uniform(0, 1, mg["n"])
+    mesh = Mesh(ctx, mg["n"], mg["tets"], 4)
+    B, W, _ = tet_precompute(mesh, mg["X0"], 1.0)
+    A, b = assemble_heat(mesh, B, W, kappa, 1e-2, T0)
+    rp, ci = mesh.pattern.host()
+    oB, oW, _ = oracle.tet_precompute(mg["X0"], mg["tets"], 1.0)
+    oA, ob = oracle.heat_assemble(mg["n"], mg["tets"], oB, oW, kappa, 1e-2, T0, rp, ci)
+    ctx.sync()
+    assert np.array_equal(_np(A), oA) and np.array_equal(_np(b), ob)
+    S = Solver(ctx, mesh.n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A, mesh.nnzb,
+               solve_opts(precond=_lib.PRECOND_JACOBI, tol=1e-8, maxiters=20000,
+                          check_every=50))
+    x = torch.zeros_like(b)
+    res = S.solve(b, x)
+    S.close()
+    assert res.status == 1, _lib.STATUS.get(res.status)
+    assert res.checks >= res.iters // 50
+    ox, oit, orr = oracle.jacobi_pcg(mesh.n, 1, rp, ci, oA, ob, np.zeros(mesh.n), 1e-8, 20000,
+                                     refresh=50)
+    assert orr <= 1e-8 and np.sqrt(res.true_normr2 / res.bnorm2) <= 1e-8
+    assert abs(res.iters - oit) <= max(3, 0.02 * oit)
+    assert oracle.relres(mesh.n, 1, rp, ci, oA, ob, _np(x)) <= 1.001e-8
