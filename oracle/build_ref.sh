@@ -1,9 +1,9 @@
 #!/bin/sh
 # Test infrastructure: compile the reference's own pattern builder and runtime
-# `loc` from its sources (read where they lie, never copied) plus the driver
+# `loc` from its sources (read where they lie, never copied) plus the wrapper
 # oracle/ref_pattern.cpp into oracle/_ref/libref_pattern.so.  Needs only g++;
 # it does not run the reference's cmake build.  Skips quietly when the
-# reference source tree is absent (the GPU machine has none).
+# reference source tree is absent.
 set -e
 REF=${SIMIT_REFERENCE_SRC:-/root/reference/src}
 HERE=$(cd "$(dirname "$0")" && pwd)

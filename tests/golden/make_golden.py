@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures in this directory from the reference tree.
 
 Run in a checkout that has the reference sources (default path below, or
-SIMIT_REFERENCE); the GPU machine has none, so the outputs are committed:
+SIMIT_REFERENCE); the machines that run the tests need not have it, so the
+outputs are committed:
 
   reference_golden.json   golden values asserted by the reference's tests,
                           extracted from their sources (file:line recorded),
