@@ -112,6 +112,30 @@ def ref_pattern(n, ep, card):
     return rowptr, colidx[:nnz].copy()
 
 
+def ref_incidence(kind, n0, n1, set_of, ep, xr=1, xc=1):
+    """The reference's own Link::ev (kind 0) / Link::ve (1) index or the And
+    of the two between vertex sets xr, xc (2), for an edge set whose endpoint
+    k lies in V0 or V1 per set_of[k] (None when not built here)."""
+    if not os.path.exists(REF_LIB):
+        return None
+    L = ctypes.CDLL(REF_LIB)
+    L.ref_incidence.restype = _I64
+    L.ref_incidence.argtypes = [ctypes.c_int, _I32, _I32, _I32, _P, _P, _I64, _I32, _I32, _P,
+                                _P, _I64]
+    card = len(set_of)
+    ep = _c(ep, np.int32)
+    so = _c(set_of, np.int32)
+    nE = ep.size // card
+    rows = nE if kind == 0 else (n1 if xr else n0)
+    cap = max(1, nE * card * card + n0 + n1)
+    rowptr = np.zeros(rows + 1, np.uint32)
+    colidx = np.zeros(cap, np.uint32)
+    nnz = L.ref_incidence(kind, n0, n1, card, _p(so), _p(ep), nE, xr, xc, _p(rowptr),
+                          _p(colidx), cap)
+    assert nnz >= 0, nnz
+    return rowptr, colidx[:nnz].copy()
+
+
 def ref_slots(ep, card, rowptr, colidx):
     if not os.path.exists(REF_LIB):
         return None

@@ -169,3 +169,34 @@ def test_rect_matrix_golden(oracle, case):
     vals = oracle.assemble_rect(sr, npr, sc, npc, 1, eb, rp, ci)
     y = oracle.spmv(nr, 1, rp, ci, vals, vec)
     assert y.tolist() == [float(v) for v in expected], name
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_incidence_and_rect_patterns_match_reference_builder(oracle, seed):
+    """The oracle's Link::ev / Link::ve / two-set And restatements against
+    the reference's own PathIndexBuilder (compiled from its sources), bit for
+    bit, on heterogeneous edge sets (V1, V1, V0, V1, V1) with repeats and on
+    a homogeneous one."""
+    if not os.path.exists(oracle.REF_LIB):
+        pytest.skip("reference pattern builder not built here")
+    g = meshgen.rng(90 + seed)
+    for set_of, n0, n1, nE in (([1, 1, 0, 1, 1], 6, 20, 40), ([0, 0, 0], 25, 1, 60)):
+        card = len(set_of)
+        ep = np.stack([g.integers(0, n1 if s else n0, size=nE) for s in set_of], 1)
+        ep[::5, 1] = ep[::5, 0]  # repeated endpoints
+        for x in sorted(set(set_of)):
+            pos = [k for k in range(card) if set_of[k] == x]
+            sel = ep[:, pos]
+            nx = n1 if x else n0
+            for kind in (0, 1):
+                ref = oracle.ref_incidence(kind, n0, n1, set_of, ep, xr=x, xc=x)
+                got = oracle.incidence_pattern(kind, nx, sel, len(pos))
+                assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
+        if 0 in set_of and 1 in set_of:
+            for xr, xc in ((0, 1), (1, 0)):
+                pr = [k for k in range(card) if set_of[k] == xr]
+                pc = [k for k in range(card) if set_of[k] == xc]
+                ref = oracle.ref_incidence(2, n0, n1, set_of, ep, xr=xr, xc=xc)
+                got = oracle.rect_pattern(n1 if xr else n0, ep[:, pr], len(pr), ep[:, pc],
+                                          len(pc))
+                assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
