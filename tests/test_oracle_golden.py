@@ -200,3 +200,32 @@ def test_incidence_and_rect_patterns_match_reference_builder(oracle, seed):
                 got = oracle.rect_pattern(n1 if xr else n0, ep[:, pr], len(pr), ep[:, pc],
                                           len(pc))
                 assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
+
+
+def test_incidence_slots_match_reference_loc(oracle):
+    """The slot every element write lands in under the oracle's incidence
+    assembly is the one the reference runtime's own `loc` returns
+    (src/runtime.cpp:19-23: the first matching column of the row), for EV
+    and VE patterns with repeated endpoints."""
+    import ctypes
+    if not os.path.exists(oracle.REF_LIB):
+        pytest.skip("reference pattern builder not built here")
+    L = ctypes.CDLL(oracle.REF_LIB)
+    L.loc.restype = ctypes.c_int
+    L.loc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    g = meshgen.rng(55)
+    n, nE, npos = 30, 80, 3
+    sel = g.integers(0, n, size=(nE, npos))
+    sel[::4, 2] = sel[::4, 0]
+    for kind in (0, 1):
+        rp, ci = oracle.incidence_pattern(kind, n, sel, npos)
+        rpi, cii = rp.astype(np.int32), ci.astype(np.int32)
+        # unit blocks mark which slot each (element, listing) write lands in
+        for e in range(nE):
+            for k in range(npos):
+                eb = np.zeros((nE, npos))
+                eb[e, k] = 1.0
+                vals = oracle.assemble_incidence(kind, sel, npos, 1, eb, rp, ci)
+                r, c = (e, int(sel[e, k])) if kind == 0 else (int(sel[e, k]), e)
+                q = L.loc(r, c, rpi.ctypes.data, cii.ctypes.data)
+                assert int(np.flatnonzero(vals)[0]) == q
