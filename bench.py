@@ -32,7 +32,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=128, help="cells per cube edge")
-    ap.add_argument("--cpu-sample", type=int, default=32, help="cells per edge of the CPU sample")
+    ap.add_argument("--cpu-sample", type=int, default=48,
+                    help="cells per edge of the CPU sample (48: about 10-15 s of one core)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
     ap.add_argument("--no-reorder", action="store_true",
                     help="keep the lattice vertex order (no space-filling-curve reordering)")
