@@ -199,6 +199,29 @@ int sg_assemble_rect(sg_ctx *ctx, int32_t nr, int32_t npos_r, int32_t npos_c,
                      const uint32_t *rowptr, const uint32_t *colidx, int dtype, int32_t bs,
                      const void *eb, void *vals);
 
+/* Element kernels compiled at run time (NVRTC, loaded on first use): the
+ * element function of a `map f to E reduce +` given as CUDA C++ source,
+ *   __device__ int element_block(long long e, int i, int j, const int *ep,
+ *                                const real *const *f, real blk[BS][BS]);
+ * (real = float or double per dtype; BS, CARD defined; ep the element's
+ * endpoints; f the fields passed to sg_jit_assemble; returns 0 where the
+ * element writes nothing), compiled with a row-owner assembly kernel for
+ * sm_103a (exact != 0: no multiply-add contraction).  The generated kernel
+ * adds every block in ascending element order, then ascending j, into the
+ * mesh's pattern, as sg_assemble_blocks does for precomputed blocks.  This
+ * is the code-generation end of the reference's map lowering
+ * (src/inline.cpp:690-888, src/lower/lower_maps.cpp:54-128) with the element
+ * function written in CUDA rather than produced from .sim by its frontend.
+ * A source that does not compile returns SG_ERR_ARG with the compiler log in
+ * sg_last_error(). */
+typedef struct sg_jit_assembly sg_jit_assembly;
+int sg_jit_assembly_create(sg_ctx *ctx, const char *element_src, int32_t card, int32_t bs,
+                           int dtype, int32_t exact, sg_jit_assembly **out);
+/* h_fields: host array of nfields (<= 8) device pointers; vals [nnzb*bs*bs]. */
+int sg_jit_assemble(sg_jit_assembly *jit, const sg_mesh *mesh, const void *const *h_fields,
+                    int32_t nfields, void *vals);
+int sg_jit_assembly_destroy(sg_jit_assembly *jit);
+
 /* precomputeTetMat (femTet.sim; apps/fem/fem_linear.sim:176-193):
  * B = inv(Ds) [nE*9], W = -det(Ds)/6 [nE], vertex mass m [n] = sum of
  * 0.25*rho*W in element order. */

@@ -83,6 +83,9 @@ SIGNATURES = {
     "sg_assemble_incidence": (_CI, [P, _CI, I64, I32, P, P, _CI, I32, P, P]),
     "sg_pattern_rect": (_CI, [P, I32, I32, I64, I32, I32, P, P, P, P, P, ctypes.POINTER(I64)]),
     "sg_assemble_rect": (_CI, [P, I32, I32, I32, P, P, P, P, P, _CI, I32, P, P]),
+    "sg_jit_assembly_create": (_CI, [P, ctypes.c_char_p, I32, I32, _CI, I32, ctypes.POINTER(P)]),
+    "sg_jit_assemble": (_CI, [P, _MP, P, I32, P]),
+    "sg_jit_assembly_destroy": (_CI, [P]),
     "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, I64, _CI, P, D, D, P, P]),
     "sg_symbsr_create": (_CI, [P, I32, P, P, I64, I32, ctypes.POINTER(P)]),
     "sg_symbsr_fill": (_CI, [P, P]),

@@ -78,7 +78,7 @@ def build(verbose=False, jobs=None):
     stamp = os.path.join(BUILD, "lib.stamp")
     if (not os.path.exists(LIB) or not os.path.exists(stamp)
             or os.path.getmtime(LIB) < newest):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-ldl"]
         subprocess.check_call(cmd)
         open(stamp, "w").write(platform.machine())
     return LIB

@@ -263,6 +263,38 @@ class RectMatrix:
         return bspmv(self.ctx, self.nr, bs, self.rowptr, self.colidx, vals, x)
 
 
+class JitAssembly:
+    """`map f to E reduce +` with the element function given as CUDA source
+    (sg_jit_assembly_create: compiled by NVRTC with a row-owner assembly
+    kernel).  assemble(mesh, fields) -> values [nnzb*bs*bs]."""
+
+    def __init__(self, ctx, element_src, card, bs, dtype=torch.float64, exact=True):
+        self.ctx, self.card, self.bs, self.dtype = ctx, card, bs, dtype
+        h = ctypes.c_void_p()
+        call("sg_jit_assembly_create", ctx.h, element_src.encode(), card, bs,
+             F64 if dtype == torch.float64 else F32, int(exact), ctypes.byref(h))
+        self.h = h.value
+
+    def assemble(self, mesh, fields):
+        fields = [_d(f, self.dtype, self.ctx.device) for f in fields]
+        self._keep = fields
+        arr = (ctypes.c_void_p * max(1, len(fields)))(*[f.data_ptr() for f in fields])
+        vals = mesh.empty(mesh.nnzb * self.bs * self.bs, self.dtype)
+        call("sg_jit_assemble", self.h, mesh.ref(), arr, len(fields), ptr(vals))
+        return vals
+
+    def close(self):
+        if self.h:
+            _lib.load().sg_jit_assembly_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def dot(ctx, a, b):
     out = ctypes.c_double()
     call("sg_dot", ctx.h, a.numel(), dtype_code(a), ptr(a), ptr(b), ctypes.byref(out))
