@@ -37,6 +37,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
     ap.add_argument("--no-reorder", action="store_true",
                     help="keep the lattice vertex order (no space-filling-curve reordering)")
+    ap.add_argument("--no-jit", action="store_true",
+                    help="skip timing the stiffness map compiled at run time (NVRTC)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-preconditioner comparison")
     ap.add_argument("--spmv-only", action="store_true",
@@ -762,6 +764,8 @@ def run_ours(args, rank, world, local):
     assembly = {"ms": asm_ms, "elements_per_s": nE / (asm_ms / 1e3),
                 "algorithmic_bytes": asm_bytes, "GBps": asm_bytes / (asm_ms / 1e3) / 1e9,
                 "kernels": "k_rows<LinTetElem> (stiffness) + k_rows<TetForceElem> (force)"}
+    if not args.no_jit:
+        assembly["jit_stiffness"] = time_jit_stiffness(ctx, prob)
 
     # --- the same system solved with the learned (symmetric) preconditioner
     # against block-Jacobi, solve only (same matrix and right-hand side) ----
@@ -857,6 +861,45 @@ def run_ours(args, rank, world, local):
         "speedup_vs_fp64_cg": (fp64["ms"] / ms) if fp64 else None,
     }
     print(json.dumps(out), flush=True)
+
+
+def time_jit_stiffness(ctx, prob):
+    """The linear-tet stiffness map of the step from its element function
+    compiled at run time (sg_jit_assembly_create), timed beside the
+    precompiled k_rows<LinTetElem>; both write the same matrix, bit for bit."""
+    import torch
+    from simit_gb300 import _lib, jit_elements, problems
+    from simit_gb300.runtime import JitAssembly, call, dtype_code, ptr
+    m, st = prob.mesh, ctx.torch_stream
+    t0 = time.perf_counter()
+    jit = JitAssembly(ctx, jit_elements.linear_tet(problems.H, problems.RHO), 4, 3,
+                      dtype=prob.dtype, exact=False)
+    compile_s = time.perf_counter() - t0
+    fields = [prob.B, prob.W, prob.mu, prob.lam, prob.c]
+    with ctx.stream():
+        out = torch.empty_like(prob.A)
+
+    def builtin():
+        call("sg_assemble_tet_stiffness", ctx.h, m.ref(), dtype_code(prob.A), _lib.MODEL_LINEAR,
+             ptr(prob.x), ptr(prob.c), ptr(prob.B), ptr(prob.W), ptr(prob.mu), ptr(prob.lam),
+             problems.H, problems.RHO, ptr(prob.A), 0)
+
+    res = {"compile_s": compile_s}
+    for name, f in (("jit_ms", lambda: jit.assemble(m, fields, out=out)), ("builtin_ms", builtin)):
+        for _ in range(2):
+            f()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(3):
+            f()
+        e1.record(st)
+        e1.synchronize()
+        res[name] = e0.elapsed_time(e1) / 3
+    ctx.sync()
+    res["bitwise_equal"] = bool(torch.equal(out, prob.A))
+    jit.close()
+    return res
 
 
 def main():

@@ -202,19 +202,27 @@ int sg_assemble_rect(sg_ctx *ctx, int32_t nr, int32_t npos_r, int32_t npos_c,
 /* Element kernels compiled at run time (NVRTC, loaded on first use): the
  * element function of a `map f to E reduce +` given as CUDA C++ source,
  *   __device__ int element_block(long long e, int i, int j, const int *ep,
- *                                const real *const *f, real blk[BS][BS]);
- * (real = float or double per dtype; BS, CARD defined; ep the element's
- * endpoints; f the fields passed to sg_jit_assemble; returns 0 where the
- * element writes nothing), compiled with a row-owner assembly kernel for
- * sm_103a (exact != 0: no multiply-add contraction).  The generated kernel
- * adds every block in ascending element order, then ascending j, into the
- * mesh's pattern, as sg_assemble_blocks does for precomputed blocks.  This
- * is the code-generation end of the reference's map lowering
- * (src/inline.cpp:690-888, src/lower/lower_maps.cpp:54-128) with the element
- * function written in CUDA rather than produced from .sim by its frontend.
+ *                                const real *const *f, sg_block *blk);
+ * (real = float or double per dtype; BS, CARD, SG_TERMS = 2 defined and
+ * sg_block = real[BS][BS]; ep the element's endpoints; f the fields passed
+ * to sg_jit_assemble, cast by the source where a field is not real).  It
+ * writes the terms element e adds to block (i, j) into blk[0..] and returns
+ * their count (0 .. SG_TERMS); each term is its own `+=` on the slot, as
+ * each write of the reference's element function is after lowering.  The
+ * source is compiled with a row-owner assembly kernel for sm_103a (exact !=
+ * 0: no multiply-add contraction) that adds, per slot and from zero, in
+ * ascending element order, then ascending j, then term, as sg_assemble_blocks
+ * does for precomputed blocks.  This is the code-generation end of the
+ * reference's map lowering (src/inline.cpp:690-888,
+ * src/lower/lower_maps.cpp:54-128) with the element function written in
+ * CUDA rather than produced from .sim by its frontend.  card 1..32, bs 1..5.
  * A source that does not compile returns SG_ERR_ARG with the compiler log in
- * sg_last_error(). */
+ * sg_last_error(); without NVRTC, SG_ERR_UNSUPPORTED. */
 typedef struct sg_jit_assembly sg_jit_assembly;
+/* Compiles the source as sg_jit_assembly_create does, without a context or
+ * a GPU; the compiler log (warnings or errors) goes to log[log_cap]. */
+int sg_jit_check_source(const char *element_src, int32_t card, int32_t bs, int dtype,
+                        int32_t exact, char *log, int64_t log_cap);
 int sg_jit_assembly_create(sg_ctx *ctx, const char *element_src, int32_t card, int32_t bs,
                            int dtype, int32_t exact, sg_jit_assembly **out);
 /* h_fields: host array of nfields (<= 8) device pointers; vals [nnzb*bs*bs]. */

@@ -14,6 +14,7 @@ I32 = ctypes.c_int32
 I64 = ctypes.c_int64
 D = ctypes.c_double
 F32, F64 = 0, 1
+ERR_ARG, ERR_CUDA, ERR_UNSUPPORTED, ERR_DEVICE, ERR_STATE = -1, -2, -3, -4, -5
 
 
 class SimitError(RuntimeError):
@@ -83,6 +84,7 @@ SIGNATURES = {
     "sg_assemble_incidence": (_CI, [P, _CI, I64, I32, P, P, _CI, I32, P, P]),
     "sg_pattern_rect": (_CI, [P, I32, I32, I64, I32, I32, P, P, P, P, P, ctypes.POINTER(I64)]),
     "sg_assemble_rect": (_CI, [P, I32, I32, I32, P, P, P, P, P, _CI, I32, P, P]),
+    "sg_jit_check_source": (_CI, [ctypes.c_char_p, I32, I32, _CI, I32, ctypes.c_char_p, I64]),
     "sg_jit_assembly_create": (_CI, [P, ctypes.c_char_p, I32, I32, _CI, I32, ctypes.POINTER(P)]),
     "sg_jit_assemble": (_CI, [P, _MP, P, I32, P]),
     "sg_jit_assembly_destroy": (_CI, [P]),

@@ -8,24 +8,32 @@
 // from a .sim program by the reference's frontend.
 //
 // The element function's contract (real is float or double, BS and CARD are
-// the block size and the endpoints per element):
+// the block size and the endpoints per element, sg_block is real[BS][BS]):
 //
 //   __device__ int element_block(long long e, int i, int j, const int *ep,
-//                                const real *const *f, real blk[BS][BS]);
+//                                const real *const *f, sg_block *blk);
 //
-// it writes block (i, j) of element e (ep: its CARD endpoints; f: the
-// caller's field arrays) and returns 0 when the element writes nothing
-// there.  The generated kernel is the row-owner form of the hand-written
-// ones: a warp owns block row v, walks its incidences in ascending element
-// order, lane j computes block (i, j), and lanes add the blocks into a
-// shared-memory image of the row in ascending j, so every slot sums its
-// contributions in the reference's order from zero.
+// it writes the terms that element e adds to block (i, j) (ep: its CARD
+// endpoints; f: the caller's field arrays) into blk[0], blk[1] and returns
+// how many there are (0 .. SG_TERMS = 2).  Each term is a separate `+=` on
+// the slot, as each write of the reference's element function is after
+// lowering (a diagonal block that receives a stiffness and a mass write gets
+// two adds).  The generated kernel is the row-owner form of the hand-written
+// ones: a warp owns block row v; its lanes compute the blocks of 32 / CARD
+// incidences of v at once (lane = k * CARD + j); then, incidence by
+// incidence in ascending element order, the lanes of (j, block row) add the
+// terms into a shared-memory image of the row, so every slot sums its
+// contributions from zero in the reference's order (ascending element, then
+// ascending j, then term).  An element that lists a vertex twice sends
+// several j to one slot: the first such j adds them all in ascending j.
 //
 // NVRTC is loaded with dlopen at the first use and the image is loaded
 // through the runtime's library API, so the library itself links neither.
 #include <dlfcn.h>
 #include <nvrtc.h>
 #include <stdint.h>
+
+#include <string.h>
 
 #include <string>
 #include <vector>
@@ -66,10 +74,13 @@ Nvrtc &nvrtc() {
 
 constexpr int JIT_MAX_FIELDS = 8;
 constexpr int JIT_WARPS = 4;
+constexpr int JIT_TERMS = 2;  // SG_TERMS of the generated source
 
 // The generated kernel around the caller's element function.
 const char *kJitPrologue = R"(
 typedef SG_REAL real;
+typedef real sg_block[BS][BS];
+#define SG_TERMS 2
 )";
 
 const char *kJitKernel = R"(
@@ -79,14 +90,20 @@ sg_jit_rows(int n, const unsigned *__restrict__ ve_ptr, const unsigned *__restri
             const int *__restrict__ ep_all, const unsigned *__restrict__ rowptr,
             const unsigned *__restrict__ colidx, int maxrow, SgFields f,
             real *__restrict__ vals, int *err) {
+  constexpr int BB = BS * BS, KI = 32 / CARD, NS = KI * CARD;
   extern __shared__ __align__(16) unsigned char sm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  real *acc_all = reinterpret_cast<real *>(sm);
-  real *acc = acc_all + (size_t)warp * maxrow * BS * BS;
-  real *stage = acc_all + (size_t)nwarp * maxrow * BS * BS + (size_t)warp * CARD * BS * BS;
-  unsigned *cols = reinterpret_cast<unsigned *>(acc_all + (size_t)nwarp * maxrow * BS * BS +
-                                                (size_t)nwarp * CARD * BS * BS) +
-                   (size_t)warp * maxrow;
+  // per warp: acc[maxrow*BB], stage[NS*SG_TERMS*BB] (reals), then cols[maxrow],
+  // slot[NS], nts[NS], colk[NS] (ints); each kind laid out warp after warp
+  real *acc = reinterpret_cast<real *>(sm) + (size_t)warp * maxrow * BB;
+  real *stage = reinterpret_cast<real *>(sm) + (size_t)nwarp * maxrow * BB +
+                (size_t)warp * NS * SG_TERMS * BB;
+  unsigned *ibase = reinterpret_cast<unsigned *>(reinterpret_cast<real *>(sm) +
+                                                 (size_t)nwarp * (maxrow * BB + NS * SG_TERMS * BB));
+  unsigned *cols = ibase + (size_t)warp * maxrow;
+  int *slot = reinterpret_cast<int *>(ibase + (size_t)nwarp * maxrow) + (size_t)warp * 3 * NS;
+  int *nts = slot + NS;
+  unsigned *colk = reinterpret_cast<unsigned *>(nts + NS);
   for (long long v = (long long)blockIdx.x * nwarp + warp; v < n;
        v += (long long)gridDim.x * nwarp) {
     const unsigned r0 = rowptr[v], rlen = rowptr[v + 1] - r0;
@@ -95,44 +112,63 @@ sg_jit_rows(int n, const unsigned *__restrict__ ve_ptr, const unsigned *__restri
       continue;
     }
     for (unsigned q = lane; q < rlen; q += 32) cols[q] = colidx[r0 + q];
-    for (unsigned q = lane; q < rlen * BS * BS; q += 32) acc[q] = real(0);
+    for (unsigned q = lane; q < rlen * BB; q += 32) acc[q] = real(0);
     __syncwarp();
-    for (unsigned it = ve_ptr[v]; it < ve_ptr[v + 1]; ++it) {
-      const unsigned t = ve_idx[it];
-      const long long e = t / CARD;
-      const int i = (int)(t - (unsigned)e * CARD);
-      const int *ep = ep_all + e * CARD;
-      int nz = 0;
-      if (lane < CARD) {
-        real blk[BS][BS];
-        for (int a = 0; a < BS; ++a)
-          for (int b = 0; b < BS; ++b) blk[a][b] = real(0);
-        nz = element_block(e, i, lane, ep, f.p, blk);
-        for (int a = 0; a < BS; ++a)
-          for (int b = 0; b < BS; ++b) stage[(lane * BS + a) * BS + b] = blk[a][b];
-      }
-      const unsigned nzmask = __ballot_sync(0xffffffffu, nz != 0);
-      __syncwarp();
-      if (lane < BS * BS) {
-        for (int j = 0; j < CARD; ++j) {
-          if (!((nzmask >> j) & 1u)) continue;
-          const unsigned col = (unsigned)ep[j];
-          unsigned lo = 0, hi = rlen;
-          while (lo < hi) {
-            const unsigned mid = (lo + hi) >> 1;
-            if (cols[mid] < col) lo = mid + 1;
-            else hi = mid;
-          }
-          if (lo >= rlen || cols[lo] != col) {
-            atomicCAS(err, 0, 3);
-            continue;
-          }
-          acc[lo * BS * BS + lane] += stage[j * BS * BS + lane];
+    const unsigned iend = ve_ptr[v + 1];
+    for (unsigned it0 = ve_ptr[v]; it0 < iend; it0 += KI) {
+      const int kn = (int)((iend - it0) < (unsigned)KI ? (iend - it0) : (unsigned)KI);
+      const int k = lane / CARD, j = lane - k * CARD;
+      if (k < kn) {
+        const unsigned t = ve_idx[it0 + k];
+        const long long e = t / CARD;
+        const int i = (int)(t - (unsigned)e * CARD);
+        const int *ep = ep_all + e * CARD;
+        sg_block blk[SG_TERMS];
+        for (int q = 0; q < SG_TERMS; ++q)
+          for (int a = 0; a < BS; ++a)
+            for (int b = 0; b < BS; ++b) blk[q][a][b] = real(0);
+        int nt = element_block(e, i, j, ep, f.p, blk);
+        nt = nt < 0 ? 0 : (nt > SG_TERMS ? SG_TERMS : nt);
+        for (int q = 0; q < nt; ++q)
+          for (int a = 0; a < BS; ++a)
+            for (int b = 0; b < BS; ++b) stage[((lane * SG_TERMS + q) * BS + a) * BS + b] = blk[q][a][b];
+        const unsigned col = (unsigned)ep[j];
+        unsigned lo = 0, hi = rlen;
+        while (lo < hi) {
+          const unsigned mid = (lo + hi) >> 1;
+          if (cols[mid] < col) lo = mid + 1;
+          else hi = mid;
         }
+        int s = (int)lo;
+        if (lo >= rlen || cols[lo] != col) {
+          if (nt > 0) atomicCAS(err, 0, 3);
+          s = -1;
+        }
+        slot[lane] = s;
+        nts[lane] = nt;
+        colk[lane] = col;
       }
       __syncwarp();
+      for (int kk = 0; kk < kn; ++kk) {
+        for (int w = lane; w < CARD * BS; w += 32) {
+          const int jw = w / BS, a = w - jw * BS, base = kk * CARD;
+          const unsigned col = colk[base + jw];
+          bool first = true;
+          for (int j2 = 0; j2 < jw; ++j2) first = first && colk[base + j2] != col;
+          const int s = slot[base + jw];
+          if (!first || s < 0) continue;
+          real *dst = acc + (size_t)s * BB + a * BS;
+          for (int jj = jw; jj < CARD; ++jj) {
+            if (colk[base + jj] != col) continue;
+            const real *src = stage + (size_t)(base + jj) * SG_TERMS * BB + a * BS;
+            for (int q = 0; q < nts[base + jj]; ++q)
+              for (int b = 0; b < BS; ++b) dst[b] += src[q * BB + b];
+          }
+        }
+        __syncwarp();
+      }
     }
-    for (unsigned q = lane; q < rlen * BS * BS; q += 32) vals[(size_t)r0 * BS * BS + q] = acc[q];
+    for (unsigned q = lane; q < rlen * BB; q += 32) vals[(size_t)r0 * BB + q] = acc[q];
     __syncwarp();
   }
 }
@@ -154,42 +190,72 @@ struct JitFields {
 
 using namespace sg;
 
-extern "C" {
+namespace {
 
-int sg_jit_assembly_create(sg_ctx *h, const char *element_src, int32_t card, int32_t bs,
-                           int dtype, int32_t exact, sg_jit_assembly **out) {
-  Ctx *c = as_ctx(h);
-  SG_REQUIRE(c && element_src && out, "sg_jit_assembly_create: null argument");
+// Compiles the generated source; on success `image` holds the CUBIN, on a
+// compile error `log` the compiler's log and the result is SG_ERR_ARG.
+int jit_compile(const char *element_src, int32_t card, int32_t bs, int dtype, int32_t exact,
+                std::vector<char> &image, std::string &log) {
+  SG_REQUIRE(element_src, "sg_jit: null source");
   SG_REQUIRE(card >= 1 && card <= 32 && bs >= 1 && bs <= 5,
-             "sg_jit_assembly_create: card %d bs %d (card 1..32, bs 1..5)", card, bs);
-  SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, "sg_jit_assembly_create: dtype %d", dtype);
+             "sg_jit: card %d bs %d (card 1..32, bs 1..5)", card, bs);
+  SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, "sg_jit: dtype %d", dtype);
   Nvrtc &N = nvrtc();
-  if (!N.ok) return set_error(SG_ERR_UNSUPPORTED, "sg_jit_assembly_create: NVRTC not found");
+  if (!N.ok) return set_error(SG_ERR_UNSUPPORTED, "sg_jit: NVRTC not found");
   std::string src = "#define SG_REAL " + std::string(dtype == SG_F64 ? "double" : "float") +
                     "\n#define BS " + std::to_string(bs) + "\n#define CARD " +
                     std::to_string(card) + "\n" + kJitPrologue + "\n" + element_src + "\n" +
                     kJitKernel;
   nvrtcProgram prog = nullptr;
   if (N.create(&prog, src.c_str(), "sg_jit_element.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
-    return set_error(SG_ERR_UNSUPPORTED, "sg_jit_assembly_create: nvrtcCreateProgram failed");
+    return set_error(SG_ERR_UNSUPPORTED, "sg_jit: nvrtcCreateProgram failed");
   std::vector<const char *> opts = {"-arch=sm_103a", "-std=c++17",
                                     exact ? "--fmad=false" : "--fmad=true"};
   const nvrtcResult rc = N.compile(prog, (int)opts.size(), opts.data());
+  size_t ls = 0;
+  N.log_size(prog, &ls);
+  log.assign(ls, '\0');
+  if (ls) N.log(prog, &log[0]);
+  if (!log.empty() && log.back() == '\0') log.pop_back();
   if (rc != NVRTC_SUCCESS) {
-    size_t ls = 0;
-    N.log_size(prog, &ls);
-    std::string log(ls, '\0');
-    if (ls) N.log(prog, &log[0]);
     N.destroy(&prog);
-    if (log.size() > 1500) log.resize(1500);
-    return set_error(SG_ERR_ARG, "sg_jit_assembly_create: the element source does not compile:\n%s",
-                     log.c_str());
+    std::string shown = log.size() > 1500 ? log.substr(0, 1500) : log;
+    return set_error(SG_ERR_ARG, "sg_jit: the element source does not compile:\n%s",
+                     shown.c_str());
   }
   size_t cs = 0;
   N.cubin_size(prog, &cs);
-  std::vector<char> image(cs);
+  image.resize(cs);
   N.cubin(prog, image.data());
   N.destroy(&prog);
+  return SG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sg_jit_check_source(const char *element_src, int32_t card, int32_t bs, int dtype,
+                        int32_t exact, char *log, int64_t log_cap) {
+  std::vector<char> image;
+  std::string lg;
+  const int rc = jit_compile(element_src, card, bs, dtype, exact, image, lg);
+  if (log && log_cap > 0) {
+    const size_t k = lg.size() < (size_t)(log_cap - 1) ? lg.size() : (size_t)(log_cap - 1);
+    memcpy(log, lg.data(), k);
+    log[k] = '\0';
+  }
+  return rc;
+}
+
+int sg_jit_assembly_create(sg_ctx *h, const char *element_src, int32_t card, int32_t bs,
+                           int dtype, int32_t exact, sg_jit_assembly **out) {
+  Ctx *c = as_ctx(h);
+  SG_REQUIRE(c && element_src && out, "sg_jit_assembly_create: null argument");
+  std::vector<char> image;
+  std::string log;
+  const int rc = jit_compile(element_src, card, bs, dtype, exact, image, log);
+  if (rc != SG_OK) return rc;
   auto *J = new JitAssembly();
   J->c = c;
   J->card = card;
@@ -222,8 +288,11 @@ int sg_jit_assemble(sg_jit_assembly *hj, const sg_mesh *m, const void *const *h_
   Ctx *c = J->c;
   const size_t rs = J->dtype == SG_F64 ? 8 : 4;
   const int maxrow = m->maxrow > 0 ? m->maxrow : 1;
-  const size_t bb = (size_t)J->bs * J->bs;
-  const size_t sh = (size_t)JIT_WARPS * (maxrow * bb * rs + J->card * bb * rs + maxrow * 4);
+  const size_t bb = (size_t)J->bs * J->bs, ns = (size_t)(32 / J->card) * J->card;
+  const size_t per_warp = maxrow * bb * rs + ns * JIT_TERMS * bb * rs + maxrow * 4 + 3 * ns * 4;
+  int warps = JIT_WARPS;
+  while (warps > 1 && warps * per_warp > 48 * 1024) warps >>= 1;
+  const size_t sh = warps * per_warp;
   if (sh > 48 * 1024)
     return set_error(SG_ERR_UNSUPPORTED, "sg_jit_assemble: a row of %d blocks exceeds shared memory",
                      maxrow);
@@ -236,8 +305,8 @@ int sg_jit_assemble(sg_jit_assembly *hj, const sg_mesh *m, const void *const *h_
   int mr = maxrow;
   int *err = c->d_err;
   void *args[] = {&n, &ve_ptr, &ve_idx, &ep, &rowptr, &colidx, &mr, &f, &vals, &err};
-  const int grid = grid_for(c, (int64_t)m->n * 32, JIT_WARPS * 32, 8);
-  SG_CHECK_CUDA(cudaLaunchKernel((const void *)J->kernel, dim3(grid), dim3(JIT_WARPS * 32), args,
+  const int grid = grid_for(c, (int64_t)m->n * 32, warps * 32, 32 / warps * 2);
+  SG_CHECK_CUDA(cudaLaunchKernel((const void *)J->kernel, dim3(grid), dim3(warps * 32), args,
                                  sh, c->stream));
   return SG_OK;
 }

@@ -263,6 +263,16 @@ class RectMatrix:
         return bspmv(self.ctx, self.nr, bs, self.rowptr, self.colidx, vals, x)
 
 
+def check_element_source(element_src, card, bs, dtype=torch.float64, exact=True):
+    """Compiles an element function as JitAssembly would (NVRTC, sm_103a)
+    without a context or a GPU; returns the compiler log, raises SimitError
+    with the log when the source does not compile."""
+    buf = ctypes.create_string_buffer(8192)
+    call("sg_jit_check_source", element_src.encode(), card, bs,
+         F64 if dtype == torch.float64 else F32, int(exact), buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
 class JitAssembly:
     """`map f to E reduce +` with the element function given as CUDA source
     (sg_jit_assembly_create: compiled by NVRTC with a row-owner assembly
@@ -275,11 +285,18 @@ class JitAssembly:
              F64 if dtype == torch.float64 else F32, int(exact), ctypes.byref(h))
         self.h = h.value
 
-    def assemble(self, mesh, fields):
-        fields = [_d(f, self.dtype, self.ctx.device) for f in fields]
+    def assemble(self, mesh, fields, out=None):
+        """fields: up to 8 arrays; floating-point ones are passed in the
+        assembly's dtype, integer ones (constraint flags) as int32.  `out`
+        (nnzb*bs*bs values) is overwritten when given."""
+        fields = [_d(f, self.dtype, self.ctx.device) if _is_float(f) else
+                  _d(f, torch.int32, self.ctx.device) for f in fields]
         self._keep = fields
         arr = (ctypes.c_void_p * max(1, len(fields)))(*[f.data_ptr() for f in fields])
-        vals = mesh.empty(mesh.nnzb * self.bs * self.bs, self.dtype)
+        vals = out if out is not None else mesh.empty(mesh.nnzb * self.bs * self.bs, self.dtype)
+        if vals.numel() < mesh.nnzb * self.bs * self.bs or vals.dtype != self.dtype:
+            raise ValueError("jit assemble: out needs %d %s values" %
+                             (mesh.nnzb * self.bs * self.bs, self.dtype))
         call("sg_jit_assemble", self.h, mesh.ref(), arr, len(fields), ptr(vals))
         return vals
 
@@ -293,6 +310,12 @@ class JitAssembly:
             self.close()
         except Exception:
             pass
+
+
+def _is_float(a):
+    if isinstance(a, torch.Tensor):
+        return a.is_floating_point()
+    return np.asarray(a).dtype.kind == "f"
 
 
 def dot(ctx, a, b):

@@ -5,43 +5,12 @@ import numpy as np
 import pytest
 import torch
 
-from simit_gb300 import meshgen
+from simit_gb300 import jit_elements, meshgen
 
 pytestmark = pytest.mark.gpu
 
-BLOCKS_SRC = r"""
-// block (i, j) of element e read from a precomputed array f[0]
-__device__ int element_block(long long e, int i, int j, const int *ep, const real *const *f,
-                             real blk[BS][BS]) {
-  const real *b = f[0] + ((e * CARD + i) * CARD + j) * BS * BS;
-  for (int a = 0; a < BS; ++a)
-    for (int c = 0; c < BS; ++c) blk[a][c] = b[a * BS + c];
-  return 1;
-}
-"""
-
-# the P1 heat element (A_ij = W/20 (1 + d_ij) + (dt kappa W) g_i.g_j, dt = 0.01)
-# in the operation order of the built-in kernel, from fields B, W, kappa
-HEAT_SRC = r"""
-__device__ void grad(const real *Bt, int i, real g[3]) {
-  for (int d = 0; d < 3; ++d)
-    g[d] = (i < 3) ? Bt[i * 3 + d] : -((Bt[0 * 3 + d] + Bt[1 * 3 + d]) + Bt[2 * 3 + d]);
-}
-__device__ int element_block(long long e, int i, int j, const int *ep, const real *const *f,
-                             real blk[BS][BS]) {
-  const real *Bt = f[0] + 9 * e;
-  real gi[3], gj[3];
-  grad(Bt, i, gi);
-  grad(Bt, j, gj);
-  const real dt = (real)0.01;
-  const real mw = f[1][e] / real(20.0);
-  const real kw = (dt * f[2][e]) * f[1][e];
-  const real mij = (i == j) ? real(2.0) * mw : mw;
-  const real gg = (gi[0] * gj[0] + gi[1] * gj[1]) + gi[2] * gj[2];
-  blk[0][0] = mij + kw * gg;
-  return 1;
-}
-"""
+BLOCKS_SRC = jit_elements.BLOCKS
+HEAT_SRC = jit_elements.heat(0.01)
 
 
 @pytest.fixture(scope="module")
@@ -90,6 +59,55 @@ def test_jit_heat_element_matches_builtin(ctx, dtype):
     got = jit.assemble(mesh, [B, W, kap])
     ctx.sync()
     assert torch.equal(got[:mesh.nnzb], A[:mesh.nnzb])
+    jit.close()
+
+
+@pytest.mark.parametrize("dtype,exact", [(torch.float32, False), (torch.float64, False),
+                                         (torch.float32, True)])
+def test_jit_linear_tet_matches_builtin(ctx, dtype, exact):
+    """The linear-elastic tetrahedron (stiffness where both vertices are free,
+    then the lumped mass as a second write on the diagonal block) as CUDA
+    source: the same matrix, bit for bit, as the precompiled closed-form
+    kernel, with per-element parameters and constrained vertices."""
+    from simit_gb300 import _lib
+    from simit_gb300.runtime import JitAssembly, Mesh, assemble_tet_stiffness, tet_precompute
+    mg = meshgen.tet_grid(7, 6, 5, disp=1e-3, seed=2)
+    nT, n = len(mg["tets"]) // 4, mg["n"]
+    g = meshgen.rng(11)
+    mu = 10 ** g.uniform(3, 5, nT)
+    lam = 10 ** g.uniform(3, 5, nT)
+    c = (g.uniform(0, 1, n) < 0.1).astype(np.int32)
+    h, rho = 0.01, 1e3
+    mesh = Mesh(ctx, n, mg["tets"], 4)
+    B, W, _ = tet_precompute(mesh, mg["X0"], rho, dtype=dtype)
+    A = assemble_tet_stiffness(mesh, _lib.MODEL_LINEAR, mg["x"], c, B, W, mu, lam, h, rho,
+                               dtype=dtype, exact=False)
+    jit = JitAssembly(ctx, jit_elements.linear_tet(h, rho), 4, 3, dtype=dtype, exact=exact)
+    got = jit.assemble(mesh, [B, W, mu, lam, c])
+    ctx.sync()
+    k = mesh.nnzb * 9
+    assert torch.equal(got[:k], A[:k])
+    jit.close()
+
+
+def test_jit_wide_elements_match_oracle(ctx, oracle):
+    """card 8, 5x5 blocks: more (j, row) pairs than lanes, fewer warps per
+    block for shared memory, elements that repeat vertices."""
+    from simit_gb300.runtime import JitAssembly, Mesh
+    card, bs = 8, 5
+    g = meshgen.rng(21)
+    n, nE = 300, 260
+    ep = g.integers(0, n, size=(nE, card)).astype(np.int32)
+    ep[::5, 3] = ep[::5, 6]
+    ep[::7, 1] = ep[::7, 0]
+    eb = g.uniform(-1, 1, size=(nE, card, card, bs, bs))
+    mesh = Mesh(ctx, n, ep.reshape(-1), card)
+    jit = JitAssembly(ctx, BLOCKS_SRC, card, bs, dtype=torch.float64)
+    got = jit.assemble(mesh, [eb.reshape(-1)])
+    ctx.sync()
+    rp, ci = mesh.pattern.host()
+    o = oracle.assemble_blocks(ep.reshape(-1), card, bs, eb, rp, ci)
+    assert np.array_equal(got[:mesh.nnzb * bs * bs].cpu().numpy(), o)
     jit.close()
 
 
