@@ -14,7 +14,16 @@ outputs are committed:
   pattern_golden.json     pattern + slot map of small meshes produced by the
                           reference's own PathIndexBuilder / `loc`
                           (oracle/_ref/libref_pattern.so)
+  tetmeshes.npz           the apps' TetGen meshes (apps/data/tet-bunny/bunny.1
+                          .node/.ele/.edge, apps/data/tet-dragon/dragon40k
+                          .node/.ele) as read by MeshVol::loadTet /
+                          loadTetEdge's rules (simit_gb300.meshgen)
+  tetmeshes_golden.json   per mesh: sizes and SHA-256 digests of the
+                          reference PathIndexBuilder's rowptr / colidx and of
+                          the `loc` slot map, for the tets and for the springs
+                          over the bunny's edges
 """
+import hashlib
 import json
 import os
 import re
@@ -26,6 +35,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 REF = os.environ.get("SIMIT_REFERENCE", "/root/reference")
+
+
+def sha(a, dtype):
+    """SHA-256 of an integer array as little-endian `dtype` bytes."""
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.dtype(dtype).newbyteorder("<"))
+                          .tobytes()).hexdigest()
 
 
 def extract_asserts(path, test_name):
@@ -152,6 +167,27 @@ def main():
                      "rowptr": rp.tolist(), "colidx": ci.tolist(), "slots": sl.tolist()}
     with open(os.path.join(HERE, "pattern_golden.json"), "w") as f:
         json.dump(out, f)
+
+    data = os.path.join(REF, "apps", "data")
+    arrays, digests = {}, {}
+    bx, bt = meshgen.load_tetgen(os.path.join(data, "tet-bunny", "bunny.1.node"),
+                                 os.path.join(data, "tet-bunny", "bunny.1.ele"))
+    be = meshgen.load_tetgen_edges(os.path.join(data, "tet-bunny", "bunny.1.edge"))
+    dx, dt = meshgen.load_tetgen(os.path.join(data, "tet-dragon", "dragon40k.node"),
+                                 os.path.join(data, "tet-dragon", "dragon40k.ele"))
+    arrays.update(bunny_x=bx, bunny_tets=bt.astype(np.int32), bunny_edges=be.astype(np.int32),
+                  dragon_x=dx, dragon_tets=dt.astype(np.int32))
+    for name, x, ep, card in (("bunny_tets", bx, bt, 4), ("bunny_edges", bx, be, 2),
+                              ("dragon_tets", dx, dt, 4)):
+        n = len(x) // 3
+        rp, ci = oracle.ref_pattern(n, ep, card)
+        sl = oracle.ref_slots(ep, card, rp, ci)
+        digests[name] = {"n": int(n), "card": card, "nE": int(len(ep) // card),
+                         "nnzb": int(len(ci)), "rowptr_sha256": sha(rp, np.uint32),
+                         "colidx_sha256": sha(ci, np.uint32), "slots_sha256": sha(sl, np.uint32)}
+    np.savez_compressed(os.path.join(HERE, "tetmeshes.npz"), **arrays)
+    with open(os.path.join(HERE, "tetmeshes_golden.json"), "w") as f:
+        json.dump(digests, f, indent=1)
     print("wrote golden fixtures to", HERE)
 
 

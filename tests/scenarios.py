@@ -3,6 +3,7 @@
 Each builder mirrors the set construction of one reference test so that the
 oracle and the GPU path can replay it and compare with its golden values.
 """
+import hashlib
 import json
 import os
 import re
@@ -144,7 +145,15 @@ def springs_from_tetgen(node_path, edge_path):
     r = 0.01) on each endpoint; apps/springs/isprings.sim constants (h = 1e-2,
     viscous = 2, gravity -9.81 y, CG while r'r > 1e-12, at most 50 steps)."""
     x = meshgen.parse_tetgen_nodes(open(node_path).read())
-    ep = meshgen.load_tetgen_edges(edge_path).reshape(-1, 2)
+    ep = meshgen.load_tetgen_edges(edge_path)
+    return springs_from_arrays(x, ep)
+
+
+def springs_from_arrays(x, ep):
+    """springs_from_tetgen on positions [n*3] and edge endpoints [nE*2]
+    already read from TetGen files."""
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    ep = np.asarray(ep, np.int32).reshape(-1, 2)
     mn, mx = x.min(0), x.max(0)
     x = (x - mn) / (mx - mn)
     d = x[ep[:, 1]] - x[ep[:, 0]]
@@ -158,6 +167,24 @@ def springs_from_tetgen(node_path, edge_path):
             "fixed": (x[:, 2] < 0.1).astype(np.uint8), "ep": ep.reshape(-1).astype(np.int32),
             "k": np.full(len(ep), 1e4), "l0": l0, "h": 1e-2, "viscous": 2.0,
             "grav": np.array([0.0, -9.81, 0.0]), "tol2": 1e-12, "maxiters": 50, "form": 0}
+
+
+def tetmeshes():
+    """The apps' TetGen meshes (bunny.1, dragon40k) as read from their
+    .node/.ele/.edge files, and the digests of the reference
+    PathIndexBuilder's pattern and `loc` slot map for each edge set."""
+    z = np.load(os.path.join(GOLDEN, "tetmeshes.npz"))
+    meshes = {k: z[k] for k in z.files}
+    with open(os.path.join(GOLDEN, "tetmeshes_golden.json")) as f:
+        digests = json.load(f)
+    return meshes, digests
+
+
+def sha(a, dtype=np.uint32):
+    """SHA-256 of an integer array as little-endian `dtype` bytes (the digest
+    tests/golden/make_golden.py records)."""
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.dtype(dtype).newbyteorder("<"))
+                          .tobytes()).hexdigest()
 
 
 def incidence_scenarios():
