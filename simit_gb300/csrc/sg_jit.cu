@@ -54,9 +54,8 @@ struct Nvrtc {
   decltype(&nvrtcDestroyProgram) destroy = nullptr;
 };
 
-Nvrtc &nvrtc() {
-  static Nvrtc N;
-  if (N.tried) return N;
+Nvrtc load_nvrtc() {
+  Nvrtc N;
   N.tried = true;
   void *h = dlopen("libnvrtc.so.13", RTLD_NOW | RTLD_LOCAL);
   if (!h) h = dlopen("libnvrtc.so", RTLD_NOW | RTLD_LOCAL);
@@ -69,6 +68,13 @@ Nvrtc &nvrtc() {
   N.cubin = (decltype(N.cubin))dlsym(h, "nvrtcGetCUBIN");
   N.destroy = (decltype(N.destroy))dlsym(h, "nvrtcDestroyProgram");
   N.ok = N.create && N.compile && N.log_size && N.log && N.cubin_size && N.cubin && N.destroy;
+  return N;
+}
+
+// Loaded once per process; the static's initialisation is thread-safe, and
+// NVRTC programs may be compiled from several threads at once.
+const Nvrtc &nvrtc() {
+  static const Nvrtc N = load_nvrtc();
   return N;
 }
 
@@ -200,7 +206,7 @@ int jit_compile(const char *element_src, int32_t card, int32_t bs, int dtype, in
   SG_REQUIRE(card >= 1 && card <= 32 && bs >= 1 && bs <= 5,
              "sg_jit: card %d bs %d (card 1..32, bs 1..5)", card, bs);
   SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, "sg_jit: dtype %d", dtype);
-  Nvrtc &N = nvrtc();
+  const Nvrtc &N = nvrtc();
   if (!N.ok) return set_error(SG_ERR_UNSUPPORTED, "sg_jit: NVRTC not found");
   std::string src = "#define SG_REAL " + std::string(dtype == SG_F64 ? "double" : "float") +
                     "\n#define BS " + std::to_string(bs) + "\n#define CARD " +

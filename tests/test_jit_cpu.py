@@ -42,3 +42,28 @@ def test_bad_shape_rejected():
     for card, bs in ((0, 1), (33, 1), (2, 0), (2, 6)):
         with pytest.raises(_lib.SimitError):
             check_element_source(jit_elements.BLOCKS, card, bs)
+
+
+def test_concurrent_compiles():
+    """Several threads compiling at once (the first use loads NVRTC) each get
+    their own result and their own error message."""
+    from concurrent.futures import ThreadPoolExecutor
+    _check(jit_elements.BLOCKS, 2, 1)  # skips when NVRTC is absent
+
+    def one(k):
+        if k % 3 == 2:
+            try:
+                check_element_source("__device__ int element_block(broken %d" % k, 2, 1)
+            except _lib.SimitError as e:
+                return ("err", str(e))
+            return ("ok", "")
+        check_element_source(jit_elements.heat(0.01 * (k + 1)), 4, 1,
+                             dtype=torch.float32 if k % 2 else torch.float64)
+        return ("ok", "")
+
+    with ThreadPoolExecutor(6) as ex:
+        res = list(ex.map(one, range(12)))
+    for k, (kind, msg) in enumerate(res):
+        assert kind == ("err" if k % 3 == 2 else "ok"), (k, msg)
+        if kind == "err":
+            assert "does not compile" in msg
