@@ -5,6 +5,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <mutex>
 #include <string>
 
 #include "../../include/simit_gb300.h"
@@ -16,11 +17,17 @@ namespace sg {
 // Per-device one-time flags (function attributes and occupancy are properties
 // of a device's context, not of the process).
 constexpr int SG_MAX_DEVICES = 64;
-inline bool first_on_device(bool (&done)[SG_MAX_DEVICES], int device) {
-  if (device < 0 || device >= SG_MAX_DEVICES) return true;
-  const bool first = !done[device];
-  done[device] = true;
-  return first;
+// Runs `init` once per device and returns its status on every call; a
+// thread that arrives while another runs it waits for it to finish, so no
+// launch can overtake the attribute it depends on.
+struct PerDeviceOnce {
+  std::once_flag flag[SG_MAX_DEVICES];
+  int rc[SG_MAX_DEVICES] = {};
+};
+template <typename F> inline int once_per_device(PerDeviceOnce &o, int device, F &&init) {
+  if (device < 0 || device >= SG_MAX_DEVICES) return init();
+  std::call_once(o.flag[device], [&] { o.rc[device] = init(); });
+  return o.rc[device];
 }
 
 struct Ctx {

@@ -288,11 +288,12 @@ static int graph_init(Ctx *c, const sg_matrix *A, GraphH *G) {
   SG_TRY(galloc(G, (void **)&g.dinv, n * 9 * 4));
   SG_TRY(alloc_layers(G));
   SG_TRY(galloc(G, (void **)&g.dres, 64));
-  static bool attr[SG_MAX_DEVICES] = {};
-  if (first_on_device(attr, c->device)) {
+  static PerDeviceOnce attr;
+  SG_TRY(once_per_device(attr, c->device, []() -> int {
     SG_CHECK_CUDA(cudaFuncSetAttribute(k_f3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
     SG_CHECK_CUDA(cudaFuncSetAttribute(k_f4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes()));
-  }
+    return SG_OK;
+  }));
   return graph_refresh(G);
 }
 
@@ -325,17 +326,20 @@ static int layers(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, con
   SG_CHECK_LAUNCH();
   // one wave of resident CTAs (a partial second wave would run the last
   // CTAs' tiles at a fraction of the occupancy)
+  static PerDeviceOnce occ_once;
   static int per_sm_dev[SG_MAX_DEVICES] = {};
-  int &per_sm = per_sm_dev[(c->device >= 0 && c->device < SG_MAX_DEVICES) ? c->device : 0];
-  if (per_sm == 0) {
+  const int dev = (c->device >= 0 && c->device < SG_MAX_DEVICES) ? c->device : 0;
+  SG_TRY(once_per_device(occ_once, dev, [&]() -> int {
     int a3 = 0, a4 = 0;
     SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a3, k_f3, TC_WARPS * 32,
                                                                 tc_smem_bytes()));
     SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a4, k_f4, TC_WARPS * 32,
                                                                 tc_smem_bytes()));
-    per_sm = a3 < a4 ? a3 : a4;
-    if (per_sm < 1) per_sm = 1;
-  }
+    per_sm_dev[dev] = a3 < a4 ? a3 : a4;
+    if (per_sm_dev[dev] < 1) per_sm_dev[dev] = 1;
+    return SG_OK;
+  }));
+  const int per_sm = per_sm_dev[dev];
   const int64_t ntile = ((int64_t)g.n + 15) / 16;
   int gt = (int)((ntile + TC_WARPS - 1) / TC_WARPS);
   const int cap = c->num_sms * per_sm;
@@ -486,8 +490,10 @@ static void learned_free(Solver *S) {
   S->ext = nullptr;
 }
 
-static const float *g_pending_params = nullptr;
-static int g_pending_form = 0;
+// solver_init calls learned_setup on the creating thread: the settings pass
+// through thread-local slots, so solvers may be created concurrently
+static thread_local const float *g_pending_params = nullptr;
+static thread_local int g_pending_form = 0;
 static int learned_setup(Solver *S) {
   LearnedExt *L = new LearnedExt();
   S->ext = L;

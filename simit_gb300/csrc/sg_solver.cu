@@ -173,11 +173,13 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
       case PK_NONE: launch_k2_v4<PK_NONE>(S, st, par); break;
       case PK_JACOBI: launch_k2_v4<PK_JACOBI>(S, st, par); break;
       case PK_BLOCK3: {
-        static bool attr[SG_MAX_DEVICES] = {};
+        static PerDeviceOnce attr;
         const size_t sm = K2W_WARPS * sizeof(K2WarpSmem);
-        if (first_on_device(attr, S->c->device))
+        SG_TRY(once_per_device(attr, S->c->device, [&]() -> int {
           SG_CHECK_CUDA(cudaFuncSetAttribute(k_cg_update_w<true, false>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+          return SG_OK;
+        }));
         const int64_t nchunks = (S->len / 12 + 31) / 32;
         int64_t grid = (nchunks + K2W_WARPS - 1) / K2W_WARPS;
         // 2 CTAs of 8 warps per SM (3 fit, and measured 3 % slower per step)
