@@ -289,16 +289,18 @@ class JitAssembly:
         """fields: up to 8 arrays; floating-point ones are passed in the
         assembly's dtype, integer ones (constraint flags) as int32.  `out`
         (nnzb*bs*bs values) is overwritten when given."""
-        fields = [_d(f, self.dtype, self.ctx.device) if _is_float(f) else
-                  _d(f, torch.int32, self.ctx.device) for f in fields]
-        self._keep = fields
-        arr = (ctypes.c_void_p * max(1, len(fields)))(*[f.data_ptr() for f in fields])
-        vals = out if out is not None else mesh.empty(mesh.nnzb * self.bs * self.bs, self.dtype)
-        if vals.numel() < mesh.nnzb * self.bs * self.bs or vals.dtype != self.dtype:
-            raise ValueError("jit assemble: out needs %d %s values" %
-                             (mesh.nnzb * self.bs * self.bs, self.dtype))
-        call("sg_jit_assemble", self.h, mesh.ref(), arr, len(fields), ptr(vals))
-        return vals
+        with self.ctx.stream():
+            fields = [_d(f, self.dtype, self.ctx.device) if _is_float(f) else
+                      _d(f, torch.int32, self.ctx.device) for f in fields]
+            self._keep = fields
+            arr = (ctypes.c_void_p * max(1, len(fields)))(*[f.data_ptr() for f in fields])
+            vals = out if out is not None else mesh.empty(mesh.nnzb * self.bs * self.bs,
+                                                          self.dtype)
+            if vals.numel() < mesh.nnzb * self.bs * self.bs or vals.dtype != self.dtype:
+                raise ValueError("jit assemble: out needs %d %s values" %
+                                 (mesh.nnzb * self.bs * self.bs, self.dtype))
+            call("sg_jit_assemble", self.h, mesh.ref(), arr, len(fields), ptr(vals))
+            return vals
 
     def close(self):
         if self.h:
