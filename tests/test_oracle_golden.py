@@ -102,6 +102,20 @@ def test_tet_grid_counts(oracle):
     assert W.min() > 0 and abs(W.sum() - 1.0) < 1e-12
 
 
+def test_tet_grid_48_pattern_matches_reference_builder(oracle):
+    """The 48^3 lattice (552,960 tets, 117,649 vertices): nnzb 1,486,513, and
+    the oracle's pattern equal to the reference's PathIndexBuilder's."""
+    m = meshgen.tet_grid(48)
+    assert (m["n"], len(m["tets"]) // 4) == (117649, 552960)
+    assert meshgen.tet_grid_counts(48) == (552960, 117649)
+    rp, ci = oracle.pattern(m["n"], m["tets"], 4)
+    assert len(ci) == 1486513
+    ref = oracle.ref_pattern(m["n"], m["tets"], 4)
+    if ref is None:
+        pytest.skip("reference pattern builder not built here")
+    assert np.array_equal(rp, ref[0]) and np.array_equal(ci, ref[1])
+
+
 def test_element_block_assembly_golden(oracle):
     """Oracle `map ... reduce +` of caller-evaluated element blocks, then the
     blocked SpMV, against the golden values of the reference's gemv_blocked*
