@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--learned-solve", action="store_true",
                     help="profiling driver: the --size system with the learned preconditioner, "
                          "capped at --iters iterations")
+    ap.add_argument("--layered", action="store_true",
+                    help="--learned-solve: evaluate the network layer by layer on the tensor "
+                         "cores instead of folded")
     ap.add_argument("--springs", action="store_true",
                     help="createBox springs 10^3: 10 implicit FP64 steps, parity vs the oracle")
     ap.add_argument("--heat", action="store_true",
@@ -420,7 +423,9 @@ def run_learned_solve(args):
         xs = torch.zeros_like(p.b)
     S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, m.nnzb,
                solve_opts(precision=_lib.SOLVE_MIXED, precond=_lib.PRECOND_LEARNED, tol=1e-8,
-                          maxiters=args.iters, learned_params=prm, learned_form=_lib.MPNN_SYM),
+                          maxiters=args.iters, learned_params=prm, learned_form=_lib.MPNN_SYM,
+                          learned_exec=_lib.MPNN_EXEC_LAYERED if args.layered
+                          else _lib.MPNN_EXEC_FOLDED),
                learned_params_keep=prm)
 
     def one():
@@ -429,8 +434,19 @@ def run_learned_solve(args):
         return S.solve(p.b, xs)
     one()
     ms, r = _ev_ms(ctx.torch_stream, one)
-    print(json.dumps({"size": args.size, "iters": r.iters, "solve_ms": ms,
-                      "ms_per_iter": ms / max(1, r.iters)}), flush=True)
+    # one application of the preconditioner alone (sg_mpnn_forward), the
+    # same evaluation mode, event-timed over 10 calls
+    g = lrn.Graph(ctx, m, p.A, form="sym")
+    g.set_exec(_lib.MPNN_EXEC_LAYERED if args.layered else _lib.MPNN_EXEC_FOLDED)
+    with ctx.stream():
+        rr = torch.rand_like(p.b, dtype=torch.float32)
+        zz = torch.empty_like(rr)
+    g.forward(prm, rr, zz)
+    fwd_ms, _ = _ev_ms(ctx.torch_stream, lambda: g.forward(prm, rr, zz), reps=10)
+    print(json.dumps({"size": args.size, "iters": r.iters, "status": r.status, "solve_ms": ms,
+                      "ms_per_iter": ms / max(1, r.iters), "apply_ms": fwd_ms,
+                      "exec": "layered" if args.layered else "folded"}), flush=True)
+    g.close()
     S.close()
 
 

@@ -397,6 +397,10 @@ typedef struct sg_solve_opts {
                                   next kernel launches while its predecessor
                                   drains); 0 (default): plain graph edges, which
                                   measured 4 % faster at 128^3 */
+  int32_t learned_exec;        /* SG_MPNN_SYM: SG_MPNN_EXEC_FOLDED (default),
+                                  SG_MPNN_EXEC_FOLDED_F32 or SG_MPNN_EXEC_LAYERED
+                                  (see sg_mpnn_graph_set_exec); the other forms
+                                  always run layered */
 } sg_solve_opts;
 
 typedef struct sg_solve_result {
@@ -499,6 +503,17 @@ int sg_mpnn_graph_refresh(sg_mpnn_graph *g);
 enum { SG_MPNN_RELU = 0, SG_MPNN_LINEAR = 1, SG_MPNN_SYM = 2 };
 /* Select the form (default SG_MPNN_RELU). */
 int sg_mpnn_graph_set_form(sg_mpnn_graph *g, int form);
+/* How sg_mpnn_forward (train = 0) evaluates the symmetric form.  With
+ * identity activations every hidden layer is a fixed linear map of the
+ * inputs and messages before it, so the network folds into three small
+ * matrices (8x6, 8x14, 3x22, computed in FP64 from the same bf16-rounded
+ * 64x64 weights): one application of M becomes six gather passes of 3- or
+ * 8-wide vectors over the pattern.  SG_MPNN_EXEC_FOLDED stores the edge
+ * weights as FP16 (2 bytes a block), SG_MPNN_EXEC_FOLDED_F32 as FP32,
+ * SG_MPNN_EXEC_LAYERED (the default here) runs the tensor-core layers.
+ * Training always runs layered. */
+enum { SG_MPNN_EXEC_FOLDED = 0, SG_MPNN_EXEC_LAYERED = 1, SG_MPNN_EXEC_FOLDED_F32 = 2 };
+int sg_mpnn_graph_set_exec(sg_mpnn_graph *g, int exec);
 int sg_mpnn_graph_destroy(sg_mpnn_graph *g);
 /* z = M(r); r, z FP32 [n*3]. */
 int sg_mpnn_forward(sg_mpnn_graph *g, const float *params, const float *r, float *z,

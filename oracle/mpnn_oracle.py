@@ -163,6 +163,82 @@ def forward_sym(params, n, rowptr, colidx, vals, r):
     return z.reshape(-1), dict(cu=cu, y=y, Li=Li, args=(params, n, rowptr, colidx, vals))
 
 
+def fold(params):
+    """The symmetric form's linear network folded into three matrices
+    (float64, from the bf16-rounded W2h/W3h): q2 = C2 [x; m1],
+    q3 = C3 [x; m1; m2], N x = C4 [x; m1; m2; m3] with m1 = Aw x,
+    m2 = Aw q2, m3 = Aw q3.  With identity activations each hidden layer is
+    a fixed linear map of the inputs and messages before it."""
+    p = unpack(params)
+    E1 = np.concatenate([p["W1s"], p["W1m"]], axis=1)               # 64 x 6
+    F2 = np.concatenate([bf16(p["W2h"]) @ E1, p["W2m"]], axis=1)     # 64 x 14
+    F3 = np.concatenate([bf16(p["W3h"]) @ F2, p["W3m"]], axis=1)     # 64 x 22
+    return p["P2"] @ E1, p["P3"] @ F2, p["Wout"] @ F3
+
+
+def forward_sym_folded(params, n, rowptr, colidx, vals, r, a=None):
+    """z = L^-T (I + N)^T (I + N) L^-1 r through the folded matrices: three
+    aggregations forward, three for the adjoint (I + N)^T (Aw symmetric).
+    a: edge weights to use (default edge_weights(); the FP16 variant passes
+    its rounded copy)."""
+    C2, C3, C4 = fold(params)
+    a0, rows, cols = edge_weights(n, rowptr, colidx, vals)
+    if a is None:
+        a = a0
+    agg = lambda x: _agg(a, rows, cols, x, n)  # noqa: E731
+    Li = chol_inv(n, rowptr, colidx, vals)
+    x = np.einsum("vij,vj->vi", Li, np.asarray(r, np.float64).reshape(n, 3))
+    m1 = agg(x)
+    q2 = np.concatenate([x, m1], 1) @ C2.T
+    m2 = agg(q2)
+    q3 = np.concatenate([x, m1, m2], 1) @ C3.T
+    m3 = agg(q3)
+    y = x + np.concatenate([x, m1, m2, m3], 1) @ C4.T
+    # adjoint: the transposed column blocks of C4, C3, C2 in reverse order
+    g3 = agg(y @ C4[:, 14:22])
+    u2 = y @ C4[:, 6:14] + g3 @ C3[:, 6:14]
+    g2 = agg(u2)
+    m1b = y @ C4[:, 3:6] + g3 @ C3[:, 3:6] + g2 @ C2[:, 3:6]
+    w = y + y @ C4[:, 0:3] + g3 @ C3[:, 0:3] + g2 @ C2[:, 0:3] + agg(m1b)
+    z = np.einsum("vji,vj->vi", Li, w)
+    return z.reshape(-1)
+
+
+def poly_coeffs(params):
+    """The symmetric form as a matrix polynomial: with N = sum_k Aw^k (x) B_k
+    (the per-vertex maps commute with the aggregation),
+    (I + N)^T (I + N) = sum_{d=0..6} Aw^d (x) G_d, G_d = sum_{j+k=d} B'_j^T B'_k,
+    B'_0 = I + B_0.  Returns G (7 x 3 x 3), float64."""
+    C2, C3, C4 = fold(params)
+    C2x, C2m1 = C2[:, 0:3], C2[:, 3:6]
+    C3x, C3m1, C3m2 = C3[:, 0:3], C3[:, 3:6], C3[:, 6:14]
+    C4x, C4m1, C4m2, C4m3 = C4[:, 0:3], C4[:, 3:6], C4[:, 6:14], C4[:, 14:22]
+    Bp = [np.eye(3) + C4x,
+          C4m1 + C4m2 @ C2x + C4m3 @ C3x,
+          C4m2 @ C2m1 + C4m3 @ (C3m1 + C3m2 @ C2x),
+          C4m3 @ C3m2 @ C2m1]
+    G = np.zeros((7, 3, 3))
+    for j in range(4):
+        for k in range(4):
+            G[j + k] += Bp[j].T @ Bp[k]
+    return G
+
+
+def forward_sym_poly(params, n, rowptr, colidx, vals, r, a=None):
+    """z = L^-T [sum_d Aw^d (x) G_d] L^-1 r by Horner's scheme
+    (w_6 = G_6 x, w_d = G_d x + Aw w_{d+1}, z = L^-T w_0)."""
+    G = poly_coeffs(params)
+    a0, rows, cols = edge_weights(n, rowptr, colidx, vals)
+    if a is None:
+        a = a0
+    Li = chol_inv(n, rowptr, colidx, vals)
+    x = np.einsum("vij,vj->vi", Li, np.asarray(r, np.float64).reshape(n, 3))
+    w = x @ G[6].T
+    for d in range(5, -1, -1):
+        w = x @ G[d].T + _agg(a, rows, cols, w, n)
+    return np.einsum("vji,vj->vi", Li, w).reshape(-1)
+
+
 def backward_sym(cache, dz):
     """Weight gradient of <dz, M r> for the symmetric form:
     grad_N(input L^-1 r, cotangent (I + N) L^-1 dz) + grad_N(input L^-1 dz,

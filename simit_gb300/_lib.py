@@ -42,7 +42,7 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("precond", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", D), ("maxiters", I32), ("verify", I32), ("check_every", I32),
                 ("reliable_delta", D), ("lanes", I32), ("batch", I32), ("learned_params", P),
-                ("learned_form", I32), ("storage", I32), ("pdl", I32)]
+                ("learned_form", I32), ("storage", I32), ("pdl", I32), ("learned_exec", I32)]
 
 
 class SolveResult(ctypes.Structure):
@@ -53,6 +53,7 @@ class SolveResult(ctypes.Structure):
 
 SOLVE_F64, SOLVE_MIXED = 0, 1
 MPNN_RELU, MPNN_LINEAR, MPNN_SYM = 0, 1, 2
+MPNN_EXEC_FOLDED, MPNN_EXEC_LAYERED, MPNN_EXEC_FOLDED_F32 = 0, 1, 2
 STORAGE_FULL, STORAGE_SYMMETRIC = 0, 1
 RESIDUAL_FP64, RESIDUAL_COMPENSATED = 0, 1
 INCIDENCE_EV, INCIDENCE_VE = 0, 1
@@ -117,6 +118,7 @@ SIGNATURES = {
     "sg_mpnn_graph_create": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(P)]),
     "sg_mpnn_graph_refresh": (_CI, [P]),
     "sg_mpnn_graph_set_form": (_CI, [P, _CI]),
+    "sg_mpnn_graph_set_exec": (_CI, [P, _CI]),
     "sg_mpnn_graph_destroy": (_CI, [P]),
     "sg_mpnn_forward": (_CI, [P, P, P, P, _CI]),
     "sg_mpnn_backward": (_CI, [P, P, P, P]),

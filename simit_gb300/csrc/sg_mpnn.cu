@@ -3,6 +3,7 @@
 #include <math.h>
 
 #include "sg_internal.cuh"
+#include "sg_mpnn_fold.cuh"
 #include "sg_mpnn_fwd.cuh"
 #include "sg_solver.h"
 #include "sg_spmv_api.h"
@@ -18,6 +19,13 @@ struct GraphH {
   // symmetric form: a second set of layer buffers over the same graph data
   // (the transposed network's pass, and the second training forward)
   GraphH *twin = nullptr;
+  // folded evaluation of the symmetric form (sg_mpnn_fold.cuh): its buffers
+  // (allocated on first use), FP16 edge weights, packed L^-1
+  int exec = SG_MPNN_EXEC_LAYERED;  // how sg_mpnn_forward evaluates (train = 0)
+  bool fold_ready = false;
+  FoldBufs fb{};
+  float *fold = nullptr;
+  __half *ah = nullptr;
 };
 
 static int galloc(GraphH *G, void **p, size_t bytes) {
@@ -220,6 +228,12 @@ static int graph_refresh(GraphH *G) {
       k_chol_inv<float><<<gr, 256, 0, c->stream>>>(g.n, g.rowptr, g.colidx, (const float *)g.vals, g.linv);
   }
   SG_CHECK_LAUNCH();
+  if (G->fold_ready) {
+    const int ge = grid_for(c, g.nnzb, 256, 8);
+    k_edge_half<<<ge, 256, 0, c->stream>>>(g.nnzb, g.a, G->ah);
+    k_pack_linv<<<gr, 256, 0, c->stream>>>(g.n, g.linv, (float *)G->fb.l6);
+    SG_CHECK_LAUNCH();
+  }
   return check_device_error(c, "mpnn graph");
 }
 
@@ -295,6 +309,71 @@ static int graph_init(Ctx *c, const sg_matrix *A, GraphH *G) {
     return SG_OK;
   }));
   return graph_refresh(G);
+}
+
+// Buffers and graph data of the folded evaluation (symmetric form only).
+static int ensure_folded(GraphH *G) {
+  if (G->fold_ready) return SG_OK;
+  Graph &g = G->g;
+  SG_REQUIRE(g.sym && g.linv, "mpnn: the folded evaluation needs the symmetric form");
+  const size_t n = (size_t)g.n;
+  FoldBufs &B = G->fb;
+  float *l6 = nullptr;
+  SG_TRY(galloc(G, (void **)&G->fold, NPOLY * 9 * 4));
+  SG_TRY(galloc(G, (void **)&G->ah, (size_t)g.nnzb * 2));
+  SG_TRY(galloc(G, (void **)&l6, n * 6 * 4));
+  B.l6 = l6;
+  for (float **p : {&B.xin, &B.w[0], &B.w[1]}) SG_TRY(galloc(G, (void **)p, n * 4 * 4));
+  B.rowptr = g.rowptr;
+  B.colidx = g.colidx;
+  B.g = G->fold;
+  G->fold_ready = true;
+  return graph_refresh(G);
+}
+
+// The folded application z = M r (symmetric form): x = L^-1 r and
+// w_6 = G_6 x (unless the iteration's K2 wrote them: xin_ready), the six
+// Horner steps, z = L^-T w_0.  part (nullable): dot partials of the last
+// step (grid np blocks); want_rr / want_zq select its slices.
+static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, bool half_a,
+                      const float *r, float *z, const float *q, double *part, int np, int want_rr,
+                      int want_zq, bool xin_ready) {
+  Ctx *c = G->c;
+  Graph &g = G->g;
+  FoldBufs B = G->fb;
+  B.a = half_a ? (const void *)G->ah : (const void *)g.a;
+  if (!xin_ready) {
+    k_lrn_xin<<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, B.g + 6 * 9, r, B.xin, B.w[0]);
+    SG_CHECK_LAUNCH();
+  }
+  const int gl = grid_for(c, (int64_t)g.n * 4, LG_T, 8);
+  const int g0 = part ? np : gl;
+  // w_6 in w[0]; step d reads w[(5 - d) & 1] and writes the other buffer
+  for (int d = 5; d >= 1; --d) {
+    float *src = B.w[(5 - d) & 1], *dst = B.w[(6 - d) & 1];
+    if (half_a)
+      k_horner<__half, false><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, nullptr,
+                                                    nullptr, nullptr, nullptr, 0, 0);
+    else
+      k_horner<float, false><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, nullptr,
+                                                   nullptr, nullptr, nullptr, 0, 0);
+  }
+  float *w1 = B.w[1];  // written by d = 1
+  if (half_a)
+    k_horner<__half, true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B, 0, w1, nullptr, r, q, z, part,
+                                                 want_rr, want_zq);
+  else
+    k_horner<float, true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B, 0, w1, nullptr, r, q, z, part,
+                                                want_rr, want_zq);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
+// Polynomial coefficients of a parameter set (one small kernel).
+static int fold_params(GraphH *G, cudaStream_t st, const float *prm) {
+  k_fold<<<1, 256, 0, st>>>(prm, G->fold);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
 }
 
 static int ensure_train(GraphH *G) {
@@ -449,10 +528,32 @@ static int backward_net(GraphH *G, const float *prm, const float *dz, float *gra
 struct LearnedExt {
   mpnn::GraphH *G = nullptr;
   const float *prm = nullptr;
+  int exec = SG_MPNN_EXEC_FOLDED;  // folded (FP16 or FP32 edge weights) or layered
 };
+
+static bool folded(const LearnedExt *L) { return L->exec != SG_MPNN_EXEC_LAYERED; }
+
+// K2 of the folded learned iteration (replaces k_cg_update_v4): r update and
+// x = L^-1 r; x += alpha p moves to K3.
+static int learned_k2(Solver *S, cudaStream_t st, int par) {
+  LearnedExt *L = (LearnedExt *)S->ext;
+  // the TMA-staged and symmetric-storage K1 leave the p.q total in ctl
+  const int pq_fin = (S->tma || S->sym) ? 1 : 0;
+  const mpnn::FoldBufs &B = L->G->fb;
+  mpnn::k_lrn_update<<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->A.n, S->part1, S->P1, pq_fin,
+                                              (const float *)S->q, (float *)S->r, B.l6,
+                                              B.g + 6 * 9, B.xin, B.w[0]);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
 
 static int learned_prec(Solver *S, cudaStream_t st) {
   LearnedExt *L = (LearnedExt *)S->ext;
+  if (folded(L))
+    // S6 leaves r.r | r.z | z.q for K3 (P2 blocks)
+    return mpnn::fold_apply(L->G, st, S->ctl, 1, L->exec == SG_MPNN_EXEC_FOLDED,
+                            (const float *)S->r, (float *)S->z, (const float *)S->q, S->part2,
+                            S->np2_ext, 1, 1, true);
   SG_TRY(mpnn::forward(L->G, st, S->ctl, 1, L->prm, (const float *)S->r, (float *)S->z, false));
   mpnn::k_rz_zq<<<S->P2, RED_T, 0, st>>>(S->ctl, S->len, (const float *)S->r, (const float *)S->z,
                                          (const float *)S->q, S->part2);
@@ -476,6 +577,13 @@ __global__ void __launch_bounds__(RED_T) k_rz_only(int64_t len, const float *r, 
 static int learned_apply(Solver *S, cudaStream_t st) {
   LearnedExt *L = (LearnedExt *)S->ext;
   // the control block's fallback flag also governs restarts
+  if (folded(L)) {
+    // the parameters may have changed since the last solve: fold them again
+    SG_TRY(mpnn::fold_params(L->G, st, L->prm));
+    return mpnn::fold_apply(L->G, st, S->ctl, 0, L->exec == SG_MPNN_EXEC_FOLDED,
+                            (const float *)S->r, (float *)S->z, nullptr, S->part3, S->P2, 0, 0,
+                            false);
+  }
   SG_TRY(mpnn::forward(L->G, st, S->ctl, 0, L->prm, (const float *)S->r, (float *)S->z, false));
   k_rz_only<<<S->P2, RED_T, 0, st>>>(S->len, (const float *)S->r, (const float *)S->z, S->part3);
   SG_CHECK_LAUNCH();
@@ -494,6 +602,7 @@ static void learned_free(Solver *S) {
 // through thread-local slots, so solvers may be created concurrently
 static thread_local const float *g_pending_params = nullptr;
 static thread_local int g_pending_form = 0;
+static thread_local int g_pending_exec = 0;
 static int learned_setup(Solver *S) {
   LearnedExt *L = new LearnedExt();
   S->ext = L;
@@ -503,9 +612,27 @@ static int learned_setup(Solver *S) {
   SG_TRY(mpnn::graph_init(S->c, &S->A, L->G));
   SG_TRY(mpnn::set_sym(L->G, g_pending_form == SG_MPNN_SYM));
   L->G->g.lin = g_pending_form != SG_MPNN_RELU;
+  // the folded evaluation serves the symmetric form; the others run layered
+  L->exec = g_pending_form == SG_MPNN_SYM ? g_pending_exec : SG_MPNN_EXEC_LAYERED;
   S->ext_prec = learned_prec;
   S->ext_prec_apply = learned_apply;
   S->flexible = 1;
+  if (folded(L)) {
+    SG_TRY(mpnn::ensure_folded(L->G));
+    S->ext_k2 = learned_k2;
+    S->k3_xupd = 1;
+    // the last Horner step runs on the passes' full grid and leaves that
+    // many partials per dot for K3
+    const int g0 = grid_for(S->c, (int64_t)S->A.n * 4, mpnn::LG_T, 8);
+    const int np = S->P1 > S->P2 ? S->P1 : S->P2;
+    if (g0 > np) {
+      void *p2 = nullptr;
+      SG_CHECK_CUDA(cudaMalloc(&p2, (size_t)g0 * 3 * 8));
+      S->allocs.push_back(p2);
+      S->part2 = (double *)p2;
+    }
+    S->np2_ext = g0;
+  }
   return SG_OK;
 }
 
@@ -518,6 +645,7 @@ int learned_solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, cons
                         Solver *S) {
   g_pending_params = params;
   g_pending_form = o->learned_form;
+  g_pending_exec = o->learned_exec;
   int rc = solver_init(c, A, o, S, learned_setup);
   g_pending_params = nullptr;
   return rc;
@@ -570,9 +698,26 @@ int sg_mpnn_graph_destroy(sg_mpnn_graph *hg) {
   return SG_OK;
 }
 
+int sg_mpnn_graph_set_exec(sg_mpnn_graph *hg, int exec) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  SG_REQUIRE(G, "sg_mpnn_graph_set_exec: null graph");
+  SG_REQUIRE(exec >= SG_MPNN_EXEC_FOLDED && exec <= SG_MPNN_EXEC_FOLDED_F32,
+             "sg_mpnn_graph_set_exec: mode %d", exec);
+  SG_REQUIRE(exec == SG_MPNN_EXEC_LAYERED || G->g.sym,
+             "sg_mpnn_graph_set_exec: the folded evaluation needs the symmetric form");
+  if (exec != SG_MPNN_EXEC_LAYERED) SG_TRY(mpnn::ensure_folded(G));
+  G->exec = exec;
+  return SG_OK;
+}
+
 int sg_mpnn_forward(sg_mpnn_graph *hg, const float *params, const float *r, float *z, int train) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
   SG_REQUIRE(G && params && r && z, "sg_mpnn_forward: null argument");
+  if (!train && G->exec != SG_MPNN_EXEC_LAYERED && G->g.sym) {
+    SG_TRY(mpnn::fold_params(G, G->c->stream, params));
+    return mpnn::fold_apply(G, G->c->stream, nullptr, 0, G->exec == SG_MPNN_EXEC_FOLDED, r, z,
+                            nullptr, nullptr, 0, 0, 0, false);
+  }
   if (train) SG_TRY(mpnn::ensure_train(G));
   return mpnn::forward(G, G->c->stream, nullptr, 0, params, r, z, train != 0);
 }

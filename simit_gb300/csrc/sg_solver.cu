@@ -165,6 +165,7 @@ static void launch_k2_v4(Solver *S, cudaStream_t st, int par) {
 
 template <typename VT, typename XT>
 static int launch_k2(Solver *S, cudaStream_t st, int par) {
+  if (S->ext_k2) return S->ext_k2(S, st, par);
   const VT *p = (const VT *)S->p, *q = (const VT *)S->q, *dinv = (const VT *)S->dinv;
   VT *r = (VT *)S->r, *z = (VT *)S->z;
   XT *x = (XT *)S->xupd;
@@ -223,9 +224,10 @@ static int launch_k2(Solver *S, cudaStream_t st, int par) {
 template <typename VT>
 static int launch_k3(Solver *S, cudaStream_t st, int par) {
   const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
+  const int np2 = S->np2_ext > 0 ? S->np2_ext : S->P2;
   if (sizeof(VT) == 4)  // K2 decided unless an external preconditioner ran after it
     SG_CHECK_CUDA(launch_k(S->c, k_cg_direction_v4, S->P2, RED_T, 0, st, S->ctl, par, S->len,
-                           (const double *)S->part2, S->P2, (int)(S->prec != PK_EXTERNAL),
+                           (const double *)S->part2, np2, (int)(S->prec != PK_EXTERNAL),
                            (const float *)z, (float *)S->p, (float *)S->xupd, S->k3_xupd));
   else
     k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z,

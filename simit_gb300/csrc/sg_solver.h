@@ -42,6 +42,12 @@ struct Solver {
   int (*ext_prec)(Solver *, cudaStream_t) = nullptr;
   int (*ext_prec_apply)(Solver *, cudaStream_t) = nullptr;
   void (*ext_free)(Solver *) = nullptr;
+  // ext_k2 (optional) replaces the iteration's K2 (the folded learned
+  // iteration's r update and x = L^-1 r)
+  int (*ext_k2)(Solver *, cudaStream_t, int par) = nullptr;
+  // > 0: K3 sums this many partials per dot (the external preconditioner's
+  // last kernel wrote them with its own grid), else P2
+  int np2_ext = 0;
   void *ext = nullptr;
   SymBsr *sym = nullptr;  // SG_STORAGE_SYMMETRIC: K1 reads the upper half
   int k3_xupd = 0;        // K3 applies x += alpha p (K2 = k_cg_update_w without x)

@@ -651,9 +651,10 @@ __global__ void __launch_bounds__(K2W_WARPS * 32) k_cg_update_w(
 // K3 for FP32 vectors: the control decisions of k_cg_direction, then
 // p = z + beta p with float4 accesses.
 // fin: K2 already took the decision and left beta in ctl->beta.
-// xupd (with fin): K2 left x += alpha p to this kernel, which applies it with
-// the direction it is about to replace; when K2 stopped the batch, the host
-// applies that last update instead (the early return below).
+// xupd: K2 left x += alpha p to this kernel, which applies it with the
+// direction it is about to replace; when K2 (fin) or this kernel (!fin)
+// stopped the batch, the host applies that last update instead (the early
+// returns below).
 static __global__ void __launch_bounds__(RED_T) k_cg_direction_v4(SolveCtl *ctl, int par, int64_t len,
                                                            const double *__restrict__ part_in,
                                                            int np2, int fin,
@@ -713,18 +714,31 @@ static __global__ void __launch_bounds__(RED_T) k_cg_direction_v4(SolveCtl *ctl,
   if (st != ST_RUNNING) return;
   const double beta = ctl->flexible ? (-ctl->last_alpha * zq) / rzold : rznew / rzold;
   const float b = (float)beta;
+  // xupd: the iteration's x += alpha p, applied here with the direction it
+  // is about to replace (on a stop above the host applies it instead)
+  const float a = (float)ctl->last_alpha;
   const int64_t nu = len / 4;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu;
        u += (int64_t)gridDim.x * blockDim.x) {
     float zv[4], pv[4];
     ld4(z, u, zv);
     ld4(p, u, pv);
+    if (xupd) {
+      float xv[4];
+      ld4(x, u, xv);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) xv[k] = xv[k] + a * pv[k];
+      st4(x, u, xv);
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) pv[k] = zv[k] + b * pv[k];
     st4(p, u, pv);
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
-    for (int64_t i = nu * 4; i < len; ++i) p[i] = z[i] + b * p[i];
+    for (int64_t i = nu * 4; i < len; ++i) {
+      if (xupd) x[i] = x[i] + a * p[i];
+      p[i] = z[i] + b * p[i];
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -66,6 +66,10 @@ class Graph:
         self.n = mesh.n
         call("sg_mpnn_graph_set_form", h, FORMS[form])
 
+    def set_exec(self, mode):
+        """_lib.MPNN_EXEC_*: how forward() evaluates the symmetric form."""
+        call("sg_mpnn_graph_set_exec", self.h, int(mode))
+
     def forward(self, params, r, z, train=False):
         call("sg_mpnn_forward", self.h, ptr(params), ptr(r), ptr(z), int(train))
 
@@ -233,8 +237,9 @@ def train(ctx, sizes=(16, 24, 32, 40, 48), n_pairs=2000, epochs=6, lr=1e-3, seed
     return params, hist
 
 
-def compare(ctx, params, ncell, seed=999, tol=1e-8, form="sym"):
-    """Flexible PCG with the network vs block-Jacobi PCG on a held-out mesh."""
+def compare(ctx, params, ncell, seed=999, tol=1e-8, form="sym", exec_mode=_lib.MPNN_EXEC_FOLDED):
+    """Flexible PCG with the network vs block-Jacobi PCG on a held-out mesh.
+    exec_mode: how the symmetric form is evaluated (_lib.MPNN_EXEC_*)."""
     host = problems.hetero_mesh(ncell, seed=seed)
     out = {}
     d = ctx.device
@@ -248,7 +253,7 @@ def compare(ctx, params, ncell, seed=999, tol=1e-8, form="sym"):
         S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, m.nnzb,
                    solve_opts(precision=_lib.SOLVE_MIXED, precond=pc, tol=tol, maxiters=100000,
                               learned_params=prm if pc == _lib.PRECOND_LEARNED else None,
-                              learned_form=FORMS[form]),
+                              learned_form=FORMS[form], learned_exec=exec_mode),
                    learned_params_keep=prm)
         x = torch.zeros_like(prob.b)
         torch.cuda.synchronize()

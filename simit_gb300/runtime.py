@@ -474,11 +474,12 @@ def assemble_heat(mesh, B, W, kappa, dt, T0, dtype=torch.float64, exact=True):
 
 def solve_opts(precision=_lib.SOLVE_F64, precond=_lib.PRECOND_NONE, stop=_lib.STOP_RELATIVE,
                tol=1e-8, maxiters=10000, verify=1, check_every=0, reliable_delta=0.1, lanes=0,
-               batch=32, learned_params=None, learned_form=0, storage=0, pdl=0):
+               batch=32, learned_params=None, learned_form=0, storage=0, pdl=0,
+               learned_exec=_lib.MPNN_EXEC_FOLDED):
     lp = learned_params.data_ptr() if learned_params is not None else None
     return _lib.SolveOpts(precision, precond, stop, tol, maxiters, verify, check_every,
                           reliable_delta, lanes, batch, lp, int(learned_form), int(storage),
-                          int(pdl))
+                          int(pdl), int(learned_exec))
 
 
 class Solver:

@@ -114,3 +114,101 @@ def test_trained_network_gain(ctx, form):
     if form == "sym":
         assert ln["fallbacks"] == 0
         assert ln["iters"] < bj["iters"]
+
+
+def test_folded_forward_matches_layered_and_oracle(ctx):
+    """The symmetric form evaluated as its degree-6 matrix polynomial (six
+    Horner gather passes) against the oracle's restatement in FP64, with
+    FP32 and with FP16 edge weights, and against the tensor-core layered
+    evaluation of the same network."""
+    from oracle import mpnn_oracle as mo
+    from simit_gb300 import learned
+    prob = _small(ctx, 6, seed=5)
+    m = prob.mesh
+    rp, ci = m.pattern.host()
+    vals = prob.A.cpu().numpy()
+    g = learned.Graph(ctx, m, prob.A, form="sym")
+    params = learned.load_weights("sym")
+    rng = np.random.Generator(np.random.Philox(12))
+    r = rng.normal(size=m.n * 3).astype(np.float32)
+    d = ctx.device
+    pt = torch.tensor(params, device=d)
+    rt = torch.tensor(r, device=d)
+    out = {}
+    for mode in (_lib.MPNN_EXEC_FOLDED_F32, _lib.MPNN_EXEC_FOLDED, _lib.MPNN_EXEC_LAYERED):
+        g.set_exec(mode)
+        zt = torch.empty_like(rt)
+        g.forward(pt, rt, zt)
+        ctx.sync()
+        out[mode] = zt.cpu().numpy().astype(np.float64)
+    z_ref = mo.forward_sym_poly(params, m.n, rp, ci, vals, r)
+    a, _, _ = mo.edge_weights(m.n, rp, ci, vals)
+    z_ref16 = mo.forward_sym_poly(params, m.n, rp, ci, vals, r,
+                                    a=a.astype(np.float16).astype(np.float64))
+    bj = np.einsum("vij,vj->vi", mo.block_jacobi(m.n, rp, ci, vals),
+                   r.reshape(-1, 3).astype(np.float64)).reshape(-1)
+    corr = np.linalg.norm(z_ref - bj)
+    assert corr > 1e-3 * np.linalg.norm(bj)
+    e32 = np.linalg.norm(out[_lib.MPNN_EXEC_FOLDED_F32] - z_ref)
+    e16 = np.linalg.norm(out[_lib.MPNN_EXEC_FOLDED] - z_ref16)
+    el = np.linalg.norm(out[_lib.MPNN_EXEC_LAYERED] - out[_lib.MPNN_EXEC_FOLDED_F32])
+    print("folded FP32 %.2e, folded FP16 %.2e, layered vs folded %.2e (of the correction %.3e)"
+          % (e32 / corr, e16 / corr, el / corr, corr))
+    # FP32 arithmetic (FP32 folded matrices and sums) against FP64
+    assert e32 <= 2e-5 * corr
+    assert e16 <= 2e-4 * corr
+    # the layered kernels carry the hidden layers as split bf16 (about 2^-16)
+    assert el <= 1e-3 * corr
+    g.close()
+    prob.close()
+
+
+def test_folded_solve_matches_layered_solve(ctx):
+    """Flexible PCG with the folded evaluation takes the iterations of the
+    layered one (the same operator) and converges to the FP64 tolerance."""
+    from simit_gb300 import learned
+    w = learned.load_weights("sym")
+    rf = learned.compare(ctx, w, 12, seed=778)
+    rl = learned.compare(ctx, w, 12, seed=778, exec_mode=_lib.MPNN_EXEC_LAYERED)
+    ff, ll = rf["learned"], rl["learned"]
+    print("folded %d iters %.1f ms, layered %d iters %.1f ms" % (ff["iters"], ff["ms"],
+                                                                 ll["iters"], ll["ms"]))
+    assert ff["status"] == 1 and ff["relres"] <= 1e-8 and ff["fallbacks"] == 0
+    assert abs(ff["iters"] - ll["iters"]) <= max(2, 0.03 * ll["iters"])
+
+
+def test_folded_forward_long_rows(ctx):
+    """A pattern with one row of 5000 entries (a vertex joined to every
+    other one) beside rows of 2-3: the Horner passes' lanes loop over the
+    long row; the result matches the oracle's polynomial."""
+    from oracle import mpnn_oracle as mo
+    from simit_gb300 import learned
+    from simit_gb300.runtime import Mesh
+    n = 5000
+    edges = np.array([(0, i) for i in range(1, n)] + [(i, i + 1) for i in range(1, n - 1)],
+                     dtype=np.int32)
+    m = Mesh(ctx, n, edges, 2)
+    rp, ci = m.pattern.host()
+    rows = np.repeat(np.arange(n), np.diff(rp.astype(np.int64)))
+    rng = np.random.Generator(np.random.Philox(13))
+    blocks = rng.normal(0, 0.1, size=(m.nnzb, 3, 3))
+    diag = rows == ci.astype(np.int64)
+    S = rng.normal(0, 0.2, size=(int(diag.sum()), 3, 3))
+    blocks[diag] = 10.0 * np.eye(3) + 0.5 * (S + np.transpose(S, (0, 2, 1)))
+    vals = blocks.reshape(-1).astype(np.float32)
+    A = torch.tensor(vals, device=ctx.device)
+    g = learned.Graph(ctx, m, A, form="sym")
+    g.set_exec(_lib.MPNN_EXEC_FOLDED)
+    params = learned.load_weights("sym")
+    r = rng.normal(size=n * 3).astype(np.float32)
+    pt = torch.tensor(params, device=ctx.device)
+    rt = torch.tensor(r, device=ctx.device)
+    zt = torch.empty_like(rt)
+    g.forward(pt, rt, zt)
+    ctx.sync()
+    a, _, _ = mo.edge_weights(n, rp, ci, vals.astype(np.float64))
+    z_ref = mo.forward_sym_poly(params, n, rp, ci, vals.astype(np.float64), r,
+                                a=a.astype(np.float16).astype(np.float64))
+    err = np.linalg.norm(zt.cpu().numpy() - z_ref)
+    assert err <= 1e-5 * np.linalg.norm(z_ref), err
+    g.close()

@@ -86,3 +86,46 @@ def test_transpose_params_is_the_adjoint(system, exact):
     NTv = wp.reshape(n, 3) - v + mo._agg(c["a"], c["rows"], c["cols"],
                                          c["h3"] @ mo.unpack(p)["W1m"], n)
     assert abs((v * Nu).sum() - (NTv * u).sum()) <= 1e-10 * abs((v * Nu).sum())
+
+
+def test_folded_operator_equals_the_layered_network(system):
+    """The folded evaluation (three small matrices, six aggregations) is the
+    same operator as the layered symmetric form: equal to its split-bf16
+    activations' accuracy (about 2^-16 of the correction), exactly in exact
+    arithmetic."""
+    n, rp, ci, A = system
+    rng = np.random.default_rng(4)
+    from simit_gb300 import learned
+    p = learned.load_weights("sym").astype(np.float64)  # the trained symmetric-form weights
+    r = rng.normal(size=n * 3)
+    zl = mo.forward_sym(p, n, rp, ci, A, r)[0]
+    zf = mo.forward_sym_folded(p, n, rp, ci, A, r)
+    bj = np.einsum("vij,vj->vi", mo.block_jacobi(n, rp, ci, A), r.reshape(n, 3)).reshape(-1)
+    corr = np.linalg.norm(zl - bj)
+    assert corr > 0
+    assert np.linalg.norm(zf - zl) <= 1e-4 * corr
+
+
+def test_folded_operator_is_exact_in_exact_arithmetic(system, exact):
+    n, rp, ci, A = system
+    rng = np.random.default_rng(5)
+    p = mo.init_params(6, out_scale=1.0).astype(np.float64)
+    r = rng.normal(size=n * 3)
+    zl = mo.forward_sym(p, n, rp, ci, A, r)[0]
+    zf = mo.forward_sym_folded(p, n, rp, ci, A, r)
+    assert np.allclose(zf, zl, rtol=1e-11, atol=1e-12 * np.abs(zl).max())
+
+
+def test_polynomial_form_equals_the_folded_operator(system, exact):
+    """The degree-6 matrix polynomial in the edge-weight aggregation (the
+    evaluation the GPU runs) equals the folded network and the layered
+    network in exact arithmetic, and its coefficients are symmetric."""
+    n, rp, ci, A = system
+    rng = np.random.default_rng(7)
+    p = mo.init_params(8, out_scale=1.0).astype(np.float64)
+    r = rng.normal(size=n * 3)
+    zl = mo.forward_sym(p, n, rp, ci, A, r)[0]
+    zp = mo.forward_sym_poly(p, n, rp, ci, A, r)
+    assert np.allclose(zp, zl, rtol=1e-11, atol=1e-12 * np.abs(zl).max())
+    G = mo.poly_coeffs(p)
+    assert np.allclose(G, np.transpose(G, (0, 2, 1)), rtol=1e-12, atol=1e-14 * np.abs(G).max())
