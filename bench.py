@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--learned-solve", action="store_true",
                     help="profiling driver: the --size system with the learned preconditioner, "
                          "capped at --iters iterations")
+    ap.add_argument("--assembly-only", action="store_true",
+                    help="profiling driver: the --size workload's assembly (stiffness map in "
+                         "place + force map), element-parallel over the colouring and by row "
+                         "owners, event-timed")
     ap.add_argument("--layered", action="store_true",
                     help="--learned-solve: evaluate the network layer by layer on the tensor "
                          "cores instead of folded")
@@ -448,6 +452,41 @@ def run_learned_solve(args):
                       "exec": "layered" if args.layered else "folded"}), flush=True)
     g.close()
     S.close()
+
+
+def run_assembly_only(args):
+    """Profiling driver: the --size heterogeneous-elasticity step's assembly
+    (stiffness map in place + force map, FP32) with the element-blocks +
+    gather plan, the coloured plan and the row owners, each event-timed over
+    --reps calls; also each plan's set-up time."""
+    import torch
+    from simit_gb300 import _lib, problems
+    from simit_gb300.runtime import Context
+    ctx = Context(0)
+    torch.cuda.set_stream(ctx.torch_stream)
+    h = problems.hetero_mesh(args.size)
+    if not args.no_reorder:
+        h = problems.reorder_hetero(h)
+    out = {"size": args.size}
+    for name, plan in (("gather", "gather"), ("colored", "colored"), ("row_owner", None)):
+        p = problems.HeteroElasticity(ctx, h, dtype=torch.float32,
+                                      precond=_lib.PRECOND_BLOCK_JACOBI, plan=plan)
+        if plan is not None:
+            ctx.sync()
+            t0 = time.perf_counter()
+            p.mesh.color_plan() if plan == "colored" else p.mesh.gather_plan()
+            ctx.sync()
+            out[name + "_plan_s"] = time.perf_counter() - t0
+            if plan == "colored":
+                out["ncolors"] = p.mesh.ncolors
+        p.assemble_in_place()
+        ms, _ = _ev_ms(ctx.torch_stream, p.assemble_in_place, reps=args.reps)
+        out[name + "_ms"] = ms
+        out[name + "_tets_per_s"] = p.mesh.nE / (ms / 1e3)
+        p.close()
+        del p
+        torch.cuda.empty_cache()
+    print(json.dumps(out), flush=True)
 
 
 def run_spmv_only(args):
@@ -928,6 +967,9 @@ def main():
         return
     if args.spmv_only:
         run_spmv_only(args)
+        return
+    if args.assembly_only:
+        run_assembly_only(args)
         return
     if args.cloth:
         rank, world, local = dist_setup(args)

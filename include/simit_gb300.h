@@ -150,7 +150,43 @@ typedef struct sg_mesh {
   const uint32_t *colidx;
   int64_t nnzb;
   int32_t maxrow;             /* sg_pattern_maxrow */
+  /* Optional element-parallel assembly plans (assembly with exact == 0
+   * computes every element once; exact == 1 always runs the row-owner
+   * kernels, the reference's element order bit for bit; NULL / 0 everywhere:
+   * row owners).  Both need slots.
+   *  - slot_src_ptr / slot_src set (sg_slot_sources): element blocks are
+   *    written once, then every slot sums its blocks in ascending element
+   *    order and every vertex its vector contributions (deterministic).
+   *  - else color_order / color_ptr set (sg_element_coloring): blocks are
+   *    added into their slots colour by colour (no two elements of a colour
+   *    share a vertex, so no atomics; deterministic, colour order). */
+  const uint32_t *slots;       /* device [nE*card*card] (sg_slots_build) */
+  const uint32_t *color_order; /* device [nE] (sg_element_coloring) */
+  const int32_t *color_ptr;    /* HOST [ncolors+1]: colour k is
+                                  color_order[color_ptr[k] .. color_ptr[k+1]) */
+  int32_t ncolors;
+  const uint32_t *slot_src_ptr; /* device [nnzb+1] (sg_slot_sources) */
+  const uint32_t *slot_src;     /* device [nE*card*card] */
 } sg_mesh;
+
+/* The inverse slot map for the element-blocks plan: for slot q, the element
+ * blocks (e*card + i)*card + j with slots[...] == q, ascending, at
+ * slot_src[slot_src_ptr[q] .. slot_src_ptr[q+1]).  Needs m->slots (and
+ * nnzb).  Replaces the per-element `loc` searches of the reference's map
+ * lowering (src/inline.cpp:524-577, src/runtime.cpp:19-23) with a gather. */
+int sg_slot_sources(sg_ctx *ctx, const sg_mesh *m, uint32_t *slot_src_ptr, uint32_t *slot_src);
+
+/* Element colouring for the plan above: no two elements of a colour share a
+ * vertex (Jones-Plassmann with hashed priorities, deterministic).
+ * color_order (device [nE]) receives the elements colour by colour,
+ * ascending index within a colour; color_ptr (HOST, SG_MAX_COLORS + 1
+ * entries) the colour offsets; *h_ncolors the colour count.  Needs the mesh's
+ * endpoints and incidence; synchronises.  No counterpart in the reference,
+ * whose GPU backend adds element blocks with float atomics
+ * (src/backend/gpu/gpu_backend.cpp:788-846). */
+#define SG_MAX_COLORS 128
+int sg_element_coloring(sg_ctx *ctx, const sg_mesh *m, uint32_t *color_order,
+                        int32_t *color_ptr, int32_t *h_ncolors);
 
 enum { SG_MODEL_LINEAR = 0, SG_MODEL_NEOHOOKEAN = 1 };
 

@@ -28,7 +28,9 @@ class SimitError(RuntimeError):
 class Mesh(ctypes.Structure):
     """sg_mesh"""
     _fields_ = [("n", I32), ("card", I32), ("nE", I64), ("endpoints", P), ("ve_ptr", P),
-                ("ve_idx", P), ("rowptr", P), ("colidx", P), ("nnzb", I64), ("maxrow", I32)]
+                ("ve_idx", P), ("rowptr", P), ("colidx", P), ("nnzb", I64), ("maxrow", I32),
+                ("slots", P), ("color_order", P), ("color_ptr", P), ("ncolors", I32),
+                ("slot_src_ptr", P), ("slot_src", P)]
 
 
 class Matrix(ctypes.Structure):
@@ -61,6 +63,7 @@ PRECOND_NONE, PRECOND_JACOBI, PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1, 2, 3
 STOP_NORMR2, STOP_NORMR, STOP_RELATIVE = 0, 1, 2
 STATUS = {1: "converged", 2: "maxiter", 3: "breakdown", 4: "nan"}
 MODEL_LINEAR, MODEL_NEOHOOKEAN = 0, 1
+MAX_COLORS = 128
 
 _MP = ctypes.POINTER(Mesh)
 _CI = ctypes.c_int
@@ -77,6 +80,8 @@ SIGNATURES = {
     "sg_pattern_count": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P, ctypes.POINTER(I64)]),
     "sg_pattern_fill": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P, P]),
     "sg_slots_build": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P]),
+    "sg_element_coloring": (ctypes.c_int, [P, ctypes.POINTER(Mesh), P, P, ctypes.POINTER(I32)]),
+    "sg_slot_sources": (ctypes.c_int, [P, ctypes.POINTER(Mesh), P, P]),
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),

@@ -54,6 +54,7 @@ template <typename T> struct AsmArgs {
   T *vals = nullptr, *f = nullptr;
   int *err = nullptr;
   int maxrow = 0;
+  int64_t nnzb = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -223,6 +224,248 @@ __global__ void __launch_bounds__(128) k_rows(AsmArgs<T> a) {
     }
     if (Elem::HAS_VEC && gl < BS) a.f[v * BS + gl] = Elem::fin_vec(a, (int32_t)v, gl, vacc);
     __syncwarp(gmask);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Element-parallel kernel (one colour of the assembly plan)
+// ---------------------------------------------------------------------------
+// Each element is computed once: the threads of an element (one per block
+// (i, j) for matrix maps, one per local vertex i for vector-only maps) add
+// its contributions into the precomputed slots / rows with plain
+// read-modify-writes.  No two elements of a colour share a vertex, so no
+// other thread touches those values during the launch; colours run in
+// order, so every value is summed in the same order on every run.  An
+// element that lists one vertex twice sends several blocks to one slot: its
+// first thread then adds all of them in turn.  Needs Elem::fin_* to be the
+// identity (the outputs start from zero and take the sums as they are).
+//
+// Sequential form (an element with a repeated vertex, one thread).
+template <class Elem, int CARD, int BS, typename T>
+__device__ __forceinline__ void colored_row(const AsmArgs<T> &a, int64_t e, int i,
+                                            const uint32_t *__restrict__ slots) {
+  const int32_t vi = a.ep[e * CARD + i];
+  if (Elem::HAS_MAT) {
+    for (int j = 0; j < CARD; ++j) {
+      const uint32_t sl = slots[(e * CARD + i) * CARD + j];
+      if ((int64_t)sl >= a.nnzb) {
+        atomicCAS(a.err, 0, 3 /* DEV_SLOT_MISSING */);
+        continue;
+      }
+      for (int l = 0; l < BS; ++l) {
+        T out[2][BS];
+        const int nt = Elem::block(a, e, i, j, l, out);
+        if (nt > 0) {
+          T *dst = a.vals + (size_t)sl * BS * BS + l * BS;
+          for (int q = 0; q < BS; ++q) {
+            T v = dst[q] + out[0][q];
+            if (nt > 1) v += out[1][q];
+            dst[q] = v;
+          }
+        }
+      }
+    }
+  }
+  if (Elem::HAS_VEC) {
+    for (int l = 0; l < BS; ++l) {
+      T o[4];
+      const int nv = Elem::vec(a, e, i, l, o);
+      if (nv > 0) {
+        T v = a.f[(int64_t)vi * BS + l];
+        for (int q = 0; q < nv; ++q) v += o[q];
+        a.f[(int64_t)vi * BS + l] = v;
+      }
+    }
+  }
+}
+
+// Usual form (distinct vertices), one thread per block (i, j) of a matrix
+// element (its old values loaded first -- independent loads, one memory
+// round trip -- then its rows added and stored), and per vertex i for the
+// vector part (thread j = 0).  Distinct vertices give distinct slots and
+// rows, so nothing aliases.
+template <class Elem, int CARD, int BS, typename T>
+__device__ __forceinline__ void colored_block(const AsmArgs<T> &a, int64_t e, int i, int j,
+                                              const uint32_t *__restrict__ slots) {
+  if (Elem::HAS_MAT) {
+    const uint32_t sl = slots[(e * CARD + i) * CARD + j];
+    if ((int64_t)sl >= a.nnzb) {
+      atomicCAS(a.err, 0, 3 /* DEV_SLOT_MISSING */);
+    } else {
+      T *dst = a.vals + (size_t)sl * BS * BS;
+      T old[BS * BS];
+#pragma unroll
+      for (int q = 0; q < BS * BS; ++q) old[q] = dst[q];
+#pragma unroll
+      for (int l = 0; l < BS; ++l) {
+        T out[2][BS];
+        const int nt = Elem::block(a, e, i, j, l, out);
+#pragma unroll
+        for (int q = 0; q < BS; ++q) {
+          if (nt > 0) old[l * BS + q] += out[0][q];
+          if (nt > 1) old[l * BS + q] += out[1][q];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < BS * BS; ++q) dst[q] = old[q];
+    }
+  }
+  if (Elem::HAS_VEC && j == 0) {
+    const int32_t vi = a.ep[e * CARD + i];
+    T fv[BS];
+#pragma unroll
+    for (int l = 0; l < BS; ++l) fv[l] = a.f[(int64_t)vi * BS + l];
+#pragma unroll
+    for (int l = 0; l < BS; ++l) {
+      T o[4];
+      const int nv = Elem::vec(a, e, i, l, o);
+      for (int q = 0; q < nv; ++q) fv[l] += o[q];
+    }
+#pragma unroll
+    for (int l = 0; l < BS; ++l) a.f[(int64_t)vi * BS + l] = fv[l];
+  }
+}
+
+template <class Elem, int CARD, int BS, typename T>
+__global__ void __launch_bounds__(256) k_colored(AsmArgs<T> a, const uint32_t *__restrict__ elist,
+                                                 int64_t cnt, const uint32_t *__restrict__ slots) {
+  constexpr int TPE = Elem::HAS_MAT ? CARD * CARD : CARD;  // threads per element
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < cnt * TPE; t += stride) {
+    const int64_t e = elist[t / TPE];
+    const int r = (int)(t % TPE);
+    const int i = Elem::HAS_MAT ? r / CARD : r, j = Elem::HAS_MAT ? r % CARD : 0;
+    const int32_t *vv = a.ep + e * CARD;
+    bool rep = false;
+#pragma unroll
+    for (int i1 = 0; i1 < CARD; ++i1)
+#pragma unroll
+      for (int i2 = i1 + 1; i2 < CARD; ++i2) rep = rep || vv[i1] == vv[i2];
+    if (!rep) {
+      colored_block<Elem, CARD, BS, T>(a, e, i, j, slots);
+    } else if (r == 0) {
+      for (int ii = 0; ii < CARD; ++ii) colored_row<Elem, CARD, BS, T>(a, e, ii, slots);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Element blocks + slot gather (the assembly plan's second form)
+// ---------------------------------------------------------------------------
+// Phase 1, element-parallel: thread (e, i, j) writes block (i, j) of element
+// e (all its terms summed) to eb[(e*CARD + i)*CARD + j] -- consecutive
+// threads, consecutive blocks, coalesced -- and for vector maps thread
+// (e, i, 0) writes vertex i's contribution to ev[e*CARD + i].  Phase 2:
+// every slot sums its contributing blocks (the inverse slot map, sorted by
+// block index, i.e. ascending element) and every vertex its contributions
+// (its incidence list, ascending element), each written once.  Each element
+// is computed once, nothing is read-modified-written, the order of every
+// sum is fixed.  Needs Elem::fin_* to be the identity.
+template <class Elem, int CARD, int BS, typename T>
+__global__ void __launch_bounds__(256) k_elem_blocks(AsmArgs<T> a, T *__restrict__ eb,
+                                                     T *__restrict__ ev) {
+  constexpr int TPE = Elem::HAS_MAT ? CARD * CARD : CARD;
+  // a CTA's 256 consecutive blocks are staged in shared memory and leave in
+  // 16-byte stores (the chunk starts 256 * BS*BS * sizeof(T) bytes apart)
+  __shared__ __align__(16) T stage[Elem::HAS_MAT ? 256 * BS * BS : 1];
+  const int64_t total = a.nE * TPE;
+  for (int64_t t0 = (int64_t)blockIdx.x * 256; t0 < total; t0 += (int64_t)gridDim.x * 256) {
+    const int64_t t = t0 + threadIdx.x;
+    if (t < total) {
+      const int64_t e = t / TPE;
+      const int r = (int)(t % TPE);
+      const int i = Elem::HAS_MAT ? r / CARD : r, j = Elem::HAS_MAT ? r % CARD : 0;
+      if (Elem::HAS_MAT) {
+#pragma unroll
+        for (int l = 0; l < BS; ++l) {
+          T out[2][BS];
+          const int nt = Elem::block(a, e, i, j, l, out);
+#pragma unroll
+          for (int q = 0; q < BS; ++q) {
+            T v = nt > 0 ? out[0][q] : T(0);
+            if (nt > 1) v += out[1][q];
+            stage[threadIdx.x * BS * BS + l * BS + q] = v;
+          }
+        }
+      }
+      if (Elem::HAS_VEC && j == 0) {
+#pragma unroll
+        for (int l = 0; l < BS; ++l) {
+          T o[4];
+          const int nv = Elem::vec(a, e, i, l, o);
+          T v = T(0);
+          for (int q = 0; q < nv; ++q) v += o[q];
+          ev[(e * CARD + i) * BS + l] = v;
+        }
+      }
+    }
+    if (Elem::HAS_MAT) {
+      __syncthreads();
+      const int64_t nval = (min(total, t0 + 256) - t0) * BS * BS;
+      T *dst = eb + t0 * BS * BS;
+      constexpr int PER = 16 / sizeof(T);
+      if (nval == 256 * BS * BS && (BS * BS * 256) % PER == 0) {
+        const float4 *src4 = reinterpret_cast<const float4 *>(stage);
+        float4 *dst4 = reinterpret_cast<float4 *>(dst);
+        for (int k = threadIdx.x; k < 256 * BS * BS / PER; k += 256) dst4[k] = src4[k];
+      } else {
+        for (int64_t k = threadIdx.x; k < nval; k += 256) dst[k] = stage[k];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// vals[q] = sum of eb blocks src[sptr[q] .. sptr[q+1]); thread per (slot,
+// row l); the block indices of up to 8 contributions are loaded before
+// their values, and all values before the sum (ascending order kept).
+template <int BS, typename T>
+__global__ void __launch_bounds__(256) k_slot_gather(int64_t nnzb, const uint32_t *__restrict__ sptr,
+                                                     const uint32_t *__restrict__ src,
+                                                     const T *__restrict__ eb, T *__restrict__ vals) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nnzb * BS; t += stride) {
+    const int64_t q = t / BS;
+    const int l = (int)(t % BS);
+    T acc[BS];
+#pragma unroll
+    for (int m = 0; m < BS; ++m) acc[m] = T(0);
+    const uint32_t k1 = sptr[q + 1];
+    for (uint32_t k0 = sptr[q]; k0 < k1; k0 += 8) {
+      uint32_t b[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) b[u] = k0 + u < k1 ? src[k0 + u] : 0u;
+      T x[8][BS];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int m = 0; m < BS; ++m)
+          x[u][m] = k0 + u < k1 ? eb[(size_t)b[u] * BS * BS + l * BS + m] : T(0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (k0 + u < k1)
+#pragma unroll
+          for (int m = 0; m < BS; ++m) acc[m] += x[u][m];
+    }
+#pragma unroll
+    for (int m = 0; m < BS; ++m) vals[q * BS * BS + l * BS + m] = acc[m];
+  }
+}
+
+// f[v] = sum of ev over v's incidences (ascending element); thread per (v, l).
+template <int BS, typename T>
+__global__ void __launch_bounds__(256) k_vert_gather(int32_t n, const uint32_t *__restrict__ ve_ptr,
+                                                     const uint32_t *__restrict__ ve_idx,
+                                                     const T *__restrict__ ev, T *__restrict__ f) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)n * BS;
+       t += stride) {
+    const int64_t v = t / BS;
+    const int l = (int)(t % BS);
+    T acc = T(0);
+    const uint32_t k1 = ve_ptr[v + 1];
+    for (uint32_t k = ve_ptr[v]; k < k1; ++k) acc += ev[(size_t)ve_idx[k] * BS + l];
+    f[t] = acc;
   }
 }
 

@@ -30,6 +30,57 @@ static int launch_rows(Ctx *c, AsmArgs<T> &a) {
   return SG_OK;
 }
 
+// The element-parallel form over the mesh's colouring plan (fast
+// instantiation only; the exact one keeps the reference's element order
+// through the row owners).  Outputs are zeroed first, then one launch per
+// colour.  Returns 1 through *used when it ran.
+template <class Elem, int CARD, int BS, typename T>
+static int launch_colored(Ctx *c, AsmArgs<T> &a, const sg_mesh *m, bool *used) {
+  *used = false;
+  if (SG_ASM_EXACT || !m->slots || m->card != CARD) return SG_OK;
+  a.err = c->d_err;
+  if (m->slot_src_ptr && m->slot_src) {
+    // element blocks (context scratch) + slot / vertex gathers
+    const size_t neb = Elem::HAS_MAT ? (size_t)m->nE * CARD * CARD * BS * BS : 0;
+    const size_t nev = Elem::HAS_VEC ? (size_t)m->nE * CARD * BS : 0;
+    Scratch s(c);
+    SG_TRY(s.reserve(Scratch::bytes_for(neb + 1, sizeof(T)) + Scratch::bytes_for(nev + 1, sizeof(T))));
+    T *eb = s.alloc<T>(neb + 1), *ev = s.alloc<T>(nev + 1);
+    if (m->nE > 0) {
+      const int64_t th = m->nE * (Elem::HAS_MAT ? CARD * CARD : CARD);
+      k_elem_blocks<Elem, CARD, BS, T><<<grid_for(c, th, 256, 8), 256, 0, c->stream>>>(a, eb, ev);
+      SG_CHECK_LAUNCH();
+    }
+    if (Elem::HAS_MAT && m->nnzb > 0) {
+      k_slot_gather<BS, T><<<grid_for(c, m->nnzb * BS, 256, 8), 256, 0, c->stream>>>(
+          m->nnzb, m->slot_src_ptr, m->slot_src, eb, a.vals);
+      SG_CHECK_LAUNCH();
+    }
+    if (Elem::HAS_VEC && m->n > 0) {
+      k_vert_gather<BS, T><<<grid_for(c, (int64_t)m->n * BS, 256, 8), 256, 0, c->stream>>>(
+          m->n, m->ve_ptr, m->ve_idx, ev, a.f);
+      SG_CHECK_LAUNCH();
+    }
+    *used = true;
+    return SG_OK;
+  }
+  if (!m->color_order || !m->color_ptr || m->ncolors <= 0) return SG_OK;
+  if (Elem::HAS_MAT)
+    SG_CHECK_CUDA(cudaMemsetAsync(a.vals, 0, (size_t)m->nnzb * BS * BS * sizeof(T), c->stream));
+  if (Elem::HAS_VEC)
+    SG_CHECK_CUDA(cudaMemsetAsync(a.f, 0, (size_t)m->n * BS * sizeof(T), c->stream));
+  for (int k = 0; k < m->ncolors; ++k) {
+    const int64_t b0 = m->color_ptr[k], cnt = (int64_t)m->color_ptr[k + 1] - b0;
+    if (cnt <= 0) continue;
+    const int64_t threads = cnt * (Elem::HAS_MAT ? CARD * CARD : CARD);
+    k_colored<Elem, CARD, BS, T><<<grid_for(c, threads, 256, 8), 256, 0, c->stream>>>(
+        a, m->color_order + b0, cnt, m->slots);
+    SG_CHECK_LAUNCH();
+  }
+  *used = true;
+  return SG_OK;
+}
+
 template <typename T>
 static void fill_mesh(AsmArgs<T> &a, const sg_mesh *m) {
   a.n = m->n;
@@ -41,6 +92,7 @@ static void fill_mesh(AsmArgs<T> &a, const sg_mesh *m) {
   a.rowptr = m->rowptr;
   a.colidx = m->colidx;
   a.maxrow = m->maxrow;
+  a.nnzb = m->nnzb;
 }
 
 template <typename T>
@@ -73,6 +125,9 @@ int heat(Ctx *c, const sg_mesh *m, const void *B, const void *W, const void *kap
   fill_mesh(a, m);
   a.B = (const T *)B; a.W = (const T *)W; a.kappa = (const T *)kappa; a.dt = (T)dt;
   a.T0 = (const T *)T0; a.vals = (T *)vals; a.f = (T *)b;
+  bool used = false;
+  SG_TRY((launch_colored<HeatElem<T>, 4, 1, T>(c, a, m, &used)));
+  if (used) return SG_OK;
   return launch_rows<HeatElem<T>, 4, 1, T>(c, a);
 }
 
@@ -96,8 +151,13 @@ int blocks(Ctx *c, const sg_mesh *m, int bs, const void *eb, void *vals) {
   fill_mesh(a, m);
   a.eb = (const T *)eb;
   a.vals = (T *)vals;
-#define SG_BLK(BSV, CV)                                                     \
-  if (bs == BSV && m->card == CV) return launch_rows<BlocksElem<T, BSV, CV>, 16, BSV, T>(c, a);
+#define SG_BLK(BSV, CV)                                                            \
+  if (bs == BSV && m->card == CV) {                                                \
+    bool used = false;                                                             \
+    SG_TRY((launch_colored<BlocksElem<T, BSV, CV>, CV, BSV, T>(c, a, m, &used)));  \
+    if (used) return SG_OK;                                                        \
+    return launch_rows<BlocksElem<T, BSV, CV>, 16, BSV, T>(c, a);                  \
+  }
   SG_BLK(1, 2) SG_BLK(1, 3) SG_BLK(1, 4)
   SG_BLK(2, 2) SG_BLK(2, 3) SG_BLK(2, 4)
   SG_BLK(3, 2) SG_BLK(3, 3) SG_BLK(3, 4)
@@ -121,8 +181,14 @@ int tet_stiffness(Ctx *c, const sg_mesh *m, int model, const void *x, const int3
       k_neo_blocks<T><<<grid_for(c, m->nE, 128, 16), 128, 0, c->stream>>>(a);
       SG_CHECK_LAUNCH();
     }
+    bool used = false;
+    SG_TRY((launch_colored<EbGatherElem<T>, 4, 3, T>(c, a, m, &used)));
+    if (used) return SG_OK;
     return launch_rows<EbGatherElem<T>, 16, 3, T>(c, a);
   }
+  bool used = false;
+  SG_TRY((launch_colored<LinTetElem<T, SG_ASM_EXACT>, 4, 3, T>(c, a, m, &used)));
+  if (used) return SG_OK;
   return launch_rows<LinTetElem<T, SG_ASM_EXACT>, 16, 3, T>(c, a);
 }
 
@@ -136,7 +202,14 @@ int tet_force(Ctx *c, const sg_mesh *m, int model, const void *x, const void *v,
   a.mu = (const T *)mu; a.lam = (const T *)lam; a.h = (T)h; a.rho = (T)rho;
   for (int q = 0; q < 3; ++q) a.grav[q] = (T)grav[q];
   a.f = (T *)f;
-  if (model == SG_MODEL_NEOHOOKEAN) return launch_rows<TetForceElem<T, true>, 4, 3, T>(c, a);
+  bool used = false;
+  if (model == SG_MODEL_NEOHOOKEAN) {
+    SG_TRY((launch_colored<TetForceElem<T, true>, 4, 3, T>(c, a, m, &used)));
+    if (used) return SG_OK;
+    return launch_rows<TetForceElem<T, true>, 4, 3, T>(c, a);
+  }
+  SG_TRY((launch_colored<TetForceElem<T, false>, 4, 3, T>(c, a, m, &used)));
+  if (used) return SG_OK;
   return launch_rows<TetForceElem<T, false>, 4, 3, T>(c, a);
 }
 

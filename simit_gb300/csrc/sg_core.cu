@@ -43,8 +43,9 @@ int check_device_error(Ctx *c, const char *what) {
                                   "(row, col) not in pattern",
                                   "row longer than the assembly accumulator",
                                   "vertex without a diagonal block",
-                                  "bulk-copy barrier wait timed out"};
-    const char *nm = (e > 0 && e < 7) ? names[e] : "unknown";
+                                  "bulk-copy barrier wait timed out",
+                                  "an element needs more than 128 colours"};
+    const char *nm = (e > 0 && e < 8) ? names[e] : "unknown";
     return set_error(SG_ERR_DEVICE, "%s: device check failed (%d: %s)", what, e,
                      nm);
   }

@@ -90,6 +90,7 @@ enum DevErr : int {
   DEV_ROW_OVERFLOW = 4,   // assembly row longer than the accumulator
   DEV_NO_DIAGONAL = 5,    // vertex without a diagonal block
   DEV_TMA_TIMEOUT = 6,    // a bulk-copy barrier wait ran out of polls
+  DEV_TOO_MANY_COLORS = 7,  // element colouring needs more than SG_MAX_COLORS
 };
 
 int set_error(int code, const char *fmt, ...);

@@ -70,9 +70,12 @@ class HeteroElasticity:
     """
 
     def __init__(self, ctx, host, dtype=torch.float32, precond=_lib.PRECOND_BLOCK_JACOBI,
-                 precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None, pdl=0):
+                 precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None, pdl=0,
+                 plan="gather"):
         self.ctx, self.host, self.dtype = ctx, host, dtype
-        self.mesh = Mesh(ctx, host["n"], host["tets"], 4)
+        # plan: the element-parallel assembly plan ("gather", "colored"; each
+        # element computed once), or None for the row-owner kernels
+        self.mesh = Mesh(ctx, host["n"], host["tets"], 4, plan=plan)
         d = ctx.device
         with ctx.stream():
             self.X0 = torch.tensor(host["X0"], dtype=dtype, device=d)

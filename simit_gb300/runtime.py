@@ -331,11 +331,20 @@ def _host_f64(a):
 
 
 class Mesh:
-    """A bound edge set + its device pattern, as the sg_mesh structure."""
+    """A bound edge set + its device pattern, as the sg_mesh structure.
 
-    def __init__(self, ctx, n, endpoints, card, with_slots=False):
+    plan: the element-parallel assembly plan that assembly with exact=False
+    uses -- "gather" (element blocks written once, then every slot and
+    vertex gathers its contributions in ascending element order), "colored"
+    (blocks added into their slots colour by colour) -- or None (row-owner
+    kernels).  colored=True is plan="colored"."""
+
+    def __init__(self, ctx, n, endpoints, card, with_slots=False, colored=False, plan=None):
         self.ctx = ctx
-        self.pattern = Pattern(ctx, n, endpoints, card, with_slots=with_slots)
+        if colored and plan is None:
+            plan = "colored"
+        assert plan in (None, "colored", "gather"), plan
+        self.pattern = Pattern(ctx, n, endpoints, card, with_slots=with_slots or plan is not None)
         p = self.pattern
         mr = ctypes.c_int32()
         call("sg_pattern_maxrow", ctx.h, n, ptr(p.rowptr), ctypes.byref(mr))
@@ -344,6 +353,47 @@ class Mesh:
         self.s = _lib.Mesh(n, card, p.nE, p.endpoints.data_ptr(), p.ve_ptr.data_ptr(),
                            p.ve_idx.data_ptr(), p.rowptr.data_ptr(), p.colidx.data_ptr(),
                            p.nnzb, self.maxrow)
+        self.ncolors = 0
+        self.plan = plan
+        if plan == "colored":
+            self.color_plan()
+        elif plan == "gather":
+            self.gather_plan()
+
+    def color_plan(self):
+        """Slots + element colouring (sg_element_coloring) set in the sg_mesh."""
+        p = self.pattern
+        with self.ctx.stream():
+            self.color_order = torch.empty(max(1, self.nE), dtype=torch.int32,
+                                           device=self.ctx.device)
+        self._color_ptr = (ctypes.c_int32 * (_lib.MAX_COLORS + 1))()
+        nc = ctypes.c_int32()
+        self.s.slots = p.slots.data_ptr()
+        call("sg_element_coloring", self.ctx.h, ctypes.byref(self.s), ptr(self.color_order),
+             ctypes.cast(self._color_ptr, ctypes.c_void_p), ctypes.byref(nc))
+        self.ncolors = nc.value
+        self.s.color_order = self.color_order.data_ptr()
+        self.s.color_ptr = ctypes.cast(self._color_ptr, ctypes.c_void_p)
+        self.s.ncolors = nc.value
+
+    def gather_plan(self):
+        """Slots + the inverse slot map (sg_slot_sources) set in the sg_mesh."""
+        p = self.pattern
+        self.s.slots = p.slots.data_ptr()
+        with self.ctx.stream():
+            self.slot_src_ptr = torch.empty(self.nnzb + 1, dtype=torch.int32,
+                                            device=self.ctx.device)
+            self.slot_src = torch.empty(max(1, self.nE * self.card * self.card),
+                                        dtype=torch.int32, device=self.ctx.device)
+        call("sg_slot_sources", self.ctx.h, ctypes.byref(self.s), ptr(self.slot_src_ptr),
+             ptr(self.slot_src))
+        self.s.slot_src_ptr = self.slot_src_ptr.data_ptr()
+        self.s.slot_src = self.slot_src.data_ptr()
+
+    def colors(self):
+        """(color_ptr list, color_order numpy) of the plan."""
+        cp = [self._color_ptr[k] for k in range(self.ncolors + 1)]
+        return cp, self.color_order[:self.nE].cpu().numpy()
 
     def ref(self):
         return ctypes.byref(self.s)
