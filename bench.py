@@ -33,7 +33,12 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=128, help="cells per cube edge")
     ap.add_argument("--cpu-sample", type=int, default=48,
-                    help="cells per edge of the CPU sample (48: about 10-15 s of one core)")
+                    help="cells per edge of the instance whose oracle FP64 solution the GPU "
+                         "solutions are compared to (48: about 15-25 s of one core)")
+    ap.add_argument("--no-cpu", action="store_true",
+                    help="skip the CPU baseline and the solution check against the oracle")
+    ap.add_argument("--no-block-jacobi", action="store_true",
+                    help="skip the block-Jacobi step (the method without the network)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 Jacobi-CG comparison")
     ap.add_argument("--no-reorder", action="store_true",
                     help="keep the lattice vertex order (no space-filling-curve reordering)")
@@ -565,55 +570,162 @@ def dist_setup(args):
 # ---------------------------------------------------------------------------
 # CPU reference arm (the oracle restatement of the reference's lowered loops)
 # ---------------------------------------------------------------------------
-def cpu_sample(ncell):
-    """Oracle on the ncell^3 instance of the same family: pattern (ordered
-    sets, as the reference's PathIndexBuilder) + FP64 assembly (element
-    order, loc slot search) + FP64 Jacobi-PCG to 1e-8, one thread."""
+# Iterations of plain FP64 Jacobi-PCG to a 1e-8 relative residual on the
+# 128^3 workload (Morton order), as the GPU arm's FP64 run counts them; the
+# CPU time per step is extrapolated with it (the CPU sample times the
+# assembly and a few iterations: the full solve takes about half an hour on
+# one core).
+FP64_JACOBI_ITERS = {128: 3195}
+
+
+def cpu_host():
+    """nproc and the CPU model of this host."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                k = ln.split(":")[0].strip().lower()
+                if k in ("model name", "cpu model", "hardware"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+            for ln in out.splitlines():
+                if ln.lower().startswith("model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"nproc": os.cpu_count(), "cpu_model": model}
+
+
+def cpu_config_sample(size, reorder=True, kmax=4):
+    """The oracle (one thread) on the size^3 workload itself: pattern
+    (ordered sets, as the reference's PathIndexBuilder; its init, untimed in
+    the step), FP64 assembly of the step (precompute + stiffness + force, in
+    element order with the loc slot search), and Jacobi-PCG iterations, the
+    per-iteration time from 1 and kmax iterations (the set-up cancels)."""
     import numpy as np
     from oracle import oracle
     from simit_gb300 import problems
-    h = problems.hetero_mesh(ncell)
+    oracle.build()
+    h = problems.hetero_mesh(size)
+    if reorder:
+        h = problems.reorder_hetero(h)
     t0 = time.perf_counter()
+    rp, ci = oracle.pattern(h["n"], h["tets"], 4)
+    t_pattern = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    B, W, _ = oracle.tet_precompute(h["X0"], h["tets"], problems.RHO)
+    A = oracle.tet_stiffness(0, h["x"], h["c"], h["tets"], B, W, h["mu"], h["lam"], problems.H,
+                             problems.RHO, rp, ci)
+    b = oracle.tet_force(0, h["x"], np.zeros(h["n"] * 3), h["c"], h["tets"], B, W, h["mu"],
+                         h["lam"], problems.H, problems.RHO, problems.GRAV)
+    t_asm = time.perf_counter() - t0
+    x0 = np.zeros(h["n"] * 3)
+    ts = {}
+    for k in (1, kmax):
+        t0 = time.perf_counter()
+        oracle.jacobi_pcg(h["n"], 3, rp, ci, A, b, x0, 1e-8, k, refresh=0)
+        ts[k] = time.perf_counter() - t0
+    return {"dofs": h["n"] * 3, "pattern_s": t_pattern, "assembly_s": t_asm,
+            "iter_s": (ts[kmax] - ts[1]) / (kmax - 1), "kmax": kmax}
+
+
+def cpu_solution(ncell, tol=1e-12):
+    """The oracle's FP64 Jacobi-PCG solution of the ncell^3 workload (lattice
+    order) to tol: the reference solution the GPU solutions are compared to."""
+    import numpy as np
+    from oracle import oracle
+    from simit_gb300 import problems
+    oracle.build()
+    h = problems.hetero_mesh(ncell)
     rp, ci = oracle.pattern(h["n"], h["tets"], 4)
     B, W, _ = oracle.tet_precompute(h["X0"], h["tets"], problems.RHO)
     A = oracle.tet_stiffness(0, h["x"], h["c"], h["tets"], B, W, h["mu"], h["lam"], problems.H,
                              problems.RHO, rp, ci)
     b = oracle.tet_force(0, h["x"], np.zeros(h["n"] * 3), h["c"], h["tets"], B, W, h["mu"],
                          h["lam"], problems.H, problems.RHO, problems.GRAV)
-    x, it, rr = oracle.jacobi_pcg(h["n"], 3, rp, ci, A, b, np.zeros(h["n"] * 3), 1e-8, 200000,
+    x, it, rr = oracle.jacobi_pcg(h["n"], 3, rp, ci, A, b, np.zeros(h["n"] * 3), tol, 400000,
                                   refresh=0)
-    t = time.perf_counter() - t0
-    dofs = h["n"] * 3
-    return {"value": dofs / t, "unit": "DOF/s", "seconds": t, "iters": it, "relres": rr,
-            "dofs": dofs}
+    return {"x": x, "iters": it, "relres": rr}
+
+
+def _cpu_child(q, size, reorder, sol_cells):
+    """Spawned before the GPU arm touches the GPU: the CPU work of the bench
+    line, run beside the GPU measurements (one core each)."""
+    try:
+        out = {"config": cpu_config_sample(size, reorder)}
+        out["solution"] = cpu_solution(sol_cells)
+        q.put(out)
+    except Exception as e:  # reported, not fatal for the GPU arm
+        q.put({"error": repr(e)})
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle's restatement of its lowered
+    loops; its own CPU backend needs LLVM and cannot be built) on the
+    workload itself, one thread: the pattern once (init), the FP64 assembly
+    once, and per step a bounded sample of Jacobi-PCG iterations; the step
+    time is assembly + the FP64 iteration count x the time per iteration."""
     if rank != 0:
         return
     from oracle import oracle
+    import numpy as np
+    from simit_gb300 import problems
     oracle.build()
-    for _ in range(args.warmup):
-        cpu_sample(args.cpu_sample)
-    vals = []
+    iters = FP64_JACOBI_ITERS.get(args.size)
+    h = problems.hetero_mesh(args.size)
+    if not args.no_reorder:
+        h = problems.reorder_hetero(h)
+    rp, ci = oracle.pattern(h["n"], h["tets"], 4)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        vals.append(cpu_sample(args.cpu_sample))
-    el = time.perf_counter() - t0
-    v = statistics.median([r["value"] for r in vals])
-    sample = ("%d^3 instance of the same family (%d DOF): ordered-set pattern + FP64 element-order "
-              "assembly + FP64 Jacobi-PCG to 1e-8, oracle restatement of the reference's CPU "
-              "loops, 1 thread" % (args.cpu_sample, vals[0]["dofs"]))
+    B, W, _ = oracle.tet_precompute(h["X0"], h["tets"], problems.RHO)
+    A = oracle.tet_stiffness(0, h["x"], h["c"], h["tets"], B, W, h["mu"], h["lam"], problems.H,
+                             problems.RHO, rp, ci)
+    b = oracle.tet_force(0, h["x"], np.zeros(h["n"] * 3), h["c"], h["tets"], B, W, h["mu"],
+                         h["lam"], problems.H, problems.RHO, problems.GRAV)
+    t_asm = time.perf_counter() - t0
+    x0 = np.zeros(h["n"] * 3)
+
+    def sample():
+        ts = []
+        for k in (1, 4):
+            t1 = time.perf_counter()
+            oracle.jacobi_pcg(h["n"], 3, rp, ci, A, b, x0, 1e-8, k, refresh=0)
+            ts.append(time.perf_counter() - t1)
+        return (ts[1] - ts[0]) / 3
+    for _ in range(args.warmup):
+        sample()
+    per = [sample() for _ in range(args.steps)]
+    t_iter = statistics.median(per)
+    dofs = h["n"] * 3
+    if iters is None:  # no recorded count: the sample's own iterations only
+        step_s = t_asm + t_iter
+        note = "no FP64 iteration count recorded for this size: assembly + one iteration"
+    else:
+        step_s = t_asm + iters * t_iter
+        note = ("assembly %.2f s + %d FP64 Jacobi-PCG iterations (the GPU arm's FP64 count) x "
+                "%.4f s per iteration (median of %d samples of 1 and 4 iterations)"
+                % (t_asm, iters, t_iter, args.steps))
+    v = dofs / step_s
+    host = cpu_host()
+    sample_txt = ("the %d^3 workload itself (%d DOF), oracle restatement of the reference's CPU "
+                  "loops, 1 thread: %s" % (args.size, dofs, note))
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "DOF/s", "n_gpus": world,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded Philox)",
-           "config": {"workload": workload_name(args.size, not args.no_reorder),
-                      "sample_cells": args.cpu_sample},
+           "config": {"workload": workload_name(args.size, not args.no_reorder), "dofs": dofs,
+                      "method": "FP64 assembly + plain FP64 Jacobi-PCG (the reference's CPU "
+                                "loops, restated)", "extrapolated": iters is not None},
            "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": 1, "kind": "port",
-                            "sample": sample},
+                            "sample": sample_txt, **host},
            "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "iters": vals[0]["iters"]}
+           "assembly_s": t_asm, "iter_s": t_iter, "iters": iters}
     print(json.dumps(out), flush=True)
 
 
@@ -694,10 +806,37 @@ def spmv_traffic(size, sym=False):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def _step_timing(prob, st, steps, warmup, barrier):
+    """Event-timed steps (assembly + refresh + solve) of a problem."""
+    import torch
+    for _ in range(warmup):
+        prob.step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    results = [prob.step() for _ in range(steps)]
+    e1.record(st)
+    barrier()
+    return e0.elapsed_time(e1) / steps, results
+
+
 def run_ours(args, rank, world, local):
+    # the CPU half of the line runs in a process spawned before any GPU call
+    cpu_q = cpu_p = None
+    if rank == 0 and not args.no_cpu:
+        import multiprocessing as mp
+        mpc = mp.get_context("spawn")
+        cpu_q = mpc.Queue()
+        cpu_p = mpc.Process(target=_cpu_child,
+                            args=(cpu_q, args.size, not args.no_reorder, args.cpu_sample),
+                            daemon=True)
+        cpu_p.start()
+    import numpy as np
     import torch
     from simit_gb300 import _lib, problems
-    from simit_gb300.runtime import Context, bspmv
+    from simit_gb300 import learned as lrn
+    from simit_gb300.runtime import Context, Solver, bspmv, solve_opts
 
     ctx = Context(local)
     torch.cuda.set_device(local)
@@ -705,8 +844,11 @@ def run_ours(args, rank, world, local):
     host = problems.hetero_mesh(args.size)
     if not args.no_reorder:
         host = problems.reorder_hetero(host)
+    with ctx.stream():
+        prm = torch.tensor(lrn.load_weights("sym"), device=ctx.device)
+    # the metric's method: FP32 assembly + learned-preconditioned mixed PCG
     prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
-                                     precond=_lib.PRECOND_BLOCK_JACOBI,
+                                     precond=_lib.PRECOND_LEARNED, learned_params=prm,
                                      storage=_lib.STORAGE_SYMMETRIC if args.sym
                                      else _lib.STORAGE_FULL, pdl=int(args.pdl))
     st = ctx.torch_stream
@@ -738,9 +880,10 @@ def run_ours(args, rank, world, local):
     value = dofs * world / (ms / 1e3)
     relres = max((r.true_normr2 / r.bnorm2) ** 0.5 for r in results)
     iters = results[-1].iters
-    # kernels per step: stiffness + force assembly, preconditioner refresh,
-    # and the solver's own count (graph kernel nodes included)
-    launches = sum(int(r.kernels) + 3 for r in results)
+    # kernels per step: stiffness + force assembly (the gather plan: element
+    # blocks, slot gather; element vectors, vertex gather), the solver's
+    # refresh and its own count (graph kernel nodes included)
+    launches = sum(int(r.kernels) + 4 + 6 for r in results)
 
     # --- end to end through host buffers (pinned) -------------------------
     n3 = prob.dofs
@@ -759,8 +902,6 @@ def run_ours(args, rank, world, local):
     d2h = u_h.numel() * 8
 
     # --- roofline of the dominant kernel: the iteration's FP32 SpMV --------
-    # (the solver's K1 without its p.q epilogue, on the same matrix and
-    # stream); the full-storage kernel is timed beside it for reference
     m = prob.mesh
     p = torch.rand(n3, dtype=torch.float32, device=ctx.device)
     q = torch.empty_like(p)
@@ -803,7 +944,9 @@ def run_ours(args, rank, world, local):
 
     # --- the step's assembly alone (stiffness map in place + force map) ----
     # algorithmic bytes: element ids and parameters (B 9, W, mu, lam) once,
-    # vertex positions once, the matrix values and the force written once
+    # vertex positions once, the matrix values and the force written once;
+    # the gather plan also writes and reads its element blocks and vectors
+    # and reads the inverse slot map (implementation bytes)
     nE = m.nE
     for _ in range(2):
         prob.assemble_in_place()
@@ -816,84 +959,105 @@ def run_ours(args, rank, world, local):
     a1.synchronize()
     asm_ms = a0.elapsed_time(a1) / 3
     asm_bytes = nE * (4 * 4 + 12 * 4) + m.n * 3 * 4 + m.nnzb * 36 + m.n * 3 * 4
+    impl_bytes = asm_bytes + 2 * nE * 16 * 36 + nE * 16 * 4 + (m.nnzb + 1) * 4 + 2 * nE * 4 * 12
     assembly = {"ms": asm_ms, "elements_per_s": nE / (asm_ms / 1e3),
                 "algorithmic_bytes": asm_bytes, "GBps": asm_bytes / (asm_ms / 1e3) / 1e9,
-                "kernels": "k_rows<LinTetElem> (stiffness) + k_rows<TetForceElem> (force)"}
+                "implementation_bytes": impl_bytes,
+                "implementation_GBps": impl_bytes / (asm_ms / 1e3) / 1e9,
+                "kernels": "element-blocks plan: k_elem_blocks<LinTetElem> + k_slot_gather "
+                           "(stiffness), k_elem_blocks<TetForceElem> + k_vert_gather (force)"}
     if not args.no_jit:
         assembly["jit_stiffness"] = time_jit_stiffness(ctx, prob)
 
-    # --- the same system solved with the learned (symmetric) preconditioner
-    # against block-Jacobi, solve only (same matrix and right-hand side) ----
-    learned = None
-    if not args.no_learned:
-        from simit_gb300 import learned as lrn
-        from simit_gb300.runtime import Solver, solve_opts
-        with ctx.stream():
-            prm = torch.tensor(lrn.load_weights("sym"), device=ctx.device)
-            xs = torch.zeros_like(prob.b)
-        S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, prob.A, m.nnzb,
-                   solve_opts(precision=_lib.SOLVE_MIXED, precond=_lib.PRECOND_LEARNED,
-                              tol=1e-8, maxiters=200000, learned_params=prm,
-                              learned_form=_lib.MPNN_SYM), learned_params_keep=prm)
-        res = {}
-        for name, solver in (("block_jacobi", prob.solver), ("learned_sym", S)):
-            def one():
-                with ctx.stream():
-                    xs.zero_()
-                return solver.solve(prob.b, xs)
-            l0 = torch.cuda.Event(enable_timing=True)
-            l1 = torch.cuda.Event(enable_timing=True)
-            l0.record(st)
-            r = one()
-            l1.record(st)
-            l1.synchronize()
-            res[name] = {"solve_ms": l0.elapsed_time(l1), "iters": r.iters,
-                         "fallbacks": r.fallbacks,
-                         "relres": (r.true_normr2 / r.bnorm2) ** 0.5}
-        S.close()
-        res["iteration_gain"] = res["block_jacobi"]["iters"] / max(1, res["learned_sym"]["iters"])
-        res["time_ratio"] = res["block_jacobi"]["solve_ms"] / res["learned_sym"]["solve_ms"]
-        learned = res
+    # --- the same step with block Jacobi (the method without the network) --
+    bj = None
+    if not args.no_block_jacobi:
+        pb = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
+                                       precond=_lib.PRECOND_BLOCK_JACOBI)
+        bms, bres = _step_timing(pb, st, max(2, args.steps // 4), 2, barrier)
+        bj = {"ms": bms, "DOF_per_s": dofs / (bms / 1e3), "iters": bres[-1].iters,
+              "relres": (bres[-1].true_normr2 / bres[-1].bnorm2) ** 0.5,
+              "method": "FP32 assembly + mixed-precision block-Jacobi PCG"}
+        pb.close()
+        del pb
+        torch.cuda.empty_cache()
 
     # --- plain FP64 Jacobi-CG on the same GPU (FP64 assembly + solve) -----
     fp64 = None
     if not args.no_fp64:
-        prob.close()
-        del prob
-        torch.cuda.empty_cache()
         p64 = problems.HeteroElasticity(ctx, host, dtype=torch.float64,
                                         precond=_lib.PRECOND_JACOBI)
-        p64.step()
-        torch.cuda.synchronize()
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        f0.record(st)
-        r64 = p64.step()
-        f1.record(st)
-        f1.synchronize()
-        ms64 = f0.elapsed_time(f1)
+        ms64, r64s = _step_timing(p64, st, 1, 1, barrier)
+        r64 = r64s[-1]
         fp64 = {"ms": ms64, "DOF_per_s": dofs / (ms64 / 1e3), "iters": r64.iters,
                 "relres": (r64.true_normr2 / r64.bnorm2) ** 0.5,
                 "method": "FP64 assembly + FP64 point-Jacobi CG (FP64 SpMV, FP64 vectors)"}
         p64.close()
+        del p64
+        torch.cuda.empty_cache()
 
+    # --- solutions against the oracle's FP64 solution (cpu_sample^3) -------
+    cpu = None
+    if cpu_p is not None:
+        cpu = cpu_q.get()
+        cpu_p.join(timeout=60)
+    parity = None
+    if cpu is not None and "solution" in cpu:
+        hs = problems.hetero_mesh(args.cpu_sample)
+        xo = np.asarray(cpu["solution"]["x"])
+        parity = {"cells": args.cpu_sample, "dofs": int(len(xo)),
+                  "oracle": "FP64 Jacobi-PCG to a %.0e relative residual (%d iterations)"
+                            % (1e-12, cpu["solution"]["iters"])}
+        cases = [("learned_mixed", _lib.PRECOND_LEARNED, torch.float32),
+                 ("block_jacobi_mixed", _lib.PRECOND_BLOCK_JACOBI, torch.float32),
+                 ("fp64_jacobi", _lib.PRECOND_JACOBI, torch.float64)]
+        for name, pc, dt in cases:
+            ps = problems.HeteroElasticity(ctx, hs, dtype=dt, precond=pc,
+                                           learned_params=prm if pc == _lib.PRECOND_LEARNED
+                                           else None)
+            r = ps.step()
+            u = ps.u.cpu().numpy()
+            parity[name] = {"relerr": float(np.linalg.norm(u - xo) / np.linalg.norm(xo)),
+                            "relres": (r.true_normr2 / r.bnorm2) ** 0.5, "iters": r.iters}
+            ps.close()
     if rank != 0:
         return
-    cpu = cpu_sample(args.cpu_sample)
+    host_cpu = cpu_host()
+    cpu_base = None
+    if cpu is not None and "config" in cpu:
+        c = cpu["config"]
+        it = fp64["iters"] if fp64 else FP64_JACOBI_ITERS.get(args.size, 0)
+        step_s = c["assembly_s"] + it * c["iter_s"]
+        cpu_base = {"value": c["dofs"] / step_s, "unit": "DOF/s", "cores": 1, "kind": "port",
+                    "sample": "the %d^3 workload itself (%d DOF), oracle restatement of the "
+                              "reference's CPU loops, 1 thread: FP64 assembly %.2f s + %d FP64 "
+                              "Jacobi-PCG iterations (this run's FP64 count) x %.4f s per "
+                              "iteration (timed over 1 and %d iterations); pattern %.2f s "
+                              "(init, not in the step)"
+                              % (args.size, c["dofs"], c["assembly_s"], it, c["iter_s"],
+                                 c["kmax"], c["pattern_s"]), **host_cpu}
+    elif cpu is not None:
+        cpu_base = {"value": None, "unit": "DOF/s", "cores": 1, "kind": "port",
+                    "sample": "failed: " + cpu.get("error", "?"), **host_cpu}
     out = {
         "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 matrix+SpMV, f64 dots/residual",
+        "dtype": "f32 matrix+SpMV+network, f64 dots/residual",
         "data": "synthetic (seeded Philox mesh, parameters and displacements)",
         "config": {"workload": workload_name(args.size, not args.no_reorder), "dofs": dofs,
                    "nnzb": m.nnzb,
-                   "method": "FP32 assembly + mixed-precision block-Jacobi PCG (FP32 matrix/"
-                             "vectors, FP64 dots, FP64 reliable updates), verified FP64 residual"
+                   "method": "FP32 assembly (element-blocks plan) + learned-preconditioned "
+                             "flexible mixed-precision PCG (symmetric form of the 3-layer "
+                             "hidden-64 message-passing network, evaluated as its degree-6 "
+                             "matrix polynomial; FP32 matrix/vectors, FP64 dots, FP64 reliable "
+                             "updates; block-Jacobi fallback), verified FP64 residual"
                              + ("; the iteration's SpMV on symmetric storage" if sym else ""),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (FP32 matrix 1.0 GB), no flush"},
-        "iters": iters, "checks": int(results[-1].checks), "relres_max": relres,
+        "iters": iters, "checks": int(results[-1].checks),
+        "fallbacks": int(results[-1].fallbacks), "relres_max": relres,
+        "learned_dof_per_s": value,
         "e2e": {"value": dofs * world / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -904,16 +1068,16 @@ def run_ours(args, rank, world, local):
                      "full_storage_spmv": {"ms_per_launch": full_ms,
                                            "algorithmic_bytes": full_bytes,
                                            "GBps": full_bytes / (full_ms / 1e3) / 1e9}},
-        "cpu_baseline": {"value": cpu["value"], "unit": "DOF/s", "cores": 1, "kind": "port",
-                         "sample": "%d^3 instance (%d DOF) of the same family: oracle pattern + "
-                                   "FP64 assembly + FP64 Jacobi-PCG to 1e-8 (%d iterations), "
-                                   "%.1f s" % (args.cpu_sample, cpu["dofs"], cpu["iters"],
-                                               cpu["seconds"])},
+        "cpu_baseline": cpu_base,
         "clocks": clk,
         "assembly": assembly,
+        "block_jacobi_mixed": bj,
         "fp64_jacobi_cg": fp64,
-        "learned_vs_block_jacobi": learned,
         "speedup_vs_fp64_cg": (fp64["ms"] / ms) if fp64 else None,
+        "target_3x_fp64_cg_met": (fp64["ms"] / ms >= 3.0) if fp64 else None,
+        "learned_vs_block_jacobi": ({"iteration_gain": bj["iters"] / max(1, iters),
+                                     "time_ratio": bj["ms"] / ms} if bj else None),
+        "solution_relerr_vs_fp64_oracle": parity,
     }
     print(json.dumps(out), flush=True)
 
@@ -934,8 +1098,16 @@ def time_jit_stiffness(ctx, prob):
     with ctx.stream():
         out = torch.empty_like(prob.A)
 
+    # the precompiled row-owner kernel (the same sg_mesh without its plan)
+    import ctypes
+    plain = _lib.Mesh.from_buffer_copy(m.s)
+    plain.slots = plain.color_order = plain.color_ptr = None
+    plain.slot_src_ptr = plain.slot_src = None
+    plain.ncolors = 0
+
     def builtin():
-        call("sg_assemble_tet_stiffness", ctx.h, m.ref(), dtype_code(prob.A), _lib.MODEL_LINEAR,
+        call("sg_assemble_tet_stiffness", ctx.h, ctypes.byref(plain), dtype_code(prob.A),
+             _lib.MODEL_LINEAR,
              ptr(prob.x), ptr(prob.c), ptr(prob.B), ptr(prob.W), ptr(prob.mu), ptr(prob.lam),
              problems.H, problems.RHO, ptr(prob.A), 0)
 

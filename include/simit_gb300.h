@@ -459,6 +459,13 @@ int sg_solver_create(sg_ctx *ctx, const sg_matrix *A, const sg_solve_opts *opts,
 /* Solve A x = b; b, x FP64 device arrays of n*bs; x holds the initial guess
  * and receives the solution.  Synchronises. */
 int sg_solver_solve(sg_solver *s, const double *b, double *x, sg_solve_result *res);
+/* The same with a right-hand side of either precision (b_dtype SG_F32 or
+ * SG_F64; an FP32 b, e.g. the force map of an FP32 assembly, is widened by
+ * the solver's own kernel into an FP64 copy it keeps) and, with x_zero = 1,
+ * the zero initial guess (x is only written).  Lets an assembly + solve step
+ * run without a separate conversion or fill. */
+int sg_solver_solve_ex(sg_solver *s, const void *b, int b_dtype, double *x, int x_zero,
+                       sg_solve_result *res);
 /* Re-read the matrix values after they changed in place (re-assembly):
  * refreshes the FP32 bulk copy and the (block-)Jacobi diagonal; the captured
  * iteration graph is kept. */

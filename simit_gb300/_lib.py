@@ -114,6 +114,7 @@ SIGNATURES = {
     "sg_solver_create": (_CI, [P, ctypes.POINTER(Matrix), ctypes.POINTER(SolveOpts),
                                ctypes.POINTER(P)]),
     "sg_solver_solve": (_CI, [P, P, P, ctypes.POINTER(SolveResult)]),
+    "sg_solver_solve_ex": (_CI, [P, P, _CI, P, _CI, ctypes.POINTER(SolveResult)]),
     "sg_solver_destroy": (_CI, [P]),
     "sg_solver_refresh": (_CI, [P]),
     "sg_dot_noalloc": (_CI, [P, I64, _CI, P, P, P]),

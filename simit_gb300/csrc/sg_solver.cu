@@ -112,6 +112,12 @@ __global__ void k_f64_to_f32(int64_t len, const double *__restrict__ a, float *_
     b[i] = (float)a[i];
 }
 
+__global__ void k_f32_to_f64(int64_t len, const float *__restrict__ a, double *__restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
 // ---------------------------------------------------------------------------
 enum Kind { KIND_F64 = 0, KIND_F64_M32 = 1, KIND_MIXED = 2 };
 
@@ -361,7 +367,10 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
   const bool mixed = S->kind == KIND_MIXED;
   memset(res, 0, sizeof(*res));
   S->launches = 0;
-  SG_CHECK_CUDA(cudaMemcpyAsync(S->xw, x, S->len * 8, cudaMemcpyDeviceToDevice, st));
+  if (S->x_zero)
+    SG_CHECK_CUDA(cudaMemsetAsync(S->xw, 0, S->len * 8, st));
+  else
+    SG_CHECK_CUDA(cudaMemcpyAsync(S->xw, x, S->len * 8, cudaMemcpyDeviceToDevice, st));
   SG_CHECK_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(SolveCtl), st));
   if (mixed) SG_CHECK_CUDA(cudaMemsetAsync(S->xlo, 0, S->len * sizeof(XT), st));
   // b'b
@@ -582,6 +591,28 @@ int sg_solver_solve(sg_solver *hs, const double *b, double *x, sg_solve_result *
   Solver *S = reinterpret_cast<Solver *>(hs);
   SG_REQUIRE(S && b && x && res, "sg_solver_solve: null argument");
   return solver_solve(S, b, x, res);
+}
+
+int sg_solver_solve_ex(sg_solver *hs, const void *b, int b_dtype, double *x, int x_zero,
+                       sg_solve_result *res) {
+  Solver *S = reinterpret_cast<Solver *>(hs);
+  SG_REQUIRE(S && b && x && res, "sg_solver_solve_ex: null argument");
+  SG_REQUIRE(b_dtype == SG_F32 || b_dtype == SG_F64, "sg_solver_solve_ex: b_dtype %d", b_dtype);
+  const double *b64 = (const double *)b;
+  if (b_dtype == SG_F32) {
+    if (!S->b64) {
+      SG_CHECK_CUDA(cudaMalloc((void **)&S->b64, (size_t)S->len * 8 + 8));
+      S->allocs.push_back(S->b64);
+    }
+    k_f32_to_f64<<<S->P2, RED_T, 0, S->c->stream>>>(S->len, (const float *)b, S->b64);
+    SG_CHECK_LAUNCH();
+    b64 = S->b64;
+  }
+  S->x_zero = x_zero ? 1 : 0;
+  const int rc = solver_solve(S, b64, x, res);
+  S->x_zero = 0;
+  if (rc == SG_OK && b_dtype == SG_F32) res->kernels += 1;
+  return rc;
 }
 
 int sg_solver_refresh(sg_solver *hs) {

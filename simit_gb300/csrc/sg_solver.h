@@ -48,6 +48,10 @@ struct Solver {
   // > 0: K3 sums this many partials per dot (the external preconditioner's
   // last kernel wrote them with its own grid), else P2
   int np2_ext = 0;
+  // sg_solver_solve_ex: the FP64 copy of an FP32 right-hand side (allocated
+  // on first use) and a zero initial guess for the current solve
+  double *b64 = nullptr;
+  int x_zero = 0;
   void *ext = nullptr;
   SymBsr *sym = nullptr;  // SG_STORAGE_SYMMETRIC: K1 reads the upper half
   int k3_xupd = 0;        // K3 applies x += alpha p (K2 = k_cg_update_w without x)

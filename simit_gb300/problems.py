@@ -71,7 +71,7 @@ class HeteroElasticity:
 
     def __init__(self, ctx, host, dtype=torch.float32, precond=_lib.PRECOND_BLOCK_JACOBI,
                  precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None, pdl=0,
-                 plan="gather"):
+                 plan="gather", learned_params=None, learned_exec=_lib.MPNN_EXEC_FOLDED):
         self.ctx, self.host, self.dtype = ctx, host, dtype
         # plan: the element-parallel assembly plan ("gather", "colored"; each
         # element computed once), or None for the row-owner kernels
@@ -85,17 +85,22 @@ class HeteroElasticity:
             self.c = torch.tensor(host["c"], device=d)
             self.v0 = torch.zeros(host["n"] * 3, dtype=dtype, device=d)
             self.u = torch.zeros(host["n"] * 3, dtype=torch.float64, device=d)
+            self.f = torch.zeros(host["n"] * 3, dtype=dtype, device=d)
         self.B, self.W, _ = tet_precompute(self.mesh, self.X0, RHO, dtype=dtype)
         self.assemble()
         if precision is None:
             precision = _lib.SOLVE_MIXED if dtype == torch.float32 else _lib.SOLVE_F64
         if storage is None:
             storage = _lib.STORAGE_FULL
+        # precond PRECOND_LEARNED: the learned preconditioner with
+        # learned_params (a device FP32 tensor), symmetric form
         self.opts = solve_opts(precision=precision, precond=precond, stop=_lib.STOP_RELATIVE,
                                tol=tol, maxiters=maxiters, verify=1, lanes=lanes,
-                               storage=storage, pdl=pdl)
+                               storage=storage, pdl=pdl, learned_params=learned_params,
+                               learned_form=_lib.MPNN_SYM, learned_exec=learned_exec)
         self.solver = Solver(ctx, self.mesh.n, 3, self.mesh.pattern.rowptr,
-                             self.mesh.pattern.colidx, self.A, self.mesh.nnzb, self.opts)
+                             self.mesh.pattern.colidx, self.A, self.mesh.nnzb, self.opts,
+                             learned_params_keep=learned_params)
 
     @property
     def dofs(self):
@@ -113,24 +118,25 @@ class HeteroElasticity:
         return self.A, self.b
 
     def assemble_in_place(self):
-        """The step's assembly: the stiffness map into A in place and the
-        force map; returns the force."""
+        """The step's assembly: the stiffness map into A and the force map
+        into f, in place; returns f."""
         m = self.mesh
-        from .runtime import call, ptr, dtype_code
+        from .runtime import call, ptr, dtype_code, _host_f64
         call("sg_assemble_tet_stiffness", self.ctx.h, m.ref(), dtype_code(self.A),
              _lib.MODEL_LINEAR, ptr(self.x), ptr(self.c), ptr(self.B), ptr(self.W), ptr(self.mu),
              ptr(self.lam), H, RHO, ptr(self.A), 0)
-        return assemble_tet_force(m, _lib.MODEL_LINEAR, self.x, self.v0, self.c, self.B, self.W,
-                                  self.mu, self.lam, H, RHO, GRAV, dtype=self.dtype, exact=False)
+        call("sg_assemble_tet_force", self.ctx.h, m.ref(), dtype_code(self.f), _lib.MODEL_LINEAR,
+             ptr(self.x), ptr(self.v0), ptr(self.c), ptr(self.B), ptr(self.W), ptr(self.mu),
+             ptr(self.lam), H, RHO, _host_f64(GRAV), ptr(self.f), 0)
+        return self.f
 
     def step(self):
-        """One pass of the hot path: assemble in place, refresh, solve from 0."""
+        """One pass of the hot path: assemble in place, refresh the solver's
+        matrix data, solve from zero (the solver widens the force to FP64
+        itself); only the library's own kernels run."""
         f = self.assemble_in_place()
-        with self.ctx.stream():
-            self.b.copy_(f)
-            self.u.zero_()
         self.solver.refresh()
-        return self.solver.solve(self.b, self.u)
+        return self.solver.solve_ex(f, self.u, x_zero=True)
 
     def step_host(self, x_host, mu_host, lam_host, u_host):
         """End to end through host buffers: pinned inputs (positions and the

@@ -553,6 +553,15 @@ class Solver:
         call("sg_solver_solve", self.h, ptr(b), ptr(x), ctypes.byref(res))
         return res
 
+    def solve_ex(self, b, x, x_zero=False):
+        """b FP32 or FP64 (widened by the solver), x FP64 (the guess unless
+        x_zero; receives the solution)."""
+        assert x.dtype == torch.float64 and b.dtype in (torch.float32, torch.float64)
+        res = _lib.SolveResult()
+        call("sg_solver_solve_ex", self.h, ptr(b), dtype_code(b), ptr(x), int(bool(x_zero)),
+             ctypes.byref(res))
+        return res
+
     def refresh(self):
         """The matrix values changed in place (re-assembly)."""
         call("sg_solver_refresh", self.h)
