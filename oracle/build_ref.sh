@@ -4,9 +4,15 @@
 # oracle/ref_pattern.cpp into oracle/_ref/libref_pattern.so.  Needs only g++;
 # it does not run the reference's cmake build.  Skips quietly when the
 # reference source tree is absent.
+#
+#   sh oracle/build_ref.sh [REFERENCE_SRC_DIR]
+#
+# The source directory (the reference's src/) comes from the argument, else
+# from SIMIT_REFERENCE_SRC, else from a reference checkout beside this
+# repository (../reference/src).
 set -e
-REF=${SIMIT_REFERENCE_SRC:-/root/reference/src}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${SIMIT_REFERENCE_SRC:-$HERE/../../reference/src}}
 OUT=$HERE/_ref
 if [ ! -f "$REF/path_indices.cpp" ]; then
   echo "build_ref: reference sources not found at $REF; skipping" >&2

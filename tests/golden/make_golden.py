@@ -1,8 +1,11 @@
 """Regenerate the golden fixtures in this directory from the reference tree.
 
-Run in a checkout that has the reference sources (default path below, or
-SIMIT_REFERENCE); the machines that run the tests need not have it, so the
-outputs are committed:
+Run with the reference checkout as the first argument (or SIMIT_REFERENCE,
+or a checkout beside this repository); the machines that run the tests need
+not have it, so the outputs are committed.  `make_golden.py [REF] lattice`
+rewrites only lattice_golden.json.
+
+
 
   reference_golden.json   golden values asserted by the reference's tests,
                           extracted from their sources (file:line recorded),
@@ -22,6 +25,10 @@ outputs are committed:
                           reference PathIndexBuilder's rowptr / colidx and of
                           the `loc` slot map, for the tets and for the springs
                           over the bunny's edges
+  lattice_golden.json     the same digests for the benchmark configurations'
+                          five-tet lattices: 64^3 (lattice order), 128^3
+                          (lattice order) and 128^3 in the workload's Morton
+                          order
 """
 import hashlib
 import json
@@ -34,7 +41,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("SIMIT_REFERENCE", "/root/reference")
+# the reference checkout: the first argument, else SIMIT_REFERENCE, else a
+# checkout beside this repository
+REF = (sys.argv[1] if len(sys.argv) > 1 and os.path.isdir(sys.argv[1])
+       else os.environ.get("SIMIT_REFERENCE", os.path.join(os.path.dirname(REPO), "reference")))
 
 
 def sha(a, dtype):
@@ -191,5 +201,33 @@ def main():
     print("wrote golden fixtures to", HERE)
 
 
+def lattice():
+    """Digests of the reference builder's pattern and slot map on the
+    configurations' lattices (a few minutes: the 128^3 pattern has 27.6M
+    blocks)."""
+    sys.path.insert(0, REPO)
+    from oracle import oracle
+    oracle.build_ref()
+    from simit_gb300 import meshgen, problems
+    cases = {"tet_grid_64": meshgen.tet_grid(64)["tets"],
+             "tet_grid_128": meshgen.tet_grid(128)["tets"]}
+    cases["tet_grid_128_morton"] = problems.reorder_hetero(problems.hetero_mesh(128))["tets"]
+    out = {}
+    for name, tets in cases.items():
+        n = int(tets.max()) + 1
+        rp, ci = oracle.ref_pattern(n, tets, 4)
+        sl = oracle.ref_slots(tets, 4, rp, ci)
+        out[name] = {"n": n, "card": 4, "nE": int(len(tets) // 4), "nnzb": int(len(ci)),
+                     "endpoints_sha256": sha(tets, np.int32),
+                     "rowptr_sha256": sha(rp, np.uint32), "colidx_sha256": sha(ci, np.uint32),
+                     "slots_sha256": sha(sl, np.uint32)}
+        print(name, out[name]["nnzb"], flush=True)
+    with open(os.path.join(HERE, "lattice_golden.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[-1] == "lattice":
+        lattice()
+    else:
+        main()
