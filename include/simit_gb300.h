@@ -579,17 +579,20 @@ int sg_mpnn_adam(sg_ctx *ctx, float *params, const float *grad, float *m, float 
  * caller cannot create an sg_ctx (its set-up allocates) or use sg_dot (its
  * partial sums live in the context's growable scratch arena).
  *
- * Same result as sg_dot (FP64 accumulation, deterministic order), computed
- * on `stream` (a cudaStream_t, NULL = legacy default stream) into the
- * caller's DEVICE double *d_out, asynchronously.  The partial sums live in a
+ * FP64 accumulation in a fixed order (deterministic for a given len; sums
+ * are split by 4096-element chunks, so the last bits may differ from
+ * sg_dot's), computed on `stream` (a cudaStream_t of the current device, NULL
+ * = legacy default stream) into the caller's DEVICE double *d_out,
+ * asynchronously.  The partial sums live in a
  * fixed static device array (SG_DOT_NOALLOC_MAX_PARTS doubles, 512 KB, held
  * by every GPU that loads the library until exit), so len is limited to
  * SG_DOT_NOALLOC_MAX_LEN elements; longer vectors are rejected with
  * SG_ERR_ARG.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) while that device is current; make it
- * before any stream capture.  Calls share the array: calls whose kernels
- * may overlap on the GPU (unordered streams) race, so order them on one
- * stream.
+ * address (cudaGetSymbolAddress) while that device is current and loads the
+ * kernels, which may allocate once; make it before any stream capture and
+ * before the stretch that must not allocate.  Calls share the array: calls
+ * whose kernels may overlap on the GPU (unordered streams) race, so order
+ * them on one stream.
  * ------------------------------------------------------------------- */
 #define SG_DOT_NOALLOC_CHUNK 4096
 #define SG_DOT_NOALLOC_MAX_PARTS 65536

@@ -153,6 +153,7 @@ extern "C" {
 
 int sg_slot_sources(sg_ctx *h, const sg_mesh *m, uint32_t *slot_src_ptr, uint32_t *slot_src) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && m && slot_src_ptr, "sg_slot_sources: null argument");
   const int64_t mm = m->nE * (int64_t)m->card * m->card;
   SG_REQUIRE(mm == 0 || (m->slots && slot_src), "sg_slot_sources: the mesh needs its slots");
@@ -182,6 +183,7 @@ int sg_slot_sources(sg_ctx *h, const sg_mesh *m, uint32_t *slot_src_ptr, uint32_
 int sg_element_coloring(sg_ctx *h, const sg_mesh *m, uint32_t *color_order, int32_t *color_ptr,
                         int32_t *h_ncolors) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && m && color_ptr && h_ncolors, "sg_element_coloring: null argument");
   SG_REQUIRE(m->nE == 0 || (color_order && m->endpoints && m->ve_ptr && m->ve_idx),
              "sg_element_coloring: the mesh needs endpoints and its incidence");

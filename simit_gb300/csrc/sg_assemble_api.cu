@@ -31,6 +31,7 @@ extern "C" {
 
 int sg_pattern_maxrow(sg_ctx *h, int32_t n, const uint32_t *rowptr, int32_t *h_maxrow) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && rowptr && h_maxrow, "sg_pattern_maxrow: null argument");
   if (n <= 0) {
     *h_maxrow = 0;
@@ -53,6 +54,7 @@ int sg_assemble_springs(sg_ctx *h, const sg_mesh *m, int dt, int form, const voi
                         const void *l0, double hh, double viscous, const double *grav,
                         void *vals, void *f, int exact) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_assemble_springs: null context");
   SG_TRY(check_mesh(m, true, "sg_assemble_springs"));
   SG_REQUIRE(m->card == 2, "sg_assemble_springs: springs have 2 endpoints, got %d", m->card);
@@ -67,6 +69,7 @@ int sg_assemble_springs(sg_ctx *h, const sg_mesh *m, int dt, int form, const voi
 int sg_assemble_scalar_springs(sg_ctx *h, const sg_mesh *m, int dt, const void *a,
                                double diag, double scale, void *vals, int exact) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_assemble_scalar_springs: null context");
   SG_TRY(check_mesh(m, true, "sg_assemble_scalar_springs"));
   SG_REQUIRE(m->card == 2 && vals && (m->nE == 0 || a), "sg_assemble_scalar_springs: bad args");
@@ -76,6 +79,7 @@ int sg_assemble_scalar_springs(sg_ctx *h, const sg_mesh *m, int dt, const void *
 int sg_assemble_blocks(sg_ctx *h, const sg_mesh *m, int dt, int bs, const void *eb, void *vals,
                        int exact) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_assemble_blocks: null context");
   SG_TRY(check_mesh(m, true, "sg_assemble_blocks"));
   SG_REQUIRE(bs >= 1 && bs <= 3 && m->card >= 2 && m->card <= 4,
@@ -87,6 +91,7 @@ int sg_assemble_blocks(sg_ctx *h, const sg_mesh *m, int dt, int bs, const void *
 int sg_tet_precompute(sg_ctx *h, const sg_mesh *m, int dt, const void *x, double rho, void *B,
                       void *W, void *mass) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_tet_precompute: null context");
   SG_TRY(check_mesh(m, false, "sg_tet_precompute"));
   SG_REQUIRE(m->card == 4 && x && mass && (m->nE == 0 || (B && W)),
@@ -98,6 +103,7 @@ int sg_assemble_tet_stiffness(sg_ctx *h, const sg_mesh *m, int dt, int model, co
                               const int32_t *cons, const void *B, const void *W, const void *mu,
                               const void *lam, double hh, double rho, void *vals, int exact) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_assemble_tet_stiffness: null context");
   SG_TRY(check_mesh(m, true, "sg_assemble_tet_stiffness"));
   SG_REQUIRE(m->card == 4 && cons && vals && (m->nE == 0 || (B && W && mu && lam)),
@@ -121,6 +127,7 @@ int sg_assemble_tet_force(sg_ctx *h, const sg_mesh *m, int dt, int model, const 
                           const void *mu, const void *lam, double hh, double rho,
                           const double *grav, void *f, int exact) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_assemble_tet_force: null context");
   SG_TRY(check_mesh(m, false, "sg_assemble_tet_force"));
   SG_REQUIRE(m->card == 4 && x && v && cons && grav && f && (m->nE == 0 || (B && W && mu && lam)),
@@ -133,6 +140,7 @@ int sg_assemble_heat(sg_ctx *h, const sg_mesh *m, int dt, const void *B, const v
                      const void *kappa, double dtt, const void *T0, void *vals, void *b,
                      int exact) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_assemble_heat: null context");
   SG_TRY(check_mesh(m, true, "sg_assemble_heat"));
   SG_REQUIRE(m->card == 4 && T0 && vals && b && (m->nE == 0 || (B && W && kappa)),

@@ -272,6 +272,7 @@ extern "C" int sg_batched_pcg(sg_ctx *h, int32_t nsys, const int32_t *sys_ptr,
                               double tol, int32_t maxiters, int32_t config, int32_t *iters,
                               int32_t *status, double *relres) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && A && sys_ptr && order && b && x && iters && status && relres,
              "sg_batched_pcg: null argument");
   SG_REQUIRE(nsys >= 1 && A->bs == 3 && A->dtype == SG_F32 && A->n >= 1,

@@ -44,8 +44,10 @@ int check_device_error(Ctx *c, const char *what) {
                                   "row longer than the assembly accumulator",
                                   "vertex without a diagonal block",
                                   "bulk-copy barrier wait timed out",
-                                  "an element needs more than 128 colours"};
-    const char *nm = (e > 0 && e < 8) ? names[e] : "unknown";
+                                  "an element needs more than 128 colours",
+                                  "bulk copies still in flight after a timeout (results "
+                                  "undefined; destroy and recreate the context)"};
+    const char *nm = (e > 0 && e < 9) ? names[e] : "unknown";
     return set_error(SG_ERR_DEVICE, "%s: device check failed (%d: %s)", what, e,
                      nm);
   }
@@ -229,7 +231,9 @@ int sg_ctx_create(int device, sg_ctx **out) {
   SG_CHECK_CUDA(cudaGetDeviceCount(&ndev));
   if (device < 0 || device >= ndev)
     return set_error(SG_ERR_ARG, "sg_ctx_create: device %d of %d", device, ndev);
-  SG_CHECK_CUDA(cudaSetDevice(device));
+  // the context's device is current while it is set up; the caller's
+  // current device is restored on return
+  DeviceGuardT<CudaDeviceApi> dg_(device);
   Ctx *c = new Ctx();
   c->device = device;
   SG_CHECK_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
@@ -245,6 +249,7 @@ int sg_ctx_create(int device, sg_ctx **out) {
 
 int sg_ctx_destroy(sg_ctx *h) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   if (!c) return SG_OK;
   ctx_release(c);
   return SG_OK;
@@ -252,6 +257,7 @@ int sg_ctx_destroy(sg_ctx *h) {
 
 int sg_ctx_sync(sg_ctx *h) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   if (!c) return set_error(SG_ERR_ARG, "sg_ctx_sync: null context");
   return check_device_error(c, "sg_ctx_sync");
 }
@@ -264,6 +270,7 @@ const char *sg_version(void) { return "simit_gb300 0.1 (sm_103a)"; }
 
 int sg_axpy(sg_ctx *h, int64_t len, int vdt, double alpha, const void *x, void *y) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && (len == 0 || (x && y)), "sg_axpy: null argument");
   SG_REQUIRE(len >= 0 && (vdt == SG_F32 || vdt == SG_F64), "sg_axpy: bad len/dtype");
   if (len == 0) return SG_OK;
@@ -279,6 +286,7 @@ int sg_axpy(sg_ctx *h, int64_t len, int vdt, double alpha, const void *x, void *
 int sg_dot(sg_ctx *h, int64_t len, int vdt, const void *a, const void *b,
            double *h_out) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && a && b && h_out, "sg_dot: null argument");
   SG_REQUIRE(len >= 0 && (vdt == SG_F32 || vdt == SG_F64), "sg_dot: bad len/dtype");
   const int T = 256;

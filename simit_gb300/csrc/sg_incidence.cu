@@ -92,6 +92,7 @@ int sg_incidence_pattern(sg_ctx *h, int kind, int32_t n, int64_t nE, int32_t npo
                          const int32_t *sel, uint32_t *rowptr, uint32_t *colidx,
                          uint32_t *slot_of) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && rowptr, "sg_incidence_pattern: null argument");
   SG_REQUIRE(kind == SG_INCIDENCE_EV || kind == SG_INCIDENCE_VE,
              "sg_incidence_pattern: kind %d", kind);
@@ -126,6 +127,7 @@ int sg_assemble_incidence(sg_ctx *h, int kind, int64_t nE, int32_t npos, const i
                           const uint32_t *slot_of, int dtype, int32_t bs, const void *eb,
                           void *vals) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_assemble_incidence: null context");
   SG_REQUIRE(kind == SG_INCIDENCE_EV || kind == SG_INCIDENCE_VE,
              "sg_assemble_incidence: kind %d", kind);
@@ -265,6 +267,7 @@ int sg_pattern_rect(sg_ctx *h, int32_t nr, int32_t nc, int64_t nE, int32_t npos_
                     const uint32_t *ve_idx, uint32_t *rowptr, uint32_t *colidx,
                     int64_t *h_nnzb) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && rowptr && h_nnzb && ve_ptr, "sg_pattern_rect: null argument");
   SG_REQUIRE(nr >= 0 && nc >= 0 && nE >= 0 && npos_r >= 1 && npos_r <= 16 && npos_c >= 1 &&
                  npos_c <= 16,
@@ -302,6 +305,7 @@ int sg_assemble_rect(sg_ctx *h, int32_t nr, int32_t npos_r, int32_t npos_c,
                      const uint32_t *rowptr, const uint32_t *colidx, int dtype, int32_t bs,
                      const void *eb, void *vals) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && ve_ptr && rowptr, "sg_assemble_rect: null argument");
   SG_REQUIRE(nr >= 0 && npos_r >= 1 && npos_r <= 16 && npos_c >= 1 && npos_c <= 16 && bs >= 1 &&
                  bs <= 4,

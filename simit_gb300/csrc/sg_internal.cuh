@@ -9,6 +9,7 @@
 #include <string>
 
 #include "../../include/simit_gb300.h"
+#include "sg_device_guard.h"
 
 namespace sg {
 
@@ -91,6 +92,8 @@ enum DevErr : int {
   DEV_NO_DIAGONAL = 5,    // vertex without a diagonal block
   DEV_TMA_TIMEOUT = 6,    // a bulk-copy barrier wait ran out of polls
   DEV_TOO_MANY_COLORS = 7,  // element colouring needs more than SG_MAX_COLORS
+  DEV_TMA_UNDRAINED = 8,    // after a timeout, a copy was still in flight at exit:
+                            // results undefined, reset the context
 };
 
 int set_error(int code, const char *fmt, ...);
@@ -156,6 +159,16 @@ inline int grid_for(const Ctx *c, int64_t work_items, int threads, int per_sm) {
 }
 
 inline Ctx *as_ctx(sg_ctx *h) { return reinterpret_cast<Ctx *>(h); }
+
+struct CudaDeviceApi {
+  static bool get(int *d) { return cudaGetDevice(d) == cudaSuccess; }
+  static bool set(int d) { return cudaSetDevice(d) == cudaSuccess; }
+};
+// Makes the context's device current for one entry point (see
+// sg_device_guard.h); a null context is a no-op.
+struct DeviceGuard : DeviceGuardT<CudaDeviceApi> {
+  explicit DeviceGuard(const Ctx *c) : DeviceGuardT<CudaDeviceApi>(c ? c->device : -1) {}
+};
 
 // dtype helpers
 inline size_t dtype_size(int dt) { return dt == SG_F64 ? 8 : 4; }

@@ -257,6 +257,7 @@ int sg_jit_check_source(const char *element_src, int32_t card, int32_t bs, int d
 int sg_jit_assembly_create(sg_ctx *h, const char *element_src, int32_t card, int32_t bs,
                            int dtype, int32_t exact, sg_jit_assembly **out) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && element_src && out, "sg_jit_assembly_create: null argument");
   std::vector<char> image;
   std::string log;
@@ -283,6 +284,7 @@ int sg_jit_assembly_create(sg_ctx *h, const char *element_src, int32_t card, int
 int sg_jit_assemble(sg_jit_assembly *hj, const sg_mesh *m, const void *const *h_fields,
                     int32_t nfields, void *vals) {
   JitAssembly *J = reinterpret_cast<JitAssembly *>(hj);
+  DeviceGuard dg_(J ? J->c : nullptr);
   SG_REQUIRE(J && m && vals, "sg_jit_assemble: null argument");
   SG_REQUIRE(m->card == J->card, "sg_jit_assemble: mesh card %d, kernel card %d", m->card,
              J->card);
@@ -319,6 +321,7 @@ int sg_jit_assemble(sg_jit_assembly *hj, const sg_mesh *m, const void *const *h_
 
 int sg_jit_assembly_destroy(sg_jit_assembly *hj) {
   JitAssembly *J = reinterpret_cast<JitAssembly *>(hj);
+  DeviceGuard dg_(J ? J->c : nullptr);
   if (!J) return SG_OK;
   cudaStreamSynchronize(J->c->stream);
   if (J->lib) cudaLibraryUnload(J->lib);

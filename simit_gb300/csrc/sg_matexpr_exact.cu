@@ -133,6 +133,7 @@ extern "C" int sg_bsr_add_diag(sg_ctx *h, int32_t n, int32_t bs, const uint32_t 
                                const void *diag, double ident, double scale, const void *vals,
                                void *out) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c, "sg_bsr_add_diag: null context");
   SG_REQUIRE(n >= 0 && bs >= 1 && bs <= 3, "sg_bsr_add_diag: n %d bs %d (bs 1..3)", n, bs);
   SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, "sg_bsr_add_diag: dtype %d", dtype);

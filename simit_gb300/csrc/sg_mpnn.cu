@@ -661,6 +661,7 @@ int sg_mpnn_nparams(void) { return mpnn::NPARAM; }
 
 int sg_mpnn_graph_create(sg_ctx *h, const sg_matrix *A, sg_mpnn_graph **out) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && A && out, "sg_mpnn_graph_create: null argument");
   mpnn::GraphH *G = new mpnn::GraphH();
   int rc = mpnn::graph_init(c, A, G);
@@ -675,6 +676,7 @@ int sg_mpnn_graph_create(sg_ctx *h, const sg_matrix *A, sg_mpnn_graph **out) {
 
 int sg_mpnn_graph_set_form(sg_mpnn_graph *hg, int form) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
   SG_REQUIRE(G, "sg_mpnn_graph_set_form: null graph");
   SG_REQUIRE(form >= SG_MPNN_RELU && form <= SG_MPNN_SYM, "sg_mpnn_graph_set_form: form %d", form);
   SG_TRY(mpnn::set_sym(G, form == SG_MPNN_SYM));
@@ -684,12 +686,14 @@ int sg_mpnn_graph_set_form(sg_mpnn_graph *hg, int form) {
 
 int sg_mpnn_graph_refresh(sg_mpnn_graph *hg) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
   SG_REQUIRE(G, "sg_mpnn_graph_refresh: null graph");
   return mpnn::graph_refresh(G);
 }
 
 int sg_mpnn_graph_destroy(sg_mpnn_graph *hg) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
   if (!G) return SG_OK;
   cudaStreamSynchronize(G->c->stream);
   Ctx *c = G->c;
@@ -700,6 +704,7 @@ int sg_mpnn_graph_destroy(sg_mpnn_graph *hg) {
 
 int sg_mpnn_graph_set_exec(sg_mpnn_graph *hg, int exec) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
   SG_REQUIRE(G, "sg_mpnn_graph_set_exec: null graph");
   SG_REQUIRE(exec >= SG_MPNN_EXEC_FOLDED && exec <= SG_MPNN_EXEC_FOLDED_F32,
              "sg_mpnn_graph_set_exec: mode %d", exec);
@@ -712,6 +717,7 @@ int sg_mpnn_graph_set_exec(sg_mpnn_graph *hg, int exec) {
 
 int sg_mpnn_forward(sg_mpnn_graph *hg, const float *params, const float *r, float *z, int train) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
   SG_REQUIRE(G && params && r && z, "sg_mpnn_forward: null argument");
   if (!train && G->exec != SG_MPNN_EXEC_LAYERED && G->g.sym) {
     SG_TRY(mpnn::fold_params(G, G->c->stream, params));
@@ -724,6 +730,7 @@ int sg_mpnn_forward(sg_mpnn_graph *hg, const float *params, const float *r, floa
 
 int sg_mpnn_backward(sg_mpnn_graph *hg, const float *params, const float *dz, float *grad) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
   SG_REQUIRE(G && params && dz && grad, "sg_mpnn_backward: null argument");
   SG_REQUIRE(G->train_ready, "sg_mpnn_backward: run sg_mpnn_forward with train=1 first");
   return mpnn::backward(G, params, dz, grad);
@@ -732,6 +739,7 @@ int sg_mpnn_backward(sg_mpnn_graph *hg, const float *params, const float *dz, fl
 int sg_mpnn_loss(sg_mpnn_graph *hg, const float *z, const float *e, double eAe, float *dz,
                  double *h_loss) {
   mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
   SG_REQUIRE(G && z && e && dz && h_loss && eAe > 0, "sg_mpnn_loss: bad argument");
   SG_REQUIRE(G->g.vdt == SG_F32, "sg_mpnn_loss: the graph's matrix must be FP32");
   SG_TRY(mpnn::ensure_train(G));
@@ -753,6 +761,7 @@ int sg_mpnn_loss(sg_mpnn_graph *hg, const float *z, const float *e, double eAe, 
 int sg_mpnn_adam(sg_ctx *h, float *params, const float *grad, float *m, float *v, int step,
                  float lr, float beta1, float beta2, float eps) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && params && grad && m && v && step >= 1, "sg_mpnn_adam: bad argument");
   const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
   mpnn::k_adam<<<(mpnn::NPARAM + 255) / 256, 256, 0, c->stream>>>(mpnn::NPARAM, params, grad, m, v,

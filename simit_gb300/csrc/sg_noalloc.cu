@@ -14,10 +14,14 @@
 // holds the array (512 KB) until the process exits.  Host code cannot use the
 // array's name as a device address (in host code it names a host-side
 // shadow), so the first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current and caches it; make that
-// first call outside any stream capture.  All calls share the one array: two
-// calls whose kernels overlap on the GPU (different streams, no ordering
-// between them) race on it, so order such calls on one stream.  Each call
+// cudaGetSymbolAddress while that device is current and caches it, and loads
+// this file's kernels (with lazy module loading the runtime would otherwise
+// load each on its first launch, which can allocate); make that first call
+// outside any stream capture and before the stretch that must not allocate.
+// `stream` must belong to the device that is current.  All calls share the
+// one array: two calls whose kernels overlap on the GPU (different streams,
+// no ordering between them) race on it, so order such calls on one stream.
+// Each call
 // overwrites every partial it later reads, so nothing is carried over from
 // the previous call's contents.
 #include <mutex>
@@ -88,6 +92,14 @@ int scratch_ptr(double **out) {
     cudaError_t e = cudaGetSymbolAddress((void **)&p, g_dot_parts);
     if (e != cudaSuccess || !p)
       return set_error(SG_ERR_CUDA, "sg_dot_noalloc: cudaGetSymbolAddress failed: %s",
+                       cudaGetErrorString(e));
+    // load the kernels now rather than at their first launch
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, k_dot_chunks<float>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_dot_chunks<double>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_dot_final);
+    if (e != cudaSuccess)
+      return set_error(SG_ERR_CUDA, "sg_dot_noalloc: loading the kernels failed: %s",
                        cudaGetErrorString(e));
     g_na_ptr[dev] = p;
   }

@@ -250,6 +250,7 @@ extern "C" {
 int sg_incidence_build(sg_ctx *h, int32_t n, const int32_t *ep, int64_t nE,
                        int32_t card, uint32_t *ve_ptr, uint32_t *ve_idx) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && ve_ptr && (nE == 0 || ve_idx), "sg_incidence_build: null argument");
   SG_TRY(check_pattern_args(n, ep, nE, card));
   const int64_t m = nE * card;
@@ -312,6 +313,7 @@ int sg_pattern_count(sg_ctx *h, int32_t n, const int32_t *ep, int64_t nE,
                      int32_t card, const uint32_t *ve_ptr, const uint32_t *ve_idx,
                      uint32_t *rowptr, int64_t *h_nnzb) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && ve_ptr && rowptr && h_nnzb, "sg_pattern_count: null argument");
   SG_TRY(check_pattern_args(n, ep, nE, card));
   Scratch s(c);
@@ -329,6 +331,7 @@ int sg_pattern_fill(sg_ctx *h, int32_t n, const int32_t *ep, int64_t nE,
                     int32_t card, const uint32_t *ve_ptr, const uint32_t *ve_idx,
                     const uint32_t *rowptr, uint32_t *colidx) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && ve_ptr && rowptr && (nE == 0 || colidx), "sg_pattern_fill: null argument");
   SG_TRY(check_pattern_args(n, ep, nE, card));
   Scratch s(c);
@@ -341,6 +344,7 @@ int sg_slots_build(sg_ctx *h, int32_t n, const int32_t *ep, int64_t nE,
                    int32_t card, const uint32_t *rowptr, const uint32_t *colidx,
                    uint32_t *slots) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && rowptr && (nE == 0 || (colidx && slots)), "sg_slots_build: null argument");
   SG_TRY(check_pattern_args(n, ep, nE, card));
   const int64_t m = nE * card;

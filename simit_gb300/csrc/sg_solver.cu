@@ -558,6 +558,7 @@ extern "C" {
 
 int sg_solver_create(sg_ctx *h, const sg_matrix *A, const sg_solve_opts *o, sg_solver **out) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && A && o && out, "sg_solver_create: null argument");
   SG_REQUIRE(A->n >= 1 && A->bs >= 1 && A->rowptr && A->colidx && A->vals,
              "sg_solver_create: bad matrix");
@@ -589,6 +590,7 @@ int sg_solver_create(sg_ctx *h, const sg_matrix *A, const sg_solve_opts *o, sg_s
 
 int sg_solver_solve(sg_solver *hs, const double *b, double *x, sg_solve_result *res) {
   Solver *S = reinterpret_cast<Solver *>(hs);
+  DeviceGuard dg_(S ? S->c : nullptr);
   SG_REQUIRE(S && b && x && res, "sg_solver_solve: null argument");
   return solver_solve(S, b, x, res);
 }
@@ -596,6 +598,7 @@ int sg_solver_solve(sg_solver *hs, const double *b, double *x, sg_solve_result *
 int sg_solver_solve_ex(sg_solver *hs, const void *b, int b_dtype, double *x, int x_zero,
                        sg_solve_result *res) {
   Solver *S = reinterpret_cast<Solver *>(hs);
+  DeviceGuard dg_(S ? S->c : nullptr);
   SG_REQUIRE(S && b && x && res, "sg_solver_solve_ex: null argument");
   SG_REQUIRE(b_dtype == SG_F32 || b_dtype == SG_F64, "sg_solver_solve_ex: b_dtype %d", b_dtype);
   const double *b64 = (const double *)b;
@@ -617,18 +620,22 @@ int sg_solver_solve_ex(sg_solver *hs, const void *b, int b_dtype, double *x, int
 
 int sg_solver_refresh(sg_solver *hs) {
   Solver *S = reinterpret_cast<Solver *>(hs);
+  DeviceGuard dg_(S ? S->c : nullptr);
   SG_REQUIRE(S, "sg_solver_refresh: null solver");
   return refresh_matrix(S);
 }
 
 int sg_solver_destroy(sg_solver *hs) {
-  solver_free(reinterpret_cast<Solver *>(hs));
+  Solver *S = reinterpret_cast<Solver *>(hs);
+  DeviceGuard dg_(S ? S->c : nullptr);
+  solver_free(S);
   return SG_OK;
 }
 
 int sg_residual(sg_ctx *h, const sg_matrix *A, const double *x, const double *b, double *r,
                 double *h_rr, int mode) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && A && x && b && r && h_rr, "sg_residual: null argument");
   SG_REQUIRE(A->n >= 1 && A->bs >= 1 && A->rowptr && A->colidx && A->vals,
              "sg_residual: bad matrix");

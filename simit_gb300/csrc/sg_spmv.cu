@@ -414,6 +414,7 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
                         const uint32_t *colidx, int vdt, const void *vals, int xdt,
                         const void *x, void *y, int32_t g) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && rowptr && colidx && vals && x && y, "sg_bspmv: null argument");
   SG_REQUIRE(n >= 0 && bs >= 1 && bs <= 16, "sg_bspmv: bad n=%d bs=%d", n, bs);
   if (n == 0) return SG_OK;

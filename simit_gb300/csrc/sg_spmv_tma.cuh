@@ -202,9 +202,15 @@ __global__ void __launch_bounds__(ROWS *G)
       ok_flag = ok ? 1 : 0;
       if (!ok) {
         atomicCAS(err, 0, 6 /* DEV_TMA_TIMEOUT */);
-        // drain the copies still in flight before leaving
-        for (int kk = k + 1; kk < my_tiles && kk <= kn; ++kk)
-          mbar_wait(&bar[kk % NST], (uint32_t)((kk / NST) & 1));
+        // no new copies; wait (bounded) on every barrier with a copy still
+        // in flight, this tile's included, before leaving; if one of those
+        // waits runs out too, a copy may still land in shared memory after
+        // the CTA exits: record that (the results are then undefined and
+        // the context should be reset)
+        bool drained = true;
+        for (int kk = k; kk < my_tiles && kk <= kn; ++kk)
+          drained = mbar_wait(&bar[kk % NST], (uint32_t)((kk / NST) & 1)) && drained;
+        if (!drained) atomicExch(err, 8 /* DEV_TMA_UNDRAINED */);
       }
     }
     __syncthreads();
@@ -327,8 +333,11 @@ __device__ __forceinline__ void wtma_body(const SolveCtl *__restrict__ ctl, int3
     if (!ok) {
       if (lane == 0) {
         atomicCAS(err, 0, 6 /* DEV_TMA_TIMEOUT */);
-        for (int64_t kk = k + 1; kk < my && kk <= kn; ++kk)
-          mbar_wait(&bar[kk % NST], (uint32_t)((kk / NST) & 1));
+        // drain every barrier with a copy in flight (see k_bsr3_tma)
+        bool drained = true;
+        for (int64_t kk = k; kk < my && kk <= kn; ++kk)
+          drained = mbar_wait(&bar[kk % NST], (uint32_t)((kk / NST) & 1)) && drained;
+        if (!drained) atomicExch(err, 8 /* DEV_TMA_UNDRAINED */);
       }
       break;
     }

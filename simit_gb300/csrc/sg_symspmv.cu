@@ -292,8 +292,11 @@ __global__ void __launch_bounds__(WTMA_WARPS * 32, 6)
     if (!ok) {
       if (lane == 0) {
         atomicCAS(err, 0, 6 /* DEV_TMA_TIMEOUT */);
-        for (int64_t kk = k + 1; kk < my && kk <= kn; ++kk)
-          mbar_wait(&bar[kk % NST], (uint32_t)((kk / NST) & 1));
+        // drain every barrier with a copy in flight (see k_bsr3_tma)
+        bool drained = true;
+        for (int64_t kk = k; kk < my && kk <= kn; ++kk)
+          drained = mbar_wait(&bar[kk % NST], (uint32_t)((kk / NST) & 1)) && drained;
+        if (!drained) atomicExch(err, 8 /* DEV_TMA_UNDRAINED */);
       }
       break;
     }
@@ -475,6 +478,7 @@ extern "C" {
 int sg_symbsr_create(sg_ctx *h, int32_t n, const uint32_t *rowptr, const uint32_t *colidx,
                      int64_t nnzb, int32_t stages, sg_symbsr **out) {
   Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
   SG_REQUIRE(c && out && rowptr && colidx, "sg_symbsr_create: null argument");
   auto *S = new SymBsr();
   const int rc = sym_create(c, n, rowptr, colidx, nnzb, stages, S);
@@ -490,18 +494,21 @@ int sg_symbsr_create(sg_ctx *h, int32_t n, const uint32_t *rowptr, const uint32_
 
 int sg_symbsr_fill(sg_symbsr *h, const float *vals) {
   SymBsr *S = reinterpret_cast<SymBsr *>(h);
+  DeviceGuard dg_(S ? S->c : nullptr);
   SG_REQUIRE(S && vals, "sg_symbsr_fill: null argument");
   return sym_fill(S, S->c->stream, vals);
 }
 
 int sg_symbsr_spmv(sg_symbsr *h, const float *x, float *y) {
   SymBsr *S = reinterpret_cast<SymBsr *>(h);
+  DeviceGuard dg_(S ? S->c : nullptr);
   SG_REQUIRE(S && x && y, "sg_symbsr_spmv: null argument");
   return sym_launch(S, S->c->stream, nullptr, false, x, y, nullptr);
 }
 
 int sg_symbsr_destroy(sg_symbsr *h) {
   SymBsr *S = reinterpret_cast<SymBsr *>(h);
+  DeviceGuard dg_(S ? S->c : nullptr);
   if (!S) return SG_OK;
   Ctx *c = S->c;
   cudaStreamSynchronize(c->stream);

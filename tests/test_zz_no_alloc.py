@@ -38,15 +38,37 @@ def test_no_alloc_dot_matches_sg_dot_twice(gpu_ctx, dtype):
     d = ctx.device
     out = torch.zeros(1, dtype=torch.float64, device=d)
     # two calls in a row with different sizes: the second must not see the
-    # first one's partial sums left in the shared static array
+    # first one's partial sums left in the shared static array; each result
+    # against the context's sg_dot and an FP64 sum on the host
     for seed, n in ((1, 3_000_001), (2, 12_345)):
         g = meshgen.rng(seed)
         a = torch.tensor(g.uniform(-1, 1, n), dtype=dtype, device=d)
         b = torch.tensor(g.uniform(-1, 1, n), dtype=dtype, device=d)
         ref = _dot_ctx(ctx, a, b)
         got = _dot_noalloc(ctx, a, b, out)
-        scale = float((a.double().abs() * b.double().abs()).sum())
+        ah, bh = a.double().cpu().numpy(), b.double().cpu().numpy()
+        host = float(np.dot(ah, bh))
+        scale = float(np.abs(ah) @ np.abs(bh))
         assert abs(got - ref) <= 1e-12 * scale, (n, got, ref)
+        assert abs(got - host) <= 1e-12 * scale, (n, got, host)
+
+
+def test_no_alloc_dot_allocates_nothing(gpu_ctx):
+    """After the first call on the device, further calls leave the device's
+    free memory unchanged."""
+    ctx = gpu_ctx
+    d = ctx.device
+    out = torch.zeros(1, dtype=torch.float64, device=d)
+    a = torch.rand(1_000_003, dtype=torch.float32, device=d)
+    b = torch.rand(1_000_003, dtype=torch.float32, device=d)
+    _dot_noalloc(ctx, a, b, out)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(d)
+    for _ in range(5):
+        _dot_noalloc(ctx, a, b, out)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(d)
+    assert free1 == free0
 
 
 MAX_LEN = 4096 * 65536  # SG_DOT_NOALLOC_MAX_LEN
