@@ -35,6 +35,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=48,
                     help="cells per edge of the instance whose oracle FP64 solution the GPU "
                          "solutions are compared to (48: about 15-25 s of one core)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="default schedules instead of the autotuners' choices")
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline and the solution check against the oracle")
     ap.add_argument("--no-block-jacobi", action="store_true",
@@ -821,6 +823,18 @@ def _step_timing(prob, st, steps, warmup, barrier):
     return e0.elapsed_time(e1) / steps, results
 
 
+def _tuned_summary(t):
+    """The autotuners' choices for the bench line."""
+    if not t:
+        return None
+    a, sp = t["assembly"], t["spmv"]
+    return {"spmv": {"g": sp["g"], "ms": sp["ms"], "default_ms": sp["default_ms"],
+                     "meaning": "g < 0: TMA variant -g-1 of sg_bspmv's table; g > 0: lanes "
+                                "per block row of the streaming kernel; 0: default"},
+            "assembly": {"plan": a["plan"], "tile": a["tile"], "ms": a["ms"],
+                         "default_ms": a["default_ms"], "times": a["times"]}}
+
+
 def run_ours(args, rank, world, local):
     # the CPU half of the line runs in a process spawned before any GPU call
     cpu_q = cpu_p = None
@@ -847,10 +861,13 @@ def run_ours(args, rank, world, local):
     with ctx.stream():
         prm = torch.tensor(lrn.load_weights("sym"), device=ctx.device)
     # the metric's method: FP32 assembly + learned-preconditioned mixed PCG
+    # tune: the assembly plan / element tile and the SpMV schedule from
+    # timings on this mesh (set-up, outside the timed steps)
     prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
                                      precond=_lib.PRECOND_LEARNED, learned_params=prm,
                                      storage=_lib.STORAGE_SYMMETRIC if args.sym
-                                     else _lib.STORAGE_FULL, pdl=int(args.pdl))
+                                     else _lib.STORAGE_FULL, pdl=int(args.pdl),
+                                     tune=not args.no_tune)
     st = ctx.torch_stream
 
     def barrier():
@@ -964,8 +981,13 @@ def run_ours(args, rank, world, local):
                 "algorithmic_bytes": asm_bytes, "GBps": asm_bytes / (asm_ms / 1e3) / 1e9,
                 "implementation_bytes": impl_bytes,
                 "implementation_GBps": impl_bytes / (asm_ms / 1e3) / 1e9,
-                "kernels": "element-blocks plan: k_elem_blocks<LinTetElem> + k_slot_gather "
-                           "(stiffness), k_elem_blocks<TetForceElem> + k_vert_gather (force)"}
+                "plan": m.plan, "tile": int(m.s.asm_tile) or 256,
+                "kernels": {"gather": "element-blocks plan: k_elem_blocks<LinTetElem> + "
+                                      "k_slot_gather (stiffness), k_elem_blocks<TetForceElem> "
+                                      "+ k_vert_gather (force)",
+                            "colored": "coloured plan: k_colored<LinTetElem>, "
+                                       "k_colored<TetForceElem> per colour",
+                            None: "row owners: k_rows<LinTetElem>, k_rows<TetForceElem>"}[m.plan]}
     if not args.no_jit:
         assembly["jit_stiffness"] = time_jit_stiffness(ctx, prob)
 
@@ -1078,6 +1100,7 @@ def run_ours(args, rank, world, local):
         "learned_vs_block_jacobi": ({"iteration_gain": bj["iters"] / max(1, iters),
                                      "time_ratio": bj["ms"] / ms} if bj else None),
         "solution_relerr_vs_fp64_oracle": parity,
+        "tuned": _tuned_summary(prob.tuned),
     }
     print(json.dumps(out), flush=True)
 

@@ -167,6 +167,9 @@ typedef struct sg_mesh {
   int32_t ncolors;
   const uint32_t *slot_src_ptr; /* device [nnzb+1] (sg_slot_sources) */
   const uint32_t *slot_src;     /* device [nE*card*card] */
+  int32_t asm_tile;             /* element tile of the element-blocks plan: threads
+                                   per CTA, 128 / 256 / 512 (0 = 256); the host
+                                   runtime's assembly tuner picks it */
 } sg_mesh;
 
 /* The inverse slot map for the element-blocks plan: for slot q, the element
@@ -406,6 +409,23 @@ typedef struct sg_matrix {
   int dtype;                 /* type of vals */
   const void *vals;
 } sg_matrix;
+
+/* SpMV autotuner: times y = A x (x of xdt) on the matrix itself with every
+ * candidate schedule sg_bspmv accepts -- the default (g = 0), every TMA
+ * variant (per-warp or CTA tiles, lanes per block row, pipeline stages; g < 0)
+ * and every streaming lane count (g = 1..32) -- reps calls each, and returns
+ * the fastest g and its time (*default_ms: the default's).  The choice is
+ * cached per (device, n, nnzb, bs, dtypes, pattern arrays); a cached choice
+ * is returned at once (*ncand = 0) unless force.  cand_g / cand_ms (cand_cap
+ * entries, optional) receive every candidate's time.  Synchronises.  Replaces
+ * the reference GPU backend's fixed 16-thread blocks
+ * (src/backend/gpu/gpu_backend.h:49-51). */
+int sg_tune_spmv(sg_ctx *ctx, const sg_matrix *A, int xdt, int reps, int force,
+                 int32_t *best_g, float *best_ms, float *default_ms, int32_t *ncand,
+                 int32_t *cand_g, float *cand_ms, int32_t cand_cap);
+/* sg_solve_opts.lanes = SG_LANES_AUTOTUNE: the solver takes its SpMV
+ * schedule from sg_tune_spmv at set-up. */
+#define SG_LANES_AUTOTUNE 1000
 
 /* Storage the iteration's SpMV reads.  SG_STORAGE_SYMMETRIC keeps the blocks
  * on and above the diagonal plus an index of the blocks below it (see

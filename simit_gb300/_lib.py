@@ -30,7 +30,7 @@ class Mesh(ctypes.Structure):
     _fields_ = [("n", I32), ("card", I32), ("nE", I64), ("endpoints", P), ("ve_ptr", P),
                 ("ve_idx", P), ("rowptr", P), ("colidx", P), ("nnzb", I64), ("maxrow", I32),
                 ("slots", P), ("color_order", P), ("color_ptr", P), ("ncolors", I32),
-                ("slot_src_ptr", P), ("slot_src", P)]
+                ("slot_src_ptr", P), ("slot_src", P), ("asm_tile", I32)]
 
 
 class Matrix(ctypes.Structure):
@@ -64,6 +64,7 @@ STOP_NORMR2, STOP_NORMR, STOP_RELATIVE = 0, 1, 2
 STATUS = {1: "converged", 2: "maxiter", 3: "breakdown", 4: "nan"}
 MODEL_LINEAR, MODEL_NEOHOOKEAN = 0, 1
 MAX_COLORS = 128
+LANES_AUTOTUNE = 1000
 
 _MP = ctypes.POINTER(Mesh)
 _CI = ctypes.c_int
@@ -82,6 +83,9 @@ SIGNATURES = {
     "sg_slots_build": (ctypes.c_int, [P, I32, P, I64, I32, P, P, P]),
     "sg_element_coloring": (ctypes.c_int, [P, ctypes.POINTER(Mesh), P, P, ctypes.POINTER(I32)]),
     "sg_slot_sources": (ctypes.c_int, [P, ctypes.POINTER(Mesh), P, P]),
+    "sg_tune_spmv": (_CI, [P, ctypes.POINTER(Matrix), _CI, _CI, _CI, ctypes.POINTER(I32),
+                           ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                           ctypes.POINTER(I32), P, P, I32]),
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),

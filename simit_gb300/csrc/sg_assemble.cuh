@@ -361,15 +361,17 @@ __global__ void __launch_bounds__(256) k_colored(AsmArgs<T> a, const uint32_t *_
 // (its incidence list, ascending element), each written once.  Each element
 // is computed once, nothing is read-modified-written, the order of every
 // sum is fixed.  Needs Elem::fin_* to be the identity.
-template <class Elem, int CARD, int BS, typename T>
-__global__ void __launch_bounds__(256) k_elem_blocks(AsmArgs<T> a, T *__restrict__ eb,
-                                                     T *__restrict__ ev) {
+// TILE threads per CTA: the element tile is TILE / TPE elements (the
+// schedule the assembly tuner picks).
+template <class Elem, int CARD, int BS, typename T, int TILE>
+__global__ void __launch_bounds__(TILE) k_elem_blocks(AsmArgs<T> a, T *__restrict__ eb,
+                                                      T *__restrict__ ev) {
   constexpr int TPE = Elem::HAS_MAT ? CARD * CARD : CARD;
-  // a CTA's 256 consecutive blocks are staged in shared memory and leave in
-  // 16-byte stores (the chunk starts 256 * BS*BS * sizeof(T) bytes apart)
-  __shared__ __align__(16) T stage[Elem::HAS_MAT ? 256 * BS * BS : 1];
+  // a CTA's TILE consecutive blocks are staged in shared memory and leave in
+  // 16-byte stores (the chunk starts TILE * BS*BS * sizeof(T) bytes apart)
+  __shared__ __align__(16) T stage[Elem::HAS_MAT ? TILE * BS * BS : 1];
   const int64_t total = a.nE * TPE;
-  for (int64_t t0 = (int64_t)blockIdx.x * 256; t0 < total; t0 += (int64_t)gridDim.x * 256) {
+  for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < total; t0 += (int64_t)gridDim.x * TILE) {
     const int64_t t = t0 + threadIdx.x;
     if (t < total) {
       const int64_t e = t / TPE;
@@ -401,15 +403,15 @@ __global__ void __launch_bounds__(256) k_elem_blocks(AsmArgs<T> a, T *__restrict
     }
     if (Elem::HAS_MAT) {
       __syncthreads();
-      const int64_t nval = (min(total, t0 + 256) - t0) * BS * BS;
+      const int64_t nval = (min(total, t0 + TILE) - t0) * BS * BS;
       T *dst = eb + t0 * BS * BS;
       constexpr int PER = 16 / sizeof(T);
-      if (nval == 256 * BS * BS && (BS * BS * 256) % PER == 0) {
+      if (nval == TILE * BS * BS && (BS * BS * TILE) % PER == 0) {
         const float4 *src4 = reinterpret_cast<const float4 *>(stage);
         float4 *dst4 = reinterpret_cast<float4 *>(dst);
-        for (int k = threadIdx.x; k < 256 * BS * BS / PER; k += 256) dst4[k] = src4[k];
+        for (int k = threadIdx.x; k < TILE * BS * BS / PER; k += TILE) dst4[k] = src4[k];
       } else {
-        for (int64_t k = threadIdx.x; k < nval; k += 256) dst[k] = stage[k];
+        for (int64_t k = threadIdx.x; k < nval; k += TILE) dst[k] = stage[k];
       }
       __syncthreads();
     }

@@ -48,7 +48,16 @@ static int launch_colored(Ctx *c, AsmArgs<T> &a, const sg_mesh *m, bool *used) {
     T *eb = s.alloc<T>(neb + 1), *ev = s.alloc<T>(nev + 1);
     if (m->nE > 0) {
       const int64_t th = m->nE * (Elem::HAS_MAT ? CARD * CARD : CARD);
-      k_elem_blocks<Elem, CARD, BS, T><<<grid_for(c, th, 256, 8), 256, 0, c->stream>>>(a, eb, ev);
+      const int tile = m->asm_tile;
+      if (tile == 128)
+        k_elem_blocks<Elem, CARD, BS, T, 128><<<grid_for(c, th, 128, 16), 128, 0, c->stream>>>(
+            a, eb, ev);
+      else if (tile == 512)
+        k_elem_blocks<Elem, CARD, BS, T, 512><<<grid_for(c, th, 512, 4), 512, 0, c->stream>>>(
+            a, eb, ev);
+      else
+        k_elem_blocks<Elem, CARD, BS, T, 256><<<grid_for(c, th, 256, 8), 256, 0, c->stream>>>(
+            a, eb, ev);
       SG_CHECK_LAUNCH();
     }
     if (Elem::HAS_MAT && m->nnzb > 0) {

@@ -744,8 +744,23 @@ int refresh_matrix(Solver *S) {
   return SG_OK;
 }
 
-int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o, Solver *S,
+int solver_init(Ctx *c, const sg_matrix *A, const sg_solve_opts *o_in, Solver *S,
                 int (*ext_setup)(Solver *)) {
+  // SG_LANES_AUTOTUNE: the SpMV schedule the tuner finds fastest on this
+  // matrix (the iteration's vectors: FP32 in mixed precision, else FP64)
+  sg_solve_opts o_tuned = *o_in;
+  const sg_solve_opts *o = &o_tuned;
+  if (o_tuned.lanes == SG_LANES_AUTOTUNE) {
+    o_tuned.lanes = 0;
+    const int xdt = o_in->precision == SG_SOLVE_MIXED ? SG_F32 : SG_F64;
+    if (!(xdt == SG_F32 && A->dtype == SG_F64)) {  // the bulk is A itself
+      int32_t g = 0;
+      float ms = 0.f;
+      SG_TRY(sg_tune_spmv(reinterpret_cast<sg_ctx *>(c), A, xdt, 10, 0, &g, &ms, nullptr,
+                          nullptr, nullptr, nullptr, 0));
+      o_tuned.lanes = g;
+    }
+  }
   S->c = c;
   ctx_retain(c);
   S->A = *A;

@@ -1,4 +1,9 @@
 // sg_bspmv: blocked SpMV entry point (y = A x) and its lanes-per-row choice.
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "sg_internal.cuh"
 #include "sg_spmv.cuh"
 #include "sg_spmv_tma.cuh"
@@ -447,4 +452,98 @@ extern "C" int sg_bspmv(sg_ctx *h, int32_t n, int32_t bs, const uint32_t *rowptr
     nnzb = *(uint32_t *)c->h_stage;
   }
   return bspmv_launch(c, n, bs, rowptr, colidx, vdt, vals, xdt, x, y, g, nnzb);
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: every lane count / TMA variant timed on the matrix itself
+// ---------------------------------------------------------------------------
+namespace sg {
+namespace {
+using TuneKey = std::tuple<int, int32_t, int64_t, int32_t, int, int, const void *, const void *>;
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int32_t, float>> g_tune_cache;
+}  // namespace
+}  // namespace sg
+
+extern "C" int sg_tune_spmv(sg_ctx *h, const sg_matrix *A, int xdt, int reps, int force,
+                            int32_t *best_g, float *best_ms, float *default_ms, int32_t *ncand,
+                            int32_t *cand_g, float *cand_ms, int32_t cand_cap) {
+  Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
+  SG_REQUIRE(c && A && A->rowptr && A->colidx && A->vals && best_g && best_ms,
+             "sg_tune_spmv: null argument");
+  SG_REQUIRE(A->n > 0 && A->bs >= 1 && A->bs <= 16, "sg_tune_spmv: bad matrix");
+  SG_REQUIRE(xdt == SG_F32 || xdt == SG_F64, "sg_tune_spmv: xdt %d", xdt);
+  if (reps < 1) reps = 10;
+  const TuneKey key{c->device, A->n, A->nnzb, A->bs, A->dtype, xdt, A->rowptr, A->colidx};
+  if (!force) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      *best_g = it->second.first;
+      *best_ms = it->second.second;
+      if (default_ms) *default_ms = -1.f;
+      if (ncand) *ncand = 0;
+      return SG_OK;
+    }
+  }
+  // candidates: the default (g = 0) first, then every TMA variant the matrix
+  // admits, then every streaming lane count
+  std::vector<int32_t> cands{0};
+  const bool aligned = ((uintptr_t)A->vals % 16 == 0) && ((uintptr_t)A->colidx % 16 == 0);
+  if ((A->bs == 3 || A->bs == 1) && aligned)
+    for (int v = 0; v < kNumTmaVariants; ++v) cands.push_back(-(v + 1));
+  for (int g : {1, 2, 4, 8, 16, 32}) cands.push_back(g);
+  const size_t xb = (size_t)A->n * A->bs * dtype_size(xdt);
+  // x and y from the context arena (contents irrelevant: zeroed)
+  Scratch s(c);
+  SG_TRY(s.reserve(Scratch::bytes_for(xb, 1) * 2 + 512));
+  unsigned char *x = s.alloc<unsigned char>(xb), *y = s.alloc<unsigned char>(xb);
+  SG_CHECK_CUDA(cudaMemsetAsync(x, 0, xb, c->stream));
+  cudaEvent_t e0, e1;
+  SG_CHECK_CUDA(cudaEventCreate(&e0));
+  SG_CHECK_CUDA(cudaEventCreate(&e1));
+  int32_t bg = 0;
+  float bms = 0.f, dms = 0.f;
+  int nc = 0;
+  int rc = SG_OK;
+  for (int32_t g : cands) {
+    rc = sg_bspmv(h, A->n, A->bs, A->rowptr, A->colidx, A->dtype, A->vals, xdt, x, y, g);
+    if (rc != SG_OK) break;
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && rc == SG_OK; ++r)
+      rc = sg_bspmv(h, A->n, A->bs, A->rowptr, A->colidx, A->dtype, A->vals, xdt, x, y, g);
+    cudaEventRecord(e1, c->stream);
+    if (rc != SG_OK) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = set_error(SG_ERR_CUDA, "sg_tune_spmv: event wait failed");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= reps;
+    if (g == 0) dms = ms;
+    if (nc == 0 || ms < bms) {
+      bms = ms;
+      bg = g;
+    }
+    if (cand_g && cand_ms && nc < cand_cap) {
+      cand_g[nc] = g;
+      cand_ms[nc] = ms;
+    }
+    ++nc;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SG_TRY(rc);
+  SG_TRY(check_device_error(c, "sg_tune_spmv"));
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = {bg, bms};
+  }
+  *best_g = bg;
+  *best_ms = bms;
+  if (default_ms) *default_ms = dms;
+  if (ncand) *ncand = nc;
+  return SG_OK;
 }

@@ -71,7 +71,8 @@ class HeteroElasticity:
 
     def __init__(self, ctx, host, dtype=torch.float32, precond=_lib.PRECOND_BLOCK_JACOBI,
                  precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None, pdl=0,
-                 plan="gather", learned_params=None, learned_exec=_lib.MPNN_EXEC_FOLDED):
+                 plan="gather", learned_params=None, learned_exec=_lib.MPNN_EXEC_FOLDED,
+                 tune=False):
         self.ctx, self.host, self.dtype = ctx, host, dtype
         # plan: the element-parallel assembly plan ("gather", "colored"; each
         # element computed once), or None for the row-owner kernels
@@ -88,8 +89,20 @@ class HeteroElasticity:
             self.f = torch.zeros(host["n"] * 3, dtype=dtype, device=d)
         self.B, self.W, _ = tet_precompute(self.mesh, self.X0, RHO, dtype=dtype)
         self.assemble()
+        # tune: the assembly plan and element tile, and the solver's SpMV
+        # schedule, from timings on this mesh and matrix
         if precision is None:
             precision = _lib.SOLVE_MIXED if dtype == torch.float32 else _lib.SOLVE_F64
+        self.tuned = None
+        if tune:
+            from .runtime import tune_spmv
+            m = self.mesh
+            self.tuned = {"assembly": m.tune_assembly(self.assemble_in_place)}
+            xdt = torch.float32 if precision == _lib.SOLVE_MIXED else torch.float64
+            # timed here (and cached); the solver's set-up takes the cached choice
+            self.tuned["spmv"] = tune_spmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx,
+                                           self.A, m.nnzb, xdt=xdt)
+            lanes = _lib.LANES_AUTOTUNE
         if storage is None:
             storage = _lib.STORAGE_FULL
         # precond PRECOND_LEARNED: the learned preconditioner with

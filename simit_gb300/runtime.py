@@ -330,6 +330,9 @@ def _host_f64(a):
     return (ctypes.c_double * len(a))(*[float(v) for v in a])
 
 
+_ASM_TUNE_CACHE = {}
+
+
 class Mesh:
     """A bound edge set + its device pattern, as the sg_mesh structure.
 
@@ -389,6 +392,69 @@ class Mesh:
              ptr(self.slot_src))
         self.s.slot_src_ptr = self.slot_src_ptr.data_ptr()
         self.s.slot_src = self.slot_src.data_ptr()
+
+    def set_asm_tile(self, tile):
+        """Element tile (threads per CTA) of the element-blocks plan."""
+        assert tile in (0, 128, 256, 512)
+        self.s.asm_tile = int(tile)
+
+    def tune_assembly(self, assemble, plans=("gather", "colored", None), tiles=(128, 256, 512),
+                      reps=3):
+        """Assembly autotuner: times `assemble()` (the caller's assembly
+        through this mesh) under every plan and, for the element-blocks plan,
+        every element tile; keeps the fastest (plans are built as needed;
+        the chosen one stays set).  The choice is cached per (n, nE, card,
+        plan set).  Returns {"plan", "tile", "ms", "default_ms", "times"}."""
+        key = (self.n, self.nE, self.card, tuple(plans), tuple(tiles))
+        if key in _ASM_TUNE_CACHE:
+            best = _ASM_TUNE_CACHE[key]
+            self._use_plan(best["plan"])
+            self.set_asm_tile(best["tile"])
+            return dict(best, cached=True)
+        times = {}
+        st = self.ctx.torch_stream
+        for plan in plans:
+            self._use_plan(plan)
+            for tile in (tiles if plan == "gather" else (0,)):
+                self.set_asm_tile(tile)
+                assemble()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                for _ in range(reps):
+                    assemble()
+                e1.record(st)
+                e1.synchronize()
+                times["%s/%d" % (plan, tile)] = e0.elapsed_time(e1) / reps
+        name = min(times, key=times.get)
+        plan, tile = name.split("/")
+        best = {"plan": None if plan == "None" else plan, "tile": int(tile), "ms": times[name],
+                "default_ms": times.get("gather/256", times.get("gather/0")), "times": times}
+        _ASM_TUNE_CACHE[key] = best
+        self._use_plan(best["plan"])
+        self.set_asm_tile(best["tile"])
+        return dict(best, cached=False)
+
+    def _use_plan(self, plan):
+        """Switch the sg_mesh to a plan (building it once)."""
+        p = self.pattern
+        self.s.slots = self.s.color_order = self.s.color_ptr = None
+        self.s.slot_src_ptr = self.s.slot_src = None
+        self.s.ncolors = 0
+        if plan == "colored":
+            if getattr(self, "color_order", None) is None:
+                self.color_plan()
+            self.s.slots = p.slots.data_ptr()
+            self.s.color_order = self.color_order.data_ptr()
+            self.s.color_ptr = ctypes.cast(self._color_ptr, ctypes.c_void_p)
+            self.s.ncolors = self.ncolors
+        elif plan == "gather":
+            if getattr(self, "slot_src", None) is None:
+                self.gather_plan()
+            self.s.slots = p.slots.data_ptr()
+            self.s.slot_src_ptr = self.slot_src_ptr.data_ptr()
+            self.s.slot_src = self.slot_src.data_ptr()
+        self.plan = plan
 
     def colors(self):
         """(color_ptr list, color_order numpy) of the plan."""
@@ -576,3 +642,24 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+def tune_spmv(ctx, n, bs, rowptr, colidx, vals, nnzb, xdt=torch.float32, reps=10, force=False):
+    """sg_tune_spmv: {"g", "ms", "default_ms", "times": {g: ms}} of the
+    fastest SpMV schedule on this matrix (cached per pattern unless force)."""
+    A = _lib.Matrix(n, bs, nnzb, rowptr.data_ptr(), colidx.data_ptr(), dtype_code(vals),
+                    vals.data_ptr())
+    g = ctypes.c_int32()
+    ms = ctypes.c_float()
+    dms = ctypes.c_float()
+    nc = ctypes.c_int32()
+    cap = 64
+    cg = (ctypes.c_int32 * cap)()
+    cms = (ctypes.c_float * cap)()
+    call("sg_tune_spmv", ctx.h, ctypes.byref(A), 1 if xdt == torch.float64 else 0, int(reps),
+         int(bool(force)), ctypes.byref(g), ctypes.byref(ms), ctypes.byref(dms),
+         ctypes.byref(nc), ctypes.cast(cg, ctypes.c_void_p), ctypes.cast(cms, ctypes.c_void_p),
+         cap)
+    times = {int(cg[k]): float(cms[k]) for k in range(min(nc.value, cap))}
+    return {"g": g.value, "ms": ms.value, "default_ms": dms.value if nc.value else None,
+            "times": times}

@@ -1,0 +1,81 @@
+"""GPU checks of the autotuners: the SpMV schedule (sg_tune_spmv: lane
+counts and TMA variants timed on the matrix) and the assembly plan and
+element tile (Mesh.tune_assembly) are never slower than the defaults on two
+mesh sizes (re-timed after tuning, 5 % for timing noise), produce the same
+results, and the solver's SG_LANES_AUTOTUNE set-up converges."""
+import numpy as np
+import pytest
+import torch
+
+from simit_gb300 import _lib, problems
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_ctx):
+    return gpu_ctx
+
+
+def _time(ctx, fn, reps=20):
+    fn()
+    st = ctx.torch_stream
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        fn()
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+@pytest.mark.parametrize("ncell", [16, 40])
+def test_tuned_spmv_not_slower_than_default(ctx, ncell):
+    from simit_gb300.runtime import bspmv, tune_spmv
+    h = problems.reorder_hetero(problems.hetero_mesh(ncell))
+    p = problems.HeteroElasticity(ctx, h, dtype=torch.float32)
+    m = p.mesh
+    t = tune_spmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, m.nnzb, force=True)
+    assert t["ms"] <= t["default_ms"] and len(t["times"]) > 10
+    with ctx.stream():
+        x = torch.rand(m.n * 3, dtype=torch.float32, device=ctx.device)
+        y0 = torch.empty_like(x)
+        y1 = torch.empty_like(x)
+
+    def run(g, y):
+        return lambda: bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, x, y, g=g)
+    td = min(_time(ctx, run(0, y0)) for _ in range(3))
+    tt = min(_time(ctx, run(t["g"], y1)) for _ in range(3))
+    print("%d^3: default %.4f ms, tuned g=%d %.4f ms" % (ncell, td, t["g"], tt))
+    assert tt <= 1.05 * td
+    ctx.sync()
+    scale = float(y0.abs().max())
+    assert float((y0 - y1).abs().max()) <= 2e-5 * scale
+    p.close()
+
+
+@pytest.mark.parametrize("ncell", [16, 40])
+def test_tuned_assembly_not_slower_than_default(ctx, ncell):
+    h = problems.reorder_hetero(problems.hetero_mesh(ncell))
+    p = problems.HeteroElasticity(ctx, h, dtype=torch.float32, tune=True)
+    a = p.tuned["assembly"]
+    assert a["ms"] <= a["default_ms"]
+    A_tuned = p.A.clone()
+    p.assemble_in_place()
+    tuned_ms = min(_time(ctx, p.assemble_in_place, 5) for _ in range(3))
+    ref = problems.HeteroElasticity(ctx, h, dtype=torch.float32, plan="gather")
+    default_ms = min(_time(ctx, ref.assemble_in_place, 5) for _ in range(3))
+    print("%d^3: assembly default %.3f ms, tuned %s/%d %.3f ms"
+          % (ncell, default_ms, a["plan"], a["tile"], tuned_ms))
+    assert tuned_ms <= 1.05 * default_ms
+    ref.assemble_in_place()
+    ctx.sync()
+    s = float(ref.A.abs().max())
+    assert float((A_tuned - ref.A).abs().max()) <= 1e-6 * s
+    # the solver took its SpMV schedule from the tuner and converges
+    r = p.step()
+    assert r.status == 1 and (r.true_normr2 / r.bnorm2) ** 0.5 <= 1e-8
+    assert p.tuned["spmv"]["g"] == p.tuned["spmv"]["g"]
+    ref.close()
+    p.close()
