@@ -287,11 +287,13 @@ class JitAssembly:
 
     def assemble(self, mesh, fields, out=None):
         """fields: up to 8 arrays; floating-point ones are passed in the
-        assembly's dtype, integer ones (constraint flags) as int32.  `out`
-        (nnzb*bs*bs values) is overwritten when given."""
+        assembly's dtype, boolean ones as one byte per value, other integer
+        ones (constraint flags) as int32.  `out` (nnzb*bs*bs values) is
+        overwritten when given."""
         with self.ctx.stream():
             fields = [_d(f, self.dtype, self.ctx.device) if _is_float(f) else
-                      _d(f, torch.int32, self.ctx.device) for f in fields]
+                      _d(f, torch.bool if _is_bool(f) else torch.int32, self.ctx.device)
+                      for f in fields]
             self._keep = fields
             arr = (ctypes.c_void_p * max(1, len(fields)))(*[f.data_ptr() for f in fields])
             vals = out if out is not None else mesh.empty(mesh.nnzb * self.bs * self.bs,
@@ -318,6 +320,12 @@ def _is_float(a):
     if isinstance(a, torch.Tensor):
         return a.is_floating_point()
     return np.asarray(a).dtype.kind == "f"
+
+
+def _is_bool(a):
+    if isinstance(a, torch.Tensor):
+        return a.dtype == torch.bool
+    return np.asarray(a).dtype.kind == "b"
 
 
 def dot(ctx, a, b):

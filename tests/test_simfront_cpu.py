@@ -1,0 +1,325 @@
+"""The `.sim` front end on the CPU: the parser over Simit programs, the
+generated element functions compiled by NVRTC for sm_103a, and the same
+generated code compiled for the host (g++, contraction off) and assembled
+in element order against the oracle's FP64 assembly.
+
+The reference's own programs (apps/fem/*.sim and the test inputs) are read
+from the reference checkout when it is present: the directory in
+SIMIT_REFERENCE, else `reference` beside the repository; those tests skip
+without it.  The programs under tests/sim were written for this repository.
+"""
+import ctypes
+import glob
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from simit_gb300 import meshgen, simfront
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SIM = os.path.join(HERE, "sim")
+REF = os.environ.get("SIMIT_REFERENCE",
+                     os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
+
+
+def _own(name):
+    with open(os.path.join(SIM, name)) as f:
+        return f.read()
+
+
+def _ref(rel):
+    p = os.path.join(REF, rel)
+    if not os.path.exists(p):
+        pytest.skip("reference checkout not found (SIMIT_REFERENCE)")
+    with open(p) as f:
+        return f.read()
+
+
+# ---------------------------------------------------------------------------
+# parser
+# ---------------------------------------------------------------------------
+def test_parser_reads_every_reference_program():
+    """Every program of the reference's apps and test inputs (outside the
+    inputs that are illegal on purpose) parses."""
+    if not os.path.isdir(os.path.join(REF, "test", "input")):
+        pytest.skip("reference checkout not found (SIMIT_REFERENCE)")
+    files = sorted(glob.glob(os.path.join(REF, "apps", "**", "*.sim"), recursive=True) +
+                   glob.glob(os.path.join(REF, "test", "input", "**", "*.sim"), recursive=True))
+    files = [f for f in files if os.sep + "illegal" + os.sep not in f]
+    assert len(files) > 100
+    failed = []
+    for p in files:
+        with open(p) as f:
+            try:
+                simfront.parse(f.read())
+            except simfront.SimError as e:
+                failed.append((os.path.relpath(p, REF), str(e)))
+    assert not failed, failed
+
+
+def test_parser_structure():
+    prog = simfront.parse(_own("tet_closed_form.sim"))
+    assert set(prog["elements"]) == {"Tet", "Vert"}
+    assert prog["elements"]["Tet"]["B"] == ("tensor", (3, 3), ("scalar", "float"), True)
+    assert prog["externs"]["tets"] == ("set", "Tet", ("verts",) * 4)
+    f = prog["funcs"]["tet_stiffness"]
+    assert [a[0] for a in f["args"]] == ["h", "rho", "e", "v"]
+    assert f["args"][3][1] == ("tuple", ((None, "Vert"),) * 4)
+    assert f["results"][0][0] == "K"
+    main = prog["funcs"]["main"]["body"][0]
+    assert main[0] == "assign" and main[2][0] == "map" and main[2][4] == "+"
+
+
+@pytest.mark.parametrize("src,msg", [
+    ("func f(e : E, v : (V*2)) -> (K : tensor[V,V](float))\n  K(v(0), v(1)) = y;\nend",
+     "unknown name"),
+    ("func f(a : float, e : E, v : (V*2)) -> (K : tensor[V,V](float))\nend", "not bound"),
+    ("func f(e : E, v : (V*2)) -> (b : tensor[V](float))\n  b(v(0)) = 1.0;\nend",
+     "no (vertex, vertex) matrix"),
+    ("func f(e : E, v : (V*2)) -> (K : tensor[V,V](tensor[3,3](float)))\n"
+     "  K(v(0), v(1)) = [1.0, 2.0];\nend", "written to a 3x3 block"),
+    ("func f(e : E, v : (V*2)) -> (K : tensor[V,V](float))\n"
+     "  x = [1.0, 2.0] * [1.0, 2.0];\nend", "product of shapes"),
+    ("func f(e : E, v : (V*2)) -> (K : tensor[V,V](float))\n  K(v(0), v(1)) = (1.0;\nend",
+     "expected )"),
+])
+def test_errors_are_reported(src, msg):
+    prog = "element E\nend\nelement V\nend\nextern Vs : set{V};\n" + src
+    with pytest.raises(simfront.SimError, match=msg.replace("(", r"\(").replace(")", r"\)")):
+        simfront.compile_map(prog, "f", {})
+
+
+# ---------------------------------------------------------------------------
+# NVRTC: the generated sources compile for sm_103a
+# ---------------------------------------------------------------------------
+def _nvrtc_check(src, card, bs, dtype, exact=True):
+    import torch
+    from simit_gb300 import _lib
+    from simit_gb300.runtime import check_element_source
+    try:
+        check_element_source(src, card, bs, dtype=dtype, exact=exact)
+    except _lib.SimitError as e:
+        if e.code == _lib.ERR_UNSUPPORTED:
+            pytest.skip("NVRTC not available: %s" % e)
+        raise
+
+
+OWN_MAPS = [("tet_closed_form.sim", "tet_stiffness", {"h": 0.01, "rho": 1e3}, None),
+            ("heat_p1.sim", "heat", {"dt": 0.01}, None),
+            ("point_mass.sim", "point_mass", {"damp": 0.5}, "M")]
+
+
+@pytest.mark.parametrize("fname,func,args,result", OWN_MAPS)
+def test_generated_sources_compile(fname, func, args, result):
+    import torch
+    r = simfront.compile_map(_own(fname), func, args, result)
+    for dt in (torch.float32, torch.float64):
+        _nvrtc_check(r["source"], r["card"], r["bs"], dt)
+
+
+REF_MAPS = [("apps/fem/fem_linear.sim", "compute_stiffness", {"h": 0.01}, None),
+            ("apps/fem/fem_neohookean.sim", "compute_stiffness", {"h": 0.01}, None),
+            ("apps/fem/fem_linear.sim", "compute_mass", {}, None),
+            ("apps/fem/poisson_2D_triangles.sim", "assemble", {}, "A"),
+            ("apps/fem/poisson_3D_tetrahedrons.sim", "assemble", {}, "A"),
+            ("apps/cloth/cloth.sim", "invMassMatrix", {}, None),
+            ("test/input/assembly/matrix_vv.sim", "f", {}, None),
+            ("test/input/assembly/edges_two_results.sim", "f", {}, "A"),
+            ("test/input/assembly/vertices_two_results.sim", "f", {}, "A")]
+
+
+@pytest.mark.parametrize("rel,func,args,result", REF_MAPS)
+def test_reference_maps_compile(rel, func, args, result):
+    import torch
+    r = simfront.compile_map(_ref(rel), func, args, result)
+    _nvrtc_check(r["source"], r["card"], r["bs"], torch.float64)
+
+
+# ---------------------------------------------------------------------------
+# host-compiled generated code against the oracle
+# ---------------------------------------------------------------------------
+HARNESS = r"""
+#include <math.h>
+#define __device__
+typedef double real;
+#define BS %(bs)d
+#define CARD %(card)d
+typedef real sg_block[BS][BS];
+#define SG_TERMS 2
+%(source)s
+// elements in order, blocks (i, j) in order, terms in order: each term a
+// separate += on its slot, as the lowered map adds them
+extern "C" void sim_assemble(long long nE, const int *ep_all, const real *const *f,
+                             const long long *slots, real *vals) {
+  for (long long e = 0; e < nE; ++e)
+    for (int i = 0; i < CARD; ++i)
+      for (int j = 0; j < CARD; ++j) {
+        sg_block blk[SG_TERMS];
+        const int nt = element_block(e, i, j, ep_all + e * CARD, f, blk);
+        real *v = vals + slots[(e * CARD + i) * CARD + j] * BS * BS;
+        for (int q = 0; q < nt; ++q)
+          for (int a = 0; a < BS; ++a)
+            for (int b = 0; b < BS; ++b) v[a * BS + b] += blk[q][a][b];
+      }
+}
+"""
+
+
+class HostMap:
+    """The generated element function compiled for the host."""
+
+    def __init__(self, info, tmp):
+        src = os.path.join(tmp, "gen.cpp")
+        so = os.path.join(tmp, "gen.so")
+        with open(src, "w") as f:
+            f.write(HARNESS % {"bs": info["bs"], "card": info["card"], "source": info["source"]})
+        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", so, src],
+                       check=True, capture_output=True)
+        self.lib = ctypes.CDLL(so)
+        self.info = info
+
+    def assemble(self, ep, slots, nnzb, fields):
+        keep = []
+        for kind, name, shape, dt in self.info["fields"]:
+            a = fields[(kind, name)] if (kind, name) in fields else fields[name]
+            a = np.ascontiguousarray(a, {"int": np.int32, "bool": np.bool_}.get(dt, np.float64))
+            keep.append(a)
+        arr = (ctypes.c_void_p * max(1, len(keep)))(*[a.ctypes.data for a in keep])
+        bs = self.info["bs"]
+        vals = np.zeros(nnzb * bs * bs)
+        ep = np.ascontiguousarray(ep, np.int32)
+        sl = np.ascontiguousarray(slots, np.int64)
+        self.lib.sim_assemble(ctypes.c_longlong(ep.size // self.info["card"]),
+                              ep.ctypes.data_as(ctypes.c_void_p), arr,
+                              sl.ctypes.data_as(ctypes.c_void_p),
+                              vals.ctypes.data_as(ctypes.c_void_p))
+        return vals
+
+
+def _tet_case(oracle, seed=3):
+    mg = meshgen.tet_grid(4, 3, 3, disp=2e-2, seed=seed)
+    tets, n = mg["tets"], mg["n"]
+    nT = len(tets) // 4
+    g = meshgen.rng(seed + 10)
+    B, W, _ = oracle.tet_precompute(mg["X0"], tets, 1e3)
+    mu = 10 ** g.uniform(3, 5, nT)
+    lam = 10 ** g.uniform(3, 5, nT)
+    c = (g.uniform(0, 1, n) < 0.15).astype(np.int32)
+    rowptr, colidx = oracle.pattern(n, tets, 4)
+    slots = oracle.slots(tets, 4, rowptr, colidx)
+    return dict(mg=mg, tets=tets, n=n, B=B, W=W, u=mu, l=lam, c=c, rowptr=rowptr,
+                colidx=colidx, slots=slots)
+
+
+@pytest.mark.parametrize("neo", [0, 1])
+def test_reference_fem_stiffness_matches_oracle(oracle, neo):
+    """The reference's compute_stiffness (apps/fem/fem_linear.sim and
+    fem_neohookean.sim), generated and compiled for the host, assembles the
+    oracle's matrix bit for bit (linear) / to rounding (neo-Hookean, whose
+    log is the host's)."""
+    rel = "apps/fem/fem_neohookean.sim" if neo else "apps/fem/fem_linear.sim"
+    info = simfront.compile_map(_ref(rel), "compute_stiffness", {"h": 0.01})
+    k = _tet_case(oracle)
+    with tempfile.TemporaryDirectory() as tmp:
+        hm = HostMap(info, tmp)
+        got = hm.assemble(k["tets"], k["slots"], len(k["colidx"]),
+                          {"B": k["B"], "W": k["W"], "u": k["u"], "l": k["l"], "c": k["c"],
+                           "x": k["mg"]["x"]})
+    want = oracle.tet_stiffness(neo, k["mg"]["x"], k["c"], k["tets"], k["B"], k["W"], k["u"],
+                                k["l"], 0.01, 1e3, k["rowptr"], k["colidx"])
+    if neo:
+        scale = np.abs(want).max()
+        assert np.abs(got - want).max() <= 1e-12 * scale
+    else:
+        assert np.array_equal(got, want)
+
+
+def test_own_closed_form_tet_matches_oracle(oracle):
+    """tests/sim/tet_closed_form.sim: the closed form of the linear element
+    agrees with the oracle's B' E B product to rounding."""
+    info = simfront.compile_map(_own("tet_closed_form.sim"), "tet_stiffness",
+                                {"h": 0.01, "rho": 1e3})
+    k = _tet_case(oracle, seed=5)
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(k["tets"], k["slots"], len(k["colidx"]), k)
+    want = oracle.tet_stiffness(0, k["mg"]["x"], k["c"], k["tets"], k["B"], k["W"], k["u"],
+                                k["l"], 0.01, 1e3, k["rowptr"], k["colidx"])
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def test_own_heat_matches_oracle(oracle):
+    """tests/sim/heat_p1.sim assembles the oracle's P1 heat matrix bit for
+    bit."""
+    info = simfront.compile_map(_own("heat_p1.sim"), "heat", {"dt": 0.01})
+    k = _tet_case(oracle, seed=7)
+    kappa = 10 ** meshgen.rng(8).uniform(-1, 1, len(k["W"]))
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(k["tets"], k["slots"], len(k["colidx"]),
+                                          {"B": k["B"], "W": k["W"], "kappa": kappa})
+    want, _ = oracle.heat_assemble(k["n"], k["tets"], k["B"], k["W"], kappa, 0.01,
+                                   np.zeros(k["n"]), k["rowptr"], k["colidx"])
+    assert np.array_equal(got, want)
+
+
+def test_point_mass_vertex_map_and_component_writes():
+    """A map over the vertices (one endpoint per element): the full block,
+    then component writes on free vertices; the vector result is left out."""
+    info = simfront.compile_map(_own("point_mass.sim"), "point_mass", {"damp": 0.5}, "M")
+    assert info["card"] == 1 and info["bs"] == 3
+    n = 7
+    m = np.linspace(1.0, 2.0, n)
+    fixed = np.array([0, 1, 0, 0, 1, 0, 0], bool)
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(np.arange(n), np.arange(n), n,
+                                          {"m": m, "fixed": fixed}).reshape(n, 3, 3)
+    want = np.zeros((n, 3, 3))
+    for p in range(n):
+        want[p] = m[p] * np.eye(3)
+        if not fixed[p]:
+            want[p, 0, 0] += 0.5 * m[p]
+            want[p, 2, 2] += (2.0 * 0.5) * m[p]
+    assert np.array_equal(got, want)
+
+
+def test_reference_poisson_triangles_matches_restatement():
+    """The reference's 2D Poisson assembly (apps/fem/poisson_2D_triangles.sim,
+    matrix A) against a numpy restatement of the same formulas."""
+    info = simfront.compile_map(_ref("apps/fem/poisson_2D_triangles.sim"), "assemble", {}, "A")
+    g = meshgen.rng(4)
+    side = 6
+    xs, ys = np.meshgrid(np.arange(side), np.arange(side), indexing="ij")
+    pts = np.stack([xs.ravel(), ys.ravel()], 1) + g.uniform(-0.2, 0.2, (side * side, 2))
+    tri = []
+    for i in range(side - 1):
+        for j in range(side - 1):
+            a, b, c, d = i * side + j, (i + 1) * side + j, i * side + j + 1, (i + 1) * side + j + 1
+            tri += [(a, b, d), (a, d, c)]
+    tri = np.array(tri, np.int32)
+    n = side * side
+    edge = np.zeros(n, bool)
+    edge[[p for p in range(n) if p // side in (0, side - 1) or p % side in (0, side - 1)]] = True
+    # dense pattern: one slot per (row, col) pair that any triangle touches
+    pairs = sorted({(int(r), int(c)) for t in tri for r in t for c in t})
+    index = {pc: k for k, pc in enumerate(pairs)}
+    slots = np.array([index[(int(t[i]), int(t[j]))] for t in tri for i in range(3)
+                      for j in range(3)], np.int64)
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(tri.ravel(), slots, len(pairs),
+                                          {"x": pts, "edge": edge})
+    want = np.zeros(len(pairs))
+    for t in tri:
+        X = np.ones((3, 3))
+        X[:, :2] = pts[t]
+        area = np.linalg.det(X)
+        abc = np.linalg.inv(X)
+        for i in range(3):
+            for j in range(3):
+                if not (edge[t[i]] or edge[t[j]]):
+                    want[index[(int(t[i]), int(t[j]))]] += \
+                        (abc[0, i] * abc[0, j] + abc[1, i] * abc[1, j]) * area
+            if edge[t[i]]:
+                want[index[(int(t[i]), int(t[i]))]] += 1.0
+    assert np.allclose(got, want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
