@@ -119,6 +119,14 @@ class Set {
     return FieldRef<T, dims...>(this, (int)fields_.size() - 1);
   }
 
+  // A field whose type is known at run time (comps values per element).
+  FieldData &add_field_raw(const std::string &name, FieldType type, int comps) {
+    FieldData f{name, type, comps, {}};
+    f.data.resize(size_ * f.comps * f.elem_size());
+    fields_.push_back(std::move(f));
+    return fields_.back();
+  }
+
   ElementRef add() {
     if (card_ != 0) throw SimitException("Set::add: edge sets take endpoints");
     return grow();
@@ -128,6 +136,19 @@ class Set {
     ElementRef r = grow();
     for (ElementRef e : {eps...}) endpoints_.push_back(e.ident);
     return r;
+  }
+
+  // An element whose card endpoints are given as an array.
+  ElementRef add_with_endpoints(const int32_t *eps) {
+    ElementRef r = grow();
+    for (int k = 0; k < card_; ++k) endpoints_.push_back(eps[k]);
+    return r;
+  }
+  // An edge set over sets that are not facade Sets (card endpoints each).
+  static std::unique_ptr<Set> edge_set(int card) {
+    std::unique_ptr<Set> s(new Set());
+    s->card_ = card;
+    return s;
   }
 
   int getSize() const { return size_; }

@@ -111,26 +111,28 @@ class Function {
   }
   bool isInitialized() const { return initialized_; }
 
-  // Copy the bound sets' fields to the device.
-  void mapArgs() {
+  // Copy the bound sets' fields to the device (the reference's unmapArgs
+  // pushes host data to the GPU: src/backend/gpu/gpu_function.cpp:181-197).
+  void unmapArgs(bool updated = true) {
+    if (!updated) return;
     for (Set *s : {V_, E_})
       for (int i = 0;; ++i) {
         FieldData *f = field_by_index(s, i);
         if (!f) break;
         check_cuda(cudaMemcpy(dev_fields_[key(s, f->name)].get(), f->data.data(), f->data.size(),
-                              cudaMemcpyHostToDevice), "mapArgs");
+                              cudaMemcpyHostToDevice), "unmapArgs");
       }
   }
-  // Copy the fields the program writes back to the host.
-  void unmapArgs(bool updated = true) {
-    if (!updated) return;
+  // Copy the fields the program writes back to the host (the reference's
+  // mapArgs pulls them: src/backend/gpu/gpu_function.cpp:174-179).
+  void mapArgs() {
     for (auto &w : written()) {
       Set *s = w.first == 0 ? V_ : E_;
       FieldData *f = s->field(w.second);
       if (!f) continue;
       check(sg_ctx_sync(ctx_), "sync");
       check_cuda(cudaMemcpy(f->data.data(), dev_fields_[key(s, f->name)].get(), f->data.size(),
-                            cudaMemcpyDeviceToHost), "unmapArgs");
+                            cudaMemcpyDeviceToHost), "mapArgs");
     }
   }
 
@@ -143,13 +145,13 @@ class Function {
     check(sg_ctx_sync(ctx_), "run");
   }
 
-  // Function::runSafe (src/function.cpp:121-129): init if needed, then
-  // map arguments, run, unmap.
+  // Function::runSafe (src/function.cpp:121-129): init if needed, push the
+  // arguments (unmapArgs), run, pull the results (mapArgs).
   void runSafe() {
     if (!initialized_) init();
-    mapArgs();
-    run();
     unmapArgs(true);
+    run();
+    mapArgs();
   }
 
   sg_solve_result lastSolve() const { return res_; }
