@@ -20,12 +20,15 @@ struct GraphH {
   // (the transposed network's pass, and the second training forward)
   GraphH *twin = nullptr;
   // folded evaluation of the symmetric form (sg_mpnn_fold.cuh): its buffers
-  // (allocated on first use), FP16 edge weights, packed L^-1
+  // (allocated on first use), the sliced-ELLPACK pattern with FP16 and FP32
+  // edge weights in slice order, packed L^-1
   int exec = SG_MPNN_EXEC_LAYERED;  // how sg_mpnn_forward evaluates (train = 0)
   bool fold_ready = false;
   FoldBufs fb{};
   float *fold = nullptr;
   __half *ah = nullptr;
+  float *af = nullptr;
+  int64_t sl_total = 0;
 };
 
 static int galloc(GraphH *G, void **p, size_t bytes) {
@@ -229,8 +232,9 @@ static int graph_refresh(GraphH *G) {
   }
   SG_CHECK_LAUNCH();
   if (G->fold_ready) {
-    const int ge = grid_for(c, g.nnzb, 256, 8);
-    k_edge_half<<<ge, 256, 0, c->stream>>>(g.nnzb, g.a, G->ah);
+    const int ge = grid_for(c, G->sl_total, 256, 8);
+    k_sell_weights<__half><<<ge, 256, 0, c->stream>>>(G->sl_total, G->fb.sl.src, g.a, G->ah);
+    k_sell_weights<float><<<ge, 256, 0, c->stream>>>(G->sl_total, G->fb.sl.src, g.a, G->af);
     k_pack_linv<<<gr, 256, 0, c->stream>>>(g.n, g.linv, (float *)G->fb.l6);
     SG_CHECK_LAUNCH();
   }
@@ -317,16 +321,50 @@ static int ensure_folded(GraphH *G) {
   Graph &g = G->g;
   SG_REQUIRE(g.sym && g.linv, "mpnn: the folded evaluation needs the symmetric form");
   const size_t n = (size_t)g.n;
+  Ctx *c = G->c;
   FoldBufs &B = G->fb;
   float *l6 = nullptr;
   SG_TRY(galloc(G, (void **)&G->fold, NPOLY * 9 * 4));
-  SG_TRY(galloc(G, (void **)&G->ah, (size_t)g.nnzb * 2));
   SG_TRY(galloc(G, (void **)&l6, n * 6 * 4));
   B.l6 = l6;
   for (float **p : {&B.xin, &B.w[0], &B.w[1]}) SG_TRY(galloc(G, (void **)p, n * 4 * 4));
-  B.rowptr = g.rowptr;
-  B.colidx = g.colidx;
   B.g = G->fold;
+  // sliced-ELLPACK copy of the pattern: rows sorted by length per window,
+  // slice sizes, their offsets, then columns and CSR sources per entry
+  const int64_t nwin = ((int64_t)g.n + SL_SIGMA - 1) / SL_SIGMA;
+  const int64_t nslice = nwin * (SL_SIGMA / SL_W);
+  SG_REQUIRE(nslice < (int64_t)1 << 30, "mpnn: %lld slices", (long long)nslice);
+  uint32_t *row = nullptr, *ptr = nullptr, *col = nullptr, *src = nullptr;
+  SG_TRY(galloc(G, (void **)&row, (size_t)nslice * SL_W * 4));
+  SG_TRY(galloc(G, (void **)&ptr, (size_t)(nslice + 1) * 4));
+  k_sell_sort<<<(unsigned)nwin, SL_SIGMA, 0, c->stream>>>(g.n, g.rowptr, row);
+  {
+    Scratch s(c);
+    SG_TRY(s.reserve(Scratch::bytes_for(nslice, 4) + scan_scratch_bytes(nslice) + 512));
+    uint32_t *cnt = s.alloc<uint32_t>(nslice);
+    k_sell_count<<<grid_for(c, nslice, 256, 8), 256, 0, c->stream>>>((int32_t)nslice, g.rowptr,
+                                                                     row, cnt);
+    SG_CHECK_LAUNCH();
+    SG_TRY(exclusive_scan_u32(c, s, cnt, ptr, nslice));
+  }
+  uint32_t total = 0;
+  SG_CHECK_CUDA(cudaMemcpyAsync(&total, ptr + nslice, 4, cudaMemcpyDeviceToHost, c->stream));
+  SG_CHECK_CUDA(cudaStreamSynchronize(c->stream));
+  SG_REQUIRE((int64_t)total >= (int64_t)g.nnzb, "mpnn: slice layout holds %u of %lld entries",
+             total, (long long)g.nnzb);
+  G->sl_total = total;
+  SG_TRY(galloc(G, (void **)&col, (size_t)total * 4));
+  SG_TRY(galloc(G, (void **)&src, (size_t)total * 4));
+  SG_TRY(galloc(G, (void **)&G->ah, (size_t)total * 2));
+  SG_TRY(galloc(G, (void **)&G->af, (size_t)total * 4));
+  k_sell_fill<<<grid_for(c, nslice * SL_W, 256, 8), 256, 0, c->stream>>>(
+      (int32_t)nslice, g.rowptr, g.colidx, row, ptr, col, src);
+  SG_CHECK_LAUNCH();
+  B.sl.nslice = (int32_t)nslice;
+  B.sl.row = row;
+  B.sl.ptr = ptr;
+  B.sl.col = col;
+  B.sl.src = src;
   G->fold_ready = true;
   return graph_refresh(G);
 }
@@ -341,12 +379,13 @@ static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate,
   Ctx *c = G->c;
   Graph &g = G->g;
   FoldBufs B = G->fb;
-  B.a = half_a ? (const void *)G->ah : (const void *)g.a;
+  B.a = half_a ? (const void *)G->ah : (const void *)G->af;
   if (!xin_ready) {
     k_lrn_xin<<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, B.g + 6 * 9, r, B.xin, B.w[0]);
     SG_CHECK_LAUNCH();
   }
-  const int gl = grid_for(c, (int64_t)g.n * 4, LG_T, 8);
+  const int gl = horner_grid(c, B.sl.nslice);
+  // the last pass leaves one dot partial per block: np of them when asked
   const int g0 = part ? np : gl;
   // w_6 in w[0]; step d reads w[(5 - d) & 1] and writes the other buffer
   for (int d = 5; d >= 1; --d) {
@@ -623,7 +662,7 @@ static int learned_setup(Solver *S) {
     S->k3_xupd = 1;
     // the last Horner step runs on the passes' full grid and leaves that
     // many partials per dot for K3
-    const int g0 = grid_for(S->c, (int64_t)S->A.n * 4, mpnn::LG_T, 8);
+    const int g0 = mpnn::horner_grid(S->c, L->G->fb.sl.nslice);
     const int np = S->P1 > S->P2 ? S->P1 : S->P2;
     if (g0 > np) {
       void *p2 = nullptr;

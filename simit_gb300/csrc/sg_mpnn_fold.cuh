@@ -21,9 +21,9 @@
 // split-bf16 activations carry the hidden layers to about 2^-16); tests
 // compare the two and the oracle's restatement.
 //
-// Layout: x and the Horner sums are [n][4] (float4 per vertex); the edge
-// weights a are FP32 or FP16 beside colidx.  A row is reduced by 4 lanes
-// (every 4th entry each, then two shuffles).
+// Layout: x and the Horner sums are [n][4] (float4 per vertex); the passes
+// read the pattern and the edge weights (FP16 by default, FP32 on request)
+// from a sliced-ELLPACK copy with one lane per row (SellGraph below).
 #pragma once
 #include <cuda_fp16.h>
 
@@ -132,13 +132,6 @@ __global__ void __launch_bounds__(256) k_fold(const float *__restrict__ prm,
   }
 }
 
-// FP16 copy of the edge weights (the folded passes' default).
-__global__ void k_edge_half(int64_t nnzb, const float *__restrict__ a, __half *__restrict__ ah) {
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnzb;
-       q += (int64_t)gridDim.x * blockDim.x)
-    ah[q] = __float2half_rn(a[q]);
-}
-
 // Packed lower-triangular L_v^-1 (l00, l10, l11, l20, l21, l22) from the
 // 9-value form k_chol_inv writes.
 __global__ void k_pack_linv(int32_t n, const float *__restrict__ linv, float *__restrict__ l6) {
@@ -155,83 +148,140 @@ __device__ __forceinline__ float ldw(const __half *a, uint32_t q) {
   return __half2float(__ldg(a + q));
 }
 
-// Weighted sum over the row [lo, hi) of sum_q a[q] src[colidx[q]][0..W) by
-// the 4 lanes of a group (sub = lane & 3 takes entries lo+sub, lo+sub+4,
-// ...); all loads of 4 entries are issued before their accumulation.  On
-// return every lane of the group holds the full sum.  SW: source row stride
-// in floats (4 for 3-wide vectors, 8 for 8-wide ones).  Every lane of the
-// warp must call it (the shuffles are warp-wide).
-template <int W, int SW, typename AT>
-__device__ __forceinline__ void row_gather(uint32_t lo, uint32_t hi, int sub,
-                                           const uint32_t *__restrict__ colidx,
-                                           const AT *__restrict__ a,
-                                           const float *__restrict__ src, float (&acc)[W]) {
-  static_assert(W == 3 || W == 8, "3- or 8-wide gathers");
-#pragma unroll
-  for (int k = 0; k < W; ++k) acc[k] = 0.f;
-  for (uint32_t qb = lo + sub; qb < hi; qb += 16) {
-    // entries past the row end reuse the first entry's column with weight 0,
-    // so all gathers are unconditional and issue back to back
-    float wq[4];
-    uint32_t u[4];
-    float4 g0[4], g1[4];
-    u[0] = __ldg(colidx + qb);
-    wq[0] = ldw(a, qb);
-#pragma unroll
-    for (int k = 1; k < 4; ++k) {
-      const uint32_t q = qb + 4 * k;
-      const bool ok = q < hi;
-      u[k] = ok ? __ldg(colidx + q) : u[0];
-      wq[k] = ok ? ldw(a, q) : 0.f;
+// ---------------------------------------------------------------------------
+// Sliced-ELLPACK copy of the pattern for the Horner passes
+// ---------------------------------------------------------------------------
+// A Horner pass gathers one 3-wide vector per edge.  With a row reduced by
+// several lanes (CSR order) one warp instruction touches the cache lines of
+// up to 32 unrelated neighbours plus 8 rows' worth of index and weight
+// segments, and the pass runs at the L1's wavefront rate, not at HBM speed.
+// The passes therefore read the pattern as SELL-32-128: rows are sorted by
+// length inside windows of SL_SIGMA rows (rows of one length stay in their
+// order), every run of 32 sorted rows is a slice that one warp processes
+// with one lane per row, and the slice's entries are stored entry-major
+// (entry k of lane l at ptr[s] + 32 k + l), so each load of indices or
+// weights is one contiguous 128 / 64 byte segment and each gather
+// instruction reads entry k of 32 rows that are close in the ordering.
+// Slices are as long as their longest row; the shorter rows are padded with
+// weight 0 and a valid column.  Built once per pattern; the weights are
+// copied into slice order at every refresh.
+constexpr int SL_W = 32;          // rows per slice: one warp, one lane each
+constexpr int SL_SIGMA = 128;     // rows per sorting window
+constexpr int SL_U = 4;           // entries per round of a Horner pass
+constexpr uint32_t SL_NONE = 0xffffffffu;
+constexpr int LG_T = 256;         // threads per CTA of the Horner passes
+constexpr int NPOLY = 7;          // polynomial degree 6
+
+struct SellGraph {
+  int32_t nslice = 0;
+  const uint32_t *row = nullptr;  // [nslice*32] row of each slice lane, SL_NONE past n
+  const uint32_t *ptr = nullptr;  // [nslice+1] first entry of each slice
+  const uint32_t *col = nullptr;  // [ptr[nslice]] column of each entry
+  const uint32_t *src = nullptr;  // [ptr[nslice]] CSR entry of each entry, SL_NONE = padding
+};
+
+// Rows of each window of SL_SIGMA sorted by decreasing length (stable).
+// One block of SL_SIGMA threads per window.
+__global__ void __launch_bounds__(SL_SIGMA) k_sell_sort(int32_t n, const uint32_t *__restrict__ rowptr,
+                                                        uint32_t *__restrict__ row) {
+  __shared__ int len[SL_SIGMA];
+  const int64_t base = (int64_t)blockIdx.x * SL_SIGMA;
+  const int i = threadIdx.x;
+  const int64_t v = base + i;
+  len[i] = v < n ? (int)(rowptr[v + 1] - rowptr[v]) : -1;
+  __syncthreads();
+  const int li = len[i];
+  int rank = 0;
+  for (int j = 0; j < SL_SIGMA; ++j) {
+    const int lj = len[j];
+    rank += (lj > li) || (lj == li && j < i);
+  }
+  row[base + rank] = v < n ? (uint32_t)v : SL_NONE;
+}
+
+// Entries of each slice: 32 x its longest row.
+__global__ void k_sell_count(int32_t nslice, const uint32_t *__restrict__ rowptr,
+                             const uint32_t *__restrict__ row, uint32_t *__restrict__ cnt) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nslice;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m = 0;
+    for (int l = 0; l < SL_W; ++l) {
+      const uint32_t v = row[s * SL_W + l];
+      if (v != SL_NONE) {
+        const uint32_t len = rowptr[v + 1] - rowptr[v];
+        m = len > m ? len : m;
+      }
     }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float4 *s4 = reinterpret_cast<const float4 *>(src + (size_t)u[k] * SW);
-      g0[k] = __ldg(s4);
-      if (W == 8) g1[k] = __ldg(s4 + 1);
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      acc[0] += wq[k] * g0[k].x;
-      acc[1] += wq[k] * g0[k].y;
-      acc[2] += wq[k] * g0[k].z;
-      if (W == 8) {
-        acc[3] += wq[k] * g0[k].w;
-        acc[4] += wq[k] * g1[k].x;
-        acc[5] += wq[k] * g1[k].y;
-        acc[6] += wq[k] * g1[k].z;
-        acc[7] += wq[k] * g1[k].w;
+    cnt[s] = m * SL_W;
+  }
+}
+
+// Columns and CSR sources of every slice entry; one thread per slice lane.
+__global__ void k_sell_fill(int32_t nslice, const uint32_t *__restrict__ rowptr,
+                            const uint32_t *__restrict__ colidx, const uint32_t *__restrict__ row,
+                            const uint32_t *__restrict__ ptr, uint32_t *__restrict__ col,
+                            uint32_t *__restrict__ src) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)nslice * SL_W;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t / SL_W;
+    const int l = (int)(t % SL_W);
+    const uint32_t v = row[t];
+    const uint32_t b = ptr[s], len = (ptr[s + 1] - b) / SL_W;
+    const uint32_t lo = v != SL_NONE ? rowptr[v] : 0u;
+    const uint32_t rl = v != SL_NONE ? rowptr[v + 1] - lo : 0u;
+    for (uint32_t k = 0; k < len; ++k) {
+      const size_t e = (size_t)b + (size_t)k * SL_W + l;
+      if (k < rl) {
+        col[e] = colidx[lo + k];
+        src[e] = lo + k;
+      } else {
+        col[e] = v != SL_NONE ? v : 0u;
+        src[e] = SL_NONE;
       }
     }
   }
-#pragma unroll
-  for (int k = 0; k < W; ++k) {
-    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 1);
-    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 2);
+}
+
+// Edge weights in slice order (FP16 for the default passes, FP32 for the
+// FP32-weight variant); padding entries get 0.
+__device__ __forceinline__ void stw(float *o, float w) { *o = w; }
+__device__ __forceinline__ void stw(__half *o, float w) { *o = __float2half_rn(w); }
+template <typename AT>
+__global__ void k_sell_weights(int64_t total, const uint32_t *__restrict__ src,
+                               const float *__restrict__ a, AT *__restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = src[e];
+    stw(out + e, q != SL_NONE ? a[q] : 0.f);
   }
+}
+
+// Blocks of a Horner pass over `nslice` slices (also the number of dot
+// partials the last pass leaves).
+inline int horner_grid(const Ctx *c, int32_t nslice) {
+  return grid_for(c, (int64_t)nslice * SL_W, LG_T, 8);
 }
 
 // Buffers of one folded application.
 struct FoldBufs {
-  const uint32_t *rowptr, *colidx;
-  const void *a;      // FP32 or FP16 edge weights
+  SellGraph sl;
+  const void *a;      // FP32 or FP16 edge weights in slice order
   const float *g;     // the 7 symmetric 3x3 coefficients G_0..G_6, row-major
   const float *l6;    // packed L^-1 [n][6]
   float *xin;         // x = L^-1 r   [n][4]
   float *w[2];        // Horner partial sums, ping-pong [n][4]
 };
 
-constexpr int LG_T = 256;  // threads per CTA of the Horner passes
-constexpr int NPOLY = 7;   // polynomial degree 6
 
-// One Horner step w_d = G_d x + Aw w_{d+1} (d = 5 .. 0).  A warp takes 8
-// consecutive rows (4 lanes each) per step; the loop condition is
-// warp-uniform so every lane reaches the shuffles.  ctl (nullable) gates on
-// the solve status (gate) and, after a fallback to block Jacobi, skips the
-// polynomial.  LAST (d = 0): z = L^-T w_0 (z = L^-T x = D^-1 r after a
-// fallback) and the dot partials of the new z when part != null: r.r at
-// part[0 .. np), r.z at part[np .. 2np), z.q at part[2np .. 3np)
-// (np = gridDim.x) when want_rr / want_zq, else r.z alone at part[0 .. np).
+// One Horner step w_d = G_d x + Aw w_{d+1} (d = 5 .. 0).  A warp takes one
+// slice (a lane per row) per step; the entry loop runs to the slice's
+// length, the same for every lane, so all lanes reach the shuffles of the
+// block sums.  ctl (nullable) gates on the solve status (gate) and, after a
+// fallback to block Jacobi, skips the polynomial.  LAST (d = 0):
+// z = L^-T w_0 (z = L^-T x = D^-1 r after a fallback) and the dot partials
+// of the new z when part != null: r.r at part[0 .. np), r.z at
+// part[np .. 2np), z.q at part[2np .. 3np) (np = gridDim.x) when want_rr /
+// want_zq, else r.z alone at part[0 .. np).
 template <typename AT, bool LAST>
 __global__ void __launch_bounds__(LG_T) k_horner(const SolveCtl *ctl, int gate, int32_t n,
                                                  FoldBufs B, int d, const float *__restrict__ src,
@@ -247,42 +297,91 @@ __global__ void __launch_bounds__(LG_T) k_horner(const SolveCtl *ctl, int gate, 
   if (fb && !LAST) return;
   if (threadIdx.x < 9) G[threadIdx.x] = B.g[d * 9 + threadIdx.x];
   __syncthreads();
-  const int lane = threadIdx.x & 31, sub = lane & 3;
+  const int lane = threadIdx.x & 31;
   const int64_t nwarp = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const AT *__restrict__ aw = (const AT *)B.a;
+  const float4 *__restrict__ s4 = reinterpret_cast<const float4 *>(src);
   DotAcc<float> rr, rz, zq;
-  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w * 8 < n;
-       w += nwarp) {
-    const int64_t v = w * 8 + (lane >> 2);
-    const bool in = v < n;
-    const uint32_t lo = (in && !fb) ? __ldg(B.rowptr + v) : 0u;
-    const uint32_t hi = (in && !fb) ? __ldg(B.rowptr + v + 1) : 0u;
-    float m[3];
-    row_gather<3, 4>(lo, hi, sub, B.colidx, (const AT *)B.a, src, m);
-    if (in && sub < 3) {
-      const float4 x4 = *reinterpret_cast<const float4 *>(B.xin + v * 4);
-      if (!LAST) {
-        dst[v * 4 + sub] = (sub == 0 ? m[0] : (sub == 1 ? m[1] : m[2])) + G[sub * 3] * x4.x +
-                           G[sub * 3 + 1] * x4.y + G[sub * 3 + 2] * x4.z;
-      } else {
-        // every lane of the group forms all of w_0 (x after a fallback)
-        float w0 = x4.x, w1 = x4.y, w2 = x4.z;
-        if (!fb) {
-          w0 = m[0] + G[0] * x4.x + G[1] * x4.y + G[2] * x4.z;
-          w1 = m[1] + G[3] * x4.x + G[4] * x4.y + G[5] * x4.z;
-          w2 = m[2] + G[6] * x4.x + G[7] * x4.y + G[8] * x4.z;
+  for (int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       s < B.sl.nslice; s += nwarp) {
+    const uint32_t v = __ldg(B.sl.row + s * SL_W + lane);
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+    if (!fb) {
+      const uint32_t b = __ldg(B.sl.ptr + s), e1 = __ldg(B.sl.ptr + s + 1);
+      const uint32_t len = (e1 - b) / SL_W;
+      const uint32_t *cp = B.sl.col + b + lane;
+      const AT *ap = aw + b + lane;
+      uint32_t k = 0;
+      // U entries per round: their index, weight and vector loads all issue
+      // before the accumulation (the last pass keeps 4: it holds more state)
+      constexpr int U = LAST ? 4 : SL_U;
+      for (; k + U <= len; k += U) {
+        uint32_t u[U];
+        float wq[U];
+        float4 g[U];
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+          u[j] = __ldg(cp + (k + j) * SL_W);
+          wq[j] = ldw(ap, (k + j) * SL_W);
         }
-        // (L^-1)^T w, L^-1 = [[l0,0,0],[l1,l2,0],[l3,l4,l5]]
-        const float *L = B.l6 + v * 6;
-        float zk;
-        if (sub == 0) zk = L[0] * w0 + L[1] * w1 + L[3] * w2;
-        else if (sub == 1) zk = L[2] * w1 + L[4] * w2;
-        else zk = L[5] * w2;
-        z[v * 3 + sub] = zk;
-        if (part) {
-          const float rk = r[v * 3 + sub];
-          if (want_rr) rr.add(rk, rk);
-          rz.add(rk, zk);
-          if (want_zq) zq.add(zk, q[v * 3 + sub]);
+#pragma unroll
+        for (int j = 0; j < U; ++j) g[j] = __ldg(s4 + u[j]);
+#pragma unroll
+        for (int j = 0; j < U; ++j) {
+          m0 += wq[j] * g[j].x;
+          m1 += wq[j] * g[j].y;
+          m2 += wq[j] * g[j].z;
+        }
+      }
+      for (; k < len; ++k) {
+        const uint32_t u = __ldg(cp + k * SL_W);
+        const float wq = ldw(ap, k * SL_W);
+        const float4 g = __ldg(s4 + u);
+        m0 += wq * g.x;
+        m1 += wq * g.y;
+        m2 += wq * g.z;
+      }
+    }
+    if (v == SL_NONE) continue;
+    const float4 x4 = *reinterpret_cast<const float4 *>(B.xin + (size_t)v * 4);
+    if (!LAST) {
+      *reinterpret_cast<float4 *>(dst + (size_t)v * 4) =
+          make_float4(m0 + G[0] * x4.x + G[1] * x4.y + G[2] * x4.z,
+                      m1 + G[3] * x4.x + G[4] * x4.y + G[5] * x4.z,
+                      m2 + G[6] * x4.x + G[7] * x4.y + G[8] * x4.z, 0.f);
+    } else {
+      float w0 = x4.x, w1 = x4.y, w2 = x4.z;
+      if (!fb) {
+        w0 = m0 + G[0] * x4.x + G[1] * x4.y + G[2] * x4.z;
+        w1 = m1 + G[3] * x4.x + G[4] * x4.y + G[5] * x4.z;
+        w2 = m2 + G[6] * x4.x + G[7] * x4.y + G[8] * x4.z;
+      }
+      // (L^-1)^T w, L^-1 = [[l0,0,0],[l1,l2,0],[l3,l4,l5]]
+      const float2 *L2 = reinterpret_cast<const float2 *>(B.l6 + (size_t)v * 6);
+      const float2 la = L2[0], lb = L2[1], lc = L2[2];
+      const float zk0 = la.x * w0 + la.y * w1 + lb.y * w2;
+      const float zk1 = lb.x * w1 + lc.x * w2;
+      const float zk2 = lc.y * w2;
+      float *zv = z + (size_t)v * 3;
+      zv[0] = zk0;
+      zv[1] = zk1;
+      zv[2] = zk2;
+      if (part) {
+        const float *rv = r + (size_t)v * 3;
+        const float r0 = rv[0], r1 = rv[1], r2 = rv[2];
+        if (want_rr) {
+          rr.add(r0, r0);
+          rr.add(r1, r1);
+          rr.add(r2, r2);
+        }
+        rz.add(r0, zk0);
+        rz.add(r1, zk1);
+        rz.add(r2, zk2);
+        if (want_zq) {
+          const float *qv = q + (size_t)v * 3;
+          zq.add(zk0, qv[0]);
+          zq.add(zk1, qv[1]);
+          zq.add(zk2, qv[2]);
         }
       }
     }
