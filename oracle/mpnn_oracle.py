@@ -224,15 +224,38 @@ def poly_coeffs(params):
     return G
 
 
-def forward_sym_poly(params, n, rowptr, colidx, vals, r, a=None):
+def bfp_round(v):
+    """Per-vertex block floating point, the storage of the GPU's FP16
+    evaluation: each row of v (n x 3) as FP16 mantissas (round to nearest
+    even) times a shared power of two that brings the row's largest |value|
+    into [0.5, 1)."""
+    v = np.asarray(v, np.float64)
+    m = np.abs(v).max(axis=1)
+    _, e = np.frexp(m)                      # m = f 2^e, f in [0.5, 1)
+    s = np.ldexp(1.0, -e)[:, None]
+    out = (v * s).astype(np.float16).astype(np.float64) / s
+    out[m == 0] = 0.0
+    return out
+
+
+def forward_sym_poly(params, n, rowptr, colidx, vals, r, a=None, bfp=False):
     """z = L^-T [sum_d Aw^d (x) G_d] L^-1 r by Horner's scheme
-    (w_6 = G_6 x, w_d = G_d x + Aw w_{d+1}, z = L^-T w_0)."""
+    (w_6 = G_6 x, w_d = G_d x + Aw w_{d+1}, z = L^-T w_0).  bfp: round x
+    and every stored w_d (d = 5..0) with bfp_round, as the GPU's FP16
+    evaluation stores them (its first step aggregates x and applies G_6
+    after the sum, Aw (G_6 x) = G_6 (Aw x))."""
     G = poly_coeffs(params)
     a0, rows, cols = edge_weights(n, rowptr, colidx, vals)
     if a is None:
         a = a0
     Li = chol_inv(n, rowptr, colidx, vals)
     x = np.einsum("vij,vj->vi", Li, np.asarray(r, np.float64).reshape(n, 3))
+    if bfp:
+        x = bfp_round(x)
+        w = bfp_round(x @ G[5].T + _agg(a, rows, cols, x, n) @ G[6].T)
+        for d in range(4, -1, -1):
+            w = bfp_round(x @ G[d].T + _agg(a, rows, cols, w, n))
+        return np.einsum("vji,vj->vi", Li, w).reshape(-1)
     w = x @ G[6].T
     for d in range(5, -1, -1):
         w = x @ G[d].T + _agg(a, rows, cols, w, n)

@@ -327,7 +327,7 @@ static int ensure_folded(GraphH *G) {
   SG_TRY(galloc(G, (void **)&G->fold, NPOLY * 9 * 4));
   SG_TRY(galloc(G, (void **)&l6, n * 6 * 4));
   B.l6 = l6;
-  for (float **p : {&B.xin, &B.w[0], &B.w[1]}) SG_TRY(galloc(G, (void **)p, n * 4 * 4));
+  for (void **p : {&B.xin, &B.w[0], &B.w[1]}) SG_TRY(galloc(G, p, n * 4 * 4));
   B.g = G->fold;
   // sliced-ELLPACK copy of the pattern: rows sorted by length per window,
   // slice sizes, their offsets, then columns and CSR sources per entry
@@ -369,10 +369,12 @@ static int ensure_folded(GraphH *G) {
   return graph_refresh(G);
 }
 
-// The folded application z = M r (symmetric form): x = L^-1 r and
-// w_6 = G_6 x (unless the iteration's K2 wrote them: xin_ready), the six
-// Horner steps, z = L^-T w_0.  part (nullable): dot partials of the last
-// step (grid np blocks); want_rr / want_zq select its slices.
+// The folded application z = M r (symmetric form): x = L^-1 r (unless the
+// iteration's K2 wrote it: xin_ready), the six Horner steps (the first one
+// gathers x and applies G_6), z = L^-T w_0.  part (nullable): dot partials of
+// the final pass (grid np blocks); want_rr / want_zq select its slices.  The
+// FP16 evaluation (half_a) stores x and the Horner sums in block floating
+// point, the FP32 one as float4.
 static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, bool half_a,
                       const float *r, float *z, const float *q, double *part, int np, int want_rr,
                       int want_zq, bool xin_ready) {
@@ -380,30 +382,36 @@ static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate,
   Graph &g = G->g;
   FoldBufs B = G->fb;
   B.a = half_a ? (const void *)G->ah : (const void *)G->af;
+  // k_lrn_finish moves r, q and z as float4
+  SG_REQUIRE(((uintptr_t)r | (uintptr_t)z | (uintptr_t)q) % 16 == 0,
+             "mpnn: r, z and q must be 16-byte aligned");
   if (!xin_ready) {
-    k_lrn_xin<<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, B.g + 6 * 9, r, B.xin, B.w[0]);
+    if (half_a)
+      k_lrn_xin<true><<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, r, B.xin);
+    else
+      k_lrn_xin<false><<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, r, B.xin);
     SG_CHECK_LAUNCH();
   }
   const int gl = horner_grid(c, B.sl.nslice);
-  // the last pass leaves one dot partial per block: np of them when asked
-  const int g0 = part ? np : gl;
-  // w_6 in w[0]; step d reads w[(5 - d) & 1] and writes the other buffer
-  for (int d = 5; d >= 1; --d) {
-    float *src = B.w[(5 - d) & 1], *dst = B.w[(6 - d) & 1];
+  // step 5 gathers x; step d < 5 reads w[(5 - d) & 1]; step d writes
+  // w[(6 - d) & 1] (w_0 in w[0])
+  for (int d = 5; d >= 0; --d) {
+    const void *src = d == 5 ? B.xin : B.w[(5 - d) & 1];
+    void *dst = B.w[(6 - d) & 1];
     if (half_a)
-      k_horner<__half, false><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, nullptr,
-                                                    nullptr, nullptr, nullptr, 0, 0);
+      k_horner<__half><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, d == 5);
     else
-      k_horner<float, false><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, nullptr,
-                                                   nullptr, nullptr, nullptr, 0, 0);
+      k_horner<float><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, d == 5);
   }
-  float *w1 = B.w[1];  // written by d = 1
+  // z = L^-T w_0 and the dots, in vertex order; one dot partial per block:
+  // np of them when asked
+  const int g0 = part ? np : gl;
   if (half_a)
-    k_horner<__half, true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B, 0, w1, nullptr, r, q, z, part,
-                                                 want_rr, want_zq);
+    k_lrn_finish<true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B.l6, B.xin, B.w[0], r, q, z, part,
+                                            want_rr, want_zq);
   else
-    k_horner<float, true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B, 0, w1, nullptr, r, q, z, part,
-                                                want_rr, want_zq);
+    k_lrn_finish<false><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B.l6, B.xin, B.w[0], r, q, z, part,
+                                             want_rr, want_zq);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
@@ -579,9 +587,14 @@ static int learned_k2(Solver *S, cudaStream_t st, int par) {
   // the TMA-staged and symmetric-storage K1 leave the p.q total in ctl
   const int pq_fin = (S->tma || S->sym) ? 1 : 0;
   const mpnn::FoldBufs &B = L->G->fb;
-  mpnn::k_lrn_update<<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->A.n, S->part1, S->P1, pq_fin,
-                                              (const float *)S->q, (float *)S->r, B.l6,
-                                              B.g + 6 * 9, B.xin, B.w[0]);
+  if (L->exec == SG_MPNN_EXEC_FOLDED)
+    mpnn::k_lrn_update<true><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->A.n, S->part1, S->P1,
+                                                      pq_fin, (const float *)S->q,
+                                                      (float *)S->r, B.l6, B.xin);
+  else
+    mpnn::k_lrn_update<false><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->A.n, S->part1, S->P1,
+                                                       pq_fin, (const float *)S->q,
+                                                       (float *)S->r, B.l6, B.xin);
   SG_CHECK_LAUNCH();
   return SG_OK;
 }

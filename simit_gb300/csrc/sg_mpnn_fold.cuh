@@ -12,10 +12,10 @@
 //
 // k_fold computes G_0..G_6 once per parameter set, in FP64, from the same
 // bf16-rounded W2h/W3h the tensor-core layers use.  One application is then
-// x = L^-1 r and w_6 = G_6 x (fused into the iteration's r update), six
-// Horner steps w_d = G_d x + Aw w_{d+1}, each a gather of a 3-wide vector
-// over the matrix pattern, and z = L^-T w_0 with the iteration's dot
-// products fused into the last step -- instead of twelve 64x64 tensor-core
+// x = L^-1 r (fused into the iteration's r update), six Horner steps
+// w_d = G_d x + Aw w_{d+1} (w_6 = G_6 x, applied after the first step's
+// gather), each a gather of a 3-wide vector over the matrix pattern, and
+// z = L^-T w_0 with the iteration's dot products fused into the last step -- instead of twelve 64x64 tensor-core
 // products per 16-vertex tile and seven gather passes of up to 8-wide
 // messages.  The operator is the one the layered kernels evaluate (their
 // split-bf16 activations carry the hidden layers to about 2^-16); tests
@@ -262,131 +262,242 @@ inline int horner_grid(const Ctx *c, int32_t nslice) {
   return grid_for(c, (int64_t)nslice * SL_W, LG_T, 8);
 }
 
-// Buffers of one folded application.
+// Vectors of the FP16 evaluation.  x and the Horner sums are stored per
+// vertex as three FP16 mantissas with a shared power-of-two exponent (block
+// floating point, 8 bytes): value = h * 2^e, the largest |h| in [0.5, 1).
+// A gather then reads 8 bytes per neighbour instead of 16, each vertex keeps
+// 11 significant bits relative to its largest component, and the shared
+// exponent (a 16-bit integer) covers any FP32 magnitude -- residuals
+// shrink by many orders during a solve, which plain FP16 would underflow.
+// Values below 2^-24 of their vertex's largest are stored as 0; a
+// non-finite value is stored as such and propagates.  The FP32 evaluation
+// keeps float4 vectors.
+__device__ __forceinline__ float pow2f(int e) {  // 2^e, e in [-126, 127]
+  return __int_as_float((127 + e) << 23);
+}
+__device__ __forceinline__ uint2 cv_encode(float a, float b, float c) {
+  const float m = fmaxf(fabsf(a), fmaxf(fabsf(b), fabsf(c)));
+  const int mb = __float_as_int(m);
+  int e = 0;
+  float s = 1.f;
+  // normal, finite m: m = f 2^e with f in [0.5, 1); keep 2^-e representable
+  if (mb >= 0x00800000 && mb < 0x7f800000) {
+    e = ((mb >> 23) & 0xff) - 126;
+    e = e < -125 ? -125 : (e > 126 ? 126 : e);
+    s = pow2f(-e);
+  } else if (mb < 0x00800000) {
+    a = b = c = 0.f;  // zero or FP32-subnormal: stored as 0
+  }
+  const __half2 ab = __floats2half2_rn(a * s, b * s);
+  const __half hc = __float2half_rn(c * s);
+  uint2 u;
+  u.x = *reinterpret_cast<const uint32_t *>(&ab);
+  u.y = (uint32_t)__half_as_ushort(hc) | ((uint32_t)(uint16_t)(int16_t)e << 16);
+  return u;
+}
+__device__ __forceinline__ void cv_decode(uint2 u, float &a, float &b, float &c) {
+  const float s = pow2f((int)(int16_t)(u.y >> 16));
+  const float2 ab = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+  a = ab.x * s;
+  b = ab.y * s;
+  c = __half2float(__ushort_as_half((unsigned short)(u.y & 0xffffu))) * s;
+}
+
+// A vertex's three values from / to a vector of the evaluation (CV: block
+// floating point, else float4).
+template <bool CV>
+__device__ __forceinline__ void ld3(const void *__restrict__ p, size_t v, float &a, float &b,
+                                    float &c) {
+  if (CV) {
+    cv_decode(__ldg(reinterpret_cast<const uint2 *>(p) + v), a, b, c);
+  } else {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(p) + v);
+    a = t.x;
+    b = t.y;
+    c = t.z;
+  }
+}
+template <bool CV>
+__device__ __forceinline__ void st3(void *__restrict__ p, size_t v, float a, float b, float c) {
+  if (CV) reinterpret_cast<uint2 *>(p)[v] = cv_encode(a, b, c);
+  else reinterpret_cast<float4 *>(p)[v] = make_float4(a, b, c, 0.f);
+}
+
+// Buffers of one folded application.  x and the Horner sums hold 16 bytes
+// per vertex: float4 in the FP32 evaluation, the first 8 in block floating
+// point in the FP16 one.
 struct FoldBufs {
   SellGraph sl;
   const void *a;      // FP32 or FP16 edge weights in slice order
   const float *g;     // the 7 symmetric 3x3 coefficients G_0..G_6, row-major
   const float *l6;    // packed L^-1 [n][6]
-  float *xin;         // x = L^-1 r   [n][4]
-  float *w[2];        // Horner partial sums, ping-pong [n][4]
+  void *xin;          // x = L^-1 r
+  void *w[2];         // Horner partial sums, ping-pong
 };
 
-
-// One Horner step w_d = G_d x + Aw w_{d+1} (d = 5 .. 0).  A warp takes one
-// slice (a lane per row) per step; the entry loop runs to the slice's
-// length, the same for every lane, so all lanes reach the shuffles of the
-// block sums.  ctl (nullable) gates on the solve status (gate) and, after a
-// fallback to block Jacobi, skips the polynomial.  LAST (d = 0):
-// z = L^-T w_0 (z = L^-T x = D^-1 r after a fallback) and the dot partials
-// of the new z when part != null: r.r at part[0 .. np), r.z at
-// part[np .. 2np), z.q at part[2np .. 3np) (np = gridDim.x) when want_rr /
-// want_zq, else r.z alone at part[0 .. np).
-template <typename AT, bool LAST>
+// One Horner step w_d = G_d x + Aw w_{d+1} (d = 5 .. 0).  The first step
+// (first != 0, d = 5) gathers x itself and applies G_6 to the sum:
+// Aw (G_6 x) = G_6 (Aw x) at every vertex, so w_6 is never stored.  A warp
+// takes one slice (a lane per row) per step and runs its entry loop to the
+// slice's length.  ctl (nullable) gates on the solve status (gate); after a
+// fallback to block Jacobi the steps do nothing (k_lrn_finish then uses x).
+// AT: edge-weight type; FP16 weights go with block-floating-point vectors.
+template <typename AT>
 __global__ void __launch_bounds__(LG_T) k_horner(const SolveCtl *ctl, int gate, int32_t n,
-                                                 FoldBufs B, int d, const float *__restrict__ src,
-                                                 float *__restrict__ dst,
-                                                 const float *__restrict__ r,
-                                                 const float *__restrict__ q,
-                                                 float *__restrict__ z, double *__restrict__ part,
-                                                 int want_rr, int want_zq) {
-  __shared__ float G[9];
-  __shared__ double sh[33];
+                                                 FoldBufs B, int d, const void *__restrict__ src,
+                                                 void *__restrict__ dst, int first) {
+  constexpr bool CV = sizeof(AT) == 2;
+  __shared__ float G[9], G6[9];
   if (ctl && gate && ctl->status != ST_RUNNING) return;
-  const bool fb = ctl && ctl->fallback;
-  if (fb && !LAST) return;
+  if (ctl && ctl->fallback) return;
   if (threadIdx.x < 9) G[threadIdx.x] = B.g[d * 9 + threadIdx.x];
+  else if (threadIdx.x < 18) G6[threadIdx.x - 9] = B.g[6 * 9 + threadIdx.x - 9];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t nwarp = (int64_t)gridDim.x * (blockDim.x >> 5);
   const AT *__restrict__ aw = (const AT *)B.a;
-  const float4 *__restrict__ s4 = reinterpret_cast<const float4 *>(src);
-  DotAcc<float> rr, rz, zq;
   for (int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
        s < B.sl.nslice; s += nwarp) {
     const uint32_t v = __ldg(B.sl.row + s * SL_W + lane);
     float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-    if (!fb) {
-      const uint32_t b = __ldg(B.sl.ptr + s), e1 = __ldg(B.sl.ptr + s + 1);
-      const uint32_t len = (e1 - b) / SL_W;
-      const uint32_t *cp = B.sl.col + b + lane;
-      const AT *ap = aw + b + lane;
-      uint32_t k = 0;
-      // U entries per round: their index, weight and vector loads all issue
-      // before the accumulation (the last pass keeps 4: it holds more state)
-      constexpr int U = LAST ? 4 : SL_U;
-      for (; k + U <= len; k += U) {
-        uint32_t u[U];
-        float wq[U];
-        float4 g[U];
+    const uint32_t b = __ldg(B.sl.ptr + s), e1 = __ldg(B.sl.ptr + s + 1);
+    const uint32_t len = (e1 - b) / SL_W;
+    const uint32_t *cp = B.sl.col + b + lane;
+    const AT *ap = aw + b + lane;
+    uint32_t k = 0;
+    // SL_U entries per round: their index, weight and vector loads all
+    // issue before the accumulation
+    for (; k + SL_U <= len; k += SL_U) {
+      uint32_t u[SL_U];
+      float wq[SL_U];
 #pragma unroll
-        for (int j = 0; j < U; ++j) {
-          u[j] = __ldg(cp + (k + j) * SL_W);
-          wq[j] = ldw(ap, (k + j) * SL_W);
-        }
-#pragma unroll
-        for (int j = 0; j < U; ++j) g[j] = __ldg(s4 + u[j]);
-#pragma unroll
-        for (int j = 0; j < U; ++j) {
-          m0 += wq[j] * g[j].x;
-          m1 += wq[j] * g[j].y;
-          m2 += wq[j] * g[j].z;
-        }
+      for (int j = 0; j < SL_U; ++j) {
+        u[j] = __ldg(cp + (k + j) * SL_W);
+        wq[j] = ldw(ap, (k + j) * SL_W);
       }
-      for (; k < len; ++k) {
-        const uint32_t u = __ldg(cp + k * SL_W);
-        const float wq = ldw(ap, k * SL_W);
-        const float4 g = __ldg(s4 + u);
-        m0 += wq * g.x;
-        m1 += wq * g.y;
-        m2 += wq * g.z;
+      float g0[SL_U], g1[SL_U], g2[SL_U];
+#pragma unroll
+      for (int j = 0; j < SL_U; ++j) ld3<CV>(src, u[j], g0[j], g1[j], g2[j]);
+#pragma unroll
+      for (int j = 0; j < SL_U; ++j) {
+        m0 += wq[j] * g0[j];
+        m1 += wq[j] * g1[j];
+        m2 += wq[j] * g2[j];
       }
+    }
+    for (; k < len; ++k) {
+      const uint32_t u = __ldg(cp + k * SL_W);
+      const float wq = ldw(ap, k * SL_W);
+      float g0, g1, g2;
+      ld3<CV>(src, u, g0, g1, g2);
+      m0 += wq * g0;
+      m1 += wq * g1;
+      m2 += wq * g2;
     }
     if (v == SL_NONE) continue;
-    const float4 x4 = *reinterpret_cast<const float4 *>(B.xin + (size_t)v * 4);
-    if (!LAST) {
-      *reinterpret_cast<float4 *>(dst + (size_t)v * 4) =
-          make_float4(m0 + G[0] * x4.x + G[1] * x4.y + G[2] * x4.z,
-                      m1 + G[3] * x4.x + G[4] * x4.y + G[5] * x4.z,
-                      m2 + G[6] * x4.x + G[7] * x4.y + G[8] * x4.z, 0.f);
+    if (first) {
+      const float t0 = m0, t1 = m1, t2 = m2;
+      m0 = G6[0] * t0 + G6[1] * t1 + G6[2] * t2;
+      m1 = G6[3] * t0 + G6[4] * t1 + G6[5] * t2;
+      m2 = G6[6] * t0 + G6[7] * t1 + G6[8] * t2;
+    }
+    float x0, x1, x2;
+    ld3<CV>(B.xin, v, x0, x1, x2);
+    st3<CV>(dst, v, m0 + G[0] * x0 + G[1] * x1 + G[2] * x2,
+            m1 + G[3] * x0 + G[4] * x1 + G[5] * x2, m2 + G[6] * x0 + G[7] * x1 + G[8] * x2);
+  }
+}
+
+// The end of an application after the last Horner step wrote w_0:
+// z = L^-T w_0 (z = L^-T x = D^-1 r after a fallback to block Jacobi) and
+// the dot partials of the new z when part != null: r.r at part[0 .. np),
+// r.z at part[np .. 2np), z.q at part[2np .. 3np) (np = gridDim.x) when
+// want_rr / want_zq, else r.z alone at part[0 .. np).  A thread takes 4
+// vertices at a time in vertex order (three float4 each of r, q and z, six
+// of L^-1: r, q and z must be 16-byte aligned); the last n % 4 vertices go
+// to thread 0 of block 0.
+template <bool CV>
+__global__ void __launch_bounds__(LG_T) k_lrn_finish(const SolveCtl *ctl, int gate, int32_t n,
+                                                     const float *__restrict__ l6,
+                                                     const void *__restrict__ xin,
+                                                     const void *__restrict__ w0,
+                                                     const float *__restrict__ r,
+                                                     const float *__restrict__ q,
+                                                     float *__restrict__ z,
+                                                     double *__restrict__ part, int want_rr,
+                                                     int want_zq) {
+  __shared__ double sh[33];
+  if (ctl && gate && ctl->status != ST_RUNNING) return;
+  const bool fb = ctl && ctl->fallback;
+  const void *w = fb ? xin : w0;
+  DotAcc<float> rr, rz, zq;
+  const int64_t nu = n / 4;
+  const float4 *l4 = reinterpret_cast<const float4 *>(l6);
+  const float4 *r4 = reinterpret_cast<const float4 *>(r);
+  const float4 *q4 = reinterpret_cast<const float4 *>(q);
+  float4 *z4 = reinterpret_cast<float4 *>(z);
+  auto one = [&](const float *L, float a, float b, float c, float *zv) {
+    // (L^-1)^T w, L^-1 = [[l0,0,0],[l1,l2,0],[l3,l4,l5]]
+    zv[0] = L[0] * a + L[1] * b + L[3] * c;
+    zv[1] = L[2] * b + L[4] * c;
+    zv[2] = L[5] * c;
+  };
+  // four vertices: L^-1 in lv[24], z into zv[12], then the dot terms
+  auto four = [&](int64_t v0, int cnt, const float *lv, bool vec) {
+    float zv[12], rv[12], qv[12];
+    for (int j = 0; j < cnt; ++j) {
+      float a, b, c;
+      ld3<CV>(w, (size_t)(v0 + j), a, b, c);
+      one(lv + 6 * j, a, b, c, zv + 3 * j);
+    }
+    if (vec) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        z4[v0 / 4 * 3 + k] = make_float4(zv[4 * k], zv[4 * k + 1], zv[4 * k + 2], zv[4 * k + 3]);
     } else {
-      float w0 = x4.x, w1 = x4.y, w2 = x4.z;
-      if (!fb) {
-        w0 = m0 + G[0] * x4.x + G[1] * x4.y + G[2] * x4.z;
-        w1 = m1 + G[3] * x4.x + G[4] * x4.y + G[5] * x4.z;
-        w2 = m2 + G[6] * x4.x + G[7] * x4.y + G[8] * x4.z;
-      }
-      // (L^-1)^T w, L^-1 = [[l0,0,0],[l1,l2,0],[l3,l4,l5]]
-      const float2 *L2 = reinterpret_cast<const float2 *>(B.l6 + (size_t)v * 6);
-      const float2 la = L2[0], lb = L2[1], lc = L2[2];
-      const float zk0 = la.x * w0 + la.y * w1 + lb.y * w2;
-      const float zk1 = lb.x * w1 + lc.x * w2;
-      const float zk2 = lc.y * w2;
-      float *zv = z + (size_t)v * 3;
-      zv[0] = zk0;
-      zv[1] = zk1;
-      zv[2] = zk2;
-      if (part) {
-        const float *rv = r + (size_t)v * 3;
-        const float r0 = rv[0], r1 = rv[1], r2 = rv[2];
-        if (want_rr) {
-          rr.add(r0, r0);
-          rr.add(r1, r1);
-          rr.add(r2, r2);
-        }
-        rz.add(r0, zk0);
-        rz.add(r1, zk1);
-        rz.add(r2, zk2);
+      for (int k = 0; k < cnt * 3; ++k) z[v0 * 3 + k] = zv[k];
+    }
+    if (!part) return;
+    if (vec) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float4 a4 = r4[v0 / 4 * 3 + k];
+        rv[4 * k] = a4.x; rv[4 * k + 1] = a4.y; rv[4 * k + 2] = a4.z; rv[4 * k + 3] = a4.w;
         if (want_zq) {
-          const float *qv = q + (size_t)v * 3;
-          zq.add(zk0, qv[0]);
-          zq.add(zk1, qv[1]);
-          zq.add(zk2, qv[2]);
+          const float4 b4 = q4[v0 / 4 * 3 + k];
+          qv[4 * k] = b4.x; qv[4 * k + 1] = b4.y; qv[4 * k + 2] = b4.z; qv[4 * k + 3] = b4.w;
         }
+      }
+    } else {
+      for (int k = 0; k < cnt * 3; ++k) {
+        rv[k] = r[v0 * 3 + k];
+        if (want_zq) qv[k] = q[v0 * 3 + k];
       }
     }
+    for (int k = 0; k < cnt * 3; ++k) {
+      if (want_rr) rr.add(rv[k], rv[k]);
+      rz.add(rv[k], zv[k]);
+      if (want_zq) zq.add(zv[k], qv[k]);
+    }
+  };
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nu;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    float lv[24];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float4 g = l4[t * 6 + k];
+      lv[4 * k] = g.x; lv[4 * k + 1] = g.y; lv[4 * k + 2] = g.z; lv[4 * k + 3] = g.w;
+    }
+    four(t * 4, 4, lv, true);
   }
-  if (!LAST || !part) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && nu * 4 < n) {
+    // the last n % 4 vertices
+    float lv[24];
+    const int cnt = (int)(n - nu * 4);
+    for (int k = 0; k < cnt * 6; ++k) lv[k] = l6[nu * 24 + k];
+    four(nu * 4, cnt, lv, false);
+  }
+  if (!part) return;
   const double t1 = block_sum(rz.value(), sh);
   const double t0 = want_rr ? block_sum(rr.value(), sh) : 0.0;
   const double t2 = want_zq ? block_sum(zq.value(), sh) : 0.0;
@@ -397,41 +508,31 @@ __global__ void __launch_bounds__(LG_T) k_horner(const SolveCtl *ctl, int gate, 
   }
 }
 
-// x = L^-1 r and w_6 = G_6 x for a fresh r (set-up, restarts and the
-// standalone forward).
-__global__ void k_lrn_xin(int32_t n, const float *__restrict__ l6, const float *__restrict__ g6,
-                          const float *__restrict__ r, float *__restrict__ xin,
-                          float *__restrict__ w6) {
-  float G[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) G[k] = __ldg(g6 + k);
+// x = L^-1 r for a fresh r (set-up, restarts and the standalone forward).
+template <bool CV>
+__global__ void k_lrn_xin(int32_t n, const float *__restrict__ l6, const float *__restrict__ r,
+                          void *__restrict__ xin) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     const float *L = l6 + v * 6;
     const float r0 = r[v * 3], r1 = r[v * 3 + 1], r2 = r[v * 3 + 2];
-    const float x0 = L[0] * r0, x1 = L[1] * r0 + L[2] * r1, x2 = L[3] * r0 + L[4] * r1 + L[5] * r2;
-    *reinterpret_cast<float4 *>(xin + v * 4) = make_float4(x0, x1, x2, 0.f);
-    *reinterpret_cast<float4 *>(w6 + v * 4) =
-        make_float4(G[0] * x0 + G[1] * x1 + G[2] * x2, G[3] * x0 + G[4] * x1 + G[5] * x2,
-                    G[6] * x0 + G[7] * x1 + G[8] * x2, 0.f);
+    st3<CV>(xin, v, L[0] * r0, L[1] * r0 + L[2] * r1, L[3] * r0 + L[4] * r1 + L[5] * r2);
   }
 }
 
-// K2 of the learned iteration: alpha = r.z / p.q; r -= alpha q; x = L^-1 r;
-// w_6 = G_6 x.  x += alpha p is left to K3 (k_cg_direction_v4 with xupd),
-// which decides the iteration from the partials the last Horner step
-// leaves.  A thread takes 4 vertices (three float4 of r and q, six of
-// L^-1, four each of x and w_6); the last n % 4 vertices go to thread 0 of
-// the last CTA.
+// K2 of the learned iteration: alpha = r.z / p.q; r -= alpha q; x = L^-1 r.
+// x += alpha p is left to K3 (k_cg_direction_v4 with xupd), which decides
+// the iteration from the partials k_lrn_finish leaves.  A thread takes 4
+// vertices (three float4 of r and q, six of L^-1, four of x); the last
+// n % 4 vertices go to thread 0 of the last CTA.
+template <bool CV>
 __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, int32_t n,
                                                       const double *__restrict__ part_in,
                                                       int np1, int pq_fin,
                                                       const float *__restrict__ q,
                                                       float *__restrict__ r,
                                                       const float *__restrict__ l6,
-                                                      const float *__restrict__ g6,
-                                                      float *__restrict__ xin,
-                                                      float *__restrict__ w6) {
+                                                      void *__restrict__ xin) {
   __shared__ double sh[33];
   if (ctl->status != ST_RUNNING) return;
   const double pq = pq_fin ? ctl->pq_tot : sum_parts(part_in, np1, sh);
@@ -442,15 +543,10 @@ __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, in
   const double alpha = ctl->rz[par] / pq;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->last_alpha = alpha;
   const float a = (float)alpha;
-  float G[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) G[k] = __ldg(g6 + k);
   const int64_t nu = n / 4;
   const float4 *q4 = reinterpret_cast<const float4 *>(q);
   float4 *r4 = reinterpret_cast<float4 *>(r);
   const float4 *l4 = reinterpret_cast<const float4 *>(l6);
-  float4 *x4 = reinterpret_cast<float4 *>(xin);
-  float4 *w4 = reinterpret_cast<float4 *>(w6);
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu;
        u += (int64_t)gridDim.x * blockDim.x) {
     float rv[12], lv[24];
@@ -473,11 +569,8 @@ __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, in
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const float *L = lv + 6 * j, *R = rv + 3 * j;
-      const float x0 = L[0] * R[0], x1 = L[1] * R[0] + L[2] * R[1],
-                  x2 = L[3] * R[0] + L[4] * R[1] + L[5] * R[2];
-      x4[u * 4 + j] = make_float4(x0, x1, x2, 0.f);
-      w4[u * 4 + j] = make_float4(G[0] * x0 + G[1] * x1 + G[2] * x2, G[3] * x0 + G[4] * x1 + G[5] * x2,
-                                  G[6] * x0 + G[7] * x1 + G[8] * x2, 0.f);
+      st3<CV>(xin, (size_t)(u * 4 + j), L[0] * R[0], L[1] * R[0] + L[2] * R[1],
+              L[3] * R[0] + L[4] * R[1] + L[5] * R[2]);
     }
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0)
@@ -488,12 +581,8 @@ __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, in
         r[v * 3 + k] = R[k];
       }
       const float *L = l6 + v * 6;
-      const float x0 = L[0] * R[0], x1 = L[1] * R[0] + L[2] * R[1],
-                  x2 = L[3] * R[0] + L[4] * R[1] + L[5] * R[2];
-      *reinterpret_cast<float4 *>(xin + v * 4) = make_float4(x0, x1, x2, 0.f);
-      *reinterpret_cast<float4 *>(w6 + v * 4) =
-          make_float4(G[0] * x0 + G[1] * x1 + G[2] * x2, G[3] * x0 + G[4] * x1 + G[5] * x2,
-                      G[6] * x0 + G[7] * x1 + G[8] * x2, 0.f);
+      st3<CV>(xin, (size_t)v, L[0] * R[0], L[1] * R[0] + L[2] * R[1],
+              L[3] * R[0] + L[4] * R[1] + L[5] * R[2]);
     }
 }
 

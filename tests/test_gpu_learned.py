@@ -118,8 +118,9 @@ def test_trained_network_gain(ctx, form):
 
 def test_folded_forward_matches_layered_and_oracle(ctx):
     """The symmetric form evaluated as its degree-6 matrix polynomial (six
-    Horner gather passes) against the oracle's restatement in FP64, with
-    FP32 and with FP16 edge weights, and against the tensor-core layered
+    Horner gather passes) against the oracle's restatement in FP64: in FP32,
+    and with FP16 edge weights and block-floating-point vectors (the oracle
+    rounding at the same points); and against the tensor-core layered
     evaluation of the same network."""
     from oracle import mpnn_oracle as mo
     from simit_gb300 import learned
@@ -143,8 +144,9 @@ def test_folded_forward_matches_layered_and_oracle(ctx):
         out[mode] = zt.cpu().numpy().astype(np.float64)
     z_ref = mo.forward_sym_poly(params, m.n, rp, ci, vals, r)
     a, _, _ = mo.edge_weights(m.n, rp, ci, vals)
+    # the FP16 evaluation: FP16 edge weights and block-floating-point vectors
     z_ref16 = mo.forward_sym_poly(params, m.n, rp, ci, vals, r,
-                                    a=a.astype(np.float16).astype(np.float64))
+                                    a=a.astype(np.float16).astype(np.float64), bfp=True)
     bj = np.einsum("vij,vj->vi", mo.block_jacobi(m.n, rp, ci, vals),
                    r.reshape(-1, 3).astype(np.float64)).reshape(-1)
     corr = np.linalg.norm(z_ref - bj)
@@ -177,10 +179,12 @@ def test_folded_solve_matches_layered_solve(ctx):
     assert abs(ff["iters"] - ll["iters"]) <= max(2, 0.03 * ll["iters"])
 
 
-def test_folded_forward_long_rows(ctx):
+@pytest.mark.parametrize("mode", [_lib.MPNN_EXEC_FOLDED, _lib.MPNN_EXEC_FOLDED_F32])
+def test_folded_forward_long_rows(ctx, mode):
     """A pattern with one row of 5000 entries (a vertex joined to every
     other one) beside rows of 2-3: the Horner passes' lanes loop over the
-    long row; the result matches the oracle's polynomial."""
+    long row; the result matches the oracle's polynomial (FP16 evaluation:
+    with the oracle rounding where the GPU stores)."""
     from oracle import mpnn_oracle as mo
     from simit_gb300 import learned
     from simit_gb300.runtime import Mesh
@@ -198,7 +202,7 @@ def test_folded_forward_long_rows(ctx):
     vals = blocks.reshape(-1).astype(np.float32)
     A = torch.tensor(vals, device=ctx.device)
     g = learned.Graph(ctx, m, A, form="sym")
-    g.set_exec(_lib.MPNN_EXEC_FOLDED)
+    g.set_exec(mode)
     params = learned.load_weights("sym")
     r = rng.normal(size=n * 3).astype(np.float32)
     pt = torch.tensor(params, device=ctx.device)
@@ -207,8 +211,10 @@ def test_folded_forward_long_rows(ctx):
     g.forward(pt, rt, zt)
     ctx.sync()
     a, _, _ = mo.edge_weights(n, rp, ci, vals.astype(np.float64))
+    half = mode == _lib.MPNN_EXEC_FOLDED
     z_ref = mo.forward_sym_poly(params, n, rp, ci, vals.astype(np.float64), r,
-                                a=a.astype(np.float16).astype(np.float64))
+                                a=a.astype(np.float16).astype(np.float64) if half else a,
+                                bfp=half)
     err = np.linalg.norm(zt.cpu().numpy() - z_ref)
     assert err <= 1e-5 * np.linalg.norm(z_ref), err
     g.close()

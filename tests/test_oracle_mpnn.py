@@ -129,3 +129,21 @@ def test_polynomial_form_equals_the_folded_operator(system, exact):
     assert np.allclose(zp, zl, rtol=1e-11, atol=1e-12 * np.abs(zl).max())
     G = mo.poly_coeffs(p)
     assert np.allclose(G, np.transpose(G, (0, 2, 1)), rtol=1e-12, atol=1e-14 * np.abs(G).max())
+
+
+def test_bfp_round_block_floating_point():
+    """The FP16 evaluation's vector storage as the oracle states it: each
+    row keeps 11 significant bits of its largest value, any magnitude."""
+    from oracle import mpnn_oracle as mo
+    rng = np.random.Generator(np.random.Philox(3))
+    v = rng.normal(size=(500, 3)) * np.exp(rng.uniform(-60, 60, size=(500, 1)))
+    v[7] = 0.0
+    v[9] = [1.0, 0.5, -0.25]          # exactly representable
+    out = mo.bfp_round(v)
+    m = np.abs(v).max(axis=1)
+    assert np.all(np.abs(out - v) <= 2.0 ** -11 * m[:, None] * (1 + 1e-12))
+    assert np.all(out[7] == 0.0) and np.array_equal(out[9], v[9])
+    # rounding is relative to the row's largest value, not to each entry
+    row = np.array([[1.0, 1e-9, 3e-4]])
+    assert mo.bfp_round(row)[0, 1] == 0.0
+    assert mo.bfp_round(row)[0, 0] == 1.0
