@@ -794,6 +794,49 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def horner_traffic(size):
+    """DRAM bytes per Horner-pass launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "horner_pass_bfp_128cube_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get("bytes_per_launch", {}).get(str(size))
+
+
+def horner_roofline(ctx, mesh, A, prm, st, reps=50):
+    """Event-timed Horner pass of the learned preconditioner (the kernel with
+    the largest share of the step: six launches per iteration) on the
+    step's own matrix: a folded FP16 graph, one forward to fill its
+    buffers, then `reps` launches of step 4.  Algorithmic bytes per pass:
+    each pattern entry's column and FP16 weight once (6 B), each vertex's
+    slice-row index (4 B), its gathered vector, its own x and the written
+    sum once each (block floating point, 8 B each)."""
+    import torch
+    from simit_gb300 import _lib
+    from simit_gb300 import learned as lrn
+    g = lrn.Graph(ctx, mesh, A, form="sym")
+    g.set_exec(_lib.MPNN_EXEC_FOLDED)
+    n3 = mesh.n * 3
+    with ctx.stream():
+        r = torch.rand(n3, dtype=torch.float32, device=ctx.device)
+        z = torch.empty_like(r)
+    g.forward(prm, r, z)
+    for _ in range(3):
+        g.fold_step(4)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        g.fold_step(4)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nbytes = mesh.nnzb * 6 + mesh.n * (4 + 8 + 8 + 8)
+    g.close()
+    return ms, nbytes
+
+
 def spmv_traffic(size, sym=False):
     """DRAM bytes per SpMV launch from a committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "spmv_sbsr3_wtma_f32_traffic.json" if sym
@@ -918,7 +961,7 @@ def run_ours(args, rank, world, local):
     h2d = (x_h.numel() + mu_h.numel() + lam_h.numel()) * 4
     d2h = u_h.numel() * 8
 
-    # --- roofline of the dominant kernel: the iteration's FP32 SpMV --------
+    # --- the iteration's FP32 SpMV, event-timed ---------------------------
     m = prob.mesh
     p = torch.rand(n3, dtype=torch.float32, device=ctx.device)
     q = torch.empty_like(p)
@@ -956,8 +999,12 @@ def run_ours(args, rank, world, local):
         else:
             full_ms = s0.elapsed_time(s1) / reps
     ctx.sync()
-    achieved = spmv_bytes / (spmv_ms / 1e3) / 1e9
+    spmv_gbs = spmv_bytes / (spmv_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
+    # --- roofline of the dominant kernel: the learned preconditioner's
+    # Horner pass (six launches per iteration, the largest share of the step)
+    horner_ms, horner_bytes = horner_roofline(ctx, m, prob.A, prm, st)
+    achieved = horner_bytes / (horner_ms / 1e3) / 1e9
 
     # --- the step's assembly alone (stiffness map in place + force map) ----
     # algorithmic bytes: element ids and parameters (B 9, W, mu, lam) once,
@@ -1084,12 +1131,18 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": spmv_traffic(args.size, sym),
-                     "kernel": kernel, "peak_kind": peak_kind,
-                     "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes,
-                     "full_storage_spmv": {"ms_per_launch": full_ms,
-                                           "algorithmic_bytes": full_bytes,
-                                           "GBps": full_bytes / (full_ms / 1e3) / 1e9}},
+                     "frac": achieved / peak, "traffic": horner_traffic(args.size),
+                     "kernel": "k_horner<__half> (one Horner step of the learned "
+                               "preconditioner: sliced-ELLPACK gather, FP16 weights, "
+                               "block-floating-point vectors; 6 launches per iteration)",
+                     "peak_kind": peak_kind, "ms_per_launch": horner_ms,
+                     "algorithmic_bytes": horner_bytes},
+        "spmv": {"kernel": kernel, "ms_per_launch": spmv_ms, "algorithmic_bytes": spmv_bytes,
+                 "GBps": spmv_gbs, "frac": spmv_gbs / peak,
+                 "traffic": spmv_traffic(args.size, sym),
+                 "full_storage_spmv": {"ms_per_launch": full_ms,
+                                       "algorithmic_bytes": full_bytes,
+                                       "GBps": full_bytes / (full_ms / 1e3) / 1e9}},
         "cpu_baseline": cpu_base,
         "clocks": clk,
         "assembly": assembly,

@@ -568,15 +568,23 @@ enum { SG_MPNN_RELU = 0, SG_MPNN_LINEAR = 1, SG_MPNN_SYM = 2 };
 int sg_mpnn_graph_set_form(sg_mpnn_graph *g, int form);
 /* How sg_mpnn_forward (train = 0) evaluates the symmetric form.  With
  * identity activations every hidden layer is a fixed linear map of the
- * inputs and messages before it, so the network folds into three small
- * matrices (8x6, 8x14, 3x22, computed in FP64 from the same bf16-rounded
- * 64x64 weights): one application of M becomes six gather passes of 3- or
- * 8-wide vectors over the pattern.  SG_MPNN_EXEC_FOLDED stores the edge
- * weights as FP16 (2 bytes a block), SG_MPNN_EXEC_FOLDED_F32 as FP32,
- * SG_MPNN_EXEC_LAYERED (the default here) runs the tensor-core layers.
- * Training always runs layered. */
+ * inputs and messages before it and commutes with the edge-weight
+ * aggregation Aw, so M = L^-T [sum_{d=0..6} Aw^d (x) G_d] L^-1 with 3x3
+ * coefficients G_d (computed in FP64 from the same bf16-rounded 64x64
+ * weights): one application is six Horner gather passes of 3-wide vectors
+ * over a sliced-ELLPACK copy of the pattern.  SG_MPNN_EXEC_FOLDED stores
+ * the edge weights as FP16 and x and the Horner sums in per-vertex block
+ * floating point (FP16 mantissas, a shared power-of-two exponent);
+ * SG_MPNN_EXEC_FOLDED_F32 keeps both in FP32; SG_MPNN_EXEC_LAYERED (the
+ * default here) runs the tensor-core layers.  Training always runs
+ * layered.  The folded evaluations need r and z 16-byte aligned. */
 enum { SG_MPNN_EXEC_FOLDED = 0, SG_MPNN_EXEC_LAYERED = 1, SG_MPNN_EXEC_FOLDED_F32 = 2 };
 int sg_mpnn_graph_set_exec(sg_mpnn_graph *g, int exec);
+/* One Horner step (d = 5 .. 0) of the folded evaluation on the graph's own
+ * buffers, as the last folded sg_mpnn_forward left them: step 5 gathers x,
+ * step d < 5 the sums step d + 1 wrote.  For timing a pass on its own; the
+ * graph's folded buffers must exist (a folded forward ran). */
+int sg_mpnn_fold_step(sg_mpnn_graph *g, int32_t d);
 int sg_mpnn_graph_destroy(sg_mpnn_graph *g);
 /* z = M(r); r, z FP32 [n*3]. */
 int sg_mpnn_forward(sg_mpnn_graph *g, const float *params, const float *r, float *z,

@@ -129,6 +129,7 @@ SIGNATURES = {
     "sg_mpnn_graph_refresh": (_CI, [P]),
     "sg_mpnn_graph_set_form": (_CI, [P, _CI]),
     "sg_mpnn_graph_set_exec": (_CI, [P, _CI]),
+    "sg_mpnn_fold_step": (_CI, [P, I32]),
     "sg_mpnn_graph_destroy": (_CI, [P]),
     "sg_mpnn_forward": (_CI, [P, P, P, P, _CI]),
     "sg_mpnn_backward": (_CI, [P, P, P, P]),

@@ -369,6 +369,43 @@ static int ensure_folded(GraphH *G) {
   return graph_refresh(G);
 }
 
+// One Horner step on a persistent grid (resident CTAs on every SM, at most
+// one warp per slice).
+static int horner_launch(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, bool half_a,
+                         const FoldBufs &B, int d, const void *src, void *dst) {
+  Ctx *c = G->c;
+  static PerDeviceOnce once;
+  static int per_sm[SG_MAX_DEVICES][2] = {};
+  const int dev = (c->device >= 0 && c->device < SG_MAX_DEVICES) ? c->device : 0;
+  SG_TRY(once_per_device(once, dev, [&]() -> int {
+    SG_CHECK_CUDA(cudaFuncSetAttribute(k_horner<__half>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ht_smem_bytes<__half>()));
+    SG_CHECK_CUDA(cudaFuncSetAttribute(k_horner<float>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ht_smem_bytes<float>()));
+    SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm[dev][0], k_horner<__half>, HT_WARPS * 32, ht_smem_bytes<__half>()));
+    SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm[dev][1], k_horner<float>, HT_WARPS * 32, ht_smem_bytes<float>()));
+    for (int k = 0; k < 2; ++k)
+      if (per_sm[dev][k] < 1) per_sm[dev][k] = 1;
+    return SG_OK;
+  }));
+  const int64_t need = ((int64_t)B.sl.nslice + HT_WARPS - 1) / HT_WARPS;
+  int64_t grid = (int64_t)c->num_sms * per_sm[dev][half_a ? 0 : 1];
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  if (half_a)
+    k_horner<__half><<<(unsigned)grid, HT_WARPS * 32, ht_smem_bytes<__half>(), st>>>(
+        ctl, gate, B, d, src, dst, d == 5, c->d_err);
+  else
+    k_horner<float><<<(unsigned)grid, HT_WARPS * 32, ht_smem_bytes<float>(), st>>>(
+        ctl, gate, B, d, src, dst, d == 5, c->d_err);
+  SG_CHECK_LAUNCH();
+  return SG_OK;
+}
+
 // The folded application z = M r (symmetric form): x = L^-1 r (unless the
 // iteration's K2 wrote it: xin_ready), the six Horner steps (the first one
 // gathers x and applies G_6), z = L^-T w_0.  part (nullable): dot partials of
@@ -392,20 +429,14 @@ static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate,
       k_lrn_xin<false><<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, r, B.xin);
     SG_CHECK_LAUNCH();
   }
-  const int gl = horner_grid(c, B.sl.nslice);
   // step 5 gathers x; step d < 5 reads w[(5 - d) & 1]; step d writes
   // w[(6 - d) & 1] (w_0 in w[0])
-  for (int d = 5; d >= 0; --d) {
-    const void *src = d == 5 ? B.xin : B.w[(5 - d) & 1];
-    void *dst = B.w[(6 - d) & 1];
-    if (half_a)
-      k_horner<__half><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, d == 5);
-    else
-      k_horner<float><<<gl, LG_T, 0, st>>>(ctl, gate, g.n, B, d, src, dst, d == 5);
-  }
+  for (int d = 5; d >= 0; --d)
+    SG_TRY(horner_launch(G, st, ctl, gate, half_a, B, d, d == 5 ? B.xin : B.w[(5 - d) & 1],
+                         B.w[(6 - d) & 1]));
   // z = L^-T w_0 and the dots, in vertex order; one dot partial per block:
   // np of them when asked
-  const int g0 = part ? np : gl;
+  const int g0 = part ? np : finish_grid(c, B.sl.nslice);
   if (half_a)
     k_lrn_finish<true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B.l6, B.xin, B.w[0], r, q, z, part,
                                             want_rr, want_zq);
@@ -675,7 +706,7 @@ static int learned_setup(Solver *S) {
     S->k3_xupd = 1;
     // the last Horner step runs on the passes' full grid and leaves that
     // many partials per dot for K3
-    const int g0 = mpnn::horner_grid(S->c, L->G->fb.sl.nslice);
+    const int g0 = mpnn::finish_grid(S->c, L->G->fb.sl.nslice);
     const int np = S->P1 > S->P2 ? S->P1 : S->P2;
     if (g0 > np) {
       void *p2 = nullptr;
@@ -765,6 +796,19 @@ int sg_mpnn_graph_set_exec(sg_mpnn_graph *hg, int exec) {
   if (exec != SG_MPNN_EXEC_LAYERED) SG_TRY(mpnn::ensure_folded(G));
   G->exec = exec;
   return SG_OK;
+}
+
+int sg_mpnn_fold_step(sg_mpnn_graph *hg, int32_t d) {
+  mpnn::GraphH *G = reinterpret_cast<mpnn::GraphH *>(hg);
+  DeviceGuard dg_(G ? G->c : nullptr);
+  SG_REQUIRE(G && d >= 0 && d <= 5, "sg_mpnn_fold_step: bad argument");
+  SG_REQUIRE(G->fold_ready && G->exec != SG_MPNN_EXEC_LAYERED,
+             "sg_mpnn_fold_step: no folded evaluation on this graph");
+  mpnn::FoldBufs B = G->fb;
+  const bool half_a = G->exec == SG_MPNN_EXEC_FOLDED;
+  B.a = half_a ? (const void *)G->ah : (const void *)G->af;
+  return mpnn::horner_launch(G, G->c->stream, nullptr, 0, half_a, B, d,
+                             d == 5 ? B.xin : B.w[(5 - d) & 1], B.w[(6 - d) & 1]);
 }
 
 int sg_mpnn_forward(sg_mpnn_graph *hg, const float *params, const float *r, float *z, int train) {

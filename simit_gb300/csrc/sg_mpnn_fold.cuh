@@ -29,6 +29,7 @@
 
 #include "sg_mpnn.cuh"
 #include "sg_solver_kernels.cuh"
+#include "sg_tma.cuh"
 
 namespace sg {
 namespace mpnn {
@@ -143,10 +144,8 @@ __global__ void k_pack_linv(int32_t n, const float *__restrict__ linv, float *__
   }
 }
 
-__device__ __forceinline__ float ldw(const float *a, uint32_t q) { return __ldg(a + q); }
-__device__ __forceinline__ float ldw(const __half *a, uint32_t q) {
-  return __half2float(__ldg(a + q));
-}
+__device__ __forceinline__ float tofloat(float w) { return w; }
+__device__ __forceinline__ float tofloat(__half w) { return __half2float(w); }
 
 // ---------------------------------------------------------------------------
 // Sliced-ELLPACK copy of the pattern for the Horner passes
@@ -167,9 +166,8 @@ __device__ __forceinline__ float ldw(const __half *a, uint32_t q) {
 // copied into slice order at every refresh.
 constexpr int SL_W = 32;          // rows per slice: one warp, one lane each
 constexpr int SL_SIGMA = 128;     // rows per sorting window
-constexpr int SL_U = 4;           // entries per round of a Horner pass
 constexpr uint32_t SL_NONE = 0xffffffffu;
-constexpr int LG_T = 256;         // threads per CTA of the Horner passes
+constexpr int LG_T = 256;         // threads per CTA of the finish kernel
 constexpr int NPOLY = 7;          // polynomial degree 6
 
 struct SellGraph {
@@ -256,9 +254,9 @@ __global__ void k_sell_weights(int64_t total, const uint32_t *__restrict__ src,
   }
 }
 
-// Blocks of a Horner pass over `nslice` slices (also the number of dot
-// partials the last pass leaves).
-inline int horner_grid(const Ctx *c, int32_t nslice) {
+// Blocks of the finish kernel of an application over `nslice` slices of
+// rows (also the number of dot partials it leaves in the solver).
+inline int finish_grid(const Ctx *c, int32_t nslice) {
   return grid_for(c, (int64_t)nslice * SL_W, LG_T, 8);
 }
 
@@ -288,18 +286,16 @@ __device__ __forceinline__ uint2 cv_encode(float a, float b, float c) {
   } else if (mb < 0x00800000) {
     a = b = c = 0.f;  // zero or FP32-subnormal: stored as 0
   }
-  const __half2 ab = __floats2half2_rn(a * s, b * s);
-  const __half hc = __float2half_rn(c * s);
   uint2 u;
-  u.x = *reinterpret_cast<const uint32_t *>(&ab);
-  u.y = (uint32_t)__half_as_ushort(hc) | ((uint32_t)(uint16_t)(int16_t)e << 16);
+  u.x = (uint32_t)__half_as_ushort(__float2half_rn(a * s)) |
+        ((uint32_t)__half_as_ushort(__float2half_rn(b * s)) << 16);
+  u.y = (uint32_t)__half_as_ushort(__float2half_rn(c * s)) | ((uint32_t)(uint16_t)(int16_t)e << 16);
   return u;
 }
 __device__ __forceinline__ void cv_decode(uint2 u, float &a, float &b, float &c) {
   const float s = pow2f((int)(int16_t)(u.y >> 16));
-  const float2 ab = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
-  a = ab.x * s;
-  b = ab.y * s;
+  a = __half2float(__ushort_as_half((unsigned short)(u.x & 0xffffu))) * s;
+  b = __half2float(__ushort_as_half((unsigned short)(u.x >> 16))) * s;
   c = __half2float(__ushort_as_half((unsigned short)(u.y & 0xffffu))) * s;
 }
 
@@ -338,62 +334,131 @@ struct FoldBufs {
 // One Horner step w_d = G_d x + Aw w_{d+1} (d = 5 .. 0).  The first step
 // (first != 0, d = 5) gathers x itself and applies G_6 to the sum:
 // Aw (G_6 x) = G_6 (Aw x) at every vertex, so w_6 is never stored.  A warp
-// takes one slice (a lane per row) per step and runs its entry loop to the
-// slice's length.  ctl (nullable) gates on the solve status (gate); after a
-// fallback to block Jacobi the steps do nothing (k_lrn_finish then uses x).
-// AT: edge-weight type; FP16 weights go with block-floating-point vectors.
+// takes one slice (a lane per row) at a time.  The slice's indices and
+// weights are staged in shared memory by bulk copies (cp.async.bulk +
+// mbarrier), HT_NST slices in flight per warp, so the gathers of one slice
+// overlap the copies of the next.  A slice's indices and weights are
+// contiguous and 128- / 64-byte aligned (slices start at multiples of 32
+// entries), so each is one copy with no tail; slices longer than HT_CAPL
+// entries per lane are read from global memory.  Every barrier wait is
+// bounded: on a timeout the warp records DEV_TMA_TIMEOUT in err, waits
+// (bounded) for its copies in flight and stops.  ctl (nullable) gates on
+// the solve status (gate); after a fallback to block Jacobi the steps do
+// nothing (k_lrn_finish then uses x).  AT: edge-weight type; FP16 weights
+// go with block-floating-point vectors.
+constexpr int HT_WARPS = 4;   // warps per CTA
+constexpr int HT_NST = 2;     // slices in flight per warp
+constexpr int HT_CAPL = 20;   // longest staged slice (entries per lane)
+
 template <typename AT>
-__global__ void __launch_bounds__(LG_T) k_horner(const SolveCtl *ctl, int gate, int32_t n,
-                                                 FoldBufs B, int d, const void *__restrict__ src,
-                                                 void *__restrict__ dst, int first) {
+__host__ __device__ constexpr size_t ht_stage_bytes() {
+  return (size_t)HT_CAPL * SL_W * (4 + sizeof(AT));
+}
+template <typename AT>
+__host__ __device__ constexpr size_t ht_smem_bytes() {
+  return (((size_t)HT_WARPS * HT_NST * 8 + 15) & ~size_t(15)) +
+         (size_t)HT_WARPS * HT_NST * ht_stage_bytes<AT>();
+}
+
+template <typename AT>
+__global__ void __launch_bounds__(HT_WARPS * 32, 1)
+    k_horner(const SolveCtl *ctl, int gate, FoldBufs B, int d,
+                 const void *__restrict__ src, void *__restrict__ dst, int first, int *err) {
   constexpr bool CV = sizeof(AT) == 2;
+  constexpr size_t CB = (size_t)HT_CAPL * SL_W * 4;
+  constexpr size_t STG = ht_stage_bytes<AT>();
+  extern __shared__ __align__(16) unsigned char sm[];
   __shared__ float G[9], G6[9];
   if (ctl && gate && ctl->status != ST_RUNNING) return;
   if (ctl && ctl->fallback) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x < 9) G[threadIdx.x] = B.g[d * 9 + threadIdx.x];
   else if (threadIdx.x < 18) G6[threadIdx.x - 9] = B.g[6 * 9 + threadIdx.x - 9];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm) + warp * HT_NST;
+  unsigned char *base =
+      sm + (((size_t)HT_WARPS * HT_NST * 8 + 15) & ~size_t(15)) + (size_t)warp * HT_NST * STG;
+  if (lane == 0) {
+    for (int b = 0; b < HT_NST; ++b) mbar_init(&bar[b], 1);
+    mbar_fence_init();
+  }
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarp = (int64_t)gridDim.x * (blockDim.x >> 5);
   const AT *__restrict__ aw = (const AT *)B.a;
-  for (int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-       s < B.sl.nslice; s += nwarp) {
-    const uint32_t v = __ldg(B.sl.row + s * SL_W + lane);
-    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-    const uint32_t b = __ldg(B.sl.ptr + s), e1 = __ldg(B.sl.ptr + s + 1);
-    const uint32_t len = (e1 - b) / SL_W;
-    const uint32_t *cp = B.sl.col + b + lane;
-    const AT *ap = aw + b + lane;
-    uint32_t k = 0;
-    // SL_U entries per round: their index, weight and vector loads all
-    // issue before the accumulation
-    for (; k + SL_U <= len; k += SL_U) {
-      uint32_t u[SL_U];
-      float wq[SL_U];
-#pragma unroll
-      for (int j = 0; j < SL_U; ++j) {
-        u[j] = __ldg(cp + (k + j) * SL_W);
-        wq[j] = ldw(ap, (k + j) * SL_W);
+  const int64_t ns = B.sl.nslice;
+  const int64_t gw = (int64_t)blockIdx.x * HT_WARPS + warp;
+  const int64_t nw = (int64_t)gridDim.x * HT_WARPS;
+  const int64_t my = gw < ns ? (ns - 1 - gw) / nw + 1 : 0;
+  // lane 0: stage slice s in buffer b (or arrive with no bytes when it is
+  // empty or longer than the buffer)
+  auto issue = [&](int64_t s, int b) {
+    const uint32_t p0 = B.sl.ptr[s], p1 = B.sl.ptr[s + 1];
+    const uint32_t len = (p1 - p0) / SL_W;
+    fence_proxy_async_smem();
+    if (len == 0 || len > (uint32_t)HT_CAPL) {
+      mbar_arrive_expect_tx(&bar[b], 0);
+      return;
+    }
+    const uint32_t cb = len * SL_W * 4, wb = len * SL_W * (uint32_t)sizeof(AT);
+    mbar_arrive_expect_tx(&bar[b], cb + wb);
+    bulk_g2s(base + (size_t)b * STG, B.sl.col + p0, cb, &bar[b]);
+    bulk_g2s(base + (size_t)b * STG + CB, aw + p0, wb, &bar[b]);
+  };
+  if (lane == 0)
+    for (int k = 0; k < HT_NST - 1 && k < my; ++k) issue(gw + k * nw, k);
+  for (int64_t k = 0; k < my; ++k) {
+    const int b = (int)(k % HT_NST);
+    const int64_t s = gw + k * nw;
+    const int64_t kn = k + HT_NST - 1;
+    if (lane == 0 && kn < my) issue(gw + kn * nw, (int)(kn % HT_NST));
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[b], (uint32_t)((k / HT_NST) & 1)));
+    if (!ok) {
+      if (lane == 0) {
+        atomicCAS(err, 0, 6 /* DEV_TMA_TIMEOUT */);
+        bool drained = true;
+        for (int64_t kk = k; kk < my && kk <= kn; ++kk)
+          drained = mbar_wait(&bar[kk % HT_NST], (uint32_t)((kk / HT_NST) & 1)) && drained;
+        if (!drained) atomicExch(err, 8 /* DEV_TMA_UNDRAINED */);
       }
-      float g0[SL_U], g1[SL_U], g2[SL_U];
+      break;
+    }
+    const uint32_t v = __ldg(B.sl.row + s * SL_W + lane);
+    const uint32_t p0 = __ldg(B.sl.ptr + s), p1 = __ldg(B.sl.ptr + s + 1);
+    const uint32_t len = (p1 - p0) / SL_W;
+    const bool staged = len <= (uint32_t)HT_CAPL;
+    const uint32_t *cp = staged ? reinterpret_cast<const uint32_t *>(base + (size_t)b * STG) + lane
+                                : B.sl.col + p0 + lane;
+    const AT *ap = staged ? reinterpret_cast<const AT *>(base + (size_t)b * STG + CB) + lane
+                          : aw + p0 + lane;
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+    uint32_t e = 0;
+    constexpr int U = 8;
+    for (; e + U <= len; e += U) {
+      uint32_t u[U];
+      float wq[U];
 #pragma unroll
-      for (int j = 0; j < SL_U; ++j) ld3<CV>(src, u[j], g0[j], g1[j], g2[j]);
+      for (int j = 0; j < U; ++j) {
+        u[j] = cp[(e + j) * SL_W];
+        wq[j] = tofloat(ap[(e + j) * SL_W]);
+      }
+      float g0[U], g1[U], g2[U];
 #pragma unroll
-      for (int j = 0; j < SL_U; ++j) {
+      for (int j = 0; j < U; ++j) ld3<CV>(src, u[j], g0[j], g1[j], g2[j]);
+#pragma unroll
+      for (int j = 0; j < U; ++j) {
         m0 += wq[j] * g0[j];
         m1 += wq[j] * g1[j];
         m2 += wq[j] * g2[j];
       }
     }
-    for (; k < len; ++k) {
-      const uint32_t u = __ldg(cp + k * SL_W);
-      const float wq = ldw(ap, k * SL_W);
+    for (; e < len; ++e) {
+      const uint32_t u = cp[e * SL_W];
+      const float wq = tofloat(ap[e * SL_W]);
       float g0, g1, g2;
       ld3<CV>(src, u, g0, g1, g2);
       m0 += wq * g0;
       m1 += wq * g1;
       m2 += wq * g2;
     }
+    __syncwarp();
     if (v == SL_NONE) continue;
     if (first) {
       const float t0 = m0, t1 = m1, t2 = m2;

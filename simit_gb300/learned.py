@@ -52,6 +52,74 @@ def load_weights(form="sym"):
     return np.load(WEIGHTS[form]).astype(np.float32)
 
 
+def _unpack(params):
+    out, o = {}, 0
+    for name, (a, b) in SHAPES:
+        out[name] = np.asarray(params[o:o + a * b], np.float64).reshape(a, b)
+        o += a * b
+    return out
+
+
+def _bf16(x):
+    """Values rounded to bfloat16 (nearest even), as the tensor-core layers
+    and the folding kernel round the 64x64 weights."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def poly_of_params(params):
+    """The symmetric form's network as a polynomial in the edge-weight
+    aggregation Aw: N = sum_{k=0..3} Aw^k (x) B_k.  Returns B (4 x 3 x 3,
+    float64) as the folding kernel forms it (bf16-rounded W2h, W3h):
+    q2 = C2 [x; m1], q3 = C3 [x; m1; m2], N x = C4 [x; m1; m2; m3] and
+    B_0 = C4x, B_1 = C4m1 + C4m2 C2x + C4m3 C3x,
+    B_2 = C4m2 C2m1 + C4m3 (C3m1 + C3m2 C2x), B_3 = C4m3 C3m2 C2m1."""
+    p = _unpack(params)
+    E1 = np.concatenate([p["W1s"], p["W1m"]], axis=1)
+    F2 = np.concatenate([_bf16(p["W2h"]) @ E1, p["W2m"]], axis=1)
+    F3 = np.concatenate([_bf16(p["W3h"]) @ F2, p["W3m"]], axis=1)
+    C2, C3, C4 = p["P2"] @ E1, p["P3"] @ F2, p["Wout"] @ F3
+    C2x, C2m1 = C2[:, 0:3], C2[:, 3:6]
+    C3x, C3m1, C3m2 = C3[:, 0:3], C3[:, 3:6], C3[:, 6:14]
+    C4x, C4m1, C4m2, C4m3 = C4[:, 0:3], C4[:, 3:6], C4[:, 6:14], C4[:, 14:22]
+    return np.stack([C4x,
+                     C4m1 + C4m2 @ C2x + C4m3 @ C3x,
+                     C4m2 @ C2m1 + C4m3 @ (C3m1 + C3m2 @ C2x),
+                     C4m3 @ C3m2 @ C2m1])
+
+
+def params_of_poly(B):
+    """Network weights (FP32[nparams]) whose polynomial is N = sum_k Aw^k (x)
+    B_k for given B (4 x 3 x 3).  The hidden layers carry their inputs and
+    messages unchanged -- h1 = [x; m1], h2 = [h1; m2], h3 = [h2; m3] through
+    0/1 weights, which bf16 holds exactly -- the message maps pass x's first
+    aggregation on (q2 = m1, q3 = m2 in their first three channels) and the
+    output layer holds the coefficients: Wout's column blocks [x | m1 | m2 |
+    m3] = [B_0 | B_1 | B_2 | B_3]."""
+    B = np.asarray(B, np.float64).reshape(4, 3, 3)
+    p = {name: np.zeros((a, b)) for name, (a, b) in SHAPES}
+    for c in range(3):
+        p["W1s"][c, c] = 1.0
+        p["W1m"][3 + c, c] = 1.0
+    for r in range(6):
+        p["W2h"][r, r] = 1.0
+    for j in range(K):
+        p["W2m"][6 + j, j] = 1.0
+    for r in range(14):
+        p["W3h"][r, r] = 1.0
+    for j in range(K):
+        p["W3m"][14 + j, j] = 1.0
+    for c in range(3):
+        p["P2"][c, 3 + c] = 1.0      # q2 = m1 (C2m1 = [I; 0], C2x = 0)
+        p["P3"][c, 6 + c] = 1.0      # q3 = m2 (C3m2 = [[I, 0], [0, 0]])
+    p["Wout"][:, 0:3] = B[0]
+    p["Wout"][:, 3:6] = B[1]
+    p["Wout"][:, 6:9] = B[2]
+    p["Wout"][:, 14:17] = B[3]
+    return np.concatenate([p[name].reshape(-1) for name, _ in SHAPES]).astype(np.float32)
+
+
 class Graph:
     """sg_mpnn_graph of a 3x3-blocked matrix."""
 
@@ -69,6 +137,11 @@ class Graph:
     def set_exec(self, mode):
         """_lib.MPNN_EXEC_*: how forward() evaluates the symmetric form."""
         call("sg_mpnn_graph_set_exec", self.h, int(mode))
+
+    def fold_step(self, d):
+        """One Horner step of the folded evaluation on the graph's own
+        buffers (sg_mpnn_fold_step; for timing a pass)."""
+        call("sg_mpnn_fold_step", self.h, d)
 
     def forward(self, params, r, z, train=False):
         call("sg_mpnn_forward", self.h, ptr(params), ptr(r), ptr(z), int(train))
@@ -235,6 +308,101 @@ def train(ctx, sizes=(16, 24, 32, 40, 48), n_pairs=2000, epochs=6, lr=1e-3, seed
         g.close()
         prob.close()
     return params, hist
+
+
+class _PcgScore:
+    """PCG iterations to tol with the symmetric form's polynomial B on one
+    seeded heterogeneous-elasticity mesh (flexible mixed PCG, folded FP16
+    evaluation) -- the quantity fit_poly minimises.  A solve that does not
+    converge within maxiters or falls back to block Jacobi scores maxiters."""
+
+    def __init__(self, ctx, ncell, seed, tol=1e-8, maxiters=20000):
+        host = problems.hetero_mesh(ncell, seed=seed)
+        self.ctx = ctx
+        self.prob = problems.HeteroElasticity(ctx, host, dtype=torch.float32,
+                                              precond=_lib.PRECOND_BLOCK_JACOBI)
+        m = self.prob.mesh
+        self.maxiters = maxiters
+        with ctx.stream():
+            self.prm = torch.zeros(nparams(), dtype=torch.float32, device=ctx.device)
+            self.x = torch.zeros_like(self.prob.b)
+        self.S = Solver(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, self.prob.A, m.nnzb,
+                        solve_opts(precision=_lib.SOLVE_MIXED, precond=_lib.PRECOND_LEARNED,
+                                   tol=tol, maxiters=maxiters, learned_params=self.prm,
+                                   learned_form=_lib.MPNN_SYM,
+                                   learned_exec=_lib.MPNN_EXEC_FOLDED),
+                        learned_params_keep=self.prm)
+
+    def __call__(self, B):
+        with self.ctx.stream():
+            self.prm.copy_(torch.from_numpy(params_of_poly(B)))
+            self.x.zero_()
+        r = self.S.solve(self.prob.b, self.x)
+        if r.status != 1 or r.fallbacks:
+            return self.maxiters
+        return r.iters
+
+    def close(self):
+        self.S.close()
+        self.prob.close()
+
+
+def fit_poly(ctx, B0=None, ncell=64, seed=321, generations=40, popsize=12, sigma=0.05,
+             rng_seed=0, log=print):
+    """Fits the symmetric form's polynomial coefficients B_0..B_3 (36
+    numbers; the network is their carrier through params_of_poly) to the
+    PCG iteration count on a seeded mesh with CMA-ES (Hansen's
+    (mu/mu_w, lambda) evolution strategy with rank-one and rank-mu updates
+    of the covariance and cumulative step-size adaptation).  B0: start
+    (default: the shipped weights' polynomial).  Returns (B, iterations,
+    history)."""
+    score = _PcgScore(ctx, ncell, seed)
+    m = (poly_of_params(load_weights("sym")) if B0 is None else np.asarray(B0)).reshape(-1)
+    n = m.size
+    lam = popsize
+    mu = lam // 2
+    w = np.log(mu + 0.5) - np.log(np.arange(1, mu + 1))
+    w /= w.sum()
+    mueff = 1.0 / np.sum(w ** 2)
+    cc = (4 + mueff / n) / (n + 4 + 2 * mueff / n)
+    cs = (mueff + 2) / (n + mueff + 5)
+    c1 = 2 / ((n + 1.3) ** 2 + mueff)
+    cmu = min(1 - c1, 2 * (mueff - 2 + 1 / mueff) / ((n + 2) ** 2 + mueff))
+    damps = 1 + 2 * max(0.0, np.sqrt((mueff - 1) / (n + 1)) - 1) + cs
+    chin = np.sqrt(n) * (1 - 1 / (4 * n) + 1 / (21 * n * n))
+    pc, ps = np.zeros(n), np.zeros(n)
+    Bm, D, C = np.eye(n), np.ones(n), np.eye(n)
+    invsqrt = np.eye(n)
+    rng = meshgen.rng(rng_seed)
+    best = (score(m.reshape(4, 3, 3)), m.copy())
+    hist = [best[0]]
+    log("start: %d iterations" % best[0])
+    for gen in range(generations):
+        z = rng.normal(size=(lam, n))
+        y = (z * D) @ Bm.T
+        xs = m + sigma * y
+        f = np.array([score(x.reshape(4, 3, 3)) for x in xs], np.float64)
+        order = np.argsort(f, kind="stable")
+        if f[order[0]] < best[0]:
+            best = (int(f[order[0]]), xs[order[0]].copy())
+        ysel = y[order[:mu]]
+        yw = w @ ysel
+        m = m + sigma * yw
+        ps = (1 - cs) * ps + np.sqrt(cs * (2 - cs) * mueff) * (invsqrt @ yw)
+        hsig = np.linalg.norm(ps) / np.sqrt(1 - (1 - cs) ** (2 * (gen + 1))) < (1.4 + 2 / (n + 1)) * chin
+        pc = (1 - cc) * pc + hsig * np.sqrt(cc * (2 - cc) * mueff) * yw
+        C = ((1 - c1 - cmu) * C + c1 * (np.outer(pc, pc) + (1 - hsig) * cc * (2 - cc) * C)
+             + cmu * (ysel.T * w) @ ysel)
+        sigma *= np.exp((cs / damps) * (np.linalg.norm(ps) / chin - 1))
+        C = (C + C.T) / 2
+        evals, Bm = np.linalg.eigh(C)
+        D = np.sqrt(np.maximum(evals, 1e-20))
+        invsqrt = Bm @ np.diag(1 / D) @ Bm.T
+        hist.append(int(f[order[0]]))
+        log("generation %d: best %d, generation best %d, median %d, sigma %.4f"
+            % (gen + 1, best[0], int(f[order[0]]), int(np.median(f)), sigma))
+    score.close()
+    return best[1].reshape(4, 3, 3), best[0], hist
 
 
 def compare(ctx, params, ncell, seed=999, tol=1e-8, form="sym", exec_mode=_lib.MPNN_EXEC_FOLDED):

@@ -147,3 +147,27 @@ def test_bfp_round_block_floating_point():
     row = np.array([[1.0, 1e-9, 3e-4]])
     assert mo.bfp_round(row)[0, 1] == 0.0
     assert mo.bfp_round(row)[0, 0] == 1.0
+
+
+def test_network_weights_of_a_polynomial():
+    """learned.params_of_poly builds network weights whose folded polynomial
+    has the given coefficients (the oracle's poly_coeffs reproduces
+    G_d = sum_{j+k=d} B'_j^T B'_k); learned.poly_of_params recovers B from
+    weights, also for the shipped ones."""
+    from oracle import mpnn_oracle as mo
+    from simit_gb300 import learned
+    rng = np.random.Generator(np.random.Philox(5))
+    B = rng.normal(0, 0.3, size=(4, 3, 3))
+    p = learned.params_of_poly(B)
+    assert p.dtype == np.float32 and p.size == mo.NPARAM
+    assert np.abs(learned.poly_of_params(p) - B).max() <= 1e-7
+    Bp = [np.eye(3) + B[0], B[1], B[2], B[3]]
+    G = np.zeros((7, 3, 3))
+    for j in range(4):
+        for k in range(4):
+            G[j + k] += Bp[j].T @ Bp[k]
+    assert np.abs(mo.poly_coeffs(p) - G).max() <= 1e-6
+    w = learned.load_weights("sym")
+    Gw = mo.poly_coeffs(w)
+    assert np.abs(mo.poly_coeffs(learned.params_of_poly(learned.poly_of_params(w))) - Gw).max() \
+        <= 1e-6 * np.abs(Gw).max()
