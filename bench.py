@@ -65,9 +65,11 @@ def parse():
     ap.add_argument("--neo", action="store_true",
                     help="neo-Hookean Newton step (64^3): FP64 vs FP32-bulk mixed precision")
     ap.add_argument("--solve-only", action="store_true",
-                    help="profiling driver: two steps of the --size system with the solver "
-                         "capped at --iters iterations")
+                    help="profiling driver: two steps of the --size system (the headline's "
+                         "method) with the solver capped at --iters iterations")
     ap.add_argument("--iters", type=int, default=64)
+    ap.add_argument("--block-jacobi", action="store_true",
+                    help="--solve-only: mixed block-Jacobi PCG instead of the learned method")
     ap.add_argument("--learned-solve", action="store_true",
                     help="profiling driver: the --size system with the learned preconditioner, "
                          "capped at --iters iterations")
@@ -394,19 +396,29 @@ def run_cloth(args, rank=0, world=1, local=0):
 
 
 def run_solve_only(args):
-    """Profiling driver: the --size heterogeneous-elasticity step (FP32
-    assembly + mixed block-Jacobi PCG) with the solver capped at --iters
-    iterations; the second step is event-timed."""
+    """Profiling driver: the --size heterogeneous-elasticity step as the
+    headline runs it (FP32 assembly with the element-blocks plan + flexible
+    mixed PCG with the learned preconditioner; --block-jacobi for mixed
+    block-Jacobi PCG) with the solver capped at --iters iterations; the
+    second step is event-timed."""
     import torch
     from simit_gb300 import _lib, problems
+    from simit_gb300 import learned as lrn
     from simit_gb300.runtime import Context
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
     h = problems.hetero_mesh(args.size)
     if not args.no_reorder:
         h = problems.reorder_hetero(h)
-    p = problems.HeteroElasticity(ctx, h, dtype=torch.float32,
-                                  precond=_lib.PRECOND_BLOCK_JACOBI, maxiters=args.iters)
+    if args.block_jacobi:
+        p = problems.HeteroElasticity(ctx, h, dtype=torch.float32,
+                                      precond=_lib.PRECOND_BLOCK_JACOBI, maxiters=args.iters)
+    else:
+        with ctx.stream():
+            prm = torch.tensor(lrn.load_weights("sym"), device=ctx.device)
+        p = problems.HeteroElasticity(ctx, h, dtype=torch.float32,
+                                      precond=_lib.PRECOND_LEARNED, learned_params=prm,
+                                      maxiters=args.iters)
     p.step()
     ms, r = _ev_ms(ctx.torch_stream, p.step)
     print(json.dumps({"size": args.size, "iters": r.iters, "status": r.status, "step_ms": ms,
