@@ -268,6 +268,21 @@ int sg_jit_assembly_create(sg_ctx *ctx, const char *element_src, int32_t card, i
 int sg_jit_assemble(sg_jit_assembly *jit, const sg_mesh *mesh, const void *const *h_fields,
                     int32_t nfields, void *vals);
 int sg_jit_assembly_destroy(sg_jit_assembly *jit);
+/* The same for a map whose result is a system vector: the source defines
+ *   __device__ int element_vector(long long e, int i, const int *ep,
+ *                                 const real *const *f, sg_vec *vec);
+ * (sg_vec = real[BS], at most SG_VTERMS = 8 terms) writing the terms
+ * element e adds to its endpoint i.  sg_jit_assemble_vector writes
+ * vals [n*bs]: each vertex adds, from zero, its incidences' terms in
+ * ascending (element, local index), each element's terms in its order (the
+ * lowered map's `+=` per write).  The handle is destroyed with
+ * sg_jit_assembly_destroy. */
+int sg_jit_check_vector_source(const char *element_src, int32_t card, int32_t bs, int dtype,
+                               int32_t exact, char *log, int64_t log_cap);
+int sg_jit_vector_create(sg_ctx *ctx, const char *element_src, int32_t card, int32_t bs,
+                         int dtype, int32_t exact, sg_jit_assembly **out);
+int sg_jit_assemble_vector(sg_jit_assembly *jit, const sg_mesh *mesh,
+                           const void *const *h_fields, int32_t nfields, void *vals);
 
 /* precomputeTetMat (femTet.sim; apps/fem/fem_linear.sim:176-193):
  * B = inv(Ds) [nE*9], W = -det(Ds)/6 [nE], vertex mass m [n] = sum of

@@ -97,6 +97,10 @@ SIGNATURES = {
     "sg_jit_check_source": (_CI, [ctypes.c_char_p, I32, I32, _CI, I32, ctypes.c_char_p, I64]),
     "sg_jit_assembly_create": (_CI, [P, ctypes.c_char_p, I32, I32, _CI, I32, ctypes.POINTER(P)]),
     "sg_jit_assemble": (_CI, [P, _MP, P, I32, P]),
+    "sg_jit_check_vector_source": (_CI, [ctypes.c_char_p, I32, I32, _CI, I32, ctypes.c_char_p,
+                                         I64]),
+    "sg_jit_vector_create": (_CI, [P, ctypes.c_char_p, I32, I32, _CI, I32, ctypes.POINTER(P)]),
+    "sg_jit_assemble_vector": (_CI, [P, _MP, P, I32, P]),
     "sg_jit_assembly_destroy": (_CI, [P]),
     "sg_bsr_add_diag": (_CI, [P, I32, I32, P, P, I64, _CI, P, D, D, P, P]),
     "sg_symbsr_create": (_CI, [P, I32, P, P, I64, I32, ctypes.POINTER(P)]),

@@ -180,9 +180,46 @@ sg_jit_rows(int n, const unsigned *__restrict__ ve_ptr, const unsigned *__restri
 }
 )";
 
+// The generated kernel around a vector element function (the result of a
+// `map f to E reduce +` that is a system vector):
+//   __device__ int element_vector(long long e, int i, const int *ep,
+//                                 const real *const *f, sg_vec *vec);
+// writes the terms element e adds to its endpoint i (sg_vec = real[BS], at
+// most SG_VTERMS) and returns their count.  A thread owns a vertex and adds,
+// from zero, its incidences' terms in ascending (element, local index),
+// each element's terms in the order it returns them -- the lowered map's
+// order, in which each write `f(v(i)) = x` is one `+=` on the vertex.
+const char *kJitVecKernel = R"(
+struct SgFields { const real *p[8]; };
+extern "C" __global__ void __launch_bounds__(128)
+sg_jit_vec(int n, const unsigned *__restrict__ ve_ptr, const unsigned *__restrict__ ve_idx,
+           const int *__restrict__ ep_all, SgFields f, real *__restrict__ vals) {
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    real acc[BS];
+    for (int a = 0; a < BS; ++a) acc[a] = real(0);
+    const unsigned iend = ve_ptr[v + 1];
+    for (unsigned it = ve_ptr[v]; it < iend; ++it) {
+      const unsigned t = ve_idx[it];
+      const long long e = t / CARD;
+      const int i = (int)(t - (unsigned)e * CARD);
+      sg_vec terms[SG_VTERMS];
+      for (int q = 0; q < SG_VTERMS; ++q)
+        for (int a = 0; a < BS; ++a) terms[q][a] = real(0);
+      int nt = element_vector(e, i, ep_all + e * CARD, f.p, terms);
+      nt = nt < 0 ? 0 : (nt > SG_VTERMS ? SG_VTERMS : nt);
+      for (int q = 0; q < nt; ++q)
+        for (int a = 0; a < BS; ++a) acc[a] += terms[q][a];
+    }
+    for (int a = 0; a < BS; ++a) vals[(size_t)v * BS + a] = acc[a];
+  }
+}
+)";
+
 struct JitAssembly {
   Ctx *c = nullptr;
   int card = 0, bs = 0, dtype = 0;
+  bool vec = false;
   cudaLibrary_t lib = nullptr;
   cudaKernel_t kernel = nullptr;
 };
@@ -201,7 +238,7 @@ namespace {
 // Compiles the generated source; on success `image` holds the CUBIN, on a
 // compile error `log` the compiler's log and the result is SG_ERR_ARG.
 int jit_compile(const char *element_src, int32_t card, int32_t bs, int dtype, int32_t exact,
-                std::vector<char> &image, std::string &log) {
+                std::vector<char> &image, std::string &log, bool vec = false) {
   SG_REQUIRE(element_src, "sg_jit: null source");
   SG_REQUIRE(card >= 1 && card <= 32 && bs >= 1 && bs <= 5,
              "sg_jit: card %d bs %d (card 1..32, bs 1..5)", card, bs);
@@ -210,8 +247,9 @@ int jit_compile(const char *element_src, int32_t card, int32_t bs, int dtype, in
   if (!N.ok) return set_error(SG_ERR_UNSUPPORTED, "sg_jit: NVRTC not found");
   std::string src = "#define SG_REAL " + std::string(dtype == SG_F64 ? "double" : "float") +
                     "\n#define BS " + std::to_string(bs) + "\n#define CARD " +
-                    std::to_string(card) + "\n" + kJitPrologue + "\n" + element_src + "\n" +
-                    kJitKernel;
+                    std::to_string(card) + "\n" + kJitPrologue +
+                    (vec ? "typedef real sg_vec[BS];\n#define SG_VTERMS 8\n" : "") + "\n" +
+                    element_src + "\n" + (vec ? kJitVecKernel : kJitKernel);
   nvrtcProgram prog = nullptr;
   if (N.create(&prog, src.c_str(), "sg_jit_element.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
     return set_error(SG_ERR_UNSUPPORTED, "sg_jit: nvrtcCreateProgram failed");
@@ -254,30 +292,81 @@ int sg_jit_check_source(const char *element_src, int32_t card, int32_t bs, int d
   return rc;
 }
 
-int sg_jit_assembly_create(sg_ctx *h, const char *element_src, int32_t card, int32_t bs,
-                           int dtype, int32_t exact, sg_jit_assembly **out) {
+int sg_jit_check_vector_source(const char *element_src, int32_t card, int32_t bs, int dtype,
+                               int32_t exact, char *log, int64_t log_cap) {
+  std::vector<char> image;
+  std::string lg;
+  const int rc = jit_compile(element_src, card, bs, dtype, exact, image, lg, true);
+  if (log && log_cap > 0) {
+    const size_t k = lg.size() < (size_t)(log_cap - 1) ? lg.size() : (size_t)(log_cap - 1);
+    memcpy(log, lg.data(), k);
+    log[k] = '\0';
+  }
+  return rc;
+}
+
+static int jit_create(sg_ctx *h, const char *element_src, int32_t card, int32_t bs, int dtype,
+                      int32_t exact, bool vec, sg_jit_assembly **out) {
   Ctx *c = as_ctx(h);
   DeviceGuard dg_(c);
-  SG_REQUIRE(c && element_src && out, "sg_jit_assembly_create: null argument");
+  SG_REQUIRE(c && element_src && out, "sg_jit: null argument");
   std::vector<char> image;
   std::string log;
-  const int rc = jit_compile(element_src, card, bs, dtype, exact, image, log);
+  const int rc = jit_compile(element_src, card, bs, dtype, exact, image, log, vec);
   if (rc != SG_OK) return rc;
   auto *J = new JitAssembly();
   J->c = c;
   J->card = card;
   J->bs = bs;
   J->dtype = dtype;
+  J->vec = vec;
   cudaError_t e = cudaLibraryLoadData(&J->lib, image.data(), nullptr, nullptr, 0, nullptr,
                                       nullptr, 0);
-  if (e == cudaSuccess) e = cudaLibraryGetKernel(&J->kernel, J->lib, "sg_jit_rows");
+  if (e == cudaSuccess)
+    e = cudaLibraryGetKernel(&J->kernel, J->lib, vec ? "sg_jit_vec" : "sg_jit_rows");
   if (e != cudaSuccess) {
     if (J->lib) cudaLibraryUnload(J->lib);
     delete J;
-    return set_error(SG_ERR_CUDA, "sg_jit_assembly_create: %s", cudaGetErrorString(e));
+    return set_error(SG_ERR_CUDA, "sg_jit: %s", cudaGetErrorString(e));
   }
   ctx_retain(c);
   *out = reinterpret_cast<sg_jit_assembly *>(J);
+  return SG_OK;
+}
+
+int sg_jit_assembly_create(sg_ctx *h, const char *element_src, int32_t card, int32_t bs,
+                           int dtype, int32_t exact, sg_jit_assembly **out) {
+  return jit_create(h, element_src, card, bs, dtype, exact, false, out);
+}
+
+int sg_jit_vector_create(sg_ctx *h, const char *element_src, int32_t card, int32_t bs,
+                         int dtype, int32_t exact, sg_jit_assembly **out) {
+  return jit_create(h, element_src, card, bs, dtype, exact, true, out);
+}
+
+int sg_jit_assemble_vector(sg_jit_assembly *hj, const sg_mesh *m, const void *const *h_fields,
+                           int32_t nfields, void *vals) {
+  JitAssembly *J = reinterpret_cast<JitAssembly *>(hj);
+  DeviceGuard dg_(J ? J->c : nullptr);
+  SG_REQUIRE(J && m && vals, "sg_jit_assemble_vector: null argument");
+  SG_REQUIRE(J->vec, "sg_jit_assemble_vector: the handle holds a matrix element function");
+  SG_REQUIRE(m->card == J->card, "sg_jit_assemble_vector: mesh card %d, kernel card %d",
+             m->card, J->card);
+  SG_REQUIRE(nfields >= 0 && nfields <= JIT_MAX_FIELDS && (nfields == 0 || h_fields),
+             "sg_jit_assemble_vector: %d fields (at most %d)", nfields, JIT_MAX_FIELDS);
+  SG_REQUIRE(m->ve_ptr && (m->nE == 0 || (m->ve_idx && m->endpoints)),
+             "sg_jit_assemble_vector: mesh incidence missing");
+  if (m->n == 0) return SG_OK;
+  Ctx *c = J->c;
+  JitFields f{};
+  for (int k = 0; k < nfields; ++k) f.p[k] = h_fields[k];
+  int n = m->n;
+  const unsigned *ve_ptr = m->ve_ptr, *ve_idx = m->ve_idx;
+  const int *ep = m->endpoints;
+  void *args[] = {&n, &ve_ptr, &ve_idx, &ep, &f, &vals};
+  const int grid = grid_for(c, (int64_t)m->n, 128, 8);
+  SG_CHECK_CUDA(cudaLaunchKernel((const void *)J->kernel, dim3(grid), dim3(128), args, 0,
+                                 c->stream));
   return SG_OK;
 }
 
@@ -286,6 +375,7 @@ int sg_jit_assemble(sg_jit_assembly *hj, const sg_mesh *m, const void *const *h_
   JitAssembly *J = reinterpret_cast<JitAssembly *>(hj);
   DeviceGuard dg_(J ? J->c : nullptr);
   SG_REQUIRE(J && m && vals, "sg_jit_assemble: null argument");
+  SG_REQUIRE(!J->vec, "sg_jit_assemble: the handle holds a vector element function");
   SG_REQUIRE(m->card == J->card, "sg_jit_assemble: mesh card %d, kernel card %d", m->card,
              J->card);
   SG_REQUIRE(nfields >= 0 && nfields <= JIT_MAX_FIELDS && (nfields == 0 || h_fields),

@@ -263,13 +263,15 @@ class RectMatrix:
         return bspmv(self.ctx, self.nr, bs, self.rowptr, self.colidx, vals, x)
 
 
-def check_element_source(element_src, card, bs, dtype=torch.float64, exact=True):
-    """Compiles an element function as JitAssembly would (NVRTC, sm_103a)
-    without a context or a GPU; returns the compiler log, raises SimitError
-    with the log when the source does not compile."""
+def check_element_source(element_src, card, bs, dtype=torch.float64, exact=True, vector=False):
+    """Compiles an element function as JitAssembly (vector=False:
+    element_block) or JitVectorAssembly (vector=True: element_vector) would
+    (NVRTC, sm_103a) without a context or a GPU; returns the compiler log,
+    raises SimitError with the log when the source does not compile."""
     buf = ctypes.create_string_buffer(8192)
-    call("sg_jit_check_source", element_src.encode(), card, bs,
-         F64 if dtype == torch.float64 else F32, int(exact), buf, len(buf))
+    call("sg_jit_check_vector_source" if vector else "sg_jit_check_source",
+         element_src.encode(), card, bs, F64 if dtype == torch.float64 else F32, int(exact),
+         buf, len(buf))
     return buf.value.decode(errors="replace")
 
 
@@ -314,6 +316,35 @@ class JitAssembly:
             self.close()
         except Exception:
             pass
+
+
+class JitVectorAssembly(JitAssembly):
+    """`map f to E reduce +` into a system vector with the element function
+    given as CUDA source (sg_jit_vector_create: element_vector, compiled by
+    NVRTC with a vertex-owner kernel).  assemble(mesh, fields) -> values
+    [n*bs]."""
+
+    def __init__(self, ctx, element_src, card, bs, dtype=torch.float64, exact=True):
+        self.ctx, self.card, self.bs, self.dtype = ctx, card, bs, dtype
+        h = ctypes.c_void_p()
+        call("sg_jit_vector_create", ctx.h, element_src.encode(), card, bs,
+             F64 if dtype == torch.float64 else F32, int(exact), ctypes.byref(h))
+        self.h = h.value
+
+    def assemble(self, mesh, fields, out=None):
+        with self.ctx.stream():
+            fields = [_d(f, self.dtype, self.ctx.device) if _is_float(f) else
+                      _d(f, torch.bool if _is_bool(f) else torch.int32, self.ctx.device)
+                      for f in fields]
+            self._keep = fields
+            arr = (ctypes.c_void_p * max(1, len(fields)))(*[f.data_ptr() for f in fields])
+            vals = out if out is not None else torch.empty(mesh.n * self.bs, dtype=self.dtype,
+                                                           device=self.ctx.device)
+            if vals.numel() < mesh.n * self.bs or vals.dtype != self.dtype:
+                raise ValueError("jit assemble_vector: out needs %d %s values" %
+                                 (mesh.n * self.bs, self.dtype))
+            call("sg_jit_assemble_vector", self.h, mesh.ref(), arr, len(fields), ptr(vals))
+            return vals
 
 
 def _is_float(a):

@@ -14,13 +14,16 @@ covers the part of that pipeline an element function of such a map needs:
   multiple assignment, `for`, `while`, `if` / `elif` / `else`, `apply`,
   tensor literals, transpose, slices, calls, field access,
   `map ... to ... reduce +`;
-* a generator that turns one element function of a matrix map into
-  `element_block(e, i, j, ep, f, blk)`: the function body runs as written
-  on local arrays, and every write `K(v(a), v(b)) = value` of the chosen
-  result matrix becomes a term of block (i, j) when (a, b) == (i, j), in
-  statement order -- one `+=` on the slot each, as the lowered map does.
-  A write of one component, `K(v(a), v(b))(r, c) = x`, adds x at (r, c)
-  only.  Dense tensor products are emitted as the lowered loops compute
+* a generator that turns one element function of a map into the element
+  function the run-time compiled assembly takes.  The function body runs
+  as written on local arrays.  For a matrix result, every write
+  `K(v(a), v(b)) = value` becomes a term of block (i, j) of
+  `element_block(e, i, j, ep, f, blk)` when (a, b) == (i, j); for a vector
+  result, every write `f(v(a)) = value` a term of endpoint i of
+  `element_vector(e, i, ep, f, vec)` when a == i.  Terms keep statement
+  order -- one `+=` each, as the lowered map does.  A write of one
+  component, `K(v(a), v(b))(r, c) = x` or `f(v(a))(r) = x`, adds x there
+  only; a scalar written to a block or a vector fills it.  Dense tensor products are emitted as the lowered loops compute
   them (each entry summed from zero over the inner index in ascending
   order), scalar-tensor and element-wise operations entry by entry, so with
   contraction off (the run-time compiler's exact mode) the values follow
@@ -641,6 +644,7 @@ class _Gen:
         self.results = {}
         self.target = None
         self.vertex_map = False
+        self.vector = False
         # shared between an element function and its helpers
         self.st = state if state is not None else {
             "fields": [], "field_index": {}, "funcs_out": [], "funcs_done": {},
@@ -840,7 +844,11 @@ class _Gen:
         if op == "^":
             raise SimError("^ of a tensor")
         if ta and tb:
-            if a.shape != b.shape:
+            # element-wise: equal shapes, or two vectors of one length (the
+            # result keeps the left one's orientation)
+            vecs = (len(a.shape) == 2 and len(b.shape) == 2 and 1 in a.shape and
+                    1 in b.shape and _size(a.shape) == _size(b.shape))
+            if a.shape != b.shape and not vecs:
                 raise SimError("%s of shapes %s and %s" % (op, a.shape, b.shape))
             return self.elementwise(a.shape, lambda q: "(%s[%s] %s %s[%s])"
                                     % (a.code, q, cop, b.code, q))
@@ -1168,6 +1176,8 @@ class _Gen:
         if tname != self.target:      # another result of the map: not assembled here
             return
         bs = self.results[tname]
+        if self.vector:
+            return self.vector_write(tname, idx, comp, rhs, env, line, bs)
         if len(idx) != 2:
             raise SimError("line %d: %r is written with %d indices" % (line, tname, len(idx)))
         a, b = (self.endpoint(x, env, line) for x in idx)
@@ -1196,11 +1206,52 @@ class _Gen:
             if v.kind == "tensor" and _size(v.shape) == bs * bs:
                 self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_term_(blk, nt_)[q_ / %d][q_ %% %d] "
                           "+= %s[q_];" % (bs * bs, bs, bs, v.code))
-            elif v.kind != "tensor" and bs == 1:
-                self.emit("sg_term_(blk, nt_)[0][0] += %s;" % self.as_scalar(v))
+            elif v.kind != "tensor" or _size(v.shape) == 1:
+                # a scalar fills the block (bs == 1: the block's one entry)
+                self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_term_(blk, nt_)[q_ / %d][q_ %% %d] "
+                          "+= %s;" % (bs * bs, bs, bs, self.as_scalar(v)))
             else:
                 raise SimError("line %d: a value of shape %s written to a %dx%d block"
                                % (line, v.shape if v.kind == "tensor" else (), bs, bs))
+        self.ind -= 1
+        self.emit("}")
+
+
+    def vector_write(self, tname, idx, comp, rhs, env, line, bs):
+        if len(idx) != 1:
+            raise SimError("line %d: %r is written with %d indices" % (line, tname, len(idx)))
+        a = self.endpoint(idx[0], env, line)
+        self.emit("if ((%s) == i) {" % a)
+        self.ind += 1
+        if comp is not None:
+            cidx = self.index_codes(comp, env)
+            if len(cidx) != 1:
+                raise SimError("line %d: a vector component takes one index" % line)
+            x = self.as_scalar(self.expr(rhs, env))
+            self.emit("const int cr_ = %s;" % cidx[0])
+            self.emit("const unsigned cb_ = 1u << cr_;")
+            self.emit("if (!copen_ || (cmask_ & cb_)) {")
+            self.emit("  nt_ = sg_open_vterm_(vec, nt_);")
+            self.emit("  copen_ = 1;")
+            self.emit("  cmask_ = 0;")
+            self.emit("}")
+            self.emit("sg_vterm_(vec, nt_)[cr_] += %s;" % x)
+            self.emit("cmask_ |= cb_;")
+        else:
+            v = self.expr(rhs, env)
+            self.emit("nt_ = sg_open_vterm_(vec, nt_);")
+            self.emit("copen_ = 0;")
+            if v.kind == "tensor" and _size(v.shape) == bs and \
+                    (len(v.shape) == 2 and 1 in v.shape or bs == 1):
+                self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_vterm_(vec, nt_)[q_] += %s[q_];"
+                          % (bs, v.code))
+            elif v.kind != "tensor" or _size(v.shape) == 1:
+                # a scalar fills the vertex's entries
+                self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_vterm_(vec, nt_)[q_] += %s;"
+                          % (bs, self.as_scalar(v)))
+            else:
+                raise SimError("line %d: a value of shape %s written to a %d-vector"
+                               % (line, v.shape if v.kind == "tensor" else (), bs))
         self.ind -= 1
         self.emit("}")
 
@@ -1219,6 +1270,17 @@ __device__ inline sg_block &sg_term_(sg_block *blk, int nt) {
 }
 """
 
+_VTERM_SUPPORT = r"""
+__device__ inline int sg_open_vterm_(sg_vec *vec, int nt) {
+  if (nt >= SG_VTERMS) return nt + 1;
+  for (int a = 0; a < BS; ++a) vec[nt][a] = real(0);
+  return nt + 1;
+}
+__device__ inline sg_vec &sg_vterm_(sg_vec *vec, int nt) {
+  return vec[(nt < SG_VTERMS ? nt : SG_VTERMS) - 1];
+}
+"""
+
 
 def _result_block(rty):
     """Block size of a system-matrix result type."""
@@ -1231,16 +1293,43 @@ def _result_block(rty):
     return sh[0]
 
 
-def compile_map(src, func, args=None, result=None):
-    """The element function `func` of a matrix map as CUDA C++ source for
-    sg_jit_assembly_create.
+def _result_vector(rty):
+    """Entries per vertex of a system-vector result type."""
+    inner = rty[2]
+    if inner[0] == "scalar":
+        return 1
+    sh = _shape_of_type(inner)
+    if len(sh) != 2 or 1 not in sh:
+        raise SimError("vector results hold scalars or vectors per vertex, not %s" % (sh,))
+    return _size(sh)
 
-    args binds the map's scalar arguments by name; result names the matrix
-    result to assemble when the function has several (writes to the others
-    are left out).  Returns {"source", "fields" [(kind, name, shape, dtype)],
-    "card", "bs", "element", "vertex", "result"}: pass the field arrays in
-    `fields` order -- element fields [nE * size], vertex fields [n * size];
-    int and bool fields as int32 / bool arrays."""
+
+def _system_results(f):
+    """{name: ("matrix" | "vector", size)} of a function's system results."""
+    out = {}
+    for rn, rty in f["results"]:
+        if rty[0] != "tensor" or any(isinstance(d, int) for d in rty[1]):
+            continue
+        if len(rty[1]) == 2:
+            out[rn] = ("matrix", _result_block(rty))
+        elif len(rty[1]) == 1:
+            out[rn] = ("vector", _result_vector(rty))
+    return out
+
+
+def compile_map(src, func, args=None, result=None):
+    """The element function `func` of a map as CUDA C++ source: for a
+    matrix result `element_block` (sg_jit_assembly_create), for a vector
+    result `element_vector` (sg_jit_vector_create).
+
+    args binds the map's scalar arguments by name; result names the result
+    to assemble when the function has several (writes to the others are
+    left out).  Returns {"source", "kind" ("matrix" | "vector"), "fields"
+    [(kind, name, shape, dtype)], "card", "bs", "element", "vertex",
+    "result"}: pass the field arrays in `fields` order -- element fields
+    [nE * size], vertex fields [n * size]; int and bool fields as int32 /
+    bool arrays.  bs is the block size (matrix) or the entries per vertex
+    (vector)."""
     prog = parse(src)
     if func not in prog["funcs"]:
         raise SimError("no function %r" % func)
@@ -1279,58 +1368,62 @@ def compile_map(src, func, args=None, result=None):
     vertex_map = card is None
     if vertex_map:
         card, vert = 1, elem
-    results = {}
-    for rn, rty in f["results"]:
-        if rty[0] == "tensor" and len(rty[1]) == 2 and \
-                not any(isinstance(d, int) for d in rty[1]):
-            results[rn] = _result_block(rty)
+    results = _system_results(f)
     if not results:
-        raise SimError("%s has no (vertex, vertex) matrix result" % func)
+        raise SimError("%s has no system (vertex-indexed) result" % func)
     if result is None:
         if len(results) != 1:
-            raise SimError("%s has %d matrix results: name one" % (func, len(results)))
+            raise SimError("%s has %d system results: name one" % (func, len(results)))
         result = next(iter(results))
     if result not in results:
-        raise SimError("%r is not a matrix result of %s" % (result, func))
+        raise SimError("%r is not a system result of %s" % (result, func))
+    kind, size = results[result]
+    vector = kind == "vector"
     g = _Gen(prog, consts)
-    g.results = {rn: results.get(rn, 0) for rn, _ in f["results"]}
+    g.results = {rn: results.get(rn, (None, 0))[1] for rn, _ in f["results"]}
     g.target = result
+    g.vector = vector
     g.vertex_map = vertex_map
     g.emit("int nt_ = 0, copen_ = 0;")
     g.emit("unsigned cmask_ = 0;")
     g.emit("(void)cmask_; (void)copen_; (void)ep;")
     g.block(f["body"], env)
-    g.emit("return nt_ < SG_TERMS ? nt_ : SG_TERMS;")
+    g.emit("return nt_ < %s ? nt_ : %s;" % (("SG_VTERMS",) * 2 if vector else ("SG_TERMS",) * 2))
     st = g.st
     if len(st["fields"]) > MAX_FIELDS:
         raise SimError("%s reads %d fields; the assembly takes at most %d"
                        % (func, len(st["fields"]), MAX_FIELDS))
-    pre = "".join(_INTRINSICS[k] for k in st["intrinsics"]) + _TERM_SUPPORT
-    source = (pre + "\n".join(st["funcs_out"]) +
-              "\n__device__ int element_block(long long e, int i, int j, const int *ep,"
-              " const real *const *f, sg_block *blk) {\n" + "\n".join(g.lines) + "\n}\n")
-    return {"source": source, "fields": list(st["fields"]), "card": card,
-            "bs": results[result], "element": elem, "vertex": vert, "result": result}
+    pre = "".join(_INTRINSICS[k] for k in st["intrinsics"]) + \
+        (_VTERM_SUPPORT if vector else _TERM_SUPPORT)
+    head = ("__device__ int element_vector(long long e, int i, const int *ep,"
+            " const real *const *f, sg_vec *vec) {\n" if vector else
+            "__device__ int element_block(long long e, int i, int j, const int *ep,"
+            " const real *const *f, sg_block *blk) {\n")
+    source = pre + "\n".join(st["funcs_out"]) + "\n" + head + "\n".join(g.lines) + "\n}\n"
+    return {"source": source, "kind": kind, "fields": list(st["fields"]), "card": card,
+            "bs": size, "element": elem, "vertex": vert, "result": result}
 
 
 class SimMap:
-    """A matrix map of a `.sim` program compiled for the GPU:
+    """A map of a `.sim` program compiled for the GPU:
     `SimMap(ctx, src, "compute_stiffness", {"h": 0.01})` parses and
     generates the element function, and NVRTC compiles it into a row-owner
-    assembly (sg_jit_assembly_create).  assemble(mesh, fields) takes the
-    field arrays by name -- {"B": ..., "W": ..., "c": ...}; an element and a
-    vertex field of the same name are told apart as ("element", name) /
-    ("vertex", name) keys -- and returns the matrix values
-    [nnzb * bs * bs] in the mesh's pattern."""
+    assembly (sg_jit_assembly_create; sg_jit_vector_create for a vector
+    result).  assemble(mesh, fields) takes the field arrays by name --
+    {"B": ..., "W": ..., "c": ...}; an element and a vertex field of the same
+    name are told apart as ("element", name) / ("vertex", name) keys -- and
+    returns the matrix values [nnzb * bs * bs] in the mesh's pattern, or the
+    vector [n * bs]."""
 
     def __init__(self, ctx, src, func, args=None, result=None, dtype=None, exact=True):
         import torch
-        from .runtime import JitAssembly
+        from .runtime import JitAssembly, JitVectorAssembly
         self.info = compile_map(src, func, args, result)
         self.card, self.bs = self.info["card"], self.info["bs"]
         self.fields = self.info["fields"]
-        self.jit = JitAssembly(ctx, self.info["source"], self.card, self.bs,
-                               dtype=torch.float64 if dtype is None else dtype, exact=exact)
+        cls = JitVectorAssembly if self.info["kind"] == "vector" else JitAssembly
+        self.jit = cls(ctx, self.info["source"], self.card, self.bs,
+                       dtype=torch.float64 if dtype is None else dtype, exact=exact)
 
     def field_arrays(self, fields):
         out = []

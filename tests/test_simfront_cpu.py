@@ -77,8 +77,8 @@ def test_parser_structure():
     ("func f(e : E, v : (V*2)) -> (K : tensor[V,V](float))\n  K(v(0), v(1)) = y;\nend",
      "unknown name"),
     ("func f(a : float, e : E, v : (V*2)) -> (K : tensor[V,V](float))\nend", "not bound"),
-    ("func f(e : E, v : (V*2)) -> (b : tensor[V](float))\n  b(v(0)) = 1.0;\nend",
-     "no (vertex, vertex) matrix"),
+    ("func f(e : E, v : (V*2)) -> (b : float)\n  b = 1.0;\nend",
+     "no system (vertex-indexed) result"),
     ("func f(e : E, v : (V*2)) -> (K : tensor[V,V](tensor[3,3](float)))\n"
      "  K(v(0), v(1)) = [1.0, 2.0];\nend", "written to a 3x3 block"),
     ("func f(e : E, v : (V*2)) -> (K : tensor[V,V](float))\n"
@@ -95,21 +95,23 @@ def test_errors_are_reported(src, msg):
 # ---------------------------------------------------------------------------
 # NVRTC: the generated sources compile for sm_103a
 # ---------------------------------------------------------------------------
-def _nvrtc_check(src, card, bs, dtype, exact=True):
-    import torch
+def _nvrtc_check(src, card, bs, dtype, exact=True, vector=False):
     from simit_gb300 import _lib
     from simit_gb300.runtime import check_element_source
     try:
-        check_element_source(src, card, bs, dtype=dtype, exact=exact)
+        check_element_source(src, card, bs, dtype=dtype, exact=exact, vector=vector)
     except _lib.SimitError as e:
         if e.code == _lib.ERR_UNSUPPORTED:
             pytest.skip("NVRTC not available: %s" % e)
         raise
 
 
+FORCE_ARGS = {"h": 0.01, "rho": 1e3, "gx": 0.0, "gy": -9.81, "gz": 0.0}
 OWN_MAPS = [("tet_closed_form.sim", "tet_stiffness", {"h": 0.01, "rho": 1e3}, None),
             ("heat_p1.sim", "heat", {"dt": 0.01}, None),
-            ("point_mass.sim", "point_mass", {"damp": 0.5}, "M")]
+            ("point_mass.sim", "point_mass", {"damp": 0.5}, "M"),
+            ("point_mass.sim", "point_mass", {"damp": 0.5}, "g"),
+            ("tet_force.sim", "tet_force", FORCE_ARGS, None)]
 
 
 @pytest.mark.parametrize("fname,func,args,result", OWN_MAPS)
@@ -117,10 +119,19 @@ def test_generated_sources_compile(fname, func, args, result):
     import torch
     r = simfront.compile_map(_own(fname), func, args, result)
     for dt in (torch.float32, torch.float64):
-        _nvrtc_check(r["source"], r["card"], r["bs"], dt)
+        _nvrtc_check(r["source"], r["card"], r["bs"], dt, vector=r["kind"] == "vector")
 
 
 REF_MAPS = [("apps/fem/fem_linear.sim", "compute_stiffness", {"h": 0.01}, None),
+            ("apps/fem/fem_linear.sim", "compute_force", {"h": 0.01}, None),
+            ("apps/fem/fem_neohookean.sim", "compute_force", {"h": 0.01}, None),
+            ("apps/cloth/cloth.sim", "stretchingForce", {}, None),
+            ("apps/cloth/cloth.sim", "bendingForce", {}, None),
+            ("test/input/program/isprings.sim", "compute_elasticity", {}, "K"),
+            ("test/input/program/isprings.sim", "compute_elasticity", {}, "fe"),
+            ("test/input/program/isprings.sim", "compute_mass_damping", {}, "MD"),
+            ("test/input/program/isprings.sim", "compute_mass_damping", {}, "fmg"),
+            ("apps/fem/poisson_2D_triangles.sim", "assemble", {}, "b"),
             ("apps/fem/fem_neohookean.sim", "compute_stiffness", {"h": 0.01}, None),
             ("apps/fem/fem_linear.sim", "compute_mass", {}, None),
             ("apps/fem/poisson_2D_triangles.sim", "assemble", {}, "A"),
@@ -135,7 +146,8 @@ REF_MAPS = [("apps/fem/fem_linear.sim", "compute_stiffness", {"h": 0.01}, None),
 def test_reference_maps_compile(rel, func, args, result):
     import torch
     r = simfront.compile_map(_ref(rel), func, args, result)
-    _nvrtc_check(r["source"], r["card"], r["bs"], torch.float64)
+    _nvrtc_check(r["source"], r["card"], r["bs"], torch.float64,
+                 vector=r["kind"] == "vector")
 
 
 # ---------------------------------------------------------------------------
@@ -168,20 +180,49 @@ extern "C" void sim_assemble(long long nE, const int *ep_all, const real *const 
 """
 
 
+HARNESS_VEC = r"""
+#include <math.h>
+#define __device__
+typedef double real;
+#define BS %(bs)d
+#define CARD %(card)d
+typedef real sg_vec[BS];
+#define SG_VTERMS 8
+%(source)s
+// elements in order, endpoints in order, terms in order: each term a
+// separate += on its vertex, as the lowered map adds them
+extern "C" void sim_assemble(long long nE, const int *ep_all, const real *const *f,
+                             const long long *unused, real *vals) {
+  (void)unused;
+  for (long long e = 0; e < nE; ++e)
+    for (int i = 0; i < CARD; ++i) {
+      sg_vec vec[SG_VTERMS];
+      const int nt = element_vector(e, i, ep_all + e * CARD, f, vec);
+      real *v = vals + (long long)ep_all[e * CARD + i] * BS;
+      for (int q = 0; q < nt; ++q)
+        for (int a = 0; a < BS; ++a) v[a] += vec[q][a];
+    }
+}
+"""
+
+
 class HostMap:
     """The generated element function compiled for the host."""
 
     def __init__(self, info, tmp):
         src = os.path.join(tmp, "gen.cpp")
         so = os.path.join(tmp, "gen.so")
+        text = HARNESS_VEC if info.get("kind") == "vector" else HARNESS
         with open(src, "w") as f:
-            f.write(HARNESS % {"bs": info["bs"], "card": info["card"], "source": info["source"]})
+            f.write(text % {"bs": info["bs"], "card": info["card"], "source": info["source"]})
         subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", so, src],
                        check=True, capture_output=True)
         self.lib = ctypes.CDLL(so)
         self.info = info
 
     def assemble(self, ep, slots, nnzb, fields):
+        """Matrix maps: values [nnzb*bs*bs] through the slot map; vector
+        maps: values [nnzb*bs] for nnzb vertices (slots unused)."""
         keep = []
         for kind, name, shape, dt in self.info["fields"]:
             a = fields[(kind, name)] if (kind, name) in fields else fields[name]
@@ -189,9 +230,9 @@ class HostMap:
             keep.append(a)
         arr = (ctypes.c_void_p * max(1, len(keep)))(*[a.ctypes.data for a in keep])
         bs = self.info["bs"]
-        vals = np.zeros(nnzb * bs * bs)
+        vals = np.zeros(nnzb * bs * (1 if self.info.get("kind") == "vector" else bs))
         ep = np.ascontiguousarray(ep, np.int32)
-        sl = np.ascontiguousarray(slots, np.int64)
+        sl = np.ascontiguousarray(slots if slots is not None else np.zeros(1), np.int64)
         self.lib.sim_assemble(ctypes.c_longlong(ep.size // self.info["card"]),
                               ep.ctypes.data_as(ctypes.c_void_p), arr,
                               sl.ctypes.data_as(ctypes.c_void_p),
@@ -323,3 +364,42 @@ def test_reference_poisson_triangles_matches_restatement():
             if edge[t[i]]:
                 want[index[(int(t[i]), int(t[i]))]] += 1.0
     assert np.allclose(got, want, rtol=1e-12, atol=1e-12 * np.abs(want).max())
+
+
+@pytest.mark.parametrize("neo", [0, 1])
+def test_reference_fem_force_matches_oracle(oracle, neo):
+    """The reference's compute_force (a vector map: the element's nodal
+    forces, gravity and momentum on free vertices), generated as an
+    element_vector function and compiled for the host, equals the oracle's
+    force bit for bit (linear) / to rounding (neo-Hookean)."""
+    rel = "apps/fem/fem_neohookean.sim" if neo else "apps/fem/fem_linear.sim"
+    info = simfront.compile_map(_ref(rel), "compute_force", {"h": 0.01})
+    assert info["kind"] == "vector" and info["bs"] == 3
+    k = _tet_case(oracle, seed=9)
+    v = meshgen.rng(12).uniform(-0.01, 0.01, k["n"] * 3)
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(k["tets"], None, k["n"],
+                                          {"B": k["B"], "W": k["W"], "u": k["u"], "l": k["l"],
+                                           "c": k["c"], "x": k["mg"]["x"], "v": v})
+    # the reference program's gravity is (0, -10, 0) and rho 1e3
+    want = oracle.tet_force(neo, k["mg"]["x"], v, k["c"], k["tets"], k["B"], k["W"], k["u"],
+                            k["l"], 0.01, 1e3, np.array([0.0, -10.0, 0.0]))
+    if neo:
+        assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    else:
+        assert np.array_equal(got, want)
+
+
+def test_own_tet_force_matches_oracle(oracle):
+    """tests/sim/tet_force.sim assembles the oracle's linear force bit for
+    bit."""
+    info = simfront.compile_map(_own("tet_force.sim"), "tet_force", FORCE_ARGS)
+    k = _tet_case(oracle, seed=13)
+    v = meshgen.rng(14).uniform(-0.01, 0.01, k["n"] * 3)
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(k["tets"], None, k["n"],
+                                          {"B": k["B"], "W": k["W"], "u": k["u"], "l": k["l"],
+                                           "c": k["c"], "x": k["mg"]["x"], "v": v})
+    want = oracle.tet_force(0, k["mg"]["x"], v, k["c"], k["tets"], k["B"], k["W"], k["u"],
+                            k["l"], 0.01, 1e3, np.array([0.0, -9.81, 0.0]))
+    assert np.array_equal(got, want)
