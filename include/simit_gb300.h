@@ -254,8 +254,10 @@ int sg_assemble_rect(sg_ctx *ctx, int32_t nr, int32_t npos_r, int32_t npos_c,
  * does for precomputed blocks.  This is the code-generation end of the
  * reference's map lowering (src/inline.cpp:690-888,
  * src/lower/lower_maps.cpp:54-128) with the element function written in
- * CUDA rather than produced from .sim by its frontend.  card 1..32, bs 1..5.
- * A source that does not compile returns SG_ERR_ARG with the compiler log in
+ * CUDA rather than produced from .sim by its frontend.  card 1..32, bs 1..16
+ * (a nested block type is one flat block: 3x3 blocks of 3x3 are bs 9); a
+ * row must fit the kernel's 48 KB of shared memory, else sg_jit_assemble
+ * returns SG_ERR_UNSUPPORTED.  A source that does not compile returns SG_ERR_ARG with the compiler log in
  * sg_last_error(); without NVRTC, SG_ERR_UNSUPPORTED. */
 typedef struct sg_jit_assembly sg_jit_assembly;
 /* Compiles the source as sg_jit_assembly_create does, without a context or

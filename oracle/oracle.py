@@ -72,6 +72,12 @@ def lib():
         L.or_add_diag_f64.argtypes = [_I32, _I32, _P, _P, _P, _D, ctypes.c_int, _D, _P, _P]
         L.or_add_diag_f32.argtypes = [_I32, _I32, _P, _P, _P, ctypes.c_float, ctypes.c_int,
                                       ctypes.c_float, _P, _P]
+        L.or_cloth_faces.argtypes = [_P, _I64, _P, _P, _P]
+        L.or_cloth_hinges.argtypes = [_P, _I64, _P, _P, _P, _P]
+        L.or_cloth_stretch.argtypes = [_I32, _P, _I64, _P, _P, _P, _P]
+        L.or_cloth_bend.argtypes = [_I32, _P, _I64, _P, _P, _P, _P, _P]
+        L.or_cloth_step.argtypes = [_I32, _P, _P, _P, _P, _I64, _P, _P, _P, _I64, _P, _P, _P,
+                                    _P, _D, _D, _D, _D]
         _lib = L
     return _lib
 
@@ -388,3 +394,58 @@ def heat_assemble(n, tets, B, W, kappa, dt, T0, rowptr, colidx):
                            _p(_c(T0, np.float64)), _p(_c(rowptr, np.uint32)),
                            _p(_c(colidx, np.uint32)), _p(A), _p(b))
     return A, b
+
+
+def cloth_faces(x, faces):
+    """Per face (apps/cloth/cloth.sim:66-102): the stretching matrix (nF, 3, 3)
+    and the rest squared edge lengths (nF, 3)."""
+    faces = _c(faces, np.int32)
+    nF = faces.size // 3
+    K = np.zeros((nF, 3, 3))
+    rest = np.zeros((nF, 3))
+    lib().or_cloth_faces(_p(_c(x, np.float64)), nF, _p(faces), _p(K), _p(rest))
+    return K, rest
+
+
+def cloth_hinges(x, hinges):
+    """Per hinge (cloth.sim:105-113): rest angle, rest length, perpendicular
+    length."""
+    hinges = _c(hinges, np.int32)
+    nH = hinges.size // 4
+    ang, ln, perp = np.zeros(nH), np.zeros(nH), np.zeros(nH)
+    lib().or_cloth_hinges(_p(_c(x, np.float64)), nH, _p(hinges), _p(ang), _p(ln), _p(perp))
+    return ang, ln, perp
+
+
+def cloth_stretch(n, x, faces, K, rest):
+    """`map stretchingForce to faces reduce +` (cloth.sim:142-164), 3 per vertex."""
+    faces = _c(faces, np.int32)
+    f = np.zeros(n * 3)
+    lib().or_cloth_stretch(n, _p(_c(x, np.float64)), faces.size // 3, _p(faces),
+                           _p(_c(K, np.float64)), _p(_c(rest, np.float64)), _p(f))
+    return f
+
+
+def cloth_bend(n, x, hinges, ang, ln, perp):
+    """`map bendingForce to hinges reduce +` (cloth.sim:166-173), 3 per vertex."""
+    hinges = _c(hinges, np.int32)
+    f = np.zeros(n * 3)
+    lib().or_cloth_bend(n, _p(_c(x, np.float64)), hinges.size // 4, _p(hinges),
+                        _p(_c(ang, np.float64)), _p(_c(ln, np.float64)),
+                        _p(_c(perp, np.float64)), _p(f))
+    return f
+
+
+def cloth_step(x, v, m, fixed, faces, K, rest, hinges, ang, ln, perp, dt, ks, kb, damping):
+    """One step of cloth.sim's `main` (cloth.sim:201-222); returns (x, v)."""
+    x = np.array(x, np.float64).reshape(-1)
+    v = np.array(v, np.float64).reshape(-1)
+    n = x.size // 3
+    faces = _c(faces, np.int32)
+    hinges = _c(hinges, np.int32)
+    lib().or_cloth_step(n, _p(x), _p(v), _p(_c(m, np.float64)), _p(_c(fixed, np.int32)),
+                        faces.size // 3, _p(faces), _p(_c(K, np.float64)),
+                        _p(_c(rest, np.float64)), hinges.size // 4, _p(hinges),
+                        _p(_c(ang, np.float64)), _p(_c(ln, np.float64)),
+                        _p(_c(perp, np.float64)), dt, ks, kb, damping)
+    return x, v

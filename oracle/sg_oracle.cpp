@@ -758,3 +758,223 @@ void or_add_diag_f32(i32 n, i32 bs, const u32 *rowptr, const u32 *colidx, const 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Cloth (apps/cloth/cloth.sim): triangle stretching over faces (card 3) and
+// dihedral bending over hinges (card 4), the per-element quantities their
+// initialisation precomputes, and one explicit step of its `main`.  Each
+// vector is a 3-array; dot(a, b) = (a0*b0 + a1*b1) + a2*b2 and
+// norm(a) = sqrt(dot(a, a)), as the lowered tensor reductions sum them.  No
+// reference test pins these forms: the restatement is checked against the
+// program's own text compiled on the host, and the GPU against it.
+// ---------------------------------------------------------------------------
+namespace {
+
+inline double cdot(const double *a, const double *b) {
+  return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+}
+
+// cloth.sim:1-5 (cross)
+inline void ccross(const double *a, const double *b, double *r) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+inline void csub(const double *a, const double *b, double *r) {
+  for (int q = 0; q < 3; ++q) r[q] = a[q] - b[q];
+}
+
+// cloth.sim:31-38 (computeAngle): the dihedral angle at edge p1-p2 between
+// the triangles (p1, p2, q1) and (p1, p2, q2).
+double cloth_angle(const double *p1, const double *p2, const double *q1, const double *q2) {
+  double ev[3], d1[3], d2[3], n1[3], n2[3], c[3];
+  csub(p2, p1, ev);
+  csub(q1, p1, d1);
+  ccross(ev, d1, n1);
+  csub(q2, p1, d2);
+  ccross(d2, ev, n2);
+  const double mag = std::sqrt(cdot(ev, ev));
+  for (int q = 0; q < 3; ++q) ev[q] = ev[q] / mag;
+  ccross(n1, n2, c);
+  return std::atan2(cdot(c, ev), cdot(n1, n2));
+}
+
+// cloth.sim:115-140 (dihedralAngleDerivatives): d theta / d(p1, p2, q1, q2).
+void cloth_angle_grad(const double *p1, const double *p2, const double *q1, const double *q2,
+                      double *dp1, double *dp2, double *dq1, double *dq2) {
+  double v11[3], v12[3], v21[3], v22[3], v[3], n1[3], n2[3];
+  csub(q1, p2, v11);
+  csub(q1, p1, v12);
+  csub(q2, p2, v21);
+  csub(q2, p1, v22);
+  csub(p2, p1, v);
+  ccross(v12, v, n1);
+  ccross(v, v22, n2);
+  const double n1n2 = cdot(n1, n1), n2n2 = cdot(n2, n2), vn = std::sqrt(cdot(v, v));
+  if (vn < 1e-8 || n1n2 < 1e-8 || n2n2 < 1e-8) {
+    for (int q = 0; q < 3; ++q) dp1[q] = dp2[q] = dq1[q] = dq2[q] = 0.0;
+    return;
+  }
+  double m12[3], m22[3];
+  for (int q = 0; q < 3; ++q) {
+    m12[q] = -v12[q];
+    m22[q] = -v22[q];
+  }
+  const double a11 = cdot(v11, v), a21 = cdot(v21, v), a12 = cdot(m12, v), a22 = cdot(m22, v);
+  for (int q = 0; q < 3; ++q) {
+    dq1[q] = (n1[q] * vn) / n1n2;
+    dq2[q] = (n2[q] * vn) / n2n2;
+    const double F11 = ((n1[q] * a11) / vn) / n1n2, F12 = ((n2[q] * a21) / vn) / n2n2;
+    const double F21 = ((n1[q] * a12) / vn) / n1n2, F22 = ((n2[q] * a22) / vn) / n2n2;
+    dp1[q] = F11 + F12;
+    dp2[q] = F21 + F22;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// cloth.sim:66-102 (precomputeFaceQuantities): per face the stretching
+// matrix K (3x3, row-major) and the rest squared edge lengths, edge i running
+// from vertex i to vertex i+1.  Edge vector u_c (c = 0, 1, 2) is the edge
+// opposite vertex c: x2-x1, x0-x2, x1-x0.
+void or_cloth_faces(const double *x, i64 nF, const i32 *faces, double *K, double *rest) {
+  for (i64 f = 0; f < nF; ++f) {
+    const double *p0 = x + 3 * (i64)faces[3 * f], *p1 = x + 3 * (i64)faces[3 * f + 1],
+                 *p2 = x + 3 * (i64)faces[3 * f + 2];
+    double ed[3][3], u[3][3], c[3];  // ed[c]: column c of edgeVectors(p0, p1, p2)
+    csub(p1, p0, ed[0]);
+    csub(p2, p1, ed[1]);
+    csub(p0, p2, ed[2]);
+    for (int q = 0; q < 3; ++q) {
+      u[0][q] = ed[1][q];
+      u[1][q] = ed[2][q];
+      u[2][q] = ed[0][q];
+    }
+    ccross(u[2], u[1], c);
+    const double A = 0.5 * std::sqrt(cdot(c, c));
+    double *Kf = K + 9 * f;
+    for (int i = 0; i < 3; ++i) {
+      const int j = (i + 1) % 3, k = (i + 2) % 3;
+      for (int l = i; l < 3; ++l) {
+        const int m = (l + 1) % 3, n = (l + 2) % 3;
+        const double e = cdot(u[k], u[m]) * cdot(u[j], u[n]) + cdot(u[k], u[n]) * cdot(u[j], u[m]);
+        Kf[i * 3 + l] = e;
+        Kf[l * 3 + i] = e;
+      }
+    }
+    const double den = ((256.0 * A) * A) * A;
+    for (int q = 0; q < 9; ++q) Kf[q] = Kf[q] / den;
+    for (int i = 0; i < 3; ++i) rest[3 * f + i] = cdot(ed[i], ed[i]);
+  }
+}
+
+// cloth.sim:105-113 (precomputeHingeQuantities): rest angle, rest length of
+// the shared edge (vertices 0, 1) and 2 (A1 + A2) / (3 |e0|).
+void or_cloth_hinges(const double *x, i64 nH, const i32 *hinges, double *angle, double *len,
+                     double *perp) {
+  for (i64 h = 0; h < nH; ++h) {
+    const double *p[4];
+    for (int a = 0; a < 4; ++a) p[a] = x + 3 * (i64)hinges[4 * h + a];
+    angle[h] = cloth_angle(p[0], p[1], p[2], p[3]);
+    double e[3], d2[3], d3[3], c2[3], c3[3];
+    csub(p[1], p[0], e);
+    csub(p[2], p[0], d2);
+    csub(p[3], p[0], d3);
+    ccross(e, d2, c2);
+    ccross(e, d3, c3);
+    const double A1 = 0.5 * std::sqrt(cdot(c2, c2)), A2 = 0.5 * std::sqrt(cdot(c3, c3));
+    const double e0 = std::sqrt(cdot(e, e));
+    perp[h] = (2.0 * (A1 + A2)) / (3.0 * e0);
+    len[h] = e0;
+  }
+}
+
+// cloth.sim:142-164 (stretchingForce, `map ... to faces reduce +`): per
+// vertex k of a face, three terms (i = 0, 1, 2)
+//   -4 (K(i,k+1) s_i v_{k+1} - K(i,k+2) s_i v_{k+2}),
+// v_c the current edge opposite vertex c and s_i its squared length minus
+// the rest one; f (3 per vertex) is zeroed, then faces in order add theirs.
+void or_cloth_stretch(i32 n, const double *x, i64 nF, const i32 *faces, const double *K,
+                      const double *rest, double *f) {
+  for (i64 i = 0; i < (i64)n * 3; ++i) f[i] = 0.0;
+  for (i64 e = 0; e < nF; ++e) {
+    const i32 *vv = faces + 3 * e;
+    const double *p0 = x + 3 * (i64)vv[0], *p1 = x + 3 * (i64)vv[1], *p2 = x + 3 * (i64)vv[2];
+    double v[3][3];
+    csub(p2, p1, v[0]);
+    csub(p0, p2, v[1]);
+    csub(p1, p0, v[2]);
+    const double r[3] = {rest[3 * e + 1], rest[3 * e + 2], rest[3 * e + 0]};
+    double s[3];
+    for (int i = 0; i < 3; ++i) s[i] = cdot(v[i], v[i]) - r[i];
+    const double *Ke = K + 9 * e;
+    for (int k = 0; k < 3; ++k) {
+      const int k2 = (k + 1) % 3, k1 = (k + 2) % 3;
+      for (int i = 0; i < 3; ++i)
+        for (int q = 0; q < 3; ++q) {
+          const double t = (Ke[i * 3 + k2] * s[i]) * v[k2][q] - (Ke[i * 3 + k1] * s[i]) * v[k1][q];
+          f[3 * (i64)vv[k] + q] += -4.0 * t;
+        }
+    }
+  }
+}
+
+// cloth.sim:166-173 (bendingForce, `map ... to hinges reduce +`): per hinge
+// vertex a, -d theta/d x_a * L / Lperp * (theta - theta_rest), one term.
+void or_cloth_bend(i32 n, const double *x, i64 nH, const i32 *hinges, const double *angle,
+                   const double *len, const double *perp, double *f) {
+  for (i64 i = 0; i < (i64)n * 3; ++i) f[i] = 0.0;
+  for (i64 h = 0; h < nH; ++h) {
+    const double *p[4];
+    for (int a = 0; a < 4; ++a) p[a] = x + 3 * (i64)hinges[4 * h + a];
+    const double th = cloth_angle(p[0], p[1], p[2], p[3]);
+    double d[4][3];
+    cloth_angle_grad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3]);
+    const double dth = th - angle[h];
+    for (int a = 0; a < 4; ++a)
+      for (int q = 0; q < 3; ++q)
+        f[3 * (i64)hinges[4 * h + a] + q] += (((-d[a][q]) * len[h]) / perp[h]) * dth;
+  }
+}
+
+// cloth.sim:201-222 (main) for one step of length dt: advance x by dt v,
+// project points inside the radius-2 sphere at the origin onto it
+// (cloth.sim:185-192, enforceConstraints, velocity corrected), then
+//   F = ks stretch + kb bend - damping v,   v += dt (g + Minv F),
+// Minv = diag(1/m) with 0 on fixed points (cloth.sim:175-183).  gravityForce
+// (cloth.sim:194-199) writes (0, -9.8, 0) and, on a fixed point, (0, 0, 0)
+// after it; writes to a map's result accumulate (src/lower/lower_maps.cpp:
+// 38-47), so every point gets g = (0, -9.8, 0).  x, v (3 per point) are
+// updated in place.
+void or_cloth_step(i32 n, double *x, double *v, const double *m, const i32 *fixed, i64 nF,
+                   const i32 *faces, const double *K, const double *rest, i64 nH,
+                   const i32 *hinges, const double *angle, const double *len,
+                   const double *perp, double dt, double ks, double kb, double damping) {
+  const i64 n3 = (i64)n * 3;
+  for (i64 i = 0; i < n3; ++i) x[i] = x[i] + dt * v[i];
+  for (i32 p = 0; p < n; ++p) {
+    double *xp = x + 3 * (i64)p, *vp = v + 3 * (i64)p;
+    const double dist = std::sqrt(cdot(xp, xp));
+    if (dist < 2.0) {
+      double np[3];
+      for (int q = 0; q < 3; ++q) np[q] = (2.0 * xp[q]) / dist;
+      for (int q = 0; q < 3; ++q) vp[q] = vp[q] + (np[q] - xp[q]) / dt;
+      for (int q = 0; q < 3; ++q) xp[q] = 1.0 * np[q];
+    }
+  }
+  std::vector<double> fs(n3), fb(n3);
+  or_cloth_stretch(n, x, nF, faces, K, rest, fs.data());
+  or_cloth_bend(n, x, nH, hinges, angle, len, perp, fb.data());
+  for (i64 i = 0; i < n3; ++i) {
+    const double tot = (fs[i] * ks + fb[i] * kb) - damping * v[i];
+    const i32 p = (i32)(i / 3);
+    const double g = i % 3 == 1 ? -9.8 : 0.0;
+    const double minv = fixed[p] > 0 ? 0.0 : 1.0 / m[p];
+    v[i] = v[i] + dt * (g + minv * tot);
+  }
+}
+
+}  // extern "C"

@@ -155,6 +155,17 @@ class Set {
   int numFields() const { return (int)fields_.size(); }
   int getCardinality() const { return card_; }
   const std::vector<int32_t> &endpoints() const { return endpoints_; }
+  int32_t *getEndpointsPtr() { return endpoints_.data(); }
+  std::vector<FieldData> &getFields() { return fields_; }
+
+  // The field holding the elements' positions, which reorder() sorts along a
+  // Hilbert curve (src/graph.h: setSpatialField / hasSpatialField).
+  void setSpatialField(const std::string &name) {
+    if (!field(name)) throw SimitException("Set::setSpatialField: no field " + name);
+    spatial_ = name;
+  }
+  bool hasSpatialField() const { return !spatial_.empty(); }
+  const std::string &getSpatialFieldName() const { return spatial_; }
   FieldData *field(const std::string &name) {
     for (auto &f : fields_)
       if (f.name == name) return &f;
@@ -172,6 +183,7 @@ class Set {
   std::vector<Set *> endpoint_sets_;
   std::vector<int32_t> endpoints_;
   std::vector<FieldData> fields_;
+  std::string spatial_;
 };
 
 template <typename T, int... dims> T *FieldRef<T, dims...>::ptr(ElementRef e) const {
@@ -181,4 +193,5 @@ template <typename T, int... dims> T *FieldRef<T, dims...>::ptr(ElementRef e) co
 
 }  // namespace simit_gb300
 
+#include "reorder.h"
 #include "simit_function.h"

@@ -240,8 +240,8 @@ namespace {
 int jit_compile(const char *element_src, int32_t card, int32_t bs, int dtype, int32_t exact,
                 std::vector<char> &image, std::string &log, bool vec = false) {
   SG_REQUIRE(element_src, "sg_jit: null source");
-  SG_REQUIRE(card >= 1 && card <= 32 && bs >= 1 && bs <= 5,
-             "sg_jit: card %d bs %d (card 1..32, bs 1..5)", card, bs);
+  SG_REQUIRE(card >= 1 && card <= 32 && bs >= 1 && bs <= 16,
+             "sg_jit: card %d bs %d (card 1..32, bs 1..16)", card, bs);
   SG_REQUIRE(dtype == SG_F32 || dtype == SG_F64, "sg_jit: dtype %d", dtype);
   const Nvrtc &N = nvrtc();
   if (!N.ok) return set_error(SG_ERR_UNSUPPORTED, "sg_jit: NVRTC not found");

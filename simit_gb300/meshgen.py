@@ -152,6 +152,43 @@ def cloth_sheet(side, seed=0, spacing=None):
             "l0": l0, "fixed": fixed}
 
 
+def cloth_mesh(side, seed=0, height=2.0, half=1.5):
+    """A side x side triangle sheet over the square [-half, half]^2 of the
+    plane y = height, as the cloth program's face and hinge sets want.
+
+    Each quad is split into two triangles along alternating diagonals, all
+    wound the same way.  Each interior edge gives a hinge (a, b, c, d): the
+    edge's endpoints a < b, then the vertices opposite it in its first and
+    second triangle.  Returns rest positions (n*3), faces (nF*3) and hinges
+    (nH*4), all row-major.
+    """
+    s = side
+    t = np.linspace(-half, half, s)
+    gi, gj = np.meshgrid(t, t, indexing="ij")
+    x = np.stack([gi, np.full_like(gi, height), gj], -1).reshape(-1, 3)
+    a, b = np.meshgrid(np.arange(s - 1), np.arange(s - 1), indexing="ij")
+    a, b = a.reshape(-1), b.reshape(-1)
+    v00, v10, v01, v11 = a * s + b, (a + 1) * s + b, a * s + b + 1, (a + 1) * s + b + 1
+    alt = ((a + b) & 1).astype(bool)
+    t0 = np.where(alt[:, None], np.stack([v00, v10, v01], 1), np.stack([v00, v10, v11], 1))
+    t1 = np.where(alt[:, None], np.stack([v10, v11, v01], 1), np.stack([v00, v11, v01], 1))
+    faces = np.concatenate([t0, t1], 0).astype(np.int32)
+    # every (edge, opposite vertex) of every face, grouped by the sorted edge
+    e = np.concatenate([faces[:, [0, 1]], faces[:, [1, 2]], faces[:, [2, 0]]], 0)
+    opp = np.concatenate([faces[:, 2], faces[:, 0], faces[:, 1]], 0)
+    lo, hi = np.minimum(e[:, 0], e[:, 1]), np.maximum(e[:, 0], e[:, 1])
+    key = lo.astype(np.int64) * (s * s) + hi
+    order = np.argsort(key, kind="stable")
+    key_s, opp_s = key[order], opp[order]
+    uniq, first, counts = np.unique(key_s, return_index=True, return_counts=True)
+    inner = counts == 2
+    k = uniq[inner]
+    hinges = np.stack([k // (s * s), k % (s * s), opp_s[first[inner]], opp_s[first[inner] + 1]],
+                      1).astype(np.int32)
+    return {"n": s * s, "x": x.reshape(-1), "faces": faces.reshape(-1),
+            "hinges": hinges.reshape(-1)}
+
+
 def _tetgen_records(text, nhead, width):
     """Records of one TetGen file as MeshVol::loadTet / loadTetEdge read them
     (src/mesh.cpp:253-321, 341-373): the first nhead tokens are the header

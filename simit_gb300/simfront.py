@@ -43,6 +43,8 @@ kernel, not a replacement for the precompiled element kernels.
 """
 import re
 
+import numpy as np
+
 KEYWORDS = {"func", "proc", "end", "for", "in", "if", "elif", "else", "var", "const", "and",
             "or", "xor", "not", "element", "extern", "export", "set", "tensor", "vector",
             "matrix", "float", "double", "int", "bool", "string", "complex", "map", "to",
@@ -645,6 +647,8 @@ class _Gen:
         self.target = None
         self.vertex_map = False
         self.vector = False
+        self.nest = None
+        self.cwords = 1
         # shared between an element function and its helpers
         self.st = state if state is not None else {
             "fields": [], "field_index": {}, "funcs_out": [], "funcs_done": {},
@@ -706,6 +710,40 @@ class _Gen:
         ctype = {"int": "int", "bool": "bool"}.get(dt, "real")
         return "reinterpret_cast<const %s *>(f[%d])" % (ctype, k), shape, dt
 
+    def arg_field(self, name, shape, dt):
+        """A map argument that is a system vector (`map f(y) to V`, y a
+        tensor[V](...)): passed like a vertex field, as ("arg", name)."""
+        key = ("arg", name)
+        st = self.st
+        if key not in st["field_index"]:
+            st["field_index"][key] = len(st["fields"])
+            st["fields"].append(("arg", name, shape, dt))
+        k = st["field_index"][key]
+        ctype = {"int": "int", "bool": "bool"}.get(dt, "real")
+        return "reinterpret_cast<const %s *>(f[%d])" % (ctype, k)
+
+    def sysvec_read(self, v, args, env):
+        """y(p) of a system-vector argument: the block of vertex p (the
+        map's element in a map over the vertices, else an endpoint)."""
+        if len(args) != 1:
+            raise SimError("a system vector is indexed by one vertex")
+        p = self.expr(args[0], env)
+        if p.kind == "element" and self.vertex_map:
+            idx = "e"
+        elif p.kind == "vertex":
+            idx = "ep[%s]" % p.code
+        else:
+            raise SimError("a system vector is indexed by a vertex")
+        ptr = self.arg_field(v.code, v.shape, v.elem)
+        if v.shape == ():
+            return _Val({"int": "int", "bool": "bool"}.get(v.elem, "scalar"),
+                        "%s[%s]" % (ptr, idx))
+        out = self.new_tensor(v.shape)
+        sz = _size(v.shape)
+        self.emit("for (int q_ = 0; q_ < %d; ++q_) %s[q_] = %s[(long long)%s * %d + q_];"
+                  % (sz, out, ptr, idx, sz))
+        return _Val("tensor", out, v.shape)
+
     def field_base(self, e, env):
         base = self.expr(e[1], env)
         if base.kind == "element":
@@ -741,12 +779,30 @@ class _Gen:
         return [self.as_scalar(self.expr(a, env), "index") for a in args]
 
     def read_index(self, v, args, env):
+        if v.kind == "sysvec":
+            return self.sysvec_read(v, args, env)
         if v.kind != "tensor":
             raise SimError("indexing a value that is not a tensor")
         if any(a[0] == "slice" for a in args):
             return self.slice(v, args, env)
-        return _Val("scalar", "%s[%s]" % (v.code, self.flat(v.shape, self.index_codes(args,
-                                                                                       env))))
+        idx = self.index_codes(args, env)
+        sub = self.sub_tensor(v, idx)
+        if sub is not None:
+            return sub
+        return _Val("scalar", "%s[%s]" % (v.code, self.flat(v.shape, idx)))
+
+    def sub_tensor(self, v, idx):
+        """v(i) of a nested block (tensor[3](tensor[3](float)) is a 3x3 local
+        value whose v(i) is a 3-vector): the leading indices select a
+        sub-tensor, which aliases v's storage.  None when idx indexes v
+        fully."""
+        sh = v.shape
+        if len(idx) >= len(sh) or (len(sh) == 2 and 1 in sh):
+            return None
+        rest = sh[len(idx):]
+        off = self.flat(sh[:len(idx)], idx) if len(idx) > 1 else idx[0]
+        shape = (rest[0], 1) if len(rest) == 1 else rest
+        return _Val("tensor", "(%s + (%s) * %d)" % (v.code, off, _size(rest)), shape)
 
     def slice(self, v, args, env):
         if len(v.shape) != 2 or len(args) != 2:
@@ -1152,14 +1208,21 @@ class _Gen:
                 self.declare(name, v, env)
             return
         if lhs[0] == "call":
-            fn, idx = lhs[1], lhs[2]
-            if fn[0] == "name" and fn[1] in self.results:
-                return self.system_write(fn[1], idx, None, rhs, env, line)
-            if fn[0] == "call" and fn[1][0] == "name" and fn[1][1] in self.results:
-                return self.system_write(fn[1][1], fn[2], idx, rhs, env, line)
-            if fn[0] == "name" and fn[1] in env and env[fn[1]].kind == "tensor":
-                v = env[fn[1]]
-                dst = "%s[%s]" % (v.code, self.flat(v.shape, self.index_codes(idx, env)))
+            # X(p, q)(ii, jj)(i2, j2): the index groups, outermost first
+            groups, node = [], lhs
+            while node[0] == "call":
+                groups.append(node[2])
+                node = node[1]
+            groups.reverse()
+            if node[0] == "name" and node[1] in self.results:
+                return self.system_write(node[1], groups[0], groups[1:], rhs, env, line)
+            if node[0] == "name" and node[1] in env and env[node[1]].kind == "tensor":
+                v = env[node[1]]
+                idx = [c for g in groups for c in self.index_codes(g, env)]
+                if len(idx) < len(v.shape) and not (len(v.shape) == 2 and 1 in v.shape):
+                    self.assign_tensor(self.sub_tensor(v, idx), self.expr(rhs, env))
+                    return
+                dst = "%s[%s]" % (v.code, self.flat(v.shape, idx))
                 self.emit("%s = %s;" % (dst, self.as_scalar(self.expr(rhs, env))))
                 return
         raise SimError("line %d: unsupported assignment target" % line)
@@ -1172,38 +1235,62 @@ class _Gen:
             return "0"
         raise SimError("line %d: the result is indexed by endpoints v(k)" % line)
 
-    def system_write(self, tname, idx, comp, rhs, env, line):
+    def system_write(self, tname, idx, comps, rhs, env, line):
+        """A write to the map's result: a whole block (comps empty) or a
+        component chain; each write adds one term, as the lowered map adds
+        it into the result (src/lower/lower_maps.cpp:38-47)."""
         if tname != self.target:      # another result of the map: not assembled here
             return
         bs = self.results[tname]
         if self.vector:
-            return self.vector_write(tname, idx, comp, rhs, env, line, bs)
+            return self.vector_write(tname, idx, comps, rhs, env, line, bs)
         if len(idx) != 2:
             raise SimError("line %d: %r is written with %d indices" % (line, tname, len(idx)))
         a, b = (self.endpoint(x, env, line) for x in idx)
         self.emit("if ((%s) == i && (%s) == j) {" % (a, b))
         self.ind += 1
-        if comp is not None:
-            cidx = self.index_codes(comp, env)
-            if len(cidx) != 2:
-                raise SimError("line %d: a block component takes two indices" % line)
-            x = self.as_scalar(self.expr(rhs, env))
-            # a component joins the open component term unless that term
-            # already holds the component; otherwise it opens a new term
-            self.emit("const int cr_ = %s, cc_ = %s;" % (cidx[0], cidx[1]))
-            self.emit("const unsigned cb_ = 1u << (cr_ * %d + cc_);" % bs)
-            self.emit("if (!copen_ || (cmask_ & cb_)) {")
-            self.emit("  nt_ = sg_open_term_(blk, nt_);")
-            self.emit("  copen_ = 1;")
-            self.emit("  cmask_ = 0;")
-            self.emit("}")
-            self.emit("sg_term_(blk, nt_)[cr_][cc_] += %s;" % x)
-            self.emit("cmask_ |= cb_;")
+        ref = "sg_term_(blk, nt_)[ck_ / %d][ck_ %% %d]" % (bs, bs)
+        opn = "sg_open_term_(blk, nt_)"
+        nest = self.nest
+        if comps:
+            cidx = [c for g in comps for c in self.index_codes(g, env)]
+            v = self.expr(rhs, env)
+            if nest is None and len(cidx) == 2:
+                self.component_write("(%s) * %d + (%s)" % (cidx[0], bs, cidx[1]),
+                                     self.as_scalar(v), opn, ref)
+            elif nest is not None and len(cidx) == 4:
+                nb = nest[1]
+                row = "(%s) * %d + (%s)" % (cidx[0], nb, cidx[2])
+                col = "(%s) * %d + (%s)" % (cidx[1], nb, cidx[3])
+                self.component_write("(%s) * %d + %s" % (row, bs, col), self.as_scalar(v),
+                                     opn, ref)
+            elif nest is not None and len(cidx) == 2:
+                # an inner block X(p, q)(ii, jj) = B (b x b) or a scalar
+                nb = nest[1]
+                self.emit("for (int u_ = 0; u_ < %d; ++u_) {" % (nb * nb))
+                self.ind += 1
+                x = self.value_at(v, "u_", nb * nb, line)
+                self.component_write("((%s) * %d + u_ / %d) * %d + (%s) * %d + u_ %% %d"
+                                     % (cidx[0], nb, nb, bs, cidx[1], nb, nb), x, opn, ref)
+                self.ind -= 1
+                self.emit("}")
+            else:
+                raise SimError("line %d: %d component indices for a block of %s"
+                               % (line, len(cidx), "%dx%d" % (bs, bs) if nest is None else
+                                  "%dx%d blocks of %dx%d" % (nest[0], nest[0], nest[1],
+                                                             nest[1])))
         else:
             v = self.expr(rhs, env)
             self.emit("nt_ = sg_open_term_(blk, nt_);")
             self.emit("copen_ = 0;")
-            if v.kind == "tensor" and _size(v.shape) == bs * bs:
+            if v.kind == "tensor" and nest is not None and len(v.shape) == 4 and \
+                    _size(v.shape) == bs * bs:
+                # a nested local [ii][jj][i2][j2] into the flat block
+                na, nb = nest
+                self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_term_(blk, nt_)"
+                          "[q_ / %d * %d + q_ / %d %% %d][q_ / %d %% %d * %d + q_ %% %d] += %s[q_];"
+                          % (bs * bs, na * nb * nb, nb, nb, nb, nb * nb, na, nb, nb, v.code))
+            elif v.kind == "tensor" and _size(v.shape) == bs * bs:
                 self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_term_(blk, nt_)[q_ / %d][q_ %% %d] "
                           "+= %s[q_];" % (bs * bs, bs, bs, v.code))
             elif v.kind != "tensor" or _size(v.shape) == 1:
@@ -1216,33 +1303,67 @@ class _Gen:
         self.ind -= 1
         self.emit("}")
 
+    def value_at(self, v, q, n, line):
+        """Entry q of an n-entry value, or the value itself if scalar."""
+        if v.kind == "tensor" and _size(v.shape) == n:
+            return "%s[%s]" % (v.code, q)
+        if v.kind != "tensor" or _size(v.shape) == 1:
+            return self.as_scalar(v)
+        raise SimError("line %d: a value of shape %s written to %d entries"
+                       % (line, v.shape, n))
 
-    def vector_write(self, tname, idx, comp, rhs, env, line, bs):
+    def component_write(self, k, x, opn, ref):
+        """Component k of the block (flat index) += x.  The component joins
+        the open component term unless that term already holds it;
+        otherwise it opens a new term."""
+        self.emit("{")
+        self.ind += 1
+        self.emit("const int ck_ = %s;" % k)
+        self.emit("if (!copen_ || ((cmask_[ck_ >> 5] >> (ck_ & 31)) & 1u)) {")
+        self.emit("  nt_ = %s;" % opn)
+        self.emit("  copen_ = 1;")
+        self.emit("  for (int w_ = 0; w_ < %d; ++w_) cmask_[w_] = 0;" % self.cwords)
+        self.emit("}")
+        self.emit("%s += %s;" % (ref, x))
+        self.emit("cmask_[ck_ >> 5] |= 1u << (ck_ & 31);")
+        self.ind -= 1
+        self.emit("}")
+
+    def vector_write(self, tname, idx, comps, rhs, env, line, bs):
         if len(idx) != 1:
             raise SimError("line %d: %r is written with %d indices" % (line, tname, len(idx)))
         a = self.endpoint(idx[0], env, line)
         self.emit("if ((%s) == i) {" % a)
         self.ind += 1
-        if comp is not None:
-            cidx = self.index_codes(comp, env)
-            if len(cidx) != 1:
-                raise SimError("line %d: a vector component takes one index" % line)
-            x = self.as_scalar(self.expr(rhs, env))
-            self.emit("const int cr_ = %s;" % cidx[0])
-            self.emit("const unsigned cb_ = 1u << cr_;")
-            self.emit("if (!copen_ || (cmask_ & cb_)) {")
-            self.emit("  nt_ = sg_open_vterm_(vec, nt_);")
-            self.emit("  copen_ = 1;")
-            self.emit("  cmask_ = 0;")
-            self.emit("}")
-            self.emit("sg_vterm_(vec, nt_)[cr_] += %s;" % x)
-            self.emit("cmask_ |= cb_;")
+        ref = "sg_vterm_(vec, nt_)[ck_]"
+        opn = "sg_open_vterm_(vec, nt_)"
+        nest = self.nest
+        if comps:
+            cidx = [c for g in comps for c in self.index_codes(g, env)]
+            v = self.expr(rhs, env)
+            if len(cidx) == 1 and nest is None:
+                self.component_write(cidx[0], self.as_scalar(v), opn, ref)
+            elif len(cidx) == 2 and nest is not None:
+                self.component_write("(%s) * %d + (%s)" % (cidx[0], nest[1], cidx[1]),
+                                     self.as_scalar(v), opn, ref)
+            elif len(cidx) == 1 and nest is not None:
+                # a row x(p)(ii) = w (b entries) or a scalar
+                nb = nest[1]
+                self.emit("for (int u_ = 0; u_ < %d; ++u_) {" % nb)
+                self.ind += 1
+                self.component_write("(%s) * %d + u_" % (cidx[0], nb),
+                                     self.value_at(v, "u_", nb, line), opn, ref)
+                self.ind -= 1
+                self.emit("}")
+            else:
+                raise SimError("line %d: %d component indices for a vertex's %d entries"
+                               % (line, len(cidx), bs))
         else:
             v = self.expr(rhs, env)
             self.emit("nt_ = sg_open_vterm_(vec, nt_);")
             self.emit("copen_ = 0;")
             if v.kind == "tensor" and _size(v.shape) == bs and \
-                    (len(v.shape) == 2 and 1 in v.shape or bs == 1):
+                    (len(v.shape) == 2 and 1 in v.shape or bs == 1 or nest is not None):
                 self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_vterm_(vec, nt_)[q_] += %s[q_];"
                           % (bs, v.code))
             elif v.kind != "tensor" or _size(v.shape) == 1:
@@ -1283,37 +1404,49 @@ __device__ inline sg_vec &sg_vterm_(sg_vec *vec, int nt) {
 
 
 def _result_block(rty):
-    """Block size of a system-matrix result type."""
+    """(block size, nesting) of a system-matrix result type.  A nested block
+    tensor[a,a](tensor[b,b](T)) is stored as one (a b) x (a b) block, entry
+    (ii, jj)(i2, jj2) at row ii*b + i2, column jj*b + j2; nesting is (a, b),
+    None for a plain block."""
     inner = rty[2]
     if inner[0] == "scalar":
-        return 1
+        return 1, None
     sh = _shape_of_type(inner)
-    if len(sh) != 2 or sh[0] != sh[1]:
-        raise SimError("blocks must be square matrices, not %s" % (sh,))
-    return sh[0]
+    if len(sh) == 2 and sh[0] == sh[1]:
+        return sh[0], None
+    if len(sh) == 4 and sh[0] == sh[1] and sh[2] == sh[3]:
+        return sh[0] * sh[2], (sh[0], sh[2])
+    raise SimError("blocks must be square matrices or square blocks of them, not %s" % (sh,))
 
 
 def _result_vector(rty):
-    """Entries per vertex of a system-vector result type."""
+    """(entries per vertex, nesting) of a system-vector result type: a
+    nested tensor[a](tensor[b](T)) (or an a x b matrix per vertex) holds a*b
+    entries, entry (ii)(jj) at ii*b + jj; nesting is (a, b), None for a
+    scalar or vector per vertex."""
     inner = rty[2]
     if inner[0] == "scalar":
-        return 1
+        return 1, None
     sh = _shape_of_type(inner)
-    if len(sh) != 2 or 1 not in sh:
-        raise SimError("vector results hold scalars or vectors per vertex, not %s" % (sh,))
-    return _size(sh)
+    if len(sh) == 2 and 1 in sh:
+        return _size(sh), None
+    if len(sh) == 2:
+        return _size(sh), sh
+    raise SimError("vector results hold scalars, vectors or matrices per vertex, not %s"
+                   % (sh,))
 
 
 def _system_results(f):
-    """{name: ("matrix" | "vector", size)} of a function's system results."""
+    """{name: ("matrix" | "vector", size, nesting)} of a function's system
+    results."""
     out = {}
     for rn, rty in f["results"]:
         if rty[0] != "tensor" or any(isinstance(d, int) for d in rty[1]):
             continue
         if len(rty[1]) == 2:
-            out[rn] = ("matrix", _result_block(rty))
+            out[rn] = ("matrix",) + _result_block(rty)
         elif len(rty[1]) == 1:
-            out[rn] = ("vector", _result_vector(rty))
+            out[rn] = ("vector",) + _result_vector(rty)
     return out
 
 
@@ -1354,6 +1487,13 @@ def compile_map(src, func, args=None, result=None):
                 raise SimError("two element arguments")
             elem = aty[1]
             env[an] = _Val("element", "e", elem=elem)
+        elif aty[0] == "tensor" and len(aty[1]) == 1 and not isinstance(aty[1][0], int):
+            # a system vector read per vertex: y(p)
+            inner = aty[2]
+            shape = () if inner[0] == "scalar" else _shape_of_type(inner)
+            while inner[0] == "tensor":
+                inner = inner[2]
+            env[an] = _Val("sysvec", an, shape, elem=inner[1])
         elif aty[0] == "tuple":
             members = aty[1]
             kinds = {m[1] for m in members}
@@ -1377,15 +1517,17 @@ def compile_map(src, func, args=None, result=None):
         result = next(iter(results))
     if result not in results:
         raise SimError("%r is not a system result of %s" % (result, func))
-    kind, size = results[result]
+    kind, size, nest = results[result]
     vector = kind == "vector"
     g = _Gen(prog, consts)
     g.results = {rn: results.get(rn, (None, 0))[1] for rn, _ in f["results"]}
+    g.nest = nest
     g.target = result
     g.vector = vector
     g.vertex_map = vertex_map
+    g.cwords = (size * (1 if vector else size) + 31) // 32
     g.emit("int nt_ = 0, copen_ = 0;")
-    g.emit("unsigned cmask_ = 0;")
+    g.emit("unsigned cmask_[%d] = {0};" % g.cwords)
     g.emit("(void)cmask_; (void)copen_; (void)ep;")
     g.block(f["body"], env)
     g.emit("return nt_ < %s ? nt_ : %s;" % (("SG_VTERMS",) * 2 if vector else ("SG_TERMS",) * 2))
@@ -1426,14 +1568,31 @@ class SimMap:
                        dtype=torch.float64 if dtype is None else dtype, exact=exact)
 
     def field_arrays(self, fields):
+        """The arrays in the generated source's order, each in its declared
+        type: int fields as int32, bool as bool, float fields as floating
+        point (the assembly then casts them to its dtype)."""
+        import torch
         out = []
         for kind, name, shape, dt in self.fields:
             if (kind, name) in fields:
-                out.append(fields[(kind, name)])
+                a = fields[(kind, name)]
             elif name in fields:
-                out.append(fields[name])
+                a = fields[name]
             else:
                 raise SimError("field %s.%s is not given" % (kind, name))
+            want = {"int": (torch.int32, np.int32), "bool": (torch.bool, np.bool_)}.get(dt)
+            if isinstance(a, torch.Tensor):
+                if want is not None and a.dtype != want[0]:
+                    a = a.to(want[0])
+                elif want is None and not a.is_floating_point():
+                    a = a.double()
+            else:
+                a = np.asarray(a)
+                if want is not None and a.dtype != want[1]:
+                    a = a.astype(want[1])
+                elif want is None and a.dtype.kind != "f":
+                    a = a.astype(np.float64)
+            out.append(a)
         return out
 
     def assemble(self, mesh, fields, out=None):

@@ -4,6 +4,8 @@
 //   test/program-isprings.cpp:91-175  (TEST(Program, isprings))
 //   test/program-cg-test.cpp:10-44    (TEST(Program, cg))
 //   test/program-fem-test.cpp:14-106  (TEST(Program, femTet), bar2k mesh)
+//   test/reorder-tests.cpp:406-441    (TEST(Program, reorderFemSpecificTest): the
+//                                      same run on the Hilbert-reordered mesh)
 // Exit code 0 when every value is within 1e-13 (SIMIT_ASSERT_FLOAT_EQ).
 #include <cmath>
 #include <cstdio>
@@ -107,7 +109,7 @@ static bool load_tet(const std::string &prefix, std::vector<double> &xv,
   return true;
 }
 
-static void test_femtet(const std::string &golden_dir) {
+static void test_femtet(const std::string &golden_dir, bool reordered) {
   std::vector<double> xv;
   std::vector<std::array<int, 4>> ev;
   if (!load_tet(golden_dir + "/bar2k", xv, ev)) {
@@ -148,6 +150,14 @@ static void test_femtet(const std::string &golden_dir) {
     u.set(t, uval);
     l.set(t, lval);
   }
+  // vertex i's values are at index at[i] after the optional reordering
+  std::vector<int> at(refs.size());
+  for (size_t i = 0; i < at.size(); ++i) at[i] = (int)i;
+  if (reordered) {
+    std::vector<int> edgeOrdering;
+    verts.setSpatialField("x");
+    reorder(tets, verts, edgeOrdering, at);
+  }
   Function pre("femTet.init");
   pre.bind("verts", &verts);
   pre.bind("tets", &tets);
@@ -158,15 +168,15 @@ static void test_femtet(const std::string &golden_dir) {
   step.bind("tets", &tets);
   step.init();
   for (int i = 0; i < 10; ++i) step.runSafe();
-  ASSERT_NEAR13(0.010771915616785779, x.get(refs[100])(0));
-  ASSERT_NEAR13(0.058853573999788439, x.get(refs[100])(1));
-  ASSERT_NEAR13(0.030899457015375883, x.get(refs[100])(2));
-  ASSERT_NEAR13(0.0028221631202928516, x.get(refs[200])(0));
-  ASSERT_NEAR13(0.017969982607667911, x.get(refs[200])(1));
-  ASSERT_NEAR13(0.012885386063393013, x.get(refs[200])(2));
-  ASSERT_NEAR13(0.02411959295647129, x.get(refs[300])(0));
-  ASSERT_NEAR13(0.052036155669135678, x.get(refs[300])(1));
-  ASSERT_NEAR13(0.030173075240629205, x.get(refs[300])(2));
+  ASSERT_NEAR13(0.010771915616785779, x.get(refs[at[100]])(0));
+  ASSERT_NEAR13(0.058853573999788439, x.get(refs[at[100]])(1));
+  ASSERT_NEAR13(0.030899457015375883, x.get(refs[at[100]])(2));
+  ASSERT_NEAR13(0.0028221631202928516, x.get(refs[at[200]])(0));
+  ASSERT_NEAR13(0.017969982607667911, x.get(refs[at[200]])(1));
+  ASSERT_NEAR13(0.012885386063393013, x.get(refs[at[200]])(2));
+  ASSERT_NEAR13(0.02411959295647129, x.get(refs[at[300]])(0));
+  ASSERT_NEAR13(0.052036155669135678, x.get(refs[at[300]])(1));
+  ASSERT_NEAR13(0.030173075240629205, x.get(refs[at[300]])(2));
 }
 
 static void test_bind_errors() {
@@ -189,7 +199,8 @@ int main(int argc, char **argv) {
   try {
     test_isprings();
     test_cg();
-    test_femtet(golden);
+    test_femtet(golden, false);
+    test_femtet(golden, true);
     test_bind_errors();
   } catch (const std::exception &e) {
     std::printf("FAIL exception: %s\n", e.what());

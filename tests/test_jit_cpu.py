@@ -39,7 +39,7 @@ def test_compile_error_carries_the_log():
 
 
 def test_bad_shape_rejected():
-    for card, bs in ((0, 1), (33, 1), (2, 0), (2, 6)):
+    for card, bs in ((0, 1), (33, 1), (2, 0), (2, 17)):
         with pytest.raises(_lib.SimitError):
             check_element_source(jit_elements.BLOCKS, card, bs)
 

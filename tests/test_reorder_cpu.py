@@ -87,3 +87,26 @@ def test_morton_order_groups_aligned_cubes():
     cubes = walk[:512].reshape(-1, 8, 3) // 2
     assert np.all(cubes == cubes[:, :1, :])
     assert sorted(vo) == list(range(side ** 3))
+
+
+def test_cpp_facade_set_reordering(tmp_path):
+    """tests/cpp/test_reorder.cpp: the facade's reorderVertexSet /
+    reorderEdgeSet / reorder on simit_gb300::Set, restating the reference's
+    reorderInt and reorderDouble tests (test/reorder-tests.cpp:177-404), with
+    the orderings' properties and error cases.  Host code only."""
+    import os
+    import subprocess
+    from simit_gb300 import _lib
+    _lib.load()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = str(tmp_path / "test_reorder")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", root, "-I",
+                           os.path.join(cuda, "include"),
+                           os.path.join(root, "tests", "cpp", "test_reorder.cpp"),
+                           "-L", os.path.join(root, "simit_gb300"), "-lsimit_gb300",
+                           "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                           "-Wl,-rpath," + os.path.join(root, "simit_gb300"), "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all passed" in r.stdout

@@ -403,3 +403,252 @@ def test_own_tet_force_matches_oracle(oracle):
     want = oracle.tet_force(0, k["mg"]["x"], v, k["c"], k["tets"], k["B"], k["W"], k["u"],
                             k["l"], 0.01, 1e3, np.array([0.0, -9.81, 0.0]))
     assert np.array_equal(got, want)
+
+
+# ---------------------------------------------------------------------------
+# cloth: triangle stretching over faces (card 3), dihedral bending over
+# hinges (card 4)
+# ---------------------------------------------------------------------------
+def _cloth_case(oracle, side=9, seed=21, noise=0.03):
+    """A sheet, its rest quantities from the oracle's restatement of the
+    cloth initialisation, and perturbed current positions."""
+    mg = meshgen.cloth_mesh(side)
+    K, rest = oracle.cloth_faces(mg["x"], mg["faces"])
+    ang, ln, perp = oracle.cloth_hinges(mg["x"], mg["hinges"])
+    x = mg["x"] + meshgen.rng(seed).normal(0.0, noise, mg["x"].size)
+    return dict(mg=mg, n=mg["n"], K=K, rest=rest, ang=ang, ln=ln, perp=perp, x=x)
+
+
+def test_cloth_oracle_rest_state_and_invariance(oracle):
+    """The restated forces vanish at the rest positions, and at perturbed
+    positions each sums to zero over the sheet (translation invariance)."""
+    k = _cloth_case(oracle)
+    X = k["mg"]["x"]
+    fs0 = oracle.cloth_stretch(k["n"], X, k["mg"]["faces"], k["K"], k["rest"])
+    fb0 = oracle.cloth_bend(k["n"], X, k["mg"]["hinges"], k["ang"], k["ln"], k["perp"])
+    assert np.abs(fs0).max() < 1e-12 and np.abs(fb0).max() < 1e-12
+    fs = oracle.cloth_stretch(k["n"], k["x"], k["mg"]["faces"], k["K"], k["rest"])
+    fb = oracle.cloth_bend(k["n"], k["x"], k["mg"]["hinges"], k["ang"], k["ln"], k["perp"])
+    for f in (fs, fb):
+        assert np.abs(f).max() > 1e-3
+        assert np.abs(f.reshape(-1, 3).sum(0)).max() < 1e-11 * np.abs(f).max() * k["n"]
+
+
+def _cloth_host(info, k, which):
+    mg = k["mg"]
+    with tempfile.TemporaryDirectory() as tmp:
+        hm = HostMap(info, tmp)
+        if which == "stretch":
+            fields = {"x": k["x"], "restLengths": k["rest"], "rest": k["rest"],
+                      "precomputedStretchingMatrix": k["K"], "K": k["K"]}
+            return hm.assemble(mg["faces"], None, k["n"], fields)
+        fields = {"x": k["x"], "restLength": k["ln"], "len": k["ln"],
+                  "restPerpLength": k["perp"], "perp": k["perp"],
+                  "restBendingAngle": k["ang"], "theta0": k["ang"]}
+        return hm.assemble(mg["hinges"], None, k["n"], fields)
+
+
+@pytest.mark.parametrize("func,which", [("stretchingForce", "stretch"),
+                                        ("bendingForce", "bend")])
+def test_reference_cloth_forces_match_oracle(oracle, func, which):
+    """The reference's own cloth forces (apps/cloth/cloth.sim:142-173),
+    generated as element_vector functions and compiled for the host, equal
+    the oracle's restatement bit for bit on a perturbed sheet."""
+    info = simfront.compile_map(_ref("apps/cloth/cloth.sim"), func)
+    assert info["kind"] == "vector" and info["card"] == (3 if which == "stretch" else 4)
+    k = _cloth_case(oracle)
+    got = _cloth_host(info, k, which)
+    mg = k["mg"]
+    if which == "stretch":
+        want = oracle.cloth_stretch(k["n"], k["x"], mg["faces"], k["K"], k["rest"])
+    else:
+        want = oracle.cloth_bend(k["n"], k["x"], mg["hinges"], k["ang"], k["ln"], k["perp"])
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("func,which", [("stretch", "stretch"), ("bend", "bend")])
+def test_own_cloth_forces_match_oracle(oracle, func, which):
+    """tests/sim/cloth_forces.sim's stretch and bend: the oracle's cloth
+    forces bit for bit, on the host."""
+    info = simfront.compile_map(_own("cloth_forces.sim"), func)
+    k = _cloth_case(oracle, side=11, seed=22)
+    got = _cloth_host(info, k, which)
+    mg = k["mg"]
+    if which == "stretch":
+        want = oracle.cloth_stretch(k["n"], k["x"], mg["faces"], k["K"], k["rest"])
+    else:
+        want = oracle.cloth_bend(k["n"], k["x"], mg["hinges"], k["ang"], k["ln"], k["perp"])
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("func", ["stretch", "bend", "gravity", "inv_mass"])
+def test_own_cloth_maps_compile(func):
+    import torch
+    r = simfront.compile_map(_own("cloth_forces.sim"), func)
+    for dt in (torch.float32, torch.float64):
+        _nvrtc_check(r["source"], r["card"], r["bs"], dt, vector=r["kind"] == "vector")
+
+
+def test_reference_cloth_gravity_accumulates_on_fixed_points():
+    """cloth.sim's gravityForce writes (0, -9.8, 0) and then, on a fixed
+    point, (0, 0, 0): the writes of a map's result accumulate, so fixed
+    points keep gravity -- the oracle's cloth step restates it so."""
+    info = simfront.compile_map(_ref("apps/cloth/cloth.sim"), "gravityForce")
+    n = 6
+    fixed = np.array([0, 1, 0, 1, 1, 0], np.int32)
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(np.arange(n, dtype=np.int32), None, n,
+                                          {"fixed": fixed})
+    want = np.tile([0.0, -9.8, 0.0], n)
+    assert np.array_equal(got, want)
+
+
+# ---------------------------------------------------------------------------
+# nested block types and component writes into blocks
+# ---------------------------------------------------------------------------
+def _diag(n):
+    """Pattern and slots of a map over the vertices (one diagonal block each)."""
+    return np.arange(n + 1, dtype=np.uint32), np.arange(n, dtype=np.uint32), np.arange(n)
+
+
+def test_reference_block_component_write():
+    """test/assembly-tests.cpp:450-471 (block_component_write): each edge
+    writes component 0 of its first endpoint's 2-vector; on the 3-vertex
+    path the result is (1, 0), (1, 0), (0, 0)."""
+    info = simfront.compile_map(_ref("test/input/assembly/block_component_write.sim"), "f")
+    assert info["kind"] == "vector" and info["bs"] == 2
+    with tempfile.TemporaryDirectory() as tmp:
+        got = HostMap(info, tmp).assemble(np.array([0, 1, 1, 2], np.int32), None, 3, {})
+    assert got.tolist() == [1, 0, 1, 0, 0, 0]
+
+
+def test_reference_blocked_nested_blocks(oracle):
+    """test/assembly-tests.cpp:429-448 (blocked): a diagonal system matrix
+    of 3x3 blocks of 3x3 blocks, a vector of 3 blocks of 3, their product
+    and a map reading it as an argument give z = 81, 324, 729 for
+    x = 1, 2, 3."""
+    src = _ref("test/input/assembly/blocked.sim")
+    n = 3
+    xs = np.array([1, 2, 3], np.int32)
+    ep = np.arange(n, dtype=np.int32)
+    rp, ci, sl = _diag(n)
+    with tempfile.TemporaryDirectory() as tmp:
+        bi = simfront.compile_map(src, "build_blocked")
+        assert bi["bs"] == 9
+        X = HostMap(bi, tmp + "/").assemble(ep, sl, n, {"x": xs})
+    with tempfile.TemporaryDirectory() as tmp:
+        vx = HostMap(simfront.compile_map(src, "promote"), tmp).assemble(ep, None, n, {"x": xs})
+    y = oracle.spmv(n, 9, rp, ci, X, vx)
+    with tempfile.TemporaryDirectory() as tmp:
+        si = simfront.compile_map(src, "sum_vectors")
+        assert si["fields"] == [("arg", "y", (3, 3), "int")]
+        z = HostMap(si, tmp).assemble(ep, None, n, {"y": y})
+    assert z.tolist() == [81, 324, 729]
+
+
+def nested_blocks_expected(n, links, w, s):
+    """tests/sim/nested_blocks.sim restated with numpy, in the maps' order of
+    operations: K (per pattern slot, 6x6 row-major, slots in element order),
+    v (6 per node), m (2 per node)."""
+    K = {}
+
+    def add(r, c, blk):
+        K[(r, c)] = K.get((r, c), np.zeros((6, 6))) + blk
+
+    m = np.zeros((n, 2))
+    for e, (p0, p1) in enumerate(links):
+        B = np.zeros((6, 6))
+        for a in range(3):
+            for b in range(3):
+                for c in range(2):
+                    for d in range(2):
+                        B[a * 2 + c, b * 2 + d] = (w[e] * ((1.0 + a) + 2.0 * b) + 0.5 * c) - 0.25 * d
+        add(p0, p0, B)
+        add(p1, p1, B)
+        C = np.zeros((6, 6))
+        C[1 * 2 + 0, 2 * 2 + 1] = -w[e]
+        add(p0, p1, C)
+        D = np.zeros((6, 6))
+        D[2 * 2 + 0, 0] = w[e]
+        D[2 * 2 + 1, 1] = 2.0 * w[e]
+        add(p1, p0, D)
+        m[p0, 0] += 1.0
+        m[p1, 1] += w[e]
+    v = np.zeros((n, 6))
+    v[:, 0::2] = s[:, None]
+    v[:, 1::2] = -s[:, None]
+    v[:, 3] = -s + 2.0 * s
+    return K, v.reshape(-1), m.reshape(-1)
+
+
+def _nested_case(oracle, n=12, nl=30, seed=41):
+    g = meshgen.rng(seed)
+    a = g.integers(0, n, nl)
+    b = (a + g.integers(1, n, nl)) % n
+    links = np.stack([a, b], 1).astype(np.int32)
+    w = g.uniform(0.5, 2.0, nl)
+    s = g.uniform(-1.0, 1.0, n)
+    rp, ci = oracle.pattern(n, links.reshape(-1), 2)
+    return links, w, s, rp, ci
+
+
+def test_own_nested_blocks_match_restatement(oracle):
+    """tests/sim/nested_blocks.sim on the host: the nested matrix and vector
+    results bit for bit against the numpy restatement, and the map over a
+    system-vector argument against K v reduced by hand."""
+    src = _own("nested_blocks.sim")
+    n = 12
+    links, w, s, rp, ci = _nested_case(oracle, n)
+    slots = oracle.slots(links.reshape(-1), 2, rp, ci)
+    Kw, vw, mw = nested_blocks_expected(n, links, w, s)
+    with tempfile.TemporaryDirectory() as tmp:
+        K = HostMap(simfront.compile_map(src, "couple"), tmp).assemble(
+            links.reshape(-1), slots, len(ci), {"w": w})
+    for r in range(n):
+        for k in range(rp[r], rp[r + 1]):
+            want = Kw.get((r, int(ci[k])), np.zeros((6, 6)))
+            assert np.array_equal(K[k * 36:(k + 1) * 36].reshape(6, 6), want), (r, ci[k])
+    ep = np.arange(n, dtype=np.int32)
+    with tempfile.TemporaryDirectory() as tmp:
+        v = HostMap(simfront.compile_map(src, "spread"), tmp).assemble(ep, None, n, {"s": s})
+    assert np.array_equal(v, vw)
+    with tempfile.TemporaryDirectory() as tmp:
+        m = HostMap(simfront.compile_map(src, "mark"), tmp).assemble(
+            links.reshape(-1), None, n, {"w": w})
+    assert np.array_equal(m, mw)
+    y = oracle.spmv(n, 6, rp, ci, K, v)
+    with tempfile.TemporaryDirectory() as tmp:
+        z = HostMap(simfront.compile_map(src, "weigh"), tmp).assemble(ep, None, n, {"y": y})
+    Y = y.reshape(n, 3, 2)
+    want = np.zeros(n)
+    for a in range(3):
+        want = (want + (a + 1.0) * Y[:, a, 0]) - Y[:, a, 1]
+    assert np.array_equal(z, want)
+
+
+def test_own_nine_by_nine_nested_diagonal(oracle):
+    """tests/sim/nested_blocks.sim's fill9 / lift9 / total9: the blocked
+    assembly test's values (81, 324, 729 for k = 1, 2, 3) through this
+    repository's program, on the host."""
+    src = _own("nested_blocks.sim")
+    n = 3
+    k = np.array([1, 2, 3], np.int32)
+    ep = np.arange(n, dtype=np.int32)
+    rp, ci, sl = _diag(n)
+    with tempfile.TemporaryDirectory() as tmp:
+        X = HostMap(simfront.compile_map(src, "fill9"), tmp).assemble(ep, sl, n, {"k": k})
+    with tempfile.TemporaryDirectory() as tmp:
+        x = HostMap(simfront.compile_map(src, "lift9"), tmp).assemble(ep, None, n, {"k": k})
+    y = oracle.spmv(n, 9, rp, ci, X, x)
+    with tempfile.TemporaryDirectory() as tmp:
+        z = HostMap(simfront.compile_map(src, "total9"), tmp).assemble(ep, None, n, {"y": y})
+    assert z.tolist() == [81, 324, 729]
+
+
+@pytest.mark.parametrize("func", ["couple", "spread", "weigh", "mark", "fill9", "lift9",
+                                  "total9"])
+def test_own_nested_block_maps_compile(func):
+    import torch
+    r = simfront.compile_map(_own("nested_blocks.sim"), func)
+    for dt in (torch.float32, torch.float64):
+        _nvrtc_check(r["source"], r["card"], r["bs"], dt, vector=r["kind"] == "vector")
