@@ -37,6 +37,9 @@ def parse():
                          "solutions are compared to (48: about 15-25 s of one core)")
     ap.add_argument("--no-tune", action="store_true",
                     help="default schedules instead of the autotuners' choices")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the heat / neo-Hookean / springs / cloth measurements that "
+                         "follow the headline")
     ap.add_argument("--no-cpu", action="store_true",
                     help="skip the CPU baseline and the solution check against the oracle")
     ap.add_argument("--no-block-jacobi", action="store_true",
@@ -168,7 +171,7 @@ def run_neo(args):
     out["fp32_bulk_rel_error_vs_fp64"] = float(np.linalg.norm(sols["fp32_bulk"] - sols["fp64"]) /
                                                np.linalg.norm(sols["fp64"]))
     out["speedup_solve"] = out["fp64"]["solve_ms"] / out["fp32_bulk"]["solve_ms"]
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_springs(args):
@@ -238,7 +241,7 @@ def run_springs(args):
         oracle.springs_step(0, xc, vc, m, L["fixed"], ep, k, L["l0"], h, 0.0, grav, orp, oci,
                             1e-16, 10000)  # r.r <= 1e-16
     cpu_step_ms = (time.perf_counter() - t0) * 1e3 / steps
-    print(json.dumps({
+    return {
         "workload": "springs createBox 10^3 (1000 vertices, 2700 springs, nnzb %d), 10 implicit "
                     "steps, FP64, CG to 1e-8" % mesh.nnzb,
         "pattern_ms": pattern_ms, "assembly_ms_median": float(np.median(asm_ms)),
@@ -248,7 +251,7 @@ def run_springs(args):
                    "assembled_values_max_rel_diff": vals_err,
                    "positions_rel_diff_after_10_steps":
                        float(np.linalg.norm(xg - xo) / np.linalg.norm(xo))},
-        "cpu_oracle_step_ms": cpu_step_ms, "cpu_cores": 1}), flush=True)
+        "cpu_oracle_step_ms": cpu_step_ms, "cpu_cores": 1}
 
 
 def run_heat(args):
@@ -303,7 +306,7 @@ def run_heat(args):
         out[name] = {"assembly_ms": ms_asm, "spmv_ms": ms_spmv, "spmv_GBps": nbytes / ms_spmv / 1e6,
                      "spmv_1000_ms": ms_spmv * 1000, "solve_ms": ms_solve, "iters": r.iters,
                      "relres": (r.true_normr2 / r.bnorm2) ** 0.5}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_cloth(args, rank=0, world=1, local=0):
@@ -383,8 +386,8 @@ def run_cloth(args, rank=0, world=1, local=0):
         item[-1].close()
     n_all = sgd.sum_over_ranks(h["n"], "cuda")
     if rank != 0:
-        return
-    print(json.dumps({"workload": "batched cloth: %d sheets, sides U{32..256}, %d vertices, "
+        return None
+    return {"workload": "batched cloth: %d sheets, sides U{32..256}, %d vertices, "
                                   "implicit springs (stretch 5e3, bend 50), PCG to 1e-6"
                                   % (args.sheets, n_all), "n_gpus": world,
                       "scaling": "strong" if world > 1 else None,
@@ -392,7 +395,7 @@ def run_cloth(args, rank=0, world=1, local=0):
                       "speedup": seq_ms / batched_ms, "all_converged": ok,
                       "iters_max": int(iters.max()), "iters_mean": float(iters.mean()),
                       "autotuned_config": cb.config, "dofs": int(n_all) * 3,
-                      "DOF_per_s_batched": n_all * 3 / (batched_ms / 1e3)}), flush=True)
+                      "DOF_per_s_batched": n_all * 3 / (batched_ms / 1e3)}
 
 
 def run_solve_only(args):
@@ -1167,7 +1170,35 @@ def run_ours(args, rank, world, local):
         "solution_relerr_vs_fp64_oracle": parity,
         "tuned": _tuned_summary(prob.tuned),
     }
+    if rank == 0 and world == 1 and not args.no_secondary:
+        out["secondary"] = run_secondary(args)
     print(json.dumps(out), flush=True)
+
+
+def run_secondary(args):
+    """The other workloads of the path, measured after the headline and
+    outside its timed region, each in its own process (`bench.py --heat`,
+    `--neo`, `--springs`, `--cloth`): P1 heat 128^3 (SpMVs and CG), one
+    neo-Hookean Newton step at 64^3, the springs createBox 10^3 steps and the
+    batched cloth sheets.  Each entry carries its wall time and exit code; a
+    run that fails records its error instead of its numbers."""
+    out = {}
+    for name, extra in (("heat", ["--size", "128"]), ("neo", ["--size", "64"]),
+                        ("springs", []), ("cloth", ["--sheets", str(args.sheets)])):
+        cmd = [sys.executable, os.path.abspath(__file__), "--" + name,
+               "--steps", str(args.steps), "--warmup", str(args.warmup)] + extra
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            res = json.loads(lines[-1]) if lines else {
+                "error": (r.stderr or r.stdout)[-400:]}
+            res["exit_code"] = r.returncode
+        except Exception as e:  # a secondary workload must not cost the headline line
+            res = {"error": "%s: %s" % (type(e).__name__, e)}
+        res["wall_s"] = time.perf_counter() - t0
+        out[name] = res
+    return out
 
 
 def time_jit_stiffness(ctx, prob):
@@ -1233,20 +1264,17 @@ def main():
         return
     if args.cloth:
         rank, world, local = dist_setup(args)
-        run_cloth(args, rank, world, local)
+        res = run_cloth(args, rank, world, local)
+        if res is not None:
+            print(json.dumps(res), flush=True)
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
         return
-    if args.neo:
-        run_neo(args)
-        return
-    if args.heat:
-        run_heat(args)
-        return
-    if args.springs:
-        run_springs(args)
-        return
+    for flag, fn in (("neo", run_neo), ("heat", run_heat), ("springs", run_springs)):
+        if getattr(args, flag):
+            print(json.dumps(fn(args)), flush=True)
+            return
     rank, world, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)

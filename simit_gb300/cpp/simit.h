@@ -195,3 +195,4 @@ template <typename T, int... dims> T *FieldRef<T, dims...>::ptr(ElementRef e) co
 
 #include "reorder.h"
 #include "simit_function.h"
+#include "map.h"

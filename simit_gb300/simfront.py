@@ -1557,15 +1557,21 @@ class SimMap:
     returns the matrix values [nnzb * bs * bs] in the mesh's pattern, or the
     vector [n * bs]."""
 
-    def __init__(self, ctx, src, func, args=None, result=None, dtype=None, exact=True):
+    def __init__(self, ctx, src, func, args=None, result=None, dtype=None, exact=True,
+                 info=None):
         import torch
         from .runtime import JitAssembly, JitVectorAssembly
-        self.info = compile_map(src, func, args, result)
+        self.info = info if info is not None else compile_map(src, func, args, result)
         self.card, self.bs = self.info["card"], self.info["bs"]
         self.fields = self.info["fields"]
         cls = JitVectorAssembly if self.info["kind"] == "vector" else JitAssembly
         self.jit = cls(ctx, self.info["source"], self.card, self.bs,
                        dtype=torch.float64 if dtype is None else dtype, exact=exact)
+
+    @classmethod
+    def from_info(cls, ctx, info, dtype=None, exact=True):
+        """A map from compile_map's result."""
+        return cls(ctx, None, None, dtype=dtype, exact=exact, info=info)
 
     def field_arrays(self, fields):
         """The arrays in the generated source's order, each in its declared

@@ -315,3 +315,40 @@ def test_sim_nine_by_nine_nested_blocks(ctx, dtype):
     assert z[:n].cpu().numpy().tolist() == (81 * k.astype(np.int64) ** 2).tolist()
     for sm in maps.values():
         sm.close()
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_sim_assembly_forms_give_reference_test_values(ctx, dtype):
+    """tests/sim/assembly_forms.sim on the GPU, on the inputs of the
+    reference's vector assembly tests (test/assembly-tests.cpp:12-217): maps
+    over the vertices and over the edges themselves, over edge sets of one,
+    two and three endpoints, and two-result maps whose matrix times vector
+    is taken by the blocked SpMV give those tests' values exactly."""
+    from simit_gb300.runtime import Mesh, bspmv
+    from tests.test_simfront_cpu import OWN_FORMS, VECTOR_ASSEMBLY_CASES, run_vector_case
+    keep = []
+
+    def vmap(info, n, ep, fields):
+        mesh = Mesh(ctx, n, ep, info["card"])
+        sm = simfront.SimMap.from_info(ctx, info, dtype=dtype)
+        keep.append(sm)
+        return sm.assemble(mesh, fields)
+
+    def mmap(info, n, ep, fields):
+        mesh = Mesh(ctx, n, ep, info["card"])
+        sm = simfront.SimMap.from_info(ctx, info, dtype=dtype)
+        keep.append(sm)
+        keep.append(mesh)
+        return sm.assemble(mesh, fields), mesh.pattern.rowptr, mesh.pattern.colidx
+
+    def spmv(n, rp, ci, A, x):
+        return bspmv(ctx, n, 1, rp, ci, A, x)
+
+    src = _own("assembly_forms.sim")
+    for case in VECTOR_ASSEMBLY_CASES:
+        got = run_vector_case(case, src, OWN_FORMS, vmap, mmap, spmv)
+        ctx.sync()
+        assert got[:case[1]].cpu().tolist() == case[5], case[0]
+    for sm in keep:
+        if isinstance(sm, simfront.SimMap):
+            sm.close()

@@ -209,9 +209,14 @@ extern "C" void sim_assemble(long long nE, const int *ep_all, const real *const 
 class HostMap:
     """The generated element function compiled for the host."""
 
+    _count = 0
+
     def __init__(self, info, tmp):
-        src = os.path.join(tmp, "gen.cpp")
-        so = os.path.join(tmp, "gen.so")
+        # a fresh file name per library: dlopen hands back an already loaded
+        # library for a path it has seen
+        HostMap._count += 1
+        src = os.path.join(tmp, "gen%d.cpp" % HostMap._count)
+        so = os.path.join(tmp, "gen%d.so" % HostMap._count)
         text = HARNESS_VEC if info.get("kind") == "vector" else HARNESS
         with open(src, "w") as f:
             f.write(text % {"bs": info["bs"], "card": info["card"], "source": info["source"]})
@@ -652,3 +657,90 @@ def test_own_nested_block_maps_compile(func):
     r = simfront.compile_map(_own("nested_blocks.sim"), func)
     for dt in (torch.float32, torch.float64):
         _nvrtc_check(r["source"], r["card"], r["bs"], dt, vector=r["kind"] == "vector")
+
+
+# ---------------------------------------------------------------------------
+# the reference's vector assembly tests (test/assembly-tests.cpp:12-217):
+# maps over the vertices, over the edges themselves, over edge sets of one,
+# two and three endpoints, and maps with two results whose product is taken
+# ---------------------------------------------------------------------------
+# (test, n vertices, endpoints (None: a map over the vertices, "self": over
+#  the edges), card, field values, expected)
+VECTOR_ASSEMBLY_CASES = [
+    ("vertices", 3, None, 1, [1, 2, 3], [2, 4, 6]),
+    ("vertices_two_results", 3, None, 1, [1, 2, 3], [6, 24, 54]),
+    ("edges_no_endpoints", 2, "self", 1, [1, 2], [2, 4]),
+    ("edges_unary", 3, [0, 2], 1, None, [1, 0, 1]),
+    ("edges_binary", 3, [0, 1, 1, 2], 2, None, [1, 2, 1]),
+    ("edges_tertiary", 4, [0, 1, 2, 1, 2, 3], 3, [10, 1], [10, 11, 11, 1]),
+    ("edges_two_results", 3, [0, 1, 1, 2], 2, [1, 2], [43, 177, 168]),
+]
+
+# the reference program's function and field of each test
+_REF_FORMS = {"vertices": ("asm", "a"), "vertices_two_results": ("f", "a"),
+              "edges_no_endpoints": ("f", "a"), "edges_unary": ("asm", None),
+              "edges_binary": ("asm", None), "edges_tertiary": ("dist", "a"),
+              "edges_two_results": ("f", "a")}
+# this repository's tests/sim/assembly_forms.sim
+OWN_FORMS = {"vertices": ("twice", "a"), "vertices_two_results": ("scaled", "a"),
+             "edges_no_endpoints": ("own", "w"), "edges_unary": ("touch1", None),
+             "edges_binary": ("touch2", None), "edges_tertiary": ("spread3", "w"),
+             "edges_two_results": ("both", "w")}
+
+
+def run_vector_case(case, src, forms, vector_map, matrix_map, spmv):
+    """One case through caller-given runners: vector_map(info, n, ep, fields)
+    and matrix_map(info, n, ep, fields) -> (values, rowptr, colidx);
+    spmv(n, rowptr, colidx, values, x).  Returns the case's result."""
+    name, n, ep, card, vals, _ = case
+    func, field = forms[name]
+    fields = {} if field is None else {field: np.array(vals, np.float64)}
+    if ep is None or ep == "self":
+        ep = np.arange(n, dtype=np.int32)
+    ep = np.asarray(ep, np.int32)
+    if name.endswith("two_results"):
+        names = [r for r, _ in simfront.parse(src)["funcs"][func]["results"]]
+        vres = simfront.compile_map(src, func, result=names[0])
+        mres = simfront.compile_map(src, func, result=names[1])
+        assert vres["kind"] == "vector" and mres["kind"] == "matrix"
+        b = vector_map(vres, n, ep, fields)
+        A, rp, ci = matrix_map(mres, n, ep, fields)
+        return spmv(n, rp, ci, A, b)
+    info = simfront.compile_map(src, func)
+    assert info["kind"] == "vector" and info["card"] == card
+    return vector_map(info, n, ep, fields)
+
+
+def _host_runners(oracle, tmp):
+    def vmap(info, n, ep, fields):
+        return HostMap(info, tmp).assemble(ep, None, n, fields)
+
+    def mmap(info, n, ep, fields):
+        rp, ci = oracle.pattern(n, ep, info["card"])
+        sl = oracle.slots(ep, info["card"], rp, ci)
+        return HostMap(info, tmp).assemble(ep, sl, len(ci), fields), rp, ci
+
+    def spmv(n, rp, ci, A, x):
+        return oracle.spmv(n, 1, rp, ci, A, x)
+    return vmap, mmap, spmv
+
+
+@pytest.mark.parametrize("case", VECTOR_ASSEMBLY_CASES, ids=[c[0] for c in VECTOR_ASSEMBLY_CASES])
+def test_reference_vector_assembly(oracle, case):
+    """The reference's own program of each test, its maps generated and
+    compiled for the host, its main's product taken by the oracle's SpMV:
+    the test's asserted values."""
+    src = _ref("test/input/assembly/%s.sim" % case[0])
+    with tempfile.TemporaryDirectory() as tmp:
+        got = run_vector_case(case, src, _REF_FORMS, *_host_runners(oracle, tmp))
+    assert got.tolist() == case[5]
+
+
+@pytest.mark.parametrize("case", VECTOR_ASSEMBLY_CASES, ids=[c[0] for c in VECTOR_ASSEMBLY_CASES])
+def test_own_assembly_forms(oracle, case):
+    """tests/sim/assembly_forms.sim on the same inputs, on the host: the same
+    values."""
+    with tempfile.TemporaryDirectory() as tmp:
+        got = run_vector_case(case, _own("assembly_forms.sim"), OWN_FORMS,
+                              *_host_runners(oracle, tmp))
+    assert got.tolist() == case[5]
