@@ -1265,9 +1265,11 @@ class _Gen:
                 self.component_write("(%s) * %d + %s" % (row, bs, col), self.as_scalar(v),
                                      opn, ref)
             elif nest is not None and len(cidx) == 2:
-                # an inner block X(p, q)(ii, jj) = B (b x b) or a scalar
+                # an inner block X(p, q)(ii, jj) = B (b x b); a scalar lands
+                # on the inner block's entry (0, 0)
                 nb = nest[1]
-                self.emit("for (int u_ = 0; u_ < %d; ++u_) {" % (nb * nb))
+                self.emit("for (int u_ = 0; u_ < %d; ++u_) {" % (1 if self.is_scalar_val(v)
+                                                                 else nb * nb))
                 self.ind += 1
                 x = self.value_at(v, "u_", nb * nb, line)
                 self.component_write("((%s) * %d + u_ / %d) * %d + (%s) * %d + u_ %% %d"
@@ -1294,14 +1296,18 @@ class _Gen:
                 self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_term_(blk, nt_)[q_ / %d][q_ %% %d] "
                           "+= %s[q_];" % (bs * bs, bs, bs, v.code))
             elif v.kind != "tensor" or _size(v.shape) == 1:
-                # a scalar fills the block (bs == 1: the block's one entry)
-                self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_term_(blk, nt_)[q_ / %d][q_ %% %d] "
-                          "+= %s;" % (bs * bs, bs, bs, self.as_scalar(v)))
+                # a scalar written to a block lands on its entry (0, 0) alone,
+                # as the lowered write `K[loc*bs*bs] += value` does (a fixed
+                # point's `MD(p,p) = 1.0` in the springs programs)
+                self.emit("sg_term_(blk, nt_)[0][0] += %s;" % self.as_scalar(v))
             else:
                 raise SimError("line %d: a value of shape %s written to a %dx%d block"
                                % (line, v.shape if v.kind == "tensor" else (), bs, bs))
         self.ind -= 1
         self.emit("}")
+
+    def is_scalar_val(self, v):
+        return v.kind != "tensor" or _size(v.shape) == 1
 
     def value_at(self, v, q, n, line):
         """Entry q of an n-entry value, or the value itself if scalar."""
@@ -1347,9 +1353,10 @@ class _Gen:
                 self.component_write("(%s) * %d + (%s)" % (cidx[0], nest[1], cidx[1]),
                                      self.as_scalar(v), opn, ref)
             elif len(cidx) == 1 and nest is not None:
-                # a row x(p)(ii) = w (b entries) or a scalar
+                # a row x(p)(ii) = w (b entries); a scalar lands on its first
                 nb = nest[1]
-                self.emit("for (int u_ = 0; u_ < %d; ++u_) {" % nb)
+                self.emit("for (int u_ = 0; u_ < %d; ++u_) {" % (1 if self.is_scalar_val(v)
+                                                                 else nb))
                 self.ind += 1
                 self.component_write("(%s) * %d + u_" % (cidx[0], nb),
                                      self.value_at(v, "u_", nb, line), opn, ref)
@@ -1367,9 +1374,9 @@ class _Gen:
                 self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_vterm_(vec, nt_)[q_] += %s[q_];"
                           % (bs, v.code))
             elif v.kind != "tensor" or _size(v.shape) == 1:
-                # a scalar fills the vertex's entries
-                self.emit("for (int q_ = 0; q_ < %d; ++q_) sg_vterm_(vec, nt_)[q_] += %s;"
-                          % (bs, self.as_scalar(v)))
+                # a scalar lands on the vertex's first entry alone (the
+                # lowered write `f[p*bs] += value`)
+                self.emit("sg_vterm_(vec, nt_)[0] += %s;" % self.as_scalar(v))
             else:
                 raise SimError("line %d: a value of shape %s written to a %d-vector"
                                % (line, v.shape if v.kind == "tensor" else (), bs))

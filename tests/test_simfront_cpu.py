@@ -744,3 +744,42 @@ def test_own_assembly_forms(oracle, case):
         got = run_vector_case(case, _own("assembly_forms.sim"), OWN_FORMS,
                               *_host_runners(oracle, tmp))
     assert got.tolist() == case[5]
+
+
+def test_reference_isprings_maps_match_oracle(oracle):
+    """test/input/program/isprings.sim's two maps generated and compiled for
+    the host -- compute_mass_damping over the points (a fixed point's
+    `MD(p,p) = 1.0`, a scalar written to a 3x3 block, lands on entry (0,0)
+    alone, as in the lowered program) and compute_elasticity over the
+    springs -- then MDK = MD + K in the lowered order: the oracle's MDK and
+    f bit for bit."""
+    src = _ref("test/input/program/isprings.sim")
+    L = meshgen.springs_lattice(4, 4, 4, 0.1, 0.01, seed=3)
+    n, ep = L["n"], L["ep"]
+    g = meshgen.rng(61)
+    fixed = g.uniform(0, 1, n) < 0.2
+    v = g.uniform(-0.1, 0.1, n * 3)
+    m = g.uniform(0.5, 1.5, n)
+    k = g.uniform(50.0, 150.0, len(L["l0"]))
+    rp, ci = oracle.pattern(n, ep, 2)
+    sl = oracle.slots(ep, 2, rp, ci)
+    prp, pci, psl = _diag(n)
+    pts = np.arange(n, dtype=np.int32)
+    vf = {"x": L["x"], "v": v, "m": m, "fixed": fixed, "k": k, "l0": L["l0"]}
+    with tempfile.TemporaryDirectory() as tmp:
+        MD = HostMap(simfront.compile_map(src, "compute_mass_damping", result="MD"),
+                     tmp).assemble(pts, psl, n, vf)
+        fmg = HostMap(simfront.compile_map(src, "compute_mass_damping", result="fmg"),
+                      tmp).assemble(pts, None, n, vf)
+        K = HostMap(simfront.compile_map(src, "compute_elasticity", result="K"),
+                    tmp).assemble(ep, sl, len(ci), vf)
+        fe = HostMap(simfront.compile_map(src, "compute_elasticity", result="fe"),
+                     tmp).assemble(ep, None, n, vf)
+    blocks = MD.reshape(n, 3, 3)
+    assert np.array_equal(blocks[fixed], np.tile([[1.0, 0, 0], [0, 0, 0], [0, 0, 0]],
+                                                 (int(fixed.sum()), 1, 1)))
+    MDK = oracle.add_diag(n, 3, rp, ci, K, diag=MD)
+    wA, wf = oracle.springs_assemble(1, L["x"], v, m, fixed.astype(np.uint8), ep, k, L["l0"],
+                                     1e-2, 1e-1, np.array([0.0, 0.0, -9.81]), rp, ci)
+    assert np.array_equal(MDK, wA)
+    assert np.array_equal(fmg + fe, wf)
