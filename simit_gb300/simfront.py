@@ -1019,7 +1019,13 @@ class _Gen:
                 outs.append(_Val("int" if rty[1] == "int" else "scalar", tn))
             else:
                 outs.append(_Val("tensor", self.new_tensor(shape), shape))
-        argc = [a.code if a.kind == "tensor" else self.as_scalar(a) for a in args]
+        argc = []
+        for a in args:
+            if a.kind == "element":
+                continue              # the helper has the map's element as `e`
+            argc.append(a.code if a.kind in ("tensor", "vertex") else self.as_scalar(a))
+        # every helper sees the map's element, endpoints and fields
+        argc += ["e", "ep", "f"]
         self.emit("%s(%s);" % (name, ", ".join(argc + [o.code for o in outs])))
         if len(outs) != nout:
             raise SimError("%s returns %d values, %d expected" % (f["name"], len(outs), nout))
@@ -1037,9 +1043,17 @@ class _Gen:
         sub = _Gen(self.prog, self.consts, self.st)
         params, env = [], {}
         for (an, aty, _), av in zip(f["args"], args):
+            if aty[0] == "element" and av.kind == "element":
+                env[an] = _Val("element", "e", elem=av.elem)
+                continue
+            if aty[0] == "element" and av.kind == "vertex":
+                # an endpoint: its local index
+                params.append("int a_%s" % an)
+                env[an] = _Val("vertex", "a_" + an, elem=av.elem)
+                continue
             if aty[0] not in ("scalar", "tensor"):
-                raise SimError("%s: only scalar and tensor arguments in called functions"
-                               % f["name"])
+                raise SimError("%s: only scalar, tensor and element arguments in called "
+                               "functions" % f["name"])
             sh = _shape_of_type(aty)
             cn = "a_" + an
             if sh == ():
@@ -1052,6 +1066,9 @@ class _Gen:
                                    % (f["name"], an, sh))
                 params.append("const real *%s" % cn)
                 env[an] = _Val("tensor", cn, sh)
+        params += ["long long e", "const int *ep", "const real *const *f"]
+        sub.emit("(void)e; (void)ep; (void)f;")
+        sub.vertex_map = self.vertex_map
         # results start from zero, as every local tensor does
         for rn, rty in f["results"]:
             sh = _shape_of_type(rty)
