@@ -4,9 +4,11 @@
 //   test/program-isprings.cpp:91-175  (TEST(Program, isprings))
 //   test/program-cg-test.cpp:10-44    (TEST(Program, cg))
 //   test/program-fem-test.cpp:14-106  (TEST(Program, femTet), bar2k mesh)
-//   test/reorder-tests.cpp:406-441    (TEST(Program, reorderFemSpecificTest): the
-//                                      same run on the Hilbert-reordered mesh)
+//   test/reorder-tests.cpp:403-471    (reorderFemSpecificTest: the same run on
+//                                      the Hilbert-reordered mesh; reorderFemTest,
+//                                      reorderCube: reordered against original)
 // Exit code 0 when every value is within 1e-13 (SIMIT_ASSERT_FLOAT_EQ).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -109,13 +111,16 @@ static bool load_tet(const std::string &prefix, std::vector<double> &xv,
   return true;
 }
 
-static void test_femtet(const std::string &golden_dir, bool reordered) {
+// femTet (test/program-fem-test.cpp:14-106's set-up) for 10 steps on the
+// TetGen mesh `prefix`, optionally reordered first (test/reorder-tests.cpp:
+// the femTest helper); the positions of the vertices by original index.
+static std::vector<double> run_femtet(const std::string &prefix, bool reordered) {
   std::vector<double> xv;
   std::vector<std::array<int, 4>> ev;
-  if (!load_tet(golden_dir + "/bar2k", xv, ev)) {
-    std::printf("FAIL cannot read %s/bar2k\n", golden_dir.c_str());
+  if (!load_tet(prefix, xv, ev)) {
+    std::printf("FAIL cannot read %s\n", prefix.c_str());
     ++g_fail;
-    return;
+    return {};
   }
   Set verts;
   Set tets(verts, verts, verts, verts);
@@ -168,15 +173,45 @@ static void test_femtet(const std::string &golden_dir, bool reordered) {
   step.bind("tets", &tets);
   step.init();
   for (int i = 0; i < 10; ++i) step.runSafe();
-  ASSERT_NEAR13(0.010771915616785779, x.get(refs[at[100]])(0));
-  ASSERT_NEAR13(0.058853573999788439, x.get(refs[at[100]])(1));
-  ASSERT_NEAR13(0.030899457015375883, x.get(refs[at[100]])(2));
-  ASSERT_NEAR13(0.0028221631202928516, x.get(refs[at[200]])(0));
-  ASSERT_NEAR13(0.017969982607667911, x.get(refs[at[200]])(1));
-  ASSERT_NEAR13(0.012885386063393013, x.get(refs[at[200]])(2));
-  ASSERT_NEAR13(0.02411959295647129, x.get(refs[at[300]])(0));
-  ASSERT_NEAR13(0.052036155669135678, x.get(refs[at[300]])(1));
-  ASSERT_NEAR13(0.030173075240629205, x.get(refs[at[300]])(2));
+  std::vector<double> out(xv.size());
+  for (size_t i = 0; i < at.size(); ++i)
+    for (int q = 0; q < 3; ++q) out[i * 3 + q] = x.get(refs[at[i]])(q);
+  return out;
+}
+
+// TEST(Program, femTet) and, reordered, TEST(Program, reorderFemSpecificTest):
+// the golden displacements of vertices 100, 200 and 300.
+static void test_femtet(const std::string &golden_dir, bool reordered) {
+  std::vector<double> x = run_femtet(golden_dir + "/bar2k", reordered);
+  if (x.empty()) return;
+  ASSERT_NEAR13(0.010771915616785779, x[100 * 3 + 0]);
+  ASSERT_NEAR13(0.058853573999788439, x[100 * 3 + 1]);
+  ASSERT_NEAR13(0.030899457015375883, x[100 * 3 + 2]);
+  ASSERT_NEAR13(0.0028221631202928516, x[200 * 3 + 0]);
+  ASSERT_NEAR13(0.017969982607667911, x[200 * 3 + 1]);
+  ASSERT_NEAR13(0.012885386063393013, x[200 * 3 + 2]);
+  ASSERT_NEAR13(0.02411959295647129, x[300 * 3 + 0]);
+  ASSERT_NEAR13(0.052036155669135678, x[300 * 3 + 1]);
+  ASSERT_NEAR13(0.030173075240629205, x[300 * 3 + 2]);
+}
+
+// TEST(Program, reorderFemTest) / reorderCube (test/reorder-tests.cpp:
+// 453-471): every vertex of the reordered run within 1e-5 of the original
+// run (SIMIT_ASSERT_FLOAT_NEAR_EQ).
+static void test_reorder_invariance(const std::string &prefix) {
+  std::vector<double> a = run_femtet(prefix, false), b = run_femtet(prefix, true);
+  if (a.empty() || a.size() != b.size()) {
+    std::printf("FAIL %s: runs of different sizes\n", prefix.c_str());
+    ++g_fail;
+    return;
+  }
+  double worst = 0;
+  for (size_t i = 0; i < a.size(); ++i) worst = std::max(worst, std::fabs(a[i] - b[i]));
+  if (!(worst <= 1e-5)) {
+    std::printf("FAIL %s: reordered run differs by %.3g\n", prefix.c_str(), worst);
+    ++g_fail;
+  }
+  std::printf("reorder %s: max |x_reordered - x| = %.3g\n", prefix.c_str(), worst);
 }
 
 static void test_bind_errors() {
@@ -201,6 +236,8 @@ int main(int argc, char **argv) {
     test_cg();
     test_femtet(golden, false);
     test_femtet(golden, true);
+    test_reorder_invariance(golden + "/bar2k");
+    test_reorder_invariance(golden + "/cube");
     test_bind_errors();
   } catch (const std::exception &e) {
     std::printf("FAIL exception: %s\n", e.what());

@@ -11,6 +11,8 @@ rewrites only lattice_golden.json.
                           extracted from their sources (file:line recorded),
                           including the incidence-matrix assembly tests
   bar2k.node, bar2k.ele   the TetGen fixture test/program-fem-test.cpp loads
+  cube.node, cube.ele     the 8-vertex TetGen fixture test/reorder-tests.cpp's
+                          reorderCube loads
   tetgen_golden.json      the TetGen .node/.ele/.edge texts of
                           test/mesh-test.cpp (TetgenTest, TetgenEdgeTest)
                           with the values those tests assert
@@ -154,9 +156,10 @@ def main():
                         "asserts": extract_assert_eq(mesh_test, name)}
     with open(os.path.join(HERE, "tetgen_golden.json"), "w") as f:
         json.dump(tetgen, f, indent=1)
-    for ext in ("node", "ele"):
-        shutil.copy(os.path.join(test, "input", "program", "fem", "bar2k." + ext),
-                    os.path.join(HERE, "bar2k." + ext))
+    for mesh in ("bar2k", "cube"):
+        for ext in ("node", "ele"):
+            shutil.copy(os.path.join(test, "input", "program", "fem", mesh + "." + ext),
+                        os.path.join(HERE, mesh + "." + ext))
 
     sys.path.insert(0, REPO)
     from oracle import oracle
