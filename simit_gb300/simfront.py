@@ -755,6 +755,11 @@ class _Gen:
         raise SimError("field %r of a value that is not an element" % e[2])
 
     def field(self, e, env):
+        if e[1][0] == "name" and e[1][1] in env and env[e[1][1]].kind == "tuple":
+            tv = env[e[1][1]]
+            names = getattr(tv, "names", [])
+            if e[2] in names:
+                return _Val("vertex", str(names.index(e[2])), elem=tv.elem)
         ptr, shape, dt, idx = self.field_base(e, env)
         if shape == ():
             return _Val({"int": "int", "bool": "bool"}.get(dt, "scalar"), "%s[%s]" % (ptr, idx))
@@ -1521,10 +1526,12 @@ def compile_map(src, func, args=None, result=None):
         elif aty[0] == "tuple":
             members = aty[1]
             kinds = {m[1] for m in members}
-            if len(kinds) != 1 or any(m[0] for m in members):
+            if len(kinds) != 1:
                 raise SimError("endpoint tuples of one element type only")
             vert, card = kinds.pop(), len(members)
             env[an] = _Val("tuple", None, elem=vert)
+            # named members, (src : Vertex, dst : Vertex): v.src is endpoint 0
+            env[an].names = [m[0] for m in members]
         else:
             raise SimError("map argument %r of type %r" % (an, aty[0]))
     if elem is None:

@@ -1,12 +1,17 @@
-"""The reference's gemv tests (test/system-gemv-tests.cpp) through the
-reference's own programs (test/input/system/*.sim): each program's map
-function generated by the `.sim` front end and compiled for the host, its
-`main` restated here step by step (the map's matrix, scalings, sums of
-matrices, the blocked SpMV from the oracle), on the sets the test builds,
-against the values the test asserts.  Sets, field values and assertions are
-read from the test file itself.  The reference checkout is found in
-SIMIT_REFERENCE, else `reference` beside the repository; the tests skip
-without it."""
+"""The reference's system tests through the reference's own programs
+(test/input/system/*.sim): each program's map functions generated by the
+`.sim` front end and compiled for the host, its `main` restated here step
+by step, on the sets the test builds, against the values the test asserts.
+Sets, field values and assertions are read from the test files themselves.
+
+* test/system-gemv-tests.cpp: the map's matrix, scalings, sums of
+  matrices, the blocked SpMV from the oracle;
+* test/system-matrices-tests.cpp and system-misc-tests.cpp (neg): sums,
+  differences and transposes of maps over different edge sets, taken on
+  dense copies of the assembled matrices, then the product.
+
+The reference checkout is found in SIMIT_REFERENCE, else `reference`
+beside the repository; the tests skip without it."""
 import os
 import re
 import tempfile
@@ -21,6 +26,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.environ.get("SIMIT_REFERENCE",
                      os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 TESTS = os.path.join(REF, "test", "system-gemv-tests.cpp")
+TEST_FILES = [os.path.join(REF, "test", f) for f in
+              ("system-gemv-tests.cpp", "system-matrices-tests.cpp", "system-misc-tests.cpp")]
 PROGS = os.path.join(REF, "test", "input", "system")
 
 # each test's main, restated: "Ab" c = A*b; "AplusA" c = (A+A)*b; "A2"
@@ -41,10 +48,11 @@ MAINS = {
 def _block(name):
     if not os.path.exists(TESTS):
         pytest.skip("reference checkout not found (SIMIT_REFERENCE)")
-    text = open(TESTS).read()
-    m = re.search(r"TEST\(system, %s\) \{(.*?)\n\}" % name, text, re.S)
-    assert m, name
-    return "\n".join(ln.split("//")[0] for ln in m.group(1).splitlines())
+    for path in TEST_FILES:
+        m = re.search(r"TEST\(system, %s\) \{(.*?)\n\}" % name, open(path).read(), re.S)
+        if m:
+            return "\n".join(ln.split("//")[0] for ln in m.group(1).splitlines())
+    raise AssertionError("no test " + name)
 
 
 def _num(s):
@@ -59,8 +67,8 @@ def parse_test(name):
     sets, refs, fvars = {}, {}, {}
     for m in re.finditer(r"Set (\w+)(?:\(([\w, ]*)\))?;", body):
         sets[m.group(1)] = {"n": 0, "fields": {}, "comps": {}, "ends": []}
-    for m in re.finditer(r"FieldRef<simit_float((?:,\s*\d+)*)>\s+(\w+)\s*=\s*(\w+)\.addField"
-                         r"<[^>]*>\(\"(\w+)\"\)", body):
+    for m in re.finditer(r"FieldRef<(?:simit_float|double|float|int)((?:,\s*\d+)*)>\s+(\w+)"
+                         r"\s*=\s*(\w+)\.addField<[^>]*>\(\"(\w+)\"\)", body):
         comps = int(np.prod([int(d) for d in re.findall(r"\d+", m.group(1))] or [1]))
         fvars[m.group(2)] = (m.group(3), m.group(4))
         sets[m.group(3)]["comps"][m.group(4)] = comps
@@ -74,15 +82,20 @@ def parse_test(name):
     for sname, s in sets.items():
         for f, c in s["comps"].items():
             s["fields"][f] = np.zeros((s["n"], c))
-    for m in re.finditer(r"(\w+)\.set\((\w+),\s*(\{[^}]*\}|[-\d.e]+)\);", body):
-        sname, fname = fvars[m.group(1)]
-        sets[sname]["fields"][fname][refs[m.group(2)][1]] = _num(m.group(3))
+    for m in re.finditer(r"(\w+)(?:\.set\((\w+),\s*|\((\w+)\)\s*=\s*)(\{[^}]*\}|[-\d.e]+)\)?;",
+                         body):
+        el = m.group(2) or m.group(3)
+        if m.group(1) in fvars and el in refs:
+            sname, fname = fvars[m.group(1)]
+            sets[sname]["fields"][fname][refs[el][1]] = _num(m.group(4))
     tensors = {}
     for m in re.finditer(r"(\w+)\((\d+)\) = ([-\d.e]+);", body):
         tensors.setdefault(m.group(1), {})[int(m.group(2))] = float(m.group(3))
     asserts = []
-    for m in re.finditer(r"ASSERT_EQ\(([-\d.e]+),\s*(?:\([\w ]+\))?\s*(\w+)\.get\((\w+)\)"
+    for m in re.finditer(r"ASSERT_EQ\(([-\d.e]+),\s*(?:\([\w ]+\))?\s*(\w+)(?:\.get)?\((\w+)\)"
                          r"(?:\((\d)\))?\)", body):
+        if m.group(2) not in fvars or m.group(3) not in refs:
+            continue
         sname, fname = fvars[m.group(2)]
         asserts.append((float(m.group(1)), sname, fname, refs[m.group(3)][1],
                         int(m.group(4) or 0)))
@@ -102,7 +115,8 @@ def _map(src, main_src, which=0):
     maps = re.findall(r"map\s+(\w+)(?:\(([^)]*)\))?\s+to\s+(\w+)", main_src)
     fn, args, target = maps[which]
     f = simfront.parse(src)["funcs"][fn]
-    vals = [float(x) for x in args.split(",")] if args else []
+    vals = [float(x) for x in args.split(",")
+            if re.fullmatch(r"\s*-?[\d.]+(e-?\d+)?\s*", x)] if args else []
     scal = [an for an, aty, _ in f["args"] if aty[0] == "scalar"]
     return fn, dict(zip(scal, vals)), target
 
@@ -167,4 +181,70 @@ def test_reference_gemv(oracle, name):
             got = out[(fname, 0)][idx, 0]
         else:   # an input the program leaves as it was
             got = sets[sname]["fields"][fname][idx, comp]
+        assert got == expected, (name, fname, idx, comp, got, expected)
+
+
+# test/system-matrices-tests.cpp and system-misc-tests.cpp: each main
+# restated on dense copies of the assembled matrices
+MATRIX_MAINS = {
+    "add": "BpC", "add_named_tuples": "BpC", "add_generics": "BpC", "sub": "BmC",
+    "add_twice": "twice", "add_transpose": "transpose", "neg": "neg",
+    "add_blocked": "blocked+", "add_double_blocked": "blocked+", "sub_blocked": "blocked-",
+}
+
+
+def _dense(A, rp, ci, n, bs):
+    D = np.zeros((n * bs, n * bs))
+    for r in range(n):
+        for k in range(rp[r], rp[r + 1]):
+            c = int(ci[k])
+            D[r * bs:(r + 1) * bs, c * bs:(c + 1) * bs] += A[k * bs * bs:(k + 1) * bs * bs].reshape(
+                bs, bs)
+    return D
+
+
+def _vector_map(tmp, src, fn, args, sets, extra):
+    info = simfront.compile_map(src, fn, args)
+    assert info["kind"] == "vector"
+    pts = [k for k, v in sets.items() if not v["ends"]][0]
+    n = sets[pts]["n"]
+    fields = {("element", f): v for f, v in sets[pts]["fields"].items()}
+    fields.update(extra)
+    return HostMap(info, tmp).assemble(np.arange(n, dtype=np.int32), None, n, fields)
+
+
+@pytest.mark.parametrize("name", sorted(MATRIX_MAINS))
+def test_reference_system_matrices(oracle, name):
+    sets, _, asserts = parse_test(name)
+    src = open(os.path.join(PROGS, name + ".sim")).read()
+    main_src = src[src.index("export func main"):]
+    kind = MATRIX_MAINS[name]
+    pts = [k for k, v in sets.items() if not v["ends"]][0]
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        mats = []
+        for which in range(1 if kind == "neg" else 2):
+            fn, args, target = _map(src, main_src, which)
+            A, rp, ci, n, bs = _assemble(oracle, tmp, src, fn, args, target, sets)
+            mats.append(_dense(A, rp, ci, n, bs))
+        F = sets[pts]["fields"]
+        if kind == "neg":
+            out["b"] = -(mats[0] @ F["a"].reshape(-1))
+        elif kind.startswith("blocked"):
+            A = mats[0] + mats[1] if kind == "blocked+" else mats[0] - mats[1]
+            fn, args, _ = _map(src, main_src, 2)
+            X = _vector_map(tmp, src, fn, args, sets, {})
+            Y = A @ X
+            fn, args, _ = _map(src, main_src, 3)
+            yname = [an for an, aty, _ in simfront.parse(src)["funcs"][fn]["args"]
+                     if aty[0] == "tensor"][0]
+            out["a"] = _vector_map(tmp, src, fn, args, sets, {("arg", yname): Y})
+        else:
+            B, C = mats
+            A = {"BpC": B + C, "BmC": B - C, "twice": (B + C) + B + C,
+                 "transpose": (B + C) + (B + C).T}[kind]
+            out["a"] = A @ F["b"].reshape(-1)
+    assert asserts
+    for expected, sname, fname, idx, comp in asserts:
+        got = out[fname][idx] if fname in out else sets[sname]["fields"][fname][idx, comp]
         assert got == expected, (name, fname, idx, comp, got, expected)
