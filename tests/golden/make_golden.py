@@ -133,6 +133,8 @@ def main():
         "isprings": extract_asserts(os.path.join(test, "program-isprings.cpp"), "isprings"),
         "cg": extract_asserts(os.path.join(test, "program-cg-test.cpp"), "cg"),
         "femTet": extract_asserts(os.path.join(test, "program-fem-test.cpp"), "femTet"),
+        "esprings": extract_asserts(os.path.join(test, "program-esprings-test.cpp"),
+                                    "esprings"),
         # assembly + SpMV of small element functions (test/input/system/*.sim,
         # test/input/assembly/matrix_vv.sim)
         "gemv_blocked": extract_assert_eq(os.path.join(test, "system-gemv-tests.cpp"),

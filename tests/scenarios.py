@@ -38,7 +38,32 @@ def golden_lookup(entry, fields):
     m = re.match(r"(\w+)\.get\(vertRefs\[(\d+)\]\)\((\d)\)$", e)
     if m:
         return fields[m.group(1)][int(m.group(2)) * 3 + int(m.group(3))]
+    # `TensorRef x1 = x.get(p1); x1(0)`: the points numbered from 1
+    m = re.match(r"([a-z])(\d+)\((\d)\)$", e)
+    if m:
+        return fields[m.group(1)][(int(m.group(2)) - 1) * 3 + int(m.group(3))]
     raise ValueError(e)
+
+
+def esprings_cube():
+    """test/program-esprings-test.cpp:10-150 (TEST(Program, esprings)): the
+    8 corners of the unit cube at rest, its 12 edges as springs (mass
+    0.0282735, rest length 0.9), 10 runs of test/input/program/esprings.sim
+    main: explicit springs, stiffness 3, gravity -9.81 z, h = 0.01."""
+    x = np.array([[i & 1, (i >> 1) & 1, (i >> 2) & 1] for i in range(8)], np.float64)
+    ends = [(0, 1), (2, 3), (4, 5), (6, 7), (0, 2), (1, 3), (4, 6), (5, 7),
+            (0, 4), (1, 5), (2, 6), (3, 7)]
+    return {"n": 8, "x": x.reshape(-1), "v": np.zeros(24),
+            "ep": np.array(ends, np.int32).reshape(-1), "m": np.full(12, 0.0282735),
+            "l0": np.full(12, 0.9), "h": 0.01, "steps": 10}
+
+
+def esprings_step(s, x, v, fg, M, fs):
+    """esprings.sim main after its three maps (numpy or torch arrays):
+    p = M .* v + h (fs + fg);  v = p ./ M;  x = x + h v."""
+    p = (M * v) + (s["h"] * (fs + fg))
+    v = p / M
+    return x + (s["h"] * v), v
 
 
 def isprings_chain():

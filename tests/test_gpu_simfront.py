@@ -352,3 +352,29 @@ def test_sim_assembly_forms_give_reference_test_values(ctx, dtype):
     for sm in keep:
         if isinstance(sm, simfront.SimMap):
             sm.close()
+
+
+def test_sim_explicit_springs_golden(ctx):
+    """tests/sim/explicit_springs.sim on the GPU: the three vector maps of
+    the explicit springs step through the vertex-owner kernel, the update
+    p = M v + h (fs + fg), v = p / M, x += h v in device arrays; after 10
+    steps the positions test/program-esprings-test.cpp asserts, to 1e-13."""
+    from simit_gb300.runtime import Mesh
+    from tests import scenarios
+    s = scenarios.esprings_cube()
+    src = _own("explicit_springs.sim")
+    mesh = Mesh(ctx, s["n"], s["ep"], 2)
+    maps = [simfront.SimMap(ctx, src, f) for f in ("weight", "lumped", "pull")]
+    d = ctx.device
+    x = torch.tensor(s["x"], device=d)
+    v = torch.tensor(s["v"], device=d)
+    for _ in range(s["steps"]):
+        fg, M, fs = (m.assemble(mesh, {"x": x, "m": s["m"], "l0": s["l0"]}) for m in maps)
+        x, v = scenarios.esprings_step(s, x, v, fg[:s["n"] * 3], M[:s["n"] * 3],
+                                       fs[:s["n"] * 3])
+    ctx.sync()
+    xh = x.cpu().numpy()
+    for g in scenarios.golden("esprings"):
+        assert abs(scenarios.golden_lookup(g, {"x": xh}) - g["expected"]) <= 1e-13, g
+    for m in maps:
+        m.close()

@@ -783,3 +783,48 @@ def test_reference_isprings_maps_match_oracle(oracle):
                                      1e-2, 1e-1, np.array([0.0, 0.0, -9.81]), rp, ci)
     assert np.array_equal(MDK, wA)
     assert np.array_equal(fmg + fe, wf)
+
+
+# ---------------------------------------------------------------------------
+# explicit springs: test/program-esprings-test.cpp
+# ---------------------------------------------------------------------------
+def _esprings_host(src, names, tmp):
+    """Ten steps of the esprings main with the program's three maps (names:
+    gravity, masses, stiffness functions) compiled for the host."""
+    from tests import scenarios
+    s = scenarios.esprings_cube()
+    maps = [HostMap(simfront.compile_map(src, f), tmp) for f in names]
+    x, v = s["x"].copy(), s["v"].copy()
+    for _ in range(s["steps"]):
+        fields = {"x": x, "m": s["m"], "l0": s["l0"]}
+        fg, M, fs = (m.assemble(s["ep"], None, s["n"], fields) for m in maps)
+        x, v = scenarios.esprings_step(s, x, v, fg, M, fs)
+    return x
+
+
+GOLD_TOL = 1e-13     # SIMIT_ASSERT_FLOAT_EQ for doubles
+
+
+def test_reference_esprings_golden():
+    """test/input/program/esprings.sim's maps generated for the host and its
+    main restated: after 10 steps the positions the test asserts
+    (test/program-esprings-test.cpp:106-145), to 1e-13."""
+    from tests import scenarios
+    src = _ref("test/input/program/esprings.sim")
+    with tempfile.TemporaryDirectory() as tmp:
+        x = _esprings_host(src, ("distribute_gravity", "distribute_masses",
+                                 "compute_stiffness"), tmp)
+    gold = scenarios.golden("esprings")
+    assert len(gold) == 24
+    for g in gold:
+        assert abs(scenarios.golden_lookup(g, {"x": x}) - g["expected"]) <= GOLD_TOL, g
+
+
+def test_own_explicit_springs_golden():
+    """tests/sim/explicit_springs.sim on the host: the esprings test's
+    positions after 10 steps."""
+    from tests import scenarios
+    with tempfile.TemporaryDirectory() as tmp:
+        x = _esprings_host(_own("explicit_springs.sim"), ("weight", "lumped", "pull"), tmp)
+    for g in scenarios.golden("esprings"):
+        assert abs(scenarios.golden_lookup(g, {"x": x}) - g["expected"]) <= GOLD_TOL, g
