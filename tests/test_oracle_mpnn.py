@@ -171,3 +171,35 @@ def test_network_weights_of_a_polynomial():
     Gw = mo.poly_coeffs(w)
     assert np.abs(mo.poly_coeffs(learned.params_of_poly(learned.poly_of_params(w))) - Gw).max() \
         <= 1e-6 * np.abs(Gw).max()
+
+
+def test_elasticity_coupling_is_mostly_anisotropic(oracle):
+    """Why scalar edge weights limit the network on elasticity: after the
+    block-Jacobi scaling L_i^-1 A_ij L_j^-T, the isotropic part (tr/3 I) of
+    the off-diagonal blocks holds well under half of their Frobenius energy
+    (about 27 % on an 8^3 lattice with E log-uniform 1e3..1e6)."""
+    from simit_gb300 import meshgen
+    mg = meshgen.tet_grid(6)
+    n, tets = mg["n"], mg["tets"]
+    nT = len(tets) // 4
+    g = np.random.default_rng(3)
+    E = 10 ** g.uniform(3, 6, nT)
+    nu = g.uniform(0.35, 0.45, nT)
+    mu, lam = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
+    B, W, _ = oracle.tet_precompute(mg["X0"], tets, 1e3)
+    rp, ci = oracle.pattern(n, tets, 4)
+    A = oracle.tet_stiffness(0, mg["x"], np.zeros(n, np.int32), tets, B, W, mu, lam, 0.01,
+                             1e3, rp, ci).reshape(-1, 3, 3)
+    Linv = np.zeros((n, 3, 3))
+    for i in range(n):
+        k = rp[i] + list(ci[rp[i]:rp[i + 1]]).index(i)
+        Linv[i] = np.linalg.inv(np.linalg.cholesky(A[k]))
+    iso = tot = 0.0
+    for i in range(n):
+        for k in range(rp[i], rp[i + 1]):
+            j = ci[k]
+            if j != i:
+                N = Linv[i] @ A[k] @ Linv[j].T
+                iso += 3 * (np.trace(N) / 3) ** 2
+                tot += float((N * N).sum())
+    assert 0.0 < iso / tot < 0.4
