@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--lanes", type=int, default=0, help="sg_bspmv lanes (g) for --spmv-only")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--f64", action="store_true", help="FP64 matrix for --spmv-only")
+    ap.add_argument("--tune-spmv", action="store_true",
+                    help="--spmv-only: also run the SpMV autotuner and print its timings")
+    ap.add_argument("--scalar", action="store_true",
+                    help="--spmv-only on the P1 heat matrix (one value per entry)")
     ap.add_argument("--sym", action="store_true",
                     help="symmetric storage for the iteration's SpMV (and for --spmv-only)")
     ap.add_argument("--pdl", action="store_true",
@@ -263,7 +267,7 @@ def run_heat(args):
     import torch
     from simit_gb300 import _lib, meshgen
     from simit_gb300.runtime import (Context, Mesh, Solver, assemble_heat, bspmv, solve_opts,
-                                     tet_precompute)
+                                     tet_precompute, tune_spmv)
     size = args.size
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
@@ -291,19 +295,29 @@ def run_heat(args):
                                                           exact=False))
         xv = torch.rand(mesh.n, dtype=dt, device=d)
         y = torch.empty_like(xv)
-        bspmv(ctx, mesh.n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A, xv, y)
-        ms_spmv, _ = _ev_ms(st, lambda: bspmv(ctx, mesh.n, 1, mesh.pattern.rowptr,
-                                             mesh.pattern.colidx, A, xv, y), reps=1000)
+        # the SpMV schedule picked by the autotuner on this matrix (cached
+        # per pattern), timed beside the default one
+        tu = tune_spmv(ctx, mesh.n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A,
+                       mesh.nnzb, xdt=dt)
+        times = {}
+        for g in sorted({0, tu["g"]}):
+            bspmv(ctx, mesh.n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A, xv, y, g)
+            times[g], _ = _ev_ms(st, lambda: bspmv(ctx, mesh.n, 1, mesh.pattern.rowptr,
+                                                  mesh.pattern.colidx, A, xv, y, g), reps=1000)
+        ms_spmv = times[tu["g"]]
         es = A.element_size()
         nbytes = mesh.nnzb * (es + 4) + (mesh.n + 1) * 4 + mesh.n * 2 * es
         S = Solver(ctx, mesh.n, 1, mesh.pattern.rowptr, mesh.pattern.colidx, A, mesh.nnzb,
                    solve_opts(precision=prec, precond=_lib.PRECOND_JACOBI, tol=1e-8,
-                              maxiters=100000))
+                              maxiters=100000, lanes=_lib.LANES_AUTOTUNE))
         b64 = b.double()
         xs = torch.zeros_like(b64)
         ms_solve, r = _ev_ms(st, lambda: S.solve(b64, xs.zero_()))
         S.close()
         out[name] = {"assembly_ms": ms_asm, "spmv_ms": ms_spmv, "spmv_GBps": nbytes / ms_spmv / 1e6,
+                     "spmv_frac": nbytes / ms_spmv / 1e6 / peaks()[0],
+                     "spmv_schedule": {"tuned_g": tu["g"], "tuned_ms": times[tu["g"]],
+                                       "default_ms": times[0]},
                      "spmv_1000_ms": ms_spmv * 1000, "solve_ms": ms_solve, "iters": r.iters,
                      "relres": (r.true_normr2 / r.bnorm2) ** 0.5}
     return out
@@ -520,6 +534,41 @@ def run_spmv_only(args):
     ctx = Context(0)
     torch.cuda.set_stream(ctx.torch_stream)
     dt = torch.float64 if args.f64 else torch.float32
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if args.scalar:
+        # the P1 heat matrix of the same lattice (one value per pattern entry)
+        import numpy as np
+        from simit_gb300 import meshgen
+        from simit_gb300.runtime import Mesh, assemble_heat, tet_precompute
+        mg = meshgen.tet_grid(args.size)
+        g = meshgen.rng(31)
+        kappa = 10 ** g.uniform(-2, 2, len(mg["tets"]) // 4)
+        if not args.no_reorder:
+            mg, vo, eo = _reorder_grid(mg, with_orders=True)
+            kappa = kappa[eo]
+        m = Mesh(ctx, mg["n"], mg["tets"], 4)
+        d = ctx.device
+        B, W, _ = tet_precompute(m, torch.tensor(mg["x"], dtype=dt, device=d), 1.0, dtype=dt)
+        A, _ = assemble_heat(m, B, W, torch.tensor(kappa, dtype=dt, device=d), 1e-2,
+                             torch.zeros(m.n, dtype=dt, device=d), dtype=dt, exact=False)
+        x = torch.rand(m.n, dtype=dt, device=d)
+        y = torch.empty_like(x)
+        s = x.element_size()
+        spmv = lambda: bspmv(ctx, m.n, 1, m.pattern.rowptr, m.pattern.colidx, A, x, y,  # noqa
+                             g=args.lanes)
+        nbytes = m.nnzb * (s + 4) + (m.n + 1) * 4 + m.n * 2 * s
+        spmv()
+        e0.record(ctx.torch_stream)
+        for _ in range(args.reps):
+            spmv()
+        e1.record(ctx.torch_stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.reps
+        print(json.dumps({"size": args.size, "scalar": True, "lanes": args.lanes,
+                          "dtype": str(dt), "nnz": m.nnzb, "ms": ms, "GBps": nbytes / ms / 1e6,
+                          "bytes": nbytes}), flush=True)
+        return
     h = problems.hetero_mesh(args.size)
     if not args.no_reorder:
         h = problems.reorder_hetero(h)
@@ -527,8 +576,6 @@ def run_spmv_only(args):
     m = p.mesh
     x = torch.rand(m.n * 3, dtype=dt, device=ctx.device)
     y = torch.empty_like(x)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     s = x.element_size()
     if args.sym:  # the symmetric-storage kernel (k_sbsr3_wtma)
         from simit_gb300.runtime import SymBsr
@@ -541,6 +588,10 @@ def run_spmv_only(args):
         spmv = lambda: bspmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, x, y,  # noqa
                              g=args.lanes)
         nbytes = m.nnzb * (9 * s + 4) + (m.n + 1) * 4 + m.n * 3 * 2 * s
+    tuned = None
+    if args.tune_spmv:
+        from simit_gb300.runtime import tune_spmv
+        tuned = tune_spmv(ctx, m.n, 3, m.pattern.rowptr, m.pattern.colidx, p.A, m.nnzb, xdt=dt)
     spmv()
     e0.record(ctx.torch_stream)
     for _ in range(args.reps):
@@ -565,7 +616,7 @@ def run_spmv_only(args):
                       "stages": args.stages, "dtype": str(dt),
                       "nnzb": m.nnzb, "ms": ms, "GBps": nbytes / ms / 1e6, "bytes": nbytes,
                       "add_diag_ms": ad_ms, "add_diag_GBps": ad_bytes / ad_ms / 1e6,
-                      "add_diag_bytes": ad_bytes}), flush=True)
+                      "add_diag_bytes": ad_bytes, "tuned": tuned}), flush=True)
 
 
 def workload_name(size, reorder=True):
@@ -798,6 +849,12 @@ class Clocks:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def spmv_bytes_f64(mesh):
+    """Algorithmic bytes of one FP64 3x3 SpMV: blocks and columns, row
+    pointers, x read and y written."""
+    return mesh.nnzb * (72 + 4) + (mesh.n + 1) * 4 + mesh.n * 3 * 16
 
 
 def peaks():
@@ -1069,13 +1126,29 @@ def run_ours(args, rank, world, local):
     # --- plain FP64 Jacobi-CG on the same GPU (FP64 assembly + solve) -----
     fp64 = None
     if not args.no_fp64:
+        # the same autotuner as the headline picks its SpMV schedule and
+        # assembly plan
         p64 = problems.HeteroElasticity(ctx, host, dtype=torch.float64,
-                                        precond=_lib.PRECOND_JACOBI)
+                                        precond=_lib.PRECOND_JACOBI, tune=True)
         ms64, r64s = _step_timing(p64, st, 1, 1, barrier)
         r64 = r64s[-1]
         fp64 = {"ms": ms64, "DOF_per_s": dofs / (ms64 / 1e3), "iters": r64.iters,
                 "relres": (r64.true_normr2 / r64.bnorm2) ** 0.5,
-                "method": "FP64 assembly + FP64 point-Jacobi CG (FP64 SpMV, FP64 vectors)"}
+                "method": "FP64 assembly + FP64 point-Jacobi CG (FP64 SpMV, FP64 vectors)",
+                "tuned": _tuned_summary(p64.tuned)}
+        # its SpMV against the FP64 FMA rate (18 flops per 3x3 block): what
+        # the FP64 step would take with the SpMV at that bound
+        from simit_gb300.runtime import fp64_fma_rate
+        s64 = p64.tuned["spmv"]["ms"]
+        fma = fp64_fma_rate(ctx)
+        nb = p64.mesh.nnzb
+        bound_ms = 18.0 * nb / (fma * 1e12) * 1e3
+        at_bound = ms64 - r64.iters * max(0.0, s64 - bound_ms)
+        fp64["spmv"] = {"ms": s64, "fp64_tflops": 18.0 * nb / (s64 * 1e-3) / 1e12,
+                        "fp64_fma_peak_tflops": fma, "frac_fp64_peak": bound_ms / s64,
+                        "GBps": spmv_bytes_f64(p64.mesh) / (s64 * 1e-3) / 1e9}
+        fp64["step_ms_with_spmv_at_fp64_bound"] = at_bound
+        fp64["speedup_if_spmv_at_fp64_bound"] = at_bound / ms
         p64.close()
         del p64
         torch.cuda.empty_cache()

@@ -374,6 +374,11 @@ int sg_bsr_add_diag(sg_ctx *ctx, int32_t n, int32_t bs, const uint32_t *rowptr,
 int sg_dot(sg_ctx *ctx, int64_t len, int vec_dtype, const void *a,
            const void *b, double *h_out);
 
+/* The device's FP64 FMA rate in TFLOP/s (2 flops per FMA), from a kernel of
+ * independent FMA chains on every SM, timed on the context's stream: the
+ * FP64 roofline of an FP64 SpMV.  Synchronises. */
+int sg_fp64_fma_rate(sg_ctx *ctx, double *tflops);
+
 /* ---------------------------------------------------------------------
  * Conjugate-gradient solves.  The reference has no CG routine: CG is user
  * code in each .sim program (apps/springs/isprings.sim:77-93,

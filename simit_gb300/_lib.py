@@ -88,6 +88,7 @@ SIGNATURES = {
                            ctypes.POINTER(I32), P, P, I32]),
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
+    "sg_fp64_fma_rate": (ctypes.c_int, [P, ctypes.POINTER(D)]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),
     "sg_residual": (_CI, [P, ctypes.POINTER(Matrix), P, P, P, ctypes.POINTER(D), _CI]),
     "sg_incidence_pattern": (_CI, [P, _CI, I32, I64, I32, P, P, P, P]),

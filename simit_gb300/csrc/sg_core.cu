@@ -219,6 +219,23 @@ void ctx_release(Ctx *c) {
   delete c;
 }
 
+// FP64 FMA rate probe: eight independent FMA chains per thread, so the FP64
+// pipe, not latency, bounds it.  The sum is stored so that nothing is
+// optimised away.
+__global__ void k_fma_rate(double *out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-9 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace sg
 
 using namespace sg;
@@ -305,6 +322,34 @@ int sg_dot(sg_ctx *h, int64_t len, int vdt, const void *a, const void *b,
   SG_CHECK_CUDA(cudaMemcpyAsync(c->h_stage, res, 8, cudaMemcpyDeviceToHost, c->stream));
   SG_CHECK_CUDA(cudaStreamSynchronize(c->stream));
   *h_out = *(double *)c->h_stage;
+  return SG_OK;
+}
+
+int sg_fp64_fma_rate(sg_ctx *h, double *tflops) {
+  Ctx *c = as_ctx(h);
+  DeviceGuard dg_(c);
+  SG_REQUIRE(c && tflops, "sg_fp64_fma_rate: null argument");
+  const int T = 256, G = c->num_sms * 8, iters = 4096, reps = 5;
+  Scratch s(c);
+  SG_TRY(s.reserve(Scratch::bytes_for((int64_t)G * T, 8) + 256));
+  double *out = s.alloc<double>((int64_t)G * T);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  SG_CHECK_CUDA(cudaEventCreate(&e0));
+  cudaError_t e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) {
+    k_fma_rate<<<G, T, 0, c->stream>>>(out, iters, 0.999999, 1e-7);  // warm-up
+    e = cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r)
+      k_fma_rate<<<G, T, 0, c->stream>>>(out, iters, 0.999999, 1e-7);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  }
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  SG_CHECK_CUDA(e);
+  *tflops = 2.0 * 8.0 * iters * (double)G * T * reps / (ms * 1e-3) / 1e12;
   return SG_OK;
 }
 

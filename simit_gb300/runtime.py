@@ -365,6 +365,13 @@ def dot(ctx, a, b):
     return out.value
 
 
+def fp64_fma_rate(ctx):
+    """sg_fp64_fma_rate: the device's FP64 FMA rate in TFLOP/s."""
+    out = ctypes.c_double()
+    call("sg_fp64_fma_rate", ctx.h, ctypes.byref(out))
+    return out.value
+
+
 def _host_f64(a):
     return (ctypes.c_double * len(a))(*[float(v) for v in a])
 

@@ -245,3 +245,12 @@ def test_dot(ctx):
     d = ctx.device
     got = dot(ctx, torch.from_numpy(a).to(d), torch.from_numpy(b).to(d))
     assert abs(got - float(np.dot(a, b))) <= 1e-12 * float(np.dot(np.abs(a), np.abs(b)))
+
+
+def test_fp64_fma_rate_is_plausible(ctx):
+    """sg_fp64_fma_rate, the FP64 roofline the bench reports the FP64 SpMV
+    against: a positive rate well below the FP32 one (GB300's FP64 is about
+    1.2 TFLOP/s)."""
+    from simit_gb300.runtime import fp64_fma_rate
+    r = fp64_fma_rate(ctx)
+    assert 0.1 < r < 20.0, r
