@@ -371,8 +371,11 @@ static int ensure_folded(GraphH *G) {
 
 // One Horner step on a persistent grid (resident CTAs on every SM, at most
 // one warp per slice).
-static int horner_launch(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, bool half_a,
-                         const FoldBufs &B, int d, const void *src, void *dst) {
+// The Horner steps' grid: one persistent wave (CTAs per SM from the
+// occupancy of the plain step), at most one warp per slice.  The last step
+// with the end of the application folded in (FIN) runs on the same grid, so
+// the solver knows its number of dot partials in advance.
+static int horner_grid(GraphH *G, bool half_a, int *out) {
   Ctx *c = G->c;
   static PerDeviceOnce once;
   static int per_sm[SG_MAX_DEVICES][2] = {};
@@ -384,6 +387,12 @@ static int horner_launch(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int ga
     SG_CHECK_CUDA(cudaFuncSetAttribute(k_horner<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)ht_smem_bytes<float>()));
+    SG_CHECK_CUDA(cudaFuncSetAttribute(k_horner<__half, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ht_smem_bytes<__half>()));
+    SG_CHECK_CUDA(cudaFuncSetAttribute(k_horner<float, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ht_smem_bytes<float>()));
     SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm[dev][0], k_horner<__half>, HT_WARPS * 32, ht_smem_bytes<__half>()));
     SG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -392,16 +401,34 @@ static int horner_launch(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int ga
       if (per_sm[dev][k] < 1) per_sm[dev][k] = 1;
     return SG_OK;
   }));
-  const int64_t need = ((int64_t)B.sl.nslice + HT_WARPS - 1) / HT_WARPS;
+  const int64_t need = ((int64_t)G->fb.sl.nslice + HT_WARPS - 1) / HT_WARPS;
   int64_t grid = (int64_t)c->num_sms * per_sm[dev][half_a ? 0 : 1];
   if (grid > need) grid = need;
   if (grid < 1) grid = 1;
-  if (half_a)
+  *out = (int)grid;
+  return SG_OK;
+}
+
+static int horner_launch(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, bool half_a,
+                         const FoldBufs &B, int d, const void *src, void *dst,
+                         const FinArgs *fa = nullptr) {
+  Ctx *c = G->c;
+  int grid = 1;
+  SG_TRY(horner_grid(G, half_a, &grid));
+  if (fa) {
+    if (half_a)
+      k_horner<__half, true><<<(unsigned)grid, HT_WARPS * 32, ht_smem_bytes<__half>(), st>>>(
+          ctl, gate, B, d, src, dst, d == 5, c->d_err, *fa);
+    else
+      k_horner<float, true><<<(unsigned)grid, HT_WARPS * 32, ht_smem_bytes<float>(), st>>>(
+          ctl, gate, B, d, src, dst, d == 5, c->d_err, *fa);
+  } else if (half_a) {
     k_horner<__half><<<(unsigned)grid, HT_WARPS * 32, ht_smem_bytes<__half>(), st>>>(
         ctl, gate, B, d, src, dst, d == 5, c->d_err);
-  else
+  } else {
     k_horner<float><<<(unsigned)grid, HT_WARPS * 32, ht_smem_bytes<float>(), st>>>(
         ctl, gate, B, d, src, dst, d == 5, c->d_err);
+  }
   SG_CHECK_LAUNCH();
   return SG_OK;
 }
@@ -414,7 +441,7 @@ static int horner_launch(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int ga
 // point, the FP32 one as float4.
 static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, bool half_a,
                       const float *r, float *z, const float *q, double *part, int np, int want_rr,
-                      int want_zq, bool xin_ready) {
+                      int want_zq, bool xin_ready, bool fused = false) {
   Ctx *c = G->c;
   Graph &g = G->g;
   FoldBufs B = G->fb;
@@ -430,10 +457,25 @@ static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate,
     SG_CHECK_LAUNCH();
   }
   // step 5 gathers x; step d < 5 reads w[(5 - d) & 1]; step d writes
-  // w[(6 - d) & 1] (w_0 in w[0])
-  for (int d = 5; d >= 0; --d)
+  // w[(6 - d) & 1] (w_0 in w[0]).  fused: step 0 ends the application itself
+  // (z and the dot partials, np of them: the steps' grid)
+  for (int d = 5; d >= 0; --d) {
+    FinArgs fa;
+    if (fused && d == 0) {
+      int hg = 0;
+      SG_TRY(horner_grid(G, half_a, &hg));
+      SG_REQUIRE(!part || np == hg, "mpnn: %d dot partials asked of a %d-CTA last step", np, hg);
+      fa.r = r;
+      fa.q = q;
+      fa.z = z;
+      fa.part = part;
+      fa.want_rr = want_rr;
+      fa.want_zq = want_zq;
+    }
     SG_TRY(horner_launch(G, st, ctl, gate, half_a, B, d, d == 5 ? B.xin : B.w[(5 - d) & 1],
-                         B.w[(6 - d) & 1]));
+                         B.w[(6 - d) & 1], (fused && d == 0) ? &fa : nullptr));
+  }
+  if (fused) return SG_OK;
   // z = L^-T w_0 and the dots, in vertex order; one dot partial per block:
   // np of them when asked
   const int g0 = part ? np : finish_grid(c, B.sl.nslice);
@@ -636,7 +678,7 @@ static int learned_prec(Solver *S, cudaStream_t st) {
     // S6 leaves r.r | r.z | z.q for K3 (P2 blocks)
     return mpnn::fold_apply(L->G, st, S->ctl, 1, L->exec == SG_MPNN_EXEC_FOLDED,
                             (const float *)S->r, (float *)S->z, (const float *)S->q, S->part2,
-                            S->np2_ext, 1, 1, true);
+                            S->np2_ext, 1, 1, true, true);
   SG_TRY(mpnn::forward(L->G, st, S->ctl, 1, L->prm, (const float *)S->r, (float *)S->z, false));
   mpnn::k_rz_zq<<<S->P2, RED_T, 0, st>>>(S->ctl, S->len, (const float *)S->r, (const float *)S->z,
                                          (const float *)S->q, S->part2);
@@ -704,9 +746,10 @@ static int learned_setup(Solver *S) {
     SG_TRY(mpnn::ensure_folded(L->G));
     S->ext_k2 = learned_k2;
     S->k3_xupd = 1;
-    // the last Horner step runs on the passes' full grid and leaves that
-    // many partials per dot for K3
-    const int g0 = mpnn::finish_grid(S->c, L->G->fb.sl.nslice);
+    // the last Horner step, with the end of the application folded in,
+    // runs on the steps' grid and leaves that many partials per dot for K3
+    int g0 = 0;
+    SG_TRY(mpnn::horner_grid(L->G, L->exec == SG_MPNN_EXEC_FOLDED, &g0));
     const int np = S->P1 > S->P2 ? S->P1 : S->P2;
     if (g0 > np) {
       void *p2 = nullptr;

@@ -346,6 +346,18 @@ struct FoldBufs {
 // the solve status (gate); after a fallback to block Jacobi the steps do
 // nothing (k_lrn_finish then uses x).  AT: edge-weight type; FP16 weights
 // go with block-floating-point vectors.
+// The end of an application folded into the last Horner step (FIN): each
+// row's w_0 becomes z = L^-T w_0 at once, and the dots r.r, r.z, z.q of the
+// new z accumulate as it goes, one partial per CTA (grid-size apart, as
+// k_lrn_finish leaves them).  part null: z alone.
+struct FinArgs {
+  const float *r = nullptr;
+  const float *q = nullptr;
+  float *z = nullptr;
+  double *part = nullptr;
+  int want_rr = 0, want_zq = 0;
+};
+
 constexpr int HT_WARPS = 4;   // warps per CTA
 constexpr int HT_NST = 2;     // slices in flight per warp
 constexpr int HT_CAPL = 20;   // longest staged slice (entries per lane)
@@ -360,18 +372,77 @@ __host__ __device__ constexpr size_t ht_smem_bytes() {
          (size_t)HT_WARPS * HT_NST * ht_stage_bytes<AT>();
 }
 
-template <typename AT>
-__global__ void __launch_bounds__(HT_WARPS * 32, 1)
+template <typename AT, bool FIN = false>
+__global__ void __launch_bounds__(HT_WARPS * 32, FIN ? 7 : 1)
     k_horner(const SolveCtl *ctl, int gate, FoldBufs B, int d,
-                 const void *__restrict__ src, void *__restrict__ dst, int first, int *err) {
+                 const void *__restrict__ src, void *__restrict__ dst, int first, int *err,
+                 FinArgs fa = FinArgs()) {
   constexpr bool CV = sizeof(AT) == 2;
   constexpr size_t CB = (size_t)HT_CAPL * SL_W * 4;
   constexpr size_t STG = ht_stage_bytes<AT>();
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ float G[9], G6[9];
+  __shared__ double shd[33];
   if (ctl && gate && ctl->status != ST_RUNNING) return;
-  if (ctl && ctl->fallback) return;
+  // after a fallback to block Jacobi the steps do nothing, and the last one
+  // (FIN) turns x itself into z = L^-T x
+  const bool fb = ctl && ctl->fallback;
+  if (fb && !FIN) return;
+  DotAcc<float> rr, rz, zq;
+  auto fin = [&](uint32_t v, float a, float b, float c) {
+    // z = (L^-1)^T w, L^-1 = [[l0,0,0],[l1,l2,0],[l3,l4,l5]], as k_lrn_finish
+    const float *L = B.l6 + (size_t)v * 6;
+    const float z0 = L[0] * a + L[1] * b + L[3] * c;
+    const float z1 = L[2] * b + L[4] * c;
+    const float z2 = L[5] * c;
+    float *zp = fa.z + (size_t)v * 3;
+    zp[0] = z0;
+    zp[1] = z1;
+    zp[2] = z2;
+    if (!fa.part) return;
+    const float *rp = fa.r + (size_t)v * 3;
+    const float r0 = rp[0], r1 = rp[1], r2 = rp[2];
+    if (fa.want_rr) {
+      rr.add(r0, r0);
+      rr.add(r1, r1);
+      rr.add(r2, r2);
+    }
+    rz.add(r0, z0);
+    rz.add(r1, z1);
+    rz.add(r2, z2);
+    if (fa.want_zq) {
+      const float *qp = fa.q + (size_t)v * 3;
+      zq.add(z0, qp[0]);
+      zq.add(z1, qp[1]);
+      zq.add(z2, qp[2]);
+    }
+  };
+  auto fin_partials = [&]() {
+    if (!FIN || !fa.part) return;
+    const double t1 = block_sum(rz.value(), shd);
+    const double t0 = fa.want_rr ? block_sum(rr.value(), shd) : 0.0;
+    const double t2 = fa.want_zq ? block_sum(zq.value(), shd) : 0.0;
+    if (threadIdx.x == 0) {
+      if (fa.want_rr) fa.part[blockIdx.x] = t0;
+      fa.part[(fa.want_rr ? gridDim.x : 0) + blockIdx.x] = t1;
+      if (fa.want_zq) fa.part[2 * gridDim.x + blockIdx.x] = t2;
+    }
+  };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (FIN && fb) {
+    // the slices as the steps take them, each row's x straight to z
+    const int64_t ns = B.sl.nslice;
+    for (int64_t s = (int64_t)blockIdx.x * HT_WARPS + warp; s < ns;
+         s += (int64_t)gridDim.x * HT_WARPS) {
+      const uint32_t v = __ldg(B.sl.row + s * SL_W + lane);
+      if (v == SL_NONE) continue;
+      float x0, x1, x2;
+      ld3<CV>(B.xin, v, x0, x1, x2);
+      fin(v, x0, x1, x2);
+    }
+    fin_partials();
+    return;
+  }
   if (threadIdx.x < 9) G[threadIdx.x] = B.g[d * 9 + threadIdx.x];
   else if (threadIdx.x < 18) G6[threadIdx.x - 9] = B.g[6 * 9 + threadIdx.x - 9];
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm) + warp * HT_NST;
@@ -468,9 +539,19 @@ __global__ void __launch_bounds__(HT_WARPS * 32, 1)
     }
     float x0, x1, x2;
     ld3<CV>(B.xin, v, x0, x1, x2);
-    st3<CV>(dst, v, m0 + G[0] * x0 + G[1] * x1 + G[2] * x2,
-            m1 + G[3] * x0 + G[4] * x1 + G[5] * x2, m2 + G[6] * x0 + G[7] * x1 + G[8] * x2);
+    const float w0 = m0 + G[0] * x0 + G[1] * x1 + G[2] * x2;
+    const float w1 = m1 + G[3] * x0 + G[4] * x1 + G[5] * x2;
+    const float w2 = m2 + G[6] * x0 + G[7] * x1 + G[8] * x2;
+    if (FIN) {
+      // w_0 as k_lrn_finish reads it: rounded to the evaluation's storage
+      float a = w0, b = w1, c = w2;
+      if (CV) cv_decode(cv_encode(w0, w1, w2), a, b, c);
+      fin(v, a, b, c);
+    } else {
+      st3<CV>(dst, v, w0, w1, w2);
+    }
   }
+  fin_partials();
 }
 
 // The end of an application after the last Horner step wrote w_0:
