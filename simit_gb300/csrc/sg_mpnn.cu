@@ -441,7 +441,8 @@ static int horner_launch(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int ga
 // point, the FP32 one as float4.
 static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate, bool half_a,
                       const float *r, float *z, const float *q, double *part, int np, int want_rr,
-                      int want_zq, bool xin_ready, bool fused = false) {
+                      int want_zq, bool xin_ready, bool fused = false,
+                      SolveCtl *decide_ctl = nullptr, int par = 0) {
   Ctx *c = G->c;
   Graph &g = G->g;
   FoldBufs B = G->fb;
@@ -471,6 +472,11 @@ static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate,
       fa.part = part;
       fa.want_rr = want_rr;
       fa.want_zq = want_zq;
+      if (decide_ctl && part && want_rr && want_zq) {
+        fa.ctl = decide_ctl;
+        fa.decide = 1;
+        fa.par = par;
+      }
     }
     SG_TRY(horner_launch(G, st, ctl, gate, half_a, B, d, d == 5 ? B.xin : B.w[(5 - d) & 1],
                          B.w[(6 - d) & 1], (fused && d == 0) ? &fa : nullptr));
@@ -672,13 +678,14 @@ static int learned_k2(Solver *S, cudaStream_t st, int par) {
   return SG_OK;
 }
 
-static int learned_prec(Solver *S, cudaStream_t st) {
+static int learned_prec(Solver *S, cudaStream_t st, int par) {
   LearnedExt *L = (LearnedExt *)S->ext;
   if (folded(L))
-    // S6 leaves r.r | r.z | z.q for K3 (P2 blocks)
+    // the last Horner step leaves r.r | r.z | z.q summed and the iteration
+    // decided (status, beta) in ctl for K3
     return mpnn::fold_apply(L->G, st, S->ctl, 1, L->exec == SG_MPNN_EXEC_FOLDED,
                             (const float *)S->r, (float *)S->z, (const float *)S->q, S->part2,
-                            S->np2_ext, 1, 1, true, true);
+                            S->np2_ext, 1, 1, true, true, S->ctl, par);
   SG_TRY(mpnn::forward(L->G, st, S->ctl, 1, L->prm, (const float *)S->r, (float *)S->z, false));
   mpnn::k_rz_zq<<<S->P2, RED_T, 0, st>>>(S->ctl, S->len, (const float *)S->r, (const float *)S->z,
                                          (const float *)S->q, S->part2);
@@ -746,6 +753,7 @@ static int learned_setup(Solver *S) {
     SG_TRY(mpnn::ensure_folded(L->G));
     S->ext_k2 = learned_k2;
     S->k3_xupd = 1;
+    S->ext_decides = 1;
     // the last Horner step, with the end of the application folded in,
     // runs on the steps' grid and leaves that many partials per dot for K3
     int g0 = 0;

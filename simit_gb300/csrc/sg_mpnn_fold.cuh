@@ -356,6 +356,11 @@ struct FinArgs {
   float *z = nullptr;
   double *part = nullptr;
   int want_rr = 0, want_zq = 0;
+  // decide (with all three dots): the CTA that finishes last also sums the
+  // partials and makes the iteration's decision (cg_decide: status, beta)
+  // for K3, which then only streams
+  SolveCtl *ctl = nullptr;
+  int decide = 0, par = 0;
 };
 
 constexpr int HT_WARPS = 4;   // warps per CTA
@@ -422,6 +427,15 @@ __global__ void __launch_bounds__(HT_WARPS * 32, FIN ? 7 : 1)
     const double t1 = block_sum(rz.value(), shd);
     const double t0 = fa.want_rr ? block_sum(rr.value(), shd) : 0.0;
     const double t2 = fa.want_zq ? block_sum(zq.value(), shd) : 0.0;
+    if (fa.decide) {
+      // r.r | r.z | z.q, each gridDim.x partials, summed in index order by
+      // the last CTA, which decides the iteration
+      const double t[3] = {t0, t1, t2};
+      double tot[3];
+      if (finalize_partials(t, 3, fa.part, &fa.ctl->tick2, tot, shd) && threadIdx.x == 0)
+        cg_decide(fa.ctl, fa.par, tot[0], tot[1], tot[2], fa.ctl->last_alpha);
+      return;
+    }
     if (threadIdx.x == 0) {
       if (fa.want_rr) fa.part[blockIdx.x] = t0;
       fa.part[(fa.want_rr ? gridDim.x : 0) + blockIdx.x] = t1;

@@ -231,9 +231,11 @@ template <typename VT>
 static int launch_k3(Solver *S, cudaStream_t st, int par) {
   const VT *z = (const VT *)(S->prec == PK_NONE ? S->r : S->z);
   const int np2 = S->np2_ext > 0 ? S->np2_ext : S->P2;
-  if (sizeof(VT) == 4)  // K2 decided unless an external preconditioner ran after it
+  // K2 decided, unless an external preconditioner ran after it and did not
+  if (sizeof(VT) == 4)
     SG_CHECK_CUDA(launch_k(S->c, k_cg_direction_v4, S->P2, RED_T, 0, st, S->ctl, par, S->len,
-                           (const double *)S->part2, np2, (int)(S->prec != PK_EXTERNAL),
+                           (const double *)S->part2, np2,
+                           (int)(S->prec != PK_EXTERNAL || S->ext_decides),
                            (const float *)z, (float *)S->p, (float *)S->xupd, S->k3_xupd));
   else
     k_cg_direction<VT><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->len, S->part2, S->P2, z,
@@ -255,7 +257,7 @@ static int capture_batch(Solver *S) {
     const int par = k & 1;
     rc = launch_k1<MT, VT>(S, st);
     if (rc == SG_OK) rc = launch_k2<VT, XT>(S, st, par);
-    if (rc == SG_OK && S->ext_prec) rc = S->ext_prec(S, st);
+    if (rc == SG_OK && S->ext_prec) rc = S->ext_prec(S, st, par);
     if (rc == SG_OK) rc = launch_k3<VT>(S, st, par);
   }
   S->c->pdl = false;

@@ -36,10 +36,13 @@ struct Solver {
   cudaGraphExec_t gexec = nullptr;
   std::vector<void *> allocs;
   // External preconditioner hooks (learned preconditioner).  ext_prec runs
-  // inside the captured iteration between K2 and K3: z = M(r) and the
-  // partials rr | rz | zq into part2.  ext_prec_apply: z = M(r) and the
-  // partials of r.z into part3 (set-up / restart).
-  int (*ext_prec)(Solver *, cudaStream_t) = nullptr;
+  // inside the captured iteration between K2 and K3 (par: the iteration's
+  // parity slot): z = M(r) and the partials rr | rz | zq into part2, or,
+  // with ext_decides, the iteration already decided in ctl (status, beta),
+  // so that K3 only streams.  ext_prec_apply: z = M(r) and the partials of
+  // r.z into part3 (set-up / restart).
+  int (*ext_prec)(Solver *, cudaStream_t, int par) = nullptr;
+  int ext_decides = 0;
   int (*ext_prec_apply)(Solver *, cudaStream_t) = nullptr;
   void (*ext_free)(Solver *) = nullptr;
   // ext_k2 (optional) replaces the iteration's K2 (the folded learned
