@@ -286,6 +286,23 @@ int sg_jit_vector_create(sg_ctx *ctx, const char *element_src, int32_t card, int
 int sg_jit_assemble_vector(sg_jit_assembly *jit, const sg_mesh *mesh,
                            const void *const *h_fields, int32_t nfields, void *vals);
 
+/* The cloth example's forces (apps/cloth/cloth.sim) as system vectors
+ * f [n*3] (`map ... to faces / hinges reduce +`), each vertex summing from
+ * zero its incidences' terms in ascending (element, local index), each
+ * element's terms in the program's order; no multiply-add contraction.
+ * sg_assemble_cloth_stretch: stretchingForce (:142-164) over faces (card 3),
+ * K [nF*9] the per-face stretching matrix (row-major), rest [nF*3] the rest
+ * squared lengths of edges 0-1, 1-2, 2-0 (precomputeFaceQuantities).
+ * sg_assemble_cloth_bend: bendingForce (:166-173) over hinges (card 4: the
+ * shared edge's endpoints, then the opposite vertices of its two
+ * triangles), angle / len / perp [nH] the rest dihedral angle, the edge's
+ * rest length and 2 (A1 + A2) / (3 len) (precomputeHingeQuantities).
+ * x [n*3]; all arrays in dtype.  Asynchronous. */
+int sg_assemble_cloth_stretch(sg_ctx *ctx, const sg_mesh *faces, int dtype, const void *x,
+                              const void *K, const void *rest, void *f);
+int sg_assemble_cloth_bend(sg_ctx *ctx, const sg_mesh *hinges, int dtype, const void *x,
+                           const void *angle, const void *len, const void *perp, void *f);
+
 /* precomputeTetMat (femTet.sim; apps/fem/fem_linear.sim:176-193):
  * B = inv(Ds) [nE*9], W = -det(Ds)/6 [nE], vertex mass m [n] = sum of
  * 0.25*rho*W in element order. */

@@ -89,6 +89,8 @@ SIGNATURES = {
     "sg_bspmv": (ctypes.c_int, [P, I32, I32, P, P, ctypes.c_int, P, ctypes.c_int, P, P, I32]),
     "sg_dot": (ctypes.c_int, [P, I64, ctypes.c_int, P, P, ctypes.POINTER(D)]),
     "sg_fp64_fma_rate": (ctypes.c_int, [P, ctypes.POINTER(D)]),
+    "sg_assemble_cloth_stretch": (ctypes.c_int, [P, P, ctypes.c_int, P, P, P, P]),
+    "sg_assemble_cloth_bend": (ctypes.c_int, [P, P, ctypes.c_int, P, P, P, P, P]),
     "sg_axpy": (ctypes.c_int, [P, I64, ctypes.c_int, D, P, P]),
     "sg_residual": (_CI, [P, ctypes.POINTER(Matrix), P, P, P, ctypes.POINTER(D), _CI]),
     "sg_incidence_pattern": (_CI, [P, _CI, I32, I64, I32, P, P, P, P]),

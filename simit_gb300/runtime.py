@@ -365,6 +365,30 @@ def dot(ctx, a, b):
     return out.value
 
 
+def assemble_cloth_stretch(mesh, x, K, rest, dtype=torch.float64):
+    """The cloth example's stretching force over a face mesh (card 3):
+    f [n*3] (sg_assemble_cloth_stretch)."""
+    d = mesh.ctx.device
+    with mesh.ctx.stream():
+        xs, Ks, rs = (_d(a, dtype, d) for a in (x, K, rest))
+        f = torch.empty(mesh.n * 3, dtype=dtype, device=d)
+    call("sg_assemble_cloth_stretch", mesh.ctx.h, mesh.ref(), dtype_code(f), ptr(xs), ptr(Ks),
+         ptr(rs), ptr(f))
+    return f
+
+
+def assemble_cloth_bend(mesh, x, angle, length, perp, dtype=torch.float64):
+    """The cloth example's bending force over a hinge mesh (card 4): f
+    [n*3] (sg_assemble_cloth_bend)."""
+    d = mesh.ctx.device
+    with mesh.ctx.stream():
+        xs, an, ln, pp = (_d(a, dtype, d) for a in (x, angle, length, perp))
+        f = torch.empty(mesh.n * 3, dtype=dtype, device=d)
+    call("sg_assemble_cloth_bend", mesh.ctx.h, mesh.ref(), dtype_code(f), ptr(xs), ptr(an),
+         ptr(ln), ptr(pp), ptr(f))
+    return f
+
+
 def fp64_fma_rate(ctx):
     """sg_fp64_fma_rate: the device's FP64 FMA rate in TFLOP/s."""
     out = ctypes.c_double()

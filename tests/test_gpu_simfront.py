@@ -378,3 +378,37 @@ def test_sim_explicit_springs_golden(ctx):
         assert abs(scenarios.golden_lookup(g, {"x": xh}) - g["expected"]) <= 1e-13, g
     for m in maps:
         m.close()
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_precompiled_cloth_forces(ctx, oracle, dtype):
+    """sg_assemble_cloth_stretch / sg_assemble_cloth_bend, the precompiled
+    kernels of the cloth example's forces: FP64 stretching bit for bit
+    against the oracle, bending within 1e-12 of the largest force (device
+    atan2); in both precisions the run-time compiled maps of
+    tests/sim/cloth_forces.sim give the same values bit for bit."""
+    from simit_gb300.runtime import Mesh, assemble_cloth_bend, assemble_cloth_stretch
+    k = _cloth_case(oracle, 29, 35)
+    mg, n = k["mg"], k["n"]
+    tris = Mesh(ctx, n, mg["faces"], 3)
+    hin = Mesh(ctx, n, mg["hinges"], 4)
+    fs = assemble_cloth_stretch(tris, k["x"], k["K"], k["rest"], dtype=dtype)
+    fb = assemble_cloth_bend(hin, k["x"], k["ang"], k["ln"], k["perp"], dtype=dtype)
+    src = _own("cloth_forces.sim")
+    st = simfront.SimMap(ctx, src, "stretch", dtype=dtype, exact=True)
+    bd = simfront.SimMap(ctx, src, "bend", dtype=dtype, exact=True)
+    js = st.assemble(tris, {"x": k["x"], "rest": k["rest"], "K": k["K"]})
+    jb = bd.assemble(hin, {"x": k["x"], "len": k["ln"], "perp": k["perp"], "theta0": k["ang"]})
+    ctx.sync()
+    assert torch.equal(fs[:n * 3], js[:n * 3])
+    assert torch.equal(fb[:n * 3], jb[:n * 3])
+    ws = oracle.cloth_stretch(n, k["x"], mg["faces"], k["K"], k["rest"])
+    wb = oracle.cloth_bend(n, k["x"], mg["hinges"], k["ang"], k["ln"], k["perp"])
+    gs, gb = fs[:n * 3].double().cpu().numpy(), fb[:n * 3].double().cpu().numpy()
+    if dtype == torch.float64:
+        assert np.array_equal(gs, ws)
+        assert _relerr(gb, wb) <= 1e-12
+    else:
+        assert _relerr(gs, ws) <= 1e-4 and _relerr(gb, wb) <= 1e-4
+    st.close()
+    bd.close()
