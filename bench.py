@@ -37,6 +37,9 @@ def parse():
                          "solutions are compared to (48: about 15-25 s of one core)")
     ap.add_argument("--no-tune", action="store_true",
                     help="default schedules instead of the autotuners' choices")
+    ap.add_argument("--reliable-delta", type=float, default=0.1,
+                    help="mixed PCG: the true residual replaces the iterated one each time "
+                         "the latter falls by this factor")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the heat / neo-Hookean / springs / cloth measurements that "
                          "follow the headline")
@@ -982,7 +985,8 @@ def run_ours(args, rank, world, local):
                                      precond=_lib.PRECOND_LEARNED, learned_params=prm,
                                      storage=_lib.STORAGE_SYMMETRIC if args.sym
                                      else _lib.STORAGE_FULL, pdl=int(args.pdl),
-                                     tune=not args.no_tune)
+                                     tune=not args.no_tune,
+                                     reliable_delta=args.reliable_delta)
     st = ctx.torch_stream
 
     def barrier():

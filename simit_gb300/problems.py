@@ -72,7 +72,7 @@ class HeteroElasticity:
     def __init__(self, ctx, host, dtype=torch.float32, precond=_lib.PRECOND_BLOCK_JACOBI,
                  precision=None, tol=1e-8, maxiters=200000, lanes=0, storage=None, pdl=0,
                  plan="gather", learned_params=None, learned_exec=_lib.MPNN_EXEC_FOLDED,
-                 tune=False):
+                 tune=False, reliable_delta=0.1):
         self.ctx, self.host, self.dtype = ctx, host, dtype
         # plan: the element-parallel assembly plan ("gather", "colored"; each
         # element computed once), or None for the row-owner kernels
@@ -109,6 +109,7 @@ class HeteroElasticity:
         # learned_params (a device FP32 tensor), symmetric form
         self.opts = solve_opts(precision=precision, precond=precond, stop=_lib.STOP_RELATIVE,
                                tol=tol, maxiters=maxiters, verify=1, lanes=lanes,
+                               reliable_delta=reliable_delta,
                                storage=storage, pdl=pdl, learned_params=learned_params,
                                learned_form=_lib.MPNN_SYM, learned_exec=learned_exec)
         self.solver = Solver(ctx, self.mesh.n, 3, self.mesh.pattern.rowptr,
