@@ -48,7 +48,8 @@ def test_tuned_spmv_not_slower_than_default(ctx, ncell):
     td = min(_time(ctx, run(0, y0)) for _ in range(3))
     tt = min(_time(ctx, run(t["g"], y1)) for _ in range(3))
     print("%d^3: default %.4f ms, tuned g=%d %.4f ms" % (ncell, td, t["g"], tt))
-    assert tt <= 1.05 * td
+    # 5 % and 5 us of timing noise (a 16^3 launch takes tens of us)
+    assert tt <= 1.05 * td + 0.005
     ctx.sync()
     scale = float(y0.abs().max())
     assert float((y0 - y1).abs().max()) <= 2e-5 * scale
@@ -68,7 +69,7 @@ def test_tuned_assembly_not_slower_than_default(ctx, ncell):
     default_ms = min(_time(ctx, ref.assemble_in_place, 5) for _ in range(3))
     print("%d^3: assembly default %.3f ms, tuned %s/%d %.3f ms"
           % (ncell, default_ms, a["plan"], a["tile"], tuned_ms))
-    assert tuned_ms <= 1.05 * default_ms
+    assert tuned_ms <= 1.05 * default_ms + 0.005
     ref.assemble_in_place()
     ctx.sync()
     s = float(ref.A.abs().max())
