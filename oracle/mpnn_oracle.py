@@ -240,15 +240,17 @@ def bfp_round(v):
 
 def forward_sym_poly(params, n, rowptr, colidx, vals, r, a=None, bfp=False):
     """z = L^-T [sum_d Aw^d (x) G_d] L^-1 r by Horner's scheme
-    (w_6 = G_6 x, w_d = G_d x + Aw w_{d+1}, z = L^-T w_0).  bfp: round x
-    and every stored w_d (d = 5..0) with bfp_round, as the GPU's FP16
-    evaluation stores them (its first step aggregates x and applies G_6
-    after the sum, Aw (G_6 x) = G_6 (Aw x))."""
+    (w_6 = G_6 x, w_d = G_d x + Aw w_{d+1}, z = L^-T w_0).  bfp: the GPU's
+    FP16 evaluation -- L^-1 rounded to BF16 (both sides), x and every stored
+    w_d (d = 5..0) rounded with bfp_round (its first step aggregates x and
+    applies G_6 after the sum, Aw (G_6 x) = G_6 (Aw x))."""
     G = poly_coeffs(params)
     a0, rows, cols = edge_weights(n, rowptr, colidx, vals)
     if a is None:
         a = a0
     Li = chol_inv(n, rowptr, colidx, vals)
+    if bfp:
+        Li = bf16(Li)
     x = np.einsum("vij,vj->vi", Li, np.asarray(r, np.float64).reshape(n, 3))
     if bfp:
         x = bfp_round(x)

@@ -235,7 +235,8 @@ static int graph_refresh(GraphH *G) {
     const int ge = grid_for(c, G->sl_total, 256, 8);
     k_sell_weights<__half><<<ge, 256, 0, c->stream>>>(G->sl_total, G->fb.sl.src, g.a, G->ah);
     k_sell_weights<float><<<ge, 256, 0, c->stream>>>(G->sl_total, G->fb.sl.src, g.a, G->af);
-    k_pack_linv<<<gr, 256, 0, c->stream>>>(g.n, g.linv, (float *)G->fb.l6);
+    k_pack_linv<<<gr, 256, 0, c->stream>>>(g.n, g.linv, (float *)G->fb.l6,
+                                           (uint32_t *)G->fb.l6b);
     SG_CHECK_LAUNCH();
   }
   return check_device_error(c, "mpnn graph");
@@ -324,9 +325,12 @@ static int ensure_folded(GraphH *G) {
   Ctx *c = G->c;
   FoldBufs &B = G->fb;
   float *l6 = nullptr;
+  uint32_t *l6b = nullptr;
   SG_TRY(galloc(G, (void **)&G->fold, NPOLY * 9 * 4));
   SG_TRY(galloc(G, (void **)&l6, n * 6 * 4));
+  SG_TRY(galloc(G, (void **)&l6b, n * 3 * 4));
   B.l6 = l6;
+  B.l6b = l6b;
   for (void **p : {&B.xin, &B.w[0], &B.w[1]}) SG_TRY(galloc(G, p, n * 4 * 4));
   B.g = G->fold;
   // sliced-ELLPACK copy of the pattern: rows sorted by length per window,
@@ -452,7 +456,7 @@ static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate,
              "mpnn: r, z and q must be 16-byte aligned");
   if (!xin_ready) {
     if (half_a)
-      k_lrn_xin<true><<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, r, B.xin);
+      k_lrn_xin<true><<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6b, r, B.xin);
     else
       k_lrn_xin<false><<<grid_for(c, g.n, 256, 8), 256, 0, st>>>(g.n, B.l6, r, B.xin);
     SG_CHECK_LAUNCH();
@@ -486,7 +490,7 @@ static int fold_apply(GraphH *G, cudaStream_t st, const SolveCtl *ctl, int gate,
   // np of them when asked
   const int g0 = part ? np : finish_grid(c, B.sl.nslice);
   if (half_a)
-    k_lrn_finish<true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B.l6, B.xin, B.w[0], r, q, z, part,
+    k_lrn_finish<true><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B.l6b, B.xin, B.w[0], r, q, z, part,
                                             want_rr, want_zq);
   else
     k_lrn_finish<false><<<g0, LG_T, 0, st>>>(ctl, gate, g.n, B.l6, B.xin, B.w[0], r, q, z, part,
@@ -669,7 +673,7 @@ static int learned_k2(Solver *S, cudaStream_t st, int par) {
   if (L->exec == SG_MPNN_EXEC_FOLDED)
     mpnn::k_lrn_update<true><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->A.n, S->part1, S->P1,
                                                       pq_fin, (const float *)S->q,
-                                                      (float *)S->r, B.l6, B.xin);
+                                                      (float *)S->r, B.l6b, B.xin);
   else
     mpnn::k_lrn_update<false><<<S->P2, RED_T, 0, st>>>(S->ctl, par, S->A.n, S->part1, S->P1,
                                                        pq_fin, (const float *)S->q,

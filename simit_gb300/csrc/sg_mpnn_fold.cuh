@@ -25,6 +25,7 @@
 // read the pattern and the edge weights (FP16 by default, FP32 on request)
 // from a sliced-ELLPACK copy with one lane per row (SellGraph below).
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include "sg_mpnn.cuh"
@@ -134,13 +135,64 @@ __global__ void __launch_bounds__(256) k_fold(const float *__restrict__ prm,
 }
 
 // Packed lower-triangular L_v^-1 (l00, l10, l11, l20, l21, l22) from the
-// 9-value form k_chol_inv writes.
-__global__ void k_pack_linv(int32_t n, const float *__restrict__ linv, float *__restrict__ l6) {
+// 9-value form k_chol_inv writes: FP32 for the FP32 evaluation (l6) and
+// BF16, rounded to nearest even, for the FP16 one (l6b, 12 bytes per vertex:
+// the factor is read twice per application, by x = L^-1 r and z = L^-T w_0,
+// and both read the same rounded factor, so M stays exactly symmetric).
+__global__ void k_pack_linv(int32_t n, const float *__restrict__ linv, float *__restrict__ l6,
+                            uint32_t *__restrict__ l6b) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     const float *L = linv + v * 9;
-    float *o = l6 + v * 6;
-    o[0] = L[0]; o[1] = L[3]; o[2] = L[4]; o[3] = L[6]; o[4] = L[7]; o[5] = L[8];
+    const float o[6] = {L[0], L[3], L[4], L[6], L[7], L[8]};
+    for (int k = 0; k < 6; ++k) l6[v * 6 + k] = o[k];
+    for (int k = 0; k < 3; ++k)
+      l6b[v * 3 + k] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(o[2 * k])) |
+                       ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(o[2 * k + 1])) << 16);
+  }
+}
+
+// L_v^-1 of one vertex (6 packed values) from the evaluation's copy: BF16
+// pairs (low half first) when CV, else FP32.
+template <bool CV>
+__device__ __forceinline__ void ld_linv(const void *__restrict__ l6, size_t v, float *L) {
+  if (CV) {
+    const uint32_t *p = reinterpret_cast<const uint32_t *>(l6) + v * 3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const uint32_t u = __ldg(p + k);
+      L[2 * k] = __uint_as_float(u << 16);
+      L[2 * k + 1] = __uint_as_float(u & 0xffff0000u);
+    }
+  } else {
+    const float *p = reinterpret_cast<const float *>(l6) + v * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) L[k] = p[k];
+  }
+}
+// The same for vertices 4u .. 4u+3 (24 values) with 16-byte loads: three
+// when CV (48 bytes), else six.
+template <bool CV>
+__device__ __forceinline__ void ld_linv4(const void *__restrict__ l6, int64_t u, float *lv) {
+  if (CV) {
+    const uint4 *p = reinterpret_cast<const uint4 *>(l6) + u * 3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const uint4 g = __ldg(p + k);
+      const uint32_t w[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        lv[8 * k + 2 * j] = __uint_as_float(w[j] << 16);
+        lv[8 * k + 2 * j + 1] = __uint_as_float(w[j] & 0xffff0000u);
+      }
+    }
+  } else {
+    const float4 *p = reinterpret_cast<const float4 *>(l6) + u * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float4 g = p[k];
+      lv[4 * k] = g.x; lv[4 * k + 1] = g.y; lv[4 * k + 2] = g.z; lv[4 * k + 3] = g.w;
+    }
   }
 }
 
@@ -326,7 +378,8 @@ struct FoldBufs {
   SellGraph sl;
   const void *a;      // FP32 or FP16 edge weights in slice order
   const float *g;     // the 7 symmetric 3x3 coefficients G_0..G_6, row-major
-  const float *l6;    // packed L^-1 [n][6]
+  const float *l6;    // packed L^-1 [n][6], FP32 (the FP32 evaluation)
+  const uint32_t *l6b;  // the same in BF16 [n][6] (the FP16 evaluation)
   void *xin;          // x = L^-1 r
   void *w[2];         // Horner partial sums, ping-pong
 };
@@ -396,7 +449,8 @@ __global__ void __launch_bounds__(HT_WARPS * 32, FIN ? 7 : 1)
   DotAcc<float> rr, rz, zq;
   auto fin = [&](uint32_t v, float a, float b, float c) {
     // z = (L^-1)^T w, L^-1 = [[l0,0,0],[l1,l2,0],[l3,l4,l5]], as k_lrn_finish
-    const float *L = B.l6 + (size_t)v * 6;
+    float L[6];
+    ld_linv<CV>(CV ? (const void *)B.l6b : (const void *)B.l6, v, L);
     const float z0 = L[0] * a + L[1] * b + L[3] * c;
     const float z1 = L[2] * b + L[4] * c;
     const float z2 = L[5] * c;
@@ -578,7 +632,7 @@ __global__ void __launch_bounds__(HT_WARPS * 32, FIN ? 7 : 1)
 // to thread 0 of block 0.
 template <bool CV>
 __global__ void __launch_bounds__(LG_T) k_lrn_finish(const SolveCtl *ctl, int gate, int32_t n,
-                                                     const float *__restrict__ l6,
+                                                     const void *__restrict__ l6,
                                                      const void *__restrict__ xin,
                                                      const void *__restrict__ w0,
                                                      const float *__restrict__ r,
@@ -592,7 +646,6 @@ __global__ void __launch_bounds__(LG_T) k_lrn_finish(const SolveCtl *ctl, int ga
   const void *w = fb ? xin : w0;
   DotAcc<float> rr, rz, zq;
   const int64_t nu = n / 4;
-  const float4 *l4 = reinterpret_cast<const float4 *>(l6);
   const float4 *r4 = reinterpret_cast<const float4 *>(r);
   const float4 *q4 = reinterpret_cast<const float4 *>(q);
   float4 *z4 = reinterpret_cast<float4 *>(z);
@@ -643,18 +696,14 @@ __global__ void __launch_bounds__(LG_T) k_lrn_finish(const SolveCtl *ctl, int ga
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nu;
        t += (int64_t)gridDim.x * blockDim.x) {
     float lv[24];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const float4 g = l4[t * 6 + k];
-      lv[4 * k] = g.x; lv[4 * k + 1] = g.y; lv[4 * k + 2] = g.z; lv[4 * k + 3] = g.w;
-    }
+    ld_linv4<CV>(l6, t, lv);
     four(t * 4, 4, lv, true);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0 && nu * 4 < n) {
     // the last n % 4 vertices
     float lv[24];
     const int cnt = (int)(n - nu * 4);
-    for (int k = 0; k < cnt * 6; ++k) lv[k] = l6[nu * 24 + k];
+    for (int j = 0; j < cnt; ++j) ld_linv<CV>(l6, (size_t)(nu * 4 + j), lv + 6 * j);
     four(nu * 4, cnt, lv, false);
   }
   if (!part) return;
@@ -670,11 +719,12 @@ __global__ void __launch_bounds__(LG_T) k_lrn_finish(const SolveCtl *ctl, int ga
 
 // x = L^-1 r for a fresh r (set-up, restarts and the standalone forward).
 template <bool CV>
-__global__ void k_lrn_xin(int32_t n, const float *__restrict__ l6, const float *__restrict__ r,
+__global__ void k_lrn_xin(int32_t n, const void *__restrict__ l6, const float *__restrict__ r,
                           void *__restrict__ xin) {
   for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
-    const float *L = l6 + v * 6;
+    float L[6];
+    ld_linv<CV>(l6, (size_t)v, L);
     const float r0 = r[v * 3], r1 = r[v * 3 + 1], r2 = r[v * 3 + 2];
     st3<CV>(xin, v, L[0] * r0, L[1] * r0 + L[2] * r1, L[3] * r0 + L[4] * r1 + L[5] * r2);
   }
@@ -691,7 +741,7 @@ __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, in
                                                       int np1, int pq_fin,
                                                       const float *__restrict__ q,
                                                       float *__restrict__ r,
-                                                      const float *__restrict__ l6,
+                                                      const void *__restrict__ l6,
                                                       void *__restrict__ xin) {
   __shared__ double sh[33];
   if (ctl->status != ST_RUNNING) return;
@@ -706,7 +756,6 @@ __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, in
   const int64_t nu = n / 4;
   const float4 *q4 = reinterpret_cast<const float4 *>(q);
   float4 *r4 = reinterpret_cast<float4 *>(r);
-  const float4 *l4 = reinterpret_cast<const float4 *>(l6);
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nu;
        u += (int64_t)gridDim.x * blockDim.x) {
     float rv[12], lv[24];
@@ -718,11 +767,7 @@ __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, in
       rv[4 * k + 2] = c.z - a * b.z;
       rv[4 * k + 3] = c.w - a * b.w;
     }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const float4 g = l4[u * 6 + k];
-      lv[4 * k] = g.x; lv[4 * k + 1] = g.y; lv[4 * k + 2] = g.z; lv[4 * k + 3] = g.w;
-    }
+    ld_linv4<CV>(l6, u, lv);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
       r4[u * 3 + k] = make_float4(rv[4 * k], rv[4 * k + 1], rv[4 * k + 2], rv[4 * k + 3]);
@@ -740,7 +785,8 @@ __global__ void __launch_bounds__(RED_T) k_lrn_update(SolveCtl *ctl, int par, in
         R[k] = r[v * 3 + k] - a * q[v * 3 + k];
         r[v * 3 + k] = R[k];
       }
-      const float *L = l6 + v * 6;
+      float L[6];
+      ld_linv<CV>(l6, (size_t)v, L);
       st3<CV>(xin, (size_t)v, L[0] * R[0], L[1] * R[0] + L[2] * R[1],
               L[3] * R[0] + L[4] * R[1] + L[5] * R[2]);
     }

@@ -413,7 +413,14 @@ static int solve_impl(Solver *S, const double *b, double *x, sg_solve_result *re
     return true_residual(S, b, out);
   };
   double rr = 0;
-  SG_TRY(check(&rr));
+  if (S->x_zero) {
+    // x = 0: the residual is b itself, exactly (no SpMV, no split of x)
+    SG_CHECK_CUDA(cudaMemcpyAsync(S->rhi, b, S->len * 8, cudaMemcpyDeviceToDevice, st));
+    rr = bb;
+    exact = true;
+  } else {
+    SG_TRY(check(&rr));
+  }
   res->normr2 = rr;
   res->true_normr2 = rr;
   int iters = 0;

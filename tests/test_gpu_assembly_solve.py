@@ -382,6 +382,29 @@ def test_solver_deterministic_and_reusable(ctx, oracle):
     assert r1.iters == r2.iters and torch.equal(x1, x2)
 
 
+@pytest.mark.parametrize("precision", [_lib.SOLVE_MIXED, _lib.SOLVE_F64])
+def test_zero_start_takes_b_as_residual(ctx, oracle, precision):
+    """solve_ex(x_zero) starts from r = b without computing b - A 0: the
+    same iterations and solution as a solve from an explicit zero guess."""
+    from simit_gb300.runtime import Solver, solve_opts
+    dt = torch.float32 if precision == _lib.SOLVE_MIXED else torch.float64
+    mesh, A, b = _elasticity_system(ctx, oracle, 8, dtype=dt)
+    S = Solver(ctx, mesh.n, 3, mesh.pattern.rowptr, mesh.pattern.colidx, A, mesh.nnzb,
+               solve_opts(precision=precision, precond=_lib.PRECOND_BLOCK_JACOBI, tol=1e-8,
+                          maxiters=20000))
+    x1 = torch.zeros_like(b)
+    r1 = S.solve(b, x1)
+    x2 = torch.full_like(b, 7.0)    # ignored: x_zero
+    r2 = S.solve_ex(b, x2, x_zero=True)
+    ctx.sync()
+    assert r1.status == r2.status == 1
+    assert r2.checks == r1.checks
+    assert abs(r1.iters - r2.iters) <= 1
+    assert float((x1 - x2).abs().max()) <= 1e-9 * float(x1.abs().max())
+    rp, ci = mesh.pattern.host()
+    assert oracle.relres(mesh.n, 3, rp, ci, _np(A), _np(b), _np(x2)) <= 1.001e-8
+
+
 def test_solver_status_codes(ctx):
     from simit_gb300.runtime import Mesh, Solver, assemble_scalar_springs, solve_opts
     ep, n = meshgen.box_springs(5, 4, 3)
