@@ -37,9 +37,10 @@ def parse():
                          "solutions are compared to (48: about 15-25 s of one core)")
     ap.add_argument("--no-tune", action="store_true",
                     help="default schedules instead of the autotuners' choices")
-    ap.add_argument("--reliable-delta", type=float, default=0.1,
+    ap.add_argument("--reliable-delta", type=float, default=0.01,
                     help="mixed PCG: the true residual replaces the iterated one each time "
-                         "the latter falls by this factor")
+                         "the latter falls by this factor (0.01: 5 replacements per 128^3 "
+                         "solve instead of 8 at 0.1, 2.4 ms less per step)")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the heat / neo-Hookean / springs / cloth measurements that "
                          "follow the headline")

@@ -28,6 +28,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace sg {
 
 template <typename T> struct AsmArgs {
@@ -349,6 +351,26 @@ __global__ void __launch_bounds__(256) k_colored(AsmArgs<T> a, const uint32_t *_
   }
 }
 
+// Elements whose (j, i) block is bitwise the transpose of their (i, j)
+// block declare SYM = true; the element-blocks plan then computes and
+// stores only the CARD (CARD + 1) / 2 blocks with i <= j, in row order
+// (0,0), (0,1), .., (0,CARD-1), (1,1), .., and the slot gather reads the
+// transpose for i > j.
+template <class E, class = void> struct elem_sym : std::false_type {};
+template <class E>
+struct elem_sym<E, std::void_t<decltype(E::SYM)>> : std::integral_constant<bool, E::SYM> {};
+__device__ __forceinline__ void tri_pair(int C, int r, int &i, int &j) {
+  i = 0;
+  while (r >= C - i) {
+    r -= C - i;
+    ++i;
+  }
+  j = i + r;
+}
+__device__ __forceinline__ int tri_index(int C, int i, int j) {  // i <= j
+  return i * C - i * (i - 1) / 2 + (j - i);
+}
+
 // ---------------------------------------------------------------------------
 // Element blocks + slot gather (the assembly plan's second form)
 // ---------------------------------------------------------------------------
@@ -366,7 +388,9 @@ __global__ void __launch_bounds__(256) k_colored(AsmArgs<T> a, const uint32_t *_
 template <class Elem, int CARD, int BS, typename T, int TILE>
 __global__ void __launch_bounds__(TILE) k_elem_blocks(AsmArgs<T> a, T *__restrict__ eb,
                                                       T *__restrict__ ev) {
-  constexpr int TPE = Elem::HAS_MAT ? CARD * CARD : CARD;
+  constexpr bool SY = elem_sym<Elem>::value;
+  static_assert(!SY || !Elem::HAS_VEC, "a symmetric element stores blocks only");
+  constexpr int TPE = Elem::HAS_MAT ? (SY ? CARD * (CARD + 1) / 2 : CARD * CARD) : CARD;
   // a CTA's TILE consecutive blocks are staged in shared memory and leave in
   // 16-byte stores (the chunk starts TILE * BS*BS * sizeof(T) bytes apart)
   __shared__ __align__(16) T stage[Elem::HAS_MAT ? TILE * BS * BS : 1];
@@ -376,7 +400,8 @@ __global__ void __launch_bounds__(TILE) k_elem_blocks(AsmArgs<T> a, T *__restric
     if (t < total) {
       const int64_t e = t / TPE;
       const int r = (int)(t % TPE);
-      const int i = Elem::HAS_MAT ? r / CARD : r, j = Elem::HAS_MAT ? r % CARD : 0;
+      int i = Elem::HAS_MAT ? r / CARD : r, j = Elem::HAS_MAT ? r % CARD : 0;
+      if (SY) tri_pair(CARD, r, i, j);
       if (Elem::HAS_MAT) {
 #pragma unroll
         for (int l = 0; l < BS; ++l) {
@@ -421,7 +446,10 @@ __global__ void __launch_bounds__(TILE) k_elem_blocks(AsmArgs<T> a, T *__restric
 // vals[q] = sum of eb blocks src[sptr[q] .. sptr[q+1]); thread per (slot,
 // row l); the block indices of up to 8 contributions are loaded before
 // their values, and all values before the sum (ascending order kept).
-template <int BS, typename T>
+// SC > 0: eb holds only the i <= j blocks of elements of SC endpoints
+// (elem_sym); a contribution b = e SC^2 + i SC + j with i > j reads block
+// (j, i) transposed.
+template <int BS, typename T, int SC = 0>
 __global__ void __launch_bounds__(256) k_slot_gather(int64_t nnzb, const uint32_t *__restrict__ sptr,
                                                      const uint32_t *__restrict__ src,
                                                      const T *__restrict__ eb, T *__restrict__ vals) {
@@ -439,10 +467,19 @@ __global__ void __launch_bounds__(256) k_slot_gather(int64_t nnzb, const uint32_
       for (int u = 0; u < 8; ++u) b[u] = k0 + u < k1 ? src[k0 + u] : 0u;
       T x[8][BS];
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
+      for (int u = 0; u < 8; ++u) {
+        size_t blk = b[u];
+        bool tr = false;
+        if (SC > 0) {
+          const uint32_t e = b[u] / (SC * SC), rr = b[u] - e * (SC * SC);
+          const int i = (int)rr / SC, j = (int)rr % SC;
+          tr = i > j;
+          blk = (size_t)e * (SC * (SC + 1) / 2) + tri_index(SC, tr ? j : i, tr ? i : j);
+        }
 #pragma unroll
         for (int m = 0; m < BS; ++m)
-          x[u][m] = k0 + u < k1 ? eb[(size_t)b[u] * BS * BS + l * BS + m] : T(0);
+          x[u][m] = k0 + u < k1 ? eb[blk * BS * BS + (tr ? m * BS + l : l * BS + m)] : T(0);
+      }
 #pragma unroll
       for (int u = 0; u < 8; ++u)
         if (k0 + u < k1)
@@ -791,6 +828,8 @@ template <typename T> struct EbGatherElem {
 // K(v(i), v(j)) += h*h*K_ij when both vertices are free; then m*I on (i, i).
 template <typename T, bool EXACT> struct LinTetElem {
   static constexpr bool HAS_MAT = true, HAS_VEC = false;
+  // the fast form's (j, i) block is bitwise the transpose of (i, j)
+  static constexpr bool SYM = !EXACT;
   static constexpr int LANES = 12;
   __device__ static void dN(const T *Bt, int vi, T g[3]) {
 #pragma unroll

@@ -41,13 +41,15 @@ static int launch_colored(Ctx *c, AsmArgs<T> &a, const sg_mesh *m, bool *used) {
   a.err = c->d_err;
   if (m->slot_src_ptr && m->slot_src) {
     // element blocks (context scratch) + slot / vertex gathers
-    const size_t neb = Elem::HAS_MAT ? (size_t)m->nE * CARD * CARD * BS * BS : 0;
+    constexpr bool SY = elem_sym<Elem>::value;
+    constexpr int BPE = SY ? CARD * (CARD + 1) / 2 : CARD * CARD;  // stored blocks per element
+    const size_t neb = Elem::HAS_MAT ? (size_t)m->nE * BPE * BS * BS : 0;
     const size_t nev = Elem::HAS_VEC ? (size_t)m->nE * CARD * BS : 0;
     Scratch s(c);
     SG_TRY(s.reserve(Scratch::bytes_for(neb + 1, sizeof(T)) + Scratch::bytes_for(nev + 1, sizeof(T))));
     T *eb = s.alloc<T>(neb + 1), *ev = s.alloc<T>(nev + 1);
     if (m->nE > 0) {
-      const int64_t th = m->nE * (Elem::HAS_MAT ? CARD * CARD : CARD);
+      const int64_t th = m->nE * (Elem::HAS_MAT ? BPE : CARD);
       const int tile = m->asm_tile;
       if (tile == 128)
         k_elem_blocks<Elem, CARD, BS, T, 128><<<grid_for(c, th, 128, 16), 128, 0, c->stream>>>(
@@ -61,7 +63,7 @@ static int launch_colored(Ctx *c, AsmArgs<T> &a, const sg_mesh *m, bool *used) {
       SG_CHECK_LAUNCH();
     }
     if (Elem::HAS_MAT && m->nnzb > 0) {
-      k_slot_gather<BS, T><<<grid_for(c, m->nnzb * BS, 256, 8), 256, 0, c->stream>>>(
+      k_slot_gather<BS, T, SY ? CARD : 0><<<grid_for(c, m->nnzb * BS, 256, 8), 256, 0, c->stream>>>(
           m->nnzb, m->slot_src_ptr, m->slot_src, eb, a.vals);
       SG_CHECK_LAUNCH();
     }

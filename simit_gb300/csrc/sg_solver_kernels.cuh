@@ -745,6 +745,64 @@ static __global__ void __launch_bounds__(RED_T) k_cg_direction_v4(SolveCtl *ctl,
 // Set-up / check kernels
 // ---------------------------------------------------------------------------
 
+// FP32 -> FP64 without the FP64 unit, which does the residual's
+// multiply-adds and is scarce on this GPU (about 2 per SM and clock): the
+// sign, the exponent rebiased by 1023 - 127 and the mantissa moved up 29
+// bits; subnormals normalised by their leading zeros; inf and NaN keep
+// their payload.  Exact, as the conversion is.
+__device__ __forceinline__ double widen_f32(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t m = u & 0x7fffffffu, e8 = m >> 23;
+  uint64_t mag;
+  if (e8 == 0) {
+    const int k = __clz(m);  // m > 0: k in [9, 31]
+    mag = m == 0 ? 0ull
+                 : ((uint64_t)(905 - k) << 52) | ((uint64_t)((m << (k - 8)) & 0x7fffffu) << 29);
+  } else if (e8 == 255) {
+    mag = (0x7ffull << 52) | ((uint64_t)(m & 0x7fffffu) << 29);
+  } else {
+    mag = ((uint64_t)m + (896ull << 23)) << 29;
+  }
+  return __longlong_as_double((long long)(((uint64_t)(u & 0x80000000u) << 32) | mag));
+}
+
+// y_row = sum of the row's FP32 3x3 blocks times FP64 x, accumulated in
+// FP64 by one multiply-add per entry (9 per block) on widened entries; a
+// lane's even and odd blocks go to separate sums, which halves the chains
+// of dependent multiply-adds.
+template <int G>
+__device__ __forceinline__ void bsr3_row_widen(const uint32_t *__restrict__ rowptr,
+                                               const uint32_t *__restrict__ colidx,
+                                               const float *__restrict__ vals,
+                                               const double *__restrict__ x, int64_t row, int gl,
+                                               unsigned mask, double &y0, double &y1,
+                                               double &y2) {
+  const uint32_t e = ldg(rowptr + row + 1);
+  uint32_t b = ldg(rowptr + row) + gl;
+  double a[2][3] = {{0, 0, 0}, {0, 0, 0}};
+  auto block = [&](uint32_t k, double *acc) {
+    const uint32_t c = ldg(colidx + k);
+    const float *v = vals + (size_t)k * 9;
+    const double x0 = ldg(x + (size_t)c * 3 + 0);
+    const double x1 = ldg(x + (size_t)c * 3 + 1);
+    const double x2 = ldg(x + (size_t)c * 3 + 2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      acc[i] = fma(widen_f32(ld_stream(v + 3 * i + 0)), x0, acc[i]);
+      acc[i] = fma(widen_f32(ld_stream(v + 3 * i + 1)), x1, acc[i]);
+      acc[i] = fma(widen_f32(ld_stream(v + 3 * i + 2)), x2, acc[i]);
+    }
+  };
+  for (; b + G < e; b += 2 * G) {
+    block(b, a[0]);
+    block(b + G, a[1]);
+  }
+  if (b < e) block(b, a[0]);
+  y0 = group_sum<G>(a[0][0] + a[1][0], mask);
+  y1 = group_sum<G>(a[0][1] + a[1][1], mask);
+  y2 = group_sum<G>(a[0][2] + a[1][2], mask);
+}
+
 // r_hi = b - A x_hi with FP64 accumulation (matrix MT, x FP64).
 template <int G, typename MT>
 __global__ void __launch_bounds__(RED_T) k_true_residual3(int32_t n,
@@ -762,11 +820,15 @@ __global__ void __launch_bounds__(RED_T) k_true_residual3(int32_t n,
   double acc = 0;
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += stride) {
     double y0, y1, y2;
-    bsr3_row<G, MT, double, double>(rowptr, colidx, vals, x, r, gl, mask, y0, y1, y2);
-    if (gl == 0) {
-      const double r0 = b[r * 3] - y0, r1 = b[r * 3 + 1] - y1, r2 = b[r * 3 + 2] - y2;
-      rhi[r * 3] = r0; rhi[r * 3 + 1] = r1; rhi[r * 3 + 2] = r2;
-      acc += r0 * r0 + r1 * r1 + r2 * r2;
+    if constexpr (sizeof(MT) == 4)
+      bsr3_row_widen<G>(rowptr, colidx, vals, x, r, gl, mask, y0, y1, y2);
+    else
+      bsr3_row<G, MT, double, double>(rowptr, colidx, vals, x, r, gl, mask, y0, y1, y2);
+    // lanes 0..2 (all hold the sums) take a component each
+    if (gl < 3) {
+      const double rv = b[r * 3 + gl] - (gl == 0 ? y0 : (gl == 1 ? y1 : y2));
+      rhi[r * 3 + gl] = rv;
+      acc = fma(rv, rv, acc);
     }
   }
   double t = block_sum(acc, sh);
@@ -839,14 +901,17 @@ __global__ void __launch_bounds__(RED_T)
         h[i] = s;
         l[i] = __fadd_rn(__fadd_rn(l[i], ol), se);
       }
-    if (gl == 0) {
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const double y = (double)h[i] + (double)l[i];
-        const double rv = b[r * 3 + i] - y;
-        rhi[r * 3 + i] = rv;
-        acc += rv * rv;
-      }
+    // every lane holds the row's sums: lanes 0..2 take a component each,
+    // so the FP64 pipe (a small fraction of the FP32 rate on this GPU) sees
+    // one add, one subtract and one multiply-add per component, the
+    // conversions done by integer operations
+    if (gl < 3) {
+      const float hv = gl == 0 ? h[0] : (gl == 1 ? h[1] : h[2]);
+      const float lv = gl == 0 ? l[0] : (gl == 1 ? l[1] : l[2]);
+      const double y = widen_f32(hv) + widen_f32(lv);
+      const double rv = b[r * 3 + gl] - y;
+      rhi[r * 3 + gl] = rv;
+      acc = fma(rv, rv, acc);
     }
   }
   double t = block_sum(acc, sh);
